@@ -1,0 +1,197 @@
+/*
+ * p2de.h — C ABI of the GB300 implementation of P2DE.jl's 2D compressible-Euler
+ * DG right-hand side and SSP-RK3 time step (libp2de_gpu.so).
+ *
+ * Every entry point returns an int status (p2de_status); no exception crosses the
+ * ABI. Host buffers are caller-owned and copied; device memory is owned by the
+ * solver handle. One handle is used from one host thread at a time.
+ *
+ * Array layouts are those of P2DE.jl (column-major Julia arrays):
+ *   SVector{4} array A[i,k]            -> A[c + 4*(i + n*k)]          (c = component)
+ *   SVector{2,SVector{4}} array B[i,k] -> B[c + 4*(d + 2*(i + n*k))]  (d = x,y)
+ *   L_local[i,d,k] (one stage)         -> L[i + (Nq+N1D)*(d + 2*k)]
+ * Node order inside an element is tensor-product GLL with r fastest,
+ * i = ir + (N+1)*is; face nodes are ordered by faces r=-1, r=+1, s=-1, s=+1,
+ * each along the face's tangential coordinate (StartUpDG's Quad convention).
+ * Julia passes reinterpret(Float64, Uq), which is bitwise this layout.
+ */
+#ifndef P2DE_H
+#define P2DE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define P2DE_ABI_VERSION 1
+
+typedef enum p2de_status {
+  P2DE_OK = 0,
+  P2DE_ERR_INVALID_ARGUMENT = 1, /* bad sizes, null pointers, unsupported N */
+  P2DE_ERR_UNSUPPORTED = 2,      /* method combination not built */
+  P2DE_ERR_CUDA = 3,             /* CUDA runtime error; see p2de_last_error */
+  P2DE_ERR_OUT_OF_MEMORY = 4,
+  P2DE_ERR_NOT_POSITIVE = 5,     /* density or internal energy <= 0 or NaN in the state */
+  P2DE_ERR_BAD_DT = 6,           /* time step <= 0 or NaN */
+  P2DE_ERR_NO_DEVICE = 7,        /* no CUDA device visible */
+  P2DE_ERR_BUDGET = 8,           /* serving: request larger than the HBM budget */
+  P2DE_ERR_NOT_FOUND = 9         /* serving: unknown request id */
+} p2de_status;
+
+/* RHS dispatch types (src/common/types/Solver.jl:1-36). */
+typedef enum p2de_rhs_type {
+  P2DE_RHS_ES_LIMITED_LOW_ORDER_POS = 0, /* LimitedDG with ChandrashekarFlux volume flux */
+  P2DE_RHS_LOW_ORDER_POSITIVITY = 1,     /* LowOrderPositivity */
+  P2DE_RHS_ENTROPY_STABLE = 2            /* FluxDiffRHS{ChandrashekarFlux} */
+} p2de_rhs_type;
+
+/* Subcell limiter bounds (Solver.jl:47-54). */
+typedef enum p2de_bound_type {
+  P2DE_BOUND_POSITIVITY = 0,                 /* PositivityBound */
+  P2DE_BOUND_POSITIVITY_AND_CELL_ENTROPY = 1 /* PositivityAndCellEntropyBound */
+} p2de_bound_type;
+
+/* Surface flux types (Solver.jl:19-22). Low order: LaxFriedrichsOnNodalVal only;
+ * high order: LaxFriedrichsOnProjectedVal only. */
+typedef enum p2de_surface_flux {
+  P2DE_FLUX_LAX_FRIEDRICHS_ON_NODAL_VAL = 0,
+  P2DE_FLUX_LAX_FRIEDRICHS_ON_PROJECTED_VAL = 1
+} p2de_surface_flux;
+
+typedef enum p2de_precision {
+  P2DE_PRECISION_FP64 = 0, /* everything in FP64 */
+  P2DE_PRECISION_MIXED = 1 /* volume/surface flux differencing in FP32 with FP32
+                              accumulation; low order, limiter, RK in FP64 */
+} p2de_precision;
+
+/* Param (Solver.jl:151-170) flattened; method choices as enums. */
+typedef struct p2de_param {
+  int32_t N;       /* polynomial degree, 1..5 */
+  int32_t K;       /* number of elements */
+  double gamma;    /* CompressibleEulerIdealGas{Dim2}(gamma) */
+  double POSTOL;   /* GlobalConstant */
+  double ZEROTOL;
+  double zeta;     /* LimitingParameter */
+  double eta;
+  double CFL;      /* TimesteppingParameter */
+  double dt0;
+  double t0;
+  double T;
+  int32_t rhs_type;                /* p2de_rhs_type */
+  int32_t bound_type;              /* p2de_bound_type */
+  int32_t low_order_surface_flux;  /* p2de_surface_flux */
+  int32_t high_order_surface_flux; /* p2de_surface_flux */
+  /* 1: reproduce limiter_utils.jl:66-70 exactly, where the 5-tuple bound
+   * (Lrho, Lrhoe, Lphi, Urho, Urhoe) is destructured into 4 names, giving
+   * Urho := Lphi = 0 and Urhoe := Urho = Inf. 0: the intended Urho = Urhoe = Inf. */
+  int32_t reference_semantics;
+  int32_t precision;               /* p2de_precision */
+} p2de_param;
+
+/* Mesh and boundary data. geom/mapP/mapI/mapO/Ival follow StateParam.bcdata
+ * (src/common/types/StateParam.jl:1-7) and GeomData (Solver.jl:185-190) for affine
+ * elements. Indices are Julia's 1-based linear indices into (Nfp, K) face arrays.
+ * mapW/mapS are boundary kinds that BCData does not have (used by the double Mach
+ * reflection problem); pass 0 counts to leave them out. */
+typedef struct p2de_mesh {
+  const double* geom;    /* K x 5, element-major: J, rxJ, sxJ, ryJ, syJ */
+  const int64_t* mapP;   /* Nfp*K, 1-based exterior face-node index (self on boundaries) */
+  const int64_t* mapI;   /* inflow (static Dirichlet) face nodes, 1-based */
+  int64_t nI;
+  const double* Ival;    /* nI x 4 conservative states */
+  const int64_t* mapO;   /* outflow (copy interior node) face nodes, 1-based */
+  int64_t nO;
+  const int64_t* mapW;   /* reflecting-wall face nodes, 1-based */
+  int64_t nW;
+  const int64_t* mapS;   /* moving oblique shock Dirichlet face nodes, 1-based */
+  int64_t nS;
+  const double* xyS;     /* nS x 2 physical coordinates of the mapS nodes */
+  /* state at mapS node (x,y), time t: post if x < shock_x0 + (y + shock_speed*t)*shock_inv_slope else pre */
+  double shock_x0;
+  double shock_inv_slope;
+  double shock_speed;
+  double shock_post[4];
+  double shock_pre[4];
+} p2de_mesh;
+
+/* Fields readable with p2de_get_field (state.preallocation members). */
+typedef enum p2de_field {
+  P2DE_FIELD_UQ = 0,      /* Nq x K SVector{4} */
+  P2DE_FIELD_RHSU = 1,    /* Nq x K SVector{4} */
+  P2DE_FIELD_RHSL = 2,    /* Nq x K SVector{4} */
+  P2DE_FIELD_RHSH = 3,    /* Nq x K SVector{4} */
+  P2DE_FIELD_RHSXYL = 4,  /* Nq x K SVector{2,SVector{4}} */
+  P2DE_FIELD_RHSXYH = 5,  /* Nq x K SVector{2,SVector{4}} */
+  P2DE_FIELD_BF_L = 6,    /* Nfp x K SVector{2,SVector{4}} */
+  P2DE_FIELD_BF_H = 7,    /* Nfp x K SVector{2,SVector{4}} */
+  P2DE_FIELD_L_LOCAL = 8, /* (Nq+N1D) x 2 x K for one stage */
+  P2DE_FIELD_RESW = 9     /* Nq x K SVector{4} */
+} p2de_field;
+
+typedef struct p2de_solver p2de_solver;
+
+/* Version of this ABI (P2DE_ABI_VERSION). */
+int p2de_abi_version(void);
+
+/* Number of doubles in a field for a solver of degree N with K elements. */
+int p2de_field_count(int32_t N, int32_t K, int32_t field, int64_t* count);
+
+/* Replaces initialize_DG (src/dg/init.jl:44-60): builds the GLL operators for
+ * degree N, uploads the mesh/BC data and allocates the device state on `device`.
+ * Uq is left zero; set it with p2de_set_Uq (init_U!, init.jl:342-361). */
+int p2de_initialize_DG(const p2de_param* param, const p2de_mesh* mesh, int device,
+                       p2de_solver** out);
+
+/* Releases the handle and its device memory. */
+int p2de_destroy(p2de_solver* s);
+
+/* Copies Nq*K*4 doubles from host into state.preallocation.Uq. */
+int p2de_set_Uq(p2de_solver* s, const double* Uq);
+
+/* Copies a field to the host; nstage (1..3) selects the L_local stage. */
+int p2de_get_field(p2de_solver* s, int32_t field, int32_t nstage, double* out);
+
+/* Replaces rhs!(state, solver, state_param, time_param) (src/dg/rhs/rhs.jl:5-13)
+ * for the LimitedDG / LowOrderPositivity / FluxDiffRHS dispatches: computes rhsU
+ * from Uq at time t with TimeParam(dt, nstage) and returns the positivity-CFL dt
+ * of low_order_graph_viscosity.jl:32-40 (stage 1) or dt unchanged otherwise. */
+int p2de_rhs(p2de_solver* s, double t, double dt, int32_t nstage, double* dt_out);
+
+/* One pass of the SSP33! time loop body (src/timestepping/SSPRK33.jl:125-139):
+ * advances Uq from *t by the returned dt and updates *t. */
+int p2de_ssp33_step(p2de_solver* s, double* t, double* dt_out);
+
+/* SSP33! (SSPRK33.jl:1-62) without snapshots: steps from param.t0 until t >= T.
+ * Returns the final time, the step count and the last dt. */
+int p2de_ssp33(p2de_solver* s, double* t_out, int64_t* steps_out, double* dt_last);
+
+/* Runs `nsteps` SSP-RK3 steps (or stops at T) with the whole step captured in a
+ * CUDA graph; t and dt stay on the device between steps. */
+int p2de_ssp33_advance(p2de_solver* s, int64_t nsteps, double* t, int64_t* steps_done);
+
+/* Device pointer of a field (for callers that keep data resident). */
+int p2de_device_ptr(p2de_solver* s, int32_t field, void** dptr);
+
+/* CUDA stream (cudaStream_t) used for every launch of this solver. */
+int p2de_set_stream(p2de_solver* s, void* stream);
+
+/* Number of kernel launches issued by this solver since creation. */
+int p2de_launch_count(p2de_solver* s, int64_t* count);
+
+/* Min density and min internal energy over all nodes of Uq (device reduction). */
+int p2de_min_rho_rhoe(p2de_solver* s, double* min_rho, double* min_rhoe);
+
+/* Min density and min internal energy of each RK stage of the last step, as
+ * recorded by the stage update: out[2*(stage-1)] = min rho, out[2*(stage-1)+1] = min rhoe. */
+int p2de_stage_minima(p2de_solver* s, double out[6]);
+
+/* Last error message of this handle (or of the last failed create when s is NULL). */
+int p2de_last_error(p2de_solver* s, char* buf, size_t len);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* P2DE_H */

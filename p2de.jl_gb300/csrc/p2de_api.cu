@@ -1,0 +1,704 @@
+// C ABI of libp2de_gpu.so (include/p2de.h): solver handle, device memory, the
+// SSP-RK3 step sequence and its CUDA-graph replay.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/p2de.h"
+#include "p2de_args.h"
+#include "p2de_launch.h"
+#include "p2de_physics.cuh"
+#include "p2de_tables.h"
+
+using namespace p2de;
+
+namespace {
+
+std::mutex g_err_mu;
+std::string g_last_create_error;
+
+// --- small kernels ------------------------------------------------------------------
+
+// SSPRK33.jl:126 and low_order_graph_viscosity.jl:230: dt = min(CFL*dt0, T - t) is the
+// stage-1 limiter dt and the initial value of the positivity-CFL minimum.
+__global__ void k_step_begin(double* scal, unsigned long long* dtmin, long long* minrec, int* status, double CFL,
+                             double dt0, double T) {
+  if (threadIdx.x != 0) return;
+  double t = scal[S_T];
+  if (!(t < T) || *status != 0) {
+    scal[S_DONE] = 1.0;
+    return;
+  }
+  scal[S_DONE] = 0.0;
+  double dt = jmin(CFL * dt0, T - t);
+  scal[S_DT_LIM] = dt;
+  if (!(dt > 0.0)) {
+    atomicOr(status, ST_BAD_DT);
+    scal[S_DONE] = 1.0;
+    return;
+  }
+  *dtmin = (unsigned long long)__double_as_longlong(dt);
+  long long inf_key = 0x7ff0000000000000LL;
+  for (int i = 0; i < 6; ++i) minrec[i] = inf_key;
+}
+
+__device__ __forceinline__ long long okey(double x) {
+  long long b = __double_as_longlong(x);
+  return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+}
+
+__global__ void k_min_rho_rhoe(const double* Uq, size_t nodes, long long* out) {
+  double rmin = INFINITY, emin = INFINITY;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < nodes; i += (size_t)gridDim.x * blockDim.x) {
+    const double* U = Uq + 4 * i;
+    double re = rhoe_ufun(U[0], U[1], U[2], U[3]);
+    rmin = fmin(rmin, U[0]);
+    emin = fmin(emin, re);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    rmin = fmin(rmin, __shfl_xor_sync(0xffffffffu, rmin, o));
+    emin = fmin(emin, __shfl_xor_sync(0xffffffffu, emin, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMin(&out[0], okey(rmin));
+    atomicMin(&out[1], okey(emin));
+  }
+}
+
+double key_to_double(long long k) {
+  long long b = k ^ ((k >> 63) & 0x7fffffffffffffffLL);
+  double d;
+  std::memcpy(&d, &b, 8);
+  return d;
+}
+
+// --- operator tables per device -------------------------------------------------------
+
+struct DeviceTables {
+  OpTable* d_tables = nullptr;  // index N1D - 2
+  bool ready = false;
+};
+std::mutex g_tab_mu;
+DeviceTables g_tabs[64];
+
+cudaError_t device_tables(int dev, double zerotol, OpTable** out) {
+  std::lock_guard<std::mutex> lk(g_tab_mu);
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  DeviceTables& t = g_tabs[dev];
+  if (!t.ready) {
+    std::vector<OpTable> h(kMaxN1D - 1);
+    for (int N = 1; N < kMaxN1D; ++N) build_op_table(N, zerotol, &h[N - 1]);
+    cudaError_t e = cudaMalloc(&t.d_tables, sizeof(OpTable) * h.size());
+    if (e != cudaSuccess) return e;
+    e = cudaMemcpy(t.d_tables, h.data(), sizeof(OpTable) * h.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return e;
+    t.ready = true;
+  }
+  *out = t.d_tables;
+  return cudaSuccess;
+}
+
+cudaError_t prepare_n1d(int n1d, StageGeometry* geo) {
+  switch (n1d) {
+    case 2: return stage_prepare<2>(geo);
+    case 3: return stage_prepare<3>(geo);
+    case 4: return stage_prepare<4>(geo);
+    case 5: return stage_prepare<5>(geo);
+    case 6: return stage_prepare<6>(geo);
+  }
+  return cudaErrorInvalidValue;
+}
+cudaError_t launch_a_n1d(int n1d, const StageArgs& a, bool mixed, cudaStream_t st) {
+  switch (n1d) {
+    case 2: return launch_stage_a<2>(a, mixed, st);
+    case 3: return launch_stage_a<3>(a, mixed, st);
+    case 4: return launch_stage_a<4>(a, mixed, st);
+    case 5: return launch_stage_a<5>(a, mixed, st);
+    case 6: return launch_stage_a<6>(a, mixed, st);
+  }
+  return cudaErrorInvalidValue;
+}
+cudaError_t launch_b_n1d(int n1d, const StageArgs& a, cudaStream_t st) {
+  switch (n1d) {
+    case 2: return launch_stage_b<2>(a, st);
+    case 3: return launch_stage_b<3>(a, st);
+    case 4: return launch_stage_b<4>(a, st);
+    case 5: return launch_stage_b<5>(a, st);
+    case 6: return launch_stage_b<6>(a, st);
+  }
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace
+
+struct p2de_solver {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  p2de_param prm{};
+  int N = 0, N1D = 0, Nq = 0, Nfp = 0, K = 0, NSF = 0;
+  StageGeometry geo{};
+  bool mixed = false;
+  bool axis_aligned = true;
+  // device memory
+  double *Uq = nullptr, *resW = nullptr, *rhsL = nullptr, *rhsH = nullptr, *rhsU = nullptr;
+  double *rhsxyL = nullptr, *rhsxyH = nullptr, *BFL = nullptr, *BFH = nullptr;
+  double *fbar = nullptr, *Lpre = nullptr, *Lfin = nullptr, *geom = nullptr, *Ival = nullptr, *xyS = nullptr;
+  double* scal = nullptr;
+  int32_t *nbr = nullptr, *bcidx = nullptr;
+  int8_t* bc = nullptr;
+  unsigned long long* dtmin = nullptr;
+  long long* minrec = nullptr;
+  long long* minbuf = nullptr;
+  int* status = nullptr;
+  OpTable* ops = nullptr;
+  StageArgs base{};
+  int64_t launches = 0;
+  cudaGraphExec_t graph = nullptr;
+  std::string err;
+  std::vector<void*> allocs;
+};
+
+namespace {
+
+int fail(p2de_solver* s, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  std::vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (s)
+    s->err = buf;
+  else {
+    std::lock_guard<std::mutex> lk(g_err_mu);
+    g_last_create_error = buf;
+  }
+  return code;
+}
+
+#define CK(call)                                                                                   \
+  do {                                                                                             \
+    cudaError_t e_ = (call);                                                                       \
+    if (e_ != cudaSuccess) return fail(s, P2DE_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+  } while (0)
+
+template <typename T>
+cudaError_t dalloc(p2de_solver* s, T** p, size_t count) {
+  void* q = nullptr;
+  size_t bytes = sizeof(T) * (count > 0 ? count : 1);
+  cudaError_t e = cudaMalloc(&q, bytes);
+  if (e != cudaSuccess) return e;
+  e = cudaMemsetAsync(q, 0, bytes, s->stream);
+  if (e != cudaSuccess) return e;
+  s->allocs.push_back(q);
+  *p = (T*)q;
+  return cudaSuccess;
+}
+
+int flags_for(const p2de_solver* s, int nstage, bool update, bool debug) {
+  int f = 0;
+  switch (s->prm.rhs_type) {
+    case P2DE_RHS_LOW_ORDER_POSITIVITY: f |= F_DO_LOW | F_RHSU_FROM_L; break;
+    case P2DE_RHS_ENTROPY_STABLE: f |= F_DO_HIGH | F_RHSU_FROM_H; break;
+    default: f |= F_DO_LOW | F_DO_HIGH | F_DO_LIMIT; break;
+  }
+  if ((f & F_DO_LOW) && nstage == 1) f |= F_CFL;
+  if (s->axis_aligned) f |= F_AXIS_ALIGNED;
+  if (s->prm.reference_semantics) f |= F_REF_SEM;
+  if (s->prm.bound_type == P2DE_BOUND_POSITIVITY_AND_CELL_ENTROPY) f |= F_CELL_ENTROPY;
+  if (update) f |= F_UPDATE;
+  if (debug) f |= F_WRITE_DEBUG;
+  return f;
+}
+
+int check_status(p2de_solver* s) {
+  int st = 0;
+  CK(cudaMemcpyAsync(&st, s->status, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  if (st & (ST_NOT_POSITIVE | ST_NAN)) return fail(s, P2DE_ERR_NOT_POSITIVE, "density or internal energy not positive (status %d)", st);
+  if (st & ST_BAD_DT) return fail(s, P2DE_ERR_BAD_DT, "time step not positive (status %d)", st);
+  return P2DE_OK;
+}
+
+// Issues the 7 launches of one SSP-RK3 step on s->stream.
+int enqueue_step(p2de_solver* s) {
+  k_step_begin<<<1, 32, 0, s->stream>>>(s->scal, s->dtmin, s->minrec, s->status, s->prm.CFL, s->prm.dt0, s->prm.T);
+  CK(cudaGetLastError());
+  s->launches += 1;
+  for (int stage = 1; stage <= 3; ++stage) {
+    StageArgs a = s->base;
+    a.nstage = stage;
+    a.flags = flags_for(s, stage, true, false);
+    CK(launch_a_n1d(s->N1D, a, s->mixed, s->stream));
+    CK(launch_b_n1d(s->N1D, a, s->stream));
+    s->launches += 2;
+  }
+  return P2DE_OK;
+}
+
+void free_all(p2de_solver* s) {
+  if (s->graph) cudaGraphExecDestroy(s->graph);
+  for (void* p : s->allocs) cudaFree(p);
+  s->allocs.clear();
+  if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
+}
+
+}  // namespace
+
+extern "C" {
+
+int p2de_abi_version(void) { return P2DE_ABI_VERSION; }
+
+int p2de_field_count(int32_t N, int32_t K, int32_t field, int64_t* count) {
+  if (!count || N < 1 || N > 5 || K < 1) return P2DE_ERR_INVALID_ARGUMENT;
+  int64_t n = N + 1, Nq = n * n, Nfp = 4 * n;
+  switch (field) {
+    case P2DE_FIELD_UQ:
+    case P2DE_FIELD_RHSU:
+    case P2DE_FIELD_RHSL:
+    case P2DE_FIELD_RHSH:
+    case P2DE_FIELD_RESW: *count = 4 * Nq * K; break;
+    case P2DE_FIELD_RHSXYL:
+    case P2DE_FIELD_RHSXYH: *count = 8 * Nq * K; break;
+    case P2DE_FIELD_BF_L:
+    case P2DE_FIELD_BF_H: *count = 8 * Nfp * K; break;
+    case P2DE_FIELD_L_LOCAL: *count = (Nq + n) * 2 * K; break;
+    default: return P2DE_ERR_INVALID_ARGUMENT;
+  }
+  return P2DE_OK;
+}
+
+int p2de_initialize_DG(const p2de_param* prm, const p2de_mesh* mesh, int device, p2de_solver** out) {
+  p2de_solver* s = nullptr;
+  if (!prm || !mesh || !out) return fail(nullptr, P2DE_ERR_INVALID_ARGUMENT, "null argument");
+  *out = nullptr;
+  if (prm->N < 1 || prm->N > 5) return fail(nullptr, P2DE_ERR_INVALID_ARGUMENT, "N=%d outside 1..5", prm->N);
+  if (prm->K < 1) return fail(nullptr, P2DE_ERR_INVALID_ARGUMENT, "K=%d", prm->K);
+  if (!mesh->geom || !mesh->mapP) return fail(nullptr, P2DE_ERR_INVALID_ARGUMENT, "geom and mapP are required");
+  if (prm->low_order_surface_flux != P2DE_FLUX_LAX_FRIEDRICHS_ON_NODAL_VAL ||
+      prm->high_order_surface_flux != P2DE_FLUX_LAX_FRIEDRICHS_ON_PROJECTED_VAL)
+    return fail(nullptr, P2DE_ERR_UNSUPPORTED,
+                "surface fluxes: only LaxFriedrichsOnNodalVal (low order) and LaxFriedrichsOnProjectedVal (high order)");
+  if (prm->rhs_type < 0 || prm->rhs_type > 2 || prm->bound_type < 0 || prm->bound_type > 1 || prm->precision < 0 ||
+      prm->precision > 1)
+    return fail(nullptr, P2DE_ERR_INVALID_ARGUMENT, "rhs_type/bound_type/precision out of range");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(nullptr, P2DE_ERR_NO_DEVICE, "no CUDA device");
+  if (device < 0 || device >= ndev) return fail(nullptr, P2DE_ERR_INVALID_ARGUMENT, "device %d of %d", device, ndev);
+  const int64_t n1 = prm->N + 1, Nfp = 4 * n1, Nq = n1 * n1;
+  const int64_t nfk = Nfp * prm->K;
+  // validate indices before anything reaches the device
+  for (int64_t i = 0; i < nfk; ++i)
+    if (mesh->mapP[i] < 1 || mesh->mapP[i] > nfk)
+      return fail(nullptr, P2DE_ERR_INVALID_ARGUMENT, "mapP[%lld]=%lld out of 1..%lld", (long long)i,
+                  (long long)mesh->mapP[i], (long long)nfk);
+  auto check_list = [&](const int64_t* m, int64_t cnt, const char* name) -> int {
+    if (cnt < 0 || (cnt > 0 && !m)) return fail(nullptr, P2DE_ERR_INVALID_ARGUMENT, "%s: bad list", name);
+    for (int64_t i = 0; i < cnt; ++i)
+      if (m[i] < 1 || m[i] > nfk)
+        return fail(nullptr, P2DE_ERR_INVALID_ARGUMENT, "%s[%lld]=%lld out of range", name, (long long)i, (long long)m[i]);
+    return P2DE_OK;
+  };
+  int rc;
+  if ((rc = check_list(mesh->mapI, mesh->nI, "mapI")) != P2DE_OK) return rc;
+  if ((rc = check_list(mesh->mapO, mesh->nO, "mapO")) != P2DE_OK) return rc;
+  if ((rc = check_list(mesh->mapW, mesh->nW, "mapW")) != P2DE_OK) return rc;
+  if ((rc = check_list(mesh->mapS, mesh->nS, "mapS")) != P2DE_OK) return rc;
+  if (mesh->nI > 0 && !mesh->Ival) return fail(nullptr, P2DE_ERR_INVALID_ARGUMENT, "Ival missing");
+  if (mesh->nS > 0 && !mesh->xyS) return fail(nullptr, P2DE_ERR_INVALID_ARGUMENT, "xyS missing");
+
+  s = new p2de_solver();
+  s->device = device;
+  s->prm = *prm;
+  s->N = prm->N;
+  s->N1D = (int)n1;
+  s->Nq = (int)Nq;
+  s->Nfp = (int)Nfp;
+  s->K = prm->K;
+  s->mixed = prm->precision == P2DE_PRECISION_MIXED;
+  auto bail = [&](int code) {
+    {
+      std::lock_guard<std::mutex> lk(g_err_mu);
+      g_last_create_error = s->err;
+    }
+    free_all(s);
+    delete s;
+    return code;
+  };
+  if (cudaSetDevice(device) != cudaSuccess) {
+    fail(s, P2DE_ERR_CUDA, "cudaSetDevice failed");
+    return bail(P2DE_ERR_CUDA);
+  }
+  if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    fail(s, P2DE_ERR_CUDA, "stream create failed");
+    return bail(P2DE_ERR_CUDA);
+  }
+  s->own_stream = true;
+  cudaError_t e = prepare_n1d(s->N1D, &s->geo);
+  if (e == cudaSuccess) e = device_tables(device, prm->ZEROTOL, &s->ops);
+  if (e != cudaSuccess) {
+    fail(s, P2DE_ERR_CUDA, "setup: %s", cudaGetErrorString(e));
+    return bail(P2DE_ERR_CUDA);
+  }
+  s->NSF = s->geo.nsf;
+  const size_t K = (size_t)s->K;
+  // host-side preprocessing: neighbour indices, boundary codes, axis alignment
+  std::vector<int32_t> nbr(nfk), bcidx(nfk, 0);
+  std::vector<int8_t> bc(nfk, BC_INTERIOR);
+  for (int64_t i = 0; i < nfk; ++i) nbr[i] = (int32_t)(mesh->mapP[i] - 1);
+  for (int64_t i = 0; i < mesh->nI; ++i) {
+    bc[mesh->mapI[i] - 1] = BC_INFLOW;
+    bcidx[mesh->mapI[i] - 1] = (int32_t)i;
+  }
+  for (int64_t i = 0; i < mesh->nO; ++i) bc[mesh->mapO[i] - 1] = BC_OUTFLOW;
+  for (int64_t i = 0; i < mesh->nW; ++i) bc[mesh->mapW[i] - 1] = BC_WALL;
+  for (int64_t i = 0; i < mesh->nS; ++i) {
+    bc[mesh->mapS[i] - 1] = BC_SHOCK;
+    bcidx[mesh->mapS[i] - 1] = (int32_t)i;
+  }
+  s->axis_aligned = true;
+  for (size_t k = 0; k < K; ++k) {
+    const double* g = mesh->geom + 5 * k;
+    if (g[2] != 0.0 || g[3] != 0.0) s->axis_aligned = false;
+    if (!(g[0] > 0.0)) {
+      fail(s, P2DE_ERR_INVALID_ARGUMENT, "J[%zu] = %g is not positive", k, g[0]);
+      return bail(P2DE_ERR_INVALID_ARGUMENT);
+    }
+  }
+#define DA(ptr, cnt)                                                                     \
+  do {                                                                                   \
+    cudaError_t ee = dalloc(s, &(ptr), (cnt));                                           \
+    if (ee != cudaSuccess) {                                                             \
+      fail(s, P2DE_ERR_OUT_OF_MEMORY, "cudaMalloc %s: %s", #ptr, cudaGetErrorString(ee)); \
+      return bail(P2DE_ERR_OUT_OF_MEMORY);                                               \
+    }                                                                                    \
+  } while (0)
+  DA(s->Uq, 4 * Nq * K);
+  DA(s->resW, 4 * Nq * K);
+  DA(s->rhsL, 4 * Nq * K);
+  DA(s->rhsH, 4 * Nq * K);
+  DA(s->rhsU, 4 * Nq * K);
+  DA(s->rhsxyL, 8 * Nq * K);
+  DA(s->rhsxyH, 8 * Nq * K);
+  DA(s->BFL, 8 * Nfp * K);
+  DA(s->BFH, 8 * Nfp * K);
+  DA(s->fbar, (size_t)s->geo.fbar_per_elem * K);
+  DA(s->Lpre, (size_t)2 * s->NSF * K);
+  DA(s->Lfin, (size_t)3 * 2 * s->NSF * K);
+  DA(s->geom, 5 * K);
+  DA(s->Ival, (size_t)4 * (mesh->nI > 0 ? mesh->nI : 1));
+  DA(s->xyS, (size_t)2 * (mesh->nS > 0 ? mesh->nS : 1));
+  DA(s->scal, (size_t)S_NSCAL);
+  DA(s->nbr, (size_t)nfk);
+  DA(s->bcidx, (size_t)nfk);
+  DA(s->bc, (size_t)nfk);
+  DA(s->dtmin, 1);
+  DA(s->minrec, 6);
+  DA(s->minbuf, 2);
+  DA(s->status, 1);
+#undef DA
+  auto up = [&](void* dst, const void* src, size_t bytes) {
+    return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s->stream);
+  };
+  e = up(s->geom, mesh->geom, sizeof(double) * 5 * K);
+  if (e == cudaSuccess) e = up(s->nbr, nbr.data(), sizeof(int32_t) * nfk);
+  if (e == cudaSuccess) e = up(s->bcidx, bcidx.data(), sizeof(int32_t) * nfk);
+  if (e == cudaSuccess) e = up(s->bc, bc.data(), nfk);
+  if (e == cudaSuccess && mesh->nI > 0) e = up(s->Ival, mesh->Ival, sizeof(double) * 4 * mesh->nI);
+  if (e == cudaSuccess && mesh->nS > 0) e = up(s->xyS, mesh->xyS, sizeof(double) * 2 * mesh->nS);
+  double sc[S_NSCAL] = {0};
+  sc[S_T] = prm->t0;
+  if (e == cudaSuccess) e = up(s->scal, sc, sizeof sc);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+  if (e != cudaSuccess) {
+    fail(s, P2DE_ERR_CUDA, "upload: %s", cudaGetErrorString(e));
+    return bail(P2DE_ERR_CUDA);
+  }
+  StageArgs& a = s->base;
+  a.K = s->K;
+  a.ops = s->ops + (s->N1D - 2);
+  a.Uq = s->Uq;
+  a.resW = s->resW;
+  a.geom = s->geom;
+  a.nbr = s->nbr;
+  a.bc = s->bc;
+  a.bcidx = s->bcidx;
+  a.Ival = s->Ival;
+  a.xyS = s->xyS;
+  a.shock_x0 = mesh->shock_x0;
+  a.shock_inv_slope = mesh->shock_inv_slope;
+  a.shock_speed = mesh->shock_speed;
+  for (int c = 0; c < 4; ++c) {
+    a.shock_post[c] = mesh->shock_post[c];
+    a.shock_pre[c] = mesh->shock_pre[c];
+  }
+  a.gamma = prm->gamma;
+  a.gm1 = prm->gamma - 1.0;
+  a.CFL = prm->CFL;
+  a.dt0 = prm->dt0;
+  a.T = prm->T;
+  a.zeta = prm->zeta;
+  a.ZEROTOL = prm->ZEROTOL;
+  a.rhsL = s->rhsL;
+  a.rhsH = s->rhsH;
+  a.rhsU = s->rhsU;
+  a.rhsxyL = s->rhsxyL;
+  a.rhsxyH = s->rhsxyH;
+  a.BFL = s->BFL;
+  a.BFH = s->BFH;
+  a.fbar = s->fbar;
+  a.Lpre = s->Lpre;
+  a.Lfin = s->Lfin;
+  a.scal = s->scal;
+  a.dtmin_bits = s->dtmin;
+  a.minrec = s->minrec;
+  a.status = s->status;
+  *out = s;
+  return P2DE_OK;
+}
+
+int p2de_destroy(p2de_solver* s) {
+  if (!s) return P2DE_OK;
+  cudaSetDevice(s->device);
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  free_all(s);
+  delete s;
+  return P2DE_OK;
+}
+
+int p2de_set_Uq(p2de_solver* s, const double* Uq) {
+  if (!s || !Uq) return P2DE_ERR_INVALID_ARGUMENT;
+  CK(cudaSetDevice(s->device));
+  CK(cudaMemcpyAsync(s->Uq, Uq, sizeof(double) * 4 * s->Nq * (size_t)s->K, cudaMemcpyHostToDevice, s->stream));
+  CK(cudaMemsetAsync(s->status, 0, sizeof(int), s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  return P2DE_OK;
+}
+
+int p2de_get_field(p2de_solver* s, int32_t field, int32_t nstage, double* out) {
+  if (!s || !out) return P2DE_ERR_INVALID_ARGUMENT;
+  int64_t cnt = 0;
+  if (p2de_field_count(s->N, s->K, field, &cnt) != P2DE_OK) return fail(s, P2DE_ERR_INVALID_ARGUMENT, "bad field %d", field);
+  const double* src = nullptr;
+  switch (field) {
+    case P2DE_FIELD_UQ: src = s->Uq; break;
+    case P2DE_FIELD_RHSU: src = s->rhsU; break;
+    case P2DE_FIELD_RHSL: src = s->rhsL; break;
+    case P2DE_FIELD_RHSH: src = s->rhsH; break;
+    case P2DE_FIELD_RHSXYL: src = s->rhsxyL; break;
+    case P2DE_FIELD_RHSXYH: src = s->rhsxyH; break;
+    case P2DE_FIELD_BF_L: src = s->BFL; break;
+    case P2DE_FIELD_BF_H: src = s->BFH; break;
+    case P2DE_FIELD_RESW: src = s->resW; break;
+    case P2DE_FIELD_L_LOCAL:
+      if (nstage < 1 || nstage > 3) return fail(s, P2DE_ERR_INVALID_ARGUMENT, "nstage %d", nstage);
+      src = s->Lfin + (size_t)(nstage - 1) * cnt;
+      break;
+  }
+  CK(cudaSetDevice(s->device));
+  CK(cudaMemcpyAsync(out, src, sizeof(double) * cnt, cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  return P2DE_OK;
+}
+
+int p2de_rhs(p2de_solver* s, double t, double dt, int32_t nstage, double* dt_out) {
+  if (!s || !dt_out || nstage < 1 || nstage > 3) return P2DE_ERR_INVALID_ARGUMENT;
+  CK(cudaSetDevice(s->device));
+  double sc[S_NSCAL] = {0};
+  sc[S_T] = t;
+  sc[S_DT_LIM] = dt;
+  sc[S_DT] = dt;
+  sc[S_DONE] = 0.0;
+  // dtarr init of calculate_lambda_and_low_order_CFL! (low_order_graph_viscosity.jl:230)
+  double dinit = std::fmin(s->prm.CFL * s->prm.dt0, s->prm.T - t);
+  if (std::isnan(s->prm.CFL * s->prm.dt0) || std::isnan(s->prm.T - t)) dinit = NAN;
+  unsigned long long bits;
+  std::memcpy(&bits, &dinit, 8);
+  CK(cudaMemcpyAsync(s->scal, sc, sizeof sc, cudaMemcpyHostToDevice, s->stream));
+  CK(cudaMemcpyAsync(s->dtmin, &bits, 8, cudaMemcpyHostToDevice, s->stream));
+  CK(cudaMemsetAsync(s->status, 0, sizeof(int), s->stream));
+  StageArgs a = s->base;
+  a.nstage = nstage;
+  a.flags = flags_for(s, nstage, false, true);
+  if (!(dinit > 0.0)) a.flags &= ~F_CFL;
+  CK(launch_a_n1d(s->N1D, a, s->mixed, s->stream));
+  CK(launch_b_n1d(s->N1D, a, s->stream));
+  s->launches += 2;
+  double result = dt;
+  if (a.flags & F_CFL) {
+    CK(cudaMemcpyAsync(&bits, s->dtmin, 8, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    std::memcpy(&result, &bits, 8);
+  } else if ((a.flags & F_DO_LOW) && nstage == 1) {
+    result = dinit;
+  }
+  int rc = check_status(s);
+  if (rc == P2DE_ERR_BAD_DT || rc == P2DE_ERR_CUDA) return rc;
+  *dt_out = result;
+  return P2DE_OK;
+}
+
+static int step_impl(p2de_solver* s, double* t, double* dt_out) {
+  CK(cudaMemcpyAsync(s->scal + S_T, t, sizeof(double), cudaMemcpyHostToDevice, s->stream));
+  int rc = enqueue_step(s);
+  if (rc != P2DE_OK) return rc;
+  double sc[S_NSCAL];
+  CK(cudaMemcpyAsync(sc, s->scal, sizeof sc, cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  rc = check_status(s);
+  if (rc != P2DE_OK) return rc;
+  if (sc[S_DONE] == 0.0) {
+    *t = sc[S_T];
+    *dt_out = sc[S_DT];
+  } else {
+    *dt_out = 0.0;
+  }
+  return P2DE_OK;
+}
+
+int p2de_ssp33_step(p2de_solver* s, double* t, double* dt_out) {
+  if (!s || !t || !dt_out) return P2DE_ERR_INVALID_ARGUMENT;
+  CK(cudaSetDevice(s->device));
+  return step_impl(s, t, dt_out);
+}
+
+static int build_graph(p2de_solver* s) {
+  if (s->graph) return P2DE_OK;
+  cudaGraph_t g;
+  CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+  int64_t before = s->launches;
+  int rc = enqueue_step(s);
+  cudaError_t e = cudaStreamEndCapture(s->stream, &g);
+  s->launches = before;  // capture does not launch
+  if (rc != P2DE_OK) return rc;
+  CK(e);
+  CK(cudaGraphInstantiate(&s->graph, g, 0));
+  CK(cudaGraphDestroy(g));
+  return P2DE_OK;
+}
+
+int p2de_ssp33_advance(p2de_solver* s, int64_t nsteps, double* t, int64_t* steps_done) {
+  if (!s || !t || nsteps < 0) return P2DE_ERR_INVALID_ARGUMENT;
+  CK(cudaSetDevice(s->device));
+  int rc = build_graph(s);
+  if (rc != P2DE_OK) return rc;
+  double sc[S_NSCAL];
+  CK(cudaMemcpyAsync(sc, s->scal, sizeof sc, cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  double steps0 = sc[S_STEPS];
+  CK(cudaMemcpyAsync(s->scal + S_T, t, sizeof(double), cudaMemcpyHostToDevice, s->stream));
+  for (int64_t i = 0; i < nsteps; ++i) {
+    CK(cudaGraphLaunch(s->graph, s->stream));
+    s->launches += 7;
+  }
+  CK(cudaMemcpyAsync(sc, s->scal, sizeof sc, cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  rc = check_status(s);
+  *t = sc[S_T];
+  if (steps_done) *steps_done = (int64_t)(sc[S_STEPS] - steps0);
+  return rc;
+}
+
+int p2de_ssp33(p2de_solver* s, double* t_out, int64_t* steps_out, double* dt_last) {
+  if (!s) return P2DE_ERR_INVALID_ARGUMENT;
+  CK(cudaSetDevice(s->device));
+  double t = s->prm.t0;
+  int64_t total = 0;
+  int rc = P2DE_OK;
+  for (;;) {
+    int64_t done = 0;
+    rc = p2de_ssp33_advance(s, 64, &t, &done);
+    total += done;
+    if (rc != P2DE_OK || done < 64 || !(t < s->prm.T)) break;
+  }
+  double sc[S_NSCAL];
+  CK(cudaMemcpyAsync(sc, s->scal, sizeof sc, cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  if (t_out) *t_out = t;
+  if (steps_out) *steps_out = total;
+  if (dt_last) *dt_last = sc[S_DT];
+  return rc;
+}
+
+int p2de_device_ptr(p2de_solver* s, int32_t field, void** dptr) {
+  if (!s || !dptr) return P2DE_ERR_INVALID_ARGUMENT;
+  switch (field) {
+    case P2DE_FIELD_UQ: *dptr = s->Uq; break;
+    case P2DE_FIELD_RHSU: *dptr = s->rhsU; break;
+    case P2DE_FIELD_RHSL: *dptr = s->rhsL; break;
+    case P2DE_FIELD_RHSH: *dptr = s->rhsH; break;
+    case P2DE_FIELD_RESW: *dptr = s->resW; break;
+    case P2DE_FIELD_L_LOCAL: *dptr = s->Lfin; break;
+    default: return fail(s, P2DE_ERR_INVALID_ARGUMENT, "no device pointer for field %d", field);
+  }
+  return P2DE_OK;
+}
+
+int p2de_set_stream(p2de_solver* s, void* stream) {
+  if (!s) return P2DE_ERR_INVALID_ARGUMENT;
+  CK(cudaSetDevice(s->device));
+  CK(cudaStreamSynchronize(s->stream));
+  if (s->graph) {
+    cudaGraphExecDestroy(s->graph);
+    s->graph = nullptr;
+  }
+  if (s->own_stream) cudaStreamDestroy(s->stream);
+  s->own_stream = false;
+  s->stream = (cudaStream_t)stream;
+  return P2DE_OK;
+}
+
+int p2de_launch_count(p2de_solver* s, int64_t* count) {
+  if (!s || !count) return P2DE_ERR_INVALID_ARGUMENT;
+  *count = s->launches;
+  return P2DE_OK;
+}
+
+int p2de_min_rho_rhoe(p2de_solver* s, double* min_rho, double* min_rhoe) {
+  if (!s || !min_rho || !min_rhoe) return P2DE_ERR_INVALID_ARGUMENT;
+  CK(cudaSetDevice(s->device));
+  long long init[2] = {0x7ff0000000000000LL, 0x7ff0000000000000LL};
+  CK(cudaMemcpyAsync(s->minbuf, init, sizeof init, cudaMemcpyHostToDevice, s->stream));
+  size_t nodes = (size_t)s->Nq * s->K;
+  int grid = (int)std::min<size_t>((nodes + 255) / 256, 152 * 8);
+  k_min_rho_rhoe<<<grid, 256, 0, s->stream>>>(s->Uq, nodes, s->minbuf);
+  CK(cudaGetLastError());
+  s->launches += 1;
+  long long outk[2];
+  CK(cudaMemcpyAsync(outk, s->minbuf, sizeof outk, cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  *min_rho = key_to_double(outk[0]);
+  *min_rhoe = key_to_double(outk[1]);
+  return P2DE_OK;
+}
+
+int p2de_stage_minima(p2de_solver* s, double out[6]) {
+  if (!s || !out) return P2DE_ERR_INVALID_ARGUMENT;
+  CK(cudaSetDevice(s->device));
+  long long k[6];
+  CK(cudaMemcpyAsync(k, s->minrec, sizeof k, cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  for (int i = 0; i < 6; ++i) out[i] = key_to_double(k[i]);
+  return P2DE_OK;
+}
+
+int p2de_last_error(p2de_solver* s, char* buf, size_t len) {
+  if (!buf || len == 0) return P2DE_ERR_INVALID_ARGUMENT;
+  std::string m;
+  if (s)
+    m = s->err;
+  else {
+    std::lock_guard<std::mutex> lk(g_err_mu);
+    m = g_last_create_error;
+  }
+  std::snprintf(buf, len, "%s", m.c_str());
+  return P2DE_OK;
+}
+
+}  // extern "C"

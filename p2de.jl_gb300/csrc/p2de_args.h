@@ -1,0 +1,67 @@
+// Launch arguments shared by the host code and the stage kernels.
+#pragma once
+
+#include <stdint.h>
+
+#include "p2de_tables.h"
+
+namespace p2de {
+
+// flag bits of StageArgs::flags
+enum : int {
+  F_DO_LOW = 1 << 0,        // low-order graph-viscosity RHS
+  F_DO_HIGH = 1 << 1,       // high-order ES flux differencing RHS
+  F_DO_LIMIT = 1 << 2,      // subcell limiter
+  F_WRITE_DEBUG = 1 << 3,   // write rhsxyL/H, BF_L/H, rhsL, rhsH to global
+  F_AXIS_ALIGNED = 1 << 4,  // all elements have sxJ = ryJ = 0
+  F_REF_SEM = 1 << 5,       // reference 4-name destructuring of the 5-tuple bound
+  F_CELL_ENTROPY = 1 << 6,  // PositivityAndCellEntropyBound
+  F_UPDATE = 1 << 7,        // stage kernel B applies the SSP-RK3 stage update
+  F_RHSU_FROM_L = 1 << 8,   // rhsU = rhsL (LowOrderPositivity)
+  F_RHSU_FROM_H = 1 << 9,   // rhsU = rhsH (FluxDiffRHS)
+  F_CFL = 1 << 10           // stage 1: low-order positivity CFL reduction
+};
+
+// boundary codes per face node
+enum : int8_t { BC_INTERIOR = 0, BC_INFLOW = 1, BC_OUTFLOW = 2, BC_WALL = 3, BC_SHOCK = 4 };
+
+// device scalar slots
+enum : int { S_T = 0, S_DT_LIM = 1, S_DT = 2, S_DONE = 3, S_STEPS = 4, S_NSCAL = 8 };
+
+// status bits
+enum : int { ST_NOT_POSITIVE = 1, ST_BAD_DT = 2, ST_NAN = 4 };
+
+struct StageArgs {
+  int K;
+  int nstage;  // 1..3
+  int flags;
+  int pad_;
+  const OpTable* ops;
+  double* Uq;
+  double* resW;
+  const double* geom;     // K x 5: J, rxJ, sxJ, ryJ, syJ
+  const int32_t* nbr;     // Nfp x K: 0-based exterior face-node linear index (mapP - 1)
+  const int8_t* bc;       // Nfp x K boundary code
+  const int32_t* bcidx;   // Nfp x K index into Ival / xyS
+  const double* Ival;     // nI x 4
+  const double* xyS;      // nS x 2
+  double shock_x0, shock_inv_slope, shock_speed;
+  double shock_post[4], shock_pre[4];
+  double gamma, gm1, CFL, dt0, T, zeta, ZEROTOL;
+  double* rhsL;
+  double* rhsH;
+  double* rhsU;
+  double* rhsxyL;
+  double* rhsxyH;
+  double* BFL;
+  double* BFH;
+  double* fbar;  // K x (2 dirs x 2 (H, L) x NSF x 4)
+  double* Lpre;  // K x 2 x (Nq+N1D), before symmetrization
+  double* Lfin;  // 3 stages x K x 2 x (Nq+N1D)
+  double* scal;  // S_* slots
+  unsigned long long* dtmin_bits;
+  long long* minrec;  // 3 stages x {min rho, min rhoe} as ordered keys
+  int* status;
+};
+
+}  // namespace p2de

@@ -1,0 +1,975 @@
+// Stage kernels for tensor-product GLL elements of N1D = N+1 nodes per line.
+//
+// Stage kernel A (one block = E consecutive elements; every phase is a flat loop
+// over (element, item) so that the FP64 pipe, the bottleneck on this part, always
+// issues full warps):
+//   low-order graph-viscosity RHS      low_order_graph_viscosity.jl:4-41
+//   high-order ES flux differencing    flux_differencing.jl:4-37
+//   subcell bounds and cell entropy    subcell.jl:163-349, 462-744; limiter_utils.jl:66-132
+// Stage kernel B: symmetrization across element faces (subcell.jl:418-456), limited
+// subcell fluxes and rhsU (subcell.jl:841-924), SSP-RK3 stage combination
+// (SSPRK33.jl:127-135) and the per-stage positivity record.
+//
+// For LGL collocation two parts of the reference's computation are identities up to
+// rounding and are not evaluated:
+//  * the entropy projection of face values, u_vfun(v_ufun(U)) (rhs.jl:242-252; the
+//    reference itself notes "we can skip LGL instead of applying identity", rhs.jl:265);
+//  * the hybridized face-volume pairs (Nq+f, fq2q[f]) of Srsh_nnz, whose contributions
+//    to QF1[Nq+f] and QF1[fq2q[f]] cancel when MinvVhT (init.jl:171) lifts QF1[Nq+f]
+//    back onto node fq2q[f].
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "p2de_args.h"
+#include "p2de_physics.cuh"
+#include "p2de_tables.h"
+
+namespace p2de {
+
+__host__ __device__ constexpr int cmax(int a, int b) { return a > b ? a : b; }
+
+template <int N1D>
+struct Cfg {
+  static constexpr int n = N1D;
+  static constexpr int Nq = n * n;
+  static constexpr int Nfp = 4 * n;
+  static constexpr int NPL = 2 * n * (n - 1);
+  static constexpr int NPH = n * n * (n - 1);
+  static constexpr int NSF = n * (n + 1);  // subcell faces per direction = Nq + N1D
+  static constexpr int E = (128 / Nq) > 0 ? (128 / Nq) : 1;
+  static constexpr int THREADS = 128;
+  static constexpr int SCR = cmax(cmax(NPL * 9, NPH * 8), 16 * NSF);
+  // shared-memory doubles per element, kernel A
+  static constexpr int O_GEO = 0;                  // 16
+  static constexpr int O_U = O_GEO + 16;           // 4 Nq
+  static constexpr int O_PRIM = O_U + 4 * Nq;      // 6 Nq (later uL[4], Lrhoe)
+  static constexpr int O_FLUX = O_PRIM + 6 * Nq;   // 8 Nq (later vq)
+  static constexpr int O_WS = O_FLUX + 8 * Nq;     // 2 Nq
+  static constexpr int O_RXYL = O_WS + 2 * Nq;     // 8 Nq
+  static constexpr int O_RXYH = O_RXYL + 8 * Nq;   // 8 Nq
+  static constexpr int O_RHSL = O_RXYH + 8 * Nq;   // 4 Nq
+  static constexpr int O_LAMI = O_RHSL + 4 * Nq;   // Nq
+  static constexpr int O_BFL = O_LAMI + Nq;        // 8 Nfp
+  static constexpr int O_BFH = O_BFL + 8 * Nfp;    // 8 Nfp
+  static constexpr int O_LAMB = O_BFH + 8 * Nfp;   // Nfp
+  static constexpr int O_SCR = O_LAMB + Nfp;       // SCR
+  static constexpr int O_EV = O_SCR + SCR;         // 4 Nq
+  static constexpr int O_L = O_EV + 4 * Nq;        // 2 NSF
+  static constexpr int O_MISC = O_L + 2 * NSF;     // 4
+  static constexpr int PER_ELEM_A = O_MISC + 4;
+  static constexpr size_t SMEM_A = sizeof(double) * PER_ELEM_A * E;
+  // kernel B
+  static constexpr int PER_ELEM_B = 2 * NSF + 16 * NSF + 8 * NSF + 8;
+  static constexpr size_t SMEM_B = sizeof(double) * PER_ELEM_B * E;
+  static constexpr int FBAR = 16 * NSF;  // per element: [dir][H/L][face][c]
+};
+
+// ordered 64-bit key of a double (monotone for non-NaN values), for atomicMin
+__device__ __forceinline__ long long order_key(double x) {
+  long long b = __double_as_longlong(x);
+  return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+}
+
+// limiter_utils.jl:108-132
+__device__ __forceinline__ double rhoe_quadratic_solve(const double* U, const double* P, double Lrhoe,
+                                                       double ZEROTOL) {
+  if (Lrhoe == __longlong_as_double(0x7ff0000000000000LL)) return 1.0;
+  // limiter_utils.jl:141-146
+  double a = P[0] * P[3] - 1.0 / 2.0 * (P[1] * P[1] + P[2] * P[2]);
+  double b = U[3] * P[0] + U[0] * P[3] - U[1] * P[1] - U[2] * P[2] - P[0] * Lrhoe;
+  double c = U[3] * U[0] - 1.0 / 2.0 * (U[1] * U[1] + U[2] * U[2]) - U[0] * Lrhoe;
+  double l = 1.0;
+  double disc = b * b - 4.0 * a * c;
+  if (disc >= 0.0) {
+    double sq = sqrt(disc);
+    double r1 = (-b + sq) / (2.0 * a);
+    double r2 = (-b - sq) / (2.0 * a);
+    if (r1 > ZEROTOL && r2 > ZEROTOL) {
+      l = jmin(r1, r2);
+    } else if (r1 > ZEROTOL && r2 < -ZEROTOL) {
+      l = r1;
+    } else if (r2 > ZEROTOL && r1 < -ZEROTOL) {
+      l = r2;
+    }
+  }
+  return l;
+}
+
+// limiting_param (limiter_utils.jl:66-70) -> limiting_param_bound_rho_rhoe (:82-96)
+// for the positivity bounds: Lrho = zeta*rhoL, Lrhoe = zeta*rhoe(uL), Urhoe = Inf, and
+// Urho = 0 (the Lphi slot, reference destructuring) or Inf.
+__device__ __forceinline__ double limiting_param_pos(const double* U, const double* P, double Lrho, double Lrhoe,
+                                                     double Urho, double ZEROTOL) {
+  double l = 1.0;
+  double up = U[0] + P[0];
+  if (up < Lrho) l = jmax((Lrho - U[0]) / P[0], 0.0);
+  if (up > Urho) l = jmin(l, jmax((Urho - U[0]) / P[0], 0.0));
+  // l is +0 or positive here; the quadratic root is > ZEROTOL or 1, never NaN, so a
+  // zero l stays zero and the root need not be evaluated.
+  if (l == 0.0) return l;
+  l = jmin(l, rhoe_quadratic_solve(U, P, Lrhoe, ZEROTOL));
+  // second solve with Urhoe = Inf returns 1.0
+  return jmin(l, 1.0);
+}
+
+// =====================================================================================
+// Kernel A
+// =====================================================================================
+template <int N1D, typename TH>
+__global__ void __launch_bounds__(Cfg<N1D>::THREADS) k_stage_a(StageArgs a) {
+  using C = Cfg<N1D>;
+  constexpr int n = C::n, Nq = C::Nq, Nfp = C::Nfp, NSF = C::NSF;
+  constexpr int PE = C::PER_ELEM_A;
+  if (a.scal[S_DONE] != 0.0) return;
+  extern __shared__ double sm[];
+  const OpTable& op = *a.ops;
+  const int tid = threadIdx.x, bs = blockDim.x;
+  const int k0 = blockIdx.x * C::E;
+  const int Ke = min(C::E, a.K - k0);
+  if (Ke <= 0) return;
+  const int flags = a.flags;
+  const bool aa = flags & F_AXIS_ALIGNED;
+  Gas<double> g{a.gamma, a.gm1, 2.0 * a.gm1};
+  const double dt_lim = a.scal[S_DT_LIM];
+  const double t_now = a.scal[S_T];
+
+  // ---- P0: geometry and state
+  for (int e = tid; e < Ke; e += bs) {
+    double* G = sm + e * PE + C::O_GEO;
+    const double* gg = a.geom + 5 * (size_t)(k0 + e);
+    double J = gg[0], rxJ = gg[1], sxJ = gg[2], ryJ = gg[3], syJ = gg[4];
+    G[0] = J;
+    G[1] = rxJ;
+    G[2] = sxJ;
+    G[3] = ryJ;
+    G[4] = syJ;
+    double gr = sqrt(rxJ * rxJ + ryJ * ryJ), gs = sqrt(sxJ * sxJ + syJ * syJ);
+    G[5] = gr;
+    G[6] = rxJ / gr;
+    G[7] = ryJ / gr;
+    G[8] = gs;
+    G[9] = sxJ / gs;
+    G[10] = syJ / gs;
+  }
+  for (int w = tid; w < Ke * Nq * 4; w += bs) {
+    int e = w / (Nq * 4), r = w % (Nq * 4);
+    sm[e * PE + C::O_U + r] = a.Uq[(size_t)k0 * Nq * 4 + w];
+  }
+  __syncthreads();
+
+  // ---- P1: per-node primitives, fluxes, wavespeeds along the r- and s-normals
+  const bool do_low = flags & F_DO_LOW, do_high = flags & F_DO_HIGH;
+  for (int w = tid; w < Ke * Nq; w += bs) {
+    int e = w / Nq, m = w % Nq;
+    double* base = sm + e * PE;
+    const double* G = base + C::O_GEO;
+    const double* U = base + C::O_U + 4 * m;
+    double rho = U[0], rhou = U[1], rhov = U[2], E = U[3];
+    double p = pfun(g, rho, rhou, rhov, E);
+    double u = rhou / rho, v = rhov / rho;
+    double* F = base + C::O_FLUX + 8 * m;
+    F[0] = rhou;
+    F[1] = rhou * u + p;
+    F[2] = rho * u * v;
+    F[3] = u * (E + p);
+    F[4] = rhov;
+    F[5] = F[2];
+    F[6] = rhov * v + p;
+    F[7] = v * (E + p);
+    double* Ws = base + C::O_WS + 2 * m;
+    Ws[0] = wavespeed_un(g, rho, G[6] * rhou + G[7] * rhov, E);
+    Ws[1] = wavespeed_un(g, rho, G[9] * rhou + G[10] * rhov, E);
+    if (do_high) {
+      double* Pm = base + C::O_PRIM + 6 * m;
+      double beta = rho / (2.0 * p);
+      Pm[0] = rho;
+      Pm[1] = u;
+      Pm[2] = v;
+      Pm[3] = beta;
+      if (sizeof(TH) == 8) {
+        Pm[4] = log(rho);
+        Pm[5] = log(beta);
+      }
+    }
+  }
+  __syncthreads();
+
+  // ---- P2: low-order volume pairs (accumulate_low_order_rhs_volume!, :139-173)
+  if (do_low) {
+    for (int w = tid; w < Ke * C::NPL; w += bs) {
+      int e = w / C::NPL, pp = w % C::NPL;
+      double* base = sm + e * PE;
+      const double* G = base + C::O_GEO;
+      int i = op.lp_i[pp], j = op.lp_j[pp], ax = op.lp_axis[pp];
+      double S = op.lp_S[pp];
+      double g1 = ax == 0 ? G[1] : G[2], g2 = ax == 0 ? G[3] : G[4], gn = ax == 0 ? G[5] : G[8];
+      double S0x = g1 * S, S0y = g2 * S;
+      double nn = fabs(S) * gn;
+      double wsi = base[C::O_WS + 2 * i + ax], wsj = base[C::O_WS + 2 * j + ax];
+      double lam = nn * jmax(wsi, wsj);
+      const double* Ui = base + C::O_U + 4 * i;
+      const double* Uj = base + C::O_U + 4 * j;
+      const double* Fi = base + C::O_FLUX + 8 * i;
+      const double* Fj = base + C::O_FLUX + 8 * j;
+      double* out = base + C::O_SCR + 9 * pp;
+      bool visc_x = fabs(S0x) > 1e-10;
+      double tx = 2.0 * S0x, ty = 2.0 * S0y;
+      if (!aa || ax == 0) {
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          double Fx = 0.5 * (Fi[c] + Fj[c]);
+          double vis = visc_x ? lam * (Uj[c] - Ui[c]) : 0.0;
+          out[c] = tx * Fx - vis;
+        }
+      } else {
+#pragma unroll
+        for (int c = 0; c < 4; ++c) out[c] = 0.0;
+      }
+      if (!aa || ax == 1) {
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          double Fy = 0.5 * (Fi[4 + c] + Fj[4 + c]);
+          double vis = visc_x ? 0.0 : lam * (Uj[c] - Ui[c]);
+          out[4 + c] = ty * Fy - vis;
+        }
+      } else {
+#pragma unroll
+        for (int c = 0; c < 4; ++c) out[4 + c] = 0.0;
+      }
+      out[8] = lam;
+    }
+    __syncthreads();
+    // ---- P3: gather Q0F1 in the order of the nnz loop; rhsxyL = 0 - Q0F1
+    for (int w = tid; w < Ke * Nq; w += bs) {
+      int e = w / Nq, m = w % Nq;
+      double* base = sm + e * PE;
+      double Q[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+      double lam = 0.0;
+      int cnt = op.lg_count[m];
+      for (int t = 0; t < cnt; ++t) {
+        int pp = op.lg_pair[m][t];
+        const double* sf = base + C::O_SCR + 9 * pp;
+        if (op.lg_sign[m][t] > 0) {
+#pragma unroll
+          for (int c = 0; c < 8; ++c) Q[c] = Q[c] + sf[c];
+        } else {
+#pragma unroll
+          for (int c = 0; c < 8; ++c) Q[c] = Q[c] + (-sf[c]);
+        }
+        lam += sf[8];
+      }
+      double* R = base + C::O_RXYL + 8 * m;
+#pragma unroll
+      for (int c = 0; c < 8; ++c) R[c] = 0.0 - Q[c];
+      base[C::O_LAMI + m] = lam;
+    }
+  }
+  __syncthreads();
+
+  // ---- P4: surface terms, shared by the low-order (:175-204) and high-order
+  //          (flux_differencing.jl:90-151, 223-272) paths
+  for (int w = tid; w < Ke * Nfp; w += bs) {
+    int e = w / Nfp, f = w % Nfp;
+    const int k = k0 + e;
+    double* base = sm + e * PE;
+    const double* G = base + C::O_GEO;
+    int side = f / n, tt = f % n;
+    int q = side == 0 ? n * tt : side == 1 ? (n - 1) + n * tt : side == 2 ? tt : tt + n * (n - 1);
+    double wt = op.w1D[tt];
+    double Bf = (side == 0 || side == 2) ? -wt : wt;
+    bool xs = side < 2;
+    double g1 = xs ? G[1] : G[2], g2 = xs ? G[3] : G[4], gn = xs ? G[5] : G[8];
+    double nh1 = xs ? G[6] : G[9], nh2 = xs ? G[7] : G[10];
+    double B1 = g1 * Bf, B2 = g2 * Bf;
+    double nn = wt * gn;
+    double n1 = Bf < 0 ? -nh1 : nh1, n2 = Bf < 0 ? -nh2 : nh2;
+    const double* Uf = base + C::O_U + 4 * q;
+    double ws_own = base[C::O_WS + 2 * q + (xs ? 0 : 1)];
+    size_t fk = (size_t)k * Nfp + f;
+    int lin = a.nbr[fk];
+    double wsP;
+    double Unb[4];
+    if (lin == (int)fk) {
+      wsP = ws_own;
+#pragma unroll
+      for (int c = 0; c < 4; ++c) Unb[c] = Uf[c];
+    } else {
+      int kP = lin / Nfp, iP = lin % Nfp;
+      int sP = iP / n, tP = iP % n;
+      int qP = sP == 0 ? n * tP : sP == 1 ? (n - 1) + n * tP : sP == 2 ? tP : tP + n * (n - 1);
+      if (kP >= k0 && kP < k0 + Ke) {
+        const double* src = sm + (kP - k0) * PE + C::O_U + 4 * qP;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) Unb[c] = src[c];
+      } else {
+        const double* src = a.Uq + ((size_t)kP * Nq + qP) * 4;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) Unb[c] = __ldg(src + c);
+      }
+      wsP = wavespeed(g, Unb, n1, n2);
+    }
+    int code = a.bc[fk];
+    double uP[4];
+    if (code == BC_INTERIOR) {
+#pragma unroll
+      for (int c = 0; c < 4; ++c) uP[c] = Unb[c];
+    } else if (code == BC_INFLOW) {
+      const double* iv = a.Ival + 4 * (size_t)a.bcidx[fk];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) uP[c] = iv[c];
+    } else if (code == BC_OUTFLOW) {
+#pragma unroll
+      for (int c = 0; c < 4; ++c) uP[c] = Uf[c];
+    } else if (code == BC_WALL) {
+      double mn = Uf[1] * n1 + Uf[2] * n2;
+      uP[0] = Uf[0];
+      uP[1] = Uf[1] - 2.0 * mn * n1;
+      uP[2] = Uf[2] - 2.0 * mn * n2;
+      uP[3] = Uf[3];
+    } else {
+      const double* xy = a.xyS + 2 * (size_t)a.bcidx[fk];
+      bool post = xy[0] < a.shock_x0 + (xy[1] + a.shock_speed * t_now) * a.shock_inv_slope;
+#pragma unroll
+      for (int c = 0; c < 4; ++c) uP[c] = post ? a.shock_post[c] : a.shock_pre[c];
+    }
+    double lamB = 0.5 * nn * jmax(ws_own, wsP);
+    double fPx[4], fPy[4];
+    fluxes(g, uP, fPx, fPy);
+    const double* Ff = base + C::O_FLUX + 8 * q;
+    double fsx[4], fsy[4], lf[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      fsx[c] = 0.5 * (Ff[c] + fPx[c]);
+      fsy[c] = 0.5 * (Ff[4 + c] + fPy[c]);
+      lf[c] = lamB * (uP[c] - Uf[c]);
+    }
+    double* BL = base + C::O_BFL + 8 * f;
+    double* BH = base + C::O_BFH + 8 * f;
+    bool lf_zero_high = (code == BC_INFLOW || code == BC_OUTFLOW || code == BC_SHOCK);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      double bx = B1 * fsx[c], by = B2 * fsy[c];
+      BL[c] = xs ? bx - lf[c] : bx;
+      BL[4 + c] = xs ? by : by - lf[c];
+      if (lf_zero_high) {
+        double lh = 0.0 * (uP[c] - Uf[c]);
+        BH[c] = xs ? bx - lh : bx;
+        BH[4 + c] = xs ? by : by - lh;
+      } else {
+        BH[c] = BL[c];
+        BH[4 + c] = BL[4 + c];
+      }
+    }
+    if (sizeof(TH) == 4 && do_high) {
+      // mixed precision: the high-order surface term in FP32
+      Gas<float> gf{(float)a.gamma, (float)a.gm1, (float)(2.0 * a.gm1)};
+      float uff[4], uPf[4], ffx[4], ffy[4], fpx[4], fpy[4];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        uff[c] = (float)Uf[c];
+        uPf[c] = (float)uP[c];
+      }
+      fluxes(gf, uff, ffx, ffy);
+      fluxes(gf, uPf, fpx, fpy);
+      float LFc = lf_zero_high ? 0.0f : (float)lamB;
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        float bx = (float)B1 * (0.5f * (ffx[c] + fpx[c]));
+        float by = (float)B2 * (0.5f * (ffy[c] + fpy[c]));
+        float l = LFc * (uPf[c] - uff[c]);
+        BH[c] = (double)(xs ? bx - l : bx);
+        BH[4 + c] = (double)(xs ? by : by - l);
+      }
+    }
+    base[C::O_LAMB + f] = lamB;
+  }
+  __syncthreads();
+
+  // ---- P5: finish the low-order RHS, scale by mass, positivity CFL
+  double dt_loc = __longlong_as_double(0x7ff0000000000000LL);
+  bool nan_seen = false;
+  if (do_low) {
+    for (int w = tid; w < Ke * Nq; w += bs) {
+      int e = w / Nq, m = w % Nq;
+      double* base = sm + e * PE;
+      int ir = m % n, is = m / n;
+      int fl[2], nf = 0;
+      if (ir == 0) fl[nf++] = is;
+      if (ir == n - 1) fl[nf++] = n + is;
+      if (is == 0) fl[nf++] = 2 * n + ir;
+      if (is == n - 1) fl[nf++] = 3 * n + ir;
+      double* R = base + C::O_RXYL + 8 * m;
+      double lam = base[C::O_LAMI + m];
+      for (int t = 0; t < nf; ++t) {
+        const double* BL = base + C::O_BFL + 8 * fl[t];
+#pragma unroll
+        for (int c = 0; c < 8; ++c) R[c] = R[c] - BL[c];
+        lam += base[C::O_LAMB + fl[t]];
+      }
+      double wJ = base[C::O_GEO] * op.wq[m];
+#pragma unroll
+      for (int c = 0; c < 8; ++c) R[c] = R[c] / wJ;
+      double* rl = base + C::O_RHSL + 4 * m;
+#pragma unroll
+      for (int c = 0; c < 4; ++c) rl[c] = R[c] + R[4 + c];
+      if (flags & F_CFL) {
+        double d = a.CFL * 0.5 * wJ / lam;
+        if (isnan(d)) nan_seen = true;
+        dt_loc = fmin(dt_loc, d);
+      }
+    }
+  }
+  if (flags & F_CFL) {
+    // block min of the CFL candidates
+    for (int o = 16; o > 0; o >>= 1) dt_loc = fmin(dt_loc, __shfl_xor_sync(0xffffffffu, dt_loc, o));
+    if ((tid & 31) == 0) {
+      if (dt_loc > 0.0) atomicMin(a.dtmin_bits, (unsigned long long)__double_as_longlong(dt_loc));
+      else if (dt_loc <= 0.0) atomicOr(a.status, ST_BAD_DT);
+    }
+    if (nan_seen) atomicOr(a.status, ST_NAN);
+  }
+  __syncthreads();
+
+  // ---- P6: high-order volume pairs (flux_differencing_volume!, :164-211)
+  if (do_high) {
+    for (int w = tid; w < Ke * C::NPH; w += bs) {
+      int e = w / C::NPH, pp = w % C::NPH;
+      double* base = sm + e * PE;
+      const double* G = base + C::O_GEO;
+      int i = op.hp_i[pp], j = op.hp_j[pp], ax = op.hp_axis[pp];
+      double S = op.hp_S[pp];
+      double Sxx = (ax == 0 ? G[1] : G[2]) * S, Sxy = (ax == 0 ? G[3] : G[4]) * S;
+      double* out = base + C::O_SCR + 8 * pp;
+      if (sizeof(TH) == 8) {
+        double Fx[4], Fy[4];
+        fS_f64(g, base + C::O_PRIM + 6 * i, base + C::O_PRIM + 6 * j, Fx, Fy);
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          out[c] = (!aa || ax == 0) ? Sxx * Fx[c] : 0.0;
+          out[4 + c] = (!aa || ax == 1) ? Sxy * Fy[c] : 0.0;
+        }
+      } else {
+        Gas<float> gf{(float)a.gamma, (float)a.gm1, (float)(2.0 * a.gm1)};
+        const double* Pi = base + C::O_PRIM + 6 * i;
+        const double* Pj = base + C::O_PRIM + 6 * j;
+        float UL[4] = {(float)Pi[0], (float)Pi[1], (float)Pi[2], (float)Pi[3]};
+        float UR[4] = {(float)Pj[0], (float)Pj[1], (float)Pj[2], (float)Pj[3]};
+        float Fx[4], Fy[4];
+        fS_f32(gf, UL, UR, Fx, Fy);
+        float sx = (float)Sxx, sy = (float)Sxy;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          out[c] = (!aa || ax == 0) ? (double)(sx * Fx[c]) : 0.0;
+          out[4 + c] = (!aa || ax == 1) ? (double)(sy * Fy[c]) : 0.0;
+        }
+      }
+    }
+    __syncthreads();
+    // ---- P7: gather QF1, lift and assemble (assemble_rhs!, :331-361)
+    for (int w = tid; w < Ke * Nq; w += bs) {
+      int e = w / Nq, m = w % Nq;
+      double* base = sm + e * PE;
+      int ir = m % n, is = m / n;
+      int fl[2], nf = 0;
+      if (ir == 0) fl[nf++] = is;
+      if (ir == n - 1) fl[nf++] = n + is;
+      if (is == 0) fl[nf++] = 2 * n + ir;
+      if (is == n - 1) fl[nf++] = 3 * n + ir;
+      double J = base[C::O_GEO];
+      double rw = op.rwq[m];
+      double* R = base + C::O_RXYH + 8 * m;
+      int cnt = op.hg_count[m];
+      if (sizeof(TH) == 8) {
+        double Q[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        for (int t = 0; t < cnt; ++t) {
+          const double* sf = base + C::O_SCR + 8 * op.hg_pair[m][t];
+          if (op.hg_sign[m][t] > 0) {
+#pragma unroll
+            for (int c = 0; c < 8; ++c) Q[c] = Q[c] + sf[c];
+          } else {
+#pragma unroll
+            for (int c = 0; c < 8; ++c) Q[c] = Q[c] + (-sf[c]);
+          }
+        }
+        double Bs[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        for (int t = 0; t < nf; ++t) {
+          const double* BH = base + C::O_BFH + 8 * fl[t];
+#pragma unroll
+          for (int c = 0; c < 8; ++c) Bs[c] = Bs[c] + rw * BH[c];
+        }
+#pragma unroll
+        for (int c = 0; c < 8; ++c) R[c] = (-(rw * Q[c] + Bs[c])) / J;
+      } else {
+        float Q[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        for (int t = 0; t < cnt; ++t) {
+          const double* sf = base + C::O_SCR + 8 * op.hg_pair[m][t];
+          float sg = op.hg_sign[m][t] > 0 ? 1.0f : -1.0f;
+#pragma unroll
+          for (int c = 0; c < 8; ++c) Q[c] = Q[c] + sg * (float)sf[c];
+        }
+        float rwf = (float)rw;
+        float Bs[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        for (int t = 0; t < nf; ++t) {
+          const double* BH = base + C::O_BFH + 8 * fl[t];
+#pragma unroll
+          for (int c = 0; c < 8; ++c) Bs[c] = Bs[c] + rwf * (float)BH[c];
+        }
+        float Jf = (float)J;
+#pragma unroll
+        for (int c = 0; c < 8; ++c) R[c] = (double)((-(rwf * Q[c] + Bs[c])) / Jf);
+      }
+    }
+  }
+  __syncthreads();
+
+  // ---- debug / non-limited outputs
+  const bool dbg = flags & F_WRITE_DEBUG;
+  const bool need_rhsL = dbg || (flags & F_RHSU_FROM_L);
+  const bool need_rhsH = dbg || (flags & F_RHSU_FROM_H);
+  if (need_rhsL && do_low) {
+    for (int w = tid; w < Ke * Nq * 4; w += bs) {
+      int e = w / (Nq * 4), r = w % (Nq * 4);
+      a.rhsL[(size_t)k0 * Nq * 4 + w] = sm[e * PE + C::O_RHSL + r];
+    }
+  }
+  if (need_rhsH && do_high) {
+    for (int w = tid; w < Ke * Nq * 4; w += bs) {
+      int e = w / (Nq * 4), r = w % (Nq * 4);
+      int m = r / 4, c = r % 4;
+      const double* R = sm + e * PE + C::O_RXYH + 8 * m;
+      a.rhsH[(size_t)k0 * Nq * 4 + w] = R[c] + R[4 + c];
+    }
+  }
+  if (dbg) {
+    for (int w = tid; w < Ke * Nq * 8; w += bs) {
+      int e = w / (Nq * 8), r = w % (Nq * 8);
+      if (do_low) a.rhsxyL[(size_t)k0 * Nq * 8 + w] = sm[e * PE + C::O_RXYL + r];
+      if (do_high) a.rhsxyH[(size_t)k0 * Nq * 8 + w] = sm[e * PE + C::O_RXYH + r];
+    }
+    for (int w = tid; w < Ke * Nfp * 8; w += bs) {
+      int e = w / (Nfp * 8), r = w % (Nfp * 8);
+      a.BFL[(size_t)k0 * Nfp * 8 + w] = sm[e * PE + C::O_BFL + r];
+      a.BFH[(size_t)k0 * Nfp * 8 + w] = sm[e * PE + C::O_BFH + r];
+    }
+  }
+  if (!(flags & F_DO_LIMIT)) return;
+
+  // ---- P8: subcell flux prefix sums (accumulate_f_bar!(::Dim2), subcell.jl:163-206)
+  //          and the low-order update uL = U + dt*rhsL (subcell.jl:269)
+  for (int w = tid; w < Ke * 8 * n; w += bs) {
+    int e = w / (8 * n), r = w % (8 * n);
+    int d = r / (4 * n), l = (r / 4) % n, c = r % 4;
+    double* base = sm + e * PE;
+    double J = base[C::O_GEO];
+    double* fb = base + C::O_SCR;  // [d][HL][face][c]
+    double* fH = fb + (d * 2 + 0) * NSF * 4;
+    double* fL = fb + (d * 2 + 1) * NSF * 4;
+    if (d == 0) {
+      int sj = l;
+      double h = base[C::O_BFH + 8 * sj + c], lo = base[C::O_BFL + 8 * sj + c];
+      fH[(0 + (n + 1) * sj) * 4 + c] = h;
+      fL[(0 + (n + 1) * sj) * 4 + c] = lo;
+      for (int si = 1; si <= n; ++si) {
+        int q = (si - 1) + n * sj;
+        double wJ = op.wq[q] * J;
+        h = h + wJ * base[C::O_RXYH + 8 * q + c];
+        lo = lo + wJ * base[C::O_RXYL + 8 * q + c];
+        fH[(si + (n + 1) * sj) * 4 + c] = h;
+        fL[(si + (n + 1) * sj) * 4 + c] = lo;
+      }
+    } else {
+      int si = l;
+      double h = base[C::O_BFH + 8 * (2 * n + si) + 4 + c], lo = base[C::O_BFL + 8 * (2 * n + si) + 4 + c];
+      fH[(si + n * 0) * 4 + c] = h;
+      fL[(si + n * 0) * 4 + c] = lo;
+      for (int sj = 1; sj <= n; ++sj) {
+        int q = si + n * (sj - 1);
+        double wJ = op.wq[q] * J;
+        h = h + wJ * base[C::O_RXYH + 8 * q + 4 + c];
+        lo = lo + wJ * base[C::O_RXYL + 8 * q + 4 + c];
+        fH[(si + n * sj) * 4 + c] = h;
+        fL[(si + n * sj) * 4 + c] = lo;
+      }
+    }
+  }
+  for (int w = tid; w < Ke * Nq; w += bs) {
+    int e = w / Nq, m = w % Nq;
+    double* base = sm + e * PE;
+    const double* U = base + C::O_U + 4 * m;
+    const double* rl = base + C::O_RHSL + 4 * m;
+    double* uL = base + C::O_PRIM + 6 * m;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) uL[c] = U[c] + dt_lim * rl[c];
+    uL[4] = a.zeta * rhoe_ufun(uL[0], uL[1], uL[2], uL[3]);
+  }
+  __syncthreads();
+
+  // ---- P9: bound evaluations, four per node (subcell_bound_limiter!(::Dim2), :288-341)
+  const double Urho = (flags & F_REF_SEM) ? 0.0 : __longlong_as_double(0x7ff0000000000000LL);
+  for (int w = tid; w < Ke * 4 * Nq; w += bs) {
+    int e = w / (4 * Nq), r = w % (4 * Nq);
+    int dh = r / Nq, m = r % Nq;
+    int ir = m % n, is = m / n;
+    double* base = sm + e * PE;
+    const double* fb = base + C::O_SCR;
+    int d = dh >> 1, h = dh & 1;
+    int fi;
+    if (d == 0)
+      fi = (ir + h) + (n + 1) * is;
+    else
+      fi = ir + n * (is + h);
+    const double* fH = fb + ((d * 2 + 0) * NSF + fi) * 4;
+    const double* fL = fb + ((d * 2 + 1) * NSF + fi) * 4;
+    double wJ = op.wq[m] * base[C::O_GEO];
+    double s4 = (h == 0 ? -4.0 : 4.0) * dt_lim;
+    double P[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) P[c] = s4 * (fH[c] - fL[c]) / wJ;
+    const double* uL = base + C::O_PRIM + 6 * m;
+    double Lrho = a.zeta * uL[0];
+    base[C::O_EV + r] = limiting_param_pos(uL, P, Lrho, uL[4], Urho, a.ZEROTOL);
+  }
+  __syncthreads();
+
+  // ---- P10: combine evaluations per subcell face; blending factor 1 (NoShockCapture)
+  for (int w = tid; w < Ke * 2 * NSF; w += bs) {
+    int e = w / (2 * NSF), r = w % (2 * NSF);
+    int d = r / NSF, fi = r % NSF;
+    double* base = sm + e * PE;
+    const double* ev = base + C::O_EV;
+    double L = 1.0;
+    if (d == 0) {
+      int si = fi % (n + 1), sj = fi / (n + 1);
+      if (si < n) L = jmin(L, ev[0 * Nq + si + n * sj]);
+      if (si > 0) L = jmin(L, ev[1 * Nq + (si - 1) + n * sj]);
+    } else {
+      int si = fi % n, sj = fi / n;
+      if (sj < n) L = jmin(L, ev[2 * Nq + si + n * sj]);
+      if (sj > 0) L = jmin(L, ev[3 * Nq + si + n * (sj - 1)]);
+    }
+    base[C::O_L + r] = jmin(L, 1.0);
+  }
+  __syncthreads();
+
+  // ---- P11: cell entropy bound (enforce_ES_subcell!, subcell.jl:462-744)
+  if (flags & F_CELL_ENTROPY) {
+    // An element-direction whose interior factors are all zero has sum(L*dvdf) = 0
+    // (or NaN) and the check of subcell.jl:676-677 is false: nothing to do.
+    for (int w = tid; w < Ke * 2; w += bs) {
+      int e = w / 2, d = w % 2;
+      double* base = sm + e * PE;
+      const double* L = base + C::O_L + d * NSF;
+      bool any = false;
+      for (int sj = 0; sj < n; ++sj)
+        for (int si = 1; si < n; ++si) {
+          double v = d == 0 ? L[si + (n + 1) * sj] : L[sj + n * si];
+          if (v != 0.0) any = true;
+        }
+      base[C::O_MISC + d] = any ? 1.0 : 0.0;
+    }
+    __syncthreads();
+    // entropy variables at the nodes of the elements that need them
+    for (int w = tid; w < Ke * Nq; w += bs) {
+      int e = w / Nq, m = w % Nq;
+      double* base = sm + e * PE;
+      if (base[C::O_MISC] == 0.0 && base[C::O_MISC + 1] == 0.0) continue;
+      const double* U = base + C::O_U + 4 * m;
+      double p = pfun(g, U[0], U[1], U[2], U[3]);
+      double s = log(p / pow(U[0], a.gamma));
+      double* vq = base + C::O_FLUX + 4 * m;
+      vq[0] = (a.gamma + 1.0 - s) - a.gm1 * U[3] / p;
+      vq[1] = U[1] * a.gm1 / p;
+      vq[2] = U[2] * a.gm1 / p;
+      vq[3] = -U[0] * a.gm1 / p;
+    }
+    __syncthreads();
+    for (int w = tid; w < Ke * 2; w += bs) {
+      int e = w / 2, d = w % 2;
+      double* base = sm + e * PE;
+      if (base[C::O_MISC + d] == 0.0) continue;
+      const double* G = base + C::O_GEO;
+      const double* vq = base + C::O_FLUX;
+      const double* fb = base + C::O_SCR;
+      const double* fH = fb + (d * 2 + 0) * NSF * 4;
+      const double* fL = fb + (d * 2 + 1) * NSF * 4;
+      double* L = base + C::O_L + d * NSF;
+      // sum_Bpsi over all face nodes in order (subcell.jl:521-529)
+      double sB = 0.0;
+      for (int f = 0; f < Nfp; ++f) {
+        int side = f / n, tt = f % n;
+        int q = side == 0 ? n * tt : side == 1 ? (n - 1) + n * tt : side == 2 ? tt : tt + n * (n - 1);
+        double Br = side == 0 ? -op.w1D[tt] : side == 1 ? op.w1D[tt] : 0.0;
+        double Bsv = side == 2 ? -op.w1D[tt] : side == 3 ? op.w1D[tt] : 0.0;
+        double Bd = d == 0 ? G[1] * Br + G[2] * Bsv : G[3] * Br + G[4] * Bsv;
+        double psi = a.gm1 * base[C::O_U + 4 * q + 1 + d];
+        sB = sB + Bd * psi;
+      }
+      constexpr int M = Nq - n;
+      double dvdf[M];
+      // dvdf and sum_dvfbarL (subcell.jl:540-562) in the reference loop order:
+      // x: line sj outer, face si = 1..n-1 inner, dvdf index (si-1) + (n-1)*sj;
+      // y: line si outer, face sj = 1..n-1 inner, dvdf index si + n*(sj-1).
+      double sdl = 0.0;
+      for (int a2 = 0; a2 < n; ++a2)
+        for (int b2 = 1; b2 < n; ++b2) {
+          int fi, idx, qm, qp;
+          if (d == 0) {
+            fi = b2 + (n + 1) * a2;
+            idx = (b2 - 1) + (n - 1) * a2;
+            qm = (b2 - 1) + n * a2;
+            qp = b2 + n * a2;
+          } else {
+            fi = a2 + n * b2;
+            idx = a2 + n * (b2 - 1);
+            qm = a2 + n * (b2 - 1);
+            qp = a2 + n * b2;
+          }
+          double pr_d[4], pr_l[4];
+#pragma unroll
+          for (int c = 0; c < 4; ++c) {
+            double fLc = fL[fi * 4 + c];
+            double dv = vq[4 * qm + c] - vq[4 * qp + c];
+            pr_d[c] = dv * (fH[fi * 4 + c] - fLc);
+            pr_l[c] = dv * fLc;
+          }
+          dvdf[idx] = ((pr_d[0] + pr_d[1]) + pr_d[2]) + pr_d[3];
+          sdl += ((pr_l[0] + pr_l[1]) + pr_l[2]) + pr_l[3];
+        }
+      // sum of L*dvdf (subcell.jl:654-670)
+      double sumLd = 0.0;
+      for (int a2 = 0; a2 < n; ++a2)
+        for (int b2 = 1; b2 < n; ++b2) {
+          int fi = d == 0 ? b2 + (n + 1) * a2 : a2 + n * b2;
+          int idx = d == 0 ? (b2 - 1) + (n - 1) * a2 : a2 + n * (b2 - 1);
+          sumLd += L[fi] * dvdf[idx];
+        }
+      double rhs = sB - sdl;
+      double est = sumLd - rhs;
+      double tol = jmax(0.0, sdl - sB);
+      if (est > tol) {
+        // sort (dvdf, index) descending in Julia's isless order, ties by index descending
+        int ord[M];
+        for (int i2 = 0; i2 < M; ++i2) ord[i2] = i2;
+        auto key_gt = [&](int x, int y) {  // true if (dvdf[x], x+1) sorts before (dvdf[y], y+1)
+          double vx = dvdf[x], vy = dvdf[y];
+          long long kx = isnan(vx) ? 0x7fffffffffffffffLL : order_key(vx);
+          long long ky = isnan(vy) ? 0x7fffffffffffffffLL : order_key(vy);
+          if (kx != ky) return kx > ky;
+          return x > y;
+        };
+        for (int i2 = 1; i2 < M; ++i2) {
+          int v = ord[i2];
+          int j2 = i2 - 1;
+          while (j2 >= 0 && key_gt(v, ord[j2])) {
+            ord[j2 + 1] = ord[j2];
+            --j2;
+          }
+          ord[j2 + 1] = v;
+        }
+        auto face_of_idx = [&](int idx) {  // 0-based dvdf index -> L face index
+          if (d == 0) {
+            int si = idx % (n - 1) + 1, sj = idx / (n - 1);
+            return si + (n + 1) * sj;
+          }
+          int si = idx % n, sj = idx / n + 1;
+          return si + n * sj;
+        };
+        int curr = 0;
+        double lhs = sumLd;
+        while (lhs > rhs + tol && curr < M) {
+          int idx = ord[curr];
+          if (dvdf[idx] < a.ZEROTOL) break;
+          lhs = lhs - L[face_of_idx(idx)] * dvdf[idx];
+          ++curr;
+        }
+        for (int i2 = 0; i2 < curr; ++i2) {
+          int idx = ord[i2];
+          int fi = face_of_idx(idx);
+          double l_new = (i2 == curr - 1) ? jmax((rhs + tol - lhs) / dvdf[idx], 0.0) : 0.0;
+          L[fi] = jmin(L[fi], l_new);
+        }
+      }
+    }
+    __syncthreads();
+  }
+
+  // ---- P12: L before symmetrization and the subcell fluxes for kernel B
+  for (int w = tid; w < Ke * 2 * NSF; w += bs) {
+    int e = w / (2 * NSF), r = w % (2 * NSF);
+    a.Lpre[(size_t)(k0 + e) * 2 * NSF + r] = sm[e * PE + C::O_L + r];
+  }
+  for (int w = tid; w < Ke * C::FBAR; w += bs) {
+    int e = w / C::FBAR, r = w % C::FBAR;
+    a.fbar[(size_t)(k0 + e) * C::FBAR + r] = sm[e * PE + C::O_SCR + r];
+  }
+}
+
+// =====================================================================================
+// Kernel B: symmetrize, blend, rhsU, SSP-RK3 stage update
+// =====================================================================================
+template <int N1D>
+__global__ void __launch_bounds__(Cfg<N1D>::THREADS) k_stage_b(StageArgs a) {
+  using C = Cfg<N1D>;
+  constexpr int n = C::n, Nq = C::Nq, Nfp = C::Nfp, NSF = C::NSF;
+  constexpr int PE = C::PER_ELEM_B;
+  if (a.scal[S_DONE] != 0.0) return;
+  extern __shared__ double sm[];
+  const OpTable& op = *a.ops;
+  const int tid = threadIdx.x, bs = blockDim.x;
+  const int k0 = blockIdx.x * C::E;
+  const int Ke = min(C::E, a.K - k0);
+  if (Ke <= 0) return;
+  const int flags = a.flags;
+  const int s = a.nstage - 1;
+  double dt;
+  if (a.nstage == 1 && (flags & F_UPDATE))
+    dt = __longlong_as_double((long long)*a.dtmin_bits);
+  else
+    dt = a.scal[S_DT];
+  const bool limited = flags & F_DO_LIMIT;
+  // smem: L [2 NSF], fbar [16 NSF], flim [8 NSF]
+  if (limited) {
+    for (int w = tid; w < Ke * 2 * NSF; w += bs) {
+      int e = w / (2 * NSF), r = w % (2 * NSF);
+      sm[e * PE + r] = a.Lpre[(size_t)(k0 + e) * 2 * NSF + r];
+    }
+    for (int w = tid; w < Ke * C::FBAR; w += bs) {
+      int e = w / C::FBAR, r = w % C::FBAR;
+      sm[e * PE + 2 * NSF + r] = a.fbar[(size_t)(k0 + e) * C::FBAR + r];
+    }
+    __syncthreads();
+    // symmetrize_limiting_parameters!(::Dim2) with subcell_index_P_x/y (limiter_utils.jl:179-237)
+    for (int w = tid; w < Ke * 4 * n; w += bs) {
+      int e = w / (4 * n), r = w % (4 * n);
+      int d = r / (2 * n), side = (r / n) % 2, tt = r % n;
+      const int k = k0 + e;
+      int iface, idx;
+      if (d == 0) {
+        iface = side ? tt + n : tt;
+        idx = (side ? n : 0) + (n + 1) * tt;
+      } else {
+        iface = side ? tt + 3 * n : tt + 2 * n;
+        idx = tt + n * (side ? n : 0);
+      }
+      int lin = a.nbr[(size_t)k * Nfp + iface];
+      int kP = lin / Nfp, iP = lin % Nfp;
+      int idxP;
+      if (d == 0) {
+        int sjP = iP % n;
+        int siP = (iP / n == 0) ? 0 : n;
+        idxP = siP + (n + 1) * sjP;
+      } else {
+        int siP = iP % n;
+        int sjP = (iP / n == 2) ? 0 : n;
+        idxP = siP + n * sjP;
+      }
+      double own = a.Lpre[(size_t)k * 2 * NSF + d * NSF + idx];
+      double par = a.Lpre[(size_t)kP * 2 * NSF + d * NSF + idxP];
+      sm[e * PE + d * NSF + idx] = jmin(own, par);
+    }
+    __syncthreads();
+    // accumulate_f_bar_limited!(::Dim2) (subcell.jl:841-876)
+    for (int w = tid; w < Ke * 2 * NSF * 4; w += bs) {
+      int e = w / (2 * NSF * 4), r = w % (2 * NSF * 4);
+      int d = r / (NSF * 4), fi = (r / 4) % NSF, c = r % 4;
+      double* base = sm + e * PE;
+      double l = base[d * NSF + fi];
+      const double* fb = base + 2 * NSF;
+      double fH = fb[((d * 2 + 0) * NSF + fi) * 4 + c];
+      double fL = fb[((d * 2 + 1) * NSF + fi) * 4 + c];
+      base[2 * NSF + 16 * NSF + (d * NSF + fi) * 4 + c] = l * fH + (1.0 - l) * fL;
+    }
+    __syncthreads();
+  }
+  // apply_subcell_limiter!(::Dim2) (subcell.jl:894-924) and the stage combination
+  double rmin = __longlong_as_double(0x7ff0000000000000LL), emin = rmin;
+  for (int w = tid; w < Ke * Nq; w += bs) {
+    int e = w / Nq, m = w % Nq;
+    const int k = k0 + e;
+    int ir = m % n, is = m / n;
+    double ru[4];
+    size_t gidx = ((size_t)k * Nq + m) * 4;
+    if (limited) {
+      const double* fl = sm + e * PE + 2 * NSF + 16 * NSF;
+      double wJ = op.wq[m] * a.geom[5 * (size_t)k];
+      const double* fx0 = fl + ((0 * NSF) + ir + (n + 1) * is) * 4;
+      const double* fx1 = fl + ((0 * NSF) + ir + 1 + (n + 1) * is) * 4;
+      const double* fy0 = fl + ((1 * NSF) + ir + n * is) * 4;
+      const double* fy1 = fl + ((1 * NSF) + ir + n * (is + 1)) * 4;
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        double x = (fx1[c] - fx0[c]) / wJ;
+        double y = (fy1[c] - fy0[c]) / wJ;
+        ru[c] = x + y;
+      }
+    } else if (flags & F_RHSU_FROM_L) {
+#pragma unroll
+      for (int c = 0; c < 4; ++c) ru[c] = a.rhsL[gidx + c];
+    } else {
+#pragma unroll
+      for (int c = 0; c < 4; ++c) ru[c] = a.rhsH[gidx + c];
+    }
+#pragma unroll
+    for (int c = 0; c < 4; ++c) a.rhsU[gidx + c] = ru[c];
+    if (flags & F_UPDATE) {
+      double U[4];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) U[c] = a.Uq[gidx + c];
+      if (a.nstage == 1) {
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          a.resW[gidx + c] = U[c];
+          U[c] = U[c] + dt * ru[c];
+        }
+      } else if (a.nstage == 2) {
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          double z = U[c] + dt * ru[c];
+          U[c] = 3.0 / 4.0 * a.resW[gidx + c] + 1.0 / 4.0 * z;
+        }
+      } else {
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          double z = U[c] + dt * ru[c];
+          U[c] = 1.0 / 3.0 * a.resW[gidx + c] + 2.0 / 3.0 * z;
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < 4; ++c) a.Uq[gidx + c] = U[c];
+      double re = rhoe_ufun(U[0], U[1], U[2], U[3]);
+      rmin = fmin(rmin, U[0]);
+      emin = fmin(emin, re);
+      if (!(U[0] > 0.0) || !(re > 0.0)) atomicOr(a.status, ST_NOT_POSITIVE);
+    }
+  }
+  if (limited) {
+    for (int w = tid; w < Ke * 2 * NSF; w += bs) {
+      int e = w / (2 * NSF), r = w % (2 * NSF);
+      a.Lfin[((size_t)s * a.K + k0 + e) * 2 * NSF + r] = sm[e * PE + r];
+    }
+  }
+  if (flags & F_UPDATE) {
+    for (int o = 16; o > 0; o >>= 1) {
+      rmin = fmin(rmin, __shfl_xor_sync(0xffffffffu, rmin, o));
+      emin = fmin(emin, __shfl_xor_sync(0xffffffffu, emin, o));
+    }
+    if ((tid & 31) == 0) {
+      atomicMin(&a.minrec[2 * s + 0], order_key(rmin));
+      atomicMin(&a.minrec[2 * s + 1], order_key(emin));
+    }
+    if (blockIdx.x == 0 && tid == 0) {
+      if (a.nstage == 1) {
+        a.scal[S_DT] = dt;
+        a.scal[S_DT_LIM] = dt;
+      }
+      if (a.nstage == 3) {
+        a.scal[S_T] = a.scal[S_T] + dt;
+        a.scal[S_STEPS] = a.scal[S_STEPS] + 1.0;
+      }
+    }
+  }
+}
+
+}  // namespace p2de

@@ -1,0 +1,189 @@
+// Host construction of the GLL operator tables (see p2de_tables.h).
+#include "p2de_tables.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+namespace p2de {
+
+// GLL nodes by Newton iteration on (1-x^2)P_N'(x) written with the Legendre
+// recurrence (Hesthaven & Warburton, Nodal Discontinuous Galerkin Methods, 2008,
+// sec. 3.2), weights 2/(N(N+1)P_N(x_i)^2), and the Lagrange differentiation matrix
+// D_ij = P_N(x_i)/(P_N(x_j)(x_i - x_j)), D_00 = -N(N+1)/4, D_NN = N(N+1)/4.
+void gll_rule(int N, double* r, double* w, double* D) {
+  const int Np = N + 1;
+  std::vector<double> x(Np), xold(Np), P(Np * (N + 1));
+  for (int i = 0; i < Np; ++i) x[i] = -std::cos(M_PI * i / N);
+  auto legendre = [&]() {
+    for (int i = 0; i < Np; ++i) {
+      double* Pi = &P[i * (N + 1)];
+      Pi[0] = 1.0;
+      if (N >= 1) Pi[1] = x[i];
+      for (int k = 2; k <= N; ++k) Pi[k] = ((2.0 * k - 1.0) * x[i] * Pi[k - 1] - (k - 1.0) * Pi[k - 2]) / k;
+    }
+  };
+  for (int it = 0; it < 100; ++it) {
+    xold = x;
+    legendre();
+    double err = 0.0;
+    for (int i = 0; i < Np; ++i) {
+      const double* Pi = &P[i * (N + 1)];
+      x[i] = xold[i] - (x[i] * Pi[N] - Pi[N - 1]) / (Np * Pi[N]);
+      err = std::max(err, std::fabs(x[i] - xold[i]));
+    }
+    if (err < 1e-16) break;
+  }
+  for (int i = 0; i < Np / 2; ++i) {
+    double a = 0.5 * (x[Np - 1 - i] - x[i]);
+    x[i] = -a;
+    x[Np - 1 - i] = a;
+  }
+  if (Np % 2 == 1) x[Np / 2] = 0.0;
+  x[0] = -1.0;
+  x[Np - 1] = 1.0;
+  legendre();
+  for (int i = 0; i < Np; ++i) {
+    double PN = P[i * (N + 1) + N];
+    r[i] = x[i];
+    w[i] = 2.0 / (N * Np * PN * PN);
+  }
+  for (int i = 0; i < Np; ++i)
+    for (int j = 0; j < Np; ++j) {
+      double v;
+      if (i != j)
+        v = P[i * (N + 1) + N] / (P[j * (N + 1) + N] * (x[i] - x[j]));
+      else if (i == 0)
+        v = -N * (N + 1) / 4.0;
+      else if (i == N)
+        v = N * (N + 1) / 4.0;
+      else
+        v = 0.0;
+      D[i * Np + j] = v;
+    }
+}
+
+int build_op_table(int N, double zerotol, OpTable* T) {
+  if (N < 1 || N + 1 > kMaxN1D) return 1;
+  std::memset(T, 0, sizeof(OpTable));
+  const int n = N + 1, Nq = n * n;
+  T->N1D = n;
+  T->Nq = Nq;
+  T->Nfp = 4 * n;
+  double r[kMaxN1D], w[kMaxN1D], D[kMaxN1D * kMaxN1D];
+  gll_rule(N, r, w, D);
+  for (int i = 0; i < n; ++i) T->w1D[i] = w[i];
+  // node i = ir + n*is; wq = wr .* ws
+  for (int is = 0; is < n; ++is)
+    for (int ir = 0; ir < n; ++ir) {
+      T->wq[ir + n * is] = w[ir] * w[is];
+      T->rwq[ir + n * is] = 1.0 / (w[ir] * w[is]);
+    }
+  // Qr = diag(wq) * kron(I, D1D), Qs = diag(wq) * kron(D1D, I), droptol'd
+  std::vector<double> Qr(Nq * Nq, 0.0), Qs(Nq * Nq, 0.0);  // row-major [i][j]
+  for (int is = 0; is < n; ++is)
+    for (int ir = 0; ir < n; ++ir)
+      for (int jr = 0; jr < n; ++jr) {
+        int i = ir + n * is, j = jr + n * is;
+        double q = T->wq[i] * D[ir * n + jr];
+        Qr[i * Nq + j] = std::fabs(q) <= zerotol ? 0.0 : q;
+      }
+  for (int ir = 0; ir < n; ++ir)
+    for (int is = 0; is < n; ++is)
+      for (int js = 0; js < n; ++js) {
+        int i = ir + n * is, j = ir + n * js;
+        double q = T->wq[i] * D[is * n + js];
+        Qs[i * Nq + j] = std::fabs(q) <= zerotol ? 0.0 : q;
+      }
+  // high-order pairs in the volume block of Srsh_db = Q - Q'
+  int p = 0;
+  for (int is = 0; is < n; ++is)
+    for (int ir = 1; ir < n; ++ir)
+      for (int jr = 0; jr < ir; ++jr) {
+        int i = ir + n * is, j = jr + n * is;
+        T->hp_i[p] = (int16_t)i;
+        T->hp_j[p] = (int16_t)j;
+        T->hp_axis[p] = 0;
+        T->hp_S[p] = Qr[i * Nq + j] - Qr[j * Nq + i];
+        ++p;
+      }
+  for (int ir = 0; ir < n; ++ir)
+    for (int is = 1; is < n; ++is)
+      for (int js = 0; js < is; ++js) {
+        int i = ir + n * is, j = ir + n * js;
+        T->hp_i[p] = (int16_t)i;
+        T->hp_j[p] = (int16_t)j;
+        T->hp_axis[p] = 1;
+        T->hp_S[p] = Qs[i * Nq + j] - Qs[j * Nq + i];
+        ++p;
+      }
+  T->nph = p;
+  // gather order per node: partners ascending (the order in which the j-outer,
+  // i-inner nnz loop of init.jl:188-195 touches the node)
+  for (int m = 0; m < Nq; ++m) {
+    std::vector<std::pair<int, int>> lst;  // (partner, pair id)
+    for (int q = 0; q < p; ++q) {
+      if (T->hp_i[q] == m) lst.push_back({T->hp_j[q], q});
+      if (T->hp_j[q] == m) lst.push_back({T->hp_i[q], q});
+    }
+    std::sort(lst.begin(), lst.end());
+    T->hg_count[m] = (int8_t)lst.size();
+    for (size_t t = 0; t < lst.size(); ++t) {
+      T->hg_pair[m][t] = (int16_t)lst[t].second;
+      T->hg_sign[m][t] = (T->hp_i[lst[t].second] == m) ? 1 : -1;
+    }
+  }
+  // low order: Q01D tridiagonal (init.jl:276-295), Qr0 = kron(M1D, Q01D), Qs0 = kron(Q01D, M1D)
+  std::vector<double> Q01(n * n, 0.0);  // row-major
+  for (int i = 0; i + 1 < n; ++i) {
+    Q01[(i + 1) * n + i] = -0.5;
+    Q01[i * n + (i + 1)] = 0.5;
+  }
+  Q01[0] = -0.5;
+  Q01[(n - 1) * n + (n - 1)] = 0.5;
+  auto Qr0 = [&](int i, int j) {
+    int ir = i % n, is = i / n, jr = j % n, js = j / n;
+    return (is == js ? w[is] : 0.0) * Q01[ir * n + jr];
+  };
+  auto Qs0 = [&](int i, int j) {
+    int ir = i % n, is = i / n, jr = j % n, js = j / n;
+    return Q01[is * n + js] * (ir == jr ? w[ir] : 0.0);
+  };
+  p = 0;
+  for (int is = 0; is < n; ++is)
+    for (int ir = 0; ir + 1 < n; ++ir) {
+      int i = (ir + 1) + n * is, j = ir + n * is;
+      T->lp_i[p] = (int16_t)i;
+      T->lp_j[p] = (int16_t)j;
+      T->lp_axis[p] = 0;
+      T->lp_S[p] = 0.5 * (Qr0(i, j) - Qr0(j, i));
+      ++p;
+    }
+  for (int ir = 0; ir < n; ++ir)
+    for (int is = 0; is + 1 < n; ++is) {
+      int i = ir + n * (is + 1), j = ir + n * is;
+      T->lp_i[p] = (int16_t)i;
+      T->lp_j[p] = (int16_t)j;
+      T->lp_axis[p] = 1;
+      T->lp_S[p] = 0.5 * (Qs0(i, j) - Qs0(j, i));
+      ++p;
+    }
+  T->npl = p;
+  for (int m = 0; m < Nq; ++m) {
+    std::vector<std::pair<int, int>> lst;
+    for (int q = 0; q < p; ++q) {
+      if (T->lp_i[q] == m) lst.push_back({T->lp_j[q], q});
+      if (T->lp_j[q] == m) lst.push_back({T->lp_i[q], q});
+    }
+    std::sort(lst.begin(), lst.end());
+    T->lg_count[m] = (int8_t)lst.size();
+    for (size_t t = 0; t < lst.size(); ++t) {
+      T->lg_pair[m][t] = (int16_t)lst[t].second;
+      T->lg_sign[m][t] = (T->lp_i[lst[t].second] == m) ? 1 : -1;
+    }
+  }
+  return 0;
+}
+
+}  // namespace p2de

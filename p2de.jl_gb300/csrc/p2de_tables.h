@@ -1,0 +1,51 @@
+// Operator tables for tensor-product GLL quads, one per N1D = N+1 in 2..6, built on
+// the host from the 1D GLL rule the way initialize_operators (src/dg/init.jl:133-228)
+// builds the dense operators, then reduced to the entries that are nonzero for LGL:
+//   Srh_db/Ssh_db volume blocks (Qr - Qr', init.jl:152-155) along r- and s-lines,
+//   Sr0/Ss0 (init.jl:312-322) on r- and s-neighbours,
+//   wq and 1/wq (the diagonal of M \ Vh', init.jl:171),
+// plus the pair lists and per-node gather orders that reproduce the accumulation
+// order of the nnz loops of init.jl:188-204.
+#pragma once
+
+#include <stdint.h>
+
+namespace p2de {
+
+constexpr int kMaxN1D = 6;
+constexpr int kMaxNq = kMaxN1D * kMaxN1D;
+constexpr int kMaxPairsHi = kMaxN1D * kMaxN1D * (kMaxN1D - 1);  // 180
+constexpr int kMaxPairsLo = 2 * kMaxN1D * (kMaxN1D - 1);        // 60
+
+struct OpTable {
+  int32_t N1D, Nq, Nfp, npl, nph;
+  int32_t pad_;
+  double w1D[kMaxN1D];
+  double wq[kMaxNq];
+  double rwq[kMaxNq];  // 1.0 / wq
+  // high-order volume pairs (i > j), r-lines first then s-lines
+  int16_t hp_i[kMaxPairsHi];
+  int16_t hp_j[kMaxPairsHi];
+  int8_t hp_axis[kMaxPairsHi];  // 0: r-line (Srh_db), 1: s-line (Ssh_db)
+  double hp_S[kMaxPairsHi];     // Srh_db[i,j] or Ssh_db[i,j]
+  // per-node gather list, partners in ascending node index: pair id, +1 when the node is i
+  int16_t hg_pair[kMaxNq][2 * (kMaxN1D - 1)];
+  int8_t hg_sign[kMaxNq][2 * (kMaxN1D - 1)];
+  // low-order pairs (i > j): r-neighbours first then s-neighbours
+  int16_t lp_i[kMaxPairsLo];
+  int16_t lp_j[kMaxPairsLo];
+  int8_t lp_axis[kMaxPairsLo];
+  double lp_S[kMaxPairsLo];  // Sr0[i,j] or Ss0[i,j]
+  int16_t lg_pair[kMaxNq][4];
+  int8_t lg_sign[kMaxNq][4];
+  int8_t lg_count[kMaxNq];
+  int8_t hg_count[kMaxNq];
+};
+
+// Builds the table for polynomial degree N (1..5). Returns 0 on success.
+int build_op_table(int N, double zerotol, OpTable* out);
+
+// The 1D GLL rule (nodes, weights) and differentiation matrix (row-major).
+void gll_rule(int N, double* r, double* w, double* D);
+
+}  // namespace p2de

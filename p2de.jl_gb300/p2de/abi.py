@@ -1,0 +1,169 @@
+"""ctypes binding of the C ABI declared in include/p2de.h (libp2de_gpu.so).
+
+The library is built in-tree (p2de.jl_gb300/_build). There is no CPU fallback:
+loading fails loudly when the library is missing.
+"""
+from __future__ import annotations
+
+import ctypes
+from ctypes import POINTER, c_char_p, c_double, c_int, c_int32, c_int64, c_size_t, c_void_p
+from pathlib import Path
+
+import numpy as np
+
+PKG_DIR = Path(__file__).resolve().parent.parent
+LIB_PATH = PKG_DIR / "_build" / "libp2de_gpu.so"
+
+# p2de_status
+P2DE_OK = 0
+STATUS_NAMES = {
+    0: "P2DE_OK",
+    1: "P2DE_ERR_INVALID_ARGUMENT",
+    2: "P2DE_ERR_UNSUPPORTED",
+    3: "P2DE_ERR_CUDA",
+    4: "P2DE_ERR_OUT_OF_MEMORY",
+    5: "P2DE_ERR_NOT_POSITIVE",
+    6: "P2DE_ERR_BAD_DT",
+    7: "P2DE_ERR_NO_DEVICE",
+    8: "P2DE_ERR_BUDGET",
+    9: "P2DE_ERR_NOT_FOUND",
+}
+
+# p2de_rhs_type
+RHS_ES_LIMITED_LOW_ORDER_POS = 0
+RHS_LOW_ORDER_POSITIVITY = 1
+RHS_ENTROPY_STABLE = 2
+# p2de_bound_type
+BOUND_POSITIVITY = 0
+BOUND_POSITIVITY_AND_CELL_ENTROPY = 1
+# p2de_surface_flux
+FLUX_LF_NODAL = 0
+FLUX_LF_PROJECTED = 1
+# p2de_precision
+PRECISION_FP64 = 0
+PRECISION_MIXED = 1
+# p2de_field
+FIELD_UQ = 0
+FIELD_RHSU = 1
+FIELD_RHSL = 2
+FIELD_RHSH = 3
+FIELD_RHSXYL = 4
+FIELD_RHSXYH = 5
+FIELD_BF_L = 6
+FIELD_BF_H = 7
+FIELD_L_LOCAL = 8
+FIELD_RESW = 9
+
+
+class P2deParam(ctypes.Structure):
+    _fields_ = [
+        ("N", c_int32),
+        ("K", c_int32),
+        ("gamma", c_double),
+        ("POSTOL", c_double),
+        ("ZEROTOL", c_double),
+        ("zeta", c_double),
+        ("eta", c_double),
+        ("CFL", c_double),
+        ("dt0", c_double),
+        ("t0", c_double),
+        ("T", c_double),
+        ("rhs_type", c_int32),
+        ("bound_type", c_int32),
+        ("low_order_surface_flux", c_int32),
+        ("high_order_surface_flux", c_int32),
+        ("reference_semantics", c_int32),
+        ("precision", c_int32),
+    ]
+
+
+class P2deMesh(ctypes.Structure):
+    _fields_ = [
+        ("geom", POINTER(c_double)),
+        ("mapP", POINTER(c_int64)),
+        ("mapI", POINTER(c_int64)),
+        ("nI", c_int64),
+        ("Ival", POINTER(c_double)),
+        ("mapO", POINTER(c_int64)),
+        ("nO", c_int64),
+        ("mapW", POINTER(c_int64)),
+        ("nW", c_int64),
+        ("mapS", POINTER(c_int64)),
+        ("nS", c_int64),
+        ("xyS", POINTER(c_double)),
+        ("shock_x0", c_double),
+        ("shock_inv_slope", c_double),
+        ("shock_speed", c_double),
+        ("shock_post", c_double * 4),
+        ("shock_pre", c_double * 4),
+    ]
+
+
+class P2deError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+# (name, restype, argtypes) of every entry point in include/p2de.h
+SOLVER_P = c_void_p
+EXPORTS = [
+    ("p2de_abi_version", c_int, []),
+    ("p2de_field_count", c_int, [c_int32, c_int32, c_int32, POINTER(c_int64)]),
+    ("p2de_initialize_DG", c_int, [POINTER(P2deParam), POINTER(P2deMesh), c_int, POINTER(c_void_p)]),
+    ("p2de_destroy", c_int, [SOLVER_P]),
+    ("p2de_set_Uq", c_int, [SOLVER_P, POINTER(c_double)]),
+    ("p2de_get_field", c_int, [SOLVER_P, c_int32, c_int32, POINTER(c_double)]),
+    ("p2de_rhs", c_int, [SOLVER_P, c_double, c_double, c_int32, POINTER(c_double)]),
+    ("p2de_ssp33_step", c_int, [SOLVER_P, POINTER(c_double), POINTER(c_double)]),
+    ("p2de_ssp33", c_int, [SOLVER_P, POINTER(c_double), POINTER(c_int64), POINTER(c_double)]),
+    ("p2de_ssp33_advance", c_int, [SOLVER_P, c_int64, POINTER(c_double), POINTER(c_int64)]),
+    ("p2de_device_ptr", c_int, [SOLVER_P, c_int32, POINTER(c_void_p)]),
+    ("p2de_set_stream", c_int, [SOLVER_P, c_void_p]),
+    ("p2de_launch_count", c_int, [SOLVER_P, POINTER(c_int64)]),
+    ("p2de_min_rho_rhoe", c_int, [SOLVER_P, POINTER(c_double), POINTER(c_double)]),
+    ("p2de_stage_minima", c_int, [SOLVER_P, POINTER(c_double)]),
+    ("p2de_last_error", c_int, [SOLVER_P, c_char_p, c_size_t]),
+]
+
+_LIB = None
+
+
+def load_library(path: Path | str | None = None) -> ctypes.CDLL:
+    """Loads libp2de_gpu.so and declares every export. Raises when it is missing."""
+    global _LIB
+    if _LIB is not None and path is None:
+        return _LIB
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise RuntimeError(
+            f"{p} is missing: build it with `python p2de.jl_gb300/build.py` "
+            "(there is no CPU fallback for the GPU path)"
+        )
+    lib = ctypes.CDLL(str(p))
+    for name, res, args in EXPORTS:
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _LIB = lib
+    return lib
+
+
+def last_error(lib, handle) -> str:
+    buf = ctypes.create_string_buffer(1024)
+    lib.p2de_last_error(handle, buf, len(buf))
+    return buf.value.decode(errors="replace")
+
+
+def check(lib, status: int, handle=None) -> None:
+    if status != P2DE_OK:
+        raise P2deError(status, last_error(lib, handle))
+
+
+def dptr(a: np.ndarray):
+    return a.ctypes.data_as(POINTER(c_double))
+
+
+def iptr(a: np.ndarray):
+    return a.ctypes.data_as(POINTER(c_int64))

@@ -1,0 +1,168 @@
+"""Uniform quadrilateral meshes with StartUpDG's conventions, as initialize_DG builds
+them (src/dg/init.jl:241-252, 265-274) and as make_periodic connects them
+(test/test_smoke.jl:22-36).
+
+Arrays mirror Julia's column-major (Nq, K) arrays: a numpy array of shape (K, Nq)
+in C order has Julia's memory layout, and so does (K, Nq, 4) for SVector{4} arrays.
+
+Conventions (StartUpDG Quad, SBP/LGL):
+  * elements ordered x fastest: k = ex + Kx*ey;
+  * nodes i = ir + (N+1)*is (r fastest), r along x, s along y;
+  * face nodes: faces r=-1, r=+1, s=-1, s=+1, each ordered along its tangent;
+  * mapP holds 1-based linear indices into (Nfp, K); boundary face nodes map to
+    themselves until make_periodic connects opposite sides.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field, replace
+
+import numpy as np
+
+
+def gll_rule(N: int) -> tuple[np.ndarray, np.ndarray]:
+    """GLL nodes and weights: Newton iteration on (1-x^2)P_N'(x) with the Legendre
+    recurrence (Hesthaven & Warburton 2008, sec. 3.2); weights 2/(N(N+1)P_N(x)^2)."""
+    Np = N + 1
+    x = -np.cos(np.pi * np.arange(Np) / N)
+
+    def legendre(xx):
+        P = np.zeros((Np, N + 1))
+        P[:, 0] = 1.0
+        if N >= 1:
+            P[:, 1] = xx
+        for k in range(2, N + 1):
+            P[:, k] = ((2.0 * k - 1.0) * xx * P[:, k - 1] - (k - 1.0) * P[:, k - 2]) / k
+        return P
+
+    for _ in range(100):
+        xold = x.copy()
+        P = legendre(x)
+        x = xold - (x * P[:, N] - P[:, N - 1]) / (Np * P[:, N])
+        if np.max(np.abs(x - xold)) < 1e-16:
+            break
+    for i in range(Np // 2):
+        a = 0.5 * (x[Np - 1 - i] - x[i])
+        x[i] = -a
+        x[Np - 1 - i] = a
+    if Np % 2 == 1:
+        x[Np // 2] = 0.0
+    x[0], x[-1] = -1.0, 1.0
+    P = legendre(x)
+    w = 2.0 / (N * Np * P[:, N] ** 2)
+    return x, w
+
+
+def face_to_node(N: int) -> np.ndarray:
+    """fq2q (0-based): volume node of each face node."""
+    n = N + 1
+    t = np.arange(n)
+    return np.concatenate([n * t, (n - 1) + n * t, t, t + n * (n - 1)])
+
+
+@dataclass
+class MeshData:
+    """The fields of StartUpDG's MeshData that P2DE.jl reads, for affine quads."""
+
+    N: int
+    K: tuple[int, int]
+    xL: tuple[float, float]
+    xR: tuple[float, float]
+    x: np.ndarray  # (K, Nq) node coordinates
+    y: np.ndarray
+    xf: np.ndarray  # (K, Nfp) face-node coordinates
+    yf: np.ndarray
+    mapM: np.ndarray  # (K, Nfp) 1-based
+    mapP: np.ndarray  # (K, Nfp) 1-based
+    mapB: np.ndarray  # boundary face nodes (1-based), those with mapP == mapM
+    geom: np.ndarray  # (K, 5): J, rxJ, sxJ, ryJ, syJ
+    sides: dict = field(default_factory=dict)  # 'left','right','bottom','top' -> 1-based face nodes
+
+    @property
+    def xq(self):
+        return self.x
+
+    @property
+    def yq(self):
+        return self.y
+
+    @property
+    def num_elements(self) -> int:
+        return self.K[0] * self.K[1]
+
+    @property
+    def J(self):
+        return self.geom[:, 0]
+
+
+def uniform_mesh(N: int, Kx: int, Ky: int, xL=(0.0, 0.0), xR=(1.0, 1.0)) -> MeshData:
+    n = N + 1
+    Nq, Nfp = n * n, 4 * n
+    K = Kx * Ky
+    r, _ = gll_rule(N)
+    hx = (xR[0] - xL[0]) / Kx
+    hy = (xR[1] - xL[1]) / Ky
+    k = np.arange(K)
+    ex, ey = k % Kx, k // Kx
+    ir = np.tile(np.arange(n), n)
+    is_ = np.repeat(np.arange(n), n)
+    x = xL[0] + hx * ex[:, None] + 0.5 * (r[ir][None, :] + 1.0) * hx
+    y = xL[1] + hy * ey[:, None] + 0.5 * (r[is_][None, :] + 1.0) * hy
+    fq2q = face_to_node(N)
+    xf, yf = x[:, fq2q], y[:, fq2q]
+    f = np.arange(Nfp)
+    mapM = 1 + f[None, :] + Nfp * k[:, None]
+    side, t = f // n, f % n
+    mapP = mapM.copy()
+    sides = {}
+    # r = -1 face of (ex, ey) <-> r = +1 face of (ex-1, ey), and so on
+    for s_, (dx, dy, other) in enumerate([(-1, 0, 1), (1, 0, 0), (0, -1, 3), (0, 1, 2)]):
+        fs = f[side == s_]
+        nx, ny = ex + dx, ey + dy
+        inside = (nx >= 0) & (nx < Kx) & (ny >= 0) & (ny < Ky)
+        kn = nx + Kx * ny
+        for ff in fs:
+            tt = ff % n
+            mapP[inside, ff] = 1 + (other * n + tt) + Nfp * kn[inside]
+        name = ["left", "right", "bottom", "top"][s_]
+        sides[name] = np.sort(np.concatenate([mapM[~inside, ff] for ff in fs]))
+    mapB = np.sort(mapM[mapP == mapM])
+    geom = np.zeros((K, 5))
+    geom[:, 0] = hx * hy / 4.0
+    geom[:, 1] = hy / 2.0
+    geom[:, 4] = hx / 2.0
+    return MeshData(N, (Kx, Ky), tuple(xL), tuple(xR), x, y, xf, yf, mapM, mapP, mapB, geom, sides)
+
+
+def make_periodic(md: MeshData, periodic=(True, True)) -> MeshData:
+    """Connects opposite boundary sides (StartUpDG make_periodic for a uniform mesh)."""
+    N = md.N
+    n = N + 1
+    Nfp = 4 * n
+    Kx, Ky = md.K
+    K = Kx * Ky
+    k = np.arange(K)
+    ex, ey = k % Kx, k // Kx
+    mapP = md.mapP.copy()
+    f = np.arange(Nfp)
+    side = f // n
+    sides = dict(md.sides)
+    if periodic[0]:
+        for s_, (dx, other) in enumerate([(-1, 1), (1, 0)]):
+            edge = (ex == 0) if dx < 0 else (ex == Kx - 1)
+            kn = ((ex + dx) % Kx) + Kx * ey
+            for ff in f[side == s_]:
+                tt = ff % n
+                mapP[edge, ff] = 1 + (other * n + tt) + Nfp * kn[edge]
+        sides["left"] = np.zeros(0, dtype=np.int64)
+        sides["right"] = np.zeros(0, dtype=np.int64)
+    if periodic[1]:
+        for s_, (dy, other) in zip((2, 3), [(-1, 3), (1, 2)]):
+            edge = (ey == 0) if dy < 0 else (ey == Ky - 1)
+            kn = ex + Kx * ((ey + dy) % Ky)
+            for ff in f[side == s_]:
+                tt = ff % n
+                mapP[edge, ff] = 1 + (other * n + tt) + Nfp * kn[edge]
+        sides["bottom"] = np.zeros(0, dtype=np.int64)
+        sides["top"] = np.zeros(0, dtype=np.int64)
+    mapB = np.sort(md.mapM[mapP == md.mapM])
+    return replace(md, mapP=mapP, mapB=mapB, sides=sides)

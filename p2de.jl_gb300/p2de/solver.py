@@ -1,0 +1,347 @@
+"""initialize_DG / rhs! / SSP33! on top of libp2de_gpu.so.
+
+Mirrors src/dg/init.jl:44-60 (initialize_DG), src/dg/rhs/rhs.jl:5-13 (rhs!) and
+src/timestepping/SSPRK33.jl:1-62 (SSP33!). `!` is not allowed in Python names,
+so rhs! and SSP33! are rhs_bang and SSP33_bang.
+"""
+from __future__ import annotations
+
+import ctypes
+from ctypes import byref, c_double, c_int64, c_void_p
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import abi
+from .mesh import MeshData, uniform_mesh
+from .types import (
+    BCData,
+    DataHistory,
+    ErrorData,
+    ESLimitedLowOrderPos,
+    EntropyStable,
+    LaxFriedrichsOnNodalVal,
+    LaxFriedrichsOnProjectedVal,
+    LobattoCollocation,
+    LowOrderPositivity,
+    NoEntropyProjectionLimiter,
+    NoShockCapture,
+    Param,
+    PositivityAndCellEntropyBound,
+    PositivityBound,
+    SubcellLimiter,
+    TimeParam,
+)
+
+
+class UnsupportedMethod(ValueError):
+    pass
+
+
+def _i64(a) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(a, dtype=np.int64).ravel())
+
+
+def _f64(a, shape=None) -> np.ndarray:
+    arr = np.ascontiguousarray(np.asarray(a, dtype=np.float64))
+    if shape is not None:
+        arr = arr.reshape(shape)
+    return arr
+
+
+@dataclass
+class Descriptor:
+    """The C descriptors of one solve plus the arrays they point into."""
+
+    param: abi.P2deParam
+    mesh: abi.P2deMesh
+    keep: tuple
+    N: int
+    K: int
+
+    @property
+    def Nq(self) -> int:
+        return (self.N + 1) ** 2
+
+    @property
+    def Nfp(self) -> int:
+        return 4 * (self.N + 1)
+
+
+def lower_param(param: Param, K: int) -> abi.P2deParam:
+    """Maps the dispatch types of Param to the C enums, rejecting what is not built."""
+    if not isinstance(param.approximation_basis, LobattoCollocation):
+        raise UnsupportedMethod("only LobattoCollocation (GLL) is built")
+    if not isinstance(param.entropyproj_limiter, NoEntropyProjectionLimiter):
+        raise UnsupportedMethod("only NoEntropyProjectionLimiter is built")
+    rhs = param.rhs
+    if isinstance(rhs, ESLimitedLowOrderPos):
+        rhs_type = abi.RHS_ES_LIMITED_LOW_ORDER_POS
+        low, high = rhs.low_order_surface_flux, rhs.high_order_surface_flux
+    elif isinstance(rhs, LowOrderPositivity):
+        rhs_type = abi.RHS_LOW_ORDER_POSITIVITY
+        low, high = rhs.surface_flux, LaxFriedrichsOnProjectedVal()
+    elif isinstance(rhs, EntropyStable):
+        rhs_type = abi.RHS_ENTROPY_STABLE
+        low, high = LaxFriedrichsOnNodalVal(), rhs.surface_flux
+    else:
+        raise UnsupportedMethod(f"rhs type {type(rhs).__name__} is not built")
+    if not isinstance(low, LaxFriedrichsOnNodalVal) or not isinstance(high, LaxFriedrichsOnProjectedVal):
+        raise UnsupportedMethod("surface fluxes: LaxFriedrichsOnNodalVal (low), LaxFriedrichsOnProjectedVal (high)")
+    lim = param.rhs_limiter
+    bound = abi.BOUND_POSITIVITY
+    if rhs_type == abi.RHS_ES_LIMITED_LOW_ORDER_POS:
+        if not isinstance(lim, SubcellLimiter) or not isinstance(lim.shockcapture, NoShockCapture):
+            raise UnsupportedMethod("LimitedDG needs SubcellLimiter(shockcapture=NoShockCapture())")
+        if isinstance(lim.bound, PositivityBound):
+            bound = abi.BOUND_POSITIVITY
+        elif isinstance(lim.bound, PositivityAndCellEntropyBound):
+            bound = abi.BOUND_POSITIVITY_AND_CELL_ENTROPY
+        else:
+            raise UnsupportedMethod(f"bound {type(lim.bound).__name__} is not built")
+    if param.precision not in ("fp64", "mixed"):
+        raise UnsupportedMethod("precision must be 'fp64' or 'mixed'")
+    gc, ts, lp = param.global_constants, param.timestepping_param, param.limiting_param
+    return abi.P2deParam(
+        N=param.N,
+        K=K,
+        gamma=param.equation.gamma,
+        POSTOL=gc.POSTOL,
+        ZEROTOL=gc.ZEROTOL,
+        zeta=lp.zeta,
+        eta=lp.eta,
+        CFL=ts.CFL,
+        dt0=ts.dt0,
+        t0=ts.t0,
+        T=ts.T,
+        rhs_type=rhs_type,
+        bound_type=bound,
+        low_order_surface_flux=abi.FLUX_LF_NODAL,
+        high_order_surface_flux=abi.FLUX_LF_PROJECTED,
+        reference_semantics=1 if param.reference_semantics else 0,
+        precision=abi.PRECISION_MIXED if param.precision == "mixed" else abi.PRECISION_FP64,
+    )
+
+
+def make_descriptor(param: Param, md: MeshData, bc: BCData) -> Descriptor:
+    K = md.num_elements
+    geom = _f64(md.geom)
+    mapP = _i64(bc.mapP)
+    mapI, mapO, mapW, mapS = _i64(bc.mapI), _i64(bc.mapO), _i64(bc.mapW), _i64(bc.mapS)
+    Ival = _f64(bc.Ival if len(bc.Ival) else np.zeros((0, 4))).reshape(-1, 4)
+    xyS = _f64(bc.xyS if len(bc.xyS) else np.zeros((0, 2))).reshape(-1, 2)
+    if mapP.size != K * 4 * (param.N + 1):
+        raise ValueError("mapP has the wrong size")
+    m = abi.P2deMesh()
+    m.geom = abi.dptr(geom)
+    m.mapP = abi.iptr(mapP)
+    m.mapI, m.nI = abi.iptr(mapI), mapI.size
+    m.Ival = abi.dptr(Ival)
+    m.mapO, m.nO = abi.iptr(mapO), mapO.size
+    m.mapW, m.nW = abi.iptr(mapW), mapW.size
+    m.mapS, m.nS = abi.iptr(mapS), mapS.size
+    m.xyS = abi.dptr(xyS)
+    m.shock_x0 = bc.shock_x0
+    m.shock_inv_slope = bc.shock_inv_slope
+    m.shock_speed = bc.shock_speed
+    for c in range(4):
+        m.shock_post[c] = bc.shock_post[c]
+        m.shock_pre[c] = bc.shock_pre[c]
+    p = lower_param(param, K)
+    return Descriptor(p, m, (geom, mapP, mapI, mapO, mapW, mapS, Ival, xyS), param.N, K)
+
+
+def evaluate_initial_condition(param: Param, md: MeshData, initial_condition) -> np.ndarray:
+    """init_U! (init.jl:342-361): Uq[i,k] = initial_condition(param, x, y), vectorised.
+    Returns (K, Nq, 4) float64 (Julia's Uq memory layout)."""
+    u = initial_condition(param, md.x, md.y)
+    if isinstance(u, (tuple, list)):
+        u = np.stack([np.broadcast_to(np.asarray(c, dtype=np.float64), md.x.shape) for c in u], axis=-1)
+    u = np.ascontiguousarray(np.asarray(u, dtype=np.float64))
+    if u.shape != md.x.shape + (4,):
+        raise ValueError(f"initial condition returned shape {u.shape}, expected {md.x.shape + (4,)}")
+    return u
+
+
+class Solver:
+    """Solver (Solver.jl:220-225) holding the GPU handle."""
+
+    def __init__(self, param: Param, md: MeshData, desc: Descriptor, device: int = 0):
+        self.param = param
+        self.md = md
+        self.desc = desc
+        self.lib = abi.load_library()
+        h = c_void_p()
+        st = self.lib.p2de_initialize_DG(byref(desc.param), byref(desc.mesh), device, byref(h))
+        abi.check(self.lib, st, None)
+        self.handle = h
+        self.K = desc.K
+        self.N = param.N
+        self.N1D = param.N + 1
+        self.Nq = self.N1D**2
+        self.Nfp = 4 * self.N1D
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self.lib.p2de_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st):
+        abi.check(self.lib, st, self.handle)
+
+    def field_count(self, field: int) -> int:
+        c = c_int64()
+        self._check(self.lib.p2de_field_count(self.N, self.K, field, byref(c)))
+        return c.value
+
+    def get_field(self, field: int, nstage: int = 1) -> np.ndarray:
+        out = np.empty(self.field_count(field), dtype=np.float64)
+        self._check(self.lib.p2de_get_field(self.handle, field, nstage, abi.dptr(out)))
+        return out
+
+    def set_Uq(self, Uq: np.ndarray) -> None:
+        U = np.ascontiguousarray(Uq, dtype=np.float64)
+        if U.size != self.field_count(abi.FIELD_UQ):
+            raise ValueError("Uq has the wrong size")
+        self._check(self.lib.p2de_set_Uq(self.handle, abi.dptr(U)))
+
+    def launch_count(self) -> int:
+        c = c_int64()
+        self._check(self.lib.p2de_launch_count(self.handle, byref(c)))
+        return c.value
+
+
+class State:
+    """State (State.jl:258-261): the preallocated arrays live on the device."""
+
+    def __init__(self, solver: Solver):
+        self._s = solver
+
+    @property
+    def Uq(self) -> np.ndarray:
+        return self._s.get_field(abi.FIELD_UQ).reshape(self._s.K, self._s.Nq, 4)
+
+    @Uq.setter
+    def Uq(self, value):
+        self._s.set_Uq(value)
+
+    def field(self, field: int, nstage: int = 1) -> np.ndarray:
+        return self._s.get_field(field, nstage)
+
+    @property
+    def rhsU(self):
+        return self.field(abi.FIELD_RHSU).reshape(self._s.K, self._s.Nq, 4)
+
+    @property
+    def rhsL(self):
+        return self.field(abi.FIELD_RHSL).reshape(self._s.K, self._s.Nq, 4)
+
+    @property
+    def rhsH(self):
+        return self.field(abi.FIELD_RHSH).reshape(self._s.K, self._s.Nq, 4)
+
+    def L_local(self, nstage: int) -> np.ndarray:
+        n = self._s.N1D
+        return self.field(abi.FIELD_L_LOCAL, nstage).reshape(self._s.K, 2, n * n + n)
+
+
+@dataclass
+class StateParam:
+    bcdata: BCData
+
+
+def initialize_DG(param: Param, initial_condition, initial_boundary_conditions, device: int = 0):
+    """initialize_DG(param, initial_condition, initial_boundary_conditions)
+    (init.jl:44-60) -> (solver, state, state_param)."""
+    md = uniform_mesh(param.N, param.K[0], param.K[1], param.xL, param.xR)
+    bcdata = initial_boundary_conditions(param, md)
+    desc = make_descriptor(param, md, bcdata)
+    solver = Solver(param, md, desc, device)
+    state = State(solver)
+    solver.set_Uq(evaluate_initial_condition(param, md, initial_condition))
+    return solver, state, StateParam(bcdata)
+
+
+def rhs_bang(state: State, solver: Solver, state_param: StateParam, time_param: TimeParam) -> float:
+    """rhs!(state, solver, state_param, time_param) (rhs.jl:5-13): fills rhsU, returns dt."""
+    out = c_double()
+    solver._check(solver.lib.p2de_rhs(solver.handle, time_param.t, time_param.dt, time_param.nstage, byref(out)))
+    return out.value
+
+
+def ssp33_step(solver: Solver, t: float) -> tuple[float, float]:
+    """One pass of the SSP33! loop body (SSPRK33.jl:125-139); returns (t_new, dt)."""
+    tt, dt = c_double(t), c_double()
+    solver._check(solver.lib.p2de_ssp33_step(solver.handle, byref(tt), byref(dt)))
+    return tt.value, dt.value
+
+
+def SSP33_bang(state: State, solver: Solver, state_param: StateParam, snapshots: bool = True) -> DataHistory:
+    """SSP33!(state, solver, state_param) (SSPRK33.jl:1-62). Steps on the device in
+    CUDA-graph chunks up to each snapshot index (mod(i, output_interval) == 0) and
+    records the final state, as the reference does at |t - T| < 1e-10."""
+    ts = solver.param.timestepping_param
+    interval = max(1, solver.param.postprocessing_param.output_interval)
+    t = ts.t0
+    i = 1
+    hist = DataHistory([], [], [], [], [])
+    while t < ts.T:
+        nxt = interval - (i % interval) if snapshots else 1 << 20
+        tt, done = c_double(t), c_int64()
+        solver._check(solver.lib.p2de_ssp33_advance(solver.handle, nxt, byref(tt), byref(done)))
+        if done.value == 0:
+            break
+        t = tt.value
+        i += done.value
+        if snapshots and (i % interval == 0 or abs(t - ts.T) < 1e-10):
+            hist.thist.append(t)
+            hist.Uhist.append(state.Uq.copy())
+            hist.Lhist.append(state.L_local(3).copy())
+    return hist
+
+
+def check_conservation(state: State, solver: Solver) -> float:
+    """check_conservation (src/dg/utils.jl:1-12): sum of J*wq*Uq over nodes and components."""
+    from .mesh import gll_rule
+
+    _, w = gll_rule(solver.N)
+    n = solver.N1D
+    wq = (w[np.tile(np.arange(n), n)] * w[np.repeat(np.arange(n), n)])
+    U = state.Uq
+    J = solver.md.geom[:, 0]
+    total = np.einsum("k,i,kic->c", J, wq, U)
+    return float(total.sum())
+
+
+def calculate_error(state: State, solver: Solver, exact_sol) -> ErrorData:
+    """calculate_error (src/dg/postprocess.jl:1-46): relative L1/L2/Linf summed over
+    components, against exact_sol(equation, x, y, T) returning (rho, u, v, p)."""
+    from .mesh import gll_rule
+    from .problems import primitive_to_conservative
+
+    _, w = gll_rule(solver.N)
+    n = solver.N1D
+    wq = (w[np.tile(np.arange(n), n)] * w[np.repeat(np.arange(n), n)])
+    U = state.Uq
+    md = solver.md
+    T = solver.param.timestepping_param.T
+    prim = exact_sol(solver.param.equation, md.x, md.y, T)
+    Ue = primitive_to_conservative(solver.param.equation, prim)
+    wJ = (wq[None, :] * md.geom[:, 0:1])[..., None]
+    err = np.abs(Ue - U)
+    L1e, L2e = (wJ * err).sum((0, 1)), (wJ * err**2).sum((0, 1))
+    Linfe = err.max((0, 1))
+    L1x, L2x = (wJ * np.abs(Ue)).sum((0, 1)), (wJ * Ue**2).sum((0, 1))
+    Linfx = np.abs(Ue).max((0, 1))
+    m = Linfx > 1e-14
+    return ErrorData(
+        float((L1e[m] / L1x[m]).sum()),
+        float((np.sqrt(L2e[m]) / np.sqrt(L2x[m])).sum()),
+        float((Linfe[m] / Linfx[m]).sum()),
+    )
