@@ -1,0 +1,382 @@
+#!/usr/bin/env python3
+"""DOF-stage updates/s of the P2DE.jl 2D Euler DG step (RHS + subcell limiter +
+SSP-RK3) on GB300.
+
+Workload (the large, limiter-heavy configuration): double Mach reflection on
+[0,4]x[0,1], 480x120 quads, N=3 (16 GLL nodes per element, 921,600 nodes), FP64,
+CFL 0.5, reflecting wall + inflow + outflow + moving-shock boundaries. A "step" is one
+SSP-RK3 step (three right-hand sides and stage updates); a DOF-stage update is one
+node (all four components) advanced through one RK stage.
+
+  value : device-resident state, CUDA-graph replay of the step, CUDA events on the
+          launching stream, K timed steps after W warm-up steps.
+  e2e   : the same steps through the public C ABI with host buffers: every step copies
+          Uq from pinned host memory to the device (p2de_set_Uq), steps
+          (p2de_ssp33_step) and reads Uq back (p2de_get_field).
+  roofline: stage kernel A (low-order RHS, high-order RHS, limiter bounds), FP64-pipe
+          bound; achieved = algorithmic FP64 operations / its mean event-timed launch;
+          peak = FP64 FMA throughput probed on this GPU in this run.
+  cpu_baseline / --impl reference: the FP64 CPU restatement (oracle/) with OpenMP on
+          all host cores; Julia, the reference's language, is not available.
+Multi-GPU: independent replicas (the path has no exchange between solves).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from ctypes import byref, c_double, c_int64, c_uint64
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "p2de.jl_gb300"))
+sys.path.insert(0, str(ROOT))
+
+METRIC = "DOF-stage updates/s, 2D Euler N=3; served solves/s + p99 vs plain, same L1 err"
+UNIT = "DOF-stage updates/s"
+
+# stage kernel A DRAM traffic per launch on this workload (dram__bytes_read.sum +
+# dram__bytes_write.sum of one ncu capture, profiles/k_stage_a_dmr480x120_n3_fp64.md)
+KERNEL_A_TRAFFIC_BYTES = 144.0e6
+
+
+def workload(name: str, precision: str):
+    from p2de import problems
+
+    if name == "dmr":
+        param, ic, bcf = problems.double_mach_reflection(N=3, Kx=480, Ky=120, T=0.2, precision=precision)
+        desc = "double Mach reflection 480x120 quads, N=3, SSP-RK3 CFL 0.5"
+    elif name == "kh256":
+        param, ic, bcf = problems.kelvin_helmholtz(N=3, Kx=256, Ky=256, T=1.0, precision=precision)
+        desc = "Kelvin-Helmholtz 256x256 quads, N=3, SSP-RK3 CFL 0.5"
+    else:
+        raise SystemExit(f"unknown workload {name}")
+    return param, ic, bcf, desc
+
+
+def build_descriptor(param, ic, bcf):
+    import p2de
+    from p2de import solver as S
+
+    md = p2de.uniform_mesh(param.N, *param.K, param.xL, param.xR)
+    bc = bcf(param, md)
+    desc = S.make_descriptor(param, md, bc)
+    U0 = S.evaluate_initial_condition(param, md, ic)
+    return md, bc, desc, U0
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    Q = (
+        "index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+        "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+        "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+    )
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=open(self.path, "w"),
+                stderr=subprocess.DEVNULL,
+            )
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        rows = []
+        try:
+            for line in open(self.path):
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        except Exception:
+            pass
+        finally:
+            if self.path:
+                try:
+                    os.unlink(self.path)
+                except OSError:
+                    pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {
+            "sm_mhz": statistics.median(sm) if sm else None,
+            "sm_max_mhz": max(mx) if mx else None,
+            "reasons": reasons,
+            "samples": len(rows),
+            "power_w_max": max(float(r[3]) for r in rows if r[3].replace(".", "").isdigit()) if rows else None,
+        }
+
+
+def cpu_baseline(desc, U0, nodes: int, budget_s: float = 12.0) -> dict:
+    """The FP64 oracle with OpenMP on every host core, over as many full steps of the
+    workload as fit in `budget_s` (at least one)."""
+    from oracle.binding import Oracle, num_threads
+
+    cores = os.cpu_count() or 1
+    o = Oracle(desc, nthreads=cores)
+    o.set_Uq(U0)
+    t = 0.0
+    t0 = time.perf_counter()
+    steps = 0
+    while True:
+        t, _ = o.step(t)
+        steps += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    el = time.perf_counter() - t0
+    o.close()
+    return {
+        "value": nodes * 3 * steps / el,
+        "unit": UNIT,
+        "cores": num_threads(),
+        "kind": "port",
+        "sample": f"{steps} full SSP-RK3 steps of the same workload from t=0 ({el:.1f} s, FP64 C++ restatement of P2DE.jl with OpenMP)",
+    }
+
+
+def run_reference(args):
+    """--impl reference: the CPU restatement on all host cores, same workload/metric."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    param, ic, bcf, wdesc = workload(args.workload, "fp64")
+    md, bc, desc, U0 = build_descriptor(param, ic, bcf)
+    from oracle.binding import Oracle, num_threads
+
+    cores = os.cpu_count() or 1
+    o = Oracle(desc, nthreads=cores)
+    o.set_Uq(U0)
+    nodes = desc.K * desc.Nq
+    t = 0.0
+    for _ in range(args.warmup):
+        t, _ = o.step(t)
+    budget = 150.0
+    t0 = time.perf_counter()
+    steps = 0
+    while steps < args.steps:
+        t, _ = o.step(t)
+        steps += 1
+        if time.perf_counter() - t0 > budget:
+            break
+    el = time.perf_counter() - t0
+    value = nodes * 3 * steps / el
+    sample = f"{steps} of {args.steps} requested full SSP-RK3 steps (time-capped at {budget:.0f} s), FP64 C++ restatement of P2DE.jl, OpenMP"
+    line = {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": value,
+        "unit": UNIT,
+        "n_gpus": args.gpus,
+        "steps": steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1e3 * el / steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": wdesc, "elements": desc.K, "nodes": nodes},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": num_threads(), "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="dmr", choices=["dmr", "kh256"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--e2e-steps", type=int, default=20)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+
+    from p2de import abi, roofline
+    from p2de import solver as S
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    param, ic, bcf, wdesc = workload(args.workload, args.precision)
+    md, bc, desc, U0 = build_descriptor(param, ic, bcf)
+    nodes = desc.K * desc.Nq
+    solver = S.Solver(param, md, desc, device=local)
+    lib = solver.lib
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    solver._check(lib.p2de_set_stream(solver.handle, ctypes.c_void_p(stream.cuda_stream)))
+    solver.set_Uq(U0)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+
+    # ---- warm-up and timed region (CUDA-graph replay, device-resident state)
+    t = c_double(0.0)
+    n = c_int64()
+    solver._check(lib.p2de_ssp33_advance(solver.handle, args.warmup, byref(t), byref(n)))
+    l0 = solver.launch_count()
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        solver._check(lib.p2de_ssp33_advance(solver.handle, args.steps, byref(t), byref(n)))
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    launches = solver.launch_count() - l0
+    steps_done = n.value
+    if dist is not None:
+        mt = torch.tensor([ms], device="cuda")
+        dist.all_reduce(mt, op=dist.ReduceOp.MAX)
+        ms = float(mt.item())
+    value = world * nodes * 3 * steps_done / (ms * 1e-3)
+    clocks = clk.summary()
+
+    # ---- per-kernel timing and the data-dependent work counter (same workload, live)
+    cnt = (c_uint64 * 1)()
+    solver._check(lib.p2de_read_counters(solver.handle, cnt, 1))
+    prof_steps = 5
+    kms = (c_double * 3)()
+    solver._check(lib.p2de_profile_steps(solver.handle, prof_steps, byref(t), kms))
+    solver._check(lib.p2de_read_counters(solver.handle, cnt, 1))
+    quad_per_launch = cnt[0] / (3 * prof_steps)
+    flops_a = roofline.stage_a_flops(param.N, desc.K, quad_per_launch)
+    peak = c_double()
+    solver._check(lib.p2de_probe_fma_peak(local, 1, byref(peak)))
+    achieved = flops_a / (kms[0] * 1e-3) / 1e12
+
+    # ---- end-to-end through the public ABI with host buffers
+    pinned = torch.empty(nodes * 4, dtype=torch.float64, pin_memory=True)
+    host = pinned.numpy()
+    solver._check(lib.p2de_get_field(solver.handle, abi.FIELD_UQ, 1, abi.dptr(host)))
+    te = c_double(t.value)
+    dte = c_double()
+    barrier()
+    e2, e3 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e2.record(stream)
+    for _ in range(args.e2e_steps):
+        solver._check(lib.p2de_set_Uq(solver.handle, abi.dptr(host)))
+        solver._check(lib.p2de_ssp33_step(solver.handle, byref(te), byref(dte)))
+        solver._check(lib.p2de_get_field(solver.handle, abi.FIELD_UQ, 1, abi.dptr(host)))
+    e3.record(stream)
+    torch.cuda.synchronize()
+    ms_e2e = e2.elapsed_time(e3)
+    if dist is not None:
+        mt = torch.tensor([ms_e2e], device="cuda")
+        dist.all_reduce(mt, op=dist.ReduceOp.MAX)
+        ms_e2e = float(mt.item())
+    e2e_value = world * nodes * 3 * args.e2e_steps / (ms_e2e * 1e-3)
+    mins = np.zeros(6)
+    solver._check(lib.p2de_stage_minima(solver.handle, abi.dptr(mins)))
+
+    if rank == 0:
+        cpu = None
+        if not args.no_cpu_baseline:
+            cpu = cpu_baseline(desc, U0, nodes)
+        bytes_ab = roofline.stage_bytes(param.N, desc.K)
+        line = {
+            "metric": METRIC,
+            "value": value,
+            "unit": UNIT,
+            "n_gpus": world,
+            "steps": steps_done,
+            "warmup": args.warmup,
+            "ms_per_step": ms / steps_done,
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "f64" if args.precision == "fp64" else "f64+f32 (mixed)",
+            "data": "synthetic",
+            "config": {
+                "workload": wdesc,
+                "elements": desc.K,
+                "nodes": nodes,
+                "precision": args.precision,
+                "parallelism": f"replicas x{world}" if world > 1 else "single solve",
+                "l2": "working set per step > L2 (stage data ~%.0f MB per launch)" % (bytes_ab["stage_a"] / 1e6),
+                "timing": "CUDA-graph replay of whole steps, CUDA events on the launching stream",
+            },
+            "e2e": {
+                "value": e2e_value,
+                "unit": UNIT,
+                "h2d_bytes_per_step": nodes * 4 * 8,
+                "d2h_bytes_per_step": nodes * 4 * 8,
+                "steps": args.e2e_steps,
+            },
+            "gpu_launches": int(launches),
+            "clocks": clocks,
+            "roofline": {
+                "bound": "fp64",
+                "kernel": "k_stage_a (low-order RHS, high-order RHS, limiter bounds)",
+                "achieved": achieved,
+                "peak": peak.value,
+                "unit": "TFLOP/s",
+                "frac": achieved / peak.value,
+                "traffic": KERNEL_A_TRAFFIC_BYTES,
+                "algorithmic_flops_per_launch": flops_a,
+                "quad_solves_per_launch": quad_per_launch,
+                "ms_per_launch": kms[0],
+                "ms_per_launch_stage_b": kms[1],
+                "stage_b_hbm_gbs": bytes_ab["stage_b"] / (kms[1] * 1e-3) / 1e9,
+                "peak_source": "p2de_probe_fma_peak: FP64 FMA chains on this GPU in this run (MEASURED_PEAKS.json has no FP64 figure)",
+            },
+            "min_rho_rhoe_last_step": [float(mins[4]), float(mins[5])],
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    solver.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

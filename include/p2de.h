@@ -187,6 +187,19 @@ int p2de_min_rho_rhoe(p2de_solver* s, double* min_rho, double* min_rhoe);
  * recorded by the stage update: out[2*(stage-1)] = min rho, out[2*(stage-1)+1] = min rhoe. */
 int p2de_stage_minima(p2de_solver* s, double out[6]);
 
+/* Runs `nsteps` SSP-RK3 steps from *t with the kernels launched one by one and
+ * CUDA events around each; returns the mean milliseconds per launch of stage kernel A
+ * (ms[0]), stage kernel B (ms[1]) and the step-begin kernel (ms[2]). */
+int p2de_profile_steps(p2de_solver* s, int64_t nsteps, double* t, double ms[3]);
+
+/* Work counters since the last reset: out[0] = quadratic internal-energy bound
+ * solves evaluated (limiter_utils.jl:108-132); the others are skipped exactly. */
+int p2de_read_counters(p2de_solver* s, uint64_t out[1], int32_t reset);
+
+/* FMA throughput of `device` in TFLOP/s (2 flops per FMA), FP64 (fp64 = 1) or FP32:
+ * the denominator of the FP64-pipe roofline. */
+int p2de_probe_fma_peak(int device, int32_t fp64, double* tflops);
+
 /* Last error message of this handle (or of the last failed create when s is NULL). */
 int p2de_last_error(p2de_solver* s, char* buf, size_t len);
 

@@ -157,6 +157,7 @@ struct p2de_solver {
   long long* minrec = nullptr;
   long long* minbuf = nullptr;
   int* status = nullptr;
+  unsigned long long* counters = nullptr;
   OpTable* ops = nullptr;
   StageArgs base{};
   int64_t launches = 0;
@@ -402,6 +403,7 @@ int p2de_initialize_DG(const p2de_param* prm, const p2de_mesh* mesh, int device,
   DA(s->minrec, 6);
   DA(s->minbuf, 2);
   DA(s->status, 1);
+  DA(s->counters, 8);
 #undef DA
   auto up = [&](void* dst, const void* src, size_t bytes) {
     return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s->stream);
@@ -459,6 +461,7 @@ int p2de_initialize_DG(const p2de_param* prm, const p2de_mesh* mesh, int device,
   a.dtmin_bits = s->dtmin;
   a.minrec = s->minrec;
   a.status = s->status;
+  a.counters = s->counters;
   *out = s;
   return P2DE_OK;
 }
@@ -568,16 +571,25 @@ int p2de_ssp33_step(p2de_solver* s, double* t, double* dt_out) {
   return step_impl(s, t, dt_out);
 }
 
+// Captures one step on a private stream (the caller's stream may be the legacy
+// default stream, which cannot be captured); the graph is replayed on s->stream.
 static int build_graph(p2de_solver* s) {
   if (s->graph) return P2DE_OK;
-  cudaGraph_t g;
-  CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+  cudaStream_t cap;
+  CK(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+  cudaStream_t user = s->stream;
+  cudaGraph_t g = nullptr;
+  s->stream = cap;
+  cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
   int64_t before = s->launches;
-  int rc = enqueue_step(s);
-  cudaError_t e = cudaStreamEndCapture(s->stream, &g);
+  int rc = (e == cudaSuccess) ? enqueue_step(s) : P2DE_OK;
+  cudaError_t e2 = (e == cudaSuccess) ? cudaStreamEndCapture(cap, &g) : e;
   s->launches = before;  // capture does not launch
+  s->stream = user;
+  cudaStreamDestroy(cap);
   if (rc != P2DE_OK) return rc;
   CK(e);
+  CK(e2);
   CK(cudaGraphInstantiate(&s->graph, g, 0));
   CK(cudaGraphDestroy(g));
   return P2DE_OK;
@@ -624,6 +636,62 @@ int p2de_ssp33(p2de_solver* s, double* t_out, int64_t* steps_out, double* dt_las
   if (steps_out) *steps_out = total;
   if (dt_last) *dt_last = sc[S_DT];
   return rc;
+}
+
+int p2de_profile_steps(p2de_solver* s, int64_t nsteps, double* t, double ms[3]) {
+  if (!s || !t || !ms || nsteps < 1) return P2DE_ERR_INVALID_ARGUMENT;
+  CK(cudaSetDevice(s->device));
+  cudaEvent_t ev[8];
+  for (int i = 0; i < 8; ++i) CK(cudaEventCreate(&ev[i]));
+  double acc[3] = {0, 0, 0};
+  CK(cudaMemcpyAsync(s->scal + S_T, t, sizeof(double), cudaMemcpyHostToDevice, s->stream));
+  int rc = P2DE_OK;
+  for (int64_t i = 0; i < nsteps && rc == P2DE_OK; ++i) {
+    CK(cudaEventRecord(ev[0], s->stream));
+    k_step_begin<<<1, 32, 0, s->stream>>>(s->scal, s->dtmin, s->minrec, s->status, s->prm.CFL, s->prm.dt0, s->prm.T);
+    CK(cudaGetLastError());
+    CK(cudaEventRecord(ev[1], s->stream));
+    for (int stage = 1; stage <= 3; ++stage) {
+      StageArgs a = s->base;
+      a.nstage = stage;
+      a.flags = flags_for(s, stage, true, false);
+      CK(launch_a_n1d(s->N1D, a, s->mixed, s->stream));
+      CK(cudaEventRecord(ev[2 * stage], s->stream));
+      CK(launch_b_n1d(s->N1D, a, s->stream));
+      CK(cudaEventRecord(ev[2 * stage + 1], s->stream));
+    }
+    s->launches += 7;
+    CK(cudaEventSynchronize(ev[7]));
+    float m;
+    CK(cudaEventElapsedTime(&m, ev[0], ev[1]));
+    acc[2] += m;
+    for (int stage = 1; stage <= 3; ++stage) {
+      CK(cudaEventElapsedTime(&m, ev[2 * stage - 1], ev[2 * stage]));
+      acc[0] += m;
+      CK(cudaEventElapsedTime(&m, ev[2 * stage], ev[2 * stage + 1]));
+      acc[1] += m;
+    }
+  }
+  for (int i = 0; i < 8; ++i) cudaEventDestroy(ev[i]);
+  ms[0] = acc[0] / (3.0 * nsteps);
+  ms[1] = acc[1] / (3.0 * nsteps);
+  ms[2] = acc[2] / nsteps;
+  double sc[S_NSCAL];
+  CK(cudaMemcpyAsync(sc, s->scal, sizeof sc, cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  *t = sc[S_T];
+  return check_status(s);
+}
+
+int p2de_read_counters(p2de_solver* s, uint64_t out[1], int32_t reset) {
+  if (!s || !out) return P2DE_ERR_INVALID_ARGUMENT;
+  CK(cudaSetDevice(s->device));
+  unsigned long long c[1];
+  CK(cudaMemcpyAsync(c, s->counters, sizeof c, cudaMemcpyDeviceToHost, s->stream));
+  if (reset) CK(cudaMemsetAsync(s->counters, 0, sizeof(unsigned long long) * 8, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  out[0] = c[0];
+  return P2DE_OK;
 }
 
 int p2de_device_ptr(p2de_solver* s, int32_t field, void** dptr) {

@@ -62,6 +62,7 @@ struct StageArgs {
   unsigned long long* dtmin_bits;
   long long* minrec;  // 3 stages x {min rho, min rhoe} as ordered keys
   int* status;
+  unsigned long long* counters;  // [0] quadratic rhoe solves evaluated by the bound phase
 };
 
 }  // namespace p2de

@@ -99,9 +99,10 @@ __device__ __forceinline__ double rhoe_quadratic_solve(const double* U, const do
 
 // limiting_param (limiter_utils.jl:66-70) -> limiting_param_bound_rho_rhoe (:82-96)
 // for the positivity bounds: Lrho = zeta*rhoL, Lrhoe = zeta*rhoe(uL), Urhoe = Inf, and
-// Urho = 0 (the Lphi slot, reference destructuring) or Inf.
+// Urho = 0 (the Lphi slot, reference destructuring) or Inf. `nquad` counts the
+// quadratic solves evaluated.
 __device__ __forceinline__ double limiting_param_pos(const double* U, const double* P, double Lrho, double Lrhoe,
-                                                     double Urho, double ZEROTOL) {
+                                                     double Urho, double ZEROTOL, unsigned& nquad) {
   double l = 1.0;
   double up = U[0] + P[0];
   if (up < Lrho) l = jmax((Lrho - U[0]) / P[0], 0.0);
@@ -109,6 +110,7 @@ __device__ __forceinline__ double limiting_param_pos(const double* U, const doub
   // l is +0 or positive here; the quadratic root is > ZEROTOL or 1, never NaN, so a
   // zero l stays zero and the root need not be evaluated.
   if (l == 0.0) return l;
+  ++nquad;
   l = jmin(l, rhoe_quadratic_solve(U, P, Lrhoe, ZEROTOL));
   // second solve with Urhoe = Inf returns 1.0
   return jmin(l, 1.0);
@@ -608,6 +610,7 @@ __global__ void __launch_bounds__(Cfg<N1D>::THREADS) k_stage_a(StageArgs a) {
 
   // ---- P9: bound evaluations, four per node (subcell_bound_limiter!(::Dim2), :288-341)
   const double Urho = (flags & F_REF_SEM) ? 0.0 : __longlong_as_double(0x7ff0000000000000LL);
+  unsigned nquad = 0;
   for (int w = tid; w < Ke * 4 * Nq; w += bs) {
     int e = w / (4 * Nq), r = w % (4 * Nq);
     int dh = r / Nq, m = r % Nq;
@@ -629,7 +632,11 @@ __global__ void __launch_bounds__(Cfg<N1D>::THREADS) k_stage_a(StageArgs a) {
     for (int c = 0; c < 4; ++c) P[c] = s4 * (fH[c] - fL[c]) / wJ;
     const double* uL = base + C::O_PRIM + 6 * m;
     double Lrho = a.zeta * uL[0];
-    base[C::O_EV + r] = limiting_param_pos(uL, P, Lrho, uL[4], Urho, a.ZEROTOL);
+    base[C::O_EV + r] = limiting_param_pos(uL, P, Lrho, uL[4], Urho, a.ZEROTOL, nquad);
+  }
+  if (a.counters) {
+    for (int o = 16; o > 0; o >>= 1) nquad += __shfl_xor_sync(0xffffffffu, nquad, o);
+    if ((tid & 31) == 0 && nquad) atomicAdd(&a.counters[0], (unsigned long long)nquad);
   }
   __syncthreads();
 

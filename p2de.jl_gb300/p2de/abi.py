@@ -123,6 +123,9 @@ EXPORTS = [
     ("p2de_launch_count", c_int, [SOLVER_P, POINTER(c_int64)]),
     ("p2de_min_rho_rhoe", c_int, [SOLVER_P, POINTER(c_double), POINTER(c_double)]),
     ("p2de_stage_minima", c_int, [SOLVER_P, POINTER(c_double)]),
+    ("p2de_profile_steps", c_int, [SOLVER_P, c_int64, POINTER(c_double), POINTER(c_double)]),
+    ("p2de_read_counters", c_int, [SOLVER_P, POINTER(ctypes.c_uint64), c_int32]),
+    ("p2de_probe_fma_peak", c_int, [c_int, c_int32, POINTER(c_double)]),
     ("p2de_last_error", c_int, [SOLVER_P, c_char_p, c_size_t]),
 ]
 
