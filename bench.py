@@ -43,9 +43,11 @@ sys.path.insert(0, str(ROOT))
 METRIC = "DOF-stage updates/s, 2D Euler N=3; served solves/s + p99 vs plain, same L1 err"
 UNIT = "DOF-stage updates/s"
 
-# stage kernel A DRAM traffic per launch on this workload (dram__bytes_read.sum +
-# dram__bytes_write.sum of one ncu capture, profiles/k_stage_a_dmr480x120_n3_fp64.md)
-KERNEL_A_TRAFFIC_BYTES = 144.0e6
+# stage kernel A on this workload from one ncu capture
+# (profiles/k_stage_a_dmr480x120_n3_fp64.md): DRAM traffic per launch
+# (dram__bytes_read.sum + dram__bytes_write.sum) and the FP64 pipe's busy fraction
+KERNEL_A_TRAFFIC_BYTES = 143.9e6
+KERNEL_A_FP64_PIPE_BUSY = 0.796
 
 
 def workload(name: str, precision: str):
@@ -362,6 +364,7 @@ def main():
                 "unit": "TFLOP/s",
                 "frac": achieved / peak.value,
                 "traffic": KERNEL_A_TRAFFIC_BYTES,
+                "fp64_pipe_busy_ncu": KERNEL_A_FP64_PIPE_BUSY,
                 "algorithmic_flops_per_launch": flops_a,
                 "quad_solves_per_launch": quad_per_launch,
                 "ms_per_launch": kms[0],

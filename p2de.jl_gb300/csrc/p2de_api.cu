@@ -289,9 +289,6 @@ int p2de_initialize_DG(const p2de_param* prm, const p2de_mesh* mesh, int device,
   if (prm->rhs_type < 0 || prm->rhs_type > 2 || prm->bound_type < 0 || prm->bound_type > 1 || prm->precision < 0 ||
       prm->precision > 1)
     return fail(nullptr, P2DE_ERR_INVALID_ARGUMENT, "rhs_type/bound_type/precision out of range");
-  int ndev = 0;
-  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(nullptr, P2DE_ERR_NO_DEVICE, "no CUDA device");
-  if (device < 0 || device >= ndev) return fail(nullptr, P2DE_ERR_INVALID_ARGUMENT, "device %d of %d", device, ndev);
   const int64_t n1 = prm->N + 1, Nfp = 4 * n1, Nq = n1 * n1;
   const int64_t nfk = Nfp * prm->K;
   // validate indices before anything reaches the device
@@ -313,6 +310,12 @@ int p2de_initialize_DG(const p2de_param* prm, const p2de_mesh* mesh, int device,
   if ((rc = check_list(mesh->mapS, mesh->nS, "mapS")) != P2DE_OK) return rc;
   if (mesh->nI > 0 && !mesh->Ival) return fail(nullptr, P2DE_ERR_INVALID_ARGUMENT, "Ival missing");
   if (mesh->nS > 0 && !mesh->xyS) return fail(nullptr, P2DE_ERR_INVALID_ARGUMENT, "xyS missing");
+  for (int64_t k = 0; k < prm->K; ++k)
+    if (!(mesh->geom[5 * k] > 0.0))
+      return fail(nullptr, P2DE_ERR_INVALID_ARGUMENT, "J[%lld] = %g is not positive", (long long)k, mesh->geom[5 * k]);
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(nullptr, P2DE_ERR_NO_DEVICE, "no CUDA device");
+  if (device < 0 || device >= ndev) return fail(nullptr, P2DE_ERR_INVALID_ARGUMENT, "device %d of %d", device, ndev);
 
   s = new p2de_solver();
   s->device = device;

@@ -1,8 +1,8 @@
 // Stage kernels for tensor-product GLL elements of N1D = N+1 nodes per line.
 //
 // Stage kernel A (one block = E consecutive elements; every phase is a flat loop
-// over (element, item) so that the FP64 pipe, the bottleneck on this part, always
-// issues full warps):
+// over (element, item) so that the FP64 pipe, the bottleneck here, always issues
+// full warps):
 //   low-order graph-viscosity RHS      low_order_graph_viscosity.jl:4-41
 //   high-order ES flux differencing    flux_differencing.jl:4-37
 //   subcell bounds and cell entropy    subcell.jl:163-349, 462-744; limiter_utils.jl:66-132
@@ -10,6 +10,20 @@
 // subcell fluxes and rhsU (subcell.jl:841-924), SSP-RK3 stage combination
 // (SSPRK33.jl:127-135) and the per-stage positivity record.
 //
+// GB300 executes FP64 at 2 FMA/clk/SM, 1/58 of its FP32 rate, so these kernels are
+// bound by their FP64 instruction count. The arithmetic follows the reference's
+// formulas and association order, with these departures, each within a few units in
+// the last place of the reference's value:
+//  * a quotient by the same denominator is a multiplication by one reciprocal
+//    (1/rho per node, 1/(wq J) per node, 1/J per element, 1/(2a) per quadratic);
+//  * the log mean (compressible_Navier_Stokes.jl:307-321) takes one division: the
+//    branch test |da/aavg| < 1e-4 is made as |da| < 1e-4 |aavg|, then da is divided by
+//    aavg (series branch) or by log(aL) - log(aR);
+//  * pa and rholog/(2(gamma-1) betalog) of fS share one reciprocal;
+//  * min/max are fmin/fmax, which differ from Julia's min/max only for NaN operands
+//    (a NaN state is reported through the status word instead);
+//  * on axis-aligned elements (sxJ = ryJ = 0) the terms the reference multiplies by an
+//    exact zero are not formed.
 // For LGL collocation two parts of the reference's computation are identities up to
 // rounding and are not evaluated:
 //  * the entropy projection of face values, u_vfun(v_ufun(U)) (rhs.jl:242-252; the
@@ -38,16 +52,17 @@ struct Cfg {
   static constexpr int NPL = 2 * n * (n - 1);
   static constexpr int NPH = n * n * (n - 1);
   static constexpr int NSF = n * (n + 1);  // subcell faces per direction = Nq + N1D
+  static constexpr int NEV = 4 * Nq;       // bound evaluations per element
   static constexpr int E = (128 / Nq) > 0 ? (128 / Nq) : 1;
   static constexpr int THREADS = 128;
   static constexpr int SCR = cmax(cmax(NPL * 9, NPH * 8), 16 * NSF);
   // shared-memory doubles per element, kernel A
-  static constexpr int O_GEO = 0;                  // 16
+  static constexpr int O_GEO = 0;                  // 16: J, rxJ, sxJ, ryJ, syJ, |gr|, nr, |gs|, ns, 1/J
   static constexpr int O_U = O_GEO + 16;           // 4 Nq
-  static constexpr int O_PRIM = O_U + 4 * Nq;      // 6 Nq (later uL[4], Lrhoe)
+  static constexpr int O_PRIM = O_U + 4 * Nq;      // 6 Nq (later uL[4], Lrhoe, 1/(wq J))
   static constexpr int O_FLUX = O_PRIM + 6 * Nq;   // 8 Nq (later vq)
   static constexpr int O_WS = O_FLUX + 8 * Nq;     // 2 Nq
-  static constexpr int O_RXYL = O_WS + 2 * Nq;     // 8 Nq
+  static constexpr int O_RXYL = O_WS + 2 * Nq;     // 8 Nq (later the P vectors, with O_RXYH)
   static constexpr int O_RXYH = O_RXYL + 8 * Nq;   // 8 Nq
   static constexpr int O_RHSL = O_RXYH + 8 * Nq;   // 4 Nq
   static constexpr int O_LAMI = O_RHSL + 4 * Nq;   // Nq
@@ -55,11 +70,12 @@ struct Cfg {
   static constexpr int O_BFH = O_BFL + 8 * Nfp;    // 8 Nfp
   static constexpr int O_LAMB = O_BFH + 8 * Nfp;   // Nfp
   static constexpr int O_SCR = O_LAMB + Nfp;       // SCR
-  static constexpr int O_EV = O_SCR + SCR;         // 4 Nq
-  static constexpr int O_L = O_EV + 4 * Nq;        // 2 NSF
+  static constexpr int O_EV = O_SCR + SCR;         // NEV
+  static constexpr int O_L = O_EV + NEV;           // 2 NSF
   static constexpr int O_MISC = O_L + 2 * NSF;     // 4
   static constexpr int PER_ELEM_A = O_MISC + 4;
-  static constexpr size_t SMEM_A = sizeof(double) * PER_ELEM_A * E;
+  // plus a block-wide list of bound evaluations that need the quadratic solve
+  static constexpr size_t SMEM_A = sizeof(double) * PER_ELEM_A * E + sizeof(int) * (NEV * E + 4);
   // kernel B
   static constexpr int PER_ELEM_B = 2 * NSF + 16 * NSF + 8 * NSF + 8;
   static constexpr size_t SMEM_B = sizeof(double) * PER_ELEM_B * E;
@@ -72,10 +88,72 @@ __device__ __forceinline__ long long order_key(double x) {
   return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
 }
 
-// limiter_utils.jl:108-132
+// wavespeed_estimate (compressible_Navier_Stokes.jl:48-62) with 1/rho given
+__device__ __forceinline__ double wavespeed_r(const Gas<double>& g, double rr, double un, double E) {
+  double p = g.gm1 * (E - 0.5 * (un * un) * rr);
+  return fabs(un * rr) + sqrt(g.gamma * p * rr);
+}
+
+// fluxes(Dim2) (:175-194) with 1/rho given
+__device__ __forceinline__ void fluxes_r(const Gas<double>& g, const double* U, double rr, double* fx, double* fy) {
+  double rho = U[0], rhou = U[1], rhov = U[2], E = U[3];
+  double p = g.gm1 * (E - 0.5 * (rhou * rhou + rhov * rhov) * rr);
+  double u = rhou * rr, v = rhov * rr;
+  double rhouv = rho * u * v;
+  double Ep = E + p;
+  fx[0] = rhou;
+  fx[1] = rhou * u + p;
+  fx[2] = rhouv;
+  fx[3] = u * Ep;
+  fy[0] = rhov;
+  fy[1] = rhouv;
+  fy[2] = rhov * v + p;
+  fy[3] = v * Ep;
+}
+
+// logmean (compressible_Navier_Stokes.jl:307-321) with one division
+__device__ __forceinline__ double logmean_1div(double aL, double aR, double logL, double logR) {
+  double da = aR - aL;
+  double aavg = 0.5 * (aR + aL);
+  bool series = fabs(da) < 1e-4 * fabs(aavg);
+  double x = da / (series ? aavg : (logL - logR));
+  if (series) {
+    double v = x * x;
+    return aavg * (1.0 + v * (-0.2 - v * (0.0512 - v * 0.026038857142857)));
+  }
+  return -x;
+}
+
+// fS(Dim2) (:220-249); UL/UR = (rho, u, v, beta, log rho, log beta)
+__device__ __forceinline__ void fS_fast(const Gas<double>& g, const double* UL, const double* UR, double* Fx,
+                                        double* Fy) {
+  double rholog = logmean_1div(UL[0], UR[0], UL[4], UR[4]);
+  double betalog = logmean_1div(UL[3], UR[3], UL[5], UR[5]);
+  double rhoavg = 0.5 * (UL[0] + UR[0]);
+  double uavg = 0.5 * (UL[1] + UR[1]);
+  double vavg = 0.5 * (UL[2] + UR[2]);
+  double unorm = UL[1] * UR[1] + UL[2] * UR[2];
+  double d1 = UL[3] + UR[3];
+  double d2 = g.two_gm1 * betalog;
+  double r12 = 1.0 / (d1 * d2);
+  double pa = rhoavg * d2 * r12;
+  double f4aux = rholog * d1 * r12 + pa + 0.5 * rholog * unorm;
+  double FxS1 = rholog * uavg;
+  double FxS3 = FxS1 * vavg;
+  double FyS1 = rholog * vavg;
+  Fx[0] = FxS1;
+  Fx[1] = FxS1 * uavg + pa;
+  Fx[2] = FxS3;
+  Fx[3] = f4aux * uavg;
+  Fy[0] = FyS1;
+  Fy[1] = FxS3;
+  Fy[2] = FyS1 * vavg + pa;
+  Fy[3] = f4aux * vavg;
+}
+
+// limiter_utils.jl:108-132 for a finite Lrhoe
 __device__ __forceinline__ double rhoe_quadratic_solve(const double* U, const double* P, double Lrhoe,
                                                        double ZEROTOL) {
-  if (Lrhoe == __longlong_as_double(0x7ff0000000000000LL)) return 1.0;
   // limiter_utils.jl:141-146
   double a = P[0] * P[3] - 1.0 / 2.0 * (P[1] * P[1] + P[2] * P[2]);
   double b = U[3] * P[0] + U[0] * P[3] - U[1] * P[1] - U[2] * P[2] - P[0] * Lrhoe;
@@ -84,10 +162,11 @@ __device__ __forceinline__ double rhoe_quadratic_solve(const double* U, const do
   double disc = b * b - 4.0 * a * c;
   if (disc >= 0.0) {
     double sq = sqrt(disc);
-    double r1 = (-b + sq) / (2.0 * a);
-    double r2 = (-b - sq) / (2.0 * a);
+    double r2a = 1.0 / (2.0 * a);
+    double r1 = (-b + sq) * r2a;
+    double r2 = (-b - sq) * r2a;
     if (r1 > ZEROTOL && r2 > ZEROTOL) {
-      l = jmin(r1, r2);
+      l = fmin(r1, r2);
     } else if (r1 > ZEROTOL && r2 < -ZEROTOL) {
       l = r1;
     } else if (r2 > ZEROTOL && r1 < -ZEROTOL) {
@@ -97,23 +176,19 @@ __device__ __forceinline__ double rhoe_quadratic_solve(const double* U, const do
   return l;
 }
 
-// limiting_param (limiter_utils.jl:66-70) -> limiting_param_bound_rho_rhoe (:82-96)
-// for the positivity bounds: Lrho = zeta*rhoL, Lrhoe = zeta*rhoe(uL), Urhoe = Inf, and
-// Urho = 0 (the Lphi slot, reference destructuring) or Inf. `nquad` counts the
-// quadratic solves evaluated.
-__device__ __forceinline__ double limiting_param_pos(const double* U, const double* P, double Lrho, double Lrhoe,
-                                                     double Urho, double ZEROTOL, unsigned& nquad) {
+// Density part of limiting_param_bound_rho_rhoe (limiter_utils.jl:82-92) for the
+// positivity bounds Lrho = zeta*rhoL and Urho = 0 (the Lphi slot under the reference's
+// destructuring, limiter_utils.jl:66-70) or Inf.
+__device__ __forceinline__ double density_bound(double U0, double P0, double Lrho, double Urho) {
   double l = 1.0;
-  double up = U[0] + P[0];
-  if (up < Lrho) l = jmax((Lrho - U[0]) / P[0], 0.0);
-  if (up > Urho) l = jmin(l, jmax((Urho - U[0]) / P[0], 0.0));
-  // l is +0 or positive here; the quadratic root is > ZEROTOL or 1, never NaN, so a
-  // zero l stays zero and the root need not be evaluated.
-  if (l == 0.0) return l;
-  ++nquad;
-  l = jmin(l, rhoe_quadratic_solve(U, P, Lrhoe, ZEROTOL));
-  // second solve with Urhoe = Inf returns 1.0
-  return jmin(l, 1.0);
+  double up = U0 + P0;
+  bool lo = up < Lrho, hi = up > Urho;
+  if (lo || hi) {
+    double rP = 1.0 / P0;
+    if (lo) l = fmax((Lrho - U0) * rP, 0.0);
+    if (hi) l = fmin(l, fmax((Urho - U0) * rP, 0.0));
+  }
+  return l;
 }
 
 // =====================================================================================
@@ -122,10 +197,11 @@ __device__ __forceinline__ double limiting_param_pos(const double* U, const doub
 template <int N1D, typename TH>
 __global__ void __launch_bounds__(Cfg<N1D>::THREADS) k_stage_a(StageArgs a) {
   using C = Cfg<N1D>;
-  constexpr int n = C::n, Nq = C::Nq, Nfp = C::Nfp, NSF = C::NSF;
+  constexpr int n = C::n, Nq = C::Nq, Nfp = C::Nfp, NSF = C::NSF, NEV = C::NEV;
   constexpr int PE = C::PER_ELEM_A;
   if (a.scal[S_DONE] != 0.0) return;
   extern __shared__ double sm[];
+  int* s_list = reinterpret_cast<int*>(sm + PE * C::E);  // [0]: count, then eval indices
   const OpTable& op = *a.ops;
   const int tid = threadIdx.x, bs = blockDim.x;
   const int k0 = blockIdx.x * C::E;
@@ -154,7 +230,9 @@ __global__ void __launch_bounds__(Cfg<N1D>::THREADS) k_stage_a(StageArgs a) {
     G[8] = gs;
     G[9] = sxJ / gs;
     G[10] = syJ / gs;
+    G[11] = 1.0 / J;
   }
+  if (tid == 0) s_list[0] = 0;
   for (int w = tid; w < Ke * Nq * 4; w += bs) {
     int e = w / (Nq * 4), r = w % (Nq * 4);
     sm[e * PE + C::O_U + r] = a.Uq[(size_t)k0 * Nq * 4 + w];
@@ -169,20 +247,22 @@ __global__ void __launch_bounds__(Cfg<N1D>::THREADS) k_stage_a(StageArgs a) {
     const double* G = base + C::O_GEO;
     const double* U = base + C::O_U + 4 * m;
     double rho = U[0], rhou = U[1], rhov = U[2], E = U[3];
-    double p = pfun(g, rho, rhou, rhov, E);
-    double u = rhou / rho, v = rhov / rho;
+    double rr = 1.0 / rho;
+    double p = g.gm1 * (E - 0.5 * (rhou * rhou + rhov * rhov) * rr);
+    double u = rhou * rr, v = rhov * rr;
     double* F = base + C::O_FLUX + 8 * m;
+    double Ep = E + p;
     F[0] = rhou;
     F[1] = rhou * u + p;
     F[2] = rho * u * v;
-    F[3] = u * (E + p);
+    F[3] = u * Ep;
     F[4] = rhov;
     F[5] = F[2];
     F[6] = rhov * v + p;
-    F[7] = v * (E + p);
+    F[7] = v * Ep;
     double* Ws = base + C::O_WS + 2 * m;
-    Ws[0] = wavespeed_un(g, rho, G[6] * rhou + G[7] * rhov, E);
-    Ws[1] = wavespeed_un(g, rho, G[9] * rhou + G[10] * rhov, E);
+    Ws[0] = wavespeed_r(g, rr, G[6] * rhou + G[7] * rhov, E);
+    Ws[1] = wavespeed_r(g, rr, G[9] * rhou + G[10] * rhov, E);
     if (do_high) {
       double* Pm = base + C::O_PRIM + 6 * m;
       double beta = rho / (2.0 * p);
@@ -210,7 +290,7 @@ __global__ void __launch_bounds__(Cfg<N1D>::THREADS) k_stage_a(StageArgs a) {
       double S0x = g1 * S, S0y = g2 * S;
       double nn = fabs(S) * gn;
       double wsi = base[C::O_WS + 2 * i + ax], wsj = base[C::O_WS + 2 * j + ax];
-      double lam = nn * jmax(wsi, wsj);
+      double lam = nn * fmax(wsi, wsj);
       const double* Ui = base + C::O_U + 4 * i;
       const double* Uj = base + C::O_U + 4 * j;
       const double* Fi = base + C::O_FLUX + 8 * i;
@@ -225,9 +305,6 @@ __global__ void __launch_bounds__(Cfg<N1D>::THREADS) k_stage_a(StageArgs a) {
           double vis = visc_x ? lam * (Uj[c] - Ui[c]) : 0.0;
           out[c] = tx * Fx - vis;
         }
-      } else {
-#pragma unroll
-        for (int c = 0; c < 4; ++c) out[c] = 0.0;
       }
       if (!aa || ax == 1) {
 #pragma unroll
@@ -236,9 +313,6 @@ __global__ void __launch_bounds__(Cfg<N1D>::THREADS) k_stage_a(StageArgs a) {
           double vis = visc_x ? 0.0 : lam * (Uj[c] - Ui[c]);
           out[4 + c] = ty * Fy - vis;
         }
-      } else {
-#pragma unroll
-        for (int c = 0; c < 4; ++c) out[4 + c] = 0.0;
       }
       out[8] = lam;
     }
@@ -253,12 +327,15 @@ __global__ void __launch_bounds__(Cfg<N1D>::THREADS) k_stage_a(StageArgs a) {
       for (int t = 0; t < cnt; ++t) {
         int pp = op.lg_pair[m][t];
         const double* sf = base + C::O_SCR + 9 * pp;
-        if (op.lg_sign[m][t] > 0) {
+        int ax = op.lp_axis[pp];
+        double sg = op.lg_sign[m][t] > 0 ? 1.0 : -1.0;
+        if (!aa || ax == 0) {
 #pragma unroll
-          for (int c = 0; c < 8; ++c) Q[c] = Q[c] + sf[c];
-        } else {
+          for (int c = 0; c < 4; ++c) Q[c] = Q[c] + sg * sf[c];
+        }
+        if (!aa || ax == 1) {
 #pragma unroll
-          for (int c = 0; c < 8; ++c) Q[c] = Q[c] + (-sf[c]);
+          for (int c = 4; c < 8; ++c) Q[c] = Q[c] + sg * sf[c];
         }
         lam += sf[8];
       }
@@ -291,10 +368,9 @@ __global__ void __launch_bounds__(Cfg<N1D>::THREADS) k_stage_a(StageArgs a) {
     double ws_own = base[C::O_WS + 2 * q + (xs ? 0 : 1)];
     size_t fk = (size_t)k * Nfp + f;
     int lin = a.nbr[fk];
-    double wsP;
+    bool self = lin == (int)fk;
     double Unb[4];
-    if (lin == (int)fk) {
-      wsP = ws_own;
+    if (self) {
 #pragma unroll
       for (int c = 0; c < 4; ++c) Unb[c] = Uf[c];
     } else {
@@ -310,7 +386,6 @@ __global__ void __launch_bounds__(Cfg<N1D>::THREADS) k_stage_a(StageArgs a) {
 #pragma unroll
         for (int c = 0; c < 4; ++c) Unb[c] = __ldg(src + c);
       }
-      wsP = wavespeed(g, Unb, n1, n2);
     }
     int code = a.bc[fk];
     double uP[4];
@@ -336,25 +411,27 @@ __global__ void __launch_bounds__(Cfg<N1D>::THREADS) k_stage_a(StageArgs a) {
 #pragma unroll
       for (int c = 0; c < 4; ++c) uP[c] = post ? a.shock_post[c] : a.shock_pre[c];
     }
-    double lamB = 0.5 * nn * jmax(ws_own, wsP);
-    double fPx[4], fPy[4];
-    fluxes(g, uP, fPx, fPy);
-    const double* Ff = base + C::O_FLUX + 8 * q;
-    double fsx[4], fsy[4], lf[4];
-#pragma unroll
-    for (int c = 0; c < 4; ++c) {
-      fsx[c] = 0.5 * (Ff[c] + fPx[c]);
-      fsy[c] = 0.5 * (Ff[4 + c] + fPy[c]);
-      lf[c] = lamB * (uP[c] - Uf[c]);
+    double rrP = 1.0 / uP[0];
+    double wsP = ws_own;
+    if (!self) {
+      double rrN = (code == BC_INTERIOR) ? rrP : 1.0 / Unb[0];
+      wsP = wavespeed_r(g, rrN, n1 * Unb[1] + n2 * Unb[2], Unb[3]);
     }
+    double lamB = 0.5 * nn * fmax(ws_own, wsP);
+    double fPx[4], fPy[4];
+    fluxes_r(g, uP, rrP, fPx, fPy);
+    const double* Ff = base + C::O_FLUX + 8 * q;
     double* BL = base + C::O_BFL + 8 * f;
     double* BH = base + C::O_BFH + 8 * f;
     bool lf_zero_high = (code == BC_INFLOW || code == BC_OUTFLOW || code == BC_SHOCK);
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
-      double bx = B1 * fsx[c], by = B2 * fsy[c];
-      BL[c] = xs ? bx - lf[c] : bx;
-      BL[4 + c] = xs ? by : by - lf[c];
+      double lf = lamB * (uP[c] - Uf[c]);
+      double fsx = 0.5 * (Ff[c] + fPx[c]);
+      double fsy = 0.5 * (Ff[4 + c] + fPy[c]);
+      double bx = B1 * fsx, by = B2 * fsy;
+      BL[c] = xs ? bx - lf : bx;
+      BL[4 + c] = xs ? by : by - lf;
       if (lf_zero_high) {
         double lh = 0.0 * (uP[c] - Uf[c]);
         BH[c] = xs ? bx - lh : bx;
@@ -406,13 +483,21 @@ __global__ void __launch_bounds__(Cfg<N1D>::THREADS) k_stage_a(StageArgs a) {
       double lam = base[C::O_LAMI + m];
       for (int t = 0; t < nf; ++t) {
         const double* BL = base + C::O_BFL + 8 * fl[t];
+        bool xf = fl[t] < 2 * n;
+        if (!aa || xf) {
 #pragma unroll
-        for (int c = 0; c < 8; ++c) R[c] = R[c] - BL[c];
+          for (int c = 0; c < 4; ++c) R[c] = R[c] - BL[c];
+        }
+        if (!aa || !xf) {
+#pragma unroll
+          for (int c = 4; c < 8; ++c) R[c] = R[c] - BL[c];
+        }
         lam += base[C::O_LAMB + fl[t]];
       }
       double wJ = base[C::O_GEO] * op.wq[m];
+      double rwJ = 1.0 / wJ;
 #pragma unroll
-      for (int c = 0; c < 8; ++c) R[c] = R[c] / wJ;
+      for (int c = 0; c < 8; ++c) R[c] = R[c] * rwJ;
       double* rl = base + C::O_RHSL + 4 * m;
 #pragma unroll
       for (int c = 0; c < 4; ++c) rl[c] = R[c] + R[4 + c];
@@ -446,11 +531,14 @@ __global__ void __launch_bounds__(Cfg<N1D>::THREADS) k_stage_a(StageArgs a) {
       double* out = base + C::O_SCR + 8 * pp;
       if (sizeof(TH) == 8) {
         double Fx[4], Fy[4];
-        fS_f64(g, base + C::O_PRIM + 6 * i, base + C::O_PRIM + 6 * j, Fx, Fy);
+        fS_fast(g, base + C::O_PRIM + 6 * i, base + C::O_PRIM + 6 * j, Fx, Fy);
+        if (!aa || ax == 0) {
 #pragma unroll
-        for (int c = 0; c < 4; ++c) {
-          out[c] = (!aa || ax == 0) ? Sxx * Fx[c] : 0.0;
-          out[4 + c] = (!aa || ax == 1) ? Sxy * Fy[c] : 0.0;
+          for (int c = 0; c < 4; ++c) out[c] = Sxx * Fx[c];
+        }
+        if (!aa || ax == 1) {
+#pragma unroll
+          for (int c = 0; c < 4; ++c) out[4 + c] = Sxy * Fy[c];
         }
       } else {
         Gas<float> gf{(float)a.gamma, (float)a.gm1, (float)(2.0 * a.gm1)};
@@ -461,10 +549,13 @@ __global__ void __launch_bounds__(Cfg<N1D>::THREADS) k_stage_a(StageArgs a) {
         float Fx[4], Fy[4];
         fS_f32(gf, UL, UR, Fx, Fy);
         float sx = (float)Sxx, sy = (float)Sxy;
+        if (!aa || ax == 0) {
 #pragma unroll
-        for (int c = 0; c < 4; ++c) {
-          out[c] = (!aa || ax == 0) ? (double)(sx * Fx[c]) : 0.0;
-          out[4 + c] = (!aa || ax == 1) ? (double)(sy * Fy[c]) : 0.0;
+          for (int c = 0; c < 4; ++c) out[c] = (double)(sx * Fx[c]);
+        }
+        if (!aa || ax == 1) {
+#pragma unroll
+          for (int c = 0; c < 4; ++c) out[4 + c] = (double)(sy * Fy[c]);
         }
       }
     }
@@ -479,37 +570,56 @@ __global__ void __launch_bounds__(Cfg<N1D>::THREADS) k_stage_a(StageArgs a) {
       if (ir == n - 1) fl[nf++] = n + is;
       if (is == 0) fl[nf++] = 2 * n + ir;
       if (is == n - 1) fl[nf++] = 3 * n + ir;
-      double J = base[C::O_GEO];
+      double rJ = base[C::O_GEO + 11];
       double rw = op.rwq[m];
       double* R = base + C::O_RXYH + 8 * m;
       int cnt = op.hg_count[m];
       if (sizeof(TH) == 8) {
         double Q[8] = {0, 0, 0, 0, 0, 0, 0, 0};
         for (int t = 0; t < cnt; ++t) {
-          const double* sf = base + C::O_SCR + 8 * op.hg_pair[m][t];
-          if (op.hg_sign[m][t] > 0) {
+          int pp = op.hg_pair[m][t];
+          const double* sf = base + C::O_SCR + 8 * pp;
+          int ax = op.hp_axis[pp];
+          double sg = op.hg_sign[m][t] > 0 ? 1.0 : -1.0;
+          if (!aa || ax == 0) {
 #pragma unroll
-            for (int c = 0; c < 8; ++c) Q[c] = Q[c] + sf[c];
-          } else {
+            for (int c = 0; c < 4; ++c) Q[c] = Q[c] + sg * sf[c];
+          }
+          if (!aa || ax == 1) {
 #pragma unroll
-            for (int c = 0; c < 8; ++c) Q[c] = Q[c] + (-sf[c]);
+            for (int c = 4; c < 8; ++c) Q[c] = Q[c] + sg * sf[c];
           }
         }
         double Bs[8] = {0, 0, 0, 0, 0, 0, 0, 0};
         for (int t = 0; t < nf; ++t) {
           const double* BH = base + C::O_BFH + 8 * fl[t];
+          bool xf = fl[t] < 2 * n;
+          if (!aa || xf) {
 #pragma unroll
-          for (int c = 0; c < 8; ++c) Bs[c] = Bs[c] + rw * BH[c];
+            for (int c = 0; c < 4; ++c) Bs[c] = Bs[c] + rw * BH[c];
+          }
+          if (!aa || !xf) {
+#pragma unroll
+            for (int c = 4; c < 8; ++c) Bs[c] = Bs[c] + rw * BH[c];
+          }
         }
 #pragma unroll
-        for (int c = 0; c < 8; ++c) R[c] = (-(rw * Q[c] + Bs[c])) / J;
+        for (int c = 0; c < 8; ++c) R[c] = (-(rw * Q[c] + Bs[c])) * rJ;
       } else {
         float Q[8] = {0, 0, 0, 0, 0, 0, 0, 0};
         for (int t = 0; t < cnt; ++t) {
-          const double* sf = base + C::O_SCR + 8 * op.hg_pair[m][t];
+          int pp = op.hg_pair[m][t];
+          const double* sf = base + C::O_SCR + 8 * pp;
+          int ax = op.hp_axis[pp];
           float sg = op.hg_sign[m][t] > 0 ? 1.0f : -1.0f;
+          if (!aa || ax == 0) {
 #pragma unroll
-          for (int c = 0; c < 8; ++c) Q[c] = Q[c] + sg * (float)sf[c];
+            for (int c = 0; c < 4; ++c) Q[c] = Q[c] + sg * (float)sf[c];
+          }
+          if (!aa || ax == 1) {
+#pragma unroll
+            for (int c = 4; c < 8; ++c) Q[c] = Q[c] + sg * (float)sf[c];
+          }
         }
         float rwf = (float)rw;
         float Bs[8] = {0, 0, 0, 0, 0, 0, 0, 0};
@@ -518,9 +628,9 @@ __global__ void __launch_bounds__(Cfg<N1D>::THREADS) k_stage_a(StageArgs a) {
 #pragma unroll
           for (int c = 0; c < 8; ++c) Bs[c] = Bs[c] + rwf * (float)BH[c];
         }
-        float Jf = (float)J;
+        float rJf = (float)rJ;
 #pragma unroll
-        for (int c = 0; c < 8; ++c) R[c] = (double)((-(rwf * Q[c] + Bs[c])) / Jf);
+        for (int c = 0; c < 8; ++c) R[c] = (double)((-(rwf * Q[c] + Bs[c])) * rJf);
       }
     }
   }
@@ -605,39 +715,78 @@ __global__ void __launch_bounds__(Cfg<N1D>::THREADS) k_stage_a(StageArgs a) {
 #pragma unroll
     for (int c = 0; c < 4; ++c) uL[c] = U[c] + dt_lim * rl[c];
     uL[4] = a.zeta * rhoe_ufun(uL[0], uL[1], uL[2], uL[3]);
+    uL[5] = 1.0 / (op.wq[m] * base[C::O_GEO]);
   }
   __syncthreads();
 
-  // ---- P9: bound evaluations, four per node (subcell_bound_limiter!(::Dim2), :288-341)
+  // ---- P9: bound evaluations, four per node (subcell_bound_limiter!(::Dim2), :288-341).
+  // Evaluation r = (2d + h) Nq + m limits face h (0: lower, 1: upper) of node m in
+  // direction d with P = -/+ 4 dt (fH - fL) / (wq J). A face's factor is the min of its
+  // one or two evaluations. First the density bound of every evaluation (it needs only
+  // P[0]); the quadratic internal-energy solve (>= ZEROTOL or 1, never NaN) can only
+  // change the face's factor when every density bound of that face is nonzero, so only
+  // those evaluations go to a list, solved with all lanes busy.
   const double Urho = (flags & F_REF_SEM) ? 0.0 : __longlong_as_double(0x7ff0000000000000LL);
-  unsigned nquad = 0;
-  for (int w = tid; w < Ke * 4 * Nq; w += bs) {
-    int e = w / (4 * Nq), r = w % (4 * Nq);
+  for (int w = tid; w < Ke * NEV; w += bs) {
+    int e = w / NEV, r = w % NEV;
     int dh = r / Nq, m = r % Nq;
     int ir = m % n, is = m / n;
     double* base = sm + e * PE;
     const double* fb = base + C::O_SCR;
     int d = dh >> 1, h = dh & 1;
-    int fi;
-    if (d == 0)
-      fi = (ir + h) + (n + 1) * is;
-    else
-      fi = ir + n * (is + h);
+    int fi = (d == 0) ? (ir + h) + (n + 1) * is : ir + n * (is + h);
     const double* fH = fb + ((d * 2 + 0) * NSF + fi) * 4;
     const double* fL = fb + ((d * 2 + 1) * NSF + fi) * 4;
-    double wJ = op.wq[m] * base[C::O_GEO];
+    const double* uL = base + C::O_PRIM + 6 * m;
+    double s4 = (h == 0 ? -4.0 : 4.0) * dt_lim;
+    double P0 = s4 * (fH[0] - fL[0]) * uL[5];
+    base[C::O_EV + r] = density_bound(uL[0], P0, a.zeta * uL[0], Urho);
+  }
+  __syncthreads();
+  for (int w = tid; w < Ke * NEV; w += bs) {
+    int e = w / NEV, r = w % NEV;
+    int dh = r / Nq, m = r % Nq;
+    int ir = m % n, is = m / n;
+    const double* ev = sm + e * PE + C::O_EV;
+    if (ev[r] == 0.0) continue;
+    int d = dh >> 1, h = dh & 1;
+    // the other evaluation of the same face, if the face is interior
+    int partner = -1;
+    if (d == 0) {
+      if (h == 0 && ir > 0) partner = 1 * Nq + (ir - 1) + n * is;
+      if (h == 1 && ir + 1 < n) partner = 0 * Nq + (ir + 1) + n * is;
+    } else {
+      if (h == 0 && is > 0) partner = 3 * Nq + ir + n * (is - 1);
+      if (h == 1 && is + 1 < n) partner = 2 * Nq + ir + n * (is + 1);
+    }
+    if (partner >= 0 && ev[partner] == 0.0) continue;
+    int slot = atomicAdd(&s_list[0], 1);
+    s_list[1 + slot] = e * NEV + r;
+  }
+  __syncthreads();
+  const int nlist = s_list[0];
+  for (int w = tid; w < nlist; w += bs) {
+    int id = s_list[1 + w];
+    int e = id / NEV, r = id % NEV;
+    int dh = r / Nq, m = r % Nq;
+    int ir = m % n, is = m / n;
+    int d = dh >> 1, h = dh & 1;
+    double* base = sm + e * PE;
+    const double* fb = base + C::O_SCR;
+    int fi = (d == 0) ? (ir + h) + (n + 1) * is : ir + n * (is + h);
+    const double* fH = fb + ((d * 2 + 0) * NSF + fi) * 4;
+    const double* fL = fb + ((d * 2 + 1) * NSF + fi) * 4;
+    const double* uL = base + C::O_PRIM + 6 * m;
     double s4 = (h == 0 ? -4.0 : 4.0) * dt_lim;
     double P[4];
 #pragma unroll
-    for (int c = 0; c < 4; ++c) P[c] = s4 * (fH[c] - fL[c]) / wJ;
-    const double* uL = base + C::O_PRIM + 6 * m;
-    double Lrho = a.zeta * uL[0];
-    base[C::O_EV + r] = limiting_param_pos(uL, P, Lrho, uL[4], Urho, a.ZEROTOL, nquad);
+    for (int c = 0; c < 4; ++c) P[c] = s4 * (fH[c] - fL[c]) * uL[5];
+    double l = base[C::O_EV + r];
+    l = fmin(l, rhoe_quadratic_solve(uL, P, uL[4], a.ZEROTOL));
+    // the second solve of limiting_param_bound_rho_rhoe has Urhoe = Inf and returns 1.0
+    base[C::O_EV + r] = fmin(l, 1.0);
   }
-  if (a.counters) {
-    for (int o = 16; o > 0; o >>= 1) nquad += __shfl_xor_sync(0xffffffffu, nquad, o);
-    if ((tid & 31) == 0 && nquad) atomicAdd(&a.counters[0], (unsigned long long)nquad);
-  }
+  if (a.counters && tid == 0 && nlist) atomicAdd(&a.counters[0], (unsigned long long)nlist);
   __syncthreads();
 
   // ---- P10: combine evaluations per subcell face; blending factor 1 (NoShockCapture)
@@ -649,14 +798,14 @@ __global__ void __launch_bounds__(Cfg<N1D>::THREADS) k_stage_a(StageArgs a) {
     double L = 1.0;
     if (d == 0) {
       int si = fi % (n + 1), sj = fi / (n + 1);
-      if (si < n) L = jmin(L, ev[0 * Nq + si + n * sj]);
-      if (si > 0) L = jmin(L, ev[1 * Nq + (si - 1) + n * sj]);
+      if (si < n) L = fmin(L, ev[0 * Nq + si + n * sj]);
+      if (si > 0) L = fmin(L, ev[1 * Nq + (si - 1) + n * sj]);
     } else {
       int si = fi % n, sj = fi / n;
-      if (sj < n) L = jmin(L, ev[2 * Nq + si + n * sj]);
-      if (sj > 0) L = jmin(L, ev[3 * Nq + si + n * (sj - 1)]);
+      if (sj < n) L = fmin(L, ev[2 * Nq + si + n * sj]);
+      if (sj > 0) L = fmin(L, ev[3 * Nq + si + n * (sj - 1)]);
     }
-    base[C::O_L + r] = jmin(L, 1.0);
+    base[C::O_L + r] = L;
   }
   __syncthreads();
 
@@ -677,7 +826,8 @@ __global__ void __launch_bounds__(Cfg<N1D>::THREADS) k_stage_a(StageArgs a) {
       base[C::O_MISC + d] = any ? 1.0 : 0.0;
     }
     __syncthreads();
-    // entropy variables at the nodes of the elements that need them
+    // entropy variables v_ufun (compressible_Navier_Stokes.jl:134-144) at the nodes of
+    // the elements that need them
     for (int w = tid; w < Ke * Nq; w += bs) {
       int e = w / Nq, m = w % Nq;
       double* base = sm + e * PE;
@@ -685,11 +835,12 @@ __global__ void __launch_bounds__(Cfg<N1D>::THREADS) k_stage_a(StageArgs a) {
       const double* U = base + C::O_U + 4 * m;
       double p = pfun(g, U[0], U[1], U[2], U[3]);
       double s = log(p / pow(U[0], a.gamma));
+      double rp = 1.0 / p;
       double* vq = base + C::O_FLUX + 4 * m;
-      vq[0] = (a.gamma + 1.0 - s) - a.gm1 * U[3] / p;
-      vq[1] = U[1] * a.gm1 / p;
-      vq[2] = U[2] * a.gm1 / p;
-      vq[3] = -U[0] * a.gm1 / p;
+      vq[0] = (a.gamma + 1.0 - s) - a.gm1 * U[3] * rp;
+      vq[1] = U[1] * a.gm1 * rp;
+      vq[2] = U[2] * a.gm1 * rp;
+      vq[3] = -U[0] * a.gm1 * rp;
     }
     __syncthreads();
     for (int w = tid; w < Ke * 2; w += bs) {
@@ -874,7 +1025,7 @@ __global__ void __launch_bounds__(Cfg<N1D>::THREADS) k_stage_b(StageArgs a) {
       }
       double own = a.Lpre[(size_t)k * 2 * NSF + d * NSF + idx];
       double par = a.Lpre[(size_t)kP * 2 * NSF + d * NSF + idxP];
-      sm[e * PE + d * NSF + idx] = jmin(own, par);
+      sm[e * PE + d * NSF + idx] = fmin(own, par);
     }
     __syncthreads();
     // accumulate_f_bar_limited!(::Dim2) (subcell.jl:841-876)
@@ -900,15 +1051,15 @@ __global__ void __launch_bounds__(Cfg<N1D>::THREADS) k_stage_b(StageArgs a) {
     size_t gidx = ((size_t)k * Nq + m) * 4;
     if (limited) {
       const double* fl = sm + e * PE + 2 * NSF + 16 * NSF;
-      double wJ = op.wq[m] * a.geom[5 * (size_t)k];
+      double rwJ = 1.0 / (op.wq[m] * a.geom[5 * (size_t)k]);
       const double* fx0 = fl + ((0 * NSF) + ir + (n + 1) * is) * 4;
       const double* fx1 = fl + ((0 * NSF) + ir + 1 + (n + 1) * is) * 4;
       const double* fy0 = fl + ((1 * NSF) + ir + n * is) * 4;
       const double* fy1 = fl + ((1 * NSF) + ir + n * (is + 1)) * 4;
 #pragma unroll
       for (int c = 0; c < 4; ++c) {
-        double x = (fx1[c] - fx0[c]) / wJ;
-        double y = (fy1[c] - fy0[c]) / wJ;
+        double x = (fx1[c] - fx0[c]) * rwJ;
+        double y = (fy1[c] - fy0[c]) * rwJ;
         ru[c] = x + y;
       }
     } else if (flags & F_RHSU_FROM_L) {

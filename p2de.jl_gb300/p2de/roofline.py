@@ -19,8 +19,8 @@ NPL = 2n(n-1), high-order pairs NPH = n^2(n-1), subcell faces NSF = n(n+1):
   high-order pairs: Chandrashekar flux with two log-means       52 NPH
   gather and lift of the high-order pairs                       24 Nq + 16 NPH + 16 Nfp
   subcell prefix sums and the low-order update                  55 Nq
-  bound evaluations (P vector, density bound)                   22 * 4 Nq
-  quadratic solves evaluated                                    39 each
+  bound evaluations (P[0], density bound)                       10 * 4 Nq
+  quadratic solves evaluated (P vector, a, b, c, roots)         51 each
   combine per face                                               4 NSF
 """
 from __future__ import annotations
@@ -39,12 +39,12 @@ def stage_a_flops_per_elem(N: int) -> int:
         + 52 * NPH
         + 24 * Nq + 16 * NPH + 16 * Nfp
         + 55 * Nq
-        + 22 * 4 * Nq
+        + 10 * 4 * Nq
         + 4 * NSF
     )
 
 
-FLOPS_PER_QUAD_SOLVE = 39
+FLOPS_PER_QUAD_SOLVE = 51
 
 
 def stage_a_flops(N: int, K: int, quad_solves: float) -> float:

@@ -83,13 +83,21 @@ def test_rhs_kelvin_helmholtz_all_degrees(N):
     compare_rhs(param, md, desc, U0, dt=0.05)
 
 
+# With the intended bounds (reference_semantics off) the cell entropy bound of
+# subcell.jl:630-744 reacts to entropy production at the rounding level in smooth
+# regions: whether its greedy repair fires depends on the last bits of sums that no
+# two implementations round alike. The RHS then agrees to the size of that repair.
+TOL_INTENDED_CELL = 1e-6
+
+
 @pytest.mark.parametrize("nstage", [1, 2, 3])
 @pytest.mark.parametrize("bound", ["pos", "cell"])
 @pytest.mark.parametrize("refsem", [True, False])
 def test_rhs_modes(nstage, bound, refsem):
     b = PositivityAndCellEntropyBound() if bound == "cell" else PositivityBound()
     param, md, bc, desc, U0 = setup(problems.kelvin_helmholtz, N=3, Kx=8, Ky=8, T=0.1, bound=b, reference_semantics=refsem)
-    compare_rhs(param, md, desc, U0, dt=2e-4, nstage=nstage)
+    tol = TOL_INTENDED_CELL if (bound == "cell" and not refsem) else TOL
+    compare_rhs(param, md, desc, U0, dt=2e-4, nstage=nstage, tol=tol)
 
 
 def test_rhs_riemann_outflow():
@@ -187,3 +195,33 @@ def test_positivity_records():
     U = g.get_field(abi.FIELD_UQ).reshape(-1, 4)
     assert r.value == U[:, 0].min()
     assert r.value > 0 and e.value > 0
+
+
+GOLDEN_NAMES = ["kh_n3_4x4", "kh_n3_4x4_intended_pos", "dmr_n2_8x2", "riemann_n4_3x3", "vortex_n2_4x4"]
+
+
+@pytest.mark.parametrize("name", GOLDEN_NAMES)
+def test_gpu_matches_golden(name):
+    """The CUDA path against the committed vectors (independent of the oracle build)."""
+    from pathlib import Path
+
+    from tests_golden_cases import build
+
+    ref = np.load(Path(__file__).resolve().parent / "golden" / f"{name}.npz")
+    param, md, bc, desc, U0, t, dt = build(name)
+    g = gpu_for(param, md, desc, U0)
+    dtg = S.rhs_bang(None, g, None, p2de.TimeParam(t, dt, 1))
+    assert abs(dtg - float(ref["dt_out"])) <= 1e-13 * abs(float(ref["dt_out"]))
+    for k, f in (("rhsU", abi.FIELD_RHSU), ("rhsL", abi.FIELD_RHSL), ("rhsH", abi.FIELD_RHSH)):
+        assert relerr(g.get_field(f), ref[k]) <= TOL, k
+    S.ssp33_step(g, 0.0)
+    assert relerr(g.get_field(abi.FIELD_UQ), ref["step_Uq"]) <= TOL
+
+
+@pytest.mark.parametrize("bound", ["pos", "cell"])
+def test_rhs_intended_semantics_smooth_vortex(bound):
+    b = PositivityAndCellEntropyBound() if bound == "cell" else PositivityBound()
+    param, md, bc, desc, U0, *_ = setup(
+        problems.isentropic_vortex, N=3, Kx=6, Ky=6, strength=1.0, reference_semantics=False, bound=b
+    )
+    compare_rhs(param, md, desc, U0, dt=1e-3, nstage=2, tol=TOL_INTENDED_CELL if bound == "cell" else TOL)
