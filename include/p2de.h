@@ -200,6 +200,47 @@ int p2de_read_counters(p2de_solver* s, uint64_t out[1], int32_t reset);
  * the denominator of the FP64-pipe roofline. */
 int p2de_probe_fma_peak(int device, int32_t fp64, double* tflops);
 
+/* ---- Right-hand side without device allocation -------------------------------------
+ * No counterpart in the reference. For callers that cannot call cudaMalloc when they
+ * need a right-hand side: a process whose device memory is reserved up front by its own
+ * pool allocator (a Julia or serving process with a fixed HBM budget), or code running
+ * while a stream is captured into a CUDA graph, where cudaMalloc/cudaFree are not
+ * allowed. All scratch (subcell fluxes, blending factors, device scalars, operator
+ * table) lives in one static device array of P2DE_NOALLOC_SCRATCH_BYTES that every GPU
+ * loading this entry point keeps until the process exits; problems needing more are
+ * rejected with P2DE_ERR_BUDGET (p2de_noalloc_max_elements gives the limit per degree).
+ * The array is shared by all calls and keeps the last call's contents, so calls that
+ * overlap on the GPU race. The first call on a device does a one-time set-up (the
+ * array's device address and kernel attributes) and should come before any stream
+ * capture. Inputs and outputs are caller-owned device arrays in the layouts above. */
+#define P2DE_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
+
+typedef struct p2de_device_mesh {
+  const double* geom;    /* device, K x 5: J, rxJ, sxJ, ryJ, syJ */
+  const int32_t* nbr;    /* device, Nfp*K: 0-based exterior face-node index (mapP - 1) */
+  const int8_t* bc;      /* device, Nfp*K: 0 interior, 1 inflow, 2 outflow, 3 wall, 4 moving shock */
+  const int32_t* bcidx;  /* device, Nfp*K: row of Ival (code 1) or xyS (code 4); may be NULL without those */
+  const double* Ival;    /* device, nI x 4 */
+  int64_t nI;
+  const double* xyS;     /* device, nS x 2 */
+  int64_t nS;
+  double shock_x0;
+  double shock_inv_slope;
+  double shock_speed;
+  double shock_post[4];
+  double shock_pre[4];
+  int32_t axis_aligned;  /* 1 if every element has sxJ = ryJ = 0 */
+} p2de_device_mesh;
+
+/* Largest K that fits the static scratch for degree N. */
+int p2de_noalloc_max_elements(int32_t N, int64_t* K_max);
+
+/* rhs! (rhs.jl:5-13) for device-resident Uq (Nq*K*4) into device rhsU, on `stream`
+ * (cudaStream_t, NULL for the legacy stream), with no device allocation. Returns the
+ * stage-1 positivity-CFL dt (or dt) in *dt_out, on the host. */
+int p2de_rhs_noalloc(const p2de_param* param, const p2de_device_mesh* mesh, const double* Uq, double t, double dt,
+                     int32_t nstage, double* rhsU, double* dt_out, void* stream);
+
 /* Last error message of this handle (or of the last failed create when s is NULL). */
 int p2de_last_error(p2de_solver* s, char* buf, size_t len);
 

@@ -99,6 +99,27 @@ class P2deMesh(ctypes.Structure):
     ]
 
 
+class P2deDeviceMesh(ctypes.Structure):
+    """p2de_device_mesh: device pointers for p2de_rhs_noalloc."""
+
+    _fields_ = [
+        ("geom", c_void_p),
+        ("nbr", c_void_p),
+        ("bc", c_void_p),
+        ("bcidx", c_void_p),
+        ("Ival", c_void_p),
+        ("nI", c_int64),
+        ("xyS", c_void_p),
+        ("nS", c_int64),
+        ("shock_x0", c_double),
+        ("shock_inv_slope", c_double),
+        ("shock_speed", c_double),
+        ("shock_post", c_double * 4),
+        ("shock_pre", c_double * 4),
+        ("axis_aligned", c_int32),
+    ]
+
+
 class P2deError(RuntimeError):
     def __init__(self, status: int, message: str):
         super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
@@ -126,6 +147,12 @@ EXPORTS = [
     ("p2de_profile_steps", c_int, [SOLVER_P, c_int64, POINTER(c_double), POINTER(c_double)]),
     ("p2de_read_counters", c_int, [SOLVER_P, POINTER(ctypes.c_uint64), c_int32]),
     ("p2de_probe_fma_peak", c_int, [c_int, c_int32, POINTER(c_double)]),
+    ("p2de_noalloc_max_elements", c_int, [c_int32, POINTER(c_int64)]),
+    (
+        "p2de_rhs_noalloc",
+        c_int,
+        [POINTER(P2deParam), POINTER(P2deDeviceMesh), c_void_p, c_double, c_double, c_int32, c_void_p, POINTER(c_double), c_void_p],
+    ),
     ("p2de_last_error", c_int, [SOLVER_P, c_char_p, c_size_t]),
 ]
 
