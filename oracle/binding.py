@@ -21,10 +21,17 @@ _LIB = None
 
 
 def build(force: bool = False) -> Path:
+    import fcntl
+
     src = HERE / "p2de_oracle.cpp"
     hdr = HERE.parent / "include" / "p2de.h"
-    if force or not LIB_PATH.exists() or LIB_PATH.stat().st_mtime < max(src.stat().st_mtime, hdr.stat().st_mtime):
-        subprocess.run(["make", "-C", str(HERE), "-B" if force else "all"], check=True, capture_output=True)
+    (HERE / "_build").mkdir(exist_ok=True)
+    with open(HERE / "_build" / ".lock", "w") as lk:  # one builder at a time across processes
+        fcntl.flock(lk, fcntl.LOCK_EX)
+        stale = not LIB_PATH.exists() or LIB_PATH.stat().st_mtime < max(src.stat().st_mtime, hdr.stat().st_mtime)
+        if force or stale:
+            subprocess.run(["make", "-C", str(HERE), "-B" if force else "all"], check=True, capture_output=True)
+        fcntl.flock(lk, fcntl.LOCK_UN)
     return LIB_PATH
 
 

@@ -134,6 +134,9 @@ def _replica_rank(rank, world, port, out):
 def test_replicas_on_two_gloo_ranks():
     import torch.multiprocessing as mp
 
+    from oracle import binding
+
+    binding.build()  # once, here: the two ranks must not rebuild it concurrently
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
     port = _free_port()
