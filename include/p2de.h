@@ -200,6 +200,56 @@ int p2de_read_counters(p2de_solver* s, uint64_t out[1], int32_t reset);
  * the denominator of the FP64-pipe roofline. */
 int p2de_probe_fma_peak(int device, int32_t fp64, double* tflops);
 
+/* ---- Batches of independent solves ---------------------------------------------------
+ * Many solves of uneven mesh size and degree advanced together: one persistent launch
+ * per RK stage over a device work list of (solve, element range) tasks; each solve keeps
+ * its own CFL step and final time. Device memory comes from one pool of pool_bytes
+ * allocated at creation (the HBM budget). A solve's result is bitwise the result the
+ * same solve has alone (p2de_ssp33_step): the element arithmetic is shared.
+ * SSP33! (SSPRK33.jl:1-62) applied to each member. */
+typedef struct p2de_batch p2de_batch;
+
+int p2de_batch_create(int device, int32_t precision, size_t pool_bytes, int32_t max_solves, p2de_batch** out);
+int p2de_batch_destroy(p2de_batch* b);
+/* Device bytes one solve takes in the pool. */
+int p2de_batch_solve_bytes(const p2de_param* param, int64_t nI, int64_t nS, size_t* bytes);
+/* Admits a solve (copies mesh data and Uq); P2DE_ERR_BUDGET when it does not fit. */
+int p2de_batch_add(p2de_batch* b, const p2de_param* param, const p2de_mesh* mesh, const double* Uq, int32_t* slot);
+/* Returns the solve's memory to the pool. */
+int p2de_batch_remove(p2de_batch* b, int32_t slot);
+/* Advances every member by nsteps SSP-RK3 steps (members at their T stay put). */
+int p2de_batch_step(p2de_batch* b, int64_t nsteps);
+int p2de_batch_state(p2de_batch* b, int32_t slot, double* t, double* dt, int64_t* steps, int32_t* done,
+                     int32_t* status);
+/* (t, steps, done, status) of every slot, out[4*slot + ...]; status -1 for empty slots. */
+int p2de_batch_states(p2de_batch* b, double* out);
+int p2de_batch_get_Uq(p2de_batch* b, int32_t slot, double* Uq);
+int p2de_batch_memory(p2de_batch* b, size_t* used, size_t* capacity);
+int p2de_batch_launch_count(p2de_batch* b, int64_t* count);
+int p2de_batch_last_error(p2de_batch* b, char* buf, size_t len);
+
+/* ---- Continuous-batching server -------------------------------------------------------
+ * A worker thread admits submitted solves into a batch as slots and HBM budget free up
+ * (first come first served, skipping requests that do not fit yet), advances the batch
+ * steps_per_tick steps at a time, and retires each solve when it reaches its T, keeping
+ * its final state for p2de_server_result. Latency = retirement - submission. */
+typedef struct p2de_server p2de_server;
+
+int p2de_server_create(int device, int32_t precision, size_t hbm_budget_bytes, int32_t max_active,
+                       int32_t steps_per_tick, p2de_server** out);
+/* Thread-safe; copies the request's data. P2DE_ERR_BUDGET if it can never fit. */
+int p2de_server_submit(p2de_server* s, const p2de_param* param, const p2de_mesh* mesh, const double* Uq,
+                       int64_t* request_id);
+/* state: 0 queued, 1 running, 2 done, 3 failed; latency in seconds once finished. */
+int p2de_server_poll(p2de_server* s, int64_t request_id, int32_t* state, double* latency_s, double* t_final,
+                     int64_t* steps);
+int p2de_server_wait(p2de_server* s, int64_t request_id, double timeout_s, int32_t* state);
+/* Copies a finished request's final Uq and forgets the request. */
+int p2de_server_result(p2de_server* s, int64_t request_id, double* Uq);
+/* completed, failed, active, queued, pool bytes in use, pool capacity, ticks, busy seconds */
+int p2de_server_stats(p2de_server* s, double out[8]);
+int p2de_server_destroy(p2de_server* s);
+
 /* ---- Right-hand side without device allocation -------------------------------------
  * No counterpart in the reference. For callers that cannot call cudaMalloc when they
  * need a right-hand side: a process whose device memory is reserved up front by its own

@@ -1,0 +1,904 @@
+// Batches of independent solves (uneven mesh sizes and degrees) advanced together by
+// one persistent launch per RK stage, and a continuous-batching server on top.
+//
+// Device memory comes from one pool allocated at creation (the HBM budget); a solve is
+// admitted when its arrays fit in the pool, and its memory returns to the pool when it
+// is removed. Per-solve time, dt, status and stage minima live in slot-indexed arrays,
+// so every solve keeps its own CFL step and final time while the stages run in
+// lockstep. The 7 launches of a step are captured once in a CUDA graph that reads the
+// work list and the solve descriptors from device memory, so changing the batch's
+// membership does not need a new capture.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <condition_variable>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/p2de.h"
+#include "p2de_args.h"
+#include "p2de_batch_kernels.cuh"
+#include "p2de_batch_launch.h"
+#include "p2de_launch.h"
+#include "p2de_tables.h"
+
+using namespace p2de;
+
+namespace {
+
+constexpr size_t kAlign = 256;
+size_t align_up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
+
+// Best-fit allocator over one device allocation, with coalescing of freed blocks.
+class Pool {
+ public:
+  char* base = nullptr;
+  size_t cap = 0, in_use = 0;
+  std::map<size_t, size_t> free_;  // offset -> size
+  std::map<size_t, size_t> used_;
+
+  cudaError_t init(size_t bytes) {
+    cap = align_up(bytes);
+    cudaError_t e = cudaMalloc(&base, cap);
+    if (e != cudaSuccess) return e;
+    free_[0] = cap;
+    return cudaSuccess;
+  }
+  void release() {
+    if (base) cudaFree(base);
+    base = nullptr;
+  }
+  bool alloc(size_t bytes, size_t* off) {
+    bytes = align_up(bytes);
+    auto best = free_.end();
+    for (auto it = free_.begin(); it != free_.end(); ++it)
+      if (it->second >= bytes && (best == free_.end() || it->second < best->second)) best = it;
+    if (best == free_.end()) return false;
+    *off = best->first;
+    size_t rest = best->second - bytes;
+    free_.erase(best);
+    if (rest) free_[*off + bytes] = rest;
+    used_[*off] = bytes;
+    in_use += bytes;
+    return true;
+  }
+  void release_block(size_t off) {
+    auto it = used_.find(off);
+    if (it == used_.end()) return;
+    size_t sz = it->second;
+    used_.erase(it);
+    in_use -= sz;
+    auto nx = free_.lower_bound(off);
+    if (nx != free_.end() && off + sz == nx->first) {
+      sz += nx->second;
+      free_.erase(nx);
+    }
+    auto pv = free_.lower_bound(off);
+    if (pv != free_.begin()) {
+      --pv;
+      if (pv->first + pv->second == off) {
+        pv->second += sz;
+        return;
+      }
+    }
+    free_[off] = sz;
+  }
+  size_t largest_free() const {
+    size_t m = 0;
+    for (auto& kv : free_) m = std::max(m, kv.second);
+    return m;
+  }
+};
+
+// offsets of a solve's arrays inside its pool block
+struct Layout {
+  size_t Uq, resW, rhsU, rhsL, rhsH, geom, fbar, Lpre, Lfin, Ival, xyS, nbr, bcidx, bc, total;
+};
+
+Layout layout_for(const p2de_param& p, int64_t nI, int64_t nS) {
+  const size_t n = p.N + 1, Nq = n * n, Nfp = 4 * n, NSF = n * (n + 1), K = (size_t)p.K;
+  const bool other = p.rhs_type != P2DE_RHS_ES_LIMITED_LOW_ORDER_POS;
+  Layout L{};
+  size_t o = 0;
+  auto take = [&](size_t bytes) {
+    size_t at = o;
+    o += align_up(bytes > 0 ? bytes : 8);
+    return at;
+  };
+  L.Uq = take(8 * 4 * Nq * K);
+  L.resW = take(8 * 4 * Nq * K);
+  L.rhsU = take(8 * 4 * Nq * K);
+  L.rhsL = take(other ? 8 * 4 * Nq * K : 8);
+  L.rhsH = take(other ? 8 * 4 * Nq * K : 8);
+  L.geom = take(8 * 5 * K);
+  L.fbar = take(8 * 16 * NSF * K);
+  L.Lpre = take(8 * 2 * NSF * K);
+  L.Lfin = take(8 * 3 * 2 * NSF * K);
+  L.Ival = take(8 * 4 * (size_t)std::max<int64_t>(nI, 1));
+  L.xyS = take(8 * 2 * (size_t)std::max<int64_t>(nS, 1));
+  L.nbr = take(4 * Nfp * K);
+  L.bcidx = take(4 * Nfp * K);
+  L.bc = take(Nfp * K);
+  L.total = o;
+  return L;
+}
+
+struct Slot {
+  bool active = false;
+  p2de_param prm{};
+  int n1d = 0;
+  size_t off = 0;
+  Layout lay{};
+};
+
+double now_s() {
+  using namespace std::chrono;
+  return duration<double>(steady_clock::now().time_since_epoch()).count();
+}
+
+}  // namespace
+
+struct p2de_batch {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool mixed = false;
+  Pool pool;
+  int max_solves = 0;
+  std::vector<Slot> slots;
+  std::vector<uint8_t> active;
+  StageArgs* d_solves = nullptr;
+  uint8_t* d_active = nullptr;
+  BatchTask* d_tasks = nullptr;
+  int* d_ntasks = nullptr;
+  unsigned* d_counters = nullptr;
+  double* d_scal = nullptr;
+  unsigned long long* d_dtmin = nullptr;
+  long long* d_minrec = nullptr;
+  int* d_status = nullptr;
+  unsigned long long* d_work = nullptr;
+  OpTable* d_tables = nullptr;
+  int task_cap = 0;
+  int grid_a = 0, grid_b = 0;
+  cudaGraphExec_t graph = nullptr;
+  bool tasks_dirty = true;
+  int64_t launches = 0;
+  std::string err;
+  std::vector<void*> allocs;
+};
+
+namespace {
+
+int bfail(p2de_batch* b, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  std::vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (b) b->err = buf;
+  return code;
+}
+
+#define BCK(call)                                                                                   \
+  do {                                                                                              \
+    cudaError_t e_ = (call);                                                                        \
+    if (e_ != cudaSuccess) return bfail(b, P2DE_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+  } while (0)
+
+template <typename T>
+cudaError_t balloc(p2de_batch* b, T** p, size_t count) {
+  void* q = nullptr;
+  cudaError_t e = cudaMalloc(&q, sizeof(T) * std::max<size_t>(count, 1));
+  if (e != cudaSuccess) return e;
+  e = cudaMemsetAsync(q, 0, sizeof(T) * std::max<size_t>(count, 1), b->stream);
+  if (e != cudaSuccess) return e;
+  b->allocs.push_back(q);
+  *p = (T*)q;
+  return cudaSuccess;
+}
+
+int validate_solve(const p2de_param* p, const p2de_mesh* m, std::string& why) {
+  char buf[256];
+  if (!p || !m || !m->geom || !m->mapP) {
+    why = "null param/mesh/geom/mapP";
+    return P2DE_ERR_INVALID_ARGUMENT;
+  }
+  if (p->N < 1 || p->N > 5 || p->K < 1) {
+    why = "N outside 1..5 or K < 1";
+    return P2DE_ERR_INVALID_ARGUMENT;
+  }
+  if (p->low_order_surface_flux != P2DE_FLUX_LAX_FRIEDRICHS_ON_NODAL_VAL ||
+      p->high_order_surface_flux != P2DE_FLUX_LAX_FRIEDRICHS_ON_PROJECTED_VAL || p->rhs_type < 0 || p->rhs_type > 2 ||
+      p->bound_type < 0 || p->bound_type > 1) {
+    why = "unsupported method";
+    return P2DE_ERR_UNSUPPORTED;
+  }
+  const int64_t nfk = (int64_t)4 * (p->N + 1) * p->K;
+  for (int64_t i = 0; i < nfk; ++i)
+    if (m->mapP[i] < 1 || m->mapP[i] > nfk) {
+      std::snprintf(buf, sizeof buf, "mapP[%lld] out of range", (long long)i);
+      why = buf;
+      return P2DE_ERR_INVALID_ARGUMENT;
+    }
+  auto chk = [&](const int64_t* a, int64_t n) {
+    if (n < 0 || (n > 0 && !a)) return false;
+    for (int64_t i = 0; i < n; ++i)
+      if (a[i] < 1 || a[i] > nfk) return false;
+    return true;
+  };
+  if (!chk(m->mapI, m->nI) || !chk(m->mapO, m->nO) || !chk(m->mapW, m->nW) || !chk(m->mapS, m->nS) ||
+      (m->nI > 0 && !m->Ival) || (m->nS > 0 && !m->xyS)) {
+    why = "boundary lists";
+    return P2DE_ERR_INVALID_ARGUMENT;
+  }
+  for (int64_t k = 0; k < p->K; ++k)
+    if (!(m->geom[5 * k] > 0.0)) {
+      why = "J not positive";
+      return P2DE_ERR_INVALID_ARGUMENT;
+    }
+  return P2DE_OK;
+}
+
+int upload_tasks(p2de_batch* b) {
+  std::vector<BatchTask> t;
+  for (int s = 0; s < b->max_solves; ++s) {
+    const Slot& sl = b->slots[s];
+    if (!sl.active) continue;
+    int E = batch_elems_per_block(sl.n1d);
+    for (int k0 = 0; k0 < sl.prm.K; k0 += E) t.push_back(BatchTask{s, k0, sl.n1d, 0});
+  }
+  // largest tasks first (work per task grows with E * N1D^3)
+  std::stable_sort(t.begin(), t.end(), [](const BatchTask& x, const BatchTask& y) {
+    auto cost = [](const BatchTask& q) { return batch_elems_per_block(q.n1d) * q.n1d * q.n1d * q.n1d; };
+    return cost(x) > cost(y);
+  });
+  if ((int)t.size() > b->task_cap) {
+    if (b->d_tasks) {
+      BCK(cudaStreamSynchronize(b->stream));
+      cudaFree(b->d_tasks);
+      b->allocs.erase(std::remove(b->allocs.begin(), b->allocs.end(), (void*)b->d_tasks), b->allocs.end());
+      b->d_tasks = nullptr;
+    }
+    b->task_cap = std::max<int>((int)t.size(), 2 * b->task_cap);
+    BCK(balloc(b, &b->d_tasks, (size_t)b->task_cap));
+    if (b->graph) {
+      cudaGraphExecDestroy(b->graph);
+      b->graph = nullptr;
+    }
+  }
+  int nt = (int)t.size();
+  if (nt) BCK(cudaMemcpyAsync(b->d_tasks, t.data(), sizeof(BatchTask) * nt, cudaMemcpyHostToDevice, b->stream));
+  BCK(cudaMemcpyAsync(b->d_ntasks, &nt, sizeof nt, cudaMemcpyHostToDevice, b->stream));
+  BCK(cudaMemcpyAsync(b->d_active, b->active.data(), b->max_solves, cudaMemcpyHostToDevice, b->stream));
+  BCK(cudaStreamSynchronize(b->stream));  // the host vectors above are temporaries
+  b->tasks_dirty = false;
+  return P2DE_OK;
+}
+
+int enqueue_batch_step(p2de_batch* b) {
+  BCK(launch_batch_begin(b->d_solves, b->d_active, b->max_solves, b->d_counters, b->stream));
+  for (int stage = 1; stage <= 3; ++stage) {
+    BCK(launch_batch_a(b->mixed, b->grid_a, b->d_solves, b->d_tasks, b->d_ntasks, b->d_counters + 2 * (stage - 1), stage,
+                       b->stream));
+    BCK(launch_batch_b(b->grid_b, b->d_solves, b->d_tasks, b->d_ntasks, b->d_counters + 2 * (stage - 1) + 1, stage,
+                       b->stream));
+  }
+  return P2DE_OK;
+}
+
+int build_batch_graph(p2de_batch* b) {
+  if (b->graph) return P2DE_OK;
+  cudaStream_t cap;
+  BCK(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+  cudaStream_t user = b->stream;
+  b->stream = cap;
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+  int rc = (e == cudaSuccess) ? enqueue_batch_step(b) : P2DE_OK;
+  cudaError_t e2 = (e == cudaSuccess) ? cudaStreamEndCapture(cap, &g) : e;
+  b->stream = user;
+  cudaStreamDestroy(cap);
+  if (rc != P2DE_OK) return rc;
+  BCK(e);
+  BCK(e2);
+  BCK(cudaGraphInstantiate(&b->graph, g, 0));
+  BCK(cudaGraphDestroy(g));
+  return P2DE_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int p2de_batch_create(int device, int32_t precision, size_t pool_bytes, int32_t max_solves, p2de_batch** out) {
+  if (!out || max_solves < 1 || pool_bytes == 0 || precision < 0 || precision > 1) return P2DE_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return P2DE_ERR_NO_DEVICE;
+  if (device < 0 || device >= ndev) return P2DE_ERR_INVALID_ARGUMENT;
+  p2de_batch* b = new p2de_batch();
+  b->device = device;
+  b->mixed = precision == P2DE_PRECISION_MIXED;
+  b->max_solves = max_solves;
+  b->slots.assign(max_solves, Slot{});
+  b->active.assign(max_solves, 0);
+  auto bail = [&](int code) {
+    for (void* p : b->allocs) cudaFree(p);
+    b->pool.release();
+    if (b->stream) cudaStreamDestroy(b->stream);
+    delete b;
+    return code;
+  };
+  if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess)
+    return bail(P2DE_ERR_CUDA);
+  if (b->pool.init(pool_bytes) != cudaSuccess) return bail(P2DE_ERR_OUT_OF_MEMORY);
+  if (balloc(b, &b->d_solves, max_solves) != cudaSuccess || balloc(b, &b->d_active, max_solves) != cudaSuccess ||
+      balloc(b, &b->d_ntasks, 1) != cudaSuccess || balloc(b, &b->d_counters, 8) != cudaSuccess ||
+      balloc(b, &b->d_scal, (size_t)max_solves * S_NSCAL) != cudaSuccess ||
+      balloc(b, &b->d_dtmin, max_solves) != cudaSuccess || balloc(b, &b->d_minrec, (size_t)6 * max_solves) != cudaSuccess ||
+      balloc(b, &b->d_status, max_solves) != cudaSuccess || balloc(b, &b->d_work, 8) != cudaSuccess ||
+      balloc(b, &b->d_tables, kMaxN1D - 1) != cudaSuccess)
+    return bail(P2DE_ERR_OUT_OF_MEMORY);
+  std::vector<OpTable> tabs(kMaxN1D - 1);
+  for (int N = 1; N < kMaxN1D; ++N) build_op_table(N, 5e-16, &tabs[N - 1]);
+  if (cudaMemcpyAsync(b->d_tables, tabs.data(), sizeof(OpTable) * tabs.size(), cudaMemcpyHostToDevice, b->stream) !=
+      cudaSuccess)
+    return bail(P2DE_ERR_CUDA);
+  for (int n = 2; n <= kMaxN1D; ++n) {
+    StageGeometry geo;
+    cudaError_t e = cudaSuccess;
+    switch (n) {
+      case 2: e = stage_prepare<2>(&geo); break;
+      case 3: e = stage_prepare<3>(&geo); break;
+      case 4: e = stage_prepare<4>(&geo); break;
+      case 5: e = stage_prepare<5>(&geo); break;
+      case 6: e = stage_prepare<6>(&geo); break;
+    }
+    if (e != cudaSuccess) return bail(P2DE_ERR_CUDA);
+  }
+  int bpa = 0, bpb = 0;
+  if (batch_prepare(b->mixed, &bpa, &bpb) != cudaSuccess || bpa < 1 || bpb < 1) return bail(P2DE_ERR_CUDA);
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return bail(P2DE_ERR_CUDA);
+  b->grid_a = prop.multiProcessorCount * bpa;
+  b->grid_b = prop.multiProcessorCount * bpb;
+  b->task_cap = 0;
+  if (cudaStreamSynchronize(b->stream) != cudaSuccess) return bail(P2DE_ERR_CUDA);
+  *out = b;
+  return P2DE_OK;
+}
+
+int p2de_batch_destroy(p2de_batch* b) {
+  if (!b) return P2DE_OK;
+  cudaSetDevice(b->device);
+  cudaStreamSynchronize(b->stream);
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  for (void* p : b->allocs) cudaFree(p);
+  b->pool.release();
+  cudaStreamDestroy(b->stream);
+  delete b;
+  return P2DE_OK;
+}
+
+int p2de_batch_solve_bytes(const p2de_param* param, int64_t nI, int64_t nS, size_t* bytes) {
+  if (!param || !bytes || param->N < 1 || param->N > 5 || param->K < 1) return P2DE_ERR_INVALID_ARGUMENT;
+  *bytes = layout_for(*param, nI, nS).total;
+  return P2DE_OK;
+}
+
+int p2de_batch_add(p2de_batch* b, const p2de_param* p, const p2de_mesh* m, const double* Uq, int32_t* slot_out) {
+  if (!b || !Uq || !slot_out) return P2DE_ERR_INVALID_ARGUMENT;
+  std::string why;
+  int rc = validate_solve(p, m, why);
+  if (rc != P2DE_OK) return bfail(b, rc, "%s", why.c_str());
+  int slot = -1;
+  for (int s = 0; s < b->max_solves; ++s)
+    if (!b->slots[s].active) {
+      slot = s;
+      break;
+    }
+  if (slot < 0) return bfail(b, P2DE_ERR_BUDGET, "all %d slots in use", b->max_solves);
+  Layout lay = layout_for(*p, m->nI, m->nS);
+  if (lay.total > b->pool.cap) return bfail(b, P2DE_ERR_BUDGET, "solve needs %zu bytes, pool has %zu", lay.total, b->pool.cap);
+  size_t off = 0;
+  if (!b->pool.alloc(lay.total, &off)) return bfail(b, P2DE_ERR_BUDGET, "pool full (%zu bytes free)", b->pool.largest_free());
+  BCK(cudaSetDevice(b->device));
+  char* base = b->pool.base + off;
+  const size_t n = p->N + 1, Nq = n * n, Nfp = 4 * n, K = p->K, nfk = Nfp * K;
+  std::vector<int32_t> nbr(nfk), bcidx(nfk, 0);
+  std::vector<int8_t> bc(nfk, BC_INTERIOR);
+  for (size_t i = 0; i < nfk; ++i) nbr[i] = (int32_t)(m->mapP[i] - 1);
+  for (int64_t i = 0; i < m->nI; ++i) {
+    bc[m->mapI[i] - 1] = BC_INFLOW;
+    bcidx[m->mapI[i] - 1] = (int32_t)i;
+  }
+  for (int64_t i = 0; i < m->nO; ++i) bc[m->mapO[i] - 1] = BC_OUTFLOW;
+  for (int64_t i = 0; i < m->nW; ++i) bc[m->mapW[i] - 1] = BC_WALL;
+  for (int64_t i = 0; i < m->nS; ++i) {
+    bc[m->mapS[i] - 1] = BC_SHOCK;
+    bcidx[m->mapS[i] - 1] = (int32_t)i;
+  }
+  bool aa = true;
+  for (size_t k = 0; k < K; ++k)
+    if (m->geom[5 * k + 2] != 0.0 || m->geom[5 * k + 3] != 0.0) aa = false;
+  auto up = [&](size_t o, const void* src, size_t bytes) {
+    return cudaMemcpyAsync(base + o, src, bytes, cudaMemcpyHostToDevice, b->stream);
+  };
+  BCK(up(lay.Uq, Uq, 8 * 4 * Nq * K));
+  BCK(up(lay.geom, m->geom, 8 * 5 * K));
+  BCK(up(lay.nbr, nbr.data(), 4 * nfk));
+  BCK(up(lay.bcidx, bcidx.data(), 4 * nfk));
+  BCK(up(lay.bc, bc.data(), nfk));
+  if (m->nI > 0) BCK(up(lay.Ival, m->Ival, 8 * 4 * m->nI));
+  if (m->nS > 0) BCK(up(lay.xyS, m->xyS, 8 * 2 * m->nS));
+  StageArgs a{};
+  a.K = p->K;
+  a.nstage = 1;
+  int f = 0;
+  switch (p->rhs_type) {
+    case P2DE_RHS_LOW_ORDER_POSITIVITY: f |= F_DO_LOW | F_RHSU_FROM_L; break;
+    case P2DE_RHS_ENTROPY_STABLE: f |= F_DO_HIGH | F_RHSU_FROM_H; break;
+    default: f |= F_DO_LOW | F_DO_HIGH | F_DO_LIMIT; break;
+  }
+  if (aa) f |= F_AXIS_ALIGNED;
+  if (p->reference_semantics) f |= F_REF_SEM;
+  if (p->bound_type == P2DE_BOUND_POSITIVITY_AND_CELL_ENTROPY) f |= F_CELL_ENTROPY;
+  a.flags = f;
+  a.ops = b->d_tables + (n - 2);
+  a.Uq = (double*)(base + lay.Uq);
+  a.resW = (double*)(base + lay.resW);
+  a.geom = (const double*)(base + lay.geom);
+  a.nbr = (const int32_t*)(base + lay.nbr);
+  a.bc = (const int8_t*)(base + lay.bc);
+  a.bcidx = (const int32_t*)(base + lay.bcidx);
+  a.Ival = (const double*)(base + lay.Ival);
+  a.xyS = (const double*)(base + lay.xyS);
+  a.shock_x0 = m->shock_x0;
+  a.shock_inv_slope = m->shock_inv_slope;
+  a.shock_speed = m->shock_speed;
+  for (int c = 0; c < 4; ++c) {
+    a.shock_post[c] = m->shock_post[c];
+    a.shock_pre[c] = m->shock_pre[c];
+  }
+  a.gamma = p->gamma;
+  a.gm1 = p->gamma - 1.0;
+  a.CFL = p->CFL;
+  a.dt0 = p->dt0;
+  a.T = p->T;
+  a.zeta = p->zeta;
+  a.ZEROTOL = p->ZEROTOL;
+  a.rhsL = (double*)(base + lay.rhsL);
+  a.rhsH = (double*)(base + lay.rhsH);
+  a.rhsU = (double*)(base + lay.rhsU);
+  a.rhsxyL = a.rhsxyH = a.BFL = a.BFH = nullptr;
+  a.fbar = (double*)(base + lay.fbar);
+  a.Lpre = (double*)(base + lay.Lpre);
+  a.Lfin = (double*)(base + lay.Lfin);
+  a.scal = b->d_scal + (size_t)slot * S_NSCAL;
+  a.dtmin_bits = b->d_dtmin + slot;
+  a.minrec = b->d_minrec + 6 * (size_t)slot;
+  a.status = b->d_status + slot;
+  a.counters = b->d_work;
+  double sc[S_NSCAL] = {0};
+  sc[S_T] = p->t0;
+  int zero = 0;
+  BCK(cudaMemcpyAsync(a.scal, sc, sizeof sc, cudaMemcpyHostToDevice, b->stream));
+  BCK(cudaMemcpyAsync(a.status, &zero, sizeof zero, cudaMemcpyHostToDevice, b->stream));
+  BCK(cudaMemcpyAsync(b->d_solves + slot, &a, sizeof a, cudaMemcpyHostToDevice, b->stream));
+  BCK(cudaStreamSynchronize(b->stream));  // host buffers above are temporaries
+  Slot& sl = b->slots[slot];
+  sl.active = true;
+  sl.prm = *p;
+  sl.n1d = (int)n;
+  sl.off = off;
+  sl.lay = lay;
+  b->active[slot] = 1;
+  b->tasks_dirty = true;
+  *slot_out = slot;
+  return P2DE_OK;
+}
+
+int p2de_batch_remove(p2de_batch* b, int32_t slot) {
+  if (!b || slot < 0 || slot >= b->max_solves || !b->slots[slot].active) return P2DE_ERR_NOT_FOUND;
+  BCK(cudaSetDevice(b->device));
+  BCK(cudaStreamSynchronize(b->stream));
+  b->pool.release_block(b->slots[slot].off);
+  b->slots[slot].active = false;
+  b->active[slot] = 0;
+  b->tasks_dirty = true;
+  return P2DE_OK;
+}
+
+int p2de_batch_step(p2de_batch* b, int64_t nsteps) {
+  if (!b || nsteps < 0) return P2DE_ERR_INVALID_ARGUMENT;
+  BCK(cudaSetDevice(b->device));
+  if (b->tasks_dirty) {
+    int rc = upload_tasks(b);
+    if (rc != P2DE_OK) return rc;
+  }
+  int rc = build_batch_graph(b);
+  if (rc != P2DE_OK) return rc;
+  for (int64_t i = 0; i < nsteps; ++i) {
+    BCK(cudaGraphLaunch(b->graph, b->stream));
+    b->launches += 7;
+  }
+  BCK(cudaStreamSynchronize(b->stream));
+  return P2DE_OK;
+}
+
+int p2de_batch_state(p2de_batch* b, int32_t slot, double* t, double* dt, int64_t* steps, int32_t* done,
+                     int32_t* status) {
+  if (!b || slot < 0 || slot >= b->max_solves || !b->slots[slot].active) return P2DE_ERR_NOT_FOUND;
+  BCK(cudaSetDevice(b->device));
+  double sc[S_NSCAL];
+  int st = 0;
+  BCK(cudaMemcpyAsync(sc, b->d_scal + (size_t)slot * S_NSCAL, sizeof sc, cudaMemcpyDeviceToHost, b->stream));
+  BCK(cudaMemcpyAsync(&st, b->d_status + slot, sizeof st, cudaMemcpyDeviceToHost, b->stream));
+  BCK(cudaStreamSynchronize(b->stream));
+  if (t) *t = sc[S_T];
+  if (dt) *dt = sc[S_DT];
+  if (steps) *steps = (int64_t)sc[S_STEPS];
+  if (done) *done = (!(sc[S_T] < b->slots[slot].prm.T) || st != 0) ? 1 : 0;
+  if (status) *status = st;
+  return P2DE_OK;
+}
+
+// All slots' (t, steps, done, status) in one transfer; out is max_solves x 4.
+int p2de_batch_states(p2de_batch* b, double* out) {
+  if (!b || !out) return P2DE_ERR_INVALID_ARGUMENT;
+  BCK(cudaSetDevice(b->device));
+  std::vector<double> sc((size_t)b->max_solves * S_NSCAL);
+  std::vector<int> st(b->max_solves);
+  BCK(cudaMemcpyAsync(sc.data(), b->d_scal, sizeof(double) * sc.size(), cudaMemcpyDeviceToHost, b->stream));
+  BCK(cudaMemcpyAsync(st.data(), b->d_status, sizeof(int) * st.size(), cudaMemcpyDeviceToHost, b->stream));
+  BCK(cudaStreamSynchronize(b->stream));
+  for (int s = 0; s < b->max_solves; ++s) {
+    double t = sc[(size_t)s * S_NSCAL + S_T];
+    bool act = b->slots[s].active;
+    out[4 * s + 0] = t;
+    out[4 * s + 1] = sc[(size_t)s * S_NSCAL + S_STEPS];
+    out[4 * s + 2] = act && (!(t < b->slots[s].prm.T) || st[s] != 0) ? 1.0 : 0.0;
+    out[4 * s + 3] = act ? (double)st[s] : -1.0;
+  }
+  return P2DE_OK;
+}
+
+int p2de_batch_get_Uq(p2de_batch* b, int32_t slot, double* Uq) {
+  if (!b || !Uq || slot < 0 || slot >= b->max_solves || !b->slots[slot].active) return P2DE_ERR_NOT_FOUND;
+  BCK(cudaSetDevice(b->device));
+  const Slot& sl = b->slots[slot];
+  size_t bytes = 8 * 4 * (size_t)sl.n1d * sl.n1d * sl.prm.K;
+  BCK(cudaMemcpyAsync(Uq, b->pool.base + sl.off + sl.lay.Uq, bytes, cudaMemcpyDeviceToHost, b->stream));
+  BCK(cudaStreamSynchronize(b->stream));
+  return P2DE_OK;
+}
+
+int p2de_batch_memory(p2de_batch* b, size_t* used, size_t* capacity) {
+  if (!b) return P2DE_ERR_INVALID_ARGUMENT;
+  if (used) *used = b->pool.in_use;
+  if (capacity) *capacity = b->pool.cap;
+  return P2DE_OK;
+}
+
+int p2de_batch_launch_count(p2de_batch* b, int64_t* count) {
+  if (!b || !count) return P2DE_ERR_INVALID_ARGUMENT;
+  *count = b->launches;
+  return P2DE_OK;
+}
+
+int p2de_batch_last_error(p2de_batch* b, char* buf, size_t len) {
+  if (!b || !buf || len == 0) return P2DE_ERR_INVALID_ARGUMENT;
+  std::snprintf(buf, len, "%s", b->err.c_str());
+  return P2DE_OK;
+}
+
+}  // extern "C"
+
+// =====================================================================================
+// Continuous-batching server
+// =====================================================================================
+namespace {
+
+struct Request {
+  int64_t id = 0;
+  p2de_param prm{};
+  std::vector<double> geom, Ival, xyS, Uq;
+  std::vector<int64_t> mapP, mapI, mapO, mapW, mapS;
+  double shock[11] = {0};
+  size_t bytes = 0;
+  int state = 0;  // 0 queued, 1 running, 2 done, 3 failed
+  int slot = -1;
+  double t_submit = 0, t_admit = 0, t_done = 0, t_final = 0;
+  int64_t steps = 0;
+  int status = 0;
+};
+
+p2de_mesh mesh_of(const Request& r) {
+  p2de_mesh m{};
+  m.geom = r.geom.data();
+  m.mapP = r.mapP.data();
+  m.mapI = r.mapI.data();
+  m.nI = (int64_t)r.mapI.size();
+  m.Ival = r.Ival.data();
+  m.mapO = r.mapO.data();
+  m.nO = (int64_t)r.mapO.size();
+  m.mapW = r.mapW.data();
+  m.nW = (int64_t)r.mapW.size();
+  m.mapS = r.mapS.data();
+  m.nS = (int64_t)r.mapS.size();
+  m.xyS = r.xyS.data();
+  m.shock_x0 = r.shock[0];
+  m.shock_inv_slope = r.shock[1];
+  m.shock_speed = r.shock[2];
+  for (int c = 0; c < 4; ++c) {
+    m.shock_post[c] = r.shock[3 + c];
+    m.shock_pre[c] = r.shock[7 + c];
+  }
+  return m;
+}
+
+}  // namespace
+
+struct p2de_server {
+  p2de_batch* batch = nullptr;
+  int max_active = 0;
+  int steps_per_tick = 1;
+  std::mutex mu;
+  std::condition_variable cv;
+  std::deque<int64_t> queue;
+  std::unordered_map<int64_t, Request> reqs;
+  std::unordered_map<int, int64_t> slot_req;
+  std::thread worker;
+  bool stop = false;
+  int64_t next_id = 1;
+  int64_t completed = 0, failed = 0, ticks = 0;
+  double busy_s = 0.0;
+  std::string err;
+};
+
+namespace {
+
+void server_loop(p2de_server* sv) {
+  cudaSetDevice(sv->batch->device);
+  std::vector<double> states((size_t)sv->batch->max_solves * 4);
+  for (;;) {
+    // admit queued requests that fit, first come first served, skipping ones that do not fit yet
+    std::vector<int64_t> admit;
+    {
+      std::unique_lock<std::mutex> lk(sv->mu);
+      sv->cv.wait(lk, [&] { return sv->stop || !sv->queue.empty() || !sv->slot_req.empty(); });
+      if (sv->stop) return;
+      int active = (int)sv->slot_req.size();
+      size_t room = sv->batch->pool.cap - sv->batch->pool.in_use;
+      for (auto it = sv->queue.begin(); it != sv->queue.end() && active + (int)admit.size() < sv->max_active;) {
+        Request& r = sv->reqs[*it];
+        if (r.bytes <= room) {
+          admit.push_back(*it);
+          room -= r.bytes;
+          it = sv->queue.erase(it);
+        } else {
+          ++it;
+        }
+      }
+    }
+    for (int64_t id : admit) {
+      Request* r;
+      {
+        std::lock_guard<std::mutex> lk(sv->mu);
+        r = &sv->reqs[id];
+      }
+      p2de_mesh m = mesh_of(*r);
+      int32_t slot = -1;
+      int rc = p2de_batch_add(sv->batch, &r->prm, &m, r->Uq.data(), &slot);
+      std::lock_guard<std::mutex> lk(sv->mu);
+      if (rc == P2DE_OK) {
+        r->state = 1;
+        r->slot = slot;
+        r->t_admit = now_s();
+        sv->slot_req[slot] = id;
+      } else if (rc == P2DE_ERR_BUDGET) {
+        sv->queue.push_front(id);  // pool fragmentation: try again after a retirement
+      } else {
+        r->state = 3;
+        r->status = rc;
+        r->t_done = now_s();
+        sv->failed++;
+        sv->cv.notify_all();
+      }
+    }
+    bool any;
+    {
+      std::lock_guard<std::mutex> lk(sv->mu);
+      any = !sv->slot_req.empty();
+    }
+    if (!any) continue;
+    double t0 = now_s();
+    int rc = p2de_batch_step(sv->batch, sv->steps_per_tick);
+    if (rc == P2DE_OK) rc = p2de_batch_states(sv->batch, states.data());
+    sv->busy_s += now_s() - t0;
+    sv->ticks++;
+    // retire finished solves
+    std::vector<std::pair<int, int64_t>> done;
+    {
+      std::lock_guard<std::mutex> lk(sv->mu);
+      for (auto& kv : sv->slot_req)
+        if (rc != P2DE_OK || states[4 * kv.first + 2] != 0.0) done.push_back({kv.first, kv.second});
+    }
+    for (auto& d : done) {
+      Request* r;
+      {
+        std::lock_guard<std::mutex> lk(sv->mu);
+        r = &sv->reqs[d.second];
+      }
+      int rc2 = p2de_batch_get_Uq(sv->batch, d.first, r->Uq.data());
+      double tt = states[4 * d.first], steps = states[4 * d.first + 1];
+      int st = (int)states[4 * d.first + 3];
+      p2de_batch_remove(sv->batch, d.first);
+      std::lock_guard<std::mutex> lk(sv->mu);
+      r->t_done = now_s();
+      r->t_final = tt;
+      r->steps = (int64_t)steps;
+      r->status = st;
+      bool ok = rc == P2DE_OK && rc2 == P2DE_OK && st == 0;
+      r->state = ok ? 2 : 3;
+      if (ok)
+        sv->completed++;
+      else
+        sv->failed++;
+      sv->slot_req.erase(d.first);
+      sv->cv.notify_all();
+    }
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int p2de_server_create(int device, int32_t precision, size_t hbm_budget_bytes, int32_t max_active,
+                       int32_t steps_per_tick, p2de_server** out) {
+  if (!out || max_active < 1 || steps_per_tick < 1) return P2DE_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  p2de_batch* b = nullptr;
+  int rc = p2de_batch_create(device, precision, hbm_budget_bytes, max_active, &b);
+  if (rc != P2DE_OK) return rc;
+  p2de_server* sv = new p2de_server();
+  sv->batch = b;
+  sv->max_active = max_active;
+  sv->steps_per_tick = steps_per_tick;
+  sv->worker = std::thread(server_loop, sv);
+  *out = sv;
+  return P2DE_OK;
+}
+
+int p2de_server_submit(p2de_server* sv, const p2de_param* p, const p2de_mesh* m, const double* Uq, int64_t* id) {
+  if (!sv || !Uq || !id) return P2DE_ERR_INVALID_ARGUMENT;
+  std::string why;
+  int rc = validate_solve(p, m, why);
+  if (rc != P2DE_OK) {
+    std::lock_guard<std::mutex> lk(sv->mu);
+    sv->err = why;
+    return rc;
+  }
+  Request r;
+  r.prm = *p;
+  const size_t n = p->N + 1, Nq = n * n, K = p->K, nfk = 4 * n * K;
+  r.geom.assign(m->geom, m->geom + 5 * K);
+  r.mapP.assign(m->mapP, m->mapP + nfk);
+  if (m->nI > 0) {
+    r.mapI.assign(m->mapI, m->mapI + m->nI);
+    r.Ival.assign(m->Ival, m->Ival + 4 * m->nI);
+  }
+  if (m->nO > 0) r.mapO.assign(m->mapO, m->mapO + m->nO);
+  if (m->nW > 0) r.mapW.assign(m->mapW, m->mapW + m->nW);
+  if (m->nS > 0) {
+    r.mapS.assign(m->mapS, m->mapS + m->nS);
+    r.xyS.assign(m->xyS, m->xyS + 2 * m->nS);
+  }
+  r.shock[0] = m->shock_x0;
+  r.shock[1] = m->shock_inv_slope;
+  r.shock[2] = m->shock_speed;
+  for (int c = 0; c < 4; ++c) {
+    r.shock[3 + c] = m->shock_post[c];
+    r.shock[7 + c] = m->shock_pre[c];
+  }
+  r.Uq.assign(Uq, Uq + 4 * Nq * K);
+  r.bytes = layout_for(*p, m->nI, m->nS).total;
+  if (r.bytes > sv->batch->pool.cap) {
+    std::lock_guard<std::mutex> lk(sv->mu);
+    sv->err = "request larger than the HBM budget";
+    return P2DE_ERR_BUDGET;
+  }
+  r.t_submit = now_s();
+  std::lock_guard<std::mutex> lk(sv->mu);
+  r.id = sv->next_id++;
+  *id = r.id;
+  sv->reqs.emplace(r.id, std::move(r));
+  sv->queue.push_back(*id);
+  sv->cv.notify_all();
+  return P2DE_OK;
+}
+
+int p2de_server_poll(p2de_server* sv, int64_t id, int32_t* state, double* latency_s, double* t_final, int64_t* steps) {
+  if (!sv) return P2DE_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(sv->mu);
+  auto it = sv->reqs.find(id);
+  if (it == sv->reqs.end()) return P2DE_ERR_NOT_FOUND;
+  const Request& r = it->second;
+  if (state) *state = r.state;
+  if (latency_s) *latency_s = r.state >= 2 ? r.t_done - r.t_submit : -1.0;
+  if (t_final) *t_final = r.t_final;
+  if (steps) *steps = r.steps;
+  return P2DE_OK;
+}
+
+// Blocks until the request is done or failed, or until timeout_s passes.
+int p2de_server_wait(p2de_server* sv, int64_t id, double timeout_s, int32_t* state) {
+  if (!sv) return P2DE_ERR_INVALID_ARGUMENT;
+  std::unique_lock<std::mutex> lk(sv->mu);
+  auto deadline = std::chrono::steady_clock::now() + std::chrono::duration<double>(timeout_s);
+  for (;;) {
+    auto it = sv->reqs.find(id);
+    if (it == sv->reqs.end()) return P2DE_ERR_NOT_FOUND;
+    if (it->second.state >= 2) {
+      if (state) *state = it->second.state;
+      return P2DE_OK;
+    }
+    if (sv->cv.wait_until(lk, deadline) == std::cv_status::timeout) {
+      if (state) *state = it->second.state;
+      return P2DE_OK;
+    }
+  }
+}
+
+// Copies the final state of a finished request and forgets the request.
+int p2de_server_result(p2de_server* sv, int64_t id, double* Uq) {
+  if (!sv || !Uq) return P2DE_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(sv->mu);
+  auto it = sv->reqs.find(id);
+  if (it == sv->reqs.end()) return P2DE_ERR_NOT_FOUND;
+  if (it->second.state < 2) return P2DE_ERR_INVALID_ARGUMENT;
+  std::memcpy(Uq, it->second.Uq.data(), sizeof(double) * it->second.Uq.size());
+  int st = it->second.state;
+  sv->reqs.erase(it);
+  return st == 2 ? P2DE_OK : P2DE_ERR_NOT_POSITIVE;
+}
+
+// stats: completed, failed, active, queued, pool bytes in use, pool capacity, ticks, busy seconds
+int p2de_server_stats(p2de_server* sv, double out[8]) {
+  if (!sv || !out) return P2DE_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(sv->mu);
+  out[0] = (double)sv->completed;
+  out[1] = (double)sv->failed;
+  out[2] = (double)sv->slot_req.size();
+  out[3] = (double)sv->queue.size();
+  out[4] = (double)sv->batch->pool.in_use;
+  out[5] = (double)sv->batch->pool.cap;
+  out[6] = (double)sv->ticks;
+  out[7] = sv->busy_s;
+  return P2DE_OK;
+}
+
+int p2de_server_destroy(p2de_server* sv) {
+  if (!sv) return P2DE_OK;
+  {
+    std::lock_guard<std::mutex> lk(sv->mu);
+    sv->stop = true;
+    sv->cv.notify_all();
+  }
+  if (sv->worker.joinable()) sv->worker.join();
+  p2de_batch_destroy(sv->batch);
+  delete sv;
+  return P2DE_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,48 @@
+// Batched stage kernels, FP64 flux differencing; kernel B and the step begin.
+#define P2DE_BATCH_COMMON_KERNELS
+#include "p2de_batch_kernels.cuh"
+#include "p2de_batch_launch.h"
+
+namespace p2de {
+
+cudaError_t batch_prepare_f64(int* bpa, int* bpb) {
+  cudaError_t e = cudaFuncSetAttribute(k_batch_a<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBatchSmemA);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(k_batch_b, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBatchSmemB);
+  if (e != cudaSuccess) return e;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpa, k_batch_a<double>, kBatchThreads, kBatchSmemA);
+  if (e != cudaSuccess) return e;
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpb, k_batch_b, kBatchThreads, kBatchSmemB);
+}
+
+cudaError_t launch_batch_a_f64(int grid, const StageArgs* solves, const BatchTask* tasks, const int* ntasks,
+                               unsigned* counter, int nstage, cudaStream_t st) {
+  k_batch_a<double><<<grid, kBatchThreads, kBatchSmemA, st>>>(solves, tasks, ntasks, counter, nstage);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch_b(int grid, const StageArgs* solves, const BatchTask* tasks, const int* ntasks,
+                           unsigned* counter, int nstage, cudaStream_t st) {
+  k_batch_b<<<grid, kBatchThreads, kBatchSmemB, st>>>(solves, tasks, ntasks, counter, nstage);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch_begin(const StageArgs* solves, const uint8_t* active, int nslots, unsigned* counters,
+                               cudaStream_t st) {
+  int grid = (nslots + 127) / 128;
+  k_batch_begin<<<grid > 0 ? grid : 1, 128, 0, st>>>(solves, active, nslots, counters);
+  return cudaGetLastError();
+}
+
+int batch_elems_per_block(int n1d) {
+  switch (n1d) {
+    case 2: return Cfg<2>::E;
+    case 3: return Cfg<3>::E;
+    case 4: return Cfg<4>::E;
+    case 5: return Cfg<5>::E;
+    case 6: return Cfg<6>::E;
+  }
+  return 0;
+}
+
+}  // namespace p2de

@@ -1,0 +1,121 @@
+// Batched stage kernels: one persistent launch per RK stage advances every active
+// solve of a batch, whatever their mesh sizes and polynomial degrees. Blocks take
+// tasks (solve, first element, N+1) from a device work list through an atomic
+// counter, copy the solve's descriptor into shared memory and run the same stage
+// bodies as the one-solve kernels, so a solve's result in a batch is bitwise the
+// result it has alone.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "p2de_args.h"
+#include "p2de_stage.cuh"
+
+namespace p2de {
+
+struct BatchTask {
+  int32_t solve;  // slot of the solve descriptor
+  int32_t k0;     // first element of the task
+  int32_t n1d;    // N + 1 of the solve
+  int32_t pad_;
+};
+
+constexpr int kBatchThreads = 128;
+
+__host__ __device__ constexpr size_t smax(size_t a, size_t b) { return a > b ? a : b; }
+// dynamic shared memory of the batched kernels: the largest over N1D = 2..6
+constexpr size_t kBatchSmemA =
+    smax(smax(smax(Cfg<2>::SMEM_A, Cfg<3>::SMEM_A), smax(Cfg<4>::SMEM_A, Cfg<5>::SMEM_A)), Cfg<6>::SMEM_A);
+constexpr size_t kBatchSmemB =
+    smax(smax(smax(Cfg<2>::SMEM_B, Cfg<3>::SMEM_B), smax(Cfg<4>::SMEM_B, Cfg<5>::SMEM_B)), Cfg<6>::SMEM_B);
+
+// Fetches the next task; returns false when the list is exhausted. The solve's
+// descriptor lands in `sa` with the stage's flags: F_UPDATE always, F_CFL at stage 1.
+__device__ __forceinline__ bool batch_next(const StageArgs* solves, const BatchTask* tasks, const int* ntasks,
+                                           unsigned* counter, int nstage, StageArgs& sa, BatchTask& tk, int& s_task) {
+  __syncthreads();  // the previous task's shared data is no longer read
+  if (threadIdx.x == 0) s_task = (int)atomicAdd(counter, 1u);
+  __syncthreads();
+  const int t = s_task;
+  if (t >= *ntasks) return false;
+  tk = tasks[t];
+  const int* src = reinterpret_cast<const int*>(solves + tk.solve);
+  int* dst = reinterpret_cast<int*>(&sa);
+  for (int i = threadIdx.x; i < (int)(sizeof(StageArgs) / sizeof(int)); i += blockDim.x) dst[i] = src[i];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    sa.nstage = nstage;
+    int f = sa.flags | F_UPDATE;
+    if (nstage == 1 && (f & F_DO_LOW)) f |= F_CFL;
+    sa.flags = f;
+  }
+  __syncthreads();
+  return true;
+}
+
+template <typename TH>
+__global__ void __launch_bounds__(kBatchThreads) k_batch_a(const StageArgs* solves, const BatchTask* tasks,
+                                                           const int* ntasks, unsigned* counter, int nstage) {
+  extern __shared__ double sm[];
+  __shared__ StageArgs sa;
+  __shared__ int s_task;
+  BatchTask tk;
+  while (batch_next(solves, tasks, ntasks, counter, nstage, sa, tk, s_task)) {
+    switch (tk.n1d) {
+      case 2: stage_a_body<2, TH>(sa, tk.k0, sm); break;
+      case 3: stage_a_body<3, TH>(sa, tk.k0, sm); break;
+      case 4: stage_a_body<4, TH>(sa, tk.k0, sm); break;
+      case 5: stage_a_body<5, TH>(sa, tk.k0, sm); break;
+      case 6: stage_a_body<6, TH>(sa, tk.k0, sm); break;
+    }
+  }
+}
+
+// Kernel B and the step begin are defined in one translation unit only.
+#ifdef P2DE_BATCH_COMMON_KERNELS
+__global__ void __launch_bounds__(kBatchThreads) k_batch_b(const StageArgs* solves, const BatchTask* tasks,
+                                                           const int* ntasks, unsigned* counter, int nstage) {
+  extern __shared__ double sm[];
+  __shared__ StageArgs sa;
+  __shared__ int s_task;
+  BatchTask tk;
+  while (batch_next(solves, tasks, ntasks, counter, nstage, sa, tk, s_task)) {
+    switch (tk.n1d) {
+      case 2: stage_b_body<2>(sa, tk.k0, sm); break;
+      case 3: stage_b_body<3>(sa, tk.k0, sm); break;
+      case 4: stage_b_body<4>(sa, tk.k0, sm); break;
+      case 5: stage_b_body<5>(sa, tk.k0, sm); break;
+      case 6: stage_b_body<6>(sa, tk.k0, sm); break;
+    }
+  }
+}
+
+// Step begin for every slot (SSPRK33.jl:126 per solve) and reset of the six task
+// counters of the step. scal/dtmin/minrec/status are slot-indexed arrays.
+__global__ void k_batch_begin(const StageArgs* solves, const uint8_t* active, int nslots, unsigned* counters) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s == 0)
+    for (int i = 0; i < 6; ++i) counters[i] = 0u;
+  if (s >= nslots || !active[s]) return;
+  const StageArgs& a = solves[s];
+  double* scal = a.scal;
+  double t = scal[S_T];
+  if (!(t < a.T) || *a.status != 0) {
+    scal[S_DONE] = 1.0;
+    return;
+  }
+  scal[S_DONE] = 0.0;
+  double dt = fmin(a.CFL * a.dt0, a.T - t);
+  scal[S_DT_LIM] = dt;
+  if (!(dt > 0.0)) {
+    atomicOr(a.status, ST_BAD_DT);
+    scal[S_DONE] = 1.0;
+    return;
+  }
+  *a.dtmin_bits = (unsigned long long)__double_as_longlong(dt);
+  for (int i = 0; i < 6; ++i) a.minrec[i] = 0x7ff0000000000000LL;
+}
+#endif  // P2DE_BATCH_COMMON_KERNELS
+
+}  // namespace p2de

@@ -194,17 +194,17 @@ __device__ __forceinline__ double density_bound(double U0, double P0, double Lrh
 // =====================================================================================
 // Kernel A
 // =====================================================================================
+// Body of kernel A for the E elements k0 .. k0+E-1 of the solve `a`; every early return
+// is uniform over the block. Used by the one-solve kernel and the batched kernel.
 template <int N1D, typename TH>
-__global__ void __launch_bounds__(Cfg<N1D>::THREADS) k_stage_a(StageArgs a) {
+__device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double* sm) {
   using C = Cfg<N1D>;
   constexpr int n = C::n, Nq = C::Nq, Nfp = C::Nfp, NSF = C::NSF, NEV = C::NEV;
   constexpr int PE = C::PER_ELEM_A;
   if (a.scal[S_DONE] != 0.0) return;
-  extern __shared__ double sm[];
   int* s_list = reinterpret_cast<int*>(sm + PE * C::E);  // [0]: count, then eval indices
   const OpTable& op = *a.ops;
   const int tid = threadIdx.x, bs = blockDim.x;
-  const int k0 = blockIdx.x * C::E;
   const int Ke = min(C::E, a.K - k0);
   if (Ke <= 0) return;
   const int flags = a.flags;
@@ -964,19 +964,25 @@ __global__ void __launch_bounds__(Cfg<N1D>::THREADS) k_stage_a(StageArgs a) {
   }
 }
 
+template <int N1D, typename TH>
+__global__ void __launch_bounds__(Cfg<N1D>::THREADS) k_stage_a(StageArgs a) {
+  extern __shared__ double sm[];
+  stage_a_body<N1D, TH>(a, blockIdx.x * Cfg<N1D>::E, sm);
+}
+
 // =====================================================================================
 // Kernel B: symmetrize, blend, rhsU, SSP-RK3 stage update
 // =====================================================================================
+// Body of kernel B for the elements k0 .. k0+E-1 of the solve `a`; the block holding
+// element 0 also advances the solve's dt and t.
 template <int N1D>
-__global__ void __launch_bounds__(Cfg<N1D>::THREADS) k_stage_b(StageArgs a) {
+__device__ __forceinline__ void stage_b_body(const StageArgs& a, int k0, double* sm) {
   using C = Cfg<N1D>;
   constexpr int n = C::n, Nq = C::Nq, Nfp = C::Nfp, NSF = C::NSF;
   constexpr int PE = C::PER_ELEM_B;
   if (a.scal[S_DONE] != 0.0) return;
-  extern __shared__ double sm[];
   const OpTable& op = *a.ops;
   const int tid = threadIdx.x, bs = blockDim.x;
-  const int k0 = blockIdx.x * C::E;
   const int Ke = min(C::E, a.K - k0);
   if (Ke <= 0) return;
   const int flags = a.flags;
@@ -1117,7 +1123,7 @@ __global__ void __launch_bounds__(Cfg<N1D>::THREADS) k_stage_b(StageArgs a) {
       atomicMin(&a.minrec[2 * s + 0], order_key(rmin));
       atomicMin(&a.minrec[2 * s + 1], order_key(emin));
     }
-    if (blockIdx.x == 0 && tid == 0) {
+    if (k0 == 0 && tid == 0) {
       if (a.nstage == 1) {
         a.scal[S_DT] = dt;
         a.scal[S_DT_LIM] = dt;
@@ -1128,6 +1134,12 @@ __global__ void __launch_bounds__(Cfg<N1D>::THREADS) k_stage_b(StageArgs a) {
       }
     }
   }
+}
+
+template <int N1D>
+__global__ void __launch_bounds__(Cfg<N1D>::THREADS) k_stage_b(StageArgs a) {
+  extern __shared__ double sm[];
+  stage_b_body<N1D>(a, blockIdx.x * Cfg<N1D>::E, sm);
 }
 
 }  // namespace p2de
