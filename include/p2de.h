@@ -200,6 +200,15 @@ int p2de_read_counters(p2de_solver* s, uint64_t out[1], int32_t reset);
  * the denominator of the FP64-pipe roofline. */
 int p2de_probe_fma_peak(int device, int32_t fp64, double* tflops);
 
+/* Elements per thread block of the stage kernels (1..epb_max, the shared-memory limit).
+ * Results do not depend on it: each element's arithmetic is the same at every value.
+ * No counterpart in the reference (a launch parameter of this implementation). */
+int p2de_set_elements_per_block(p2de_solver* s, int32_t epb);
+int p2de_get_elements_per_block(p2de_solver* s, int32_t* epb, int32_t* epb_max);
+/* Times stage kernel A at candidate elements-per-block (stage scratch only: the
+ * state is unchanged), keeps the fastest and returns it with its milliseconds. */
+int p2de_autotune(p2de_solver* s, int32_t* best_epb, double* best_ms);
+
 /* ---- Batches of independent solves ---------------------------------------------------
  * Many solves of uneven mesh size and degree advanced together: one persistent launch
  * per RK stage over a device work list of (solve, element range) tasks; each solve keeps
@@ -227,6 +236,14 @@ int p2de_batch_get_Uq(p2de_batch* b, int32_t slot, double* Uq);
 int p2de_batch_memory(p2de_batch* b, size_t* used, size_t* capacity);
 int p2de_batch_launch_count(p2de_batch* b, int64_t* count);
 int p2de_batch_last_error(p2de_batch* b, char* buf, size_t len);
+/* Elements per block of the batch's tasks for degree N (1..5); as for one solve,
+ * results do not depend on it. */
+int p2de_batch_set_elements_per_block(p2de_batch* b, int32_t N, int32_t epb);
+int p2de_batch_get_elements_per_block(p2de_batch* b, int32_t N, int32_t* epb, int32_t* epb_max);
+/* Per degree present, times batched stage kernel A over that degree's members at
+ * candidate elements-per-block (no state changes) and keeps the fastest;
+ * best_epb[N-1] receives it (0 for absent degrees). */
+int p2de_batch_autotune(p2de_batch* b, int32_t best_epb[5]);
 
 /* ---- Continuous-batching server -------------------------------------------------------
  * A worker thread admits submitted solves into a batch as slots and HBM budget free up

@@ -5,6 +5,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <algorithm>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -427,6 +428,7 @@ int p2de_initialize_DG(const p2de_param* prm, const p2de_mesh* mesh, int device,
   }
   StageArgs& a = s->base;
   a.K = s->K;
+  a.epb = s->geo.elems_per_block;
   a.ops = s->ops + (s->N1D - 2);
   a.Uq = s->Uq;
   a.resW = s->resW;
@@ -684,6 +686,81 @@ int p2de_profile_steps(p2de_solver* s, int64_t nsteps, double* t, double ms[3]) 
   CK(cudaStreamSynchronize(s->stream));
   *t = sc[S_T];
   return check_status(s);
+}
+
+int p2de_set_elements_per_block(p2de_solver* s, int32_t epb) {
+  if (!s) return P2DE_ERR_INVALID_ARGUMENT;
+  if (epb < 1 || epb > s->geo.elems_per_block_max)
+    return fail(s, P2DE_ERR_INVALID_ARGUMENT, "elements per block %d outside 1..%d", epb, s->geo.elems_per_block_max);
+  CK(cudaSetDevice(s->device));
+  CK(cudaStreamSynchronize(s->stream));
+  s->base.epb = epb;
+  if (s->graph) {
+    cudaGraphExecDestroy(s->graph);
+    s->graph = nullptr;
+  }
+  return P2DE_OK;
+}
+
+int p2de_get_elements_per_block(p2de_solver* s, int32_t* epb, int32_t* epb_max) {
+  if (!s) return P2DE_ERR_INVALID_ARGUMENT;
+  if (epb) *epb = s->base.epb;
+  if (epb_max) *epb_max = s->geo.elems_per_block_max;
+  return P2DE_OK;
+}
+
+// Times stage kernel A (stage 2 flags, state left unchanged: no update) for each
+// candidate elements-per-block and keeps the fastest.
+int p2de_autotune(p2de_solver* s, int32_t* best_epb, double* best_ms) {
+  if (!s) return P2DE_ERR_INVALID_ARGUMENT;
+  CK(cudaSetDevice(s->device));
+  const int emax = s->geo.elems_per_block_max, edef = s->geo.elems_per_block;
+  std::vector<int> cand;
+  for (int e : {1, 2, 3, 4, 6, 8, 12, 16, 24, 32, edef})
+    if (e <= emax && std::find(cand.begin(), cand.end(), e) == cand.end()) cand.push_back(e);
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  double sc[S_NSCAL] = {0};
+  CK(cudaMemcpyAsync(sc, s->scal, sizeof sc, cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  double keep[S_NSCAL];
+  std::memcpy(keep, sc, sizeof sc);
+  sc[S_DONE] = 0.0;
+  if (!(sc[S_DT_LIM] > 0.0)) sc[S_DT_LIM] = std::fmin(s->prm.CFL * s->prm.dt0, s->prm.T - s->prm.t0);
+  CK(cudaMemcpyAsync(s->scal, sc, sizeof sc, cudaMemcpyHostToDevice, s->stream));
+  int best = edef;
+  double bms = 1e30;
+  for (int e : cand) {
+    StageArgs a = s->base;
+    a.epb = e;
+    a.nstage = 2;
+    a.flags = flags_for(s, 2, false, false);
+    float tot = 0.f;
+    for (int rep = 0; rep < 4; ++rep) {
+      CK(cudaEventRecord(e0, s->stream));
+      CK(launch_a_n1d(s->N1D, a, s->mixed, s->stream));
+      CK(cudaEventRecord(e1, s->stream));
+      CK(cudaEventSynchronize(e1));
+      float ms;
+      CK(cudaEventElapsedTime(&ms, e0, e1));
+      if (rep > 0) tot += ms;  // first launch warms up
+    }
+    s->launches += 4;
+    double ms = tot / 3.0;
+    if (ms < bms) {
+      bms = ms;
+      best = e;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  CK(cudaMemcpyAsync(s->scal, keep, sizeof keep, cudaMemcpyHostToDevice, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  int rc = p2de_set_elements_per_block(s, best);
+  if (best_epb) *best_epb = best;
+  if (best_ms) *best_ms = bms;
+  return rc;
 }
 
 int p2de_read_counters(p2de_solver* s, uint64_t out[1], int32_t reset) {

@@ -35,7 +35,7 @@ struct StageArgs {
   int K;
   int nstage;  // 1..3
   int flags;
-  int pad_;
+  int epb;  // elements per block (<= the degree's maximum, Cfg::E_MAX)
   const OpTable* ops;
   double* Uq;
   double* resW;

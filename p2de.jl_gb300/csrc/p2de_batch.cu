@@ -168,7 +168,10 @@ struct p2de_batch {
   unsigned long long* d_work = nullptr;
   OpTable* d_tables = nullptr;
   int task_cap = 0;
+  int sms = 0;
   int grid_a = 0, grid_b = 0;
+  size_t smem_a = 0, smem_b = 0;  // launch shared memory of the captured graph
+  int epb[kMaxN1D + 1] = {};     // elements per block per N1D
   cudaGraphExec_t graph = nullptr;
   bool tasks_dirty = true;
   int64_t launches = 0;
@@ -248,19 +251,40 @@ int validate_solve(const p2de_param* p, const p2de_mesh* m, std::string& why) {
   return P2DE_OK;
 }
 
-int upload_tasks(p2de_batch* b) {
+std::vector<BatchTask> build_tasks(const p2de_batch* b, size_t* smem_a, size_t* smem_b) {
   std::vector<BatchTask> t;
+  *smem_a = 0;
+  *smem_b = 0;
   for (int s = 0; s < b->max_solves; ++s) {
     const Slot& sl = b->slots[s];
     if (!sl.active) continue;
-    int E = batch_elems_per_block(sl.n1d);
-    for (int k0 = 0; k0 < sl.prm.K; k0 += E) t.push_back(BatchTask{s, k0, sl.n1d, 0});
+    int E = b->epb[sl.n1d];
+    *smem_a = std::max(*smem_a, batch_smem_a(sl.n1d, E));
+    *smem_b = std::max(*smem_b, batch_smem_b(sl.n1d, E));
+    for (int k0 = 0; k0 < sl.prm.K; k0 += E) t.push_back(BatchTask{s, k0, sl.n1d, E});
   }
-  // largest tasks first (work per task grows with E * N1D^3)
+  // largest tasks first (work per task grows with elements * N1D^3)
   std::stable_sort(t.begin(), t.end(), [](const BatchTask& x, const BatchTask& y) {
-    auto cost = [](const BatchTask& q) { return batch_elems_per_block(q.n1d) * q.n1d * q.n1d * q.n1d; };
+    auto cost = [](const BatchTask& q) { return q.epb * q.n1d * q.n1d * q.n1d; };
     return cost(x) > cost(y);
   });
+  if (*smem_a == 0) *smem_a = batch_smem_a(2, 1);
+  if (*smem_b == 0) *smem_b = batch_smem_b(2, 1);
+  return t;
+}
+
+int upload_tasks(p2de_batch* b) {
+  size_t sa = 0, sb = 0;
+  std::vector<BatchTask> t = build_tasks(b, &sa, &sb);
+  if (sa != b->smem_a || sb != b->smem_b) {  // launch configuration changes: new capture
+    b->smem_a = sa;
+    b->smem_b = sb;
+    if (b->graph) {
+      BCK(cudaStreamSynchronize(b->stream));
+      cudaGraphExecDestroy(b->graph);
+      b->graph = nullptr;
+    }
+  }
   if ((int)t.size() > b->task_cap) {
     if (b->d_tasks) {
       BCK(cudaStreamSynchronize(b->stream));
@@ -287,16 +311,28 @@ int upload_tasks(p2de_batch* b) {
 int enqueue_batch_step(p2de_batch* b) {
   BCK(launch_batch_begin(b->d_solves, b->d_active, b->max_solves, b->d_counters, b->stream));
   for (int stage = 1; stage <= 3; ++stage) {
-    BCK(launch_batch_a(b->mixed, b->grid_a, b->d_solves, b->d_tasks, b->d_ntasks, b->d_counters + 2 * (stage - 1), stage,
-                       b->stream));
-    BCK(launch_batch_b(b->grid_b, b->d_solves, b->d_tasks, b->d_ntasks, b->d_counters + 2 * (stage - 1) + 1, stage,
-                       b->stream));
+    BCK(launch_batch_a(b->mixed, b->grid_a, b->smem_a, b->d_solves, b->d_tasks, b->d_ntasks,
+                       b->d_counters + 2 * (stage - 1), stage, b->stream));
+    BCK(launch_batch_b(b->grid_b, b->smem_b, b->d_solves, b->d_tasks, b->d_ntasks, b->d_counters + 2 * (stage - 1) + 1,
+                       stage, b->stream));
   }
+  return P2DE_OK;
+}
+
+// persistent grids: resident blocks per SM at the current shared memory, times the SMs
+int size_grids(p2de_batch* b) {
+  int bpa = 0, bpb = 0;
+  BCK(batch_occupancy(b->mixed, b->smem_a, b->smem_b, &bpa, &bpb));
+  if (bpa < 1 || bpb < 1) return bfail(b, P2DE_ERR_CUDA, "batched kernels do not fit an SM");
+  b->grid_a = b->sms * bpa;
+  b->grid_b = b->sms * bpb;
   return P2DE_OK;
 }
 
 int build_batch_graph(p2de_batch* b) {
   if (b->graph) return P2DE_OK;
+  int rg = size_grids(b);
+  if (rg != P2DE_OK) return rg;
   cudaStream_t cap;
   BCK(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
   cudaStream_t user = b->stream;
@@ -365,12 +401,11 @@ int p2de_batch_create(int device, int32_t precision, size_t pool_bytes, int32_t 
     }
     if (e != cudaSuccess) return bail(P2DE_ERR_CUDA);
   }
-  int bpa = 0, bpb = 0;
-  if (batch_prepare(b->mixed, &bpa, &bpb) != cudaSuccess || bpa < 1 || bpb < 1) return bail(P2DE_ERR_CUDA);
+  if (batch_prepare(b->mixed) != cudaSuccess) return bail(P2DE_ERR_CUDA);
   cudaDeviceProp prop;
   if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return bail(P2DE_ERR_CUDA);
-  b->grid_a = prop.multiProcessorCount * bpa;
-  b->grid_b = prop.multiProcessorCount * bpb;
+  b->sms = prop.multiProcessorCount;
+  for (int n = 2; n <= kMaxN1D; ++n) b->epb[n] = batch_elems_per_block(n);
   b->task_cap = 0;
   if (cudaStreamSynchronize(b->stream) != cudaSuccess) return bail(P2DE_ERR_CUDA);
   *out = b;
@@ -533,6 +568,118 @@ int p2de_batch_step(p2de_batch* b, int64_t nsteps) {
   }
   BCK(cudaStreamSynchronize(b->stream));
   return P2DE_OK;
+}
+
+int p2de_batch_set_elements_per_block(p2de_batch* b, int32_t N, int32_t epb) {
+  if (!b || N < 1 || N + 1 > kMaxN1D) return P2DE_ERR_INVALID_ARGUMENT;
+  const int emax = batch_elems_per_block_max(N + 1);
+  if (epb < 1 || epb > emax)
+    return bfail(b, P2DE_ERR_INVALID_ARGUMENT, "elements per block %d outside 1..%d", epb, emax);
+  if (b->epb[N + 1] != epb) {
+    b->epb[N + 1] = epb;
+    b->tasks_dirty = true;
+  }
+  return P2DE_OK;
+}
+
+int p2de_batch_get_elements_per_block(p2de_batch* b, int32_t N, int32_t* epb, int32_t* epb_max) {
+  if (!b || N < 1 || N + 1 > kMaxN1D) return P2DE_ERR_INVALID_ARGUMENT;
+  if (epb) *epb = b->epb[N + 1];
+  if (epb_max) *epb_max = batch_elems_per_block_max(N + 1);
+  return P2DE_OK;
+}
+
+// For each degree present in the batch, times batched stage kernel A (stage 2 flags;
+// it writes only stage scratch, so no solve's state changes) over that degree's
+// solves for each candidate elements-per-block, and keeps the fastest.
+int p2de_batch_autotune(p2de_batch* b, int32_t best_epb[5]) {
+  if (!b) return P2DE_ERR_INVALID_ARGUMENT;
+  BCK(cudaSetDevice(b->device));
+  BCK(cudaStreamSynchronize(b->stream));
+  if (best_epb)
+    for (int i = 0; i < 5; ++i) best_epb[i] = 0;
+  std::vector<double> keep((size_t)b->max_solves * S_NSCAL);
+  BCK(cudaMemcpyAsync(keep.data(), b->d_scal, sizeof(double) * keep.size(), cudaMemcpyDeviceToHost, b->stream));
+  BCK(cudaStreamSynchronize(b->stream));
+  std::vector<double> sc = keep;
+  int64_t ksum = 0;
+  for (int s = 0; s < b->max_solves; ++s) {
+    const Slot& sl = b->slots[s];
+    if (!sl.active) continue;
+    ksum += sl.prm.K;
+    double* q = &sc[(size_t)s * S_NSCAL];
+    q[S_DONE] = 0.0;
+    if (!(q[S_DT_LIM] > 0.0)) q[S_DT_LIM] = std::fmin(sl.prm.CFL * sl.prm.dt0, sl.prm.T - sl.prm.t0);
+  }
+  if (ksum == 0) return P2DE_OK;
+  if (ksum > b->task_cap) {  // room for one task per element
+    if (b->d_tasks) {
+      cudaFree(b->d_tasks);
+      b->allocs.erase(std::remove(b->allocs.begin(), b->allocs.end(), (void*)b->d_tasks), b->allocs.end());
+      b->d_tasks = nullptr;
+    }
+    b->task_cap = (int)ksum;
+    BCK(balloc(b, &b->d_tasks, (size_t)b->task_cap));
+  }
+  if (b->graph) {  // the task list is rewritten below
+    cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+  }
+  b->tasks_dirty = true;
+  BCK(cudaMemcpyAsync(b->d_scal, sc.data(), sizeof(double) * sc.size(), cudaMemcpyHostToDevice, b->stream));
+  cudaEvent_t e0, e1;
+  BCK(cudaEventCreate(&e0));
+  BCK(cudaEventCreate(&e1));
+  int rc = P2DE_OK;
+  unsigned* counter = b->d_counters + 6;
+  for (int n1d = 2; n1d <= kMaxN1D && rc == P2DE_OK; ++n1d) {
+    bool present = false;
+    for (int s = 0; s < b->max_solves; ++s) present |= b->slots[s].active && b->slots[s].n1d == n1d;
+    if (!present) continue;
+    const int emax = batch_elems_per_block_max(n1d), edef = batch_elems_per_block(n1d);
+    int best = b->epb[n1d];
+    double bms = 1e30;
+    for (int e : {1, 2, 3, 4, 6, 8, 12, 16, 24, 32, edef}) {
+      if (e > emax) continue;
+      std::vector<BatchTask> t;
+      for (int s = 0; s < b->max_solves; ++s) {
+        const Slot& sl = b->slots[s];
+        if (!sl.active || sl.n1d != n1d) continue;
+        for (int k0 = 0; k0 < sl.prm.K; k0 += e) t.push_back(BatchTask{s, k0, n1d, e});
+      }
+      int nt = (int)t.size();
+      int bpa = 0, bpb = 0;
+      const size_t sma = batch_smem_a(n1d, e);
+      cudaError_t ce = batch_occupancy(b->mixed, sma, batch_smem_b(n1d, e), &bpa, &bpb);
+      if (ce != cudaSuccess || bpa < 1) continue;
+      const int grid = std::min(b->sms * bpa, nt);
+      BCK(cudaMemcpyAsync(b->d_tasks, t.data(), sizeof(BatchTask) * nt, cudaMemcpyHostToDevice, b->stream));
+      BCK(cudaMemcpyAsync(b->d_ntasks, &nt, sizeof nt, cudaMemcpyHostToDevice, b->stream));
+      float tot = 0.f;
+      for (int rep = 0; rep < 4; ++rep) {
+        BCK(cudaMemsetAsync(counter, 0, sizeof(unsigned), b->stream));
+        BCK(cudaEventRecord(e0, b->stream));
+        BCK(launch_batch_a(b->mixed, grid, sma, b->d_solves, b->d_tasks, b->d_ntasks, counter, 2, b->stream));
+        BCK(cudaEventRecord(e1, b->stream));
+        BCK(cudaEventSynchronize(e1));
+        float ms;
+        BCK(cudaEventElapsedTime(&ms, e0, e1));
+        if (rep > 0) tot += ms;  // first launch warms up
+      }
+      b->launches += 4;
+      if (tot / 3.0 < bms) {
+        bms = tot / 3.0;
+        best = e;
+      }
+    }
+    b->epb[n1d] = best;
+    if (best_epb) best_epb[n1d - 2] = best;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  BCK(cudaMemcpyAsync(b->d_scal, keep.data(), sizeof(double) * keep.size(), cudaMemcpyHostToDevice, b->stream));
+  BCK(cudaStreamSynchronize(b->stream));  // the host vectors above are temporaries
+  return rc;
 }
 
 int p2de_batch_state(p2de_batch* b, int32_t slot, double* t, double* dt, int64_t* steps, int32_t* done,

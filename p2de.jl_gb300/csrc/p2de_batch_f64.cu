@@ -5,25 +5,28 @@
 
 namespace p2de {
 
-cudaError_t batch_prepare_f64(int* bpa, int* bpb) {
-  cudaError_t e = cudaFuncSetAttribute(k_batch_a<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBatchSmemA);
+cudaError_t batch_prepare_f64() {
+  cudaError_t e = cudaFuncSetAttribute(k_batch_a<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)kBatchSmemAMax);
   if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(k_batch_b, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBatchSmemB);
-  if (e != cudaSuccess) return e;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpa, k_batch_a<double>, kBatchThreads, kBatchSmemA);
-  if (e != cudaSuccess) return e;
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpb, k_batch_b, kBatchThreads, kBatchSmemB);
+  return cudaFuncSetAttribute(k_batch_b, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBatchSmemBMax);
 }
 
-cudaError_t launch_batch_a_f64(int grid, const StageArgs* solves, const BatchTask* tasks, const int* ntasks,
-                               unsigned* counter, int nstage, cudaStream_t st) {
-  k_batch_a<double><<<grid, kBatchThreads, kBatchSmemA, st>>>(solves, tasks, ntasks, counter, nstage);
+cudaError_t batch_occupancy_f64(size_t smem_a, size_t smem_b, int* bpa, int* bpb) {
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpa, k_batch_a<double>, kBatchThreads, smem_a);
+  if (e != cudaSuccess) return e;
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(bpb, k_batch_b, kBatchThreads, smem_b);
+}
+
+cudaError_t launch_batch_a_f64(int grid, size_t smem, const StageArgs* solves, const BatchTask* tasks,
+                               const int* ntasks, unsigned* counter, int nstage, cudaStream_t st) {
+  k_batch_a<double><<<grid, kBatchThreads, smem, st>>>(solves, tasks, ntasks, counter, nstage);
   return cudaGetLastError();
 }
 
-cudaError_t launch_batch_b(int grid, const StageArgs* solves, const BatchTask* tasks, const int* ntasks,
+cudaError_t launch_batch_b(int grid, size_t smem, const StageArgs* solves, const BatchTask* tasks, const int* ntasks,
                            unsigned* counter, int nstage, cudaStream_t st) {
-  k_batch_b<<<grid, kBatchThreads, kBatchSmemB, st>>>(solves, tasks, ntasks, counter, nstage);
+  k_batch_b<<<grid, kBatchThreads, smem, st>>>(solves, tasks, ntasks, counter, nstage);
   return cudaGetLastError();
 }
 
@@ -41,6 +44,39 @@ int batch_elems_per_block(int n1d) {
     case 4: return Cfg<4>::E;
     case 5: return Cfg<5>::E;
     case 6: return Cfg<6>::E;
+  }
+  return 0;
+}
+
+int batch_elems_per_block_max(int n1d) {
+  switch (n1d) {
+    case 2: return Cfg<2>::E_MAX;
+    case 3: return Cfg<3>::E_MAX;
+    case 4: return Cfg<4>::E_MAX;
+    case 5: return Cfg<5>::E_MAX;
+    case 6: return Cfg<6>::E_MAX;
+  }
+  return 0;
+}
+
+size_t batch_smem_a(int n1d, int epb) {
+  switch (n1d) {
+    case 2: return Cfg<2>::smem_a(epb);
+    case 3: return Cfg<3>::smem_a(epb);
+    case 4: return Cfg<4>::smem_a(epb);
+    case 5: return Cfg<5>::smem_a(epb);
+    case 6: return Cfg<6>::smem_a(epb);
+  }
+  return 0;
+}
+
+size_t batch_smem_b(int n1d, int epb) {
+  switch (n1d) {
+    case 2: return Cfg<2>::smem_b(epb);
+    case 3: return Cfg<3>::smem_b(epb);
+    case 4: return Cfg<4>::smem_b(epb);
+    case 5: return Cfg<5>::smem_b(epb);
+    case 6: return Cfg<6>::smem_b(epb);
   }
   return 0;
 }

@@ -18,17 +18,22 @@ struct BatchTask {
   int32_t solve;  // slot of the solve descriptor
   int32_t k0;     // first element of the task
   int32_t n1d;    // N + 1 of the solve
-  int32_t pad_;
+  int32_t epb;    // elements in this task (<= the degree's elements per block)
 };
 
 constexpr int kBatchThreads = 128;
 
 __host__ __device__ constexpr size_t smax(size_t a, size_t b) { return a > b ? a : b; }
-// dynamic shared memory of the batched kernels: the largest over N1D = 2..6
-constexpr size_t kBatchSmemA =
-    smax(smax(smax(Cfg<2>::SMEM_A, Cfg<3>::SMEM_A), smax(Cfg<4>::SMEM_A, Cfg<5>::SMEM_A)), Cfg<6>::SMEM_A);
-constexpr size_t kBatchSmemB =
-    smax(smax(smax(Cfg<2>::SMEM_B, Cfg<3>::SMEM_B), smax(Cfg<4>::SMEM_B, Cfg<5>::SMEM_B)), Cfg<6>::SMEM_B);
+// largest dynamic shared memory the batched kernels may be launched with: the largest
+// over N1D = 2..6 at each degree's maximum elements per block
+constexpr size_t kBatchSmemAMax =
+    smax(smax(smax(Cfg<2>::smem_a(Cfg<2>::E_MAX), Cfg<3>::smem_a(Cfg<3>::E_MAX)),
+              smax(Cfg<4>::smem_a(Cfg<4>::E_MAX), Cfg<5>::smem_a(Cfg<5>::E_MAX))),
+         Cfg<6>::smem_a(Cfg<6>::E_MAX));
+constexpr size_t kBatchSmemBMax =
+    smax(smax(smax(Cfg<2>::smem_b(Cfg<2>::E_MAX), Cfg<3>::smem_b(Cfg<3>::E_MAX)),
+              smax(Cfg<4>::smem_b(Cfg<4>::E_MAX), Cfg<5>::smem_b(Cfg<5>::E_MAX))),
+         Cfg<6>::smem_b(Cfg<6>::E_MAX));
 
 // Fetches the next task; returns false when the list is exhausted. The solve's
 // descriptor lands in `sa` with the stage's flags: F_UPDATE always, F_CFL at stage 1.
@@ -46,6 +51,7 @@ __device__ __forceinline__ bool batch_next(const StageArgs* solves, const BatchT
   __syncthreads();
   if (threadIdx.x == 0) {
     sa.nstage = nstage;
+    sa.epb = tk.epb;
     int f = sa.flags | F_UPDATE;
     if (nstage == 1 && (f & F_DO_LOW)) f |= F_CFL;
     sa.flags = f;

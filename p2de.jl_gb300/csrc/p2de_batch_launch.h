@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <stddef.h>
 #include <stdint.h>
 
 #include "p2de_args.h"
@@ -10,15 +11,19 @@ namespace p2de {
 
 struct BatchTask;
 
-// Sets the kernels' shared-memory limits and returns resident blocks per SM of the
-// stage kernels (the persistent grid is that times the SM count).
-cudaError_t batch_prepare(bool mixed, int* blocks_per_sm_a, int* blocks_per_sm_b);
-cudaError_t launch_batch_a(bool mixed, int grid, const StageArgs* solves, const BatchTask* tasks, const int* ntasks,
-                           unsigned* counter, int nstage, cudaStream_t st);
-cudaError_t launch_batch_b(int grid, const StageArgs* solves, const BatchTask* tasks, const int* ntasks,
+// Sets the kernels' largest shared-memory limits.
+cudaError_t batch_prepare(bool mixed);
+// Resident blocks per SM of the stage kernels at the given dynamic shared memory.
+cudaError_t batch_occupancy(bool mixed, size_t smem_a, size_t smem_b, int* blocks_per_sm_a, int* blocks_per_sm_b);
+cudaError_t launch_batch_a(bool mixed, int grid, size_t smem, const StageArgs* solves, const BatchTask* tasks,
+                           const int* ntasks, unsigned* counter, int nstage, cudaStream_t st);
+cudaError_t launch_batch_b(int grid, size_t smem, const StageArgs* solves, const BatchTask* tasks, const int* ntasks,
                            unsigned* counter, int nstage, cudaStream_t st);
 cudaError_t launch_batch_begin(const StageArgs* solves, const uint8_t* active, int nslots, unsigned* counters,
                                cudaStream_t st);
-int batch_elems_per_block(int n1d);
+int batch_elems_per_block(int n1d);      // default
+int batch_elems_per_block_max(int n1d);  // shared-memory limit
+size_t batch_smem_a(int n1d, int epb);
+size_t batch_smem_b(int n1d, int epb);
 
 }  // namespace p2de

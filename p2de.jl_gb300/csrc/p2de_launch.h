@@ -8,7 +8,8 @@
 namespace p2de {
 
 struct StageGeometry {
-  int elems_per_block;
+  int elems_per_block;      // default
+  int elems_per_block_max;  // largest allowed (shared-memory limit)
   int threads;
   size_t smem_a;
   size_t smem_b;

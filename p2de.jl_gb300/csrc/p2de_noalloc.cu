@@ -171,6 +171,7 @@ extern "C" int p2de_rhs_noalloc(const p2de_param* prm, const p2de_device_mesh* m
 
   StageArgs a{};
   a.K = prm->K;
+  a.epb = geo.elems_per_block;
   a.nstage = nstage;
   int f = 0;
   switch (prm->rhs_type) {

@@ -75,10 +75,15 @@ struct Cfg {
   static constexpr int O_MISC = O_L + 2 * NSF;     // 4
   static constexpr int PER_ELEM_A = O_MISC + 4;
   // plus a block-wide list of bound evaluations that need the quadratic solve
-  static constexpr size_t SMEM_A = sizeof(double) * PER_ELEM_A * E + sizeof(int) * (NEV * E + 4);
+  static constexpr size_t smem_a(int e) { return sizeof(double) * PER_ELEM_A * e + sizeof(int) * (NEV * e + 4); }
+  static constexpr size_t SMEM_A = smem_a(E);
   // kernel B
   static constexpr int PER_ELEM_B = 2 * NSF + 16 * NSF + 8 * NSF + 8;
-  static constexpr size_t SMEM_B = sizeof(double) * PER_ELEM_B * E;
+  static constexpr size_t smem_b(int e) { return sizeof(double) * PER_ELEM_B * e; }
+  static constexpr size_t SMEM_B = smem_b(E);
+  // largest elements-per-block whose kernel-A shared memory fits 224 KB (capped at 32)
+  static constexpr int E_MAX_RAW = (int)((224 * 1024 - 64) / (sizeof(double) * PER_ELEM_A + sizeof(int) * NEV));
+  static constexpr int E_MAX = E_MAX_RAW < 32 ? E_MAX_RAW : 32;
   static constexpr int FBAR = 16 * NSF;  // per element: [dir][H/L][face][c]
 };
 
@@ -202,10 +207,11 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
   constexpr int n = C::n, Nq = C::Nq, Nfp = C::Nfp, NSF = C::NSF, NEV = C::NEV;
   constexpr int PE = C::PER_ELEM_A;
   if (a.scal[S_DONE] != 0.0) return;
-  int* s_list = reinterpret_cast<int*>(sm + PE * C::E);  // [0]: count, then eval indices
+  const int E = a.epb;
+  int* s_list = reinterpret_cast<int*>(sm + PE * E);  // [0]: count, then eval indices
   const OpTable& op = *a.ops;
   const int tid = threadIdx.x, bs = blockDim.x;
-  const int Ke = min(C::E, a.K - k0);
+  const int Ke = min(E, a.K - k0);
   if (Ke <= 0) return;
   const int flags = a.flags;
   const bool aa = flags & F_AXIS_ALIGNED;
@@ -967,7 +973,7 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
 template <int N1D, typename TH>
 __global__ void __launch_bounds__(Cfg<N1D>::THREADS) k_stage_a(StageArgs a) {
   extern __shared__ double sm[];
-  stage_a_body<N1D, TH>(a, blockIdx.x * Cfg<N1D>::E, sm);
+  stage_a_body<N1D, TH>(a, blockIdx.x * a.epb, sm);
 }
 
 // =====================================================================================
@@ -983,7 +989,7 @@ __device__ __forceinline__ void stage_b_body(const StageArgs& a, int k0, double*
   if (a.scal[S_DONE] != 0.0) return;
   const OpTable& op = *a.ops;
   const int tid = threadIdx.x, bs = blockDim.x;
-  const int Ke = min(C::E, a.K - k0);
+  const int Ke = min(a.epb, a.K - k0);
   if (Ke <= 0) return;
   const int flags = a.flags;
   const int s = a.nstage - 1;
@@ -1139,7 +1145,7 @@ __device__ __forceinline__ void stage_b_body(const StageArgs& a, int k0, double*
 template <int N1D>
 __global__ void __launch_bounds__(Cfg<N1D>::THREADS) k_stage_b(StageArgs a) {
   extern __shared__ double sm[];
-  stage_b_body<N1D>(a, blockIdx.x * Cfg<N1D>::E, sm);
+  stage_b_body<N1D>(a, blockIdx.x * a.epb, sm);
 }
 
 }  // namespace p2de

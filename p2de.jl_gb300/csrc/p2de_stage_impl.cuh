@@ -10,13 +10,16 @@ template <int N1D>
 cudaError_t stage_prepare(StageGeometry* geo) {
   using C = Cfg<N1D>;
   cudaError_t e;
-  e = cudaFuncSetAttribute(k_stage_a<N1D, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::SMEM_A);
+  e = cudaFuncSetAttribute(k_stage_a<N1D, double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)C::smem_a(C::E_MAX));
   if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(k_stage_a<N1D, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::SMEM_A);
+  e = cudaFuncSetAttribute(k_stage_a<N1D, float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)C::smem_a(C::E_MAX));
   if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(k_stage_b<N1D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::SMEM_B);
+  e = cudaFuncSetAttribute(k_stage_b<N1D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::smem_b(C::E_MAX));
   if (e != cudaSuccess) return e;
   geo->elems_per_block = C::E;
+  geo->elems_per_block_max = C::E_MAX;
   geo->threads = C::THREADS;
   geo->smem_a = C::SMEM_A;
   geo->smem_b = C::SMEM_B;
@@ -28,19 +31,21 @@ cudaError_t stage_prepare(StageGeometry* geo) {
 template <int N1D>
 cudaError_t launch_stage_a(const StageArgs& a, bool mixed, cudaStream_t st) {
   using C = Cfg<N1D>;
-  int grid = (a.K + C::E - 1) / C::E;
+  if (a.epb < 1 || a.epb > C::E_MAX) return cudaErrorInvalidValue;
+  int grid = (a.K + a.epb - 1) / a.epb;
   if (mixed)
-    k_stage_a<N1D, float><<<grid, C::THREADS, C::SMEM_A, st>>>(a);
+    k_stage_a<N1D, float><<<grid, C::THREADS, C::smem_a(a.epb), st>>>(a);
   else
-    k_stage_a<N1D, double><<<grid, C::THREADS, C::SMEM_A, st>>>(a);
+    k_stage_a<N1D, double><<<grid, C::THREADS, C::smem_a(a.epb), st>>>(a);
   return cudaGetLastError();
 }
 
 template <int N1D>
 cudaError_t launch_stage_b(const StageArgs& a, cudaStream_t st) {
   using C = Cfg<N1D>;
-  int grid = (a.K + C::E - 1) / C::E;
-  k_stage_b<N1D><<<grid, C::THREADS, C::SMEM_B, st>>>(a);
+  if (a.epb < 1 || a.epb > C::E_MAX) return cudaErrorInvalidValue;
+  int grid = (a.K + a.epb - 1) / a.epb;
+  k_stage_b<N1D><<<grid, C::THREADS, C::smem_b(a.epb), st>>>(a);
   return cudaGetLastError();
 }
 

@@ -147,6 +147,9 @@ EXPORTS = [
     ("p2de_profile_steps", c_int, [SOLVER_P, c_int64, POINTER(c_double), POINTER(c_double)]),
     ("p2de_read_counters", c_int, [SOLVER_P, POINTER(ctypes.c_uint64), c_int32]),
     ("p2de_probe_fma_peak", c_int, [c_int, c_int32, POINTER(c_double)]),
+    ("p2de_set_elements_per_block", c_int, [SOLVER_P, c_int32]),
+    ("p2de_get_elements_per_block", c_int, [SOLVER_P, POINTER(c_int32), POINTER(c_int32)]),
+    ("p2de_autotune", c_int, [SOLVER_P, POINTER(c_int32), POINTER(c_double)]),
     ("p2de_batch_create", c_int, [c_int, c_int32, c_size_t, c_int32, POINTER(c_void_p)]),
     ("p2de_batch_destroy", c_int, [c_void_p]),
     ("p2de_batch_solve_bytes", c_int, [POINTER(P2deParam), c_int64, c_int64, POINTER(c_size_t)]),
@@ -163,6 +166,9 @@ EXPORTS = [
     ("p2de_batch_memory", c_int, [c_void_p, POINTER(c_size_t), POINTER(c_size_t)]),
     ("p2de_batch_launch_count", c_int, [c_void_p, POINTER(c_int64)]),
     ("p2de_batch_last_error", c_int, [c_void_p, c_char_p, c_size_t]),
+    ("p2de_batch_set_elements_per_block", c_int, [c_void_p, c_int32, c_int32]),
+    ("p2de_batch_get_elements_per_block", c_int, [c_void_p, c_int32, POINTER(c_int32), POINTER(c_int32)]),
+    ("p2de_batch_autotune", c_int, [c_void_p, POINTER(c_int32)]),
     ("p2de_server_create", c_int, [c_int, c_int32, c_size_t, c_int32, c_int32, POINTER(c_void_p)]),
     ("p2de_server_submit", c_int, [c_void_p, POINTER(P2deParam), POINTER(P2deMesh), POINTER(c_double), POINTER(c_int64)]),
     (

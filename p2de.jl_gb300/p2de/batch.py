@@ -85,6 +85,20 @@ class Batch:
         self._check(self.lib.p2de_batch_launch_count(self.h, byref(c)))
         return c.value
 
+    def elements_per_block(self, N: int) -> tuple[int, int]:
+        e, m = c_int32(), c_int32()
+        self._check(self.lib.p2de_batch_get_elements_per_block(self.h, N, byref(e), byref(m)))
+        return e.value, m.value
+
+    def set_elements_per_block(self, N: int, epb: int) -> None:
+        self._check(self.lib.p2de_batch_set_elements_per_block(self.h, N, int(epb)))
+
+    def autotune(self) -> dict[int, int]:
+        """Fastest elements-per-block per degree present; {N: epb}."""
+        out = (c_int32 * 5)()
+        self._check(self.lib.p2de_batch_autotune(self.h, out))
+        return {N: out[N - 1] for N in range(1, 6) if out[N - 1] > 0}
+
     def close(self):
         if getattr(self, "h", None):
             self.lib.p2de_batch_destroy(self.h)

@@ -7,7 +7,7 @@ so rhs! and SSP33! are rhs_bang and SSP33_bang.
 from __future__ import annotations
 
 import ctypes
-from ctypes import byref, c_double, c_int64, c_void_p
+from ctypes import byref, c_double, c_int32, c_int64, c_void_p
 from dataclasses import dataclass
 
 import numpy as np
@@ -215,6 +215,21 @@ class Solver:
         c = c_int64()
         self._check(self.lib.p2de_launch_count(self.handle, byref(c)))
         return c.value
+
+    def elements_per_block(self) -> tuple[int, int]:
+        """(current, largest) elements per thread block of the stage kernels."""
+        e, m = c_int32(), c_int32()
+        self._check(self.lib.p2de_get_elements_per_block(self.handle, byref(e), byref(m)))
+        return e.value, m.value
+
+    def set_elements_per_block(self, epb: int) -> None:
+        self._check(self.lib.p2de_set_elements_per_block(self.handle, int(epb)))
+
+    def autotune(self) -> tuple[int, float]:
+        """Keeps the fastest elements-per-block for stage kernel A; returns it with its ms."""
+        e, ms = c_int32(), c_double()
+        self._check(self.lib.p2de_autotune(self.handle, byref(e), byref(ms)))
+        return e.value, ms.value
 
 
 class State:
