@@ -215,21 +215,312 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def _advance(solver, nsteps, t):
+    """nsteps graph-replayed steps from time t; returns (t, steps done)."""
+    tt, n = c_double(t), c_int64()
+    solver._check(solver.lib.p2de_ssp33_advance(solver.handle, nsteps, byref(tt), byref(n)))
+    return tt.value, n.value
+
+
+def _timed_alone(param, md, desc, U0, warmup, steps):
+    """One solve alone on the single-solve path: (seconds for `steps` steps after
+    `warmup`, final Uq, steps done). Device time by CUDA events on the solver's stream."""
+    import torch
+
+    from p2de import abi
+    from p2de import solver as S
+
+    g = S.Solver(param, md, desc)
+    st = torch.cuda.Stream()
+    g._check(g.lib.p2de_set_stream(g.handle, ctypes.c_void_p(st.cuda_stream)))
+    g.set_Uq(U0)
+    t, _ = _advance(g, warmup, 0.0)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(st)
+    t, n = _advance(g, steps, t)
+    e1.record(st)
+    torch.cuda.synchronize()
+    U = g.get_field(abi.FIELD_UQ)
+    g.close()
+    return e0.elapsed_time(e1) * 1e-3, U, n
+
+
+def run_batch64(args):
+    """Many uneven solves in one persistent launch per RK stage: 64 four-quadrant
+    Riemann problems (meshes 32^2..192^2, N in {2,3,4}), mixed precision, autotuned
+    elements-per-block, CUDA-graph-captured step; against each solve alone on the
+    plain (FP64, single-solve) path. A step advances every member by one SSP-RK3 step."""
+    import torch
+
+    from p2de import workloads as W
+    from p2de.batch import Batch, solve_bytes
+
+    torch.cuda.set_device(0)
+    cases = W.riemann_batch_cases(64, seed=3)
+    steps, warm = args.steps, args.warmup
+    built = {p: [W.build_case(c, p) for c in cases] for p in ("mixed", "fp64")}
+    nodes = np.array([c.nodes for c in cases], dtype=np.float64)
+    out = {}
+    finals = {}
+    for prec in ("mixed", "fp64"):
+        descs = [b[3] for b in built[prec]]
+        pool = int(sum(solve_bytes(d) for d in descs) * 1.05) + (64 << 20)
+        b = Batch(pool_bytes=pool, max_solves=len(cases), precision=prec)
+        slots = [b.add(bb[3], bb[4]) for bb in built[prec]]
+        t0 = time.perf_counter()
+        tuned = b.autotune() if not args.no_autotune else {}
+        tune_s = time.perf_counter() - t0
+        b.step(warm)
+        s0 = b.states()[slots, 1].copy()
+        with ClockSampler(0) as clk:
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            b.step(steps)
+            el = time.perf_counter() - t0
+        s1 = b.states()[slots, 1]
+        dof = float(np.sum(nodes * 3 * (s1 - s0)))
+        out[prec] = {"value": dof / el, "seconds": el, "steps_per_member_min": int(np.min(s1 - s0)),
+                     "autotuned_elements_per_block": {str(k): v for k, v in tuned.items()},
+                     "autotune_s": tune_s, "pool_bytes": pool, "clocks": clk.summary()}
+        finals[prec] = [b.Uq(s) for s in slots]
+        b.close()
+    # each member alone on the single-solve path, same warm-up and step count
+    alone = {}
+    ref_U = []
+    for prec in ("fp64", "mixed"):
+        tot, dof = 0.0, 0.0
+        for c, (param, md, bc, desc, U0) in zip(cases, built[prec]):
+            sec, U, n = _timed_alone(param, md, desc, U0, warm, steps)
+            tot += sec
+            dof += c.nodes * 3 * n
+            if prec == "fp64":
+                ref_U.append(U)
+        alone[prec] = {"value": dof / tot, "seconds": tot}
+    # accuracy of the batched mixed members against the FP64 solves (same steps)
+    errs = []
+    for c, bb, U, R in zip(cases, built["fp64"], finals["mixed"], ref_U):
+        Wq = W.quadrature_weights(c.N, bb[1].geom)
+        errs.append(W.relative_errors(U, R, Wq)["rho"]["L1"])
+    fp64_batch_vs_alone = max(float(np.max(np.abs(U - R))) for U, R in zip(finals["fp64"], ref_U))
+    total_nodes = int(nodes.sum())
+    line = {
+        "metric": METRIC,
+        "value": out["mixed"]["value"],
+        "unit": UNIT,
+        "n_gpus": 1,
+        "steps": steps,
+        "warmup": warm,
+        "ms_per_step": 1e3 * out["mixed"]["seconds"] / steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64+f32 (mixed)",
+        "data": "synthetic",
+        "config": {
+            "workload": "64 four-quadrant Riemann problems, meshes 32^2..192^2, N in {2,3,4}, one batch",
+            "nodes": total_nodes,
+            "timing": "host wall clock around the batched steps (synchronised); alone: CUDA events",
+            "l2": "working set ~%.1f GB > L2" % (out["mixed"]["pool_bytes"] / 1e9),
+        },
+        "batched_mixed": out["mixed"],
+        "batched_fp64": out["fp64"],
+        "alone_fp64_plain": alone["fp64"],
+        "alone_mixed": alone["mixed"],
+        "speedup_batched_mixed_vs_alone_fp64": out["mixed"]["value"] / alone["fp64"]["value"],
+        "rho_L1_rel_err_mixed_vs_fp64": {"max": max(errs), "median": float(np.median(errs))},
+        "fp64_batched_vs_alone_max_abs_diff": fp64_batch_vs_alone,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_serve(args):
+    """Continuous batching: a Poisson stream of solves (Kelvin-Helmholtz, four-quadrant
+    Riemann, isentropic vortex; meshes 16^2..256^2, N 2..5) submitted to the native
+    server at their arrival times, against a one-at-a-time queue on the plain FP64
+    single-solve path fed by the same stream. Latency = completion - arrival."""
+    import threading
+
+    import torch
+
+    from p2de import abi
+    from p2de import solver as S
+    from p2de import workloads as W
+    from p2de.batch import Server
+
+    torch.cuda.set_device(0)
+    rates = [float(r) for r in args.serve_rates.split(",")]
+    lines = []
+    for rate in rates:
+        stream = W.serving_stream(args.serve_requests, rate, seed=5, time_scale=args.serve_time_scale)
+        built = {p: [W.build_case(c, p) for c in stream] for p in ("mixed", "fp64")}
+        # served (mixed precision, continuous batching)
+        sv = Server(hbm_budget_bytes=int(args.serve_budget_gb * 1e9), max_active=args.serve_max_active,
+                    steps_per_tick=args.serve_steps_per_tick, precision="mixed")
+        rids = [None] * len(stream)
+        t_start = time.perf_counter()
+
+        def feeder():
+            for i, (c, bb) in enumerate(zip(stream, built["mixed"])):
+                d = t_start + c.arrival - time.perf_counter()
+                if d > 0:
+                    time.sleep(d)
+                rids[i] = sv.submit(bb[3], bb[4])
+
+        th = threading.Thread(target=feeder)
+        th.start()
+        th.join()
+        served_U, lat = [], []
+        for rid in rids:
+            while sv.wait(rid, 600.0) < Server.DONE:
+                pass
+            info = sv.poll(rid)
+            lat.append(info.latency_s)
+            served_U.append(sv.result(rid))
+        makespan = time.perf_counter() - t_start
+        stats = sv.stats()
+        sv.close()
+        # one-at-a-time plain FP64 queue over the same stream
+        plat, plain_U = [], []
+        t_start = time.perf_counter()
+        busy = 0.0
+        for c, (param, md, bc, desc, U0) in zip(stream, built["fp64"]):
+            now = time.perf_counter() - t_start
+            if now < c.arrival:
+                time.sleep(c.arrival - now)
+            t1 = time.perf_counter()
+            g = S.Solver(param, md, desc)
+            g.set_Uq(U0)
+            tt, n, dtl = c_double(), c_int64(), c_double()
+            g._check(g.lib.p2de_ssp33(g.handle, byref(tt), byref(n), byref(dtl)))
+            plain_U.append(g.get_field(abi.FIELD_UQ))
+            g.close()
+            t2 = time.perf_counter()
+            busy += t2 - t1
+            plat.append(t2 - t_start - c.arrival)
+        plain_makespan = time.perf_counter() - t_start
+        errs = []
+        for c, bb, U, R in zip(stream, built["fp64"], served_U, plain_U):
+            errs.append(W.relative_errors(U, R, W.quadrature_weights(c.N, bb[1].geom))["rho"]["L1"])
+        lines.append({
+            "rate_req_per_s": rate,
+            "requests": len(stream),
+            "served": {"solves_per_s": len(stream) / makespan, "p50_s": float(np.percentile(lat, 50)),
+                       "p99_s": float(np.percentile(lat, 99)), "makespan_s": makespan, "ticks": stats["ticks"],
+                       "busy_s": stats["busy_s"]},
+            "plain_queue": {"solves_per_s": len(stream) / plain_makespan, "p50_s": float(np.percentile(plat, 50)),
+                            "p99_s": float(np.percentile(plat, 99)), "makespan_s": plain_makespan, "busy_s": busy},
+            "rho_L1_rel_err_served_vs_fp64": {"max": max(errs), "median": float(np.median(errs))},
+        })
+    line = {
+        "metric": METRIC,
+        "value": lines[-1]["served"]["solves_per_s"],
+        "unit": "solves/s",
+        "n_gpus": 1,
+        "higher_is_better": True,
+        "dtype": "f64+f32 (mixed)",
+        "data": "synthetic",
+        "config": {
+            "workload": "Poisson stream of 2D Euler solves (KH, four-quadrant Riemann, isentropic vortex), "
+                        "meshes 16^2..256^2, N 2..5",
+            "t_final": f"U[0.05, 0.5] x {args.serve_time_scale}",
+            "hbm_budget_gb": args.serve_budget_gb,
+            "max_active": args.serve_max_active,
+            "steps_per_tick": args.serve_steps_per_tick,
+        },
+        "sweep": lines,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_mixed_report(args):
+    """Mixed precision against all-FP64 on Kelvin-Helmholtz 256^2 to T: L1/Linf per
+    component, total-entropy drift, positivity margin, speedup."""
+    import torch
+
+    from p2de import abi, problems
+    from p2de import solver as S
+    from p2de import workloads as W
+
+    torch.cuda.set_device(0)
+    res = {}
+    for N in [int(x) for x in args.mixed_N.split(",")]:
+        runs = {}
+        for prec in ("fp64", "mixed"):
+            param, ic, bcf = problems.kelvin_helmholtz(N=N, Kx=256, Ky=256, T=args.T, precision=prec)
+            md, bc, desc, U0 = build_descriptor(param, ic, bcf)
+            Wq = W.quadrature_weights(N, md.geom)
+            g = S.Solver(param, md, desc)
+            st = torch.cuda.Stream()
+            g._check(g.lib.p2de_set_stream(g.handle, ctypes.c_void_p(st.cuda_stream)))
+            g.set_Uq(U0)
+            t, steps, dev_s = 0.0, 0, 0.0
+            minr, mine = np.inf, np.inf
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            while t < args.T:
+                e0.record(st)
+                t, n = _advance(g, 200, t)
+                e1.record(st)
+                torch.cuda.synchronize()
+                dev_s += e0.elapsed_time(e1) * 1e-3
+                steps += n
+                r, e = c_double(), c_double()
+                g._check(g.lib.p2de_min_rho_rhoe(g.handle, byref(r), byref(e)))
+                minr, mine = min(minr, r.value), min(mine, e.value)
+                if n == 0:
+                    break
+            mins = np.zeros(6)
+            g._check(g.lib.p2de_stage_minima(g.handle, abi.dptr(mins)))
+            U = g.get_field(abi.FIELD_UQ)
+            g.close()
+            runs[prec] = {"U": U, "t": t, "steps": steps, "seconds": dev_s, "min_rho": minr, "min_rhoe": mine,
+                          "entropy0": W.total_entropy(U0, Wq), "entropyT": W.total_entropy(U, Wq),
+                          "nodes": desc.K * desc.Nq, "last_stage_minima": mins.tolist()}
+        f, m = runs["fp64"], runs["mixed"]
+        res[f"N={N}"] = {
+            "T": args.T,
+            "steps": {"fp64": f["steps"], "mixed": m["steps"]},
+            "errors_mixed_vs_fp64": W.relative_errors(m["U"], f["U"], W.quadrature_weights(N, md.geom)),
+            "entropy_drift_rel": {p: (r["entropyT"] - r["entropy0"]) / abs(r["entropy0"]) for p, r in runs.items()},
+            "min_rho": {p: r["min_rho"] for p, r in runs.items()},
+            "min_rhoe": {p: r["min_rhoe"] for p, r in runs.items()},
+            "dof_stage_per_s": {p: r["nodes"] * 3 * r["steps"] / r["seconds"] for p, r in runs.items()},
+            "speedup_mixed": (m["nodes"] * 3 * m["steps"] / m["seconds"]) / (f["nodes"] * 3 * f["steps"] / f["seconds"]),
+        }
+    print(json.dumps({"metric": METRIC, "unit": UNIT, "workload": "Kelvin-Helmholtz 256x256, mixed vs FP64",
+                      "data": "synthetic", "report": res}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="dmr", choices=["dmr", "kh256"])
+    ap.add_argument("--workload", default="dmr", choices=["dmr", "kh256", "batch64", "serve", "mixed-report"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--serve-rates", default="20,100,500")
+    ap.add_argument("--serve-requests", type=int, default=100)
+    ap.add_argument("--serve-time-scale", type=float, default=0.01)
+    ap.add_argument("--serve-budget-gb", type=float, default=150.0)
+    ap.add_argument("--serve-max-active", type=int, default=64)
+    ap.add_argument("--serve-steps-per-tick", type=int, default=4)
+    ap.add_argument("--mixed-N", default="3,5")
+    ap.add_argument("--T", type=float, default=1.0)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "batch64":
+        return run_batch64(args)
+    if args.workload == "serve":
+        return run_serve(args)
+    if args.workload == "mixed-report":
+        return run_mixed_report(args)
 
     import torch
 
