@@ -63,7 +63,7 @@ __device__ __forceinline__ bool batch_next(const StageArgs* solves, const BatchT
 template <typename TH>
 __global__ void __launch_bounds__(kBatchThreads) k_batch_a(const StageArgs* solves, const BatchTask* tasks,
                                                            const int* ntasks, unsigned* counter, int nstage) {
-  extern __shared__ double sm[];
+  extern __shared__ __align__(16) double sm[];
   __shared__ StageArgs sa;
   __shared__ int s_task;
   BatchTask tk;
@@ -82,7 +82,7 @@ __global__ void __launch_bounds__(kBatchThreads) k_batch_a(const StageArgs* solv
 #ifdef P2DE_BATCH_COMMON_KERNELS
 __global__ void __launch_bounds__(kBatchThreads) k_batch_b(const StageArgs* solves, const BatchTask* tasks,
                                                            const int* ntasks, unsigned* counter, int nstage) {
-  extern __shared__ double sm[];
+  extern __shared__ __align__(16) double sm[];
   __shared__ StageArgs sa;
   __shared__ int s_task;
   BatchTask tk;

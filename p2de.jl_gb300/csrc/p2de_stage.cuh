@@ -15,7 +15,8 @@
 // formulas and association order, with these departures, each within a few units in
 // the last place of the reference's value:
 //  * a quotient by the same denominator is a multiplication by one reciprocal
-//    (1/rho per node, 1/(wq J) per node, 1/J per element, 1/(2a) per quadratic);
+//    (1/rho per node, 1/J per element, 1/(2a) per quadratic; 1/(wq J) is (1/J)(1/wq));
+//  * the entropy log(p / rho^gamma) of the entropy variables is log p - gamma log rho;
 //  * the log mean (compressible_Navier_Stokes.jl:307-321) takes one division: the
 //    branch test |da/aavg| < 1e-4 is made as |da| < 1e-4 |aavg|, then da is divided by
 //    aavg (series branch) or by log(aL) - log(aR);
@@ -73,7 +74,9 @@ struct Cfg {
   static constexpr int O_EV = O_SCR + SCR;         // NEV
   static constexpr int O_L = O_EV + NEV;           // 2 NSF
   static constexpr int O_MISC = O_L + 2 * NSF;     // 4
-  static constexpr int PER_ELEM_A = O_MISC + 4;
+  // even, so that every element's block (and its FP32 float4 vectors) is 16-byte aligned
+  static constexpr int PER_ELEM_A = (O_MISC + 4 + 1) & ~1;
+  static_assert(PER_ELEM_A % 2 == 0 && O_PRIM % 2 == 0, "16-byte alignment of per-element data");
   // plus a block-wide list of bound evaluations that need the quadratic solve
   static constexpr size_t smem_a(int e) { return sizeof(double) * PER_ELEM_A * e + sizeof(int) * (NEV * e + 4); }
   static constexpr size_t SMEM_A = smem_a(E);
@@ -94,15 +97,27 @@ __device__ __forceinline__ long long order_key(double x) {
 }
 
 // wavespeed_estimate (compressible_Navier_Stokes.jl:48-62) with 1/rho given
+// (E - 0.5*(un*un)*rr as one FMA: the factor 0.5 is exact, so the value is unchanged;
+// gamma*(gamma-1) is one constant)
 __device__ __forceinline__ double wavespeed_r(const Gas<double>& g, double rr, double un, double E) {
-  double p = g.gm1 * (E - 0.5 * (un * un) * rr);
-  return fabs(un * rr) + sqrt(g.gamma * p * rr);
+  double pe = fma(-0.5, (un * un) * rr, E);
+  return fabs(un * rr) + sqrt((g.gamma * g.gm1) * pe * rr);
+}
+
+// x == +-0 by its bits (integer pipe instead of the FP64 pipe)
+__device__ __forceinline__ bool is_zero_bits(double x) { return (__double_as_longlong(x) << 1) == 0; }
+
+// min of two values in [0, Inf] (either zero's sign) or NaN, by their magnitude bits: a
+// NaN loses against any number, as with fmin; the result of a zero is +0
+__device__ __forceinline__ double min_nonneg_bits(double a, double b) {
+  long long x = __double_as_longlong(a) & 0x7fffffffffffffffLL, y = __double_as_longlong(b) & 0x7fffffffffffffffLL;
+  return __longlong_as_double(x < y ? x : y);
 }
 
 // fluxes(Dim2) (:175-194) with 1/rho given
 __device__ __forceinline__ void fluxes_r(const Gas<double>& g, const double* U, double rr, double* fx, double* fy) {
   double rho = U[0], rhou = U[1], rhov = U[2], E = U[3];
-  double p = g.gm1 * (E - 0.5 * (rhou * rhou + rhov * rhov) * rr);
+  double p = g.gm1 * fma(-0.5, (rhou * rhou + rhov * rhov) * rr, E);
   double u = rhou * rr, v = rhov * rr;
   double rhouv = rho * u * v;
   double Ep = E + p;
@@ -114,6 +129,21 @@ __device__ __forceinline__ void fluxes_r(const Gas<double>& g, const double* U, 
   fy[1] = rhouv;
   fy[2] = rhov * v + p;
   fy[3] = v * Ep;
+}
+
+// the x (xaxis) or y flux of fluxes_r alone
+__device__ __forceinline__ void flux_axis_r(const Gas<double>& g, const double* U, double rr, bool xaxis, double* f) {
+  double rho = U[0], rhou = U[1], rhov = U[2], E = U[3];
+  double p = g.gm1 * fma(-0.5, (rhou * rhou + rhov * rhov) * rr, E);
+  double u = rhou * rr, v = rhov * rr;
+  double rhouv = rho * u * v;
+  double Ep = E + p;
+  double mn = xaxis ? rhou : rhov, un = xaxis ? u : v;
+  double fn = mn * un + p;
+  f[0] = mn;
+  f[1] = xaxis ? fn : rhouv;
+  f[2] = xaxis ? rhouv : fn;
+  f[3] = un * Ep;
 }
 
 // logmean (compressible_Navier_Stokes.jl:307-321) with one division
@@ -237,6 +267,14 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
     G[9] = sxJ / gs;
     G[10] = syJ / gs;
     G[11] = 1.0 / J;
+    if (sizeof(TH) == 4) {  // FP32 copies for the high-order terms: rxJ, sxJ, ryJ, syJ, 1/J
+      float* Gf = reinterpret_cast<float*>(G + 12);
+      Gf[0] = (float)rxJ;
+      Gf[1] = (float)sxJ;
+      Gf[2] = (float)ryJ;
+      Gf[3] = (float)syJ;
+      Gf[4] = (float)G[11];
+    }
   }
   if (tid == 0) s_list[0] = 0;
   for (int w = tid; w < Ke * Nq * 4; w += bs) {
@@ -254,7 +292,7 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
     const double* U = base + C::O_U + 4 * m;
     double rho = U[0], rhou = U[1], rhov = U[2], E = U[3];
     double rr = 1.0 / rho;
-    double p = g.gm1 * (E - 0.5 * (rhou * rhou + rhov * rhov) * rr);
+    double p = g.gm1 * fma(-0.5, (rhou * rhou + rhov * rhov) * rr, E);
     double u = rhou * rr, v = rhov * rr;
     double* F = base + C::O_FLUX + 8 * m;
     double Ep = E + p;
@@ -270,15 +308,19 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
     Ws[0] = wavespeed_r(g, rr, G[6] * rhou + G[7] * rhov, E);
     Ws[1] = wavespeed_r(g, rr, G[9] * rhou + G[10] * rhov, E);
     if (do_high) {
-      double* Pm = base + C::O_PRIM + 6 * m;
-      double beta = rho / (2.0 * p);
-      Pm[0] = rho;
-      Pm[1] = u;
-      Pm[2] = v;
-      Pm[3] = beta;
       if (sizeof(TH) == 8) {
+        double* Pm = base + C::O_PRIM + 6 * m;
+        double beta = rho / (2.0 * p);
+        Pm[0] = rho;
+        Pm[1] = u;
+        Pm[2] = v;
+        Pm[3] = beta;
         Pm[4] = log(rho);
         Pm[5] = log(beta);
+      } else {
+        // FP32 (rho, u, v, beta) per node, converted once here rather than per pair
+        float rf = (float)rho;
+        reinterpret_cast<float4*>(base + C::O_PRIM)[m] = make_float4(rf, (float)u, (float)v, rf / (2.0f * (float)p));
       }
     }
   }
@@ -303,21 +345,19 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
       const double* Fj = base + C::O_FLUX + 8 * j;
       double* out = base + C::O_SCR + 9 * pp;
       bool visc_x = fabs(S0x) > 1e-10;
-      double tx = 2.0 * S0x, ty = 2.0 * S0y;
+      // 2 S0 * (fi + fj)/2 is S0 * (fi + fj) exactly (power-of-two factors)
       if (!aa || ax == 0) {
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
-          double Fx = 0.5 * (Fi[c] + Fj[c]);
           double vis = visc_x ? lam * (Uj[c] - Ui[c]) : 0.0;
-          out[c] = tx * Fx - vis;
+          out[c] = fma(S0x, Fi[c] + Fj[c], -vis);
         }
       }
       if (!aa || ax == 1) {
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
-          double Fy = 0.5 * (Fi[4 + c] + Fj[4 + c]);
           double vis = visc_x ? 0.0 : lam * (Uj[c] - Ui[c]);
-          out[4 + c] = ty * Fy - vis;
+          out[4 + c] = fma(S0y, Fi[4 + c] + Fj[4 + c], -vis);
         }
       }
       out[8] = lam;
@@ -347,7 +387,7 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
       }
       double* R = base + C::O_RXYL + 8 * m;
 #pragma unroll
-      for (int c = 0; c < 8; ++c) R[c] = 0.0 - Q[c];
+      for (int c = 0; c < 8; ++c) R[c] = -Q[c];
       base[C::O_LAMI + m] = lam;
     }
   }
@@ -424,48 +464,44 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
       wsP = wavespeed_r(g, rrN, n1 * Unb[1] + n2 * Unb[2], Unb[3]);
     }
     double lamB = 0.5 * nn * fmax(ws_own, wsP);
-    double fPx[4], fPy[4];
-    fluxes_r(g, uP, rrP, fPx, fPy);
     const double* Ff = base + C::O_FLUX + 8 * q;
     double* BL = base + C::O_BFL + 8 * f;
     double* BH = base + C::O_BFH + 8 * f;
     bool lf_zero_high = (code == BC_INFLOW || code == BC_OUTFLOW || code == BC_SHOCK);
-#pragma unroll
-    for (int c = 0; c < 4; ++c) {
-      double lf = lamB * (uP[c] - Uf[c]);
-      double fsx = 0.5 * (Ff[c] + fPx[c]);
-      double fsy = 0.5 * (Ff[4 + c] + fPy[c]);
-      double bx = B1 * fsx, by = B2 * fsy;
-      BL[c] = xs ? bx - lf : bx;
-      BL[4 + c] = xs ? by : by - lf;
-      if (lf_zero_high) {
-        double lh = 0.0 * (uP[c] - Uf[c]);
-        BH[c] = xs ? bx - lh : bx;
-        BH[4 + c] = xs ? by : by - lh;
-      } else {
-        BH[c] = BL[c];
-        BH[4 + c] = BL[4 + c];
-      }
-    }
-    if (sizeof(TH) == 4 && do_high) {
-      // mixed precision: the high-order surface term in FP32
-      Gas<float> gf{(float)a.gamma, (float)a.gm1, (float)(2.0 * a.gm1)};
-      float uff[4], uPf[4], ffx[4], ffy[4], fpx[4], fpy[4];
+    // B * (f(U) + f(uP))/2 with the exact factor 1/2 taken into B
+    const double hB1 = 0.5 * B1, hB2 = 0.5 * B2;
+    if (aa) {
+      // sxJ = ryJ = 0: the face's terms have only its own axis' half; the other is zero
+      double fP[4];
+      flux_axis_r(g, uP, rrP, xs, fP);
+      const double hB = xs ? hB1 : hB2;
+      const int o = xs ? 0 : 4;
 #pragma unroll
       for (int c = 0; c < 4; ++c) {
-        uff[c] = (float)Uf[c];
-        uPf[c] = (float)uP[c];
+        double lf = lamB * (uP[c] - Uf[c]);
+        double b = hB * (Ff[o + c] + fP[c]);
+        double bl = b - lf;
+        BL[o + c] = bl;
+        BL[4 - o + c] = 0.0;
+        BH[o + c] = lf_zero_high ? b : bl;
+        BH[4 - o + c] = 0.0;
       }
-      fluxes(gf, uff, ffx, ffy);
-      fluxes(gf, uPf, fpx, fpy);
-      float LFc = lf_zero_high ? 0.0f : (float)lamB;
+    } else {
+      double fPx[4], fPy[4];
+      fluxes_r(g, uP, rrP, fPx, fPy);
 #pragma unroll
       for (int c = 0; c < 4; ++c) {
-        float bx = (float)B1 * (0.5f * (ffx[c] + fpx[c]));
-        float by = (float)B2 * (0.5f * (ffy[c] + fpy[c]));
-        float l = LFc * (uPf[c] - uff[c]);
-        BH[c] = (double)(xs ? bx - l : bx);
-        BH[4 + c] = (double)(xs ? by : by - l);
+        double lf = lamB * (uP[c] - Uf[c]);
+        double bx = hB1 * (Ff[c] + fPx[c]), by = hB2 * (Ff[4 + c] + fPy[c]);
+        BL[c] = xs ? bx - lf : bx;
+        BL[4 + c] = xs ? by : by - lf;
+        if (lf_zero_high) {
+          BH[c] = bx;
+          BH[4 + c] = by;
+        } else {
+          BH[c] = BL[c];
+          BH[4 + c] = BL[4 + c];
+        }
       }
     }
     base[C::O_LAMB + f] = lamB;
@@ -501,7 +537,10 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
         lam += base[C::O_LAMB + fl[t]];
       }
       double wJ = base[C::O_GEO] * op.wq[m];
-      double rwJ = 1.0 / wJ;
+      double rwJ = base[C::O_GEO + 11] * op.rwq[m];  // (1/J)(1/wq)
+      // wJ and 1/wJ for the limiter (the wavespeeds are no longer needed)
+      base[C::O_WS + 2 * m] = wJ;
+      base[C::O_WS + 2 * m + 1] = rwJ;
 #pragma unroll
       for (int c = 0; c < 8; ++c) R[c] = R[c] * rwJ;
       double* rl = base + C::O_RHSL + 4 * m;
@@ -527,6 +566,7 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
 
   // ---- P6: high-order volume pairs (flux_differencing_volume!, :164-211)
   if (do_high) {
+    const Gas<float> gf{(float)a.gamma, (float)a.gm1, (float)(2.0 * a.gm1)};
     for (int w = tid; w < Ke * C::NPH; w += bs) {
       int e = w / C::NPH, pp = w % C::NPH;
       double* base = sm + e * PE;
@@ -547,21 +587,23 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
           for (int c = 0; c < 4; ++c) out[4 + c] = Sxy * Fy[c];
         }
       } else {
-        Gas<float> gf{(float)a.gamma, (float)a.gm1, (float)(2.0 * a.gm1)};
-        const double* Pi = base + C::O_PRIM + 6 * i;
-        const double* Pj = base + C::O_PRIM + 6 * j;
-        float UL[4] = {(float)Pi[0], (float)Pi[1], (float)Pi[2], (float)Pi[3]};
-        float UR[4] = {(float)Pj[0], (float)Pj[1], (float)Pj[2], (float)Pj[3]};
+        const float4* Pf = reinterpret_cast<const float4*>(base + C::O_PRIM);
+        const float4 qi = Pf[i], qj = Pf[j];
+        const float UL[4] = {qi.x, qi.y, qi.z, qi.w};
+        const float UR[4] = {qj.x, qj.y, qj.z, qj.w};
+        const float* Gf = reinterpret_cast<const float*>(G + 12);
+        const float Sf = op.hp_Sf[pp];
+        const float sx = (ax == 0 ? Gf[0] : Gf[1]) * Sf, sy = (ax == 0 ? Gf[2] : Gf[3]) * Sf;
         float Fx[4], Fy[4];
         fS_f32(gf, UL, UR, Fx, Fy);
-        float sx = (float)Sxx, sy = (float)Sxy;
+        float* outf = reinterpret_cast<float*>(base + C::O_SCR) + 8 * pp;
         if (!aa || ax == 0) {
 #pragma unroll
-          for (int c = 0; c < 4; ++c) out[c] = (double)(sx * Fx[c]);
+          for (int c = 0; c < 4; ++c) outf[c] = sx * Fx[c];
         }
         if (!aa || ax == 1) {
 #pragma unroll
-          for (int c = 0; c < 4; ++c) out[4 + c] = (double)(sy * Fy[c]);
+          for (int c = 0; c < 4; ++c) outf[4 + c] = sy * Fy[c];
         }
       }
     }
@@ -612,29 +654,37 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
 #pragma unroll
         for (int c = 0; c < 8; ++c) R[c] = (-(rw * Q[c] + Bs[c])) * rJ;
       } else {
+        const float* sfb = reinterpret_cast<const float*>(base + C::O_SCR);
         float Q[8] = {0, 0, 0, 0, 0, 0, 0, 0};
         for (int t = 0; t < cnt; ++t) {
           int pp = op.hg_pair[m][t];
-          const double* sf = base + C::O_SCR + 8 * pp;
+          const float* sf = sfb + 8 * pp;
           int ax = op.hp_axis[pp];
           float sg = op.hg_sign[m][t] > 0 ? 1.0f : -1.0f;
           if (!aa || ax == 0) {
 #pragma unroll
-            for (int c = 0; c < 4; ++c) Q[c] = Q[c] + sg * (float)sf[c];
+            for (int c = 0; c < 4; ++c) Q[c] = Q[c] + sg * sf[c];
           }
           if (!aa || ax == 1) {
 #pragma unroll
-            for (int c = 4; c < 8; ++c) Q[c] = Q[c] + sg * (float)sf[c];
+            for (int c = 4; c < 8; ++c) Q[c] = Q[c] + sg * sf[c];
           }
         }
-        float rwf = (float)rw;
+        const float rwf = op.rwqf[m];
         float Bs[8] = {0, 0, 0, 0, 0, 0, 0, 0};
         for (int t = 0; t < nf; ++t) {
           const double* BH = base + C::O_BFH + 8 * fl[t];
+          bool xf = fl[t] < 2 * n;
+          if (!aa || xf) {
 #pragma unroll
-          for (int c = 0; c < 8; ++c) Bs[c] = Bs[c] + rwf * (float)BH[c];
+            for (int c = 0; c < 4; ++c) Bs[c] = Bs[c] + rwf * (float)BH[c];
+          }
+          if (!aa || !xf) {
+#pragma unroll
+            for (int c = 4; c < 8; ++c) Bs[c] = Bs[c] + rwf * (float)BH[c];
+          }
         }
-        float rJf = (float)rJ;
+        const float rJf = reinterpret_cast<const float*>(base + C::O_GEO + 12)[4];
 #pragma unroll
         for (int c = 0; c < 8; ++c) R[c] = (double)((-(rwf * Q[c] + Bs[c])) * rJf);
       }
@@ -680,7 +730,7 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
     int e = w / (8 * n), r = w % (8 * n);
     int d = r / (4 * n), l = (r / 4) % n, c = r % 4;
     double* base = sm + e * PE;
-    double J = base[C::O_GEO];
+    const double* wJq = base + C::O_WS;  // wq J per node, 2 apart
     double* fb = base + C::O_SCR;  // [d][HL][face][c]
     double* fH = fb + (d * 2 + 0) * NSF * 4;
     double* fL = fb + (d * 2 + 1) * NSF * 4;
@@ -691,7 +741,7 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
       fL[(0 + (n + 1) * sj) * 4 + c] = lo;
       for (int si = 1; si <= n; ++si) {
         int q = (si - 1) + n * sj;
-        double wJ = op.wq[q] * J;
+        double wJ = wJq[2 * q];
         h = h + wJ * base[C::O_RXYH + 8 * q + c];
         lo = lo + wJ * base[C::O_RXYL + 8 * q + c];
         fH[(si + (n + 1) * sj) * 4 + c] = h;
@@ -704,7 +754,7 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
       fL[(si + n * 0) * 4 + c] = lo;
       for (int sj = 1; sj <= n; ++sj) {
         int q = si + n * (sj - 1);
-        double wJ = op.wq[q] * J;
+        double wJ = wJq[2 * q];
         h = h + wJ * base[C::O_RXYH + 8 * q + 4 + c];
         lo = lo + wJ * base[C::O_RXYL + 8 * q + 4 + c];
         fH[(si + n * sj) * 4 + c] = h;
@@ -721,7 +771,7 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
 #pragma unroll
     for (int c = 0; c < 4; ++c) uL[c] = U[c] + dt_lim * rl[c];
     uL[4] = a.zeta * rhoe_ufun(uL[0], uL[1], uL[2], uL[3]);
-    uL[5] = 1.0 / (op.wq[m] * base[C::O_GEO]);
+    uL[5] = (4.0 * dt_lim) * base[C::O_WS + 2 * m + 1];  // 4 dt / (wq J)
   }
   __syncthreads();
 
@@ -744,8 +794,8 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
     const double* fH = fb + ((d * 2 + 0) * NSF + fi) * 4;
     const double* fL = fb + ((d * 2 + 1) * NSF + fi) * 4;
     const double* uL = base + C::O_PRIM + 6 * m;
-    double s4 = (h == 0 ? -4.0 : 4.0) * dt_lim;
-    double P0 = s4 * (fH[0] - fL[0]) * uL[5];
+    double P0 = (fH[0] - fL[0]) * uL[5];
+    if (h == 0) P0 = -P0;
     base[C::O_EV + r] = density_bound(uL[0], P0, a.zeta * uL[0], Urho);
   }
   __syncthreads();
@@ -754,7 +804,7 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
     int dh = r / Nq, m = r % Nq;
     int ir = m % n, is = m / n;
     const double* ev = sm + e * PE + C::O_EV;
-    if (ev[r] == 0.0) continue;
+    if (is_zero_bits(ev[r])) continue;
     int d = dh >> 1, h = dh & 1;
     // the other evaluation of the same face, if the face is interior
     int partner = -1;
@@ -765,7 +815,7 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
       if (h == 0 && is > 0) partner = 3 * Nq + ir + n * (is - 1);
       if (h == 1 && is + 1 < n) partner = 2 * Nq + ir + n * (is + 1);
     }
-    if (partner >= 0 && ev[partner] == 0.0) continue;
+    if (partner >= 0 && is_zero_bits(ev[partner])) continue;
     int slot = atomicAdd(&s_list[0], 1);
     s_list[1 + slot] = e * NEV + r;
   }
@@ -783,10 +833,12 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
     const double* fH = fb + ((d * 2 + 0) * NSF + fi) * 4;
     const double* fL = fb + ((d * 2 + 1) * NSF + fi) * 4;
     const double* uL = base + C::O_PRIM + 6 * m;
-    double s4 = (h == 0 ? -4.0 : 4.0) * dt_lim;
     double P[4];
 #pragma unroll
-    for (int c = 0; c < 4; ++c) P[c] = s4 * (fH[c] - fL[c]) * uL[5];
+    for (int c = 0; c < 4; ++c) {
+      double t = (fH[c] - fL[c]) * uL[5];
+      P[c] = h == 0 ? -t : t;
+    }
     double l = base[C::O_EV + r];
     l = fmin(l, rhoe_quadratic_solve(uL, P, uL[4], a.ZEROTOL));
     // the second solve of limiting_param_bound_rho_rhoe has Urhoe = Inf and returns 1.0
@@ -804,12 +856,12 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
     double L = 1.0;
     if (d == 0) {
       int si = fi % (n + 1), sj = fi / (n + 1);
-      if (si < n) L = fmin(L, ev[0 * Nq + si + n * sj]);
-      if (si > 0) L = fmin(L, ev[1 * Nq + (si - 1) + n * sj]);
+      if (si < n) L = min_nonneg_bits(L, ev[0 * Nq + si + n * sj]);
+      if (si > 0) L = min_nonneg_bits(L, ev[1 * Nq + (si - 1) + n * sj]);
     } else {
       int si = fi % n, sj = fi / n;
-      if (sj < n) L = fmin(L, ev[2 * Nq + si + n * sj]);
-      if (sj > 0) L = fmin(L, ev[3 * Nq + si + n * (sj - 1)]);
+      if (sj < n) L = min_nonneg_bits(L, ev[2 * Nq + si + n * sj]);
+      if (sj > 0) L = min_nonneg_bits(L, ev[3 * Nq + si + n * (sj - 1)]);
     }
     base[C::O_L + r] = L;
   }
@@ -827,7 +879,7 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
       for (int sj = 0; sj < n; ++sj)
         for (int si = 1; si < n; ++si) {
           double v = d == 0 ? L[si + (n + 1) * sj] : L[sj + n * si];
-          if (v != 0.0) any = true;
+          if (!is_zero_bits(v)) any = true;
         }
       base[C::O_MISC + d] = any ? 1.0 : 0.0;
     }
@@ -840,7 +892,7 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
       if (base[C::O_MISC] == 0.0 && base[C::O_MISC + 1] == 0.0) continue;
       const double* U = base + C::O_U + 4 * m;
       double p = pfun(g, U[0], U[1], U[2], U[3]);
-      double s = log(p / pow(U[0], a.gamma));
+      double s = log(p) - a.gamma * log(U[0]);  // log(p / rho^gamma)
       double rp = 1.0 / p;
       double* vq = base + C::O_FLUX + 4 * m;
       vq[0] = (a.gamma + 1.0 - s) - a.gm1 * U[3] * rp;
@@ -972,7 +1024,7 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
 
 template <int N1D, typename TH>
 __global__ void __launch_bounds__(Cfg<N1D>::THREADS) k_stage_a(StageArgs a) {
-  extern __shared__ double sm[];
+  extern __shared__ __align__(16) double sm[];
   stage_a_body<N1D, TH>(a, blockIdx.x * a.epb, sm);
 }
 
@@ -1144,7 +1196,7 @@ __device__ __forceinline__ void stage_b_body(const StageArgs& a, int k0, double*
 
 template <int N1D>
 __global__ void __launch_bounds__(Cfg<N1D>::THREADS) k_stage_b(StageArgs a) {
-  extern __shared__ double sm[];
+  extern __shared__ __align__(16) double sm[];
   stage_b_body<N1D>(a, blockIdx.x * a.epb, sm);
 }
 

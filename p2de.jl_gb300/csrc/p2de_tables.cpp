@@ -119,6 +119,8 @@ int build_op_table(int N, double zerotol, OpTable* T) {
         ++p;
       }
   T->nph = p;
+  for (int q = 0; q < p; ++q) T->hp_Sf[q] = (float)T->hp_S[q];
+  for (int m = 0; m < Nq; ++m) T->rwqf[m] = (float)T->rwq[m];
   // gather order per node: partners ascending (the order in which the j-outer,
   // i-inner nnz loop of init.jl:188-195 touches the node)
   for (int m = 0; m < Nq; ++m) {

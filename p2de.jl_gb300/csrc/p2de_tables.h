@@ -40,6 +40,9 @@ struct OpTable {
   int8_t lg_sign[kMaxNq][4];
   int8_t lg_count[kMaxNq];
   int8_t hg_count[kMaxNq];
+  // FP32 copies for the mixed-precision high-order terms
+  float hp_Sf[kMaxPairsHi];
+  float rwqf[kMaxNq];
 };
 
 // Builds the table for polynomial degree N (1..5). Returns 0 on success.
