@@ -214,11 +214,19 @@ __device__ __forceinline__ double rhoe_quadratic_solve(const double* U, const do
 // Density part of limiting_param_bound_rho_rhoe (limiter_utils.jl:82-92) for the
 // positivity bounds Lrho = zeta*rhoL and Urho = 0 (the Lphi slot under the reference's
 // destructuring, limiter_utils.jl:66-70) or Inf.
-__device__ __forceinline__ double density_bound(double U0, double P0, double Lrho, double Urho) {
+// With upper0 (Urho = 0), U0 > 0 and U0 + P0 not below Lrho, the factor
+// fmin(1, fmax((0 - U0)/P0, 0)) is 0 for P0 >= +0 and 1 for P0 <= -0 with |P0| < U0/2
+// (the quotient is then above 2), so it is set without the division; hU0 = U0/2.
+__device__ __forceinline__ double density_bound(double U0, double P0, double Lrho, bool upper0, double hU0) {
+  const double Urho = upper0 ? 0.0 : __longlong_as_double(0x7ff0000000000000LL);
   double l = 1.0;
   double up = U0 + P0;
   bool lo = up < Lrho, hi = up > Urho;
   if (lo || hi) {
+    if (!lo && upper0 && __double_as_longlong(U0) > 0) {
+      if (!signbit(P0)) return 0.0;
+      if (-P0 < hU0) return 1.0;
+    }
     double rP = 1.0 / P0;
     if (lo) l = fmax((Lrho - U0) * rP, 0.0);
     if (hi) l = fmin(l, fmax((Urho - U0) * rP, 0.0));
@@ -772,6 +780,9 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
     for (int c = 0; c < 4; ++c) uL[c] = U[c] + dt_lim * rl[c];
     uL[4] = a.zeta * rhoe_ufun(uL[0], uL[1], uL[2], uL[3]);
     uL[5] = (4.0 * dt_lim) * base[C::O_WS + 2 * m + 1];  // 4 dt / (wq J)
+    double* lim = base + C::O_FLUX + 4 * Nq + 2 * m;       // density bound: Lrho, rho/2
+    lim[0] = a.zeta * uL[0];
+    lim[1] = 0.5 * uL[0];
   }
   __syncthreads();
 
@@ -782,7 +793,7 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
   // P[0]); the quadratic internal-energy solve (>= ZEROTOL or 1, never NaN) can only
   // change the face's factor when every density bound of that face is nonzero, so only
   // those evaluations go to a list, solved with all lanes busy.
-  const double Urho = (flags & F_REF_SEM) ? 0.0 : __longlong_as_double(0x7ff0000000000000LL);
+  const bool upper0 = flags & F_REF_SEM;  // Urho = 0 (reference semantics) or Inf
   for (int w = tid; w < Ke * NEV; w += bs) {
     int e = w / NEV, r = w % NEV;
     int dh = r / Nq, m = r % Nq;
@@ -796,7 +807,8 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
     const double* uL = base + C::O_PRIM + 6 * m;
     double P0 = (fH[0] - fL[0]) * uL[5];
     if (h == 0) P0 = -P0;
-    base[C::O_EV + r] = density_bound(uL[0], P0, a.zeta * uL[0], Urho);
+    const double* lim = base + C::O_FLUX + 4 * Nq + 2 * m;
+    base[C::O_EV + r] = density_bound(uL[0], P0, lim[0], upper0, lim[1]);
   }
   __syncthreads();
   for (int w = tid; w < Ke * NEV; w += bs) {
@@ -1051,8 +1063,9 @@ __device__ __forceinline__ void stage_b_body(const StageArgs& a, int k0, double*
   else
     dt = a.scal[S_DT];
   const bool limited = flags & F_DO_LIMIT;
-  // smem: L [2 NSF], fbar [16 NSF], flim [8 NSF]
+  // smem: L [2 NSF], fbar [16 NSF], flim [8 NSF], 1/J
   if (limited) {
+    for (int e = tid; e < Ke; e += bs) sm[e * PE + 26 * NSF] = 1.0 / a.geom[5 * (size_t)(k0 + e)];
     for (int w = tid; w < Ke * 2 * NSF; w += bs) {
       int e = w / (2 * NSF), r = w % (2 * NSF);
       sm[e * PE + r] = a.Lpre[(size_t)(k0 + e) * 2 * NSF + r];
@@ -1101,12 +1114,14 @@ __device__ __forceinline__ void stage_b_body(const StageArgs& a, int k0, double*
       const double* fb = base + 2 * NSF;
       double fH = fb[((d * 2 + 0) * NSF + fi) * 4 + c];
       double fL = fb[((d * 2 + 1) * NSF + fi) * 4 + c];
-      base[2 * NSF + 16 * NSF + (d * NSF + fi) * 4 + c] = l * fH + (1.0 - l) * fL;
+      // l fH + (1 - l) fL as fL + l (fH - fL): one rounding fewer, and exactly fL at l = 0
+      base[2 * NSF + 16 * NSF + (d * NSF + fi) * 4 + c] = fma(l, fH - fL, fL);
     }
     __syncthreads();
   }
   // apply_subcell_limiter!(::Dim2) (subcell.jl:894-924) and the stage combination
-  double rmin = __longlong_as_double(0x7ff0000000000000LL), emin = rmin;
+  // minima as ordered integer keys (integer pipe)
+  long long rmin = order_key(__longlong_as_double(0x7ff0000000000000LL)), emin = rmin;
   for (int w = tid; w < Ke * Nq; w += bs) {
     int e = w / Nq, m = w % Nq;
     const int k = k0 + e;
@@ -1115,7 +1130,7 @@ __device__ __forceinline__ void stage_b_body(const StageArgs& a, int k0, double*
     size_t gidx = ((size_t)k * Nq + m) * 4;
     if (limited) {
       const double* fl = sm + e * PE + 2 * NSF + 16 * NSF;
-      double rwJ = 1.0 / (op.wq[m] * a.geom[5 * (size_t)k]);
+      double rwJ = sm[e * PE + 26 * NSF] * op.rwq[m];  // (1/J)(1/wq)
       const double* fx0 = fl + ((0 * NSF) + ir + (n + 1) * is) * 4;
       const double* fx1 = fl + ((0 * NSF) + ir + 1 + (n + 1) * is) * 4;
       const double* fy0 = fl + ((1 * NSF) + ir + n * is) * 4;
@@ -1161,9 +1176,13 @@ __device__ __forceinline__ void stage_b_body(const StageArgs& a, int k0, double*
 #pragma unroll
       for (int c = 0; c < 4; ++c) a.Uq[gidx + c] = U[c];
       double re = rhoe_ufun(U[0], U[1], U[2], U[3]);
-      rmin = fmin(rmin, U[0]);
-      emin = fmin(emin, re);
-      if (!(U[0] > 0.0) || !(re > 0.0)) atomicOr(a.status, ST_NOT_POSITIVE);
+      long long kr = order_key(U[0]), ke = order_key(re);
+      rmin = kr < rmin ? kr : rmin;
+      emin = ke < emin ? ke : emin;
+      // not (> 0): -0, negative or NaN, i.e. bits <= 0 or above +Inf's
+      if (__double_as_longlong(U[0]) <= 0 || __double_as_longlong(U[0]) > 0x7ff0000000000000LL ||
+          __double_as_longlong(re) <= 0 || __double_as_longlong(re) > 0x7ff0000000000000LL)
+        atomicOr(a.status, ST_NOT_POSITIVE);
     }
   }
   if (limited) {
@@ -1174,12 +1193,13 @@ __device__ __forceinline__ void stage_b_body(const StageArgs& a, int k0, double*
   }
   if (flags & F_UPDATE) {
     for (int o = 16; o > 0; o >>= 1) {
-      rmin = fmin(rmin, __shfl_xor_sync(0xffffffffu, rmin, o));
-      emin = fmin(emin, __shfl_xor_sync(0xffffffffu, emin, o));
+      long long x = __shfl_xor_sync(0xffffffffu, rmin, o), y = __shfl_xor_sync(0xffffffffu, emin, o);
+      rmin = x < rmin ? x : rmin;
+      emin = y < emin ? y : emin;
     }
     if ((tid & 31) == 0) {
-      atomicMin(&a.minrec[2 * s + 0], order_key(rmin));
-      atomicMin(&a.minrec[2 * s + 1], order_key(emin));
+      atomicMin(&a.minrec[2 * s + 0], rmin);
+      atomicMin(&a.minrec[2 * s + 1], emin);
     }
     if (k0 == 0 && tid == 0) {
       if (a.nstage == 1) {
