@@ -546,6 +546,8 @@ def main():
     torch.cuda.set_stream(stream)
     solver._check(lib.p2de_set_stream(solver.handle, ctypes.c_void_p(stream.cuda_stream)))
     solver.set_Uq(U0)
+    epb_default = solver.elements_per_block()[0]
+    epb = epb_default if args.no_autotune else solver.autotune()[0]
 
     def barrier():
         torch.cuda.synchronize()
@@ -637,6 +639,8 @@ def main():
                 "parallelism": f"replicas x{world}" if world > 1 else "single solve",
                 "l2": "working set per step > L2 (stage data ~%.0f MB per launch)" % (bytes_ab["stage_a"] / 1e6),
                 "timing": "CUDA-graph replay of whole steps, CUDA events on the launching stream",
+                "elements_per_block": epb,
+                "elements_per_block_source": "default" if args.no_autotune else f"autotuned (default {epb_default})",
             },
             "e2e": {
                 "value": e2e_value,

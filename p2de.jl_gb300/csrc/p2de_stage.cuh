@@ -54,28 +54,30 @@ struct Cfg {
   static constexpr int NPH = n * n * (n - 1);
   static constexpr int NSF = n * (n + 1);  // subcell faces per direction = Nq + N1D
   static constexpr int NEV = 4 * Nq;       // bound evaluations per element
-  static constexpr int E = (128 / Nq) > 0 ? (128 / Nq) : 1;
+  static constexpr int E = (64 / Nq) > 0 ? (64 / Nq) : 1;  // default elements per block
   static constexpr int THREADS = 128;
   static constexpr int SCR = cmax(cmax(NPL * 9, NPH * 8), 16 * NSF);
-  // shared-memory doubles per element, kernel A
+  // shared-memory doubles per element, kernel A; regions whose lifetimes (phases) do not
+  // overlap share storage
   static constexpr int O_GEO = 0;                  // 16: J, rxJ, sxJ, ryJ, syJ, |gr|, nr, |gs|, ns, 1/J
   static constexpr int O_U = O_GEO + 16;           // 4 Nq
-  static constexpr int O_PRIM = O_U + 4 * Nq;      // 6 Nq (later uL[4], Lrhoe, 1/(wq J))
-  static constexpr int O_FLUX = O_PRIM + 6 * Nq;   // 8 Nq (later vq)
-  static constexpr int O_WS = O_FLUX + 8 * Nq;     // 2 Nq
-  static constexpr int O_RXYL = O_WS + 2 * Nq;     // 8 Nq (later the P vectors, with O_RXYH)
-  static constexpr int O_RXYH = O_RXYL + 8 * Nq;   // 8 Nq
-  static constexpr int O_RHSL = O_RXYH + 8 * Nq;   // 4 Nq
-  static constexpr int O_LAMI = O_RHSL + 4 * Nq;   // Nq
-  static constexpr int O_BFL = O_LAMI + Nq;        // 8 Nfp
-  static constexpr int O_BFH = O_BFL + 8 * Nfp;    // 8 Nfp
-  static constexpr int O_LAMB = O_BFH + 8 * Nfp;   // Nfp
-  static constexpr int O_SCR = O_LAMB + Nfp;       // SCR
-  static constexpr int O_EV = O_SCR + SCR;         // NEV
-  static constexpr int O_L = O_EV + NEV;           // 2 NSF
-  static constexpr int O_MISC = O_L + 2 * NSF;     // 4
+  static constexpr int O_PRIM = O_U + 4 * Nq;      // 6 Nq: primitives (P1-P6); uL[4], Lrhoe, 4dt/(wq J) (P8-P9)
+  static constexpr int O_FLUX = O_PRIM + 6 * Nq;   // 8 Nq: nodal fluxes (P1-P4)
+  static constexpr int O_RXYH = O_FLUX;            //       high-order rhsxy (P7-P8)
+  static constexpr int O_EV = O_FLUX;              //       bound evaluations NEV = 4 Nq (P9-P10), then vq (P11)
+  static constexpr int O_L = O_FLUX + 4 * Nq;      //       subcell factors 2 NSF (P10-P12)
+  static constexpr int O_MISC = O_L + 2 * NSF;     //       4 (P11)
+  static constexpr int O_WS = O_FLUX + 8 * Nq;     // 2 Nq: wavespeeds (P1-P4); wq J, 1/(wq J) (P5-P8)
+  static constexpr int O_RXYL = O_WS + 2 * Nq;     // 8 Nq (P3-P8)
+  static constexpr int O_RHSL = O_RXYL + 8 * Nq;   // 4 Nq (P5-P8); density-bound Lrho, rho/2 (P8-P9)
+  static constexpr int O_LAMI = O_RHSL + 4 * Nq;   // Nq (P3-P5)
+  static constexpr int O_BFL = O_LAMI + Nq;        // 8 Nfp (P4-P8)
+  static constexpr int O_BFH = O_BFL + 8 * Nfp;    // 8 Nfp (P4-P8)
+  static constexpr int O_LAMB = O_BFH + 8 * Nfp;   // Nfp (P4-P5)
+  static constexpr int O_SCR = O_LAMB + Nfp;       // SCR: pair terms (P2-P3, P6-P7), subcell fluxes (P8-P12)
+  static_assert(O_MISC + 4 <= O_WS, "limiter data fit the flux region");
   // even, so that every element's block (and its FP32 float4 vectors) is 16-byte aligned
-  static constexpr int PER_ELEM_A = (O_MISC + 4 + 1) & ~1;
+  static constexpr int PER_ELEM_A = (O_SCR + SCR + 1) & ~1;
   static_assert(PER_ELEM_A % 2 == 0 && O_PRIM % 2 == 0, "16-byte alignment of per-element data");
   // plus a block-wide list of bound evaluations that need the quadratic solve
   static constexpr size_t smem_a(int e) { return sizeof(double) * PER_ELEM_A * e + sizeof(int) * (NEV * e + 4); }
@@ -780,7 +782,7 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
     for (int c = 0; c < 4; ++c) uL[c] = U[c] + dt_lim * rl[c];
     uL[4] = a.zeta * rhoe_ufun(uL[0], uL[1], uL[2], uL[3]);
     uL[5] = (4.0 * dt_lim) * base[C::O_WS + 2 * m + 1];  // 4 dt / (wq J)
-    double* lim = base + C::O_FLUX + 4 * Nq + 2 * m;       // density bound: Lrho, rho/2
+    double* lim = base + C::O_RHSL + 4 * m;  // density bound: Lrho, rho/2 (rl is read above)
     lim[0] = a.zeta * uL[0];
     lim[1] = 0.5 * uL[0];
   }
@@ -807,7 +809,7 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
     const double* uL = base + C::O_PRIM + 6 * m;
     double P0 = (fH[0] - fL[0]) * uL[5];
     if (h == 0) P0 = -P0;
-    const double* lim = base + C::O_FLUX + 4 * Nq + 2 * m;
+    const double* lim = base + C::O_RHSL + 4 * m;
     base[C::O_EV + r] = density_bound(uL[0], P0, lim[0], upper0, lim[1]);
   }
   __syncthreads();
