@@ -106,6 +106,15 @@ __device__ __forceinline__ double wavespeed_r(const Gas<double>& g, double rr, d
   return fabs(un * rr) + sqrt((g.gamma * g.gm1) * pe * rr);
 }
 
+// x with its sign flipped when sign < 0 (integer pipe): q + signed(x, s) is q + s*x for s = +-1
+__device__ __forceinline__ double signed_by(double x, int sign) {
+  return __longlong_as_double(__double_as_longlong(x) ^ (sign < 0 ? (long long)0x8000000000000000ULL : 0LL));
+}
+
+__device__ __forceinline__ float signed_by(float x, int sign) {
+  return __int_as_float(__float_as_int(x) ^ (sign < 0 ? (int)0x80000000u : 0));
+}
+
 // x == +-0 by its bits (integer pipe instead of the FP64 pipe)
 __device__ __forceinline__ bool is_zero_bits(double x) { return (__double_as_longlong(x) << 1) == 0; }
 
@@ -356,14 +365,22 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
       double* out = base + C::O_SCR + 9 * pp;
       bool visc_x = fabs(S0x) > 1e-10;
       // 2 S0 * (fi + fj)/2 is S0 * (fi + fj) exactly (power-of-two factors)
-      if (!aa || ax == 0) {
+      if (aa) {
+        // the pair's terms on the other axis are zero; one instruction stream for both axes
+        const int o = 4 * ax;
+        const double S0 = ax == 0 ? S0x : S0y;
+        const bool vis_on = ax == 0 ? visc_x : !visc_x;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          double vis = vis_on ? lam * (Uj[c] - Ui[c]) : 0.0;
+          out[o + c] = fma(S0, Fi[o + c] + Fj[o + c], -vis);
+        }
+      } else {
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
           double vis = visc_x ? lam * (Uj[c] - Ui[c]) : 0.0;
           out[c] = fma(S0x, Fi[c] + Fj[c], -vis);
         }
-      }
-      if (!aa || ax == 1) {
 #pragma unroll
         for (int c = 0; c < 4; ++c) {
           double vis = visc_x ? 0.0 : lam * (Uj[c] - Ui[c]);
@@ -380,20 +397,28 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
       double Q[8] = {0, 0, 0, 0, 0, 0, 0, 0};
       double lam = 0.0;
       int cnt = op.lg_count[m];
-      for (int t = 0; t < cnt; ++t) {
-        int pp = op.lg_pair[m][t];
-        const double* sf = base + C::O_SCR + 9 * pp;
-        int ax = op.lp_axis[pp];
-        double sg = op.lg_sign[m][t] > 0 ? 1.0 : -1.0;
-        if (!aa || ax == 0) {
+      if (aa) {
+        // r-line pairs feed the x half, s-line pairs the y half, each in the merged order
 #pragma unroll
-          for (int c = 0; c < 4; ++c) Q[c] = Q[c] + sg * sf[c];
-        }
-        if (!aa || ax == 1) {
+        for (int ax = 0; ax < 2; ++ax) {
+          const int ca = op.lga_count[ax][m];
+          for (int t = 0; t < ca; ++t) {
+            const double* sf = base + C::O_SCR + 9 * op.lga_pair[ax][m][t];
+            const int sg = op.lga_sign[ax][m][t];
 #pragma unroll
-          for (int c = 4; c < 8; ++c) Q[c] = Q[c] + sg * sf[c];
+            for (int c = 0; c < 4; ++c) Q[4 * ax + c] = Q[4 * ax + c] + signed_by(sf[4 * ax + c], sg);
+          }
         }
-        lam += sf[8];
+        for (int t = 0; t < cnt; ++t) lam += base[C::O_SCR + 9 * op.lg_pair[m][t] + 8];
+      } else {
+        for (int t = 0; t < cnt; ++t) {
+          int pp = op.lg_pair[m][t];
+          const double* sf = base + C::O_SCR + 9 * pp;
+          const int sg = op.lg_sign[m][t];
+#pragma unroll
+          for (int c = 0; c < 8; ++c) Q[c] = Q[c] + signed_by(sf[c], sg);
+          lam += sf[8];
+        }
       }
       double* R = base + C::O_RXYL + 8 * m;
 #pragma unroll
@@ -533,18 +558,26 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
       if (is == n - 1) fl[nf++] = 3 * n + ir;
       double* R = base + C::O_RXYL + 8 * m;
       double lam = base[C::O_LAMI + m];
-      for (int t = 0; t < nf; ++t) {
-        const double* BL = base + C::O_BFL + 8 * fl[t];
-        bool xf = fl[t] < 2 * n;
-        if (!aa || xf) {
+      if (aa) {
+        // at most one x face (its x half) and one y face (its y half); absent ones add 0
+        const int fx = ir == 0 ? is : (ir == n - 1 ? n + is : -1);
+        const int fy = is == 0 ? 2 * n + ir : (is == n - 1 ? 3 * n + ir : -1);
+        const double* BLx = base + C::O_BFL + 8 * (fx < 0 ? 0 : fx);
+        const double* BLy = base + C::O_BFL + 8 * (fy < 0 ? 0 : fy);
 #pragma unroll
-          for (int c = 0; c < 4; ++c) R[c] = R[c] - BL[c];
+        for (int c = 0; c < 4; ++c) {
+          R[c] = R[c] - (fx < 0 ? 0.0 : BLx[c]);
+          R[4 + c] = R[4 + c] - (fy < 0 ? 0.0 : BLy[4 + c]);
         }
-        if (!aa || !xf) {
+        lam = lam + (fx < 0 ? 0.0 : base[C::O_LAMB + (fx < 0 ? 0 : fx)]);
+        lam = lam + (fy < 0 ? 0.0 : base[C::O_LAMB + (fy < 0 ? 0 : fy)]);
+      } else {
+        for (int t = 0; t < nf; ++t) {
+          const double* BL = base + C::O_BFL + 8 * fl[t];
 #pragma unroll
-          for (int c = 4; c < 8; ++c) R[c] = R[c] - BL[c];
+          for (int c = 0; c < 8; ++c) R[c] = R[c] - BL[c];
+          lam += base[C::O_LAMB + fl[t]];
         }
-        lam += base[C::O_LAMB + fl[t]];
       }
       double wJ = base[C::O_GEO] * op.wq[m];
       double rwJ = base[C::O_GEO + 11] * op.rwq[m];  // (1/J)(1/wq)
@@ -632,66 +665,76 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
       double rw = op.rwq[m];
       double* R = base + C::O_RXYH + 8 * m;
       int cnt = op.hg_count[m];
+      // on axis-aligned elements r-line pairs and x faces feed the x half only, s-line
+      // pairs and y faces the y half (gathers in the merged lists' order)
+      const int fx = ir == 0 ? is : (ir == n - 1 ? n + is : -1);
+      const int fy = is == 0 ? 2 * n + ir : (is == n - 1 ? 3 * n + ir : -1);
       if (sizeof(TH) == 8) {
         double Q[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-        for (int t = 0; t < cnt; ++t) {
-          int pp = op.hg_pair[m][t];
-          const double* sf = base + C::O_SCR + 8 * pp;
-          int ax = op.hp_axis[pp];
-          double sg = op.hg_sign[m][t] > 0 ? 1.0 : -1.0;
-          if (!aa || ax == 0) {
-#pragma unroll
-            for (int c = 0; c < 4; ++c) Q[c] = Q[c] + sg * sf[c];
-          }
-          if (!aa || ax == 1) {
-#pragma unroll
-            for (int c = 4; c < 8; ++c) Q[c] = Q[c] + sg * sf[c];
-          }
-        }
         double Bs[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-        for (int t = 0; t < nf; ++t) {
-          const double* BH = base + C::O_BFH + 8 * fl[t];
-          bool xf = fl[t] < 2 * n;
-          if (!aa || xf) {
+        if (aa) {
 #pragma unroll
-            for (int c = 0; c < 4; ++c) Bs[c] = Bs[c] + rw * BH[c];
+          for (int ax = 0; ax < 2; ++ax)
+            for (int t = 0; t < n - 1; ++t) {
+              const double* sf = base + C::O_SCR + 8 * op.hga_pair[ax][m][t];
+              const int sg = op.hga_sign[ax][m][t];
+#pragma unroll
+              for (int c = 0; c < 4; ++c) Q[4 * ax + c] = Q[4 * ax + c] + signed_by(sf[4 * ax + c], sg);
+            }
+          const double* BHx = base + C::O_BFH + 8 * (fx < 0 ? 0 : fx);
+          const double* BHy = base + C::O_BFH + 8 * (fy < 0 ? 0 : fy);
+#pragma unroll
+          for (int c = 0; c < 4; ++c) {
+            Bs[c] = fx < 0 ? 0.0 : rw * BHx[c];
+            Bs[4 + c] = fy < 0 ? 0.0 : rw * BHy[4 + c];
           }
-          if (!aa || !xf) {
+        } else {
+          for (int t = 0; t < cnt; ++t) {
+            const double* sf = base + C::O_SCR + 8 * op.hg_pair[m][t];
+            const int sg = op.hg_sign[m][t];
 #pragma unroll
-            for (int c = 4; c < 8; ++c) Bs[c] = Bs[c] + rw * BH[c];
+            for (int c = 0; c < 8; ++c) Q[c] = Q[c] + signed_by(sf[c], sg);
+          }
+          for (int t = 0; t < nf; ++t) {
+            const double* BH = base + C::O_BFH + 8 * fl[t];
+#pragma unroll
+            for (int c = 0; c < 8; ++c) Bs[c] = Bs[c] + rw * BH[c];
           }
         }
 #pragma unroll
         for (int c = 0; c < 8; ++c) R[c] = (-(rw * Q[c] + Bs[c])) * rJ;
       } else {
         const float* sfb = reinterpret_cast<const float*>(base + C::O_SCR);
-        float Q[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-        for (int t = 0; t < cnt; ++t) {
-          int pp = op.hg_pair[m][t];
-          const float* sf = sfb + 8 * pp;
-          int ax = op.hp_axis[pp];
-          float sg = op.hg_sign[m][t] > 0 ? 1.0f : -1.0f;
-          if (!aa || ax == 0) {
-#pragma unroll
-            for (int c = 0; c < 4; ++c) Q[c] = Q[c] + sg * sf[c];
-          }
-          if (!aa || ax == 1) {
-#pragma unroll
-            for (int c = 4; c < 8; ++c) Q[c] = Q[c] + sg * sf[c];
-          }
-        }
         const float rwf = op.rwqf[m];
+        float Q[8] = {0, 0, 0, 0, 0, 0, 0, 0};
         float Bs[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-        for (int t = 0; t < nf; ++t) {
-          const double* BH = base + C::O_BFH + 8 * fl[t];
-          bool xf = fl[t] < 2 * n;
-          if (!aa || xf) {
+        if (aa) {
 #pragma unroll
-            for (int c = 0; c < 4; ++c) Bs[c] = Bs[c] + rwf * (float)BH[c];
+          for (int ax = 0; ax < 2; ++ax)
+            for (int t = 0; t < n - 1; ++t) {
+              const float* sf = sfb + 8 * op.hga_pair[ax][m][t];
+              const int sg = op.hga_sign[ax][m][t];
+#pragma unroll
+              for (int c = 0; c < 4; ++c) Q[4 * ax + c] = Q[4 * ax + c] + signed_by(sf[4 * ax + c], sg);
+            }
+          const double* BHx = base + C::O_BFH + 8 * (fx < 0 ? 0 : fx);
+          const double* BHy = base + C::O_BFH + 8 * (fy < 0 ? 0 : fy);
+#pragma unroll
+          for (int c = 0; c < 4; ++c) {
+            Bs[c] = fx < 0 ? 0.0f : rwf * (float)BHx[c];
+            Bs[4 + c] = fy < 0 ? 0.0f : rwf * (float)BHy[4 + c];
           }
-          if (!aa || !xf) {
+        } else {
+          for (int t = 0; t < cnt; ++t) {
+            const float* sf = sfb + 8 * op.hg_pair[m][t];
+            const int sg = op.hg_sign[m][t];
 #pragma unroll
-            for (int c = 4; c < 8; ++c) Bs[c] = Bs[c] + rwf * (float)BH[c];
+            for (int c = 0; c < 8; ++c) Q[c] = Q[c] + signed_by(sf[c], sg);
+          }
+          for (int t = 0; t < nf; ++t) {
+            const double* BH = base + C::O_BFH + 8 * fl[t];
+#pragma unroll
+            for (int c = 0; c < 8; ++c) Bs[c] = Bs[c] + rwf * (float)BH[c];
           }
         }
         const float rJf = reinterpret_cast<const float*>(base + C::O_GEO + 12)[4];

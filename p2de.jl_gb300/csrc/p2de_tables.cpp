@@ -131,10 +131,18 @@ int build_op_table(int N, double zerotol, OpTable* T) {
     }
     std::sort(lst.begin(), lst.end());
     T->hg_count[m] = (int8_t)lst.size();
+    int na[2] = {0, 0};
     for (size_t t = 0; t < lst.size(); ++t) {
-      T->hg_pair[m][t] = (int16_t)lst[t].second;
-      T->hg_sign[m][t] = (T->hp_i[lst[t].second] == m) ? 1 : -1;
+      const int q = lst[t].second;
+      T->hg_pair[m][t] = (int16_t)q;
+      T->hg_sign[m][t] = (T->hp_i[q] == m) ? 1 : -1;
+      const int ax = T->hp_axis[q];
+      if (na[ax] >= n - 1) return 3;
+      T->hga_pair[ax][m][na[ax]] = (int16_t)q;
+      T->hga_sign[ax][m][na[ax]] = T->hg_sign[m][t];
+      ++na[ax];
     }
+    if (na[0] != n - 1 || na[1] != n - 1) return 3;
   }
   // low order: Q01D tridiagonal (init.jl:276-295), Qr0 = kron(M1D, Q01D), Qs0 = kron(Q01D, M1D)
   std::vector<double> Q01(n * n, 0.0);  // row-major
@@ -181,8 +189,15 @@ int build_op_table(int N, double zerotol, OpTable* T) {
     std::sort(lst.begin(), lst.end());
     T->lg_count[m] = (int8_t)lst.size();
     for (size_t t = 0; t < lst.size(); ++t) {
-      T->lg_pair[m][t] = (int16_t)lst[t].second;
-      T->lg_sign[m][t] = (T->lp_i[lst[t].second] == m) ? 1 : -1;
+      const int q = lst[t].second;
+      T->lg_pair[m][t] = (int16_t)q;
+      T->lg_sign[m][t] = (T->lp_i[q] == m) ? 1 : -1;
+      const int ax = T->lp_axis[q];
+      const int c = T->lga_count[ax][m];
+      if (c >= 2) return 3;
+      T->lga_pair[ax][m][c] = (int16_t)q;
+      T->lga_sign[ax][m][c] = T->lg_sign[m][t];
+      T->lga_count[ax][m] = (int8_t)(c + 1);
     }
   }
   return 0;

@@ -43,6 +43,13 @@ struct OpTable {
   // FP32 copies for the mixed-precision high-order terms
   float hp_Sf[kMaxPairsHi];
   float rwqf[kMaxNq];
+  // the gather lists split by axis (r-line partners, s-line partners), each in the
+  // merged lists' order; used where a pair contributes to its own axis only
+  int16_t hga_pair[2][kMaxNq][kMaxN1D - 1];
+  int8_t hga_sign[2][kMaxNq][kMaxN1D - 1];
+  int16_t lga_pair[2][kMaxNq][2];
+  int8_t lga_sign[2][kMaxNq][2];
+  int8_t lga_count[2][kMaxNq];
 };
 
 // Builds the table for polynomial degree N (1..5). Returns 0 on success.
