@@ -268,31 +268,27 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
   const double dt_lim = a.scal[S_DT_LIM];
   const double t_now = a.scal[S_T];
 
-  // ---- P0: geometry and state
-  for (int e = tid; e < Ke; e += bs) {
+  // ---- P0: geometry and state. One item per (element, factor), so that no thread runs
+  //      the whole chain of square roots and divisions: G = J, rxJ, sxJ, ryJ, syJ,
+  //      |gr|, nr (2), |gs|, ns (2), 1/J, then FP32 rxJ, sxJ, ryJ, syJ, 1/J (mixed)
+  constexpr int NG = sizeof(TH) == 4 ? 17 : 12;
+  for (int w = tid; w < Ke * NG; w += bs) {
+    const int e = w / NG, q = w % NG;
     double* G = sm + e * PE + C::O_GEO;
     const double* gg = a.geom + 5 * (size_t)(k0 + e);
-    double J = gg[0], rxJ = gg[1], sxJ = gg[2], ryJ = gg[3], syJ = gg[4];
-    G[0] = J;
-    G[1] = rxJ;
-    G[2] = sxJ;
-    G[3] = ryJ;
-    G[4] = syJ;
-    double gr = sqrt(rxJ * rxJ + ryJ * ryJ), gs = sqrt(sxJ * sxJ + syJ * syJ);
-    G[5] = gr;
-    G[6] = rxJ / gr;
-    G[7] = ryJ / gr;
-    G[8] = gs;
-    G[9] = sxJ / gs;
-    G[10] = syJ / gs;
-    G[11] = 1.0 / J;
-    if (sizeof(TH) == 4) {  // FP32 copies for the high-order terms: rxJ, sxJ, ryJ, syJ, 1/J
+    if (q < 5) {
+      G[q] = gg[q];
+    } else if (q < 11) {
+      const bool r = q < 8;  // r-normal: (rxJ, ryJ); s-normal: (sxJ, syJ)
+      const double g1 = r ? gg[1] : gg[2], g2 = r ? gg[3] : gg[4];
+      const double gn = sqrt(g1 * g1 + g2 * g2);
+      const int j = (q - 5) % 3;
+      G[q] = j == 0 ? gn : (j == 1 ? g1 : g2) / gn;
+    } else if (q == 11) {
+      G[11] = 1.0 / gg[0];
+    } else {
       float* Gf = reinterpret_cast<float*>(G + 12);
-      Gf[0] = (float)rxJ;
-      Gf[1] = (float)sxJ;
-      Gf[2] = (float)ryJ;
-      Gf[3] = (float)syJ;
-      Gf[4] = (float)G[11];
+      Gf[q - 12] = q < 16 ? (float)gg[q - 11] : (float)(1.0 / gg[0]);
     }
   }
   if (tid == 0) s_list[0] = 0;
