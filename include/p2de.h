@@ -62,8 +62,11 @@ typedef enum p2de_surface_flux {
 
 typedef enum p2de_precision {
   P2DE_PRECISION_FP64 = 0, /* everything in FP64 */
-  P2DE_PRECISION_MIXED = 1 /* volume/surface flux differencing in FP32 with FP32
-                              accumulation; low order, limiter, RK in FP64 */
+  P2DE_PRECISION_MIXED = 1, /* volume flux differencing in FP32 with FP32
+                               accumulation; low order, limiter, RK in FP64 */
+  P2DE_PRECISION_MIXED_ACC64 = 2 /* volume two-point fluxes in FP32, their gather and
+                                    lift accumulated in FP64 (a pair's term then cancels
+                                    exactly between its two nodes); the rest as MIXED */
 } p2de_precision;
 
 /* Param (Solver.jl:151-170) flattened; method choices as enums. */

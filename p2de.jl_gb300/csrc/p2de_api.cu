@@ -214,6 +214,7 @@ int flags_for(const p2de_solver* s, int nstage, bool update, bool debug) {
   if (s->axis_aligned) f |= F_AXIS_ALIGNED;
   if (s->prm.reference_semantics) f |= F_REF_SEM;
   if (s->prm.bound_type == P2DE_BOUND_POSITIVITY_AND_CELL_ENTROPY) f |= F_CELL_ENTROPY;
+  if (s->prm.precision == P2DE_PRECISION_MIXED_ACC64) f |= F_ACC64;
   if (update) f |= F_UPDATE;
   if (debug) f |= F_WRITE_DEBUG;
   return f;
@@ -288,7 +289,7 @@ int p2de_initialize_DG(const p2de_param* prm, const p2de_mesh* mesh, int device,
     return fail(nullptr, P2DE_ERR_UNSUPPORTED,
                 "surface fluxes: only LaxFriedrichsOnNodalVal (low order) and LaxFriedrichsOnProjectedVal (high order)");
   if (prm->rhs_type < 0 || prm->rhs_type > 2 || prm->bound_type < 0 || prm->bound_type > 1 || prm->precision < 0 ||
-      prm->precision > 1)
+      prm->precision > 2)
     return fail(nullptr, P2DE_ERR_INVALID_ARGUMENT, "rhs_type/bound_type/precision out of range");
   const int64_t n1 = prm->N + 1, Nfp = 4 * n1, Nq = n1 * n1;
   const int64_t nfk = Nfp * prm->K;
@@ -326,7 +327,7 @@ int p2de_initialize_DG(const p2de_param* prm, const p2de_mesh* mesh, int device,
   s->Nq = (int)Nq;
   s->Nfp = (int)Nfp;
   s->K = prm->K;
-  s->mixed = prm->precision == P2DE_PRECISION_MIXED;
+  s->mixed = prm->precision != P2DE_PRECISION_FP64;
   auto bail = [&](int code) {
     {
       std::lock_guard<std::mutex> lk(g_err_mu);

@@ -19,7 +19,8 @@ enum : int {
   F_UPDATE = 1 << 7,        // stage kernel B applies the SSP-RK3 stage update
   F_RHSU_FROM_L = 1 << 8,   // rhsU = rhsL (LowOrderPositivity)
   F_RHSU_FROM_H = 1 << 9,   // rhsU = rhsH (FluxDiffRHS)
-  F_CFL = 1 << 10           // stage 1: low-order positivity CFL reduction
+  F_CFL = 1 << 10,          // stage 1: low-order positivity CFL reduction
+  F_ACC64 = 1 << 11         // FP32 kernel: pair fluxes gathered and lifted in FP64
 };
 
 // boundary codes per face node

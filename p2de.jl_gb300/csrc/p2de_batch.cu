@@ -152,6 +152,7 @@ struct p2de_batch {
   int device = 0;
   cudaStream_t stream = nullptr;
   bool mixed = false;
+  int precision = 0;
   Pool pool;
   int max_solves = 0;
   std::vector<Slot> slots;
@@ -356,14 +357,15 @@ int build_batch_graph(p2de_batch* b) {
 extern "C" {
 
 int p2de_batch_create(int device, int32_t precision, size_t pool_bytes, int32_t max_solves, p2de_batch** out) {
-  if (!out || max_solves < 1 || pool_bytes == 0 || precision < 0 || precision > 1) return P2DE_ERR_INVALID_ARGUMENT;
+  if (!out || max_solves < 1 || pool_bytes == 0 || precision < 0 || precision > 2) return P2DE_ERR_INVALID_ARGUMENT;
   *out = nullptr;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return P2DE_ERR_NO_DEVICE;
   if (device < 0 || device >= ndev) return P2DE_ERR_INVALID_ARGUMENT;
   p2de_batch* b = new p2de_batch();
   b->device = device;
-  b->mixed = precision == P2DE_PRECISION_MIXED;
+  b->mixed = precision != P2DE_PRECISION_FP64;
+  b->precision = precision;
   b->max_solves = max_solves;
   b->slots.assign(max_solves, Slot{});
   b->active.assign(max_solves, 0);
@@ -487,6 +489,7 @@ int p2de_batch_add(p2de_batch* b, const p2de_param* p, const p2de_mesh* m, const
   if (aa) f |= F_AXIS_ALIGNED;
   if (p->reference_semantics) f |= F_REF_SEM;
   if (p->bound_type == P2DE_BOUND_POSITIVITY_AND_CELL_ENTROPY) f |= F_CELL_ENTROPY;
+  if (b->precision == P2DE_PRECISION_MIXED_ACC64) f |= F_ACC64;
   a.flags = f;
   a.ops = b->d_tables + (n - 2);
   a.Uq = (double*)(base + lay.Uq);

@@ -183,6 +183,7 @@ extern "C" int p2de_rhs_noalloc(const p2de_param* prm, const p2de_device_mesh* m
   if (prm->reference_semantics) f |= F_REF_SEM;
   if (prm->bound_type == P2DE_BOUND_POSITIVITY_AND_CELL_ENTROPY) f |= F_CELL_ENTROPY;
   if (mesh->axis_aligned) f |= F_AXIS_ALIGNED;
+  if (prm->precision == P2DE_PRECISION_MIXED_ACC64) f |= F_ACC64;
   a.flags = f;
   a.ops = (const OpTable*)(scr + H_TABLE);
   a.Uq = const_cast<double*>(Uq);
@@ -220,7 +221,7 @@ extern "C" int p2de_rhs_noalloc(const p2de_param* prm, const p2de_device_mesh* m
   a.minrec = (long long*)(scr + H_MINREC);
   a.status = status;
   a.counters = (unsigned long long*)(scr + H_COUNTERS);
-  if (launch_a(n1d, a, prm->precision == P2DE_PRECISION_MIXED, st) != cudaSuccess) return P2DE_ERR_CUDA;
+  if (launch_a(n1d, a, prm->precision != P2DE_PRECISION_FP64, st) != cudaSuccess) return P2DE_ERR_CUDA;
   if (launch_b(n1d, a, st) != cudaSuccess) return P2DE_ERR_CUDA;
   double dtres = dt;
   int stv = 0;

@@ -604,6 +604,8 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
   __syncthreads();
 
   // ---- P6: high-order volume pairs (flux_differencing_volume!, :164-211)
+  // FP32 kernel with FP64 accumulation of the pair terms
+  const bool acc64 = sizeof(TH) == 4 && (flags & F_ACC64);
   if (do_high) {
     const Gas<float> gf{(float)a.gamma, (float)a.gm1, (float)(2.0 * a.gm1)};
     for (int w = tid; w < Ke * C::NPH; w += bs) {
@@ -635,14 +637,26 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
         const float sx = (ax == 0 ? Gf[0] : Gf[1]) * Sf, sy = (ax == 0 ? Gf[2] : Gf[3]) * Sf;
         float Fx[4], Fy[4];
         fS_f32(gf, UL, UR, Fx, Fy);
-        float* outf = reinterpret_cast<float*>(base + C::O_SCR) + 8 * pp;
-        if (!aa || ax == 0) {
+        if (acc64) {  // the FP32 terms stored as FP64 for an exactly cancelling FP64 gather
+          double* outd = base + C::O_SCR + 8 * pp;
+          if (!aa || ax == 0) {
 #pragma unroll
-          for (int c = 0; c < 4; ++c) outf[c] = sx * Fx[c];
-        }
-        if (!aa || ax == 1) {
+            for (int c = 0; c < 4; ++c) outd[c] = (double)(sx * Fx[c]);
+          }
+          if (!aa || ax == 1) {
 #pragma unroll
-          for (int c = 0; c < 4; ++c) outf[4 + c] = sy * Fy[c];
+            for (int c = 0; c < 4; ++c) outd[4 + c] = (double)(sy * Fy[c]);
+          }
+        } else {
+          float* outf = reinterpret_cast<float*>(base + C::O_SCR) + 8 * pp;
+          if (!aa || ax == 0) {
+#pragma unroll
+            for (int c = 0; c < 4; ++c) outf[c] = sx * Fx[c];
+          }
+          if (!aa || ax == 1) {
+#pragma unroll
+            for (int c = 0; c < 4; ++c) outf[4 + c] = sy * Fy[c];
+          }
         }
       }
     }
@@ -665,7 +679,7 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
       // pairs and y faces the y half (gathers in the merged lists' order)
       const int fx = ir == 0 ? is : (ir == n - 1 ? n + is : -1);
       const int fy = is == 0 ? 2 * n + ir : (is == n - 1 ? 3 * n + ir : -1);
-      if (sizeof(TH) == 8) {
+      if (sizeof(TH) == 8 || acc64) {
         double Q[8] = {0, 0, 0, 0, 0, 0, 0, 0};
         double Bs[8] = {0, 0, 0, 0, 0, 0, 0, 0};
         if (aa) {

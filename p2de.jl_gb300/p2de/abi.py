@@ -42,6 +42,8 @@ FLUX_LF_PROJECTED = 1
 # p2de_precision
 PRECISION_FP64 = 0
 PRECISION_MIXED = 1
+PRECISION_MIXED_ACC64 = 2
+PRECISIONS = {"fp64": PRECISION_FP64, "mixed": PRECISION_MIXED, "mixed-acc64": PRECISION_MIXED_ACC64}
 # p2de_field
 FIELD_UQ = 0
 FIELD_RHSU = 1

@@ -27,7 +27,7 @@ class Batch:
     def __init__(self, pool_bytes: int, max_solves: int = 64, precision: str = "fp64", device: int = 0):
         self.lib = abi.load_library()
         h = c_void_p()
-        st = self.lib.p2de_batch_create(device, 1 if precision == "mixed" else 0, pool_bytes, max_solves, byref(h))
+        st = self.lib.p2de_batch_create(device, abi.PRECISIONS[precision], pool_bytes, max_solves, byref(h))
         abi.check(self.lib, st, None)
         self.h = h
         self.max_solves = max_solves
@@ -126,7 +126,7 @@ class Server:
                  device: int = 0):
         self.lib = abi.load_library()
         h = c_void_p()
-        st = self.lib.p2de_server_create(device, 1 if precision == "mixed" else 0, hbm_budget_bytes, max_active,
+        st = self.lib.p2de_server_create(device, abi.PRECISIONS[precision], hbm_budget_bytes, max_active,
                                          steps_per_tick, byref(h))
         abi.check(self.lib, st, None)
         self.h = h

@@ -99,8 +99,8 @@ def lower_param(param: Param, K: int) -> abi.P2deParam:
             bound = abi.BOUND_POSITIVITY_AND_CELL_ENTROPY
         else:
             raise UnsupportedMethod(f"bound {type(lim.bound).__name__} is not built")
-    if param.precision not in ("fp64", "mixed"):
-        raise UnsupportedMethod("precision must be 'fp64' or 'mixed'")
+    if param.precision not in abi.PRECISIONS:
+        raise UnsupportedMethod("precision must be one of " + ", ".join(abi.PRECISIONS))
     gc, ts, lp = param.global_constants, param.timestepping_param, param.limiting_param
     return abi.P2deParam(
         N=param.N,
@@ -119,7 +119,7 @@ def lower_param(param: Param, K: int) -> abi.P2deParam:
         low_order_surface_flux=abi.FLUX_LF_NODAL,
         high_order_surface_flux=abi.FLUX_LF_PROJECTED,
         reference_semantics=1 if param.reference_semantics else 0,
-        precision=abi.PRECISION_MIXED if param.precision == "mixed" else abi.PRECISION_FP64,
+        precision=abi.PRECISIONS[param.precision],
     )
 
 

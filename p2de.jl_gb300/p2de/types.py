@@ -168,7 +168,8 @@ class PostprocessingParameter:
 class Param:
     """Param (Solver.jl:151-170). reference_semantics and precision select the
     GB300 modes: reference_semantics=True reproduces the bound destructuring of
-    limiter_utils.jl:66-70; precision is "fp64" or "mixed"."""
+    limiter_utils.jl:66-70; precision is "fp64", "mixed" (FP32 flux differencing with FP32
+    accumulation) or "mixed-acc64" (FP32 two-point fluxes, FP64 gather and lift)."""
 
     N: int
     K: tuple[int, int]

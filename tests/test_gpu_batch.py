@@ -45,7 +45,7 @@ def c_run(g):
     return t.value, n.value, dt.value
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "mixed-acc64"])
 def test_batch_members_equal_their_solo_runs(precision):
     cases = mix_cases(precision)
     b = Batch(pool_bytes=2 << 30, max_solves=16, precision=precision)
