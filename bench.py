@@ -46,8 +46,8 @@ UNIT = "DOF-stage updates/s"
 # stage kernel A on this workload from one ncu capture
 # (profiles/k_stage_a_dmr480x120_n3_fp64.md): DRAM traffic per launch
 # (dram__bytes_read.sum + dram__bytes_write.sum) and the FP64 pipe's busy fraction
-KERNEL_A_TRAFFIC_BYTES = 143.9e6
-KERNEL_A_FP64_PIPE_BUSY = 0.796
+KERNEL_A_TRAFFIC_BYTES = 142.2e6
+KERNEL_A_FP64_PIPE_BUSY = 0.857
 
 
 def workload(name: str, precision: str):
@@ -222,7 +222,7 @@ def _advance(solver, nsteps, t):
     return tt.value, n.value
 
 
-def _timed_alone(param, md, desc, U0, warmup, steps):
+def _timed_alone(param, md, desc, U0, warmup, steps, tune=True):
     """One solve alone on the single-solve path: (seconds for `steps` steps after
     `warmup`, final Uq, steps done). Device time by CUDA events on the solver's stream."""
     import torch
@@ -234,6 +234,8 @@ def _timed_alone(param, md, desc, U0, warmup, steps):
     st = torch.cuda.Stream()
     g._check(g.lib.p2de_set_stream(g.handle, ctypes.c_void_p(st.cuda_stream)))
     g.set_Uq(U0)
+    if tune:
+        g.autotune()
     t, _ = _advance(g, warmup, 0.0)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
@@ -259,11 +261,11 @@ def run_batch64(args):
     torch.cuda.set_device(0)
     cases = W.riemann_batch_cases(64, seed=3)
     steps, warm = args.steps, args.warmup
-    built = {p: [W.build_case(c, p) for c in cases] for p in ("mixed", "fp64")}
+    built = {p: [W.build_case(c, p) for c in cases] for p in ("mixed", "mixed-acc64", "fp64")}
     nodes = np.array([c.nodes for c in cases], dtype=np.float64)
     out = {}
     finals = {}
-    for prec in ("mixed", "fp64"):
+    for prec in ("mixed", "mixed-acc64", "fp64"):
         descs = [b[3] for b in built[prec]]
         pool = int(sum(solve_bytes(d) for d in descs) * 1.05) + (64 << 20)
         b = Batch(pool_bytes=pool, max_solves=len(cases), precision=prec)
@@ -291,17 +293,18 @@ def run_batch64(args):
     for prec in ("fp64", "mixed"):
         tot, dof = 0.0, 0.0
         for c, (param, md, bc, desc, U0) in zip(cases, built[prec]):
-            sec, U, n = _timed_alone(param, md, desc, U0, warm, steps)
+            sec, U, n = _timed_alone(param, md, desc, U0, warm, steps, tune=not args.no_autotune)
             tot += sec
             dof += c.nodes * 3 * n
             if prec == "fp64":
                 ref_U.append(U)
         alone[prec] = {"value": dof / tot, "seconds": tot}
     # accuracy of the batched mixed members against the FP64 solves (same steps)
-    errs = []
-    for c, bb, U, R in zip(cases, built["fp64"], finals["mixed"], ref_U):
+    errs, errs64 = [], []
+    for c, bb, U, U64, R in zip(cases, built["fp64"], finals["mixed"], finals["mixed-acc64"], ref_U):
         Wq = W.quadrature_weights(c.N, bb[1].geom)
         errs.append(W.relative_errors(U, R, Wq)["rho"]["L1"])
+        errs64.append(W.relative_errors(U64, R, Wq)["rho"]["L1"])
     fp64_batch_vs_alone = max(float(np.max(np.abs(U - R))) for U, R in zip(finals["fp64"], ref_U))
     total_nodes = int(nodes.sum())
     line = {
@@ -324,11 +327,13 @@ def run_batch64(args):
             "l2": "working set ~%.1f GB > L2" % (out["mixed"]["pool_bytes"] / 1e9),
         },
         "batched_mixed": out["mixed"],
+        "batched_mixed_acc64": out["mixed-acc64"],
         "batched_fp64": out["fp64"],
         "alone_fp64_plain": alone["fp64"],
         "alone_mixed": alone["mixed"],
         "speedup_batched_mixed_vs_alone_fp64": out["mixed"]["value"] / alone["fp64"]["value"],
         "rho_L1_rel_err_mixed_vs_fp64": {"max": max(errs), "median": float(np.median(errs))},
+        "rho_L1_rel_err_mixed_acc64_vs_fp64": {"max": max(errs64), "median": float(np.median(errs64))},
         "fp64_batched_vs_alone_max_abs_diff": fp64_batch_vs_alone,
     }
     print(json.dumps(line), flush=True)
@@ -353,15 +358,16 @@ def run_serve(args):
     lines = []
     for rate in rates:
         stream = W.serving_stream(args.serve_requests, rate, seed=5, time_scale=args.serve_time_scale)
-        built = {p: [W.build_case(c, p) for c in stream] for p in ("mixed", "fp64")}
-        # served (mixed precision, continuous batching)
+        sp = args.serve_precision
+        built = {p: [W.build_case(c, p) for c in stream] for p in (sp, "fp64")}
+        # served (continuous batching)
         sv = Server(hbm_budget_bytes=int(args.serve_budget_gb * 1e9), max_active=args.serve_max_active,
-                    steps_per_tick=args.serve_steps_per_tick, precision="mixed")
+                    steps_per_tick=args.serve_steps_per_tick, precision=sp)
         rids = [None] * len(stream)
         t_start = time.perf_counter()
 
         def feeder():
-            for i, (c, bb) in enumerate(zip(stream, built["mixed"])):
+            for i, (c, bb) in enumerate(zip(stream, built[sp])):
                 d = t_start + c.arrival - time.perf_counter()
                 if d > 0:
                     time.sleep(d)
@@ -418,7 +424,7 @@ def run_serve(args):
         "unit": "solves/s",
         "n_gpus": 1,
         "higher_is_better": True,
-        "dtype": "f64+f32 (mixed)",
+        "dtype": f"f64+f32 ({args.serve_precision})",
         "data": "synthetic",
         "config": {
             "workload": "Poisson stream of 2D Euler solves (KH, four-quadrant Riemann, isentropic vortex), "
@@ -446,7 +452,7 @@ def run_mixed_report(args):
     res = {}
     for N in [int(x) for x in args.mixed_N.split(",")]:
         runs = {}
-        for prec in ("fp64", "mixed"):
+        for prec in ("fp64", "mixed", "mixed-acc64"):
             param, ic, bcf = problems.kelvin_helmholtz(N=N, Kx=256, Ky=256, T=args.T, precision=prec)
             md, bc, desc, U0 = build_descriptor(param, ic, bcf)
             Wq = W.quadrature_weights(N, md.geom)
@@ -454,6 +460,8 @@ def run_mixed_report(args):
             st = torch.cuda.Stream()
             g._check(g.lib.p2de_set_stream(g.handle, ctypes.c_void_p(st.cuda_stream)))
             g.set_Uq(U0)
+            if not args.no_autotune:
+                g.autotune()
             t, steps, dev_s = 0.0, 0, 0.0
             minr, mine = np.inf, np.inf
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -476,16 +484,18 @@ def run_mixed_report(args):
             runs[prec] = {"U": U, "t": t, "steps": steps, "seconds": dev_s, "min_rho": minr, "min_rhoe": mine,
                           "entropy0": W.total_entropy(U0, Wq), "entropyT": W.total_entropy(U, Wq),
                           "nodes": desc.K * desc.Nq, "last_stage_minima": mins.tolist()}
-        f, m = runs["fp64"], runs["mixed"]
+        f, m, m64 = runs["fp64"], runs["mixed"], runs["mixed-acc64"]
         res[f"N={N}"] = {
             "T": args.T,
-            "steps": {"fp64": f["steps"], "mixed": m["steps"]},
+            "steps": {p: r["steps"] for p, r in runs.items()},
             "errors_mixed_vs_fp64": W.relative_errors(m["U"], f["U"], W.quadrature_weights(N, md.geom)),
+            "errors_mixed_acc64_vs_fp64": W.relative_errors(m64["U"], f["U"], W.quadrature_weights(N, md.geom)),
             "entropy_drift_rel": {p: (r["entropyT"] - r["entropy0"]) / abs(r["entropy0"]) for p, r in runs.items()},
             "min_rho": {p: r["min_rho"] for p, r in runs.items()},
             "min_rhoe": {p: r["min_rhoe"] for p, r in runs.items()},
             "dof_stage_per_s": {p: r["nodes"] * 3 * r["steps"] / r["seconds"] for p, r in runs.items()},
             "speedup_mixed": (m["nodes"] * 3 * m["steps"] / m["seconds"]) / (f["nodes"] * 3 * f["steps"] / f["seconds"]),
+            "speedup_mixed_acc64": (m64["nodes"] * 3 * m64["steps"] / m64["seconds"]) / (f["nodes"] * 3 * f["steps"] / f["seconds"]),
         }
     print(json.dumps({"metric": METRIC, "unit": UNIT, "workload": "Kelvin-Helmholtz 256x256, mixed vs FP64",
                       "data": "synthetic", "report": res}), flush=True)
@@ -498,7 +508,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="dmr", choices=["dmr", "kh256", "batch64", "serve", "mixed-report"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed", "mixed-acc64"])
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
@@ -508,6 +518,7 @@ def main():
     ap.add_argument("--serve-budget-gb", type=float, default=150.0)
     ap.add_argument("--serve-max-active", type=int, default=64)
     ap.add_argument("--serve-steps-per-tick", type=int, default=4)
+    ap.add_argument("--serve-precision", default="mixed-acc64", choices=["fp64", "mixed", "mixed-acc64"])
     ap.add_argument("--mixed-N", default="3,5")
     ap.add_argument("--T", type=float, default=1.0)
     args = ap.parse_args()
@@ -629,7 +640,7 @@ def main():
             "higher_is_better": True,
             "scaling": "weak",
             "vs_baseline": None,
-            "dtype": "f64" if args.precision == "fp64" else "f64+f32 (mixed)",
+            "dtype": "f64" if args.precision == "fp64" else f"f64+f32 ({args.precision})",
             "data": "synthetic",
             "config": {
                 "workload": wdesc,
