@@ -17,9 +17,10 @@
 //  * a quotient by the same denominator is a multiplication by one reciprocal
 //    (1/rho per node, 1/J per element, 1/(2a) per quadratic; 1/(wq J) is (1/J)(1/wq));
 //  * the entropy log(p / rho^gamma) of the entropy variables is log p - gamma log rho;
-//  * the log mean (compressible_Navier_Stokes.jl:307-321) takes one division: the
+//  * the log mean (compressible_Navier_Stokes.jl:307-321) takes one quotient: the
 //    branch test |da/aavg| < 1e-4 is made as |da| < 1e-4 |aavg|, then da is divided by
-//    aavg (series branch) or by log(aL) - log(aR);
+//    aavg (series branch) or by log(aL) - log(aR); the two log means of a two-point
+//    flux share one reciprocal for their quotients;
 //  * pa and rholog/(2(gamma-1) betalog) of fS share one reciprocal;
 //  * min/max are fmin/fmax, which differ from Julia's min/max only for NaN operands
 //    (a NaN state is reported through the status word instead);
@@ -157,24 +158,26 @@ __device__ __forceinline__ void flux_axis_r(const Gas<double>& g, const double* 
   f[3] = un * Ep;
 }
 
-// logmean (compressible_Navier_Stokes.jl:307-321) with one division
-__device__ __forceinline__ double logmean_1div(double aL, double aR, double logL, double logR) {
-  double da = aR - aL;
-  double aavg = 0.5 * (aR + aL);
-  bool series = fabs(da) < 1e-4 * fabs(aavg);
-  double x = da / (series ? aavg : (logL - logR));
-  if (series) {
-    double v = x * x;
-    return aavg * (1.0 + v * (-0.2 - v * (0.0512 - v * 0.026038857142857)));
-  }
-  return -x;
+// logmean (compressible_Navier_Stokes.jl:307-321), series branch, for x = da/aavg
+__device__ __forceinline__ double logmean_series(double aavg, double x) {
+  double v = x * x;
+  return aavg * (1.0 + v * (-0.2 - v * (0.0512 - v * 0.026038857142857)));
 }
 
-// fS(Dim2) (:220-249); UL/UR = (rho, u, v, beta, log rho, log beta)
+// fS(Dim2) (:220-249); UL/UR = (rho, u, v, beta, log rho, log beta). The quotients of
+// the two log means (logmean_1div) share one reciprocal: da_r/den_r = da_r den_b/(den_r den_b).
 __device__ __forceinline__ void fS_fast(const Gas<double>& g, const double* UL, const double* UR, double* Fx,
                                         double* Fy) {
-  double rholog = logmean_1div(UL[0], UR[0], UL[4], UR[4]);
-  double betalog = logmean_1div(UL[3], UR[3], UL[5], UR[5]);
+  const double da_r = UR[0] - UL[0], av_r = 0.5 * (UR[0] + UL[0]);
+  const bool ser_r = fabs(da_r) < 1e-4 * fabs(av_r);
+  const double den_r = ser_r ? av_r : (UL[4] - UR[4]);
+  const double da_b = UR[3] - UL[3], av_b = 0.5 * (UR[3] + UL[3]);
+  const bool ser_b = fabs(da_b) < 1e-4 * fabs(av_b);
+  const double den_b = ser_b ? av_b : (UL[5] - UR[5]);
+  const double rd = 1.0 / (den_r * den_b);
+  const double x_r = da_r * (den_b * rd), x_b = da_b * (den_r * rd);
+  double rholog = ser_r ? logmean_series(av_r, x_r) : -x_r;
+  double betalog = ser_b ? logmean_series(av_b, x_b) : -x_b;
   double rhoavg = 0.5 * (UL[0] + UR[0]);
   double uavg = 0.5 * (UL[1] + UR[1]);
   double vavg = 0.5 * (UL[2] + UR[2]);
