@@ -93,6 +93,9 @@ struct Cfg {
   static constexpr int FBAR = 16 * NSF;  // per element: [dir][H/L][face][c]
 };
 
+// 1/x correctly rounded (the same value as 1.0 / x)
+__device__ __forceinline__ double rcp(double x) { return __drcp_rn(x); }
+
 // ordered 64-bit key of a double (monotone for non-NaN values), for atomicMin
 __device__ __forceinline__ long long order_key(double x) {
   long long b = __double_as_longlong(x);
@@ -174,7 +177,7 @@ __device__ __forceinline__ void fS_fast(const Gas<double>& g, const double* UL, 
   const double da_b = UR[3] - UL[3], av_b = 0.5 * (UR[3] + UL[3]);
   const bool ser_b = fabs(da_b) < 1e-4 * fabs(av_b);
   const double den_b = ser_b ? av_b : (UL[5] - UR[5]);
-  const double rd = 1.0 / (den_r * den_b);
+  const double rd = rcp(den_r * den_b);
   const double x_r = da_r * (den_b * rd), x_b = da_b * (den_r * rd);
   double rholog = ser_r ? logmean_series(av_r, x_r) : -x_r;
   double betalog = ser_b ? logmean_series(av_b, x_b) : -x_b;
@@ -184,7 +187,7 @@ __device__ __forceinline__ void fS_fast(const Gas<double>& g, const double* UL, 
   double unorm = UL[1] * UR[1] + UL[2] * UR[2];
   double d1 = UL[3] + UR[3];
   double d2 = g.two_gm1 * betalog;
-  double r12 = 1.0 / (d1 * d2);
+  double r12 = rcp(d1 * d2);
   double pa = rhoavg * d2 * r12;
   double f4aux = rholog * d1 * r12 + pa + 0.5 * rholog * unorm;
   double FxS1 = rholog * uavg;
@@ -211,7 +214,7 @@ __device__ __forceinline__ double rhoe_quadratic_solve(const double* U, const do
   double disc = b * b - 4.0 * a * c;
   if (disc >= 0.0) {
     double sq = sqrt(disc);
-    double r2a = 1.0 / (2.0 * a);
+    double r2a = rcp(2.0 * a);
     double r1 = (-b + sq) * r2a;
     double r2 = (-b - sq) * r2a;
     if (r1 > ZEROTOL && r2 > ZEROTOL) {
@@ -241,7 +244,7 @@ __device__ __forceinline__ double density_bound(double U0, double P0, double Lrh
       if (!signbit(P0)) return 0.0;
       if (-P0 < hU0) return 1.0;
     }
-    double rP = 1.0 / P0;
+    double rP = rcp(P0);
     if (lo) l = fmax((Lrho - U0) * rP, 0.0);
     if (hi) l = fmin(l, fmax((Urho - U0) * rP, 0.0));
   }
@@ -288,10 +291,10 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
       const int j = (q - 5) % 3;
       G[q] = j == 0 ? gn : (j == 1 ? g1 : g2) / gn;
     } else if (q == 11) {
-      G[11] = 1.0 / gg[0];
+      G[11] = rcp(gg[0]);
     } else {
       float* Gf = reinterpret_cast<float*>(G + 12);
-      Gf[q - 12] = q < 16 ? (float)gg[q - 11] : (float)(1.0 / gg[0]);
+      Gf[q - 12] = q < 16 ? (float)gg[q - 11] : (float)rcp(gg[0]);
     }
   }
   if (tid == 0) s_list[0] = 0;
@@ -309,7 +312,7 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
     const double* G = base + C::O_GEO;
     const double* U = base + C::O_U + 4 * m;
     double rho = U[0], rhou = U[1], rhov = U[2], E = U[3];
-    double rr = 1.0 / rho;
+    double rr = rcp(rho);
     double p = g.gm1 * fma(-0.5, (rhou * rhou + rhov * rhov) * rr, E);
     double u = rhou * rr, v = rhov * rr;
     double* F = base + C::O_FLUX + 8 * m;
@@ -328,7 +331,7 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
     if (do_high) {
       if (sizeof(TH) == 8) {
         double* Pm = base + C::O_PRIM + 6 * m;
-        double beta = rho / (2.0 * p);
+        double beta = rho * rcp(2.0 * p);
         Pm[0] = rho;
         Pm[1] = u;
         Pm[2] = v;
@@ -491,10 +494,10 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
 #pragma unroll
       for (int c = 0; c < 4; ++c) uP[c] = post ? a.shock_post[c] : a.shock_pre[c];
     }
-    double rrP = 1.0 / uP[0];
+    double rrP = rcp(uP[0]);
     double wsP = ws_own;
     if (!self) {
-      double rrN = (code == BC_INTERIOR) ? rrP : 1.0 / Unb[0];
+      double rrN = (code == BC_INTERIOR) ? rrP : rcp(Unb[0]);
       wsP = wavespeed_r(g, rrN, n1 * Unb[1] + n2 * Unb[2], Unb[3]);
     }
     double lamB = 0.5 * nn * fmax(ws_own, wsP);
@@ -589,7 +592,7 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
 #pragma unroll
       for (int c = 0; c < 4; ++c) rl[c] = R[c] + R[4 + c];
       if (flags & F_CFL) {
-        double d = a.CFL * 0.5 * wJ / lam;
+        double d = a.CFL * 0.5 * wJ * rcp(lam);
         if (isnan(d)) nan_seen = true;
         dt_loc = fmin(dt_loc, d);
       }
@@ -836,7 +839,7 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
     double* uL = base + C::O_PRIM + 6 * m;
 #pragma unroll
     for (int c = 0; c < 4; ++c) uL[c] = U[c] + dt_lim * rl[c];
-    uL[4] = a.zeta * rhoe_ufun(uL[0], uL[1], uL[2], uL[3]);
+    uL[4] = a.zeta * fma(-0.5, (uL[1] * uL[1] + uL[2] * uL[2]) * rcp(uL[0]), uL[3]);  // zeta rhoe_ufun(uL)
     uL[5] = (4.0 * dt_lim) * base[C::O_WS + 2 * m + 1];  // 4 dt / (wq J)
     double* lim = base + C::O_RHSL + 4 * m;  // density bound: Lrho, rho/2 (rl is read above)
     lim[0] = a.zeta * uL[0];
@@ -1123,7 +1126,7 @@ __device__ __forceinline__ void stage_b_body(const StageArgs& a, int k0, double*
   const bool limited = flags & F_DO_LIMIT;
   // smem: L [2 NSF], fbar [16 NSF], flim [8 NSF], 1/J
   if (limited) {
-    for (int e = tid; e < Ke; e += bs) sm[e * PE + 26 * NSF] = 1.0 / a.geom[5 * (size_t)(k0 + e)];
+    for (int e = tid; e < Ke; e += bs) sm[e * PE + 26 * NSF] = rcp(a.geom[5 * (size_t)(k0 + e)]);
     for (int w = tid; w < Ke * 2 * NSF; w += bs) {
       int e = w / (2 * NSF), r = w % (2 * NSF);
       sm[e * PE + r] = a.Lpre[(size_t)(k0 + e) * 2 * NSF + r];
@@ -1233,7 +1236,7 @@ __device__ __forceinline__ void stage_b_body(const StageArgs& a, int k0, double*
       }
 #pragma unroll
       for (int c = 0; c < 4; ++c) a.Uq[gidx + c] = U[c];
-      double re = rhoe_ufun(U[0], U[1], U[2], U[3]);
+      double re = fma(-0.5, (U[1] * U[1] + U[2] * U[2]) * rcp(U[0]), U[3]);  // rhoe_ufun(U)
       long long kr = order_key(U[0]), ke = order_key(re);
       rmin = kr < rmin ? kr : rmin;
       emin = ke < emin ? ke : emin;
