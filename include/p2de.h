@@ -186,6 +186,16 @@ int p2de_launch_count(p2de_solver* s, int64_t* count);
 /* Min density and min internal energy over all nodes of Uq (device reduction). */
 int p2de_min_rho_rhoe(p2de_solver* s, double* min_rho, double* min_rhoe);
 
+/* check_conservation (src/dg/utils.jl:1-12) on the device: totals[c] = sum over elements
+ * and nodes of J wq Uq[c]; *sum = the four summed (the reference's return value). Either
+ * output may be NULL. Deterministic: fixed grid and reduction order. */
+int p2de_check_conservation(p2de_solver* s, double totals[4], double* sum);
+
+/* calculate_error (src/dg/postprocess.jl:1-46) on the device against exact conservative
+ * values at the nodes (host array in the layout of Uq): out = relative L1, L2, Linf
+ * errors summed over the components whose exact Linf norm exceeds 1e-14. */
+int p2de_calculate_error(p2de_solver* s, const double* exact_Uq, double out[3]);
+
 /* Min density and min internal energy of each RK stage of the last step, as
  * recorded by the stage update: out[2*(stage-1)] = min rho, out[2*(stage-1)+1] = min rhoe. */
 int p2de_stage_minima(p2de_solver* s, double out[6]);

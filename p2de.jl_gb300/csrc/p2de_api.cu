@@ -4,6 +4,7 @@
 
 #include <cmath>
 #include <cstdarg>
+#include <cstddef>
 #include <cstdio>
 #include <algorithm>
 #include <cstring>
@@ -13,6 +14,7 @@
 
 #include "../../include/p2de.h"
 #include "p2de_args.h"
+#include "p2de_diag.h"
 #include "p2de_launch.h"
 #include "p2de_physics.cuh"
 #include "p2de_tables.h"
@@ -160,6 +162,8 @@ struct p2de_solver {
   int* status = nullptr;
   unsigned long long* counters = nullptr;
   OpTable* ops = nullptr;
+  double *diag_partial = nullptr, *diag_out = nullptr, *exact = nullptr;  // diagnostics, on first use
+  int diag_nblocks = 0;
   StageArgs base{};
   int64_t launches = 0;
   cudaGraphExec_t graph = nullptr;
@@ -824,6 +828,73 @@ int p2de_min_rho_rhoe(p2de_solver* s, double* min_rho, double* min_rhoe) {
   CK(cudaStreamSynchronize(s->stream));
   *min_rho = key_to_double(outk[0]);
   *min_rhoe = key_to_double(outk[1]);
+  return P2DE_OK;
+}
+
+namespace {
+
+int diag_prepare(p2de_solver* s, bool exact) {
+  if (!s->diag_partial) {
+    cudaDeviceProp prop;
+    CK(cudaGetDeviceProperties(&prop, s->device));
+    s->diag_nblocks = diag_blocks(prop.multiProcessorCount);
+    CK(dalloc(s, &s->diag_partial, (size_t)24 * s->diag_nblocks));
+    CK(dalloc(s, &s->diag_out, 24));
+  }
+  if (exact && !s->exact) CK(dalloc(s, &s->exact, (size_t)4 * s->Nq * s->K));
+  return P2DE_OK;
+}
+
+const double* device_wq(const p2de_solver* s) {
+  const OpTable* t = s->ops + (s->N1D - 2);  // the tables of N1D = 2..6 in order
+  return reinterpret_cast<const double*>(reinterpret_cast<const char*>(t) + offsetof(OpTable, wq));
+}
+
+}  // namespace
+
+// check_conservation (src/dg/utils.jl:1-12) on the device
+int p2de_check_conservation(p2de_solver* s, double totals[4], double* sum) {
+  if (!s) return P2DE_ERR_INVALID_ARGUMENT;
+  CK(cudaSetDevice(s->device));
+  int rc = diag_prepare(s, false);
+  if (rc != P2DE_OK) return rc;
+  CK(launch_weighted_sum(s->Uq, s->geom, device_wq(s), s->Nq, (long long)s->Nq * s->K, s->diag_nblocks,
+                         s->diag_partial, s->diag_out, s->stream));
+  s->launches += 2;
+  double t[4];
+  CK(cudaMemcpyAsync(t, s->diag_out, sizeof t, cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  if (totals)
+    for (int c = 0; c < 4; ++c) totals[c] = t[c];
+  if (sum) *sum = ((t[0] + t[1]) + t[2]) + t[3];
+  return P2DE_OK;
+}
+
+// calculate_error (src/dg/postprocess.jl:1-46) on the device, against exact conservative
+// values at the nodes (host array in the layout of Uq)
+int p2de_calculate_error(p2de_solver* s, const double* exact_Uq, double out[3]) {
+  if (!s || !exact_Uq || !out) return P2DE_ERR_INVALID_ARGUMENT;
+  CK(cudaSetDevice(s->device));
+  int rc = diag_prepare(s, true);
+  if (rc != P2DE_OK) return rc;
+  const size_t n = (size_t)4 * s->Nq * s->K;
+  CK(cudaMemcpyAsync(s->exact, exact_Uq, sizeof(double) * n, cudaMemcpyHostToDevice, s->stream));
+  CK(launch_error_norms(s->Uq, s->exact, s->geom, device_wq(s), s->Nq, (long long)s->Nq * s->K, s->diag_nblocks,
+                        s->diag_partial, s->diag_out, s->stream));
+  s->launches += 2;
+  double v[24];
+  CK(cudaMemcpyAsync(v, s->diag_out, sizeof v, cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  double L1 = 0.0, L2 = 0.0, Linf = 0.0;
+  for (int c = 0; c < 4; ++c)
+    if (v[20 + c] > 1e-14) {
+      L1 += v[0 + c] / v[12 + c];
+      L2 += std::sqrt(v[4 + c]) / std::sqrt(v[16 + c]);
+      Linf += v[8 + c] / v[20 + c];
+    }
+  out[0] = L1;
+  out[1] = L2;
+  out[2] = Linf;
   return P2DE_OK;
 }
 

@@ -322,41 +322,34 @@ def SSP33_bang(state: State, solver: Solver, state_param: StateParam, snapshots:
 
 
 def check_conservation(state: State, solver: Solver) -> float:
-    """check_conservation (src/dg/utils.jl:1-12): sum of J*wq*Uq over nodes and components."""
-    from .mesh import gll_rule
+    """check_conservation (src/dg/utils.jl:1-12): sum of J*wq*Uq over nodes and
+    components, reduced on the device."""
+    total = c_double()
+    solver._check(solver.lib.p2de_check_conservation(solver.handle, None, byref(total)))
+    return total.value
 
-    _, w = gll_rule(solver.N)
-    n = solver.N1D
-    wq = (w[np.tile(np.arange(n), n)] * w[np.repeat(np.arange(n), n)])
-    U = state.Uq
-    J = solver.md.geom[:, 0]
-    total = np.einsum("k,i,kic->c", J, wq, U)
-    return float(total.sum())
+
+def conservation_totals(solver: Solver) -> np.ndarray:
+    """The four component totals of check_conservation."""
+    out = np.zeros(4)
+    solver._check(solver.lib.p2de_check_conservation(solver.handle, abi.dptr(out), None))
+    return out
+
+
+def exact_nodal_values(solver: Solver, exact_sol, t: float) -> np.ndarray:
+    """exact_solution(::CompressibleIdealGas{Dim2}, ...) (src/dg/postprocess.jl:54-59) at
+    every node: conservative values in the layout of Uq."""
+    from .problems import primitive_to_conservative
+
+    prim = exact_sol(solver.param.equation, solver.md.x, solver.md.y, t)
+    return np.ascontiguousarray(primitive_to_conservative(solver.param.equation, prim), dtype=np.float64)
 
 
 def calculate_error(state: State, solver: Solver, exact_sol) -> ErrorData:
     """calculate_error (src/dg/postprocess.jl:1-46): relative L1/L2/Linf summed over
-    components, against exact_sol(equation, x, y, T) returning (rho, u, v, p)."""
-    from .mesh import gll_rule
-    from .problems import primitive_to_conservative
-
-    _, w = gll_rule(solver.N)
-    n = solver.N1D
-    wq = (w[np.tile(np.arange(n), n)] * w[np.repeat(np.arange(n), n)])
-    U = state.Uq
-    md = solver.md
-    T = solver.param.timestepping_param.T
-    prim = exact_sol(solver.param.equation, md.x, md.y, T)
-    Ue = primitive_to_conservative(solver.param.equation, prim)
-    wJ = (wq[None, :] * md.geom[:, 0:1])[..., None]
-    err = np.abs(Ue - U)
-    L1e, L2e = (wJ * err).sum((0, 1)), (wJ * err**2).sum((0, 1))
-    Linfe = err.max((0, 1))
-    L1x, L2x = (wJ * np.abs(Ue)).sum((0, 1)), (wJ * Ue**2).sum((0, 1))
-    Linfx = np.abs(Ue).max((0, 1))
-    m = Linfx > 1e-14
-    return ErrorData(
-        float((L1e[m] / L1x[m]).sum()),
-        float((np.sqrt(L2e[m]) / np.sqrt(L2x[m])).sum()),
-        float((Linfe[m] / Linfx[m]).sum()),
-    )
+    components, against exact_sol(equation, x, y, T) returning (rho, u, v, p); the
+    norms are reduced on the device."""
+    Ue = exact_nodal_values(solver, exact_sol, solver.param.timestepping_param.T)
+    out = np.zeros(3)
+    solver._check(solver.lib.p2de_calculate_error(solver.handle, abi.dptr(Ue), abi.dptr(out)))
+    return ErrorData(float(out[0]), float(out[1]), float(out[2]))
