@@ -49,8 +49,12 @@ typedef enum p2de_rhs_type {
 
 /* Subcell limiter bounds (Solver.jl:47-54). */
 typedef enum p2de_bound_type {
-  P2DE_BOUND_POSITIVITY = 0,                 /* PositivityBound */
-  P2DE_BOUND_POSITIVITY_AND_CELL_ENTROPY = 1 /* PositivityAndCellEntropyBound */
+  P2DE_BOUND_POSITIVITY = 0,                  /* PositivityBound */
+  P2DE_BOUND_POSITIVITY_AND_CELL_ENTROPY = 1, /* PositivityAndCellEntropyBound */
+  P2DE_BOUND_TVD = 2,                         /* TVDBound (subcell.jl:112-141): density in the
+                                                 min/max of the low-order density over the
+                                                 node and its low_order_stencil */
+  P2DE_BOUND_TVD_AND_CELL_ENTROPY = 3         /* TVDAndCellEntropyBound */
 } p2de_bound_type;
 
 /* Surface flux types (Solver.jl:19-22). Low order: LaxFriedrichsOnNodalVal only;

@@ -895,6 +895,60 @@ struct Solver {
     return limiting_param_bound_rho_rhoe(UL, P, bv[0], bv[1], bv[3], bv[4]);
   }
 
+  bool tvd() const { return prm.bound_type == P2DE_BOUND_TVD || prm.bound_type == P2DE_BOUND_TVD_AND_CELL_ENTROPY; }
+  bool cell_entropy() const {
+    return prm.bound_type == P2DE_BOUND_POSITIVITY_AND_CELL_ENTROPY || prm.bound_type == P2DE_BOUND_TVD_AND_CELL_ENTROPY;
+  }
+
+  // quad_index_to_quad_index_P(::Dim2) (limiter_utils.jl:199-212): the volume node across
+  // the face of boundary node q in `direction` (1: r, 2: s); q2fq lists the r-face first
+  int quad_index_to_quad_index_P(int q, int k, int direction, int& kP) const {
+    const int ir = q % N1D, is = q / N1D;
+    int faces[2], nf = 0;
+    if (ir == 0) faces[nf++] = is;
+    if (ir == N) faces[nf++] = N1D + is;
+    if (is == 0) faces[nf++] = 2 * N1D + ir;
+    if (is == N) faces[nf++] = 3 * N1D + ir;
+    const int iface = nf == 1 ? faces[0] : faces[direction - 1];
+    int iP;
+    face_of(mapP[iface + (size_t)Nfp * k], iP, kP);
+    return fq2q[iP];
+  }
+
+  // initialize_TVD_bounds!(::Dim2) (subcell.jl:112-141) with low_order_stencil
+  // (limiter_utils.jl:222-231)
+  std::vector<double> rhoL_tvd, lbound_rho, ubound_rho;
+  void initialize_TVD_bounds(double dt) {
+    rhoL_tvd.assign((size_t)Nq * K, 0.0);
+    lbound_rho.assign((size_t)Nq * K, 0.0);
+    ubound_rho.assign((size_t)Nq * K, 0.0);
+#pragma omp parallel for schedule(static)
+    for (int k = 0; k < K; ++k)
+      for (int i = 0; i < Nq; ++i) {
+        size_t ik = i + (size_t)Nq * k;
+        rhoL_tvd[ik] = Uq[ik][0] + dt * rhsL[ik][0];
+      }
+#pragma omp parallel for schedule(static)
+    for (int k = 0; k < K; ++k)
+      for (int j = 0; j < N1D; ++j)
+        for (int i = 0; i < N1D; ++i) {
+          const int q = i + N1D * j;
+          int kk[4], qq[4];
+          if (i - 1 >= 0) { qq[0] = q - 1; kk[0] = k; } else qq[0] = quad_index_to_quad_index_P(q, k, 1, kk[0]);
+          if (i + 1 <= N) { qq[1] = q + 1; kk[1] = k; } else qq[1] = quad_index_to_quad_index_P(q, k, 1, kk[1]);
+          if (j - 1 >= 0) { qq[2] = q - N1D; kk[2] = k; } else qq[2] = quad_index_to_quad_index_P(q, k, 2, kk[2]);
+          if (j + 1 <= N) { qq[3] = q + N1D; kk[3] = k; } else qq[3] = quad_index_to_quad_index_P(q, k, 2, kk[3]);
+          double lb = rhoL_tvd[q + (size_t)Nq * k], ub = lb;
+          for (int s = 0; s < 4; ++s) {
+            double v = rhoL_tvd[qq[s] + (size_t)Nq * kk[s]];
+            lb = jmin(lb, v);
+            ub = jmax(ub, v);
+          }
+          lbound_rho[q + (size_t)Nq * k] = lb;
+          ubound_rho[q + (size_t)Nq * k] = ub;
+        }
+  }
+
   void apply_rhs_limiter(double dt, int nstage) {
     const int s = nstage - 1;
     const int N1Dp1 = N1D + 1;
@@ -902,6 +956,7 @@ struct Solver {
     // initialize_entropy_bounds! -> lbound_s_modified = 0.0 (subcell.jl:4-6)
     const double l_shock = 1.0;
     const double lbound_s = 0.0;
+    if (tvd()) initialize_TVD_bounds(dt);
     // accumulate_f_bar!(::Dim2) (subcell.jl:163-206)
 #pragma omp parallel for schedule(static)
     for (int k = 0; k < K; ++k) {
@@ -953,7 +1008,12 @@ struct Solver {
       auto eval = [&](int q, const V4& dF, double sgn) {
         double wJ = wq[q] * Jq[q + (size_t)Nq * k];
         const V4& u = uL[q];
+        // rho_bound (subcell.jl:352-387): TVD or positivity
         double Lrho = zeta * u[0], Urho = kInf;
+        if (tvd()) {
+          Lrho = lbound_rho[q + (size_t)Nq * k];
+          Urho = ubound_rho[q + (size_t)Nq * k];
+        }
         double bv[5] = {Lrho, zeta * eq.rhoe_ufun(u), lbound_s, Urho, Urhoe};
         V4 P;
         for (int c = 0; c < 4; ++c) P[c] = sgn * 4.0 * dt * dF[c] / wJ;
@@ -987,7 +1047,7 @@ struct Solver {
         for (int d = 0; d < 2; ++d) L_local[LL(i, d, k, s)] = jmin(L_local[LL(i, d, k, s)], l_shock);
     }
     // enforce_ES_subcell! (subcell.jl:462-466) for PositivityAndCellEntropyBound
-    if (prm.bound_type == P2DE_BOUND_POSITIVITY_AND_CELL_ENTROPY) {
+    if (cell_entropy()) {
       initialize_ES_subcell_limiting();
       enforce_ES_subcell_volume(s);
       // enforce_ES_subcell_interface!(::LobattoCollocation) is a no-op (subcell.jl:755-757)

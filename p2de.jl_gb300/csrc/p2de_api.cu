@@ -117,7 +117,7 @@ cudaError_t prepare_n1d(int n1d, StageGeometry* geo) {
   }
   return cudaErrorInvalidValue;
 }
-cudaError_t launch_a_n1d(int n1d, const StageArgs& a, bool mixed, cudaStream_t st) {
+cudaError_t launch_a_one(int n1d, const StageArgs& a, bool mixed, cudaStream_t st) {
   switch (n1d) {
     case 2: return launch_stage_a<2>(a, mixed, st);
     case 3: return launch_stage_a<3>(a, mixed, st);
@@ -126,6 +126,18 @@ cudaError_t launch_a_n1d(int n1d, const StageArgs& a, bool mixed, cudaStream_t s
     case 6: return launch_stage_a<6>(a, mixed, st);
   }
   return cudaErrorInvalidValue;
+}
+// kernel A. The TVD bounds need every element's low-order density: a first launch stops
+// after the low-order RHS and stores them, then the full launch reads its stencils.
+int a_launches(const StageArgs& a) { return (a.flags & F_TVD) ? 2 : 1; }
+cudaError_t launch_a_n1d(int n1d, const StageArgs& a, bool mixed, cudaStream_t st) {
+  if (a.flags & F_TVD) {
+    StageArgs lo = a;
+    lo.flags = (a.flags | F_LOW_ONLY) & ~(F_CFL | F_WRITE_DEBUG);
+    cudaError_t e = launch_a_one(n1d, lo, mixed, st);
+    if (e != cudaSuccess) return e;
+  }
+  return launch_a_one(n1d, a, mixed, st);
 }
 cudaError_t launch_b_n1d(int n1d, const StageArgs& a, cudaStream_t st) {
   switch (n1d) {
@@ -163,6 +175,7 @@ struct p2de_solver {
   unsigned long long* counters = nullptr;
   OpTable* ops = nullptr;
   double *diag_partial = nullptr, *diag_out = nullptr, *exact = nullptr;  // diagnostics, on first use
+  double* rhoL = nullptr;                                                  // TVD bounds only
   int diag_nblocks = 0;
   StageArgs base{};
   int64_t launches = 0;
@@ -217,7 +230,12 @@ int flags_for(const p2de_solver* s, int nstage, bool update, bool debug) {
   if ((f & F_DO_LOW) && nstage == 1) f |= F_CFL;
   if (s->axis_aligned) f |= F_AXIS_ALIGNED;
   if (s->prm.reference_semantics) f |= F_REF_SEM;
-  if (s->prm.bound_type == P2DE_BOUND_POSITIVITY_AND_CELL_ENTROPY) f |= F_CELL_ENTROPY;
+  if (s->prm.bound_type == P2DE_BOUND_POSITIVITY_AND_CELL_ENTROPY ||
+      s->prm.bound_type == P2DE_BOUND_TVD_AND_CELL_ENTROPY)
+    f |= F_CELL_ENTROPY;
+  if ((s->prm.bound_type == P2DE_BOUND_TVD || s->prm.bound_type == P2DE_BOUND_TVD_AND_CELL_ENTROPY) &&
+      (f & F_DO_LIMIT))
+    f |= F_TVD;
   if (s->prm.precision == P2DE_PRECISION_MIXED_ACC64) f |= F_ACC64;
   if (update) f |= F_UPDATE;
   if (debug) f |= F_WRITE_DEBUG;
@@ -244,9 +262,16 @@ int enqueue_step(p2de_solver* s) {
     a.flags = flags_for(s, stage, true, false);
     CK(launch_a_n1d(s->N1D, a, s->mixed, s->stream));
     CK(launch_b_n1d(s->N1D, a, s->stream));
-    s->launches += 2;
+    s->launches += a_launches(a) + 1;
   }
   return P2DE_OK;
+}
+
+// launches of one step: the step begin, then per stage kernel A (twice for TVD bounds), B
+int step_launches(const p2de_solver* s) {
+  StageArgs a = s->base;
+  a.flags = flags_for(s, 2, true, false);
+  return 1 + 3 * (a_launches(a) + 1);
 }
 
 void free_all(p2de_solver* s) {
@@ -292,7 +317,7 @@ int p2de_initialize_DG(const p2de_param* prm, const p2de_mesh* mesh, int device,
       prm->high_order_surface_flux != P2DE_FLUX_LAX_FRIEDRICHS_ON_PROJECTED_VAL)
     return fail(nullptr, P2DE_ERR_UNSUPPORTED,
                 "surface fluxes: only LaxFriedrichsOnNodalVal (low order) and LaxFriedrichsOnProjectedVal (high order)");
-  if (prm->rhs_type < 0 || prm->rhs_type > 2 || prm->bound_type < 0 || prm->bound_type > 1 || prm->precision < 0 ||
+  if (prm->rhs_type < 0 || prm->rhs_type > 2 || prm->bound_type < 0 || prm->bound_type > 3 || prm->precision < 0 ||
       prm->precision > 2)
     return fail(nullptr, P2DE_ERR_INVALID_ARGUMENT, "rhs_type/bound_type/precision out of range");
   const int64_t n1 = prm->N + 1, Nfp = 4 * n1, Nq = n1 * n1;
@@ -472,6 +497,10 @@ int p2de_initialize_DG(const p2de_param* prm, const p2de_mesh* mesh, int device,
   a.minrec = s->minrec;
   a.status = s->status;
   a.counters = s->counters;
+  if (prm->bound_type == P2DE_BOUND_TVD || prm->bound_type == P2DE_BOUND_TVD_AND_CELL_ENTROPY) {
+    if (dalloc(s, &s->rhoL, (size_t)Nq * prm->K) != cudaSuccess) return bail(P2DE_ERR_OUT_OF_MEMORY);
+    a.rhoL = s->rhoL;
+  }
   *out = s;
   return P2DE_OK;
 }
@@ -542,7 +571,7 @@ int p2de_rhs(p2de_solver* s, double t, double dt, int32_t nstage, double* dt_out
   if (!(dinit > 0.0)) a.flags &= ~F_CFL;
   CK(launch_a_n1d(s->N1D, a, s->mixed, s->stream));
   CK(launch_b_n1d(s->N1D, a, s->stream));
-  s->launches += 2;
+  s->launches += a_launches(a) + 1;
   double result = dt;
   if (a.flags & F_CFL) {
     CK(cudaMemcpyAsync(&bits, s->dtmin, 8, cudaMemcpyDeviceToHost, s->stream));
@@ -617,7 +646,7 @@ int p2de_ssp33_advance(p2de_solver* s, int64_t nsteps, double* t, int64_t* steps
   CK(cudaMemcpyAsync(s->scal + S_T, t, sizeof(double), cudaMemcpyHostToDevice, s->stream));
   for (int64_t i = 0; i < nsteps; ++i) {
     CK(cudaGraphLaunch(s->graph, s->stream));
-    s->launches += 7;
+    s->launches += step_launches(s);
   }
   CK(cudaMemcpyAsync(sc, s->scal, sizeof sc, cudaMemcpyDeviceToHost, s->stream));
   CK(cudaStreamSynchronize(s->stream));
@@ -670,7 +699,7 @@ int p2de_profile_steps(p2de_solver* s, int64_t nsteps, double* t, double ms[3]) 
       CK(launch_b_n1d(s->N1D, a, s->stream));
       CK(cudaEventRecord(ev[2 * stage + 1], s->stream));
     }
-    s->launches += 7;
+    s->launches += step_launches(s);
     CK(cudaEventSynchronize(ev[7]));
     float m;
     CK(cudaEventElapsedTime(&m, ev[0], ev[1]));
@@ -751,7 +780,7 @@ int p2de_autotune(p2de_solver* s, int32_t* best_epb, double* best_ms) {
       CK(cudaEventElapsedTime(&ms, e0, e1));
       if (rep > 0) tot += ms;  // first launch warms up
     }
-    s->launches += 4;
+    s->launches += 4 * a_launches(a);
     double ms = tot / 3.0;
     if (ms < bms) {
       bms = ms;

@@ -20,7 +20,9 @@ enum : int {
   F_RHSU_FROM_L = 1 << 8,   // rhsU = rhsL (LowOrderPositivity)
   F_RHSU_FROM_H = 1 << 9,   // rhsU = rhsH (FluxDiffRHS)
   F_CFL = 1 << 10,          // stage 1: low-order positivity CFL reduction
-  F_ACC64 = 1 << 11         // FP32 kernel: pair fluxes gathered and lifted in FP64
+  F_ACC64 = 1 << 11,        // FP32 kernel: pair fluxes gathered and lifted in FP64
+  F_TVD = 1 << 12,          // TVD density bounds from the low-order densities in rhoL
+  F_LOW_ONLY = 1 << 13      // kernel A stops after the low-order RHS and stores rhoL
 };
 
 // boundary codes per face node
@@ -64,6 +66,7 @@ struct StageArgs {
   long long* minrec;  // 3 stages x {min rho, min rhoe} as ordered keys
   int* status;
   unsigned long long* counters;  // [0] quadratic rhoe solves evaluated by the bound phase
+  double* rhoL;  // K x Nq low-order densities U + dt rhsL (TVD bounds only)
 };
 
 }  // namespace p2de

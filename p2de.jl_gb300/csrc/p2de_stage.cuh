@@ -93,6 +93,9 @@ struct Cfg {
   static constexpr int FBAR = 16 * NSF;  // per element: [dir][H/L][face][c]
 };
 
+// U + dt rhsL, the low-order update (one form everywhere, so values agree bitwise)
+__device__ __forceinline__ double low_update(double u, double dt, double r) { return fma(dt, r, u); }
+
 // 1/x correctly rounded (the same value as 1.0 / x)
 __device__ __forceinline__ double rcp(double x) { return __drcp_rn(x); }
 
@@ -231,11 +234,12 @@ __device__ __forceinline__ double rhoe_quadratic_solve(const double* U, const do
 // Density part of limiting_param_bound_rho_rhoe (limiter_utils.jl:82-92) for the
 // positivity bounds Lrho = zeta*rhoL and Urho = 0 (the Lphi slot under the reference's
 // destructuring, limiter_utils.jl:66-70) or Inf.
-// With upper0 (Urho = 0), U0 > 0 and U0 + P0 not below Lrho, the factor
+// Density part of limiting_param_bound_rho_rhoe for [Lrho, Urho]. upper0: Urho = 0 (the
+// Lphi slot under the reference's destructuring). With upper0, U0 > 0 and U0 + P0 not below Lrho, the factor
 // fmin(1, fmax((0 - U0)/P0, 0)) is 0 for P0 >= +0 and 1 for P0 <= -0 with |P0| < U0/2
 // (the quotient is then above 2), so it is set without the division; hU0 = U0/2.
-__device__ __forceinline__ double density_bound(double U0, double P0, double Lrho, bool upper0, double hU0) {
-  const double Urho = upper0 ? 0.0 : __longlong_as_double(0x7ff0000000000000LL);
+__device__ __forceinline__ double density_bound(double U0, double P0, double Lrho, double Urho, bool upper0,
+                                                double hU0) {
   double l = 1.0;
   double up = U0 + P0;
   bool lo = up < Lrho, hi = up > Urho;
@@ -608,6 +612,15 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
     if (nan_seen) atomicOr(a.status, ST_NAN);
   }
   __syncthreads();
+  if (flags & F_LOW_ONLY) {
+    // the low-order densities for the TVD bounds of the next launch (subcell.jl:112-125)
+    for (int w = tid; w < Ke * Nq; w += bs) {
+      int e = w / Nq, m = w % Nq;
+      const double* base = sm + e * PE;
+      a.rhoL[(size_t)(k0 + e) * Nq + m] = low_update(base[C::O_U + 4 * m], dt_lim, base[C::O_RHSL + 4 * m]);
+    }
+    return;
+  }
 
   // ---- P6: high-order volume pairs (flux_differencing_volume!, :164-211)
   // FP32 kernel with FP64 accumulation of the pair terms
@@ -838,11 +851,46 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
     const double* rl = base + C::O_RHSL + 4 * m;
     double* uL = base + C::O_PRIM + 6 * m;
 #pragma unroll
-    for (int c = 0; c < 4; ++c) uL[c] = U[c] + dt_lim * rl[c];
+    for (int c = 0; c < 4; ++c) uL[c] = low_update(U[c], dt_lim, rl[c]);
     uL[4] = a.zeta * fma(-0.5, (uL[1] * uL[1] + uL[2] * uL[2]) * rcp(uL[0]), uL[3]);  // zeta rhoe_ufun(uL)
     uL[5] = (4.0 * dt_lim) * base[C::O_WS + 2 * m + 1];  // 4 dt / (wq J)
-    double* lim = base + C::O_RHSL + 4 * m;  // density bound: Lrho, rho/2 (rl is read above)
-    lim[0] = a.zeta * uL[0];
+    // density bounds (rho_bound, subcell.jl:352-387): Lrho, rho/2, Urho (rl is read above)
+    double* lim = base + C::O_RHSL + 4 * m;
+    if (flags & F_TVD) {
+      // min/max of the low-order density over the node and its low_order_stencil
+      // (limiter_utils.jl:222-231): r-neighbours, then s-neighbours, across a face through
+      // quad_index_to_quad_index_P (:199-212), whose q2fq lists the r-face first
+      const int ir = m % n, is = m / n, k = k0 + e;
+      const double* rl_g = a.rhoL;
+      double lb = rl_g[(size_t)k * Nq + m], ub = lb;
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        const int dir = t >> 1, up = t & 1;  // 0: r, 1: s; lower or upper neighbour
+        const int c = dir == 0 ? ir : is;
+        size_t idx;
+        if (up ? c < n - 1 : c > 0) {
+          idx = (size_t)k * Nq + m + (dir == 0 ? 1 : n) * (up ? 1 : -1);
+        } else {
+          // the face of this node in direction dir (a node on one face has only that one)
+          int f;
+          if (dir == 0 && (ir == 0 || ir == n - 1)) f = ir == 0 ? is : n + is;
+          else if (dir == 1 && (is == 0 || is == n - 1)) f = is == 0 ? 2 * n + ir : 3 * n + ir;
+          else f = ir == 0 ? is : (ir == n - 1 ? n + is : (is == 0 ? 2 * n + ir : 3 * n + ir));
+          const int lin = a.nbr[(size_t)k * Nfp + f];
+          const int kP = lin / Nfp, iP = lin % Nfp, sP = iP / n, tP = iP % n;
+          const int qP = sP == 0 ? n * tP : sP == 1 ? (n - 1) + n * tP : sP == 2 ? tP : tP + n * (n - 1);
+          idx = (size_t)kP * Nq + qP;
+        }
+        const double v = rl_g[idx];
+        lb = fmin(lb, v);
+        ub = fmax(ub, v);
+      }
+      lim[0] = lb;
+      lim[2] = ub;
+    } else {
+      lim[0] = a.zeta * uL[0];
+      lim[2] = __longlong_as_double(0x7ff0000000000000LL);
+    }
     lim[1] = 0.5 * uL[0];
   }
   __syncthreads();
@@ -854,7 +902,9 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
   // P[0]); the quadratic internal-energy solve (>= ZEROTOL or 1, never NaN) can only
   // change the face's factor when every density bound of that face is nonzero, so only
   // those evaluations go to a list, solved with all lanes busy.
-  const bool upper0 = flags & F_REF_SEM;  // Urho = 0 (reference semantics) or Inf
+  // the 5-tuple bound (Lrho, Lrhoe, Lphi = 0, Urho_i, Urhoe = Inf) read as 4 names under
+  // the reference semantics: Urho = 0 and Urhoe = Urho_i (limiter_utils.jl:66-70)
+  const bool upper0 = flags & F_REF_SEM;
   for (int w = tid; w < Ke * NEV; w += bs) {
     int e = w / NEV, r = w % NEV;
     int dh = r / Nq, m = r % Nq;
@@ -869,7 +919,7 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
     double P0 = (fH[0] - fL[0]) * uL[5];
     if (h == 0) P0 = -P0;
     const double* lim = base + C::O_RHSL + 4 * m;
-    base[C::O_EV + r] = density_bound(uL[0], P0, lim[0], upper0, lim[1]);
+    base[C::O_EV + r] = density_bound(uL[0], P0, lim[0], upper0 ? 0.0 : lim[2], upper0, lim[1]);
   }
   __syncthreads();
   for (int w = tid; w < Ke * NEV; w += bs) {
@@ -914,7 +964,10 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
     }
     double l = base[C::O_EV + r];
     l = fmin(l, rhoe_quadratic_solve(uL, P, uL[4], a.ZEROTOL));
-    // the second solve of limiting_param_bound_rho_rhoe has Urhoe = Inf and returns 1.0
+    // the second solve of limiting_param_bound_rho_rhoe: Urhoe = Urho_i (the TVD upper
+    // density bound) under the reference semantics, else Inf, for which it returns 1.0
+    const double Urhoe = upper0 ? base[C::O_RHSL + 4 * m + 2] : __longlong_as_double(0x7ff0000000000000LL);
+    if (upper0 && (flags & F_TVD)) l = fmin(l, rhoe_quadratic_solve(uL, P, Urhoe, a.ZEROTOL));
     base[C::O_EV + r] = fmin(l, 1.0);
   }
   if (a.counters && tid == 0 && nlist) atomicAdd(&a.counters[0], (unsigned long long)nlist);

@@ -36,6 +36,8 @@ RHS_ENTROPY_STABLE = 2
 # p2de_bound_type
 BOUND_POSITIVITY = 0
 BOUND_POSITIVITY_AND_CELL_ENTROPY = 1
+BOUND_TVD = 2
+BOUND_TVD_AND_CELL_ENTROPY = 3
 # p2de_surface_flux
 FLUX_LF_NODAL = 0
 FLUX_LF_PROJECTED = 1

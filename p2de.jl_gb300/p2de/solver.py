@@ -31,6 +31,8 @@ from .types import (
     PositivityBound,
     SubcellLimiter,
     TimeParam,
+    TVDAndCellEntropyBound,
+    TVDBound,
 )
 
 
@@ -97,6 +99,10 @@ def lower_param(param: Param, K: int) -> abi.P2deParam:
             bound = abi.BOUND_POSITIVITY
         elif isinstance(lim.bound, PositivityAndCellEntropyBound):
             bound = abi.BOUND_POSITIVITY_AND_CELL_ENTROPY
+        elif isinstance(lim.bound, TVDAndCellEntropyBound):
+            bound = abi.BOUND_TVD_AND_CELL_ENTROPY
+        elif isinstance(lim.bound, TVDBound):
+            bound = abi.BOUND_TVD
         else:
             raise UnsupportedMethod(f"bound {type(lim.bound).__name__} is not built")
     if param.precision not in abi.PRECISIONS:

@@ -127,6 +127,10 @@ class TVDBound:
     pass
 
 
+class TVDAndCellEntropyBound:
+    pass
+
+
 @dataclass(frozen=True)
 class SubcellLimiter:
     bound: Any = field(default_factory=PositivityBound)

@@ -9,7 +9,14 @@ import pytest
 import p2de
 from p2de import abi, problems
 from p2de import solver as S
-from p2de.types import PositivityAndCellEntropyBound, PositivityBound, LowOrderPositivity, EntropyStable
+from p2de.types import (
+    EntropyStable,
+    LowOrderPositivity,
+    PositivityAndCellEntropyBound,
+    PositivityBound,
+    TVDAndCellEntropyBound,
+    TVDBound,
+)
 
 from conftest import relerr
 from helpers import setup
@@ -90,14 +97,41 @@ def test_rhs_kelvin_helmholtz_all_degrees(N):
 TOL_INTENDED_CELL = 1e-6
 
 
+BOUNDS = {"pos": PositivityBound(), "cell": PositivityAndCellEntropyBound(), "tvd": TVDBound(),
+          "tvd-cell": TVDAndCellEntropyBound()}
+
+
 @pytest.mark.parametrize("nstage", [1, 2, 3])
-@pytest.mark.parametrize("bound", ["pos", "cell"])
+@pytest.mark.parametrize("bound", list(BOUNDS))
 @pytest.mark.parametrize("refsem", [True, False])
 def test_rhs_modes(nstage, bound, refsem):
-    b = PositivityAndCellEntropyBound() if bound == "cell" else PositivityBound()
-    param, md, bc, desc, U0 = setup(problems.kelvin_helmholtz, N=3, Kx=8, Ky=8, T=0.1, bound=b, reference_semantics=refsem)
-    tol = TOL_INTENDED_CELL if (bound == "cell" and not refsem) else TOL
+    param, md, bc, desc, U0 = setup(problems.kelvin_helmholtz, N=3, Kx=8, Ky=8, T=0.1, bound=BOUNDS[bound],
+                                    reference_semantics=refsem)
+    tol = TOL_INTENDED_CELL if (bound.endswith("cell") and not refsem) else TOL
     compare_rhs(param, md, desc, U0, dt=2e-4, nstage=nstage, tol=tol)
+
+
+@pytest.mark.parametrize("refsem", [True, False])
+@pytest.mark.parametrize("problem,kw", [
+    (problems.riemann2d, dict(N=2, Kx=9, Ky=7, T=0.2, seed=3)),
+    (problems.double_mach_reflection, dict(N=3, Kx=16, Ky=4, T=0.2)),
+    (problems.riemann2d, dict(N=5, Kx=4, Ky=3, T=0.2, seed=6)),
+])
+def test_tvd_bounds_steps_match(problem, kw, refsem):
+    """TVD bounds (subcell.jl:112-141): stencils across element faces and domain
+    boundaries, both semantics, five steps against the oracle."""
+    param, md, bc, desc, U0 = setup(problem, bound=TVDBound(), reference_semantics=refsem, **kw)
+    compare_rhs(param, md, desc, U0, dt=1e-3, nstage=2)
+    o = oracle_for(desc, U0)
+    g = gpu_for(param, md, desc, U0)
+    to, tg = 0.0, 0.0
+    for _ in range(5):
+        to, _ = o.step(to)
+        tg, _ = S.ssp33_step(g, tg)
+    assert abs(tg - to) <= 1e-13 * abs(to)
+    assert relerr(g.get_field(abi.FIELD_UQ), o.get_field(abi.FIELD_UQ)) <= TOL
+    g.close()
+    o.close()
 
 
 def test_rhs_riemann_outflow():

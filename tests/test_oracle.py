@@ -9,7 +9,7 @@ import pytest
 import p2de
 from p2de import abi, problems
 from p2de import solver as S
-from p2de.types import PositivityAndCellEntropyBound, PositivityBound
+from p2de.types import PositivityAndCellEntropyBound, PositivityBound, TVDAndCellEntropyBound, TVDBound
 
 from conftest import relerr
 from helpers import setup
@@ -125,7 +125,7 @@ def test_conservation_periodic():
 
 
 @pytest.mark.parametrize("refsem", [True, False])
-@pytest.mark.parametrize("bound", [PositivityBound(), PositivityAndCellEntropyBound()])
+@pytest.mark.parametrize("bound", [PositivityBound(), PositivityAndCellEntropyBound(), TVDBound(), TVDAndCellEntropyBound()])
 def test_positivity_and_factor_range(refsem, bound):
     param, md, bc, desc, U0 = setup(problems.riemann2d, N=3, Kx=8, Ky=8, T=0.2, seed=2, bound=bound, reference_semantics=refsem)
     o = Oracle(desc, nthreads=2)
@@ -140,6 +140,51 @@ def test_positivity_and_factor_range(refsem, bound):
         for s in (1, 2, 3):
             L = o.get_field(abi.FIELD_L_LOCAL, s)
             assert np.all((L >= 0) & (L <= 1))
+
+
+def tvd_bounds_np(md, N, rhoL):
+    """low_order_stencil (limiter_utils.jl:222-231) min/max of rhoL, restated with numpy
+    on the mesh's mapP (q2fq: the r-face first at corners)."""
+    n = N + 1
+    K = rhoL.shape[0]
+    Nfp = 4 * n
+    mapP = md.mapP.reshape(K, Nfp) - 1
+    fq2q = np.concatenate([n * np.arange(n), N + n * np.arange(n), np.arange(n), np.arange(n) + n * N])
+    lb, ub = rhoL.copy(), rhoL.copy()
+    for k in range(K):
+        for q in range(n * n):
+            i, j = q % n, q // n
+            faces = ([j] if i == 0 else []) + ([n + j] if i == N else []) + ([2 * n + i] if j == 0 else []) + ([3 * n + i] if j == N else [])
+
+            def across(direction):
+                f = faces[0] if len(faces) == 1 else faces[direction - 1]
+                lin = mapP[k, f]
+                return lin // Nfp, fq2q[lin % Nfp]
+
+            st = [(k, q - 1) if i > 0 else across(1), (k, q + 1) if i < N else across(1),
+                  (k, q - n) if j > 0 else across(2), (k, q + n) if j < N else across(2)]
+            for kk, qq in st:
+                lb[k, q] = min(lb[k, q], rhoL[kk, qq])
+                ub[k, q] = max(ub[k, q], rhoL[kk, qq])
+    return lb, ub
+
+
+def test_tvd_bounds_hold_after_a_stage():
+    """TVDBound with the intended bounds: the stage-1 update's density stays within the
+    min/max of the low-order density over each node's stencil (subcell.jl:112-141)."""
+    param, md, bc, desc, U0 = setup(problems.riemann2d, N=3, Kx=6, Ky=5, T=0.2, seed=5, bound=TVDBound(),
+                                    reference_semantics=False)
+    o = Oracle(desc, nthreads=2)
+    o.set_Uq(U0)
+    dt = 2e-3
+    o.rhs(0.0, dt, 2)
+    rhoL = (U0[..., 0] + dt * o.get_field(abi.FIELD_RHSL).reshape(desc.K, -1, 4)[..., 0])
+    lb, ub = tvd_bounds_np(md, param.N, rhoL)
+    rho1 = U0[..., 0] + dt * o.get_field(abi.FIELD_RHSU).reshape(desc.K, -1, 4)[..., 0]
+    tol = 1e-12 * np.abs(rho1).max()
+    assert np.all(rho1 >= lb - tol) and np.all(rho1 <= ub + tol)
+    L = o.get_field(abi.FIELD_L_LOCAL, 2)
+    assert L.min() < 1.0  # the bounds are active somewhere
 
 
 def test_reference_semantics_give_low_order_rhs():
