@@ -17,6 +17,7 @@
 #include "p2de_diag.h"
 #include "p2de_launch.h"
 #include "p2de_physics.cuh"
+#include "p2de_stage.cuh"
 #include "p2de_tables.h"
 
 using namespace p2de;
@@ -72,6 +73,13 @@ __global__ void k_min_rho_rhoe(const double* Uq, size_t nodes, long long* out) {
     atomicMin(&out[0], okey(rmin));
     atomicMin(&out[1], okey(emin));
   }
+}
+
+__global__ void k_geom_table(const double* geom, int K, double* out) {
+  const long long w = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (w >= (long long)K * kGeomFactors) return;
+  const int k = (int)(w / kGeomFactors), q = (int)(w % kGeomFactors);
+  geom_factor(geom + 5 * (size_t)k, q, out + (size_t)k * kGeomStride);
 }
 
 double key_to_double(long long k) {
@@ -152,6 +160,14 @@ cudaError_t launch_b_n1d(int n1d, const StageArgs& a, cudaStream_t st) {
 
 }  // namespace
 
+namespace p2de {
+cudaError_t launch_geom_table(const double* geom, int K, double* out, cudaStream_t st) {
+  const long long items = (long long)K * kGeomFactors;
+  k_geom_table<<<(int)((items + 255) / 256), 256, 0, st>>>(geom, K, out);
+  return cudaGetLastError();
+}
+}  // namespace p2de
+
 struct p2de_solver {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -165,6 +181,7 @@ struct p2de_solver {
   double *Uq = nullptr, *resW = nullptr, *rhsL = nullptr, *rhsH = nullptr, *rhsU = nullptr;
   double *rhsxyL = nullptr, *rhsxyH = nullptr, *BFL = nullptr, *BFH = nullptr;
   double *fbar = nullptr, *Lpre = nullptr, *Lfin = nullptr, *geom = nullptr, *Ival = nullptr, *xyS = nullptr;
+  double* geomx = nullptr;  // K x 16 geometry factors
   double* scal = nullptr;
   int32_t *nbr = nullptr, *bcidx = nullptr;
   int8_t* bc = nullptr;
@@ -427,6 +444,7 @@ int p2de_initialize_DG(const p2de_param* prm, const p2de_mesh* mesh, int device,
   DA(s->Lpre, (size_t)2 * s->NSF * K);
   DA(s->Lfin, (size_t)3 * 2 * s->NSF * K);
   DA(s->geom, 5 * K);
+  DA(s->geomx, (size_t)kGeomStride * K);
   DA(s->Ival, (size_t)4 * (mesh->nI > 0 ? mesh->nI : 1));
   DA(s->xyS, (size_t)2 * (mesh->nS > 0 ? mesh->nS : 1));
   DA(s->scal, (size_t)S_NSCAL);
@@ -443,6 +461,7 @@ int p2de_initialize_DG(const p2de_param* prm, const p2de_mesh* mesh, int device,
     return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s->stream);
   };
   e = up(s->geom, mesh->geom, sizeof(double) * 5 * K);
+  if (e == cudaSuccess) e = launch_geom_table(s->geom, (int)K, s->geomx, s->stream);
   if (e == cudaSuccess) e = up(s->nbr, nbr.data(), sizeof(int32_t) * nfk);
   if (e == cudaSuccess) e = up(s->bcidx, bcidx.data(), sizeof(int32_t) * nfk);
   if (e == cudaSuccess) e = up(s->bc, bc.data(), nfk);
@@ -463,6 +482,7 @@ int p2de_initialize_DG(const p2de_param* prm, const p2de_mesh* mesh, int device,
   a.Uq = s->Uq;
   a.resW = s->resW;
   a.geom = s->geom;
+  a.geomx = s->geomx;
   a.nbr = s->nbr;
   a.bc = s->bc;
   a.bcidx = s->bcidx;

@@ -67,6 +67,7 @@ struct StageArgs {
   int* status;
   unsigned long long* counters;  // [0] quadratic rhoe solves evaluated by the bound phase
   double* rhoL;  // K x Nq low-order densities U + dt rhsL (TVD bounds only)
+  const double* geomx;  // K x 16 geometry factors (geom_factor), or null: computed per launch
 };
 
 }  // namespace p2de

@@ -102,7 +102,7 @@ class Pool {
 
 // offsets of a solve's arrays inside its pool block
 struct Layout {
-  size_t Uq, resW, rhsU, rhsL, rhsH, geom, fbar, Lpre, Lfin, Ival, xyS, nbr, bcidx, bc, total;
+  size_t Uq, resW, rhsU, rhsL, rhsH, geom, geomx, fbar, Lpre, Lfin, Ival, xyS, nbr, bcidx, bc, total;
 };
 
 Layout layout_for(const p2de_param& p, int64_t nI, int64_t nS) {
@@ -121,6 +121,7 @@ Layout layout_for(const p2de_param& p, int64_t nI, int64_t nS) {
   L.rhsL = take(other ? 8 * 4 * Nq * K : 8);
   L.rhsH = take(other ? 8 * 4 * Nq * K : 8);
   L.geom = take(8 * 5 * K);
+  L.geomx = take(8 * 16 * K);
   L.fbar = take(8 * 16 * NSF * K);
   L.Lpre = take(8 * 2 * NSF * K);
   L.Lfin = take(8 * 3 * 2 * NSF * K);
@@ -472,6 +473,7 @@ int p2de_batch_add(p2de_batch* b, const p2de_param* p, const p2de_mesh* m, const
   };
   BCK(up(lay.Uq, Uq, 8 * 4 * Nq * K));
   BCK(up(lay.geom, m->geom, 8 * 5 * K));
+  BCK(launch_geom_table((const double*)(base + lay.geom), (int)K, (double*)(base + lay.geomx), b->stream));
   BCK(up(lay.nbr, nbr.data(), 4 * nfk));
   BCK(up(lay.bcidx, bcidx.data(), 4 * nfk));
   BCK(up(lay.bc, bc.data(), nfk));
@@ -495,6 +497,7 @@ int p2de_batch_add(p2de_batch* b, const p2de_param* p, const p2de_mesh* m, const
   a.Uq = (double*)(base + lay.Uq);
   a.resW = (double*)(base + lay.resW);
   a.geom = (const double*)(base + lay.geom);
+  a.geomx = (const double*)(base + lay.geomx);
   a.nbr = (const int32_t*)(base + lay.nbr);
   a.bc = (const int8_t*)(base + lay.bc);
   a.bcidx = (const int32_t*)(base + lay.bcidx);

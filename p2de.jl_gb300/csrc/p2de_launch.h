@@ -24,4 +24,7 @@ cudaError_t launch_stage_a(const StageArgs& a, bool mixed, cudaStream_t st);
 template <int N1D>
 cudaError_t launch_stage_b(const StageArgs& a, cudaStream_t st);
 
+// Per-element geometry factors (geom_factor) for K elements: out has 16 doubles per element.
+cudaError_t launch_geom_table(const double* geom, int K, double* out, cudaStream_t st);
+
 }  // namespace p2de

@@ -99,6 +99,28 @@ __device__ __forceinline__ double low_update(double u, double dt, double r) { re
 // 1/x correctly rounded (the same value as 1.0 / x)
 __device__ __forceinline__ double rcp(double x) { return __drcp_rn(x); }
 
+// Geometry factor q of an element from gg = (J, rxJ, sxJ, ryJ, syJ): slots 0-4 copy gg,
+// then |gr|, nr (2), |gs|, ns (2), 1/J; slots 12-14 hold FP32 rxJ, sxJ, ryJ, syJ, 1/J
+// (q = 12..16 write float q-12). Used by the per-element table and by P0 without one.
+__device__ __forceinline__ void geom_factor(const double* gg, int q, double* G) {
+  if (q < 5) {
+    G[q] = gg[q];
+  } else if (q < 11) {
+    const bool r = q < 8;  // r-normal: (rxJ, ryJ); s-normal: (sxJ, syJ)
+    const double g1 = r ? gg[1] : gg[2], g2 = r ? gg[3] : gg[4];
+    const double gn = sqrt(g1 * g1 + g2 * g2);
+    const int j = (q - 5) % 3;
+    G[q] = j == 0 ? gn : (j == 1 ? g1 : g2) / gn;
+  } else if (q == 11) {
+    G[11] = __drcp_rn(gg[0]);
+  } else {
+    float* Gf = reinterpret_cast<float*>(G + 12);
+    Gf[q - 12] = q < 16 ? (float)gg[q - 11] : (float)__drcp_rn(gg[0]);
+  }
+}
+constexpr int kGeomFactors = 17;  // q = 0..16
+constexpr int kGeomStride = 16;   // doubles per element in the table
+
 // ordered 64-bit key of a double (monotone for non-NaN values), for atomicMin
 __device__ __forceinline__ long long order_key(double x) {
   long long b = __double_as_longlong(x);
@@ -278,27 +300,19 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
   const double dt_lim = a.scal[S_DT_LIM];
   const double t_now = a.scal[S_T];
 
-  // ---- P0: geometry and state. One item per (element, factor), so that no thread runs
-  //      the whole chain of square roots and divisions: G = J, rxJ, sxJ, ryJ, syJ,
-  //      |gr|, nr (2), |gs|, ns (2), 1/J, then FP32 rxJ, sxJ, ryJ, syJ, 1/J (mixed)
-  constexpr int NG = sizeof(TH) == 4 ? 17 : 12;
-  for (int w = tid; w < Ke * NG; w += bs) {
-    const int e = w / NG, q = w % NG;
-    double* G = sm + e * PE + C::O_GEO;
-    const double* gg = a.geom + 5 * (size_t)(k0 + e);
-    if (q < 5) {
-      G[q] = gg[q];
-    } else if (q < 11) {
-      const bool r = q < 8;  // r-normal: (rxJ, ryJ); s-normal: (sxJ, syJ)
-      const double g1 = r ? gg[1] : gg[2], g2 = r ? gg[3] : gg[4];
-      const double gn = sqrt(g1 * g1 + g2 * g2);
-      const int j = (q - 5) % 3;
-      G[q] = j == 0 ? gn : (j == 1 ? g1 : g2) / gn;
-    } else if (q == 11) {
-      G[11] = rcp(gg[0]);
-    } else {
-      float* Gf = reinterpret_cast<float*>(G + 12);
-      Gf[q - 12] = q < 16 ? (float)gg[q - 11] : (float)rcp(gg[0]);
+  // ---- P0: geometry and state. The geometry factors (geom_factor) come from the
+  //      solve's per-element table when it has one (made once at set-up), else one item
+  //      per (element, factor)
+  if (a.geomx) {
+    for (int w = tid; w < Ke * kGeomStride; w += bs) {
+      const int e = w / kGeomStride, q = w % kGeomStride;
+      sm[e * PE + C::O_GEO + q] = a.geomx[(size_t)k0 * kGeomStride + w];
+    }
+  } else {
+    constexpr int NG = sizeof(TH) == 4 ? kGeomFactors : 12;
+    for (int w = tid; w < Ke * NG; w += bs) {
+      const int e = w / NG, q = w % NG;
+      geom_factor(a.geom + 5 * (size_t)(k0 + e), q, sm + e * PE + C::O_GEO);
     }
   }
   if (tid == 0) s_list[0] = 0;
@@ -808,6 +822,10 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
 
   // ---- P8: subcell flux prefix sums (accumulate_f_bar!(::Dim2), subcell.jl:163-206)
   //          and the low-order update uL = U + dt*rhsL (subcell.jl:269)
+  // Item (e, d, line l, c); x lines (d = 0, line sj) start at face sj and run through
+  // faces si + (n+1) sj and nodes (si-1) + n sj; y lines (d = 1, line si) start at face
+  // 2n + si and run through faces si + n sj and nodes si + n (sj-1). Both as strides, so
+  // a warp's x and y items share every instruction.
   for (int w = tid; w < Ke * 8 * n; w += bs) {
     int e = w / (8 * n), r = w % (8 * n);
     int d = r / (4 * n), l = (r / 4) % n, c = r % 4;
@@ -816,32 +834,20 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
     double* fb = base + C::O_SCR;  // [d][HL][face][c]
     double* fH = fb + (d * 2 + 0) * NSF * 4;
     double* fL = fb + (d * 2 + 1) * NSF * 4;
-    if (d == 0) {
-      int sj = l;
-      double h = base[C::O_BFH + 8 * sj + c], lo = base[C::O_BFL + 8 * sj + c];
-      fH[(0 + (n + 1) * sj) * 4 + c] = h;
-      fL[(0 + (n + 1) * sj) * 4 + c] = lo;
-      for (int si = 1; si <= n; ++si) {
-        int q = (si - 1) + n * sj;
-        double wJ = wJq[2 * q];
-        h = h + wJ * base[C::O_RXYH + 8 * q + c];
-        lo = lo + wJ * base[C::O_RXYL + 8 * q + c];
-        fH[(si + (n + 1) * sj) * 4 + c] = h;
-        fL[(si + (n + 1) * sj) * 4 + c] = lo;
-      }
-    } else {
-      int si = l;
-      double h = base[C::O_BFH + 8 * (2 * n + si) + 4 + c], lo = base[C::O_BFL + 8 * (2 * n + si) + 4 + c];
-      fH[(si + n * 0) * 4 + c] = h;
-      fL[(si + n * 0) * 4 + c] = lo;
-      for (int sj = 1; sj <= n; ++sj) {
-        int q = si + n * (sj - 1);
-        double wJ = wJq[2 * q];
-        h = h + wJ * base[C::O_RXYH + 8 * q + 4 + c];
-        lo = lo + wJ * base[C::O_RXYL + 8 * q + 4 + c];
-        fH[(si + n * sj) * 4 + c] = h;
-        fL[(si + n * sj) * 4 + c] = lo;
-      }
+    const int f0 = d == 0 ? l : 2 * n + l;       // boundary face where the line starts
+    const int fs = d == 0 ? 1 : n, fb0 = d == 0 ? (n + 1) * l : l;  // subcell faces
+    const int qs = d == 0 ? 1 : n, qb0 = d == 0 ? n * l : l;        // nodes
+    const int o = 4 * d + c;
+    double h = base[C::O_BFH + 8 * f0 + o], lo = base[C::O_BFL + 8 * f0 + o];
+    fH[fb0 * 4 + c] = h;
+    fL[fb0 * 4 + c] = lo;
+    for (int t = 1; t <= n; ++t) {
+      const int q = qb0 + qs * (t - 1);
+      const double wJ = wJq[2 * q];
+      h = h + wJ * base[C::O_RXYH + 8 * q + o];
+      lo = lo + wJ * base[C::O_RXYL + 8 * q + o];
+      fH[(fb0 + fs * t) * 4 + c] = h;
+      fL[(fb0 + fs * t) * 4 + c] = lo;
     }
   }
   for (int w = tid; w < Ke * Nq; w += bs) {

@@ -72,9 +72,11 @@ def test_batch_admission_by_budget_and_reuse():
         b.add(cases[2][3], cases[2][4])
     assert ei.value.status == 8
     b.remove(s0)
-    s2 = b.add(cases[4][3], cases[4][4])  # smaller than the freed block
+    j = min(range(2, len(cases)), key=lambda i: sizes[i])  # fits the freed block
+    assert sizes[j] <= sizes[0]
+    s2 = b.add(cases[j][3], cases[j][4])
     b.run_to_end(chunk=20)
-    U_alone, _, _ = alone(cases[4][0], cases[4][1], cases[4][3], cases[4][4])
+    U_alone, _, _ = alone(cases[j][0], cases[j][1], cases[j][3], cases[j][4])
     np.testing.assert_array_equal(b.Uq(s2), U_alone)
     used, cap = b.memory()
     assert used <= cap
