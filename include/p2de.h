@@ -25,7 +25,7 @@
 extern "C" {
 #endif
 
-#define P2DE_ABI_VERSION 1
+#define P2DE_ABI_VERSION 2
 
 typedef enum p2de_status {
   P2DE_OK = 0,
@@ -95,6 +95,13 @@ typedef struct p2de_param {
    * Urho := Lphi = 0 and Urhoe := Urho = Inf. 0: the intended Urho = Urhoe = Inf. */
   int32_t reference_semantics;
   int32_t precision;               /* p2de_precision */
+  /* SubcellLimiter's shockcapture (Solver.jl:65-74): 0 NoShockCapture, 1
+   * HennemannShockCapture(a, c), whose per-element blending factor
+   * (shock_capture.jl:118-137) caps every subcell factor of the element. */
+  int32_t shock_capture;
+  int32_t reserved_;               /* 0 */
+  double shock_capture_a;
+  double shock_capture_c;
 } p2de_param;
 
 /* Mesh and boundary data. geom/mapP/mapI/mapO/Ival follow StateParam.bcdata

@@ -338,12 +338,101 @@ struct Solver {
   // ---------------------------------------------------------------------------
   // initialize_operators (init.jl:133-228) for LGL quads (init.jl:97-103, 307-340)
   // ---------------------------------------------------------------------------
+  // inv(VDM) (init.jl:224) for LGL: VDM = vandermonde(Quad(), N, r, s) of NodesAndModes,
+  // the orthonormal Legendre products P_i(r) P_j(s) (mode i + N1D j) at the nodes
+  std::vector<double> VDMinv;  // Nq x Nq, row-major
+  static double legendre_orthonormal(int n, double x) {
+    double p0 = 1.0, p1 = x;
+    if (n == 0) return std::sqrt(0.5);
+    for (int k = 1; k < n; ++k) {
+      double p2 = ((2.0 * k + 1.0) * x * p1 - k * p0) / (k + 1.0);
+      p0 = p1;
+      p1 = p2;
+    }
+    return std::sqrt((2.0 * n + 1.0) / 2.0) * p1;
+  }
+  void build_vdm_inv() {
+    std::vector<double> A((size_t)Nq * Nq), Inv((size_t)Nq * Nq, 0.0);
+    for (int is = 0; is < N1D; ++is)
+      for (int ir = 0; ir < N1D; ++ir)
+        for (int j = 0; j < N1D; ++j)
+          for (int i = 0; i < N1D; ++i)
+            A[(size_t)(ir + N1D * is) * Nq + (i + N1D * j)] = legendre_orthonormal(i, r1D[ir]) * legendre_orthonormal(j, r1D[is]);
+    for (int i = 0; i < Nq; ++i) Inv[(size_t)i * Nq + i] = 1.0;
+    // Gauss-Jordan elimination with partial pivoting
+    for (int c = 0; c < Nq; ++c) {
+      int piv = c;
+      for (int r = c + 1; r < Nq; ++r)
+        if (std::fabs(A[(size_t)r * Nq + c]) > std::fabs(A[(size_t)piv * Nq + c])) piv = r;
+      if (piv != c)
+        for (int j = 0; j < Nq; ++j) {
+          std::swap(A[(size_t)c * Nq + j], A[(size_t)piv * Nq + j]);
+          std::swap(Inv[(size_t)c * Nq + j], Inv[(size_t)piv * Nq + j]);
+        }
+      const double d = A[(size_t)c * Nq + c];
+      for (int j = 0; j < Nq; ++j) {
+        A[(size_t)c * Nq + j] /= d;
+        Inv[(size_t)c * Nq + j] /= d;
+      }
+      for (int r = 0; r < Nq; ++r) {
+        if (r == c) continue;
+        const double f = A[(size_t)r * Nq + c];
+        if (f == 0.0) continue;
+        for (int j = 0; j < Nq; ++j) {
+          A[(size_t)r * Nq + j] -= f * A[(size_t)c * Nq + j];
+          Inv[(size_t)r * Nq + j] -= f * Inv[(size_t)c * Nq + j];
+        }
+      }
+    }
+    VDMinv = Inv;
+  }
+
+  // initialize_smoothness_indicator!(::Dim2) and update_blending_factor!
+  // (HennemannShockCapture) (shock_capture.jl:49-81, 92-103, 118-137): per element, the
+  // modal energies of rho*p; blending factor max(min(1 - alpha, 1), 1/2)
+  std::vector<double> blending_factor;
+  void update_blending_factor() {
+    blending_factor.assign(K, 1.0);
+    if (prm.shock_capture != 1) return;
+    const double a = prm.shock_capture_a, c = prm.shock_capture_c;
+    const double TN = a * std::pow(10.0, -c * std::pow((double)(N + 1), 0.25));
+    const double alphamax = 0.5, alphaE0 = 0.0001;
+    const double s_factor = std::log((1 - alphaE0) / alphaE0);
+#pragma omp parallel for schedule(static)
+    for (int k = 0; k < K; ++k) {
+      std::vector<double> ind(Nq), modal(Nq);
+      for (int i = 0; i < Nq; ++i) {
+        const V4& U = Uq[i + (size_t)Nq * k];
+        ind[i] = U[0] * eq.pfun(U);
+      }
+      for (int i = 0; i < Nq; ++i) {
+        double sum = 0.0;
+        for (int j = 0; j < Nq; ++j) sum += VDMinv[(size_t)i * Nq + j] * ind[j];
+        modal[i] = sum;
+      }
+      double modeN = 0.0, modeNm1 = 0.0, total = 0.0;
+      int count = 0;
+      for (int j = 0; j <= N; ++j)
+        for (int i = 0; i <= N; ++i) {
+          const double energy = modal[count] * modal[count];
+          if (i == N || j == N) modeN += energy;
+          if (i == N - 1 || j == N - 1) modeNm1 += energy;
+          total += energy;
+          ++count;
+        }
+      const double smooth = jmax(modeN / total, modeNm1 / total);
+      const double alpha = 1.0 / (1.0 + std::exp(-s_factor / TN * (smooth - TN)));
+      blending_factor[k] = jmax(jmin(1.0 - alpha, 1.0), alphamax);
+    }
+  }
+
   void build_operators() {
     N1D = N + 1;
     Nq = N1D * N1D;
     Nfp = 4 * N1D;
     Nh = Nq + Nfp;
     gll_rule(N, r1D, w1D, D1D);
+    build_vdm_inv();
     const double ZEROTOL = prm.ZEROTOL;
     // tensor-product nodes, r fastest: i = ir + N1D*is
     wq.assign(Nq, 0.0);
@@ -952,9 +1041,10 @@ struct Solver {
   void apply_rhs_limiter(double dt, int nstage) {
     const int s = nstage - 1;
     const int N1Dp1 = N1D + 1;
-    // update_blending_factor!(NoShockCapture) -> 1.0; update_smoothness_factor! -> 0.0;
+    // update_blending_factor! (NoShockCapture: 1.0; HennemannShockCapture: per element);
+    // update_smoothness_factor! -> 0.0;
     // initialize_entropy_bounds! -> lbound_s_modified = 0.0 (subcell.jl:4-6)
-    const double l_shock = 1.0;
+    update_blending_factor();
     const double lbound_s = 0.0;
     if (tvd()) initialize_TVD_bounds(dt);
     // accumulate_f_bar!(::Dim2) (subcell.jl:163-206)
@@ -1044,7 +1134,7 @@ struct Solver {
         }
       }
       for (int i = 0; i < Nq + N1D; ++i)
-        for (int d = 0; d < 2; ++d) L_local[LL(i, d, k, s)] = jmin(L_local[LL(i, d, k, s)], l_shock);
+        for (int d = 0; d < 2; ++d) L_local[LL(i, d, k, s)] = jmin(L_local[LL(i, d, k, s)], blending_factor[k]);
     }
     // enforce_ES_subcell! (subcell.jl:462-466) for PositivityAndCellEntropyBound
     if (cell_entropy()) {

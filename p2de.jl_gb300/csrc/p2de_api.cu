@@ -254,6 +254,7 @@ int flags_for(const p2de_solver* s, int nstage, bool update, bool debug) {
       (f & F_DO_LIMIT))
     f |= F_TVD;
   if (s->prm.precision == P2DE_PRECISION_MIXED_ACC64) f |= F_ACC64;
+  if (s->prm.shock_capture == 1 && (f & F_DO_LIMIT)) f |= F_SHOCK;
   if (update) f |= F_UPDATE;
   if (debug) f |= F_WRITE_DEBUG;
   return f;
@@ -335,7 +336,7 @@ int p2de_initialize_DG(const p2de_param* prm, const p2de_mesh* mesh, int device,
     return fail(nullptr, P2DE_ERR_UNSUPPORTED,
                 "surface fluxes: only LaxFriedrichsOnNodalVal (low order) and LaxFriedrichsOnProjectedVal (high order)");
   if (prm->rhs_type < 0 || prm->rhs_type > 2 || prm->bound_type < 0 || prm->bound_type > 3 || prm->precision < 0 ||
-      prm->precision > 2)
+      prm->precision > 2 || prm->shock_capture < 0 || prm->shock_capture > 1)
     return fail(nullptr, P2DE_ERR_INVALID_ARGUMENT, "rhs_type/bound_type/precision out of range");
   const int64_t n1 = prm->N + 1, Nfp = 4 * n1, Nq = n1 * n1;
   const int64_t nfk = Nfp * prm->K;
@@ -517,6 +518,7 @@ int p2de_initialize_DG(const p2de_param* prm, const p2de_mesh* mesh, int device,
   a.minrec = s->minrec;
   a.status = s->status;
   a.counters = s->counters;
+  set_shock_capture(a, prm->N, prm->shock_capture_a, prm->shock_capture_c);
   if (prm->bound_type == P2DE_BOUND_TVD || prm->bound_type == P2DE_BOUND_TVD_AND_CELL_ENTROPY) {
     if (dalloc(s, &s->rhoL, (size_t)Nq * prm->K) != cudaSuccess) return bail(P2DE_ERR_OUT_OF_MEMORY);
     a.rhoL = s->rhoL;

@@ -1,6 +1,8 @@
 // Launch arguments shared by the host code and the stage kernels.
 #pragma once
 
+#include <cmath>
+
 #include <stdint.h>
 
 #include "p2de_tables.h"
@@ -22,7 +24,8 @@ enum : int {
   F_CFL = 1 << 10,          // stage 1: low-order positivity CFL reduction
   F_ACC64 = 1 << 11,        // FP32 kernel: pair fluxes gathered and lifted in FP64
   F_TVD = 1 << 12,          // TVD density bounds from the low-order densities in rhoL
-  F_LOW_ONLY = 1 << 13      // kernel A stops after the low-order RHS and stores rhoL
+  F_LOW_ONLY = 1 << 13,     // kernel A stops after the low-order RHS and stores rhoL
+  F_SHOCK = 1 << 14         // HennemannShockCapture blending factor caps the subcell factors
 };
 
 // boundary codes per face node
@@ -68,6 +71,16 @@ struct StageArgs {
   unsigned long long* counters;  // [0] quadratic rhoe solves evaluated by the bound phase
   double* rhoL;  // K x Nq low-order densities U + dt rhsL (TVD bounds only)
   const double* geomx;  // K x 16 geometry factors (geom_factor), or null: computed per launch
+  double sc_TN, sc_q;   // HennemannShockCapture: TN and -log((1-1e-4)/1e-4) / TN
 };
+
+// StageArgs shock-capture constants of update_blending_factor! (shock_capture.jl:123-126)
+inline void set_shock_capture(StageArgs& a, int N, double sc_a, double sc_c) {
+  const double TN = sc_a * std::pow(10.0, -sc_c * std::pow((double)(N + 1), 0.25));
+  const double alphaE0 = 0.0001;
+  const double s_factor = std::log((1 - alphaE0) / alphaE0);
+  a.sc_TN = TN;
+  a.sc_q = -s_factor / TN;
+}
 
 }  // namespace p2de

@@ -223,7 +223,7 @@ int validate_solve(const p2de_param* p, const p2de_mesh* m, std::string& why) {
   }
   if (p->low_order_surface_flux != P2DE_FLUX_LAX_FRIEDRICHS_ON_NODAL_VAL ||
       p->high_order_surface_flux != P2DE_FLUX_LAX_FRIEDRICHS_ON_PROJECTED_VAL || p->rhs_type < 0 || p->rhs_type > 2 ||
-      p->bound_type < 0 || p->bound_type > 1) {
+      p->bound_type < 0 || p->bound_type > 1 || p->shock_capture < 0 || p->shock_capture > 1) {
     why = "unsupported method";
     return P2DE_ERR_UNSUPPORTED;
   }
@@ -492,7 +492,9 @@ int p2de_batch_add(p2de_batch* b, const p2de_param* p, const p2de_mesh* m, const
   if (p->reference_semantics) f |= F_REF_SEM;
   if (p->bound_type == P2DE_BOUND_POSITIVITY_AND_CELL_ENTROPY) f |= F_CELL_ENTROPY;
   if (b->precision == P2DE_PRECISION_MIXED_ACC64) f |= F_ACC64;
+  if (p->shock_capture == 1 && (f & F_DO_LIMIT)) f |= F_SHOCK;
   a.flags = f;
+  set_shock_capture(a, p->N, p->shock_capture_a, p->shock_capture_c);
   a.ops = b->d_tables + (n - 2);
   a.Uq = (double*)(base + lay.Uq);
   a.resW = (double*)(base + lay.resW);

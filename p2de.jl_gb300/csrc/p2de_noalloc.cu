@@ -112,7 +112,8 @@ extern "C" int p2de_rhs_noalloc(const p2de_param* prm, const p2de_device_mesh* m
   if (prm->N < 1 || prm->N > 5 || prm->K < 1 || nstage < 1 || nstage > 3) return P2DE_ERR_INVALID_ARGUMENT;
   if (prm->low_order_surface_flux != P2DE_FLUX_LAX_FRIEDRICHS_ON_NODAL_VAL ||
       prm->high_order_surface_flux != P2DE_FLUX_LAX_FRIEDRICHS_ON_PROJECTED_VAL || prm->rhs_type < 0 ||
-      prm->rhs_type > 2 || prm->bound_type < 0 || prm->bound_type > 1)
+      prm->rhs_type > 2 || prm->bound_type < 0 || prm->bound_type > 1 || prm->shock_capture < 0 ||
+      prm->shock_capture > 1)
     return P2DE_ERR_UNSUPPORTED;
   const int n1d = prm->N + 1;
   const size_t K = (size_t)prm->K;
@@ -184,7 +185,9 @@ extern "C" int p2de_rhs_noalloc(const p2de_param* prm, const p2de_device_mesh* m
   if (prm->bound_type == P2DE_BOUND_POSITIVITY_AND_CELL_ENTROPY) f |= F_CELL_ENTROPY;
   if (mesh->axis_aligned) f |= F_AXIS_ALIGNED;
   if (prm->precision == P2DE_PRECISION_MIXED_ACC64) f |= F_ACC64;
+  if (prm->shock_capture == 1 && (f & F_DO_LIMIT)) f |= F_SHOCK;
   a.flags = f;
+  set_shock_capture(a, prm->N, prm->shock_capture_a, prm->shock_capture_c);
   a.ops = (const OpTable*)(scr + H_TABLE);
   a.Uq = const_cast<double*>(Uq);
   a.resW = nullptr;

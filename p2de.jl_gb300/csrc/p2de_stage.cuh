@@ -346,6 +346,7 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
     double* Ws = base + C::O_WS + 2 * m;
     Ws[0] = wavespeed_r(g, rr, G[6] * rhou + G[7] * rhov, E);
     Ws[1] = wavespeed_r(g, rr, G[9] * rhou + G[10] * rhov, E);
+    if (flags & F_SHOCK) base[C::O_LAMI + m] = rho * p;  // the indicator rho p (shock_capture.jl:92-103)
     if (do_high) {
       if (sizeof(TH) == 8) {
         double* Pm = base + C::O_PRIM + 6 * m;
@@ -364,6 +365,36 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
     }
   }
   __syncthreads();
+
+  // ---- P1b: HennemannShockCapture (shock_capture.jl:49-81, 118-137): modal energies of
+  //      the indicator through inv(VDM), smoothness max(E_N, E_{N-1}) / E, blending
+  //      factor max(min(1 - alpha, 1), 1/2) into G[15]
+  if (flags & F_SHOCK) {
+    for (int w = tid; w < Ke * Nq; w += bs) {
+      const int e = w / Nq, i = w % Nq;
+      double* base = sm + e * PE;
+      const double* Vi = op.VDMinv + i * Nq;
+      double sum = 0.0;
+      for (int j = 0; j < Nq; ++j) sum = fma(Vi[j], base[C::O_LAMI + j], sum);
+      base[C::O_SCR + i] = sum * sum;
+    }
+    __syncthreads();
+    for (int e = tid; e < Ke; e += bs) {
+      double* base = sm + e * PE;
+      double modeN = 0.0, modeNm1 = 0.0, total = 0.0;
+      for (int j = 0; j < n; ++j)
+        for (int i = 0; i < n; ++i) {
+          const double energy = base[C::O_SCR + i + n * j];
+          if (i == n - 1 || j == n - 1) modeN += energy;
+          if (i == n - 2 || j == n - 2) modeNm1 += energy;
+          total += energy;
+        }
+      const double smooth = fmax(modeN / total, modeNm1 / total);
+      const double alpha = 1.0 / (1.0 + exp(a.sc_q * (smooth - a.sc_TN)));
+      base[C::O_GEO + 15] = fmax(fmin(1.0 - alpha, 1.0), 0.5);
+    }
+    __syncthreads();
+  }
 
   // ---- P2: low-order volume pairs (accumulate_low_order_rhs_volume!, :139-173)
   if (do_low) {
@@ -985,7 +1016,8 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
     int d = r / NSF, fi = r % NSF;
     double* base = sm + e * PE;
     const double* ev = base + C::O_EV;
-    double L = 1.0;
+    // 1, or the element's shock-capture blending factor (the final min of subcell.jl:345)
+    double L = (flags & F_SHOCK) ? base[C::O_GEO + 15] : 1.0;
     if (d == 0) {
       int si = fi % (n + 1), sj = fi / (n + 1);
       if (si < n) L = min_nonneg_bits(L, ev[0 * Nq + si + n * sj]);

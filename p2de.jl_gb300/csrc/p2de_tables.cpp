@@ -64,6 +64,55 @@ void gll_rule(int N, double* r, double* w, double* D) {
     }
 }
 
+namespace {
+
+// Legendre polynomial of degree n normalized on [-1, 1] (three-term recurrence)
+double legendre_normalized(int n, double x) {
+  if (n == 0) return std::sqrt(0.5);
+  double p0 = 1.0, p1 = x;
+  for (int k = 1; k < n; ++k) {
+    const double p2 = ((2.0 * k + 1.0) * x * p1 - k * p0) / (k + 1.0);
+    p0 = p1;
+    p1 = p2;
+  }
+  return std::sqrt((2.0 * n + 1.0) / 2.0) * p1;
+}
+
+// inverse of a small dense matrix (row-major m x m) by Gauss-Jordan with partial pivoting
+bool invert(std::vector<double> A, int m, double* inv) {
+  std::vector<double> I((size_t)m * m, 0.0);
+  for (int i = 0; i < m; ++i) I[(size_t)i * m + i] = 1.0;
+  for (int c = 0; c < m; ++c) {
+    int piv = c;
+    for (int r = c + 1; r < m; ++r)
+      if (std::fabs(A[(size_t)r * m + c]) > std::fabs(A[(size_t)piv * m + c])) piv = r;
+    if (A[(size_t)piv * m + c] == 0.0) return false;
+    if (piv != c)
+      for (int j = 0; j < m; ++j) {
+        std::swap(A[(size_t)c * m + j], A[(size_t)piv * m + j]);
+        std::swap(I[(size_t)c * m + j], I[(size_t)piv * m + j]);
+      }
+    const double d = A[(size_t)c * m + c];
+    for (int j = 0; j < m; ++j) {
+      A[(size_t)c * m + j] /= d;
+      I[(size_t)c * m + j] /= d;
+    }
+    for (int r = 0; r < m; ++r) {
+      if (r == c) continue;
+      const double f = A[(size_t)r * m + c];
+      if (f == 0.0) continue;
+      for (int j = 0; j < m; ++j) {
+        A[(size_t)r * m + j] -= f * A[(size_t)c * m + j];
+        I[(size_t)r * m + j] -= f * I[(size_t)c * m + j];
+      }
+    }
+  }
+  for (size_t i = 0; i < I.size(); ++i) inv[i] = I[i];
+  return true;
+}
+
+}  // namespace
+
 int build_op_table(int N, double zerotol, OpTable* T) {
   if (N < 1 || N + 1 > kMaxN1D) return 1;
   std::memset(T, 0, sizeof(OpTable));
@@ -119,6 +168,15 @@ int build_op_table(int N, double zerotol, OpTable* T) {
         ++p;
       }
   T->nph = p;
+  {
+    std::vector<double> V((size_t)Nq * Nq);
+    for (int is = 0; is < n; ++is)
+      for (int ir = 0; ir < n; ++ir)
+        for (int j = 0; j < n; ++j)
+          for (int i = 0; i < n; ++i)
+            V[(size_t)(ir + n * is) * Nq + (i + n * j)] = legendre_normalized(i, r[ir]) * legendre_normalized(j, r[is]);
+    if (!invert(V, Nq, T->VDMinv)) return 4;
+  }
   for (int q = 0; q < p; ++q) T->hp_Sf[q] = (float)T->hp_S[q];
   for (int m = 0; m < Nq; ++m) T->rwqf[m] = (float)T->rwq[m];
   // gather order per node: partners ascending (the order in which the j-outer,

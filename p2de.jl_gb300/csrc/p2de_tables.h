@@ -50,6 +50,9 @@ struct OpTable {
   int16_t lga_pair[2][kMaxNq][2];
   int8_t lga_sign[2][kMaxNq][2];
   int8_t lga_count[2][kMaxNq];
+  // inv(VDM) of the orthonormal Legendre products P_i(r) P_j(s), mode i + N1D j (init.jl:224),
+  // row-major Nq x Nq: the modal coefficients of nodal values (HennemannShockCapture)
+  double VDMinv[kMaxNq * kMaxNq];
 };
 
 // Builds the table for polynomial degree N (1..5). Returns 0 on success.

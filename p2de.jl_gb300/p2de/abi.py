@@ -78,6 +78,10 @@ class P2deParam(ctypes.Structure):
         ("high_order_surface_flux", c_int32),
         ("reference_semantics", c_int32),
         ("precision", c_int32),
+        ("shock_capture", c_int32),
+        ("reserved_", c_int32),
+        ("shock_capture_a", c_double),
+        ("shock_capture_c", c_double),
     ]
 
 

@@ -33,6 +33,7 @@ from .types import (
     TimeParam,
     TVDAndCellEntropyBound,
     TVDBound,
+    HennemannShockCapture,
 )
 
 
@@ -92,9 +93,14 @@ def lower_param(param: Param, K: int) -> abi.P2deParam:
         raise UnsupportedMethod("surface fluxes: LaxFriedrichsOnNodalVal (low), LaxFriedrichsOnProjectedVal (high)")
     lim = param.rhs_limiter
     bound = abi.BOUND_POSITIVITY
+    shock, sc_a, sc_c = 0, 0.0, 0.0
     if rhs_type == abi.RHS_ES_LIMITED_LOW_ORDER_POS:
-        if not isinstance(lim, SubcellLimiter) or not isinstance(lim.shockcapture, NoShockCapture):
-            raise UnsupportedMethod("LimitedDG needs SubcellLimiter(shockcapture=NoShockCapture())")
+        if not isinstance(lim, SubcellLimiter):
+            raise UnsupportedMethod("LimitedDG needs SubcellLimiter")
+        if isinstance(lim.shockcapture, HennemannShockCapture):
+            shock, sc_a, sc_c = 1, float(lim.shockcapture.a), float(lim.shockcapture.c)
+        elif not isinstance(lim.shockcapture, NoShockCapture):
+            raise UnsupportedMethod(f"shock capture {type(lim.shockcapture).__name__} is not built")
         if isinstance(lim.bound, PositivityBound):
             bound = abi.BOUND_POSITIVITY
         elif isinstance(lim.bound, PositivityAndCellEntropyBound):
@@ -124,6 +130,9 @@ def lower_param(param: Param, K: int) -> abi.P2deParam:
         bound_type=bound,
         low_order_surface_flux=abi.FLUX_LF_NODAL,
         high_order_surface_flux=abi.FLUX_LF_PROJECTED,
+        shock_capture=shock,
+        shock_capture_a=sc_a,
+        shock_capture_c=sc_c,
         reference_semantics=1 if param.reference_semantics else 0,
         precision=abi.PRECISIONS[param.precision],
     )

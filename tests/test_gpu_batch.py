@@ -108,3 +108,24 @@ def test_server_rejects_a_request_larger_than_the_budget():
         sv.submit(desc, U0)
     assert ei.value.status == 8
     sv.close()
+
+
+def test_batch_member_with_shock_capture_equals_alone():
+    """Members with HennemannShockCapture keep their per-solve blending constants in the
+    batch; the result equals the solve alone."""
+    from p2de.types import HennemannShockCapture, PositivityAndCellEntropyBound, SubcellLimiter
+
+    param, md, bc, desc, U0 = setup(problems.riemann2d, N=3, Kx=10, Ky=8, T=0.01, seed=12)
+    ps = replace(param, rhs_limiter=SubcellLimiter(bound=PositivityAndCellEntropyBound(),
+                                                   shockcapture=HennemannShockCapture(a=0.4, c=1.7)))
+    ds = S.make_descriptor(ps, md, bc)
+    b = Batch(pool_bytes=1 << 30, max_solves=4)
+    s0 = b.add(ds, U0)
+    s1 = b.add(desc, U0)  # the same problem without shock capture
+    b.run_to_end(chunk=10)
+    U_sc, _, _ = alone(ps, md, ds, U0)
+    U_no, _, _ = alone(param, md, desc, U0)
+    np.testing.assert_array_equal(b.Uq(s0), U_sc)
+    np.testing.assert_array_equal(b.Uq(s1), U_no)
+    assert np.abs(U_sc - U_no).max() > 0  # the capture changed the solution
+    b.close()

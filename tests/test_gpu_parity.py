@@ -11,6 +11,8 @@ from p2de import abi, problems
 from p2de import solver as S
 from p2de.types import (
     EntropyStable,
+    HennemannShockCapture,
+    SubcellLimiter,
     LowOrderPositivity,
     PositivityAndCellEntropyBound,
     PositivityBound,
@@ -109,6 +111,31 @@ def test_rhs_modes(nstage, bound, refsem):
                                     reference_semantics=refsem)
     tol = TOL_INTENDED_CELL if (bound.endswith("cell") and not refsem) else TOL
     compare_rhs(param, md, desc, U0, dt=2e-4, nstage=nstage, tol=tol)
+
+
+@pytest.mark.parametrize("N", [1, 2, 3, 4, 5])
+@pytest.mark.parametrize("bound,refsem", [("pos", False), ("cell", True), ("tvd", True)])
+def test_shock_capture_matches(N, bound, refsem):
+    """HennemannShockCapture (shock_capture.jl:49-137): per-element blending factor from
+    the modal energies of rho p, capping every subcell factor (subcell.jl:345-347)."""
+    from dataclasses import replace
+
+    param, md, bc, desc, U0 = setup(problems.riemann2d, N=N, Kx=6, Ky=5, T=0.2, seed=4, bound=BOUNDS[bound],
+                                    reference_semantics=refsem)
+    ps = replace(param, rhs_limiter=SubcellLimiter(bound=BOUNDS[bound], shockcapture=HennemannShockCapture(a=0.5, c=1.8)))
+    ds = S.make_descriptor(ps, md, bc)
+    compare_rhs(ps, md, ds, U0, dt=1e-3, nstage=2)
+    o = oracle_for(ds, U0)
+    g = gpu_for(ps, md, ds, U0)
+    to, tg = 0.0, 0.0
+    for _ in range(3):
+        to, _ = o.step(to)
+        tg, _ = S.ssp33_step(g, tg)
+    assert relerr(g.get_field(abi.FIELD_UQ), o.get_field(abi.FIELD_UQ)) <= TOL
+    L = g.get_field(abi.FIELD_L_LOCAL, 3).reshape(ds.K, -1)
+    assert L.max(axis=1).min() <= 0.5 + 1e-15 or refsem  # capped elements at the discontinuities
+    g.close()
+    o.close()
 
 
 @pytest.mark.parametrize("refsem", [True, False])

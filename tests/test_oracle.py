@@ -9,7 +9,14 @@ import pytest
 import p2de
 from p2de import abi, problems
 from p2de import solver as S
-from p2de.types import PositivityAndCellEntropyBound, PositivityBound, TVDAndCellEntropyBound, TVDBound
+from p2de.types import (
+    HennemannShockCapture,
+    PositivityAndCellEntropyBound,
+    PositivityBound,
+    SubcellLimiter,
+    TVDAndCellEntropyBound,
+    TVDBound,
+)
 
 from conftest import relerr
 from helpers import setup
@@ -185,6 +192,48 @@ def test_tvd_bounds_hold_after_a_stage():
     assert np.all(rho1 >= lb - tol) and np.all(rho1 <= ub + tol)
     L = o.get_field(abi.FIELD_L_LOCAL, 2)
     assert L.min() < 1.0  # the bounds are active somewhere
+
+
+def with_shock_capture(param, a=0.5, c=1.8):
+    from dataclasses import replace
+
+    return replace(param, rhs_limiter=SubcellLimiter(bound=param.rhs_limiter.bound,
+                                                      shockcapture=HennemannShockCapture(a=a, c=c)))
+
+
+def test_shock_capture_blending_of_a_free_stream():
+    """A constant state has only the constant mode: smoothness 0, so alpha = alphaE0 and
+    every factor is 1 - 1e-4 (shock_capture.jl:118-137) when no bound is active."""
+    from dataclasses import replace
+
+    param, ic, bcf = _constant_state_problem(N=3)
+    param = replace(with_shock_capture(param), reference_semantics=False)
+    md = p2de.uniform_mesh(param.N, *param.K, param.xL, param.xR)
+    bc = bcf(param, md)
+    desc = S.make_descriptor(param, md, bc)
+    U0 = S.evaluate_initial_condition(param, md, ic)
+    o = Oracle(desc, nthreads=1)
+    o.set_Uq(U0)
+    o.rhs(0.0, 1e-3, 2)
+    L = o.get_field(abi.FIELD_L_LOCAL, 2)
+    np.testing.assert_allclose(L, 1.0 - 1.0 / (1.0 + 9999.0), rtol=1e-14)
+
+
+def test_shock_capture_caps_factors_at_shocks():
+    param, md, bc, desc, U0 = setup(problems.riemann2d, N=3, Kx=8, Ky=8, T=0.2, seed=2, reference_semantics=False)
+    o0 = Oracle(desc, nthreads=2)
+    o0.set_Uq(U0)
+    o0.rhs(0.0, 1e-3, 2)
+    L0 = o0.get_field(abi.FIELD_L_LOCAL, 2).reshape(desc.K, -1)
+    ps = with_shock_capture(param)
+    o = Oracle(S.make_descriptor(ps, md, bc), nthreads=2)
+    o.set_Uq(U0)
+    o.rhs(0.0, 1e-3, 2)
+    L = o.get_field(abi.FIELD_L_LOCAL, 2).reshape(desc.K, -1)
+    assert np.all(L <= L0 + 1e-15) and np.all(L >= 0)
+    Lmax = L.max(axis=1)
+    assert Lmax.min() <= 0.5 + 1e-15  # elements at the discontinuities get alphamax
+    assert Lmax.max() > 0.99          # smooth elements are barely capped
 
 
 def test_reference_semantics_give_low_order_rhs():
