@@ -774,9 +774,6 @@ int p2de_autotune(p2de_solver* s, int32_t* best_epb, double* best_ms) {
   std::vector<int> cand;
   for (int e : {1, 2, 3, 4, 6, 8, 12, 16, 24, 32, edef})
     if (e <= emax && std::find(cand.begin(), cand.end(), e) == cand.end()) cand.push_back(e);
-  cudaEvent_t e0, e1;
-  CK(cudaEventCreate(&e0));
-  CK(cudaEventCreate(&e1));
   double sc[S_NSCAL] = {0};
   CK(cudaMemcpyAsync(sc, s->scal, sizeof sc, cudaMemcpyDeviceToHost, s->stream));
   CK(cudaStreamSynchronize(s->stream));
@@ -787,6 +784,11 @@ int p2de_autotune(p2de_solver* s, int32_t* best_epb, double* best_ms) {
   CK(cudaMemcpyAsync(s->scal, sc, sizeof sc, cudaMemcpyHostToDevice, s->stream));
   int best = edef;
   double bms = 1e30;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  // the timings; whatever they return, the events go and the scalars come back below
+  auto timings = [&]() -> int {
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
   for (int e : cand) {
     StageArgs a = s->base;
     a.epb = e;
@@ -809,10 +811,14 @@ int p2de_autotune(p2de_solver* s, int32_t* best_epb, double* best_ms) {
       best = e;
     }
   }
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
+  return P2DE_OK;
+  };
+  const int rt = timings();
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
   CK(cudaMemcpyAsync(s->scal, keep, sizeof keep, cudaMemcpyHostToDevice, s->stream));
   CK(cudaStreamSynchronize(s->stream));
+  if (rt != P2DE_OK) return rt;
   int rc = p2de_set_elements_per_block(s, best);
   if (best_epb) *best_epb = best;
   if (best_ms) *best_ms = bms;

@@ -635,12 +635,13 @@ int p2de_batch_autotune(p2de_batch* b, int32_t best_epb[5]) {
   }
   b->tasks_dirty = true;
   BCK(cudaMemcpyAsync(b->d_scal, sc.data(), sizeof(double) * sc.size(), cudaMemcpyHostToDevice, b->stream));
-  cudaEvent_t e0, e1;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  unsigned* counter = b->d_counters + 6;
+  // the timings; whatever they return, the events go and the scalars come back below
+  auto timings = [&]() -> int {
   BCK(cudaEventCreate(&e0));
   BCK(cudaEventCreate(&e1));
-  int rc = P2DE_OK;
-  unsigned* counter = b->d_counters + 6;
-  for (int n1d = 2; n1d <= kMaxN1D && rc == P2DE_OK; ++n1d) {
+  for (int n1d = 2; n1d <= kMaxN1D; ++n1d) {
     bool present = false;
     for (int s = 0; s < b->max_solves; ++s) present |= b->slots[s].active && b->slots[s].n1d == n1d;
     if (!present) continue;
@@ -683,8 +684,11 @@ int p2de_batch_autotune(p2de_batch* b, int32_t best_epb[5]) {
     b->epb[n1d] = best;
     if (best_epb) best_epb[n1d - 2] = best;
   }
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
+  return P2DE_OK;
+  };
+  const int rc = timings();
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
   BCK(cudaMemcpyAsync(b->d_scal, keep.data(), sizeof(double) * keep.size(), cudaMemcpyHostToDevice, b->stream));
   BCK(cudaStreamSynchronize(b->stream));  // the host vectors above are temporaries
   return rc;

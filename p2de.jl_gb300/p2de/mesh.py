@@ -166,3 +166,19 @@ def make_periodic(md: MeshData, periodic=(True, True)) -> MeshData:
         sides["top"] = np.zeros(0, dtype=np.int64)
     mapB = np.sort(md.mapM[mapP == md.mapM])
     return replace(md, mapP=mapP, mapB=mapB, sides=sides)
+
+
+def rotated(md: MeshData, theta: float) -> MeshData:
+    """The same elements and connectivity with every node rotated by theta about the
+    origin: affine elements whose geometric factors have sxJ, ryJ != 0 (the general,
+    not axis-aligned, case of the kernels)."""
+    c, s = np.cos(theta), np.sin(theta)
+    x, y = c * md.x - s * md.y, s * md.x + c * md.y
+    xf, yf = c * md.xf - s * md.yf, s * md.xf + c * md.yf
+    g = md.geom.copy()
+    rxJ, syJ = md.geom[:, 1], md.geom[:, 4]  # hy/2, hx/2 of the axis-aligned element
+    g[:, 1] = c * rxJ      # rxJ =  ys
+    g[:, 2] = -s * syJ     # sxJ = -yr
+    g[:, 3] = s * rxJ      # ryJ = -xs
+    g[:, 4] = c * syJ      # syJ =  xr
+    return replace(md, x=x, y=y, xf=xf, yf=yf, geom=g)

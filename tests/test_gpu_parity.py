@@ -113,6 +113,84 @@ def test_rhs_modes(nstage, bound, refsem):
     compare_rhs(param, md, desc, U0, dt=2e-4, nstage=nstage, tol=tol)
 
 
+def rotated_setup(problem, theta, **kw):
+    import p2de
+
+    param, ic, bcf = problem(**kw)[:3]
+    md = p2de.mesh.rotated(p2de.uniform_mesh(param.N, *param.K, param.xL, param.xR), theta)
+    bc = bcf(param, md)
+    desc = S.make_descriptor(param, md, bc)
+    U0 = S.evaluate_initial_condition(param, md, ic)
+    return param, md, bc, desc, U0
+
+
+# On elements that are not axis-aligned, some limiter decisions are rounding-level: under
+# the reference's semantics (the density bound with Urho = 0) and at contact-like fronts
+# a one-ulp change of the input flips subcell factors and moves rhsU at O(1), in the
+# oracle as much as on the GPU. Exact parity is asserted where the problem is well
+# conditioned (the strong vortex under the intended semantics: a one-ulp input change
+# moves rhsU by < 1e-12); elsewhere the limiter-independent fields must agree and the
+# limited result must keep its properties.
+ROTATED_TOL = {"pos": TOL, "cell": 1e-10, "tvd": 1e-10, "tvd-cell": 1e-10}
+
+
+@pytest.mark.parametrize("nstage", [1, 2, 3])
+@pytest.mark.parametrize("bound", list(BOUNDS))
+def test_rotated_elements_rhs(nstage, bound):
+    """Elements with sxJ, ryJ != 0: the general (not axis-aligned) paths of every phase."""
+    param, md, bc, desc, U0 = rotated_setup(problems.isentropic_vortex, 0.35, N=3, Kx=6, Ky=5, T=0.05,
+                                            strength=8.5, bound=BOUNDS[bound], reference_semantics=False)
+    compare_rhs(param, md, desc, U0, dt=2e-4, nstage=nstage, tol=ROTATED_TOL[bound])
+
+
+def test_rotated_elements_rhs_shear_layer():
+    param, md, bc, desc, U0 = rotated_setup(problems.kelvin_helmholtz, 0.35, N=3, Kx=8, Ky=7, T=0.1,
+                                            bound=PositivityBound(), reference_semantics=False)
+    compare_rhs(param, md, desc, U0, dt=2e-4, nstage=2)
+
+
+@pytest.mark.parametrize("bound", ["pos", "cell"])
+def test_rotated_elements_reference_semantics(bound):
+    """Reference semantics on rotated elements: the low- and high-order parts agree to
+    rounding; the subcell factors stay in [0, 1] and the limited update keeps the density
+    positive."""
+    param, md, bc, desc, U0 = rotated_setup(problems.kelvin_helmholtz, 0.35, N=3, Kx=8, Ky=7, T=0.1,
+                                            bound=BOUNDS[bound], reference_semantics=True)
+    o = oracle_for(desc, U0)
+    g = gpu_for(param, md, desc, U0)
+    dt = 2e-4
+    dto = o.rhs(0.0, dt, 1)
+    dtg = S.rhs_bang(None, g, None, p2de.TimeParam(0.0, dt, 1))
+    assert abs(dtg - dto) <= 1e-13 * abs(dto)
+    for f in (abi.FIELD_RHSL, abi.FIELD_RHSH, abi.FIELD_BF_L, abi.FIELD_BF_H, abi.FIELD_RHSXYL, abi.FIELD_RHSXYH):
+        assert relerr(g.get_field(f), o.get_field(f), floor=1e-300) <= TOL, f
+    L = g.get_field(abi.FIELD_L_LOCAL, 1)
+    assert np.all((L >= 0) & (L <= 1))
+    rhsU = g.get_field(abi.FIELD_RHSU).reshape(desc.K, -1, 4)
+    assert np.all(np.isfinite(rhsU))
+    U1 = np.reshape(U0, rhsU.shape) + dtg * rhsU
+    assert U1[..., 0].min() > 0
+    g.close()
+    o.close()
+
+
+@pytest.mark.parametrize("N", [1, 2, 4, 5])
+@pytest.mark.parametrize("bound", ["pos", "cell"])
+def test_rotated_elements_steps(N, bound):
+    param, md, bc, desc, U0 = rotated_setup(problems.isentropic_vortex, -0.6, N=N, Kx=6, Ky=5, T=0.05,
+                                            strength=8.5, bound=BOUNDS[bound], reference_semantics=False)
+    o = oracle_for(desc, U0)
+    g = gpu_for(param, md, desc, U0)
+    to, tg = 0.0, 0.0
+    for _ in range(4):
+        to, _ = o.step(to)
+        tg, _ = S.ssp33_step(g, tg)
+    assert abs(tg - to) <= 1e-13 * abs(to)
+    assert relerr(g.get_field(abi.FIELD_UQ), o.get_field(abi.FIELD_UQ)) <= ROTATED_TOL[bound]
+    g.close()
+    o.close()
+
+
 @pytest.mark.parametrize("N", [1, 2, 3, 4, 5])
 @pytest.mark.parametrize("bound,refsem", [("pos", False), ("cell", True), ("tvd", True)])
 def test_shock_capture_matches(N, bound, refsem):

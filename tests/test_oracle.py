@@ -112,6 +112,19 @@ def test_free_stream_preservation(N):
         assert np.max(np.abs(o.get_field(f))) < 1e-11
 
 
+def test_free_stream_on_rotated_elements():
+    """Affine elements with sxJ, ryJ != 0 (every node rotated): a constant state stays
+    constant (the general geometric path of the oracle)."""
+    param, ic, bcf = _constant_state_problem(N=3)
+    md = p2de.mesh.rotated(p2de.uniform_mesh(param.N, *param.K, param.xL, param.xR), 0.4)
+    desc = S.make_descriptor(param, md, bcf(param, md))
+    U0 = S.evaluate_initial_condition(param, md, ic)
+    o = Oracle(desc, nthreads=1)
+    o.set_Uq(U0)
+    o.rhs(0.0, 1e-3, 1)
+    assert np.abs(o.get_field(abi.FIELD_RHSU)).max() < 1e-12
+
+
 def test_conservation_periodic():
     param, md, bc, desc, U0 = setup(problems.kelvin_helmholtz, N=3, Kx=6, Ky=6, T=0.1)
     o = Oracle(desc, nthreads=2)
