@@ -501,13 +501,62 @@ def run_mixed_report(args):
                       "data": "synthetic", "report": res}), flush=True)
 
 
+def run_limiter_report(args):
+    """The double Mach reflection 480x120 N=3 step (FP64) under every limiter the one-solve
+    path has, in both bound semantics: DOF-stage updates/s and ms per step for each, same
+    steps and warm-up, autotuned elements per block."""
+    import torch
+
+    from p2de import problems
+    from p2de.types import (
+        HennemannShockCapture,
+        PositivityAndCellEntropyBound,
+        PositivityAndMinEntropyBound,
+        PositivityAndRelaxedCellEntropyBound,
+        PositivityAndRelaxedMinEntropyBound,
+        PositivityBound,
+        SubcellLimiter,
+        TVDAndMinEntropyBound,
+        TVDBound,
+        ZhangShuLimiter,
+    )
+
+    torch.cuda.set_device(0)
+    limiters = {
+        "positivity-and-cell-entropy (bench default)": SubcellLimiter(bound=PositivityAndCellEntropyBound()),
+        "positivity": SubcellLimiter(bound=PositivityBound()),
+        "positivity + hennemann": SubcellLimiter(bound=PositivityBound(), shockcapture=HennemannShockCapture()),
+        "tvd": SubcellLimiter(bound=TVDBound()),
+        "min-entropy": SubcellLimiter(bound=PositivityAndMinEntropyBound()),
+        "relaxed-min-entropy": SubcellLimiter(bound=PositivityAndRelaxedMinEntropyBound()),
+        "tvd-and-min-entropy": SubcellLimiter(bound=TVDAndMinEntropyBound()),
+        "relaxed-cell-entropy(0.5)": SubcellLimiter(bound=PositivityAndRelaxedCellEntropyBound(beta=0.5)),
+        "zhang-shu": ZhangShuLimiter(),
+    }
+    res = {}
+    for name, lim in limiters.items():
+        rep = {}
+        for refsem in (True, False):
+            param, ic, bcf = problems.double_mach_reflection(N=3, Kx=480, Ky=120, T=0.2, rhs_limiter=lim,
+                                                             reference_semantics=refsem)
+            md, bc, desc, U0 = build_descriptor(param, ic, bcf)
+            sec, U, n = _timed_alone(param, md, desc, U0, args.warmup, args.steps, tune=not args.no_autotune)
+            rep["reference_semantics" if refsem else "intended"] = {
+                "dof_stage_per_s": desc.K * desc.Nq * 3 * n / sec, "ms_per_step": 1e3 * sec / n, "steps": n,
+                "min_rho": float(np.reshape(U, (-1, 4))[:, 0].min())}
+        res[name] = rep
+    print(json.dumps({"metric": METRIC, "unit": UNIT, "workload": "double Mach reflection 480x120, N=3, FP64, per limiter",
+                      "data": "synthetic", "report": res}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="dmr", choices=["dmr", "kh256", "batch64", "serve", "mixed-report"])
+    ap.add_argument("--workload", default="dmr",
+                    choices=["dmr", "kh256", "batch64", "serve", "mixed-report", "limiter-report"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed", "mixed-acc64"])
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -532,6 +581,8 @@ def main():
         return run_serve(args)
     if args.workload == "mixed-report":
         return run_mixed_report(args)
+    if args.workload == "limiter-report":
+        return run_limiter_report(args)
 
     import torch
 

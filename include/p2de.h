@@ -25,7 +25,7 @@
 extern "C" {
 #endif
 
-#define P2DE_ABI_VERSION 2
+#define P2DE_ABI_VERSION 3
 
 typedef enum p2de_status {
   P2DE_OK = 0,
@@ -54,8 +54,28 @@ typedef enum p2de_bound_type {
   P2DE_BOUND_TVD = 2,                         /* TVDBound (subcell.jl:112-141): density in the
                                                  min/max of the low-order density over the
                                                  node and its low_order_stencil */
-  P2DE_BOUND_TVD_AND_CELL_ENTROPY = 3         /* TVDAndCellEntropyBound */
+  P2DE_BOUND_TVD_AND_CELL_ENTROPY = 3,        /* TVDAndCellEntropyBound */
+  /* modified specific entropy phi = rhoe rho^(-gamma) >= Lphi - POSTOL by bisection
+     (limiter_utils.jl:19-24,43-50), Lphi the min of phi over the node and its
+     low_order_stencil (subcell.jl:53-72) */
+  P2DE_BOUND_POSITIVITY_AND_MIN_ENTROPY = 4,          /* PositivityAndMinEntropyBound */
+  P2DE_BOUND_POSITIVITY_AND_RELAXED_MIN_ENTROPY = 5,  /* ...RelaxedMinEntropyBound: Lphi blended
+                                                         with the global initial min of phi by
+                                                         the smoothness factor (subcell.jl:937-956) */
+  P2DE_BOUND_POSITIVITY_AND_RELAXED_CELL_ENTROPY = 6, /* ...RelaxedCellEntropyBound(beta): entropy
+                                                         target scaled by 1 - beta eps_k (:750-753) */
+  P2DE_BOUND_TVD_AND_MIN_ENTROPY = 7,                 /* TVDAndMinEntropyBound */
+  P2DE_BOUND_TVD_AND_RELAXED_MIN_ENTROPY = 8,         /* TVDAndRelaxedMinEntropyBound */
+  P2DE_BOUND_TVD_AND_RELAXED_CELL_ENTROPY = 9         /* TVDAndRelaxedCellEntropyBound(beta) */
 } p2de_bound_type;
+
+/* RHS limiters (Solver.jl:72-91). */
+typedef enum p2de_rhs_limiter {
+  P2DE_LIMITER_SUBCELL = 0,   /* SubcellLimiter(bound, shockcapture) */
+  P2DE_LIMITER_ZHANG_SHU = 1  /* ZhangShuLimiter(shockcapture): one factor per element from
+                                 the positivity bounds at its nodes (zhangshu.jl:4-45);
+                                 bound_type is not read */
+} p2de_rhs_limiter;
 
 /* Surface flux types (Solver.jl:19-22). Low order: LaxFriedrichsOnNodalVal only;
  * high order: LaxFriedrichsOnProjectedVal only. */
@@ -99,9 +119,10 @@ typedef struct p2de_param {
    * HennemannShockCapture(a, c), whose per-element blending factor
    * (shock_capture.jl:118-137) caps every subcell factor of the element. */
   int32_t shock_capture;
-  int32_t reserved_;               /* 0 */
+  int32_t rhs_limiter;             /* p2de_rhs_limiter */
   double shock_capture_a;
   double shock_capture_c;
+  double bound_beta;               /* beta of the Relaxed...CellEntropyBound types, else unused */
 } p2de_param;
 
 /* Mesh and boundary data. geom/mapP/mapI/mapO/Ival follow StateParam.bcdata
@@ -141,7 +162,9 @@ typedef enum p2de_field {
   P2DE_FIELD_BF_L = 6,    /* Nfp x K SVector{2,SVector{4}} */
   P2DE_FIELD_BF_H = 7,    /* Nfp x K SVector{2,SVector{4}} */
   P2DE_FIELD_L_LOCAL = 8, /* (Nq+N1D) x 2 x K for one stage */
-  P2DE_FIELD_RESW = 9     /* Nq x K SVector{4} */
+  P2DE_FIELD_RESW = 9,    /* Nq x K SVector{4} */
+  P2DE_FIELD_L = 10       /* K for one stage: ZhangShuLimiter's factor L[k, nstage] before the
+                             shock-capture cap (zhangshu.jl:44) */
 } p2de_field;
 
 typedef struct p2de_solver p2de_solver;

@@ -6,6 +6,7 @@
 //   rhs_low_graph_visc!          src/dg/rhs/low_order_graph_viscosity.jl:4-41
 //   rhs_fluxdiff!                src/dg/rhs/flux_differencing.jl:4-37
 //   apply_rhs_limiter!(Subcell)  src/dg/limiter/limiter.jl:20-56, subcell.jl, limiter_utils.jl
+//   apply_rhs_limiter!(ZhangShu) src/dg/limiter/limiter.jl:8-18, zhangshu.jl
 //   SSP33!                       src/timestepping/SSPRK33.jl:1-62
 // with the operators of initialize_operators (src/dg/init.jl:133-228) rebuilt from
 // the GLL rule for tensor-product quads. Loop orders, association orders and the
@@ -27,6 +28,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <initializer_list>
 #include <string>
 #include <vector>
 
@@ -387,17 +389,16 @@ struct Solver {
     VDMinv = Inv;
   }
 
-  // initialize_smoothness_indicator!(::Dim2) and update_blending_factor!
-  // (HennemannShockCapture) (shock_capture.jl:49-81, 92-103, 118-137): per element, the
-  // modal energies of rho*p; blending factor max(min(1 - alpha, 1), 1/2)
-  std::vector<double> blending_factor;
-  void update_blending_factor() {
-    blending_factor.assign(K, 1.0);
-    if (prm.shock_capture != 1) return;
-    const double a = prm.shock_capture_a, c = prm.shock_capture_c;
-    const double TN = a * std::pow(10.0, -c * std::pow((double)(N + 1), 0.25));
-    const double alphamax = 0.5, alphaE0 = 0.0001;
-    const double s_factor = std::log((1 - alphaE0) / alphaE0);
+  // initialize_smoothness_indicator!(::Dim2) (shock_capture.jl:47-81, 92-103): per
+  // element, the modal energies of rho*p through inv(VDM); smooth_indicator =
+  // max(E_N, E_{N-1}) / E. update_blending_factor! (HennemannShockCapture, :118-137):
+  // max(min(1 - alpha, 1), 1/2). update_smoothness_factor! (subcell.jl:927-956): 0 for
+  // the plain positivity/TVD/cell-entropy bounds, 1 for the min-entropy bounds, and for
+  // the relaxed bounds 0 / 1 / 1/2 - 1/2 sin(pi (s_k - s_0) / 2) with s_k the log10 of
+  // the indicator, s_0 = log10(N^-4) and kappa = 1.
+  std::vector<double> blending_factor, smooth_indicator, smooth_factor;
+  void update_smoothness() {
+    smooth_indicator.assign(K, 0.0);
 #pragma omp parallel for schedule(static)
     for (int k = 0; k < K; ++k) {
       std::vector<double> ind(Nq), modal(Nq);
@@ -420,9 +421,29 @@ struct Solver {
           total += energy;
           ++count;
         }
-      const double smooth = jmax(modeN / total, modeNm1 / total);
-      const double alpha = 1.0 / (1.0 + std::exp(-s_factor / TN * (smooth - TN)));
-      blending_factor[k] = jmax(jmin(1.0 - alpha, 1.0), alphamax);
+      smooth_indicator[k] = jmax(modeN / total, modeNm1 / total);
+    }
+    blending_factor.assign(K, 1.0);
+    if (prm.shock_capture == 1) {
+      const double a = prm.shock_capture_a, c = prm.shock_capture_c;
+      const double TN = a * std::pow(10.0, -c * std::pow((double)(N + 1), 0.25));
+      const double alphamax = 0.5, alphaE0 = 0.0001;
+      const double s_factor = std::log((1 - alphaE0) / alphaE0);
+      for (int k = 0; k < K; ++k) {
+        const double alpha = 1.0 / (1.0 + std::exp(-s_factor / TN * (smooth_indicator[k] - TN)));
+        blending_factor[k] = jmax(jmin(1.0 - alpha, 1.0), alphamax);
+      }
+    }
+    smooth_factor.assign(K, min_entropy() && !relaxed() ? 1.0 : 0.0);
+    if (relaxed()) {
+      const double kappa = 1.0;
+      const double s0 = std::log(1.0 / ((double)N * N * N * N)) / std::log(10.0);
+      for (int k = 0; k < K; ++k) {
+        const double sk = std::log(smooth_indicator[k]) / std::log(10.0);
+        if (sk < s0 - kappa) smooth_factor[k] = 0.0;
+        else if (sk > s0 + kappa) smooth_factor[k] = 1.0;
+        else smooth_factor[k] = 0.5 - 0.5 * std::sin(3.141592653589793 * (sk - s0) / (2 * kappa));
+      }
     }
   }
 
@@ -565,6 +586,7 @@ struct Solver {
     fstar_H.assign(nf, V2x4{});
     fstar_L.assign(nf, V2x4{});
     L_local.assign((size_t)(Nq + N1D) * 2 * K * Ns, 0.0);
+    L_elem.assign((size_t)K * Ns, 0.0);
     flux.assign(nh, V2x4{});
     Q0F1.assign(nq, V2x4{});
     wavespeed_f.assign(nf, 0.0);
@@ -984,16 +1006,91 @@ struct Solver {
     return limiting_param_bound_rho_rhoe(UL, P, bv[0], bv[1], bv[3], bv[4]);
   }
 
-  bool tvd() const { return prm.bound_type == P2DE_BOUND_TVD || prm.bound_type == P2DE_BOUND_TVD_AND_CELL_ENTROPY; }
+  // bound families (Solver.jl:47-62)
+  bool bound_is(std::initializer_list<int> l) const {
+    for (int b : l)
+      if (prm.bound_type == b) return true;
+    return false;
+  }
+  bool tvd() const {
+    return bound_is({P2DE_BOUND_TVD, P2DE_BOUND_TVD_AND_CELL_ENTROPY, P2DE_BOUND_TVD_AND_MIN_ENTROPY,
+                     P2DE_BOUND_TVD_AND_RELAXED_MIN_ENTROPY, P2DE_BOUND_TVD_AND_RELAXED_CELL_ENTROPY});
+  }
   bool cell_entropy() const {
-    return prm.bound_type == P2DE_BOUND_POSITIVITY_AND_CELL_ENTROPY || prm.bound_type == P2DE_BOUND_TVD_AND_CELL_ENTROPY;
+    return bound_is({P2DE_BOUND_POSITIVITY_AND_CELL_ENTROPY, P2DE_BOUND_TVD_AND_CELL_ENTROPY,
+                     P2DE_BOUND_POSITIVITY_AND_RELAXED_CELL_ENTROPY, P2DE_BOUND_TVD_AND_RELAXED_CELL_ENTROPY});
+  }
+  bool min_entropy() const {
+    return bound_is({P2DE_BOUND_POSITIVITY_AND_MIN_ENTROPY, P2DE_BOUND_POSITIVITY_AND_RELAXED_MIN_ENTROPY,
+                     P2DE_BOUND_TVD_AND_MIN_ENTROPY, P2DE_BOUND_TVD_AND_RELAXED_MIN_ENTROPY});
+  }
+  bool relaxed() const {
+    return bound_is({P2DE_BOUND_POSITIVITY_AND_RELAXED_MIN_ENTROPY, P2DE_BOUND_TVD_AND_RELAXED_MIN_ENTROPY,
+                     P2DE_BOUND_POSITIVITY_AND_RELAXED_CELL_ENTROPY, P2DE_BOUND_TVD_AND_RELAXED_CELL_ENTROPY});
+  }
+
+  // s_modified_ufun (compressible_Navier_Stokes.jl:80-85): rhoe rho^(-gamma)
+  double s_modified(const V4& U) const { return eq.rhoe_ufun(U) * std::pow(U[0], -eq.gamma); }
+
+  // limiting_param(::SubcellLimiter, min-entropy bounds) (limiter_utils.jl:19-24): the
+  // 5-tuple read as 5 names; the positivity factor, then bisection (nonlinear_solvers.jl:3-20)
+  // for phi(UL + l P) >= Lphi - POSTOL over [0, lpos] (limiting_param_bound_phi, :43-50)
+  double limiting_param_min_entropy(const V4& UL, const V4& P, const double bv[5]) const {
+    const double lpos = limiting_param_bound_rho_rhoe(UL, P, bv[0], bv[1], bv[3], bv[4]);
+    const double Lphi = bv[2];
+    auto f = [&](double l) { return s_modified(add(UL, scal(l, P))) >= Lphi - prm.POSTOL; };
+    double x_valid = 0.0, x_invalid = lpos;
+    if (f(x_invalid)) return x_invalid;
+    for (int iter = 0; iter <= 20; ++iter) {
+      const double x_new = 0.5 * (x_valid + x_invalid);
+      if (f(x_new)) x_valid = x_new;
+      else x_invalid = x_new;
+    }
+    return x_valid;
+  }
+
+  // low_order_stencil (limiter_utils.jl:222-231): the r-neighbours, then the s-neighbours,
+  // across an element face through quad_index_to_quad_index_P
+  void low_order_stencil(int q, int k, int kk[4], int qq[4]) const {
+    const int i = q % N1D, j = q / N1D;
+    if (i - 1 >= 0) { qq[0] = q - 1; kk[0] = k; } else qq[0] = quad_index_to_quad_index_P(q, k, 1, kk[0]);
+    if (i + 1 <= N) { qq[1] = q + 1; kk[1] = k; } else qq[1] = quad_index_to_quad_index_P(q, k, 1, kk[1]);
+    if (j - 1 >= 0) { qq[2] = q - N1D; kk[2] = k; } else qq[2] = quad_index_to_quad_index_P(q, k, 2, kk[2]);
+    if (j + 1 <= N) { qq[3] = q + N1D; kk[3] = k; } else qq[3] = quad_index_to_quad_index_P(q, k, 2, kk[3]);
+  }
+
+  // initialize_s_modified! (subcell.jl:21-35) and initialize_lower_bound!(::Dim2) (:53-72):
+  // Lphi = eps_k min(phi over the node and its stencil) + (1 - eps_k) min phi(initial)
+  std::vector<double> s_mod, lbound_s_modified;
+  double s_modified_min = 0.0;  // zeros(Float64, 1) until t == t0 at stage 1
+  void initialize_entropy_bounds(double t, int nstage) {
+    s_mod.assign((size_t)Nq * K, 0.0);
+    lbound_s_modified.assign((size_t)Nq * K, 0.0);
+#pragma omp parallel for schedule(static)
+    for (size_t i = 0; i < s_mod.size(); ++i) s_mod[i] = s_modified(Uq[i]);
+    if (t == prm.t0 && nstage == 1) {
+      double m = s_mod[0];
+      for (size_t i = 1; i < s_mod.size(); ++i) m = jmin(m, s_mod[i]);
+      s_modified_min = m;
+    }
+#pragma omp parallel for schedule(static)
+    for (int k = 0; k < K; ++k) {
+      const double epsk = smooth_factor[k];
+      for (int q = 0; q < Nq; ++q) {
+        int kk[4], qq[4];
+        low_order_stencil(q, k, kk, qq);
+        double lb = s_mod[q + (size_t)Nq * k];
+        for (int t4 = 0; t4 < 4; ++t4) lb = jmin(lb, s_mod[qq[t4] + (size_t)Nq * kk[t4]]);
+        lbound_s_modified[q + (size_t)Nq * k] = epsk * lb + (1 - epsk) * s_modified_min;
+      }
+    }
   }
 
   // quad_index_to_quad_index_P(::Dim2) (limiter_utils.jl:199-212): the volume node across
   // the face of boundary node q in `direction` (1: r, 2: s); q2fq lists the r-face first
   int quad_index_to_quad_index_P(int q, int k, int direction, int& kP) const {
     const int ir = q % N1D, is = q / N1D;
-    int faces[2], nf = 0;
+    int faces[4] = {0, 0, 0, 0}, nf = 0;
     if (ir == 0) faces[nf++] = is;
     if (ir == N) faces[nf++] = N1D + is;
     if (is == 0) faces[nf++] = 2 * N1D + ir;
@@ -1023,10 +1120,7 @@ struct Solver {
         for (int i = 0; i < N1D; ++i) {
           const int q = i + N1D * j;
           int kk[4], qq[4];
-          if (i - 1 >= 0) { qq[0] = q - 1; kk[0] = k; } else qq[0] = quad_index_to_quad_index_P(q, k, 1, kk[0]);
-          if (i + 1 <= N) { qq[1] = q + 1; kk[1] = k; } else qq[1] = quad_index_to_quad_index_P(q, k, 1, kk[1]);
-          if (j - 1 >= 0) { qq[2] = q - N1D; kk[2] = k; } else qq[2] = quad_index_to_quad_index_P(q, k, 2, kk[2]);
-          if (j + 1 <= N) { qq[3] = q + N1D; kk[3] = k; } else qq[3] = quad_index_to_quad_index_P(q, k, 2, kk[3]);
+          low_order_stencil(q, k, kk, qq);
           double lb = rhoL_tvd[q + (size_t)Nq * k], ub = lb;
           for (int s = 0; s < 4; ++s) {
             double v = rhoL_tvd[qq[s] + (size_t)Nq * kk[s]];
@@ -1038,14 +1132,15 @@ struct Solver {
         }
   }
 
-  void apply_rhs_limiter(double dt, int nstage) {
+  // apply_rhs_limiter!(::SubcellLimiter) (limiter.jl:20-56)
+  void apply_rhs_limiter(double t, double dt, int nstage) {
     const int s = nstage - 1;
     const int N1Dp1 = N1D + 1;
-    // update_blending_factor! (NoShockCapture: 1.0; HennemannShockCapture: per element);
-    // update_smoothness_factor! -> 0.0;
-    // initialize_entropy_bounds! -> lbound_s_modified = 0.0 (subcell.jl:4-6)
-    update_blending_factor();
-    const double lbound_s = 0.0;
+    // smoothness indicator, blending factor (NoShockCapture: 1.0), smoothness factor;
+    // initialize_entropy_bounds!: lbound_s_modified = 0.0 except for the min-entropy
+    // bounds (subcell.jl:4-19)
+    update_smoothness();
+    if (min_entropy()) initialize_entropy_bounds(t, nstage);
     if (tvd()) initialize_TVD_bounds(dt);
     // accumulate_f_bar!(::Dim2) (subcell.jl:163-206)
 #pragma omp parallel for schedule(static)
@@ -1104,10 +1199,11 @@ struct Solver {
           Lrho = lbound_rho[q + (size_t)Nq * k];
           Urho = ubound_rho[q + (size_t)Nq * k];
         }
-        double bv[5] = {Lrho, zeta * eq.rhoe_ufun(u), lbound_s, Urho, Urhoe};
+        const double Lphi = min_entropy() ? lbound_s_modified[q + (size_t)Nq * k] : 0.0;
+        double bv[5] = {Lrho, zeta * eq.rhoe_ufun(u), Lphi, Urho, Urhoe};
         V4 P;
         for (int c = 0; c < 4; ++c) P[c] = sgn * 4.0 * dt * dF[c] / wJ;
-        return limiting_param(u, P, bv);
+        return min_entropy() ? limiting_param_min_entropy(u, P, bv) : limiting_param(u, P, bv);
       };
       for (int sj = 0; sj < N1D; ++sj) {
         for (int si = 0; si < N1D; ++si) {
@@ -1262,12 +1358,16 @@ struct Solver {
       double sumx = 0.0;
       for (int sj = 0; sj < N1D; ++sj)
         for (int si = 1; si < N1D; ++si) sumx += Lx(si, sj) * dx[(si - 1) + N1Dm1 * sj];
+      // rhs_es: relaxed bounds scale the target by 1 - beta eps_k (subcell.jl:750-753)
+      const double scale = relaxed() ? 1 - prm.bound_beta * smooth_factor[k] : 1.0;
       double rhsx = sum_Bpsi[k][0] - sum_dvfbarL[k][0];
+      if (relaxed()) rhsx = scale * rhsx;
       double est_x = sumx - rhsx;
       double sumy = 0.0;
       for (int si = 0; si < N1D; ++si)
         for (int sj = 1; sj < N1D; ++sj) sumy += Ly(si, sj) * dy[si + N1D * (sj - 1)];
       double rhsy = sum_Bpsi[k][1] - sum_dvfbarL[k][1];
+      if (relaxed()) rhsy = scale * rhsy;
       double est_y = sumy - rhsy;
       double tolx = jmax(0.0, sum_dvfbarL[k][0] - sum_Bpsi[k][0]);
       double toly = jmax(0.0, sum_dvfbarL[k][1] - sum_Bpsi[k][1]);
@@ -1324,6 +1424,33 @@ struct Solver {
     }
   }
 
+  // apply_rhs_limiter!(::ZhangShuLimiter) (limiter.jl:8-18), apply_zhang_shu_limiter!
+  // (zhangshu.jl:4-25), zhang_shu_bound_limiter! (:35-45) with limiting_param
+  // (::ZhangShuLimiter) (limiter_utils.jl:4-8): bounds (zeta rhoL, zeta rhoeL, Inf, Inf)
+  std::vector<double> L_elem;  // L[k, nstage], K x Ns
+  void apply_zhang_shu(double dt, int nstage) {
+    const int s = nstage - 1;
+    update_smoothness();
+    const double zeta = prm.zeta;
+#pragma omp parallel for schedule(static)
+    for (int k = 0; k < K; ++k) {
+      double l = 1.0;
+      for (int i = 0; i < Nq; ++i) {
+        const size_t ik = i + (size_t)Nq * k;
+        const V4 uL = add(Uq[ik], scal(dt, rhsL[ik]));
+        const V4 P = scal(dt, sub(rhsH[ik], rhsL[ik]));
+        const double li = jmin(1.0, limiting_param_bound_rho_rhoe(uL, P, zeta * uL[0], zeta * eq.rhoe_ufun(uL), kInf, kInf));
+        l = jmin(l, li);
+      }
+      L_elem[k + (size_t)K * s] = l;
+      l = jmin(l, blending_factor[k]);
+      for (int i = 0; i < Nq; ++i) {
+        const size_t ik = i + (size_t)Nq * k;
+        rhsU[ik] = add(scal(1 - l, rhsL[ik]), scal(l, rhsH[ik]));
+      }
+    }
+  }
+
   // ---------------------------------------------------------------------------
   // rhs! (rhs.jl:5-13, 183-213)
   // ---------------------------------------------------------------------------
@@ -1345,7 +1472,8 @@ struct Solver {
         entropy_projection();
         double d = rhs_low_graph_visc(t, dt, nstage);
         rhs_fluxdiff(t);
-        apply_rhs_limiter(dt, nstage);
+        if (prm.rhs_limiter == P2DE_LIMITER_ZHANG_SHU) apply_zhang_shu(dt, nstage);
+        else apply_rhs_limiter(t, dt, nstage);
         return d;
       }
     }
@@ -1388,6 +1516,10 @@ int validate(const p2de_param* p, const p2de_mesh* m, std::string& err) {
   }
   if (!m->geom || !m->mapP) {
     err = "geom and mapP are required";
+    return P2DE_ERR_INVALID_ARGUMENT;
+  }
+  if (p->bound_type < 0 || p->bound_type > 9 || p->rhs_limiter < 0 || p->rhs_limiter > 1) {
+    err = "bound_type must be in 0..9 and rhs_limiter in 0..1";
     return P2DE_ERR_INVALID_ARGUMENT;
   }
   if (p->low_order_surface_flux != P2DE_FLUX_LAX_FRIEDRICHS_ON_NODAL_VAL ||
@@ -1524,6 +1656,11 @@ int oracle_get_field(oracle_solver* o, int field, int nstage, double* out) {
       break;
     }
     case P2DE_FIELD_RESW: cp4(s.resW); break;
+    case P2DE_FIELD_L: {
+      if (nstage < 1 || nstage > 3) return P2DE_ERR_INVALID_ARGUMENT;
+      std::memcpy(out, s.L_elem.data() + (size_t)s.K * (nstage - 1), sizeof(double) * s.K);
+      break;
+    }
     default: return P2DE_ERR_INVALID_ARGUMENT;
   }
   return P2DE_OK;

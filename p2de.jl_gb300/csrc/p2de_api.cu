@@ -82,6 +82,40 @@ __global__ void k_geom_table(const double* geom, int K, double* out) {
   geom_factor(geom + 5 * (size_t)k, q, out + (size_t)k * kGeomStride);
 }
 
+// initialize_s_modified! (subcell.jl:21-35): at t == t0, stage 1, the minimum of
+// phi = rhoe rho^(-gamma) over every node (NaN if any is NaN, as Julia's minimum). One
+// block of 1024 threads, so the result does not depend on the order of atomics.
+__global__ void __launch_bounds__(1024) k_phi_min(const double* Uq, size_t nodes, double gamma, const double* scal,
+                                                  double t0, double* out) {
+  if (scal[S_DONE] != 0.0 || scal[S_T] != t0) return;
+  __shared__ double wmin[32];
+  __shared__ int wnan[32];
+  double m = INFINITY;
+  int isn = 0;
+  for (size_t i = threadIdx.x; i < nodes; i += blockDim.x) {
+    const double* U = Uq + 4 * i;
+    const double v = s_modified(U[0], U[1], U[2], U[3], gamma);
+    if (isnan(v)) isn = 1;
+    else m = fmin(m, v);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    m = fmin(m, __shfl_xor_sync(0xffffffffu, m, o));
+    isn |= __shfl_xor_sync(0xffffffffu, isn, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    wmin[threadIdx.x >> 5] = m;
+    wnan[threadIdx.x >> 5] = isn;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
+      m = fmin(m, wmin[w]);
+      isn |= wnan[w];
+    }
+    *out = isn ? NAN : m;
+  }
+}
+
 double key_to_double(long long k) {
   long long b = k ^ ((k >> 63) & 0x7fffffffffffffffLL);
   double d;
@@ -136,9 +170,19 @@ cudaError_t launch_a_one(int n1d, const StageArgs& a, bool mixed, cudaStream_t s
   return cudaErrorInvalidValue;
 }
 // kernel A. The TVD bounds need every element's low-order density: a first launch stops
-// after the low-order RHS and stores them, then the full launch reads its stencils.
-int a_launches(const StageArgs& a) { return (a.flags & F_TVD) ? 2 : 1; }
+// after the low-order RHS and stores them, then the full launch reads its stencils. The
+// relaxed min-entropy bounds need the initial state's minimum of phi: at stage 1 a
+// one-block reduction runs first (it returns at once unless t == t0).
+bool needs_phi_min(const StageArgs& a) {
+  return (a.flags & F_MIN_ENTROPY) && (a.flags & F_RELAXED) && a.nstage == 1;
+}
+int a_launches(const StageArgs& a) { return ((a.flags & F_TVD) ? 2 : 1) + (needs_phi_min(a) ? 1 : 0); }
 cudaError_t launch_a_n1d(int n1d, const StageArgs& a, bool mixed, cudaStream_t st) {
+  if (needs_phi_min(a)) {
+    k_phi_min<<<1, 1024, 0, st>>>(a.Uq, (size_t)a.K * n1d * n1d, a.gamma, a.scal, a.t0, a.phimin);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
   if (a.flags & F_TVD) {
     StageArgs lo = a;
     lo.flags = (a.flags | F_LOW_ONLY) & ~(F_CFL | F_WRITE_DEBUG);
@@ -193,6 +237,8 @@ struct p2de_solver {
   OpTable* ops = nullptr;
   double *diag_partial = nullptr, *diag_out = nullptr, *exact = nullptr;  // diagnostics, on first use
   double* rhoL = nullptr;                                                  // TVD bounds only
+  double* Lelem = nullptr;                                                 // 3 x K ZhangShuLimiter factors
+  double* phimin = nullptr;                                                // initial min of phi
   int diag_nblocks = 0;
   StageArgs base{};
   int64_t launches = 0;
@@ -246,15 +292,18 @@ int flags_for(const p2de_solver* s, int nstage, bool update, bool debug) {
   }
   if ((f & F_DO_LOW) && nstage == 1) f |= F_CFL;
   if (s->axis_aligned) f |= F_AXIS_ALIGNED;
-  if (s->prm.reference_semantics) f |= F_REF_SEM;
-  if (s->prm.bound_type == P2DE_BOUND_POSITIVITY_AND_CELL_ENTROPY ||
-      s->prm.bound_type == P2DE_BOUND_TVD_AND_CELL_ENTROPY)
-    f |= F_CELL_ENTROPY;
-  if ((s->prm.bound_type == P2DE_BOUND_TVD || s->prm.bound_type == P2DE_BOUND_TVD_AND_CELL_ENTROPY) &&
-      (f & F_DO_LIMIT))
-    f |= F_TVD;
+  if (f & F_DO_LIMIT) {
+    if (s->prm.rhs_limiter == P2DE_LIMITER_ZHANG_SHU) {
+      f = (f & ~F_DO_LIMIT) | F_ZHANG_SHU;  // the bound type is not read
+    } else {
+      const int b = s->prm.bound_type;
+      f |= bound_flags(b);
+      // the min-entropy bounds read their 5-tuple with 5 names (limiter_utils.jl:19-24)
+      if (s->prm.reference_semantics && !(f & F_MIN_ENTROPY)) f |= F_REF_SEM;
+    }
+  }
   if (s->prm.precision == P2DE_PRECISION_MIXED_ACC64) f |= F_ACC64;
-  if (s->prm.shock_capture == 1 && (f & F_DO_LIMIT)) f |= F_SHOCK;
+  if (s->prm.shock_capture == 1 && (f & (F_DO_LIMIT | F_ZHANG_SHU))) f |= F_SHOCK;
   if (update) f |= F_UPDATE;
   if (debug) f |= F_WRITE_DEBUG;
   return f;
@@ -287,9 +336,14 @@ int enqueue_step(p2de_solver* s) {
 
 // launches of one step: the step begin, then per stage kernel A (twice for TVD bounds), B
 int step_launches(const p2de_solver* s) {
-  StageArgs a = s->base;
-  a.flags = flags_for(s, 2, true, false);
-  return 1 + 3 * (a_launches(a) + 1);
+  int n = 1;
+  for (int stage = 1; stage <= 3; ++stage) {
+    StageArgs a = s->base;
+    a.nstage = stage;
+    a.flags = flags_for(s, stage, true, false);
+    n += a_launches(a) + 1;
+  }
+  return n;
 }
 
 void free_all(p2de_solver* s) {
@@ -319,6 +373,7 @@ int p2de_field_count(int32_t N, int32_t K, int32_t field, int64_t* count) {
     case P2DE_FIELD_BF_L:
     case P2DE_FIELD_BF_H: *count = 8 * Nfp * K; break;
     case P2DE_FIELD_L_LOCAL: *count = (Nq + n) * 2 * K; break;
+    case P2DE_FIELD_L: *count = K; break;
     default: return P2DE_ERR_INVALID_ARGUMENT;
   }
   return P2DE_OK;
@@ -335,9 +390,10 @@ int p2de_initialize_DG(const p2de_param* prm, const p2de_mesh* mesh, int device,
       prm->high_order_surface_flux != P2DE_FLUX_LAX_FRIEDRICHS_ON_PROJECTED_VAL)
     return fail(nullptr, P2DE_ERR_UNSUPPORTED,
                 "surface fluxes: only LaxFriedrichsOnNodalVal (low order) and LaxFriedrichsOnProjectedVal (high order)");
-  if (prm->rhs_type < 0 || prm->rhs_type > 2 || prm->bound_type < 0 || prm->bound_type > 3 || prm->precision < 0 ||
-      prm->precision > 2 || prm->shock_capture < 0 || prm->shock_capture > 1)
-    return fail(nullptr, P2DE_ERR_INVALID_ARGUMENT, "rhs_type/bound_type/precision out of range");
+  if (prm->rhs_type < 0 || prm->rhs_type > 2 || prm->bound_type < 0 || prm->bound_type > 9 || prm->precision < 0 ||
+      prm->precision > 2 || prm->shock_capture < 0 || prm->shock_capture > 1 || prm->rhs_limiter < 0 ||
+      prm->rhs_limiter > 1)
+    return fail(nullptr, P2DE_ERR_INVALID_ARGUMENT, "rhs_type/bound_type/precision/rhs_limiter out of range");
   const int64_t n1 = prm->N + 1, Nfp = 4 * n1, Nq = n1 * n1;
   const int64_t nfk = Nfp * prm->K;
   // validate indices before anything reaches the device
@@ -457,6 +513,8 @@ int p2de_initialize_DG(const p2de_param* prm, const p2de_mesh* mesh, int device,
   DA(s->minbuf, 2);
   DA(s->status, 1);
   DA(s->counters, 8);
+  DA(s->Lelem, (size_t)3 * K);
+  DA(s->phimin, 1);
 #undef DA
   auto up = [&](void* dst, const void* src, size_t bytes) {
     return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s->stream);
@@ -519,7 +577,10 @@ int p2de_initialize_DG(const p2de_param* prm, const p2de_mesh* mesh, int device,
   a.status = s->status;
   a.counters = s->counters;
   set_shock_capture(a, prm->N, prm->shock_capture_a, prm->shock_capture_c);
-  if (prm->bound_type == P2DE_BOUND_TVD || prm->bound_type == P2DE_BOUND_TVD_AND_CELL_ENTROPY) {
+  set_bound_constants(a, prm->N, prm->t0, prm->POSTOL, prm->bound_beta);
+  a.Lelem = s->Lelem;
+  a.phimin = s->phimin;
+  if (bound_flags(prm->bound_type) & F_TVD) {
     if (dalloc(s, &s->rhoL, (size_t)Nq * prm->K) != cudaSuccess) return bail(P2DE_ERR_OUT_OF_MEMORY);
     a.rhoL = s->rhoL;
   }
@@ -563,6 +624,10 @@ int p2de_get_field(p2de_solver* s, int32_t field, int32_t nstage, double* out) {
     case P2DE_FIELD_L_LOCAL:
       if (nstage < 1 || nstage > 3) return fail(s, P2DE_ERR_INVALID_ARGUMENT, "nstage %d", nstage);
       src = s->Lfin + (size_t)(nstage - 1) * cnt;
+      break;
+    case P2DE_FIELD_L:
+      if (nstage < 1 || nstage > 3) return fail(s, P2DE_ERR_INVALID_ARGUMENT, "nstage %d", nstage);
+      src = s->Lelem + (size_t)(nstage - 1) * cnt;
       break;
   }
   CK(cudaSetDevice(s->device));

@@ -25,7 +25,10 @@ enum : int {
   F_ACC64 = 1 << 11,        // FP32 kernel: pair fluxes gathered and lifted in FP64
   F_TVD = 1 << 12,          // TVD density bounds from the low-order densities in rhoL
   F_LOW_ONLY = 1 << 13,     // kernel A stops after the low-order RHS and stores rhoL
-  F_SHOCK = 1 << 14         // HennemannShockCapture blending factor caps the subcell factors
+  F_SHOCK = 1 << 14,        // HennemannShockCapture blending factor caps the subcell factors
+  F_ZHANG_SHU = 1 << 15,    // ZhangShuLimiter: one factor per element, rhsU written by kernel A
+  F_MIN_ENTROPY = 1 << 16,  // min-entropy bounds: bisection for phi >= Lphi - POSTOL
+  F_RELAXED = 1 << 17       // relaxed bounds: smoothness factor from the modal energies
 };
 
 // boundary codes per face node
@@ -72,6 +75,11 @@ struct StageArgs {
   double* rhoL;  // K x Nq low-order densities U + dt rhsL (TVD bounds only)
   const double* geomx;  // K x 16 geometry factors (geom_factor), or null: computed per launch
   double sc_TN, sc_q;   // HennemannShockCapture: TN and -log((1-1e-4)/1e-4) / TN
+  double* Lelem;        // 3 stages x K: ZhangShuLimiter factors (F_ZHANG_SHU)
+  double* phimin;       // [0]: min of phi = rhoe rho^-gamma over the state at t0, stage 1
+  double t0, POSTOL;
+  double s0;            // log10(N^-4), the centre of the smoothness ramp (subcell.jl:944)
+  double beta;          // relaxed cell-entropy bounds: target scale 1 - beta eps_k
 };
 
 // StageArgs shock-capture constants of update_blending_factor! (shock_capture.jl:123-126)
@@ -81,6 +89,32 @@ inline void set_shock_capture(StageArgs& a, int N, double sc_a, double sc_c) {
   const double s_factor = std::log((1 - alphaE0) / alphaE0);
   a.sc_TN = TN;
   a.sc_q = -s_factor / TN;
+}
+
+// flag bits of a SubcellLimiter bound type (p2de_bound_type, Solver.jl:47-62)
+inline int bound_flags(int bound_type) {
+  switch (bound_type) {
+    case 1: return F_CELL_ENTROPY;                            // PositivityAndCellEntropyBound
+    case 2: return F_TVD;                                     // TVDBound
+    case 3: return F_TVD | F_CELL_ENTROPY;                    // TVDAndCellEntropyBound
+    case 4: return F_MIN_ENTROPY;                             // PositivityAndMinEntropyBound
+    case 5: return F_MIN_ENTROPY | F_RELAXED;                 // PositivityAndRelaxedMinEntropyBound
+    case 6: return F_CELL_ENTROPY | F_RELAXED;                // PositivityAndRelaxedCellEntropyBound
+    case 7: return F_TVD | F_MIN_ENTROPY;                     // TVDAndMinEntropyBound
+    case 8: return F_TVD | F_MIN_ENTROPY | F_RELAXED;         // TVDAndRelaxedMinEntropyBound
+    case 9: return F_TVD | F_CELL_ENTROPY | F_RELAXED;        // TVDAndRelaxedCellEntropyBound
+    default: return 0;                                        // PositivityBound
+  }
+}
+
+// StageArgs constants of the min-entropy and relaxed bounds: t0 (the stage at which the
+// initial minimum of phi is taken), POSTOL, s0 = log10(N^-4) (subcell.jl:944, with N^-4
+// as Float64(N)^-4) and the relaxed cell-entropy beta
+inline void set_bound_constants(StageArgs& a, int N, double t0, double POSTOL, double beta) {
+  a.t0 = t0;
+  a.POSTOL = POSTOL;
+  a.s0 = std::log(1.0 / ((double)N * N * N * N)) / std::log(10.0);
+  a.beta = beta;
 }
 
 }  // namespace p2de

@@ -60,8 +60,9 @@ struct Cfg {
   static constexpr int SCR = cmax(cmax(NPL * 9, NPH * 8), 16 * NSF);
   // shared-memory doubles per element, kernel A; regions whose lifetimes (phases) do not
   // overlap share storage
-  static constexpr int O_GEO = 0;                  // 16: J, rxJ, sxJ, ryJ, syJ, |gr|, nr, |gs|, ns, 1/J
-  static constexpr int O_U = O_GEO + 16;           // 4 Nq
+  static constexpr int O_GEO = 0;                  // 18: J, rxJ, sxJ, ryJ, syJ, |gr|, nr, |gs|, ns, 1/J,
+                                                   // FP32 copies (12-14), blending (15), smoothness (16) factors
+  static constexpr int O_U = O_GEO + 18;           // 4 Nq
   static constexpr int O_PRIM = O_U + 4 * Nq;      // 6 Nq: primitives (P1-P6); uL[4], Lrhoe, 4dt/(wq J) (P8-P9)
   static constexpr int O_FLUX = O_PRIM + 6 * Nq;   // 8 Nq: nodal fluxes (P1-P4)
   static constexpr int O_RXYH = O_FLUX;            //       high-order rhsxy (P7-P8)
@@ -277,6 +278,33 @@ __device__ __forceinline__ double density_bound(double U0, double P0, double Lrh
   return l;
 }
 
+// s_modified_ufun (compressible_Navier_Stokes.jl:80-85): phi = rhoe rho^(-gamma), with
+// rhoe_ufun written as the reference writes it
+__device__ __forceinline__ double s_modified(double rho, double rhou, double rhov, double E, double gamma) {
+  const double rhoe = E - 0.5 * (rhou * rhou + rhov * rhov) / rho;
+  return rhoe * pow(rho, -gamma);
+}
+
+// limiting_param_bound_phi (limiter_utils.jl:43-50) through bisection (nonlinear_solvers.jl:3-20):
+// the l in [0, lpos] closest to lpos, on the grid of 21 halvings, with
+// phi(U + l P) >= thr (thr = Lphi - POSTOL); f(0) is assumed, as the reference does.
+__device__ __forceinline__ double bisect_phi(const double* U, const double* P, double lpos, double thr,
+                                             double gamma) {
+  auto f = [&](double l) {
+    return s_modified(U[0] + l * P[0], U[1] + l * P[1], U[2] + l * P[2], U[3] + l * P[3], gamma) >= thr;
+  };
+  double x_valid = 0.0, x_invalid = lpos;
+  if (f(x_invalid)) return x_invalid;
+  for (int iter = 0; iter <= 20; ++iter) {
+    const double x_new = 0.5 * (x_valid + x_invalid);
+    if (f(x_new))
+      x_valid = x_new;
+    else
+      x_invalid = x_new;
+  }
+  return x_valid;
+}
+
 // =====================================================================================
 // Kernel A
 // =====================================================================================
@@ -346,7 +374,7 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
     double* Ws = base + C::O_WS + 2 * m;
     Ws[0] = wavespeed_r(g, rr, G[6] * rhou + G[7] * rhov, E);
     Ws[1] = wavespeed_r(g, rr, G[9] * rhou + G[10] * rhov, E);
-    if (flags & F_SHOCK) base[C::O_LAMI + m] = rho * p;  // the indicator rho p (shock_capture.jl:92-103)
+    if (flags & (F_SHOCK | F_RELAXED)) base[C::O_LAMI + m] = rho * p;  // the indicator rho p (shock_capture.jl:92-103)
     if (do_high) {
       if (sizeof(TH) == 8) {
         double* Pm = base + C::O_PRIM + 6 * m;
@@ -366,10 +394,11 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
   }
   __syncthreads();
 
-  // ---- P1b: HennemannShockCapture (shock_capture.jl:49-81, 118-137): modal energies of
-  //      the indicator through inv(VDM), smoothness max(E_N, E_{N-1}) / E, blending
-  //      factor max(min(1 - alpha, 1), 1/2) into G[15]
-  if (flags & F_SHOCK) {
+  // ---- P1b: smoothness indicator (shock_capture.jl:49-81): modal energies of the
+  //      indicator through inv(VDM), smoothness max(E_N, E_{N-1}) / E. Hennemann
+  //      blending factor max(min(1 - alpha, 1), 1/2) (:118-137) into G[15]; the relaxed
+  //      bounds' smoothness factor (update_smoothness_factor!, subcell.jl:937-956) into G[16]
+  if (flags & (F_SHOCK | F_RELAXED)) {
     for (int w = tid; w < Ke * Nq; w += bs) {
       const int e = w / Nq, i = w % Nq;
       double* base = sm + e * PE;
@@ -390,8 +419,22 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
           total += energy;
         }
       const double smooth = fmax(modeN / total, modeNm1 / total);
-      const double alpha = 1.0 / (1.0 + exp(a.sc_q * (smooth - a.sc_TN)));
-      base[C::O_GEO + 15] = fmax(fmin(1.0 - alpha, 1.0), 0.5);
+      if (flags & F_SHOCK) {
+        const double alpha = 1.0 / (1.0 + exp(a.sc_q * (smooth - a.sc_TN)));
+        base[C::O_GEO + 15] = fmax(fmin(1.0 - alpha, 1.0), 0.5);
+      }
+      if (flags & F_RELAXED) {
+        // kappa = 1; log(10, x) = log(x) / log(10)
+        const double sk = log(smooth) / log(10.0);
+        double eps;
+        if (sk < a.s0 - 1.0)
+          eps = 0.0;
+        else if (sk > a.s0 + 1.0)
+          eps = 1.0;
+        else
+          eps = 0.5 - 0.5 * sin(3.141592653589793 * (sk - a.s0) / 2.0);
+        base[C::O_GEO + 16] = eps;
+      }
     }
     __syncthreads();
   }
@@ -849,6 +892,47 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
       a.BFH[(size_t)k0 * Nfp * 8 + w] = sm[e * PE + C::O_BFH + r];
     }
   }
+  if (flags & F_ZHANG_SHU) {
+    // ---- ZhangShuLimiter (zhangshu.jl:4-45): per node, the largest l in [0, 1] with
+    //      uL + l P inside (zeta rhoL, zeta rhoeL, Inf, Inf), uL = U + dt rhsL,
+    //      P = dt (rhsH - rhsL); L[k] = the element's min; rhsU = (1 - l) rhsL + l rhsH
+    //      with l = min(L[k], blending factor)
+    for (int w = tid; w < Ke * Nq; w += bs) {
+      int e = w / Nq, m = w % Nq;
+      double* base = sm + e * PE;
+      const double* U = base + C::O_U + 4 * m;
+      const double* rl = base + C::O_RHSL + 4 * m;
+      const double* R = base + C::O_RXYH + 8 * m;
+      double uL[4], P[4];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        uL[c] = low_update(U[c], dt_lim, rl[c]);
+        P[c] = dt_lim * ((R[c] + R[4 + c]) - rl[c]);
+      }
+      const double Lrhoe = a.zeta * fma(-0.5, (uL[1] * uL[1] + uL[2] * uL[2]) * rcp(uL[0]), uL[3]);
+      double l = density_bound(uL[0], P[0], a.zeta * uL[0], __longlong_as_double(0x7ff0000000000000LL), false, 0.0);
+      l = fmin(l, rhoe_quadratic_solve(uL, P, Lrhoe, a.ZEROTOL));
+      base[C::O_SCR + m] = fmin(1.0, l);
+    }
+    __syncthreads();
+    for (int e = tid; e < Ke; e += bs) {
+      double* base = sm + e * PE;
+      double l = 1.0;
+      for (int m = 0; m < Nq; ++m) l = fmin(l, base[C::O_SCR + m]);
+      a.Lelem[(size_t)(a.nstage - 1) * a.K + k0 + e] = l;
+      base[C::O_SCR + Nq] = (flags & F_SHOCK) ? fmin(l, base[C::O_GEO + 15]) : l;
+    }
+    __syncthreads();
+    for (int w = tid; w < Ke * Nq * 4; w += bs) {
+      int e = w / (Nq * 4), r = w % (Nq * 4);
+      int m = r / 4, c = r % 4;
+      const double* base = sm + e * PE;
+      const double l = base[C::O_SCR + Nq];
+      const double* R = base + C::O_RXYH + 8 * m;
+      a.rhsU[(size_t)k0 * Nq * 4 + w] = (1.0 - l) * base[C::O_RHSL + r] + l * (R[c] + R[4 + c]);
+    }
+    return;
+  }
   if (!(flags & F_DO_LIMIT)) return;
 
   // ---- P8: subcell flux prefix sums (accumulate_f_bar!(::Dim2), subcell.jl:163-206)
@@ -893,32 +977,31 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
     uL[5] = (4.0 * dt_lim) * base[C::O_WS + 2 * m + 1];  // 4 dt / (wq J)
     // density bounds (rho_bound, subcell.jl:352-387): Lrho, rho/2, Urho (rl is read above)
     double* lim = base + C::O_RHSL + 4 * m;
+    const int ir = m % n, is = m / n, k = k0 + e;
+    // global node index of stencil member t of low_order_stencil (limiter_utils.jl:222-231):
+    // r-neighbours, then s-neighbours, across a face through quad_index_to_quad_index_P
+    // (:199-212), whose q2fq lists the r-face first
+    auto stencil = [&](int t) -> size_t {
+      const int dir = t >> 1, up = t & 1;  // 0: r, 1: s; lower or upper neighbour
+      const int c = dir == 0 ? ir : is;
+      if (up ? c < n - 1 : c > 0) return (size_t)k * Nq + m + (dir == 0 ? 1 : n) * (up ? 1 : -1);
+      // the face of this node in direction dir (a node on one face has only that one)
+      int f;
+      if (dir == 0 && (ir == 0 || ir == n - 1)) f = ir == 0 ? is : n + is;
+      else if (dir == 1 && (is == 0 || is == n - 1)) f = is == 0 ? 2 * n + ir : 3 * n + ir;
+      else f = ir == 0 ? is : (ir == n - 1 ? n + is : (is == 0 ? 2 * n + ir : 3 * n + ir));
+      const int lin = a.nbr[(size_t)k * Nfp + f];
+      const int kP = lin / Nfp, iP = lin % Nfp, sP = iP / n, tP = iP % n;
+      const int qP = sP == 0 ? n * tP : sP == 1 ? (n - 1) + n * tP : sP == 2 ? tP : tP + n * (n - 1);
+      return (size_t)kP * Nq + qP;
+    };
     if (flags & F_TVD) {
-      // min/max of the low-order density over the node and its low_order_stencil
-      // (limiter_utils.jl:222-231): r-neighbours, then s-neighbours, across a face through
-      // quad_index_to_quad_index_P (:199-212), whose q2fq lists the r-face first
-      const int ir = m % n, is = m / n, k = k0 + e;
+      // min/max of the low-order density over the node and its stencil (subcell.jl:112-141)
       const double* rl_g = a.rhoL;
       double lb = rl_g[(size_t)k * Nq + m], ub = lb;
 #pragma unroll
       for (int t = 0; t < 4; ++t) {
-        const int dir = t >> 1, up = t & 1;  // 0: r, 1: s; lower or upper neighbour
-        const int c = dir == 0 ? ir : is;
-        size_t idx;
-        if (up ? c < n - 1 : c > 0) {
-          idx = (size_t)k * Nq + m + (dir == 0 ? 1 : n) * (up ? 1 : -1);
-        } else {
-          // the face of this node in direction dir (a node on one face has only that one)
-          int f;
-          if (dir == 0 && (ir == 0 || ir == n - 1)) f = ir == 0 ? is : n + is;
-          else if (dir == 1 && (is == 0 || is == n - 1)) f = is == 0 ? 2 * n + ir : 3 * n + ir;
-          else f = ir == 0 ? is : (ir == n - 1 ? n + is : (is == 0 ? 2 * n + ir : 3 * n + ir));
-          const int lin = a.nbr[(size_t)k * Nfp + f];
-          const int kP = lin / Nfp, iP = lin % Nfp, sP = iP / n, tP = iP % n;
-          const int qP = sP == 0 ? n * tP : sP == 1 ? (n - 1) + n * tP : sP == 2 ? tP : tP + n * (n - 1);
-          idx = (size_t)kP * Nq + qP;
-        }
-        const double v = rl_g[idx];
+        const double v = rl_g[stencil(t)];
         lb = fmin(lb, v);
         ub = fmax(ub, v);
       }
@@ -927,6 +1010,22 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
     } else {
       lim[0] = a.zeta * uL[0];
       lim[2] = __longlong_as_double(0x7ff0000000000000LL);
+    }
+    if (flags & F_MIN_ENTROPY) {
+      // initialize_lower_bound!(::Dim2) (subcell.jl:53-72): Lphi = eps_k min(phi over the
+      // node and its stencil) + (1 - eps_k) phi_min; eps_k = 1 unless relaxed; the
+      // bisection's threshold Lphi - POSTOL in lim[3]
+      double lb = s_modified(U[0], U[1], U[2], U[3], a.gamma);
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        const double* Un = a.Uq + 4 * stencil(t);
+        lb = fmin(lb, s_modified(Un[0], Un[1], Un[2], Un[3], a.gamma));
+      }
+      if (flags & F_RELAXED) {
+        const double eps = base[C::O_GEO + 16];
+        lb = eps * lb + (1 - eps) * a.phimin[0];
+      }
+      lim[3] = lb - a.POSTOL;
     }
     lim[1] = 0.5 * uL[0];
   }
@@ -1005,6 +1104,8 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
     // density bound) under the reference semantics, else Inf, for which it returns 1.0
     const double Urhoe = upper0 ? base[C::O_RHSL + 4 * m + 2] : __longlong_as_double(0x7ff0000000000000LL);
     if (upper0 && (flags & F_TVD)) l = fmin(l, rhoe_quadratic_solve(uL, P, Urhoe, a.ZEROTOL));
+    // min-entropy bounds (limiter_utils.jl:19-24): l is lpos, then the bisection
+    if (flags & F_MIN_ENTROPY) l = bisect_phi(uL, P, l, base[C::O_RHSL + 4 * m + 3], a.gamma);
     base[C::O_EV + r] = fmin(l, 1.0);
   }
   if (a.counters && tid == 0 && nlist) atomicAdd(&a.counters[0], (unsigned long long)nlist);
@@ -1126,6 +1227,8 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
           sumLd += L[fi] * dvdf[idx];
         }
       double rhs = sB - sdl;
+      // rhs_es of the relaxed bounds (subcell.jl:750-753)
+      if (flags & F_RELAXED) rhs = (1 - a.beta * G[16]) * rhs;
       double est = sumLd - rhs;
       double tol = jmax(0.0, sdl - sB);
       if (est > tol) {
@@ -1296,6 +1399,9 @@ __device__ __forceinline__ void stage_b_body(const StageArgs& a, int k0, double*
     } else if (flags & F_RHSU_FROM_L) {
 #pragma unroll
       for (int c = 0; c < 4; ++c) ru[c] = a.rhsL[gidx + c];
+    } else if (flags & F_ZHANG_SHU) {
+#pragma unroll
+      for (int c = 0; c < 4; ++c) ru[c] = a.rhsU[gidx + c];
     } else {
 #pragma unroll
       for (int c = 0; c < 4; ++c) ru[c] = a.rhsH[gidx + c];

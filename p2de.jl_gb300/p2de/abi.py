@@ -38,6 +38,15 @@ BOUND_POSITIVITY = 0
 BOUND_POSITIVITY_AND_CELL_ENTROPY = 1
 BOUND_TVD = 2
 BOUND_TVD_AND_CELL_ENTROPY = 3
+BOUND_POSITIVITY_AND_MIN_ENTROPY = 4
+BOUND_POSITIVITY_AND_RELAXED_MIN_ENTROPY = 5
+BOUND_POSITIVITY_AND_RELAXED_CELL_ENTROPY = 6
+BOUND_TVD_AND_MIN_ENTROPY = 7
+BOUND_TVD_AND_RELAXED_MIN_ENTROPY = 8
+BOUND_TVD_AND_RELAXED_CELL_ENTROPY = 9
+# p2de_rhs_limiter
+LIMITER_SUBCELL = 0
+LIMITER_ZHANG_SHU = 1
 # p2de_surface_flux
 FLUX_LF_NODAL = 0
 FLUX_LF_PROJECTED = 1
@@ -57,6 +66,7 @@ FIELD_BF_L = 6
 FIELD_BF_H = 7
 FIELD_L_LOCAL = 8
 FIELD_RESW = 9
+FIELD_L = 10
 
 
 class P2deParam(ctypes.Structure):
@@ -79,9 +89,10 @@ class P2deParam(ctypes.Structure):
         ("reference_semantics", c_int32),
         ("precision", c_int32),
         ("shock_capture", c_int32),
-        ("reserved_", c_int32),
+        ("rhs_limiter", c_int32),
         ("shock_capture_a", c_double),
         ("shock_capture_c", c_double),
+        ("bound_beta", c_double),
     ]
 
 

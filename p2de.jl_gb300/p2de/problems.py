@@ -39,11 +39,14 @@ def primitive_to_conservative(equation, prim) -> np.ndarray:
     return np.stack([rho, rho * u, rho * v, E], axis=-1)
 
 
-def default_param(N, K, xL, xR, T, CFL=0.5, dt0=None, bound=None, precision="fp64", reference_semantics=True, output_interval=100000):
+def default_param(N, K, xL, xR, T, CFL=0.5, dt0=None, bound=None, precision="fp64", reference_semantics=True,
+                  output_interval=100000, rhs_limiter=None):
     """Param with the smoke test's constants (test/test_smoke.jl:57-67): POSTOL=1e-14,
     ZEROTOL=5e-16, zeta=0.1, eta=0.5; ESLimitedLowOrderPos(LaxFriedrichsOnNodalVal,
-    LaxFriedrichsOnProjectedVal), NoEntropyProjectionLimiter, SubcellLimiter. dt0
-    defaults to T so that the positivity CFL governs the step."""
+    LaxFriedrichsOnProjectedVal), NoEntropyProjectionLimiter, SubcellLimiter(bound) unless
+    rhs_limiter is given. dt0 defaults to T so that the positivity CFL governs the step."""
+    if rhs_limiter is None:
+        rhs_limiter = SubcellLimiter(bound=bound if bound is not None else PositivityAndCellEntropyBound())
     return Param(
         N=N,
         K=tuple(K),
@@ -55,7 +58,7 @@ def default_param(N, K, xL, xR, T, CFL=0.5, dt0=None, bound=None, precision="fp6
         postprocessing_param=PostprocessingParameter(output_interval=output_interval),
         equation=CompressibleEulerIdealGas(1.4),
         rhs=ESLimitedLowOrderPos(),
-        rhs_limiter=SubcellLimiter(bound=bound if bound is not None else PositivityAndCellEntropyBound()),
+        rhs_limiter=rhs_limiter,
         reference_semantics=reference_semantics,
         precision=precision,
     )

@@ -28,17 +28,39 @@ from .types import (
     NoShockCapture,
     Param,
     PositivityAndCellEntropyBound,
+    PositivityAndMinEntropyBound,
+    PositivityAndRelaxedCellEntropyBound,
+    PositivityAndRelaxedMinEntropyBound,
     PositivityBound,
     SubcellLimiter,
     TimeParam,
     TVDAndCellEntropyBound,
+    TVDAndMinEntropyBound,
+    TVDAndRelaxedCellEntropyBound,
+    TVDAndRelaxedMinEntropyBound,
     TVDBound,
     HennemannShockCapture,
+    ZhangShuLimiter,
 )
 
 
 class UnsupportedMethod(ValueError):
     pass
+
+
+# SubcellLimiter bound types (Solver.jl:47-62) -> p2de_bound_type
+BOUND_CODES = {
+    PositivityBound: abi.BOUND_POSITIVITY,
+    PositivityAndCellEntropyBound: abi.BOUND_POSITIVITY_AND_CELL_ENTROPY,
+    TVDBound: abi.BOUND_TVD,
+    TVDAndCellEntropyBound: abi.BOUND_TVD_AND_CELL_ENTROPY,
+    PositivityAndMinEntropyBound: abi.BOUND_POSITIVITY_AND_MIN_ENTROPY,
+    PositivityAndRelaxedMinEntropyBound: abi.BOUND_POSITIVITY_AND_RELAXED_MIN_ENTROPY,
+    PositivityAndRelaxedCellEntropyBound: abi.BOUND_POSITIVITY_AND_RELAXED_CELL_ENTROPY,
+    TVDAndMinEntropyBound: abi.BOUND_TVD_AND_MIN_ENTROPY,
+    TVDAndRelaxedMinEntropyBound: abi.BOUND_TVD_AND_RELAXED_MIN_ENTROPY,
+    TVDAndRelaxedCellEntropyBound: abi.BOUND_TVD_AND_RELAXED_CELL_ENTROPY,
+}
 
 
 def _i64(a) -> np.ndarray:
@@ -93,24 +115,23 @@ def lower_param(param: Param, K: int) -> abi.P2deParam:
         raise UnsupportedMethod("surface fluxes: LaxFriedrichsOnNodalVal (low), LaxFriedrichsOnProjectedVal (high)")
     lim = param.rhs_limiter
     bound = abi.BOUND_POSITIVITY
+    limiter, beta = abi.LIMITER_SUBCELL, 0.0
     shock, sc_a, sc_c = 0, 0.0, 0.0
     if rhs_type == abi.RHS_ES_LIMITED_LOW_ORDER_POS:
-        if not isinstance(lim, SubcellLimiter):
-            raise UnsupportedMethod("LimitedDG needs SubcellLimiter")
+        if isinstance(lim, ZhangShuLimiter):
+            limiter = abi.LIMITER_ZHANG_SHU
+        elif not isinstance(lim, SubcellLimiter):
+            raise UnsupportedMethod("LimitedDG needs SubcellLimiter or ZhangShuLimiter")
         if isinstance(lim.shockcapture, HennemannShockCapture):
             shock, sc_a, sc_c = 1, float(lim.shockcapture.a), float(lim.shockcapture.c)
         elif not isinstance(lim.shockcapture, NoShockCapture):
             raise UnsupportedMethod(f"shock capture {type(lim.shockcapture).__name__} is not built")
-        if isinstance(lim.bound, PositivityBound):
-            bound = abi.BOUND_POSITIVITY
-        elif isinstance(lim.bound, PositivityAndCellEntropyBound):
-            bound = abi.BOUND_POSITIVITY_AND_CELL_ENTROPY
-        elif isinstance(lim.bound, TVDAndCellEntropyBound):
-            bound = abi.BOUND_TVD_AND_CELL_ENTROPY
-        elif isinstance(lim.bound, TVDBound):
-            bound = abi.BOUND_TVD
-        else:
-            raise UnsupportedMethod(f"bound {type(lim.bound).__name__} is not built")
+        if isinstance(lim, SubcellLimiter):
+            code = BOUND_CODES.get(type(lim.bound))
+            if code is None:
+                raise UnsupportedMethod(f"bound {type(lim.bound).__name__} is not built")
+            bound = code
+            beta = float(getattr(lim.bound, "beta", 0.0))
     if param.precision not in abi.PRECISIONS:
         raise UnsupportedMethod("precision must be one of " + ", ".join(abi.PRECISIONS))
     gc, ts, lp = param.global_constants, param.timestepping_param, param.limiting_param
@@ -133,6 +154,8 @@ def lower_param(param: Param, K: int) -> abi.P2deParam:
         shock_capture=shock,
         shock_capture_a=sc_a,
         shock_capture_c=sc_c,
+        rhs_limiter=limiter,
+        bound_beta=beta,
         reference_semantics=1 if param.reference_semantics else 0,
         precision=abi.PRECISIONS[param.precision],
     )
@@ -310,6 +333,14 @@ def ssp33_step(solver: Solver, t: float) -> tuple[float, float]:
     tt, dt = c_double(t), c_double()
     solver._check(solver.lib.p2de_ssp33_step(solver.handle, byref(tt), byref(dt)))
     return tt.value, dt.value
+
+
+def ssp33(solver: Solver) -> tuple[float, int, float]:
+    """The whole SSP33! time loop (SSPRK33.jl:1-62) on the device without snapshots;
+    returns (t, steps, last dt)."""
+    t, n, dt = c_double(), c_int64(), c_double()
+    solver._check(solver.lib.p2de_ssp33(solver.handle, byref(t), byref(n), byref(dt)))
+    return t.value, n.value, dt.value
 
 
 def SSP33_bang(state: State, solver: Solver, state_param: StateParam, snapshots: bool = True) -> DataHistory:

@@ -131,6 +131,19 @@ class TVDAndCellEntropyBound:
     pass
 
 
+class TVDAndMinEntropyBound:
+    pass
+
+
+class TVDAndRelaxedMinEntropyBound:
+    pass
+
+
+@dataclass(frozen=True)
+class TVDAndRelaxedCellEntropyBound:
+    beta: float = 0.5
+
+
 @dataclass(frozen=True)
 class SubcellLimiter:
     bound: Any = field(default_factory=PositivityBound)

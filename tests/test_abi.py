@@ -34,7 +34,7 @@ def test_library_exports_every_declared_symbol():
     for name in declared_functions():
         assert hasattr(lib, name), name
     lib2 = abi.load_library()
-    assert lib2.p2de_abi_version() == 2
+    assert lib2.p2de_abi_version() == 3
 
 
 def test_field_counts():
@@ -43,6 +43,7 @@ def test_field_counts():
     assert lib.p2de_field_count(3, 10, abi.FIELD_UQ, byref(c)) == 0 and c.value == 4 * 16 * 10
     assert lib.p2de_field_count(3, 10, abi.FIELD_BF_H, byref(c)) == 0 and c.value == 8 * 16 * 10
     assert lib.p2de_field_count(3, 10, abi.FIELD_L_LOCAL, byref(c)) == 0 and c.value == 20 * 2 * 10
+    assert lib.p2de_field_count(3, 10, abi.FIELD_L, byref(c)) == 0 and c.value == 10
     assert lib.p2de_field_count(6, 10, abi.FIELD_UQ, byref(c)) == 1  # N outside 1..5
     assert lib.p2de_field_count(3, 10, 42, byref(c)) == 1
 

@@ -8,9 +8,18 @@ import numpy as np
 import pytest
 
 import p2de
-from p2de import problems
+from p2de import abi, problems
 from p2de import solver as S
-from p2de.types import EntropyStable, GaussCollocation, LowOrderPositivity, PositivityAndRelaxedCellEntropyBound, SubcellLimiter
+from p2de.types import (
+    EntropyStable,
+    GaussCollocation,
+    HennemannShockCapture,
+    LowOrderPositivity,
+    NoRHSLimiter,
+    PositivityAndRelaxedCellEntropyBound,
+    SubcellLimiter,
+    ZhangShuLimiter,
+)
 
 
 @pytest.mark.parametrize("N,Kx,Ky", [(1, 3, 2), (3, 4, 5), (5, 2, 2)])
@@ -64,8 +73,12 @@ def test_lowering_rejects_what_is_not_built():
     assert S.lower_param(replace(param, rhs=EntropyStable()), K).rhs_type == 2
     with pytest.raises(S.UnsupportedMethod):
         S.lower_param(replace(param, approximation_basis=GaussCollocation()), K)
+    relaxed = S.lower_param(replace(param, rhs_limiter=SubcellLimiter(bound=PositivityAndRelaxedCellEntropyBound(0.25))), K)
+    assert relaxed.bound_type == abi.BOUND_POSITIVITY_AND_RELAXED_CELL_ENTROPY and relaxed.bound_beta == 0.25
+    zs = S.lower_param(replace(param, rhs_limiter=ZhangShuLimiter(shockcapture=HennemannShockCapture())), K)
+    assert zs.rhs_limiter == abi.LIMITER_ZHANG_SHU and zs.shock_capture == 1
     with pytest.raises(S.UnsupportedMethod):
-        S.lower_param(replace(param, rhs_limiter=SubcellLimiter(bound=PositivityAndRelaxedCellEntropyBound(0.5))), K)
+        S.lower_param(replace(param, rhs_limiter=NoRHSLimiter()), K)
     with pytest.raises(S.UnsupportedMethod):
         S.lower_param(replace(param, precision="bf16"), K)
     assert S.lower_param(replace(param, precision="mixed"), K).precision == 1
