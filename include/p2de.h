@@ -69,6 +69,21 @@ typedef enum p2de_bound_type {
   P2DE_BOUND_TVD_AND_RELAXED_CELL_ENTROPY = 9         /* TVDAndRelaxedCellEntropyBound(beta) */
 } p2de_bound_type;
 
+/* Approximation bases (Solver.jl:38-40): collocation on the tensor-product LGL nodes, or
+ * on the Gauss nodes with extrapolation to the face Gauss points (init.jl:83-131). */
+typedef enum p2de_basis {
+  P2DE_BASIS_LOBATTO = 0,  /* LobattoCollocation */
+  P2DE_BASIS_GAUSS = 1     /* GaussCollocation */
+} p2de_basis;
+
+/* Entropy-projection limiters (Solver.jl:41-43): Gauss faces take the entropy variables
+ * extrapolated by theta Vf + (1 - theta) Vf_low, theta per face node from the bounds of
+ * filter.jl:91-130 by bisection. */
+typedef enum p2de_entropyproj_limiter {
+  P2DE_ENTROPYPROJ_NONE = 0,                       /* NoEntropyProjectionLimiter */
+  P2DE_ENTROPYPROJ_NODEWISE_SCALED_EXTRAPOLATION = 1 /* NodewiseScaledExtrapolation */
+} p2de_entropyproj_limiter;
+
 /* RHS limiters (Solver.jl:72-91). */
 typedef enum p2de_rhs_limiter {
   P2DE_LIMITER_SUBCELL = 0,   /* SubcellLimiter(bound, shockcapture) */
@@ -123,6 +138,8 @@ typedef struct p2de_param {
   double shock_capture_a;
   double shock_capture_c;
   double bound_beta;               /* beta of the Relaxed...CellEntropyBound types, else unused */
+  int32_t approximation_basis;     /* p2de_basis */
+  int32_t entropyproj_limiter;     /* p2de_entropyproj_limiter */
 } p2de_param;
 
 /* Mesh and boundary data. geom/mapP/mapI/mapO/Ival follow StateParam.bcdata
@@ -163,8 +180,10 @@ typedef enum p2de_field {
   P2DE_FIELD_BF_H = 7,    /* Nfp x K SVector{2,SVector{4}} */
   P2DE_FIELD_L_LOCAL = 8, /* (Nq+N1D) x 2 x K for one stage */
   P2DE_FIELD_RESW = 9,    /* Nq x K SVector{4} */
-  P2DE_FIELD_L = 10       /* K for one stage: ZhangShuLimiter's factor L[k, nstage] before the
+  P2DE_FIELD_L = 10,      /* K for one stage: ZhangShuLimiter's factor L[k, nstage] before the
                              shock-capture cap (zhangshu.jl:44) */
+  P2DE_FIELD_THETA_LOCAL = 11 /* Nfp x K for one stage: the entropy-projection limiting factor
+                                 theta_local[i, k, nstage] (1 without the limiter) */
 } p2de_field;
 
 typedef struct p2de_solver p2de_solver;

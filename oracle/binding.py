@@ -106,7 +106,7 @@ class Oracle:
     def count(self, field: int) -> int:
         n, Nq, Nfp, K = self.N1D, self.Nq, self.Nfp, self.K
         return {0: 4 * Nq * K, 1: 4 * Nq * K, 2: 4 * Nq * K, 3: 4 * Nq * K, 4: 8 * Nq * K, 5: 8 * Nq * K,
-                6: 8 * Nfp * K, 7: 8 * Nfp * K, 8: (Nq + n) * 2 * K, 9: 4 * Nq * K, 10: K}[field]
+                6: 8 * Nfp * K, 7: 8 * Nfp * K, 8: (Nq + n) * 2 * K, 9: 4 * Nq * K, 10: K, 11: Nfp * K}[field]
 
     def set_Uq(self, Uq):
         U = np.ascontiguousarray(Uq, dtype=np.float64).ravel()

@@ -255,6 +255,76 @@ void gll_rule(int N, std::vector<double>& r, std::vector<double>& w, std::vector
     }
 }
 
+// ---------------------------------------------------------------------------
+// Gauss-Legendre rule (gauss_quad(0, 0, N) of NodesAndModes): the N+1 roots of P_{N+1}
+// by Newton iteration from x_i = cos(pi (i + 3/4) / (N + 3/2)), weights
+// 2 / ((1 - x^2) P'_{N+1}(x)^2). The Lagrange basis on these nodes in barycentric form
+// (Berrut & Trefethen 2004): D_ij = (l_j / l_i) / (x_i - x_j), D_ii = -sum_j D_ij, and
+// the values at r = -1, +1 (the face extrapolation of construct_gauss_reference_data,
+// init.jl:111-131).
+// ---------------------------------------------------------------------------
+void gauss_rule(int N, std::vector<double>& r, std::vector<double>& w, std::vector<double>& D,
+                std::vector<double>& ell_m1, std::vector<double>& ell_p1) {
+  const int n = N + 1;
+  r.assign(n, 0.0);
+  w.assign(n, 0.0);
+  D.assign(n * n, 0.0);
+  ell_m1.assign(n, 0.0);
+  ell_p1.assign(n, 0.0);
+  auto legendre = [&](double x, double& P, double& dP) {  // P_n(x), P_n'(x)
+    double p0 = 1.0, p1 = x;
+    for (int k = 2; k <= n; ++k) {
+      double p2 = ((2.0 * k - 1.0) * x * p1 - (k - 1.0) * p0) / k;
+      p0 = p1;
+      p1 = p2;
+    }
+    P = n == 1 ? x : p1;
+    if (n == 1) p0 = 1.0;
+    dP = n * (x * P - p0) / (x * x - 1.0);
+  };
+  for (int i = 0; i < n; ++i) {
+    double x = -std::cos(3.141592653589793 * (i + 0.75) / (n + 0.5));
+    for (int it = 0; it < 100; ++it) {
+      double P, dP;
+      legendre(x, P, dP);
+      double dx = P / dP;
+      x -= dx;
+      if (std::fabs(dx) < 1e-16) break;
+    }
+    r[i] = x;
+  }
+  for (int i = 0; i < n / 2; ++i) {  // exact symmetry
+    double a = 0.5 * (r[n - 1 - i] - r[i]);
+    r[i] = -a;
+    r[n - 1 - i] = a;
+  }
+  if (n % 2 == 1) r[n / 2] = 0.0;
+  for (int i = 0; i < n; ++i) {
+    double P, dP;
+    legendre(r[i], P, dP);
+    w[i] = 2.0 / ((1.0 - r[i] * r[i]) * dP * dP);
+  }
+  std::vector<double> lam(n, 1.0);
+  for (int j = 0; j < n; ++j)
+    for (int k = 0; k < n; ++k)
+      if (k != j) lam[j] /= (r[j] - r[k]);
+  for (int i = 0; i < n; ++i) {
+    double diag = 0.0;
+    for (int j = 0; j < n; ++j)
+      if (j != i) {
+        D[i * n + j] = (lam[j] / lam[i]) / (r[i] - r[j]);
+        diag -= D[i * n + j];
+      }
+    D[i * n + i] = diag;
+  }
+  for (int side = 0; side < 2; ++side) {
+    const double x = side == 0 ? -1.0 : 1.0;
+    double den = 0.0;
+    for (int j = 0; j < n; ++j) den += lam[j] / (x - r[j]);
+    for (int j = 0; j < n; ++j) (side == 0 ? ell_m1 : ell_p1)[j] = (lam[j] / (x - r[j])) / den;
+  }
+}
+
 struct Solver {
   // sizes (SizeData, Solver.jl:173-183)
   int N, N1D, Nq, Nfp, Nh, K, Ns = 3;
@@ -452,7 +522,11 @@ struct Solver {
     Nq = N1D * N1D;
     Nfp = 4 * N1D;
     Nh = Nq + Nfp;
-    gll_rule(N, r1D, w1D, D1D);
+    std::vector<double> ell_m1, ell_p1;  // Lagrange basis at r = -1, +1 (Gauss)
+    if (gauss())
+      gauss_rule(N, r1D, w1D, D1D, ell_m1, ell_p1);
+    else
+      gll_rule(N, r1D, w1D, D1D);
     build_vdm_inv();
     const double ZEROTOL = prm.ZEROTOL;
     // tensor-product nodes, r fastest: i = ir + N1D*is
@@ -491,12 +565,25 @@ struct Solver {
       Bs[2 * N1D + j] = w1D[j] * -1.0;
       Bs[3 * N1D + j] = w1D[j] * 1.0;
     }
-    // Vf: LGL face extrapolation is a selection matrix (init.jl:338-340 uses it as Vf_low,
-    // rounding its near-one entries to one at init.jl:180-185).
+    // Vf_low: the face node's nearest volume node (init.jl:324-340); for LGL it is also Vf
+    // (a selection matrix; init.jl:180-185 rounds its near-one entries to one). Gauss:
+    // Vf extrapolates along the line normal to the face, Vf[f, i] = l_a(-1 or +1) for the
+    // node a of that line (construct_gauss_reference_data, init.jl:111-131).
     Vf.assign(Nfp * Nq, 0.0);
     for (int f = 0; f < Nfp; ++f) Vf[f + (size_t)Nfp * fq2q[f]] = 1.0;
     Vf_low = Vf;
-    // hybridized SBP (init.jl:152-155): Srsh_db = [Q-Q', Ef'B; -B Ef, 0]
+    if (gauss()) {
+      std::fill(Vf.begin(), Vf.end(), 0.0);
+      for (int f = 0; f < Nfp; ++f) {
+        const int side = f / N1D, t = f % N1D;
+        const std::vector<double>& ell = (side % 2 == 0) ? ell_m1 : ell_p1;
+        for (int a = 0; a < N1D; ++a) {
+          const int i = side < 2 ? a + N1D * t : t + N1D * a;
+          Vf[f + (size_t)Nfp * i] = std::fabs(ell[a]) <= ZEROTOL ? 0.0 : ell[a];
+        }
+      }
+    }
+    // hybridized SBP (init.jl:152-155): Srsh_db = [Q-Q', Ef'B; -B Ef, 0], Ef = Vf Pq = Vf
     Srh_db.assign((size_t)Nh * Nh, 0.0);
     Ssh_db.assign((size_t)Nh * Nh, 0.0);
     for (int j = 0; j < Nq; ++j)
@@ -504,22 +591,32 @@ struct Solver {
         Srh_db[i + (size_t)Nh * j] = Qr[i + Nq * j] - Qr[j + Nq * i];
         Ssh_db[i + (size_t)Nh * j] = Qs[i + Nq * j] - Qs[j + Nq * i];
       }
-    for (int f = 0; f < Nfp; ++f) {
-      int i = fq2q[f];
-      Srh_db[i + (size_t)Nh * (Nq + f)] = Br[f];
-      Ssh_db[i + (size_t)Nh * (Nq + f)] = Bs[f];
-      Srh_db[(Nq + f) + (size_t)Nh * i] = -Br[f];
-      Ssh_db[(Nq + f) + (size_t)Nh * i] = -Bs[f];
+    for (int f = 0; f < Nfp; ++f)
+      for (int i = 0; i < Nq; ++i) {
+        const double e = Vf[f + (size_t)Nfp * i];
+        if (e == 0.0) continue;
+        Srh_db[i + (size_t)Nh * (Nq + f)] = e * Br[f];
+        Ssh_db[i + (size_t)Nh * (Nq + f)] = e * Bs[f];
+        Srh_db[(Nq + f) + (size_t)Nh * i] = -(Br[f] * e);
+        Ssh_db[(Nq + f) + (size_t)Nh * i] = -(Bs[f] * e);
+      }
+    if (gauss()) {  // droptol! of the hybridized 0.5 [...] (init.jl:152-154)
+      for (auto& q : Srh_db)
+        if (std::fabs(0.5 * q) <= ZEROTOL) q = 0.0;
+      for (auto& q : Ssh_db)
+        if (std::fabs(0.5 * q) <= ZEROTOL) q = 0.0;
     }
     // MinvVhT = M \ Vh', MinvVfT = M \ Vf' (init.jl:171-172), M = diag(wq)
     MinvVhT.assign((size_t)Nq * Nh, 0.0);
     MinvVfT.assign((size_t)Nq * Nfp, 0.0);
     for (int i = 0; i < Nq; ++i) MinvVhT[i + (size_t)Nq * i] = 1.0 / wq[i];
-    for (int f = 0; f < Nfp; ++f) {
-      int i = fq2q[f];
-      MinvVhT[i + (size_t)Nq * (Nq + f)] = Vf[f + (size_t)Nfp * i] / wq[i];
-      MinvVfT[i + (size_t)Nq * f] = Vf[f + (size_t)Nfp * i] / wq[i];
-    }
+    for (int f = 0; f < Nfp; ++f)
+      for (int i = 0; i < Nq; ++i) {
+        const double e = Vf[f + (size_t)Nfp * i];
+        if (e == 0.0) continue;
+        MinvVhT[i + (size_t)Nq * (Nq + f)] = e / wq[i];
+        MinvVfT[i + (size_t)Nq * f] = e / wq[i];
+      }
     // low order operators (init.jl:276-295, 312-322): Q01D tridiagonal, Sr0 = 0.5(Qr0-Qr0')
     std::vector<double> Q01D(N1D * N1D, 0.0);  // column-major
     for (int i = 0; i < N1D; ++i) {
@@ -587,6 +684,7 @@ struct Solver {
     fstar_L.assign(nf, V2x4{});
     L_local.assign((size_t)(Nq + N1D) * 2 * K * Ns, 0.0);
     L_elem.assign((size_t)K * Ns, 0.0);
+    theta_local.assign((size_t)Nfp * K * Ns, 1.0);
     flux.assign(nh, V2x4{});
     Q0F1.assign(nq, V2x4{});
     wavespeed_f.assign(nf, 0.0);
@@ -637,7 +735,20 @@ struct Solver {
   // ---------------------------------------------------------------------------
   // entropy_projection!(::NoEntropyProjectionLimiter) (rhs.jl:217-268)
   // ---------------------------------------------------------------------------
-  void entropy_projection() {
+  // entropy_projection! (rhs.jl:59-133): volume nodes keep Uq; face node f takes
+  // u(sum_j (theta Vf[f,j] + (1 - theta) Vf_low[f,j]) v(Uq_j)), theta = 1 without the
+  // limiter (entropy_projection_face_node!, :87-95)
+  std::vector<double> theta_local;  // Nfp x K x Ns
+  V4 face_entropy_var(int f, int k, double th) const {
+    V4 acc{0.0, 0.0, 0.0, 0.0};
+    for (int j = 0; j < Nq; ++j) {
+      double c = th * Vf[f + (size_t)Nfp * j] + (1.0 - th) * Vf_low[f + (size_t)Nfp * j];
+      acc = add(acc, scal(c, vq[j + (size_t)Nq * k]));
+    }
+    return acc;
+  }
+  void entropy_projection(int nstage) {
+    const int s = nstage - 1;
 #pragma omp parallel for schedule(static)
     for (int k = 0; k < K; ++k) {
       for (int i = 0; i < Nq; ++i) vq[i + (size_t)Nq * k] = eq.v_ufun(Uq[i + (size_t)Nq * k]);
@@ -645,15 +756,53 @@ struct Solver {
         v_tilde[i + (size_t)Nh * k] = vq[i + (size_t)Nq * k];
         u_tilde[i + (size_t)Nh * k] = Uq[i + (size_t)Nq * k];
       }
-      const double l = 1.0;
       for (int f = 0; f < Nfp; ++f) {
-        V4 acc{0.0, 0.0, 0.0, 0.0};
-        for (int j = 0; j < Nq; ++j) {
-          double c = l * Vf[f + (size_t)Nfp * j] + (1.0 - l) * Vf_low[f + (size_t)Nfp * j];
-          acc = add(acc, scal(c, vq[j + (size_t)Nq * k]));
-        }
+        const double l = scaled_extrapolation() ? theta_local[f + (size_t)Nfp * (k + (size_t)K * s)] : 1.0;
+        V4 acc = face_entropy_var(f, k, l);
         v_tilde[Nq + f + (size_t)Nh * k] = acc;
         u_tilde[Nq + f + (size_t)Nh * k] = eq.u_vfun(acc);
+      }
+    }
+  }
+
+  // compute_entropyproj_limiting_param!(::GaussCollocation) (filter.jl:6-16),
+  // calc_face_values! (:28-46), solve_theta!(::NodewiseScaledExtrapolation) (:53-62):
+  // per face node the largest theta on the bisection grid of [0, 1] whose face value is
+  // well defined (vE < -POSTOL) and inside the bounds of check_bound_on_face_node (:91-102)
+  void solve_theta(int nstage) {
+    const int s = nstage - 1;
+    const double eps = prm.POSTOL, zeta = prm.zeta, eta = prm.eta;
+#pragma omp parallel for schedule(static)
+    for (int k = 0; k < K; ++k) {
+      for (int i = 0; i < Nq; ++i) vq[i + (size_t)Nq * k] = eq.v_ufun(Uq[i + (size_t)Nq * k]);
+      for (int f = 0; f < Nfp; ++f) {
+        V4 Ufv{0.0, 0.0, 0.0, 0.0}, VUf{0.0, 0.0, 0.0, 0.0};
+        for (int j = 0; j < Nq; ++j) {
+          Ufv = add(Ufv, scal(Vf[f + (size_t)Nfp * j], Uq[j + (size_t)Nq * k]));
+          VUf = add(VUf, scal(Vf[f + (size_t)Nfp * j], vq[j + (size_t)Nq * k]));
+        }
+        const double rhoef = eq.rhoe_ufun(Ufv);
+        auto ok = [&](double th) {
+          V4 vt = face_entropy_var(f, k, th);
+          if (!(vt[3] < -eps)) return false;  // update_limited_entropyproj_vars_on_face_node! (:111-130)
+          V4 ut = eq.u_vfun(vt);
+          const double v3 = vt[3], rho = ut[0], rhoe = eq.rhoe_ufun(ut);
+          return v3 < jmin(zeta * VUf[3], -eps) && rho > jmax((1 - eta) * Ufv[0], eps) &&
+                 rho < (1 + eta) * Ufv[0] && rhoe > jmax((1 - eta) * rhoef, eps) && rhoe < (1 + eta) * rhoef;
+        };
+        // bisection(f, 0.0, 1.0) (nonlinear_solvers.jl:3-20)
+        double x_valid = 0.0, x_invalid = 1.0, th;
+        if (ok(x_invalid)) {
+          th = x_invalid;
+        } else {
+          for (int iter = 0; iter <= 20; ++iter) {
+            const double x_new = 0.5 * (x_valid + x_invalid);
+            if (ok(x_new)) x_valid = x_new;
+            else x_invalid = x_new;
+          }
+          th = x_valid;
+        }
+        theta_local[f + (size_t)Nfp * (k + (size_t)K * s)] = th;
       }
     }
   }
@@ -821,7 +970,7 @@ struct Solver {
   // ---------------------------------------------------------------------------
   // rhs_fluxdiff! (flux_differencing.jl:4-37)
   // ---------------------------------------------------------------------------
-  void rhs_fluxdiff(double t) {
+  void rhs_fluxdiff(double t, int nstage) {
     // calculate_primitive_variables! (:39-70)
 #pragma omp parallel for schedule(static)
     for (int k = 0; k < K; ++k)
@@ -934,18 +1083,37 @@ struct Solver {
       }
     // assemble_rhs! (:331-361), project_flux_difference_to_quad_unlimited! (:274-281):
     // generic mat-vec C[i] = sum_j A[i,j]*B[j] accumulated column by column.
+    // With any theta < 1 on the element (is_Vf_limited, :316-318), the lift uses
+    // (1/wq) [I, Vf_new'] with Vf_new = theta Vf + (1 - theta) Vf_low per face row
+    // (project_flux_difference_to_quad!(::ScaledExtrapolation), :288-314)
+    const int s = nstage - 1;
 #pragma omp parallel for schedule(static)
     for (int k = 0; k < K; ++k) {
+      const double* th = &theta_local[(size_t)Nfp * (k + (size_t)K * s)];
+      bool limited = false;
+      for (int f = 0; f < Nfp; ++f) limited = limited || th[f] < 1.0;
+      std::vector<double> Mh;
+      if (limited) {
+        Mh.assign((size_t)Nq * Nh, 0.0);
+        for (int i = 0; i < Nq; ++i) {
+          const double rw = 1 / wq[i];
+          Mh[i + (size_t)Nq * i] = rw * 1.0;
+          for (int f = 0; f < Nfp; ++f)
+            Mh[i + (size_t)Nq * (Nq + f)] = rw * (th[f] * Vf[f + (size_t)Nfp * i] + (1 - th[f]) * Vf_low[f + (size_t)Nfp * i]);
+        }
+      }
+      const double* MVh = limited ? Mh.data() : MinvVhT.data();
+      const double* MVf = limited ? Mh.data() + (size_t)Nq * Nq : MinvVfT.data();
       for (int i = 0; i < Nq; ++i) {
         V2x4 a{}, b{};
         for (int j = 0; j < Nh; ++j) {
-          double m = MinvVhT[i + (size_t)Nq * j];
+          double m = MVh[i + (size_t)Nq * j];
           const V2x4& q = QF1[j + (size_t)Nh * k];
           a.x = add(a.x, scal(m, q.x));
           a.y = add(a.y, scal(m, q.y));
         }
         for (int f = 0; f < Nfp; ++f) {
-          double m = MinvVfT[i + (size_t)Nq * f];
+          double m = MVf[i + (size_t)Nq * f];
           const V2x4& q = BF_H[f + (size_t)Nfp * k];
           b.x = add(b.x, scal(m, q.x));
           b.y = add(b.y, scal(m, q.y));
@@ -1004,6 +1172,11 @@ struct Solver {
     if (prm.reference_semantics)
       return limiting_param_bound_rho_rhoe(UL, P, bv[0], bv[1], bv[2], bv[3]);
     return limiting_param_bound_rho_rhoe(UL, P, bv[0], bv[1], bv[3], bv[4]);
+  }
+
+  bool gauss() const { return prm.approximation_basis == P2DE_BASIS_GAUSS; }
+  bool scaled_extrapolation() const {
+    return prm.entropyproj_limiter == P2DE_ENTROPYPROJ_NODEWISE_SCALED_EXTRAPOLATION;
   }
 
   // bound families (Solver.jl:47-62)
@@ -1455,23 +1628,26 @@ struct Solver {
   // rhs! (rhs.jl:5-13, 183-213)
   // ---------------------------------------------------------------------------
   double rhs(double t, double dt, int nstage) {
+    // init_rhs! (rhs.jl:15-24): theta_local = 1, then the limiter's theta (filter.jl:1-16)
+    std::fill(theta_local.begin() + (size_t)Nfp * K * (nstage - 1), theta_local.begin() + (size_t)Nfp * K * nstage, 1.0);
+    if (gauss() && scaled_extrapolation()) solve_theta(nstage);
     switch (prm.rhs_type) {
       case P2DE_RHS_LOW_ORDER_POSITIVITY: {  // rhs.jl:183-189
-        entropy_projection();
+        entropy_projection(nstage);
         double d = rhs_low_graph_visc(t, dt, nstage);
         rhsU = rhsL;
         return d;
       }
       case P2DE_RHS_ENTROPY_STABLE: {  // rhs.jl:191-197
-        entropy_projection();
-        rhs_fluxdiff(t);
+        entropy_projection(nstage);
+        rhs_fluxdiff(t, nstage);
         rhsU = rhsH;
         return dt;
       }
       default: {  // rhs.jl:199-213
-        entropy_projection();
+        entropy_projection(nstage);
         double d = rhs_low_graph_visc(t, dt, nstage);
-        rhs_fluxdiff(t);
+        rhs_fluxdiff(t, nstage);
         if (prm.rhs_limiter == P2DE_LIMITER_ZHANG_SHU) apply_zhang_shu(dt, nstage);
         else apply_rhs_limiter(t, dt, nstage);
         return d;
@@ -1516,6 +1692,11 @@ int validate(const p2de_param* p, const p2de_mesh* m, std::string& err) {
   }
   if (!m->geom || !m->mapP) {
     err = "geom and mapP are required";
+    return P2DE_ERR_INVALID_ARGUMENT;
+  }
+  if (p->approximation_basis < 0 || p->approximation_basis > 1 || p->entropyproj_limiter < 0 ||
+      p->entropyproj_limiter > 1) {
+    err = "approximation_basis and entropyproj_limiter must be 0 or 1";
     return P2DE_ERR_INVALID_ARGUMENT;
   }
   if (p->bound_type < 0 || p->bound_type > 9 || p->rhs_limiter < 0 || p->rhs_limiter > 1) {
@@ -1659,6 +1840,12 @@ int oracle_get_field(oracle_solver* o, int field, int nstage, double* out) {
     case P2DE_FIELD_L: {
       if (nstage < 1 || nstage > 3) return P2DE_ERR_INVALID_ARGUMENT;
       std::memcpy(out, s.L_elem.data() + (size_t)s.K * (nstage - 1), sizeof(double) * s.K);
+      break;
+    }
+    case P2DE_FIELD_THETA_LOCAL: {
+      if (nstage < 1 || nstage > 3) return P2DE_ERR_INVALID_ARGUMENT;
+      size_t n = (size_t)s.Nfp * s.K;
+      std::memcpy(out, s.theta_local.data() + n * (nstage - 1), sizeof(double) * n);
       break;
     }
     default: return P2DE_ERR_INVALID_ARGUMENT;

@@ -137,8 +137,12 @@ cudaError_t device_tables(int dev, double zerotol, OpTable** out) {
   if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
   DeviceTables& t = g_tabs[dev];
   if (!t.ready) {
-    std::vector<OpTable> h(kMaxN1D - 1);
-    for (int N = 1; N < kMaxN1D; ++N) build_op_table(N, zerotol, &h[N - 1]);
+    // LGL tables for N1D = 2..6, then the Gauss tables in the same order
+    std::vector<OpTable> h(2 * (kMaxN1D - 1));
+    for (int N = 1; N < kMaxN1D; ++N) {
+      build_op_table(N, zerotol, &h[N - 1], 0);
+      build_op_table(N, zerotol, &h[kMaxN1D - 1 + N - 1], 1);
+    }
     cudaError_t e = cudaMalloc(&t.d_tables, sizeof(OpTable) * h.size());
     if (e != cudaSuccess) return e;
     e = cudaMemcpy(t.d_tables, h.data(), sizeof(OpTable) * h.size(), cudaMemcpyHostToDevice);
@@ -176,8 +180,26 @@ cudaError_t launch_a_one(int n1d, const StageArgs& a, bool mixed, cudaStream_t s
 bool needs_phi_min(const StageArgs& a) {
   return (a.flags & F_MIN_ENTROPY) && (a.flags & F_RELAXED) && a.nstage == 1;
 }
-int a_launches(const StageArgs& a) { return ((a.flags & F_TVD) ? 2 : 1) + (needs_phi_min(a) ? 1 : 0); }
+int a_launches(const StageArgs& a) {
+  return ((a.flags & F_TVD) ? 2 : 1) + (needs_phi_min(a) ? 1 : 0) + ((a.flags & F_GAUSS) ? 1 : 0);
+}
+cudaError_t launch_gauss_proj_n1d(int n1d, const StageArgs& a, cudaStream_t st) {
+  switch (n1d) {
+    case 2: return launch_gauss_proj<2>(a, st);
+    case 3: return launch_gauss_proj<3>(a, st);
+    case 4: return launch_gauss_proj<4>(a, st);
+    case 5: return launch_gauss_proj<5>(a, st);
+    case 6: return launch_gauss_proj<6>(a, st);
+  }
+  return cudaErrorInvalidValue;
+}
+// Gauss collocation: the face projection of the stage first (every element's projected
+// face states must exist before kernel A reads its neighbours')
 cudaError_t launch_a_n1d(int n1d, const StageArgs& a, bool mixed, cudaStream_t st) {
+  if (a.flags & F_GAUSS) {
+    cudaError_t e = launch_gauss_proj_n1d(n1d, a, st);
+    if (e != cudaSuccess) return e;
+  }
   if (needs_phi_min(a)) {
     k_phi_min<<<1, 1024, 0, st>>>(a.Uq, (size_t)a.K * n1d * n1d, a.gamma, a.scal, a.t0, a.phimin);
     cudaError_t e = cudaGetLastError();
@@ -239,6 +261,8 @@ struct p2de_solver {
   double* rhoL = nullptr;                                                  // TVD bounds only
   double* Lelem = nullptr;                                                 // 3 x K ZhangShuLimiter factors
   double* phimin = nullptr;                                                // initial min of phi
+  bool gauss = false;                                                      // GaussCollocation
+  double *ufproj = nullptr, *theta = nullptr;                              // Gauss face projection
   int diag_nblocks = 0;
   StageArgs base{};
   int64_t launches = 0;
@@ -283,6 +307,11 @@ cudaError_t dalloc(p2de_solver* s, T** p, size_t count) {
   return cudaSuccess;
 }
 
+// the operator table of the solve: LGL tables for N1D = 2..6, then the Gauss tables
+const OpTable* table_of(const p2de_solver* s) {
+  return s->ops + (s->N1D - 2) + (s->gauss ? kMaxN1D - 1 : 0);
+}
+
 int flags_for(const p2de_solver* s, int nstage, bool update, bool debug) {
   int f = 0;
   switch (s->prm.rhs_type) {
@@ -304,6 +333,10 @@ int flags_for(const p2de_solver* s, int nstage, bool update, bool debug) {
   }
   if (s->prm.precision == P2DE_PRECISION_MIXED_ACC64) f |= F_ACC64;
   if (s->prm.shock_capture == 1 && (f & (F_DO_LIMIT | F_ZHANG_SHU))) f |= F_SHOCK;
+  if (s->gauss) {
+    f |= F_GAUSS;
+    if (s->prm.entropyproj_limiter == P2DE_ENTROPYPROJ_NODEWISE_SCALED_EXTRAPOLATION) f |= F_EPROJ;
+  }
   if (update) f |= F_UPDATE;
   if (debug) f |= F_WRITE_DEBUG;
   return f;
@@ -374,6 +407,7 @@ int p2de_field_count(int32_t N, int32_t K, int32_t field, int64_t* count) {
     case P2DE_FIELD_BF_H: *count = 8 * Nfp * K; break;
     case P2DE_FIELD_L_LOCAL: *count = (Nq + n) * 2 * K; break;
     case P2DE_FIELD_L: *count = K; break;
+    case P2DE_FIELD_THETA_LOCAL: *count = Nfp * K; break;
     default: return P2DE_ERR_INVALID_ARGUMENT;
   }
   return P2DE_OK;
@@ -394,6 +428,15 @@ int p2de_initialize_DG(const p2de_param* prm, const p2de_mesh* mesh, int device,
       prm->precision > 2 || prm->shock_capture < 0 || prm->shock_capture > 1 || prm->rhs_limiter < 0 ||
       prm->rhs_limiter > 1)
     return fail(nullptr, P2DE_ERR_INVALID_ARGUMENT, "rhs_type/bound_type/precision/rhs_limiter out of range");
+  if (prm->approximation_basis < 0 || prm->approximation_basis > 1 || prm->entropyproj_limiter < 0 ||
+      prm->entropyproj_limiter > 1)
+    return fail(nullptr, P2DE_ERR_INVALID_ARGUMENT, "approximation_basis/entropyproj_limiter out of range");
+  if (prm->approximation_basis == P2DE_BASIS_GAUSS) {
+    if (prm->precision != P2DE_PRECISION_FP64)
+      return fail(nullptr, P2DE_ERR_UNSUPPORTED, "GaussCollocation runs in FP64 only");
+    if (prm->rhs_limiter == P2DE_LIMITER_SUBCELL && (bound_flags(prm->bound_type) & F_CELL_ENTROPY))
+      return fail(nullptr, P2DE_ERR_UNSUPPORTED, "cell-entropy bounds on GaussCollocation are not built");
+  }
   const int64_t n1 = prm->N + 1, Nfp = 4 * n1, Nq = n1 * n1;
   const int64_t nfk = Nfp * prm->K;
   // validate indices before anything reaches the device
@@ -456,6 +499,11 @@ int p2de_initialize_DG(const p2de_param* prm, const p2de_mesh* mesh, int device,
     return bail(P2DE_ERR_CUDA);
   }
   s->NSF = s->geo.nsf;
+  s->gauss = prm->approximation_basis == P2DE_BASIS_GAUSS;
+  if (s->gauss) {  // kernel A's Gauss layout is larger: its own elements per block
+    s->geo.elems_per_block = s->geo.elems_per_block_gauss;
+    s->geo.elems_per_block_max = s->geo.elems_per_block_max_gauss;
+  }
   const size_t K = (size_t)s->K;
   // host-side preprocessing: neighbour indices, boundary codes, axis alignment
   std::vector<int32_t> nbr(nfk), bcidx(nfk, 0);
@@ -537,7 +585,7 @@ int p2de_initialize_DG(const p2de_param* prm, const p2de_mesh* mesh, int device,
   StageArgs& a = s->base;
   a.K = s->K;
   a.epb = s->geo.elems_per_block;
-  a.ops = s->ops + (s->N1D - 2);
+  a.ops = table_of(s);
   a.Uq = s->Uq;
   a.resW = s->resW;
   a.geom = s->geom;
@@ -580,6 +628,14 @@ int p2de_initialize_DG(const p2de_param* prm, const p2de_mesh* mesh, int device,
   set_bound_constants(a, prm->N, prm->t0, prm->POSTOL, prm->bound_beta);
   a.Lelem = s->Lelem;
   a.phimin = s->phimin;
+  a.eta = prm->eta;
+  if (s->gauss) {
+    if (dalloc(s, &s->ufproj, (size_t)4 * Nfp * prm->K) != cudaSuccess ||
+        dalloc(s, &s->theta, (size_t)3 * Nfp * prm->K) != cudaSuccess)
+      return bail(P2DE_ERR_OUT_OF_MEMORY);
+    a.ufproj = s->ufproj;
+    a.theta = s->theta;
+  }
   if (bound_flags(prm->bound_type) & F_TVD) {
     if (dalloc(s, &s->rhoL, (size_t)Nq * prm->K) != cudaSuccess) return bail(P2DE_ERR_OUT_OF_MEMORY);
     a.rhoL = s->rhoL;
@@ -628,6 +684,14 @@ int p2de_get_field(p2de_solver* s, int32_t field, int32_t nstage, double* out) {
     case P2DE_FIELD_L:
       if (nstage < 1 || nstage > 3) return fail(s, P2DE_ERR_INVALID_ARGUMENT, "nstage %d", nstage);
       src = s->Lelem + (size_t)(nstage - 1) * cnt;
+      break;
+    case P2DE_FIELD_THETA_LOCAL:
+      if (nstage < 1 || nstage > 3) return fail(s, P2DE_ERR_INVALID_ARGUMENT, "nstage %d", nstage);
+      if (!s->gauss) {  // theta_local = 1 (clear_entropyproj_limiting_parameter_cache!)
+        for (int64_t i = 0; i < cnt; ++i) out[i] = 1.0;
+        return P2DE_OK;
+      }
+      src = s->theta + (size_t)(nstage - 1) * cnt;
       break;
   }
   CK(cudaSetDevice(s->device));
@@ -968,7 +1032,7 @@ int diag_prepare(p2de_solver* s, bool exact) {
 }
 
 const double* device_wq(const p2de_solver* s) {
-  const OpTable* t = s->ops + (s->N1D - 2);  // the tables of N1D = 2..6 in order
+  const OpTable* t = table_of(s);
   return reinterpret_cast<const double*>(reinterpret_cast<const char*>(t) + offsetof(OpTable, wq));
 }
 

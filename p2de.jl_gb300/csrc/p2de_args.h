@@ -28,7 +28,9 @@ enum : int {
   F_SHOCK = 1 << 14,        // HennemannShockCapture blending factor caps the subcell factors
   F_ZHANG_SHU = 1 << 15,    // ZhangShuLimiter: one factor per element, rhsU written by kernel A
   F_MIN_ENTROPY = 1 << 16,  // min-entropy bounds: bisection for phi >= Lphi - POSTOL
-  F_RELAXED = 1 << 17       // relaxed bounds: smoothness factor from the modal energies
+  F_RELAXED = 1 << 17,      // relaxed bounds: smoothness factor from the modal energies
+  F_GAUSS = 1 << 18,        // GaussCollocation: projected face states, face pairs, Vf lift
+  F_EPROJ = 1 << 19         // NodewiseScaledExtrapolation: theta per face node
 };
 
 // boundary codes per face node
@@ -80,6 +82,9 @@ struct StageArgs {
   double t0, POSTOL;
   double s0;            // log10(N^-4), the centre of the smoothness ramp (subcell.jl:944)
   double beta;          // relaxed cell-entropy bounds: target scale 1 - beta eps_k
+  double* ufproj;       // K x Nfp x 4: entropy-projected face states (GaussCollocation)
+  double* theta;        // 3 stages x K x Nfp: entropy-projection limiting factors
+  double eta;           // LimitingParameter eta (bounds of the projected face states)
 };
 
 // StageArgs shock-capture constants of update_blending_factor! (shock_capture.jl:123-126)

@@ -92,6 +92,22 @@ struct Cfg {
   static constexpr int E_MAX_RAW = (int)((224 * 1024 - 64) / (sizeof(double) * PER_ELEM_A + sizeof(int) * NEV));
   static constexpr int E_MAX = E_MAX_RAW < 32 ? E_MAX_RAW : 32;
   static constexpr int FBAR = 16 * NSF;  // per element: [dir][H/L][face][c]
+  // GaussCollocation (kernel A with GAUSS): after the LGL layout, the projected face
+  // states, their primitives, theta, the face rows of QF1 and the volume-face pair terms
+  static constexpr int O_UF = (O_SCR + SCR + 1) & ~1;  // 4 Nfp
+  static constexpr int O_PF = O_UF + 4 * Nfp;       // 6 Nfp
+  static constexpr int O_TH = O_PF + 6 * Nfp;       // Nfp
+  static constexpr int O_QFF = O_TH + Nfp;          // 8 Nfp
+  static constexpr int O_FPT = O_QFF + 8 * Nfp;     // 8 Nfp n: pair (face f, line node a) at f n + a
+  static constexpr int PER_ELEM_G = (O_FPT + 8 * Nfp * n + 1) & ~1;
+  static constexpr size_t smem_g(int e) { return sizeof(double) * PER_ELEM_G * e + sizeof(int) * (NEV * e + 4); }
+  static constexpr int E_G = (64 / Nq) > 0 ? (64 / Nq) : 1;
+  static constexpr int E_MAX_G_RAW = (int)((224 * 1024 - 64) / (sizeof(double) * PER_ELEM_G + sizeof(int) * NEV));
+  static constexpr int E_MAX_G = E_MAX_G_RAW < 32 ? E_MAX_G_RAW : 32;
+  static_assert(O_UF % 2 == 0 && E_G <= E_MAX_G, "Gauss layout");
+  // the face projection kernel: U and v(U) per node
+  static constexpr int PER_ELEM_P = 8 * Nq;
+  static constexpr size_t smem_p(int e) { return sizeof(double) * PER_ELEM_P * e; }
 };
 
 // U + dt rhsL, the low-order update (one form everywhere, so values agree bitwise)
@@ -305,16 +321,136 @@ __device__ __forceinline__ double bisect_phi(const double* U, const double* P, d
   return x_valid;
 }
 
+// v_ufun(::CompressibleIdealGas{Dim2}) (compressible_Navier_Stokes.jl:134-144), with
+// s = log(p) - gamma log(rho) for log(p / rho^gamma)
+__device__ __forceinline__ void v_ufun_d(const Gas<double>& g, const double* U, double* V) {
+  const double p = g.gm1 * (U[3] - 0.5 * (U[1] * U[1] + U[2] * U[2]) / U[0]);
+  const double s = log(p) - g.gamma * log(U[0]);
+  V[0] = (g.gamma + 1.0 - s) - g.gm1 * U[3] / p;
+  V[1] = U[1] * g.gm1 / p;
+  V[2] = U[2] * g.gm1 / p;
+  V[3] = -U[0] * g.gm1 / p;
+}
+
+// u_vfun(::CompressibleIdealGas{Dim2}) (:155-163) with rhoe_vfun (:99-104) and s_vfun (:93-97)
+__device__ __forceinline__ void u_vfun_d(const Gas<double>& g, const double* V, double* U) {
+  const double q = (V[1] * V[1] + V[2] * V[2]) / (2.0 * V[3]);
+  const double s = g.gamma - V[0] + q;
+  const double rhoeV = pow(g.gm1 / pow(-V[3], g.gamma), 1.0 / g.gm1) * exp(-s / g.gm1);
+  U[0] = -rhoeV * V[3];
+  U[1] = rhoeV * V[1];
+  U[2] = rhoeV * V[2];
+  U[3] = rhoeV * (1.0 - q);
+}
+
+// =====================================================================================
+// Face projection (GaussCollocation)
+// =====================================================================================
+// compute_entropyproj_limiting_param!(::GaussCollocation) (filter.jl:6-16), calc_face_values!
+// (:28-46), solve_theta!(::NodewiseScaledExtrapolation) (:53-62) with the bounds of
+// check_bound_on_face_node (:91-102), then entropy_projection_face_node! (rhs.jl:87-95):
+// per face node the values Vf U, Vf v(U) along the line normal to the face, theta by the
+// reference's bisection on [0, 1] (theta = 1 without the limiter), and the projected state
+// u(sum_a (theta Vf + (1 - theta) Vf_low)_a v_a), written to ufproj and theta.
+template <int N1D>
+__device__ __forceinline__ void gauss_proj_body(const StageArgs& a, int k0, double* sm) {
+  using C = Cfg<N1D>;
+  constexpr int n = C::n, Nq = C::Nq, Nfp = C::Nfp, PE = C::PER_ELEM_P;
+  if (a.scal[S_DONE] != 0.0) return;
+  const OpTable& op = *a.ops;
+  const int tid = threadIdx.x, bs = blockDim.x;
+  const int Ke = min(a.epb, a.K - k0);
+  if (Ke <= 0) return;
+  const Gas<double> g{a.gamma, a.gm1, 2.0 * a.gm1};
+  for (int w = tid; w < Ke * Nq * 4; w += bs) {
+    const int e = w / (Nq * 4), r = w % (Nq * 4);
+    sm[e * PE + r] = a.Uq[(size_t)k0 * Nq * 4 + w];
+  }
+  __syncthreads();
+  for (int w = tid; w < Ke * Nq; w += bs) {
+    const int e = w / Nq, m = w % Nq;
+    v_ufun_d(g, sm + e * PE + 4 * m, sm + e * PE + 4 * Nq + 4 * m);
+  }
+  __syncthreads();
+  const double eps = a.POSTOL;
+  for (int w = tid; w < Ke * Nfp; w += bs) {
+    const int e = w / Nfp, f = w % Nfp, k = k0 + e;
+    const int side = f / n, t = f % n;
+    const double* ell = (side % 2 == 0) ? op.ellm : op.ellp;
+    const int alow = (side % 2 == 0) ? 0 : n - 1;  // the node of Vf_low (fq2q)
+    const double* U = sm + e * PE;
+    const double* vq = U + 4 * Nq;
+    int node[n];
+#pragma unroll
+    for (int i = 0; i < n; ++i) node[i] = side < 2 ? i + n * t : t + n * i;
+    double Uf[4] = {0, 0, 0, 0}, VUf[4] = {0, 0, 0, 0};
+#pragma unroll
+    for (int i = 0; i < n; ++i) {
+      if (ell[i] == 0.0) continue;
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        Uf[c] = Uf[c] + ell[i] * U[4 * node[i] + c];
+        VUf[c] = VUf[c] + ell[i] * vq[4 * node[i] + c];
+      }
+    }
+    const double rhoef = Uf[3] - 0.5 * (Uf[1] * Uf[1] + Uf[2] * Uf[2]) / Uf[0];
+    auto project = [&](double th, double* vt) {
+#pragma unroll
+      for (int c = 0; c < 4; ++c) vt[c] = 0.0;
+#pragma unroll
+      for (int i = 0; i < n; ++i) {
+        const double cf = th * ell[i] + (1.0 - th) * (i == alow ? 1.0 : 0.0);
+#pragma unroll
+        for (int c = 0; c < 4; ++c) vt[c] = vt[c] + cf * vq[4 * node[i] + c];
+      }
+    };
+    auto ok = [&](double th) {
+      double vt[4], ut[4];
+      project(th, vt);
+      if (!(vt[3] < -eps)) return false;
+      u_vfun_d(g, vt, ut);
+      const double rhoe = ut[3] - 0.5 * (ut[1] * ut[1] + ut[2] * ut[2]) / ut[0];
+      return vt[3] < fmin(a.zeta * VUf[3], -eps) && ut[0] > fmax((1 - a.eta) * Uf[0], eps) &&
+             ut[0] < (1 + a.eta) * Uf[0] && rhoe > fmax((1 - a.eta) * rhoef, eps) && rhoe < (1 + a.eta) * rhoef;
+    };
+    double th = 1.0;
+    if ((a.flags & F_EPROJ) && !ok(1.0)) {
+      double x_valid = 0.0, x_invalid = 1.0;
+      for (int iter = 0; iter <= 20; ++iter) {
+        const double x_new = 0.5 * (x_valid + x_invalid);
+        if (ok(x_new))
+          x_valid = x_new;
+        else
+          x_invalid = x_new;
+      }
+      th = x_valid;
+    }
+    double vt[4], ut[4];
+    project(th, vt);
+    u_vfun_d(g, vt, ut);
+#pragma unroll
+    for (int c = 0; c < 4; ++c) a.ufproj[((size_t)k * Nfp + f) * 4 + c] = ut[c];
+    a.theta[((size_t)(a.nstage - 1) * a.K + k) * Nfp + f] = th;
+  }
+}
+
+template <int N1D>
+__global__ void __launch_bounds__(Cfg<N1D>::THREADS) k_gauss_proj(StageArgs a) {
+  extern __shared__ __align__(16) double sm[];
+  gauss_proj_body<N1D>(a, blockIdx.x * a.epb, sm);
+}
+
 // =====================================================================================
 // Kernel A
 // =====================================================================================
 // Body of kernel A for the E elements k0 .. k0+E-1 of the solve `a`; every early return
 // is uniform over the block. Used by the one-solve kernel and the batched kernel.
-template <int N1D, typename TH>
+template <int N1D, typename TH, bool GAUSS = false>
 __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double* sm) {
   using C = Cfg<N1D>;
   constexpr int n = C::n, Nq = C::Nq, Nfp = C::Nfp, NSF = C::NSF, NEV = C::NEV;
-  constexpr int PE = C::PER_ELEM_A;
+  constexpr int PE = GAUSS ? C::PER_ELEM_G : C::PER_ELEM_A;
+  static_assert(!GAUSS || sizeof(TH) == 8, "Gauss collocation runs in FP64");
   if (a.scal[S_DONE] != 0.0) return;
   const int E = a.epb;
   int* s_list = reinterpret_cast<int*>(sm + PE * E);  // [0]: count, then eval indices
@@ -347,6 +483,16 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
   for (int w = tid; w < Ke * Nq * 4; w += bs) {
     int e = w / (Nq * 4), r = w % (Nq * 4);
     sm[e * PE + C::O_U + r] = a.Uq[(size_t)k0 * Nq * 4 + w];
+  }
+  if (GAUSS) {  // the projected face states and theta of this stage (face projection kernel)
+    for (int w = tid; w < Ke * Nfp * 4; w += bs) {
+      int e = w / (Nfp * 4), r = w % (Nfp * 4);
+      sm[e * PE + C::O_UF + r] = a.ufproj[(size_t)k0 * Nfp * 4 + w];
+    }
+    for (int w = tid; w < Ke * Nfp; w += bs) {
+      int e = w / Nfp, f = w % Nfp;
+      sm[e * PE + C::O_TH + f] = a.theta[((size_t)(a.nstage - 1) * a.K + k0 + e) * Nfp + f];
+    }
   }
   __syncthreads();
 
@@ -390,6 +536,32 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
         float rf = (float)rho;
         reinterpret_cast<float4*>(base + C::O_PRIM)[m] = make_float4(rf, (float)u, (float)v, rf / (2.0f * (float)p));
       }
+    }
+  }
+  if (GAUSS) {
+    // primitives of the projected face states (calculate_primitive_variables!, :39-52)
+    for (int w = tid; w < Ke * Nfp; w += bs) {
+      int e = w / Nfp, f = w % Nfp;
+      double* base = sm + e * PE;
+      const double* U = base + C::O_UF + 4 * f;
+      const double rr = rcp(U[0]);
+      const double p = g.gm1 * fma(-0.5, (U[1] * U[1] + U[2] * U[2]) * rr, U[3]);
+      const double beta = U[0] * rcp(2.0 * p);
+      double* Pm = base + C::O_PF + 6 * f;
+      Pm[0] = U[0];
+      Pm[1] = U[1] * rr;
+      Pm[2] = U[2] * rr;
+      Pm[3] = beta;
+      Pm[4] = log(U[0]);
+      Pm[5] = log(beta);
+    }
+    // is_Vf_limited (flux_differencing.jl:316-318): any theta < 1 on the element, into G[17]
+    for (int e = tid; e < Ke; e += bs) {
+      double* base = sm + e * PE;
+      double lim = 0.0;
+      for (int f = 0; f < Nfp; ++f)
+        if (base[C::O_TH + f] < 1.0) lim = 1.0;
+      base[C::O_GEO + 17] = lim;
     }
   }
   __syncthreads();
@@ -636,6 +808,80 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
     base[C::O_LAMB + f] = lamB;
   }
   __syncthreads();
+  if (GAUSS && do_high) {
+    // ---- P4g: the high-order surface flux on the projected face states
+    //      (calculate_interface_dissipation_coeff!, enforce_BC!, flux_differencing.jl:90-151;
+    //      accumulate_numerical_flux! with LaxFriedrichsOnProjectedVal, :223-272): the
+    //      neighbour's projected state across the face; outflow takes the own node's Uq,
+    //      walls reflect the own projected state; LF coefficient from both wavespeeds
+    for (int w = tid; w < Ke * Nfp; w += bs) {
+      int e = w / Nfp, f = w % Nfp;
+      const int k = k0 + e;
+      double* base = sm + e * PE;
+      const double* G = base + C::O_GEO;
+      int side = f / n, tt = f % n;
+      int q = side == 0 ? n * tt : side == 1 ? (n - 1) + n * tt : side == 2 ? tt : tt + n * (n - 1);
+      double wt = op.w1D[tt];
+      double Bf = (side == 0 || side == 2) ? -wt : wt;
+      bool xs = side < 2;
+      double g1 = xs ? G[1] : G[2], g2 = xs ? G[3] : G[4], gn = xs ? G[5] : G[8];
+      double nh1 = xs ? G[6] : G[9], nh2 = xs ? G[7] : G[10];
+      double B1 = g1 * Bf, B2 = g2 * Bf;
+      double nn = wt * gn;
+      double n1 = Bf < 0 ? -nh1 : nh1, n2 = Bf < 0 ? -nh2 : nh2;
+      const double* uf = base + C::O_UF + 4 * f;
+      size_t fk = (size_t)k * Nfp + f;
+      int lin = a.nbr[fk];
+      bool self = lin == (int)fk;
+      double ufn[4];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) ufn[c] = self ? uf[c] : __ldg(a.ufproj + 4 * (size_t)lin + c);
+      int code = a.bc[fk];
+      double uP[4];
+      if (code == BC_INTERIOR) {
+#pragma unroll
+        for (int c = 0; c < 4; ++c) uP[c] = ufn[c];
+      } else if (code == BC_INFLOW) {
+        const double* iv = a.Ival + 4 * (size_t)a.bcidx[fk];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) uP[c] = iv[c];
+      } else if (code == BC_OUTFLOW) {
+        const double* Uq = base + C::O_U + 4 * q;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) uP[c] = Uq[c];
+      } else if (code == BC_WALL) {
+        double mn = uf[1] * n1 + uf[2] * n2;
+        uP[0] = uf[0];
+        uP[1] = uf[1] - 2.0 * mn * n1;
+        uP[2] = uf[2] - 2.0 * mn * n2;
+        uP[3] = uf[3];
+      } else {
+        const double* xy = a.xyS + 2 * (size_t)a.bcidx[fk];
+        bool post = xy[0] < a.shock_x0 + (xy[1] + a.shock_speed * t_now) * a.shock_inv_slope;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) uP[c] = post ? a.shock_post[c] : a.shock_pre[c];
+      }
+      const double rrf = rcp(uf[0]);
+      const double lam = wavespeed_r(g, rrf, n1 * uf[1] + n2 * uf[2], uf[3]);
+      const double lamN = self ? lam : wavespeed_r(g, rcp(ufn[0]), n1 * ufn[1] + n2 * ufn[2], ufn[3]);
+      double LFc = 0.5 * nn * fmax(lam, lamN);
+      if (code == BC_INFLOW || code == BC_OUTFLOW || code == BC_SHOCK) LFc = 0.0;
+      double ffx[4], ffy[4], fPx[4], fPy[4];
+      fluxes_r(g, uf, rrf, ffx, ffy);
+      fluxes_r(g, uP, rcp(uP[0]), fPx, fPy);
+      const double hB1 = 0.5 * B1, hB2 = 0.5 * B2;
+      double* BH = base + C::O_BFH + 8 * f;
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const double lf = LFc * (uP[c] - uf[c]);
+        const double bx = (aa && !xs) ? 0.0 : hB1 * (ffx[c] + fPx[c]);
+        const double by = (aa && xs) ? 0.0 : hB2 * (ffy[c] + fPy[c]);
+        BH[c] = xs ? bx - lf : bx;
+        BH[4 + c] = xs ? by : by - lf;
+      }
+    }
+    __syncthreads();
+  }
 
   // ---- P5: finish the low-order RHS, scale by mass, positivity CFL
   double dt_loc = __longlong_as_double(0x7ff0000000000000LL);
@@ -767,7 +1013,106 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
         }
       }
     }
+    if (GAUSS) {
+      // ---- P6g: the volume-face pairs (Nq + f, j) of Srsh_db, -B Ef (init.jl:152-155):
+      //      S = -(B_f Vf[f, j]) on the face's axis, fS(projected face state, node j)
+      for (int w = tid; w < Ke * Nfp * n; w += bs) {
+        int e = w / (Nfp * n), r = w % (Nfp * n);
+        int f = r / n, ai = r % n;
+        double* base = sm + e * PE;
+        const double* G = base + C::O_GEO;
+        const int side = f / n, tt = f % n;
+        const int j = side < 2 ? ai + n * tt : tt + n * ai;
+        const double ell = (side % 2 == 0) ? op.ellm[ai] : op.ellp[ai];
+        const double wt = op.w1D[tt];
+        const double Bf = (side == 0 || side == 2) ? -wt : wt;
+        const double Sv = -(Bf * ell);  // Srh_db (r faces) or Ssh_db (s faces); the other is 0
+        const bool xs = side < 2;
+        const double Sxx = (xs ? G[1] : G[2]) * Sv, Sxy = (xs ? G[3] : G[4]) * Sv;
+        double* out = base + C::O_FPT + 8 * r;
+        double Fx[4], Fy[4];
+        fS_fast(g, base + C::O_PF + 6 * f, base + C::O_PRIM + 6 * j, Fx, Fy);
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          out[c] = (aa && !xs) ? 0.0 : Sxx * Fx[c];
+          out[4 + c] = (aa && xs) ? 0.0 : Sxy * Fy[c];
+        }
+      }
+    }
     __syncthreads();
+    if (GAUSS) {
+      // face rows of QF1: the pair terms of each face node in the nnz order (j ascending)
+      for (int w = tid; w < Ke * Nfp * 8; w += bs) {
+        int e = w / (Nfp * 8), r = w % (Nfp * 8);
+        int f = r / 8, c = r % 8;
+        double* base = sm + e * PE;
+        const double* T = base + C::O_FPT + 8 * n * f;
+        double q = 0.0;
+        for (int ai = 0; ai < n; ++ai) q = q + T[8 * ai + c];
+        base[C::O_QFF + 8 * f + c] = q;
+      }
+      __syncthreads();
+      // ---- P7g: QF1 of the volume nodes (volume pairs in the gather order, then minus the
+      //      face pair terms, faces ascending), lift with M \ Vh' = [1/wq, Vf'/wq] or, on an
+      //      element with theta < 1, (1/wq) [I, Vf_new'] with Vf_new = theta Vf + (1 - theta)
+      //      Vf_low (project_flux_difference_to_quad!, :274-314), assemble (:331-361)
+      for (int w = tid; w < Ke * Nq; w += bs) {
+        int e = w / Nq, m = w % Nq;
+        double* base = sm + e * PE;
+        int ir = m % n, is = m / n;
+        const double rJ = base[C::O_GEO + 11];
+        const double rw = op.rwq[m], wqm = op.wq[m];
+        const bool limited = base[C::O_GEO + 17] != 0.0;
+        double Q[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        if (aa) {
+#pragma unroll
+          for (int ax = 0; ax < 2; ++ax)
+            for (int t = 0; t < n - 1; ++t) {
+              const double* sf = base + C::O_SCR + 8 * op.hga_pair[ax][m][t];
+              const int sg = op.hga_sign[ax][m][t];
+#pragma unroll
+              for (int c = 0; c < 4; ++c) Q[4 * ax + c] = Q[4 * ax + c] + signed_by(sf[4 * ax + c], sg);
+            }
+        } else {
+          const int cnt = op.hg_count[m];
+          for (int t = 0; t < cnt; ++t) {
+            const double* sf = base + C::O_SCR + 8 * op.hg_pair[m][t];
+            const int sg = op.hg_sign[m][t];
+#pragma unroll
+            for (int c = 0; c < 8; ++c) Q[c] = Q[c] + signed_by(sf[c], sg);
+          }
+        }
+        const int fl[4] = {is, n + is, 2 * n + ir, 3 * n + ir};
+        const int pos[4] = {ir, ir, is, is};  // the node's place on each face's line
+        double mf[4];
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+          const int f = fl[t];
+          const double* T = base + C::O_FPT + 8 * (n * f + pos[t]);
+#pragma unroll
+          for (int c = 0; c < 8; ++c) Q[c] = Q[c] - T[c];
+          const double ell = (t % 2 == 0) ? op.ellm[pos[t]] : op.ellp[pos[t]];
+          if (limited) {
+            const double th = base[C::O_TH + f];
+            const double low = pos[t] == ((t % 2 == 0) ? 0 : n - 1) ? 1.0 : 0.0;
+            mf[t] = rw * (th * ell + (1 - th) * low);
+          } else {
+            mf[t] = ell / wqm;
+          }
+        }
+        double* R = base + C::O_RXYH + 8 * m;
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+          double av = rw * Q[c], bv = 0.0;
+#pragma unroll
+          for (int t = 0; t < 4; ++t) {
+            av = av + mf[t] * base[C::O_QFF + 8 * fl[t] + c];
+            bv = bv + mf[t] * base[C::O_BFH + 8 * fl[t] + c];
+          }
+          R[c] = (-(av + bv)) * rJ;
+        }
+      }
+    } else {
     // ---- P7: gather QF1, lift and assemble (assemble_rhs!, :331-361)
     for (int w = tid; w < Ke * Nq; w += bs) {
       int e = w / Nq, m = w % Nq;
@@ -858,6 +1203,7 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
 #pragma unroll
         for (int c = 0; c < 8; ++c) R[c] = (double)((-(rwf * Q[c] + Bs[c])) * rJf);
       }
+    }
     }
   }
   __syncthreads();
@@ -1289,10 +1635,10 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
   }
 }
 
-template <int N1D, typename TH>
+template <int N1D, typename TH, bool GAUSS = false>
 __global__ void __launch_bounds__(Cfg<N1D>::THREADS) k_stage_a(StageArgs a) {
   extern __shared__ __align__(16) double sm[];
-  stage_a_body<N1D, TH>(a, blockIdx.x * a.epb, sm);
+  stage_a_body<N1D, TH, GAUSS>(a, blockIdx.x * a.epb, sm);
 }
 
 // =====================================================================================

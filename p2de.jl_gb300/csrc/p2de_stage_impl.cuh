@@ -18,8 +18,13 @@ cudaError_t stage_prepare(StageGeometry* geo) {
   if (e != cudaSuccess) return e;
   e = cudaFuncSetAttribute(k_stage_b<N1D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::smem_b(C::E_MAX));
   if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(k_stage_a<N1D, double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)C::smem_g(C::E_MAX_G));
+  if (e != cudaSuccess) return e;
   geo->elems_per_block = C::E;
   geo->elems_per_block_max = C::E_MAX;
+  geo->elems_per_block_gauss = C::E_G;
+  geo->elems_per_block_max_gauss = C::E_MAX_G;
   geo->threads = C::THREADS;
   geo->smem_a = C::SMEM_A;
   geo->smem_b = C::SMEM_B;
@@ -31,12 +36,27 @@ cudaError_t stage_prepare(StageGeometry* geo) {
 template <int N1D>
 cudaError_t launch_stage_a(const StageArgs& a, bool mixed, cudaStream_t st) {
   using C = Cfg<N1D>;
+  if (a.flags & F_GAUSS) {
+    if (mixed || a.epb < 1 || a.epb > C::E_MAX_G) return cudaErrorInvalidValue;
+    int grid = (a.K + a.epb - 1) / a.epb;
+    k_stage_a<N1D, double, true><<<grid, C::THREADS, C::smem_g(a.epb), st>>>(a);
+    return cudaGetLastError();
+  }
   if (a.epb < 1 || a.epb > C::E_MAX) return cudaErrorInvalidValue;
   int grid = (a.K + a.epb - 1) / a.epb;
   if (mixed)
     k_stage_a<N1D, float><<<grid, C::THREADS, C::smem_a(a.epb), st>>>(a);
   else
     k_stage_a<N1D, double><<<grid, C::THREADS, C::smem_a(a.epb), st>>>(a);
+  return cudaGetLastError();
+}
+
+template <int N1D>
+cudaError_t launch_gauss_proj(const StageArgs& a, cudaStream_t st) {
+  using C = Cfg<N1D>;
+  if (a.epb < 1 || a.epb > C::E_MAX_G) return cudaErrorInvalidValue;
+  int grid = (a.K + a.epb - 1) / a.epb;
+  k_gauss_proj<N1D><<<grid, C::THREADS, C::smem_p(a.epb), st>>>(a);
   return cudaGetLastError();
 }
 

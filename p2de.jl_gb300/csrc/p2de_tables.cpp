@@ -64,6 +64,68 @@ void gll_rule(int N, double* r, double* w, double* D) {
     }
 }
 
+// Gauss-Legendre nodes: the roots of P_{N+1} by Newton iteration from
+// x_i = -cos(pi (i + 3/4) / (N + 3/2)), weights 2 / ((1 - x^2) P'_{N+1}(x)^2); the
+// Lagrange basis in barycentric form (Berrut & Trefethen, SIAM Review 46, 2004):
+// D_ij = (l_j / l_i) / (x_i - x_j), D_ii = -sum_j D_ij, values at -1 and +1 from the
+// second barycentric formula.
+void gauss_rule(int N, double* r, double* w, double* D, double* ellm, double* ellp) {
+  const int n = N + 1;
+  auto legendre = [&](double x, double& P, double& dP) {  // P_n(x) and P_n'(x)
+    double p0 = 1.0, p1 = x;
+    for (int k = 2; k <= n; ++k) {
+      const double p2 = ((2.0 * k - 1.0) * x * p1 - (k - 1.0) * p0) / k;
+      p0 = p1;
+      p1 = p2;
+    }
+    P = p1;
+    dP = n * (x * p1 - p0) / (x * x - 1.0);
+  };
+  for (int i = 0; i < n; ++i) {
+    double x = -std::cos(M_PI * (i + 0.75) / (n + 0.5));
+    for (int it = 0; it < 100; ++it) {
+      double P, dP;
+      legendre(x, P, dP);
+      const double dx = P / dP;
+      x -= dx;
+      if (std::fabs(dx) < 1e-16) break;
+    }
+    r[i] = x;
+  }
+  for (int i = 0; i < n / 2; ++i) {
+    const double a = 0.5 * (r[n - 1 - i] - r[i]);
+    r[i] = -a;
+    r[n - 1 - i] = a;
+  }
+  if (n % 2 == 1) r[n / 2] = 0.0;
+  for (int i = 0; i < n; ++i) {
+    double P, dP;
+    legendre(r[i], P, dP);
+    w[i] = 2.0 / ((1.0 - r[i] * r[i]) * dP * dP);
+  }
+  double lam[kMaxN1D];
+  for (int j = 0; j < n; ++j) {
+    lam[j] = 1.0;
+    for (int k = 0; k < n; ++k)
+      if (k != j) lam[j] /= (r[j] - r[k]);
+  }
+  for (int i = 0; i < n; ++i) {
+    double diag = 0.0;
+    for (int j = 0; j < n; ++j)
+      if (j != i) {
+        D[i * n + j] = (lam[j] / lam[i]) / (r[i] - r[j]);
+        diag -= D[i * n + j];
+      }
+    D[i * n + i] = diag;
+  }
+  for (int side = 0; side < 2; ++side) {
+    const double x = side == 0 ? -1.0 : 1.0;
+    double den = 0.0;
+    for (int j = 0; j < n; ++j) den += lam[j] / (x - r[j]);
+    for (int j = 0; j < n; ++j) (side == 0 ? ellm : ellp)[j] = (lam[j] / (x - r[j])) / den;
+  }
+}
+
 namespace {
 
 // Legendre polynomial of degree n normalized on [-1, 1] (three-term recurrence)
@@ -113,15 +175,26 @@ bool invert(std::vector<double> A, int m, double* inv) {
 
 }  // namespace
 
-int build_op_table(int N, double zerotol, OpTable* T) {
-  if (N < 1 || N + 1 > kMaxN1D) return 1;
+int build_op_table(int N, double zerotol, OpTable* T, int basis) {
+  if (N < 1 || N + 1 > kMaxN1D || basis < 0 || basis > 1) return 1;
   std::memset(T, 0, sizeof(OpTable));
   const int n = N + 1, Nq = n * n;
   T->N1D = n;
   T->Nq = Nq;
   T->Nfp = 4 * n;
+  T->basis = basis;
   double r[kMaxN1D], w[kMaxN1D], D[kMaxN1D * kMaxN1D];
-  gll_rule(N, r, w, D);
+  if (basis == 1) {
+    gauss_rule(N, r, w, D, T->ellm, T->ellp);
+    for (int a = 0; a < n; ++a) {  // droptol'd like Vf (init.jl:140-143)
+      if (std::fabs(T->ellm[a]) <= zerotol) T->ellm[a] = 0.0;
+      if (std::fabs(T->ellp[a]) <= zerotol) T->ellp[a] = 0.0;
+    }
+  } else {
+    gll_rule(N, r, w, D);
+    T->ellm[0] = 1.0;
+    T->ellp[N] = 1.0;
+  }
   for (int i = 0; i < n; ++i) T->w1D[i] = w[i];
   // node i = ir + n*is; wq = wr .* ws
   for (int is = 0; is < n; ++is)

@@ -19,7 +19,7 @@ constexpr int kMaxPairsLo = 2 * kMaxN1D * (kMaxN1D - 1);        // 60
 
 struct OpTable {
   int32_t N1D, Nq, Nfp, npl, nph;
-  int32_t pad_;
+  int32_t basis;  // p2de_basis: 0 LGL nodes, 1 Gauss nodes
   double w1D[kMaxN1D];
   double wq[kMaxNq];
   double rwq[kMaxNq];  // 1.0 / wq
@@ -53,10 +53,19 @@ struct OpTable {
   // inv(VDM) of the orthonormal Legendre products P_i(r) P_j(s), mode i + N1D j (init.jl:224),
   // row-major Nq x Nq: the modal coefficients of nodal values (HennemannShockCapture)
   double VDMinv[kMaxNq * kMaxNq];
+  // Gauss nodes: the Lagrange basis at r = -1 and r = +1, the face extrapolation Vf
+  // along a line (construct_gauss_reference_data, init.jl:111-131); LGL: unit vectors
+  double ellm[kMaxN1D];
+  double ellp[kMaxN1D];
 };
 
-// Builds the table for polynomial degree N (1..5). Returns 0 on success.
-int build_op_table(int N, double zerotol, OpTable* out);
+// Builds the table for polynomial degree N (1..5) on the LGL (basis 0) or Gauss (basis 1)
+// nodes. Returns 0 on success.
+int build_op_table(int N, double zerotol, OpTable* out, int basis = 0);
+
+// The 1D Gauss-Legendre rule (nodes, weights), differentiation matrix (row-major) and the
+// Lagrange basis at -1 and +1.
+void gauss_rule(int N, double* r, double* w, double* D, double* ellm, double* ellp);
 
 // The 1D GLL rule (nodes, weights) and differentiation matrix (row-major).
 void gll_rule(int N, double* r, double* w, double* D);

@@ -67,6 +67,12 @@ FIELD_BF_H = 7
 FIELD_L_LOCAL = 8
 FIELD_RESW = 9
 FIELD_L = 10
+FIELD_THETA_LOCAL = 11
+# p2de_basis, p2de_entropyproj_limiter
+BASIS_LOBATTO = 0
+BASIS_GAUSS = 1
+ENTROPYPROJ_NONE = 0
+ENTROPYPROJ_NODEWISE_SCALED_EXTRAPOLATION = 1
 
 
 class P2deParam(ctypes.Structure):
@@ -93,6 +99,8 @@ class P2deParam(ctypes.Structure):
         ("shock_capture_a", c_double),
         ("shock_capture_c", c_double),
         ("bound_beta", c_double),
+        ("approximation_basis", c_int32),
+        ("entropyproj_limiter", c_int32),
     ]
 
 

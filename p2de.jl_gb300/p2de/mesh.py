@@ -52,6 +52,34 @@ def gll_rule(N: int) -> tuple[np.ndarray, np.ndarray]:
     return x, w
 
 
+def gauss_rule(N: int) -> tuple[np.ndarray, np.ndarray]:
+    """Gauss-Legendre nodes and weights (gauss_quad(0, 0, N)): Newton iteration on
+    P_{N+1} from x_i = -cos(pi (i + 3/4) / (N + 3/2)); weights 2/((1-x^2) P'_{N+1}(x)^2)."""
+    n = N + 1
+
+    def legendre(x):
+        p0, p1 = np.ones_like(x), x.copy()
+        for k in range(2, n + 1):
+            p0, p1 = p1, ((2.0 * k - 1.0) * x * p1 - (k - 1.0) * p0) / k
+        dP = n * (x * p1 - p0) / (x * x - 1.0)
+        return p1, dP
+
+    x = -np.cos(np.pi * (np.arange(n) + 0.75) / (n + 0.5))
+    for _ in range(100):
+        P, dP = legendre(x)
+        dx = P / dP
+        x = x - dx
+        if np.max(np.abs(dx)) < 1e-16:
+            break
+    for i in range(n // 2):
+        a = 0.5 * (x[n - 1 - i] - x[i])
+        x[i], x[n - 1 - i] = -a, a
+    if n % 2 == 1:
+        x[n // 2] = 0.0
+    _, dP = legendre(x)
+    return x, 2.0 / ((1.0 - x * x) * dP * dP)
+
+
 def face_to_node(N: int) -> np.ndarray:
     """fq2q (0-based): volume node of each face node."""
     n = N + 1
@@ -94,11 +122,13 @@ class MeshData:
         return self.geom[:, 0]
 
 
-def uniform_mesh(N: int, Kx: int, Ky: int, xL=(0.0, 0.0), xR=(1.0, 1.0)) -> MeshData:
+def uniform_mesh(N: int, Kx: int, Ky: int, xL=(0.0, 0.0), xR=(1.0, 1.0), basis: str = "lobatto") -> MeshData:
+    """basis "lobatto": nodes and face nodes on the LGL points (RefElemData(Quad(), SBP(), N));
+    "gauss": nodes on the Gauss points, face nodes at the face Gauss points (init.jl:83-93)."""
     n = N + 1
     Nq, Nfp = n * n, 4 * n
     K = Kx * Ky
-    r, _ = gll_rule(N)
+    r, _ = gauss_rule(N) if basis == "gauss" else gll_rule(N)
     hx = (xR[0] - xL[0]) / Kx
     hy = (xR[1] - xL[1]) / Ky
     k = np.arange(K)
@@ -107,9 +137,12 @@ def uniform_mesh(N: int, Kx: int, Ky: int, xL=(0.0, 0.0), xR=(1.0, 1.0)) -> Mesh
     is_ = np.repeat(np.arange(n), n)
     x = xL[0] + hx * ex[:, None] + 0.5 * (r[ir][None, :] + 1.0) * hx
     y = xL[1] + hy * ey[:, None] + 0.5 * (r[is_][None, :] + 1.0) * hy
-    fq2q = face_to_node(N)
-    xf, yf = x[:, fq2q], y[:, fq2q]
     f = np.arange(Nfp)
+    # face f on side f // n (r = -1, r = +1, s = -1, s = +1) at tangential point f % n
+    fr = np.where(f // n == 0, -1.0, np.where(f // n == 1, 1.0, r[f % n]))
+    fs_ = np.where(f // n == 2, -1.0, np.where(f // n == 3, 1.0, r[f % n]))
+    xf = xL[0] + hx * ex[:, None] + 0.5 * (fr[None, :] + 1.0) * hx
+    yf = xL[1] + hy * ey[:, None] + 0.5 * (fs_[None, :] + 1.0) * hy
     mapM = 1 + f[None, :] + Nfp * k[:, None]
     side, t = f // n, f % n
     mapP = mapM.copy()

@@ -21,6 +21,8 @@ from .types import (
     ESLimitedLowOrderPos,
     GlobalConstant,
     LimitingParameter,
+    LobattoCollocation,
+    NoEntropyProjectionLimiter,
     Param,
     PositivityAndCellEntropyBound,
     PostprocessingParameter,
@@ -40,7 +42,7 @@ def primitive_to_conservative(equation, prim) -> np.ndarray:
 
 
 def default_param(N, K, xL, xR, T, CFL=0.5, dt0=None, bound=None, precision="fp64", reference_semantics=True,
-                  output_interval=100000, rhs_limiter=None):
+                  output_interval=100000, rhs_limiter=None, approximation_basis=None, entropyproj_limiter=None):
     """Param with the smoke test's constants (test/test_smoke.jl:57-67): POSTOL=1e-14,
     ZEROTOL=5e-16, zeta=0.1, eta=0.5; ESLimitedLowOrderPos(LaxFriedrichsOnNodalVal,
     LaxFriedrichsOnProjectedVal), NoEntropyProjectionLimiter, SubcellLimiter(bound) unless
@@ -59,6 +61,8 @@ def default_param(N, K, xL, xR, T, CFL=0.5, dt0=None, bound=None, precision="fp6
         equation=CompressibleEulerIdealGas(1.4),
         rhs=ESLimitedLowOrderPos(),
         rhs_limiter=rhs_limiter,
+        approximation_basis=approximation_basis if approximation_basis is not None else LobattoCollocation(),
+        entropyproj_limiter=entropyproj_limiter if entropyproj_limiter is not None else NoEntropyProjectionLimiter(),
         reference_semantics=reference_semantics,
         precision=precision,
     )

@@ -22,7 +22,9 @@ from .types import (
     EntropyStable,
     LaxFriedrichsOnNodalVal,
     LaxFriedrichsOnProjectedVal,
+    GaussCollocation,
     LobattoCollocation,
+    NodewiseScaledExtrapolation,
     LowOrderPositivity,
     NoEntropyProjectionLimiter,
     NoShockCapture,
@@ -95,10 +97,18 @@ class Descriptor:
 
 def lower_param(param: Param, K: int) -> abi.P2deParam:
     """Maps the dispatch types of Param to the C enums, rejecting what is not built."""
-    if not isinstance(param.approximation_basis, LobattoCollocation):
-        raise UnsupportedMethod("only LobattoCollocation (GLL) is built")
-    if not isinstance(param.entropyproj_limiter, NoEntropyProjectionLimiter):
-        raise UnsupportedMethod("only NoEntropyProjectionLimiter is built")
+    if isinstance(param.approximation_basis, LobattoCollocation):
+        basis = abi.BASIS_LOBATTO
+    elif isinstance(param.approximation_basis, GaussCollocation):
+        basis = abi.BASIS_GAUSS
+    else:
+        raise UnsupportedMethod(f"basis {type(param.approximation_basis).__name__} is not built")
+    if isinstance(param.entropyproj_limiter, NoEntropyProjectionLimiter):
+        eproj = abi.ENTROPYPROJ_NONE
+    elif isinstance(param.entropyproj_limiter, NodewiseScaledExtrapolation):
+        eproj = abi.ENTROPYPROJ_NODEWISE_SCALED_EXTRAPOLATION
+    else:
+        raise UnsupportedMethod(f"entropy projection limiter {type(param.entropyproj_limiter).__name__} is not built")
     rhs = param.rhs
     if isinstance(rhs, ESLimitedLowOrderPos):
         rhs_type = abi.RHS_ES_LIMITED_LOW_ORDER_POS
@@ -132,6 +142,8 @@ def lower_param(param: Param, K: int) -> abi.P2deParam:
                 raise UnsupportedMethod(f"bound {type(lim.bound).__name__} is not built")
             bound = code
             beta = float(getattr(lim.bound, "beta", 0.0))
+            if basis == abi.BASIS_GAUSS and "CellEntropy" in type(lim.bound).__name__:
+                raise UnsupportedMethod("cell-entropy bounds on Gauss collocation are not built")
     if param.precision not in abi.PRECISIONS:
         raise UnsupportedMethod("precision must be one of " + ", ".join(abi.PRECISIONS))
     gc, ts, lp = param.global_constants, param.timestepping_param, param.limiting_param
@@ -156,9 +168,18 @@ def lower_param(param: Param, K: int) -> abi.P2deParam:
         shock_capture_c=sc_c,
         rhs_limiter=limiter,
         bound_beta=beta,
+        approximation_basis=basis,
+        entropyproj_limiter=eproj,
         reference_semantics=1 if param.reference_semantics else 0,
         precision=abi.PRECISIONS[param.precision],
     )
+
+
+def mesh_for(param: Param) -> MeshData:
+    """The uniform mesh of initialize_uniform_mesh_data (init.jl:241-252) with the nodes
+    of param's basis."""
+    basis = "gauss" if isinstance(param.approximation_basis, GaussCollocation) else "lobatto"
+    return uniform_mesh(param.N, param.K[0], param.K[1], param.xL, param.xR, basis=basis)
 
 
 def make_descriptor(param: Param, md: MeshData, bc: BCData) -> Descriptor:
@@ -312,7 +333,7 @@ class StateParam:
 def initialize_DG(param: Param, initial_condition, initial_boundary_conditions, device: int = 0):
     """initialize_DG(param, initial_condition, initial_boundary_conditions)
     (init.jl:44-60) -> (solver, state, state_param)."""
-    md = uniform_mesh(param.N, param.K[0], param.K[1], param.xL, param.xR)
+    md = mesh_for(param)
     bcdata = initial_boundary_conditions(param, md)
     desc = make_descriptor(param, md, bcdata)
     solver = Solver(param, md, desc, device)

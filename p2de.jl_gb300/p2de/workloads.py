@@ -82,7 +82,7 @@ def build_case(case: Case, precision: str = "fp64"):
         param, ic, bcf, _ = problems.isentropic_vortex(**case.extra, **kw)
     else:
         raise ValueError(f"unknown family {case.family}")
-    md = uniform_mesh(param.N, *param.K, param.xL, param.xR)
+    md = S.mesh_for(param)
     bc = bcf(param, md)
     desc = S.make_descriptor(param, md, bc)
     U0 = S.evaluate_initial_condition(param, md, ic)

@@ -10,7 +10,7 @@ def setup(problem, **kw):
     """Returns (param, md, bc, desc, U0) for a problem factory of p2de.problems."""
     out = problem(**kw)
     param, ic, bcf = out[0], out[1], out[2]
-    md = p2de.uniform_mesh(param.N, param.K[0], param.K[1], param.xL, param.xR)
+    md = S.mesh_for(param)
     bc = bcf(param, md)
     desc = S.make_descriptor(param, md, bc)
     U0 = S.evaluate_initial_condition(param, md, ic)

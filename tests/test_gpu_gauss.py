@@ -1,0 +1,136 @@
+"""GPU parity of GaussCollocation with NodewiseScaledExtrapolation (init.jl:83-131,
+filter.jl, rhs.jl:59-133, flux_differencing.jl:283-361) against the FP64 oracle: the
+face projection (theta per face node by bisection, projected face states), the
+volume-face pairs of the hybridized operator, the surface flux on projected states and
+the theta-dependent lift, under the subcell limiter's positivity and min-entropy bounds
+and under Zhang-Shu, on periodic, outflow and double-Mach-reflection boundaries.
+"""
+import numpy as np
+import pytest
+
+import p2de
+from p2de import abi, problems
+from p2de import solver as S
+from p2de.types import (
+    GaussCollocation,
+    HennemannShockCapture,
+    NodewiseScaledExtrapolation,
+    NoEntropyProjectionLimiter,
+    PositivityAndMinEntropyBound,
+    PositivityBound,
+    SubcellLimiter,
+    TVDBound,
+    ZhangShuLimiter,
+)
+
+from conftest import relerr
+from helpers import setup
+from test_gpu_parity import TOL, compare_rhs, gpu_for, oracle_for
+
+pytestmark = pytest.mark.gpu
+
+GAUSS = dict(approximation_basis=GaussCollocation(), entropyproj_limiter=NodewiseScaledExtrapolation())
+LIMITERS = {
+    "positivity": SubcellLimiter(bound=PositivityBound()),
+    "zhang-shu": ZhangShuLimiter(),
+    "positivity+hennemann": SubcellLimiter(bound=PositivityBound(), shockcapture=HennemannShockCapture()),
+    "tvd": SubcellLimiter(bound=TVDBound()),
+}
+PROBLEMS = {
+    "vortex": (problems.isentropic_vortex, dict(Kx=5, Ky=5, T=0.2)),
+    "riemann": (problems.riemann2d, dict(Kx=6, Ky=5, T=0.2, seed=4)),
+    "dmr": (problems.double_mach_reflection, dict(Kx=16, Ky=4, T=0.2)),
+}
+
+
+def compare_theta(g, o, K, nstage):
+    tg, to = g.get_field(abi.FIELD_THETA_LOCAL, nstage), o.get_field(abi.FIELD_THETA_LOCAL, nstage)
+    assert tg.shape == to.shape
+    assert np.all((tg >= 0) & (tg <= 1))
+    np.testing.assert_array_equal(tg, to)
+
+
+@pytest.mark.parametrize("N", [1, 2, 3, 4, 5])
+@pytest.mark.parametrize("problem", list(PROBLEMS))
+def test_gauss_rhs(N, problem):
+    prob, kw = PROBLEMS[problem]
+    param, md, bc, desc, U0 = setup(prob, N=N, rhs_limiter=LIMITERS["positivity"], **GAUSS, **kw)
+    compare_rhs(param, md, desc, U0, dt=1e-3, nstage=1)
+    o = oracle_for(desc, U0)
+    g = gpu_for(param, md, desc, U0)
+    o.rhs(0.0, 1e-3, 2)
+    S.rhs_bang(None, g, None, p2de.TimeParam(0.0, 1e-3, 2))
+    compare_theta(g, o, desc.K, 2)
+    assert relerr(g.get_field(abi.FIELD_RHSU), o.get_field(abi.FIELD_RHSU)) <= TOL
+    g.close()
+    o.close()
+
+
+@pytest.mark.parametrize("limiter", list(LIMITERS))
+@pytest.mark.parametrize("problem", list(PROBLEMS))
+def test_gauss_steps(problem, limiter):
+    prob, kw = PROBLEMS[problem]
+    param, md, bc, desc, U0 = setup(prob, N=3, rhs_limiter=LIMITERS[limiter], **GAUSS, **kw)
+    o = oracle_for(desc, U0)
+    g = gpu_for(param, md, desc, U0)
+    to, tg = 0.0, 0.0
+    for _ in range(3):
+        to, _ = o.step(to)
+        tg, _ = S.ssp33_step(g, tg)
+    assert abs(tg - to) <= 1e-13 * abs(to) and to < param.timestepping_param.T  # every step ran
+    assert relerr(g.get_field(abi.FIELD_UQ), o.get_field(abi.FIELD_UQ)) <= TOL
+    for ns in (1, 2, 3):
+        compare_theta(g, o, desc.K, ns)
+    g.close()
+    o.close()
+
+
+@pytest.mark.parametrize("N", [2, 4])
+def test_gauss_without_projection_limiter(N):
+    """NoEntropyProjectionLimiter on Gauss nodes: theta = 1 everywhere."""
+    param, md, bc, desc, U0 = setup(problems.riemann2d, N=N, Kx=6, Ky=5, T=0.2, seed=4,
+                                    rhs_limiter=ZhangShuLimiter(), approximation_basis=GaussCollocation(),
+                                    entropyproj_limiter=NoEntropyProjectionLimiter())
+    compare_rhs(param, md, desc, U0, dt=1e-3, nstage=2)
+
+
+@pytest.mark.parametrize("N", [1, 3])
+def test_gauss_min_entropy(N):
+    param, md, bc, desc, U0 = setup(problems.riemann2d, N=N, Kx=6, Ky=5, T=0.2, seed=4,
+                                    rhs_limiter=SubcellLimiter(bound=PositivityAndMinEntropyBound()), **GAUSS)
+    compare_rhs(param, md, desc, U0, dt=1e-3, nstage=1, interior_L=False)
+
+
+def test_gauss_reference_example_configuration():
+    """The reference's Kelvin-Helmholtz example (examples/2D/kelvin-helmholtz.jl:44-55:
+    GaussCollocation, NodewiseScaledExtrapolation, positivity bound, zeta 0.1, eta 1.0,
+    CFL 0.5) on a 16 x 16 mesh of its domain, 5 steps."""
+    from dataclasses import replace
+
+    param, md, bc, desc, U0 = setup(problems.kelvin_helmholtz, N=3, Kx=16, Ky=16, T=0.1,
+                                    rhs_limiter=LIMITERS["positivity"], **GAUSS)
+    param = replace(param, limiting_param=p2de.LimitingParameter(zeta=0.1, eta=1.0))
+    desc = S.make_descriptor(param, md, bc)
+    o = oracle_for(desc, U0)
+    g = gpu_for(param, md, desc, U0)
+    to, tg = 0.0, 0.0
+    for _ in range(5):
+        to, _ = o.step(to)
+        tg, _ = S.ssp33_step(g, tg)
+    assert relerr(g.get_field(abi.FIELD_UQ), o.get_field(abi.FIELD_UQ)) <= TOL
+    g.close()
+    o.close()
+
+
+def test_gauss_rejects_what_is_not_built():
+    from dataclasses import replace
+
+    from p2de.types import PositivityAndCellEntropyBound
+
+    param, md, bc, desc, U0 = setup(problems.riemann2d, N=2, Kx=4, Ky=4, T=0.2, seed=4,
+                                    rhs_limiter=SubcellLimiter(bound=PositivityBound()), **GAUSS)
+    with pytest.raises(S.UnsupportedMethod):
+        S.lower_param(replace(param, rhs_limiter=SubcellLimiter(bound=PositivityAndCellEntropyBound())), desc.K)
+    mixed = S.make_descriptor(replace(param, precision="mixed"), md, bc)
+    with pytest.raises(p2de.P2deError):
+        S.Solver(replace(param, precision="mixed"), md, mixed)

@@ -15,8 +15,10 @@ from p2de.types import (
     GaussCollocation,
     HennemannShockCapture,
     LowOrderPositivity,
+    NodewiseScaledExtrapolation,
     NoRHSLimiter,
     PositivityAndRelaxedCellEntropyBound,
+    PositivityBound,
     SubcellLimiter,
     ZhangShuLimiter,
 )
@@ -71,8 +73,12 @@ def test_lowering_rejects_what_is_not_built():
     assert S.lower_param(param, K).rhs_type == 0
     assert S.lower_param(replace(param, rhs=LowOrderPositivity()), K).rhs_type == 1
     assert S.lower_param(replace(param, rhs=EntropyStable()), K).rhs_type == 2
-    with pytest.raises(S.UnsupportedMethod):
+    with pytest.raises(S.UnsupportedMethod):  # cell-entropy bounds on Gauss nodes
         S.lower_param(replace(param, approximation_basis=GaussCollocation()), K)
+    g = S.lower_param(replace(param, approximation_basis=GaussCollocation(), entropyproj_limiter=NodewiseScaledExtrapolation(),
+                              rhs_limiter=SubcellLimiter(bound=PositivityBound())), K)
+    assert g.approximation_basis == abi.BASIS_GAUSS
+    assert g.entropyproj_limiter == abi.ENTROPYPROJ_NODEWISE_SCALED_EXTRAPOLATION
     relaxed = S.lower_param(replace(param, rhs_limiter=SubcellLimiter(bound=PositivityAndRelaxedCellEntropyBound(0.25))), K)
     assert relaxed.bound_type == abi.BOUND_POSITIVITY_AND_RELAXED_CELL_ENTROPY and relaxed.bound_beta == 0.25
     zs = S.lower_param(replace(param, rhs_limiter=ZhangShuLimiter(shockcapture=HennemannShockCapture())), K)

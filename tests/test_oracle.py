@@ -22,6 +22,8 @@ from p2de.types import (
     TVDAndRelaxedMinEntropyBound,
     TVDBound,
     ZhangShuLimiter,
+    GaussCollocation,
+    NodewiseScaledExtrapolation,
 )
 
 from conftest import relerr
@@ -376,6 +378,85 @@ def test_reference_smoke_matrix_runs(limiter):
             param, md, lambda prm, x, y: problems.primitive_to_conservative(prm.equation, exact(prm.equation, x, y, t)))
         assert np.abs(U - np.reshape(Ue, U.shape))[:, 0].max() < 0.2
         o.close()
+
+
+GAUSS = dict(approximation_basis=GaussCollocation(), entropyproj_limiter=NodewiseScaledExtrapolation())
+
+
+@pytest.mark.parametrize("N", [1, 2, 3, 4])
+def test_gauss_free_stream_preservation(N):
+    """GaussCollocation (init.jl:83-131): a constant state stays constant; the face
+    extrapolation reproduces constants, theta stays 1."""
+    param, md, bc, desc, U0 = setup(problems.isentropic_vortex, N=N, Kx=4, Ky=4, T=0.01, strength=0.0,
+                                    rhs_limiter=SubcellLimiter(bound=PositivityBound()), **GAUSS)
+    o = Oracle(desc, nthreads=1)
+    o.set_Uq(U0)
+    o.rhs(0.0, 1e-3, 1)
+    assert np.abs(o.get_field(abi.FIELD_RHSU)).max() < 1e-12
+    assert np.all(o.get_field(abi.FIELD_THETA_LOCAL, 1) == 1.0)
+    o.close()
+
+
+def test_gauss_conservation_with_limited_projection():
+    """theta Vf + (1 - theta) Vf_low keeps the partition of unity of each face row, so the
+    limited lift conserves mass, momentum and energy on a periodic mesh."""
+    param, md, bc, desc, U0 = setup(problems.isentropic_vortex, N=3, Kx=5, Ky=5, T=0.05,
+                                    rhs_limiter=SubcellLimiter(bound=PositivityBound()), **GAUSS)
+    from p2de.mesh import gauss_rule
+
+    _, w = gauss_rule(3)
+    wq = np.outer(w, w).ravel()
+    J = md.geom[:, 0]
+    tot = lambda U: np.einsum("k,i,kic->c", J, wq, np.reshape(U, (desc.K, -1, 4)))
+    o = Oracle(desc, nthreads=2)
+    o.set_Uq(U0)
+    t = 0.0
+    for _ in range(4):
+        t, _ = o.step(t)
+    assert o.get_field(abi.FIELD_THETA_LOCAL, 1).min() < 1.0  # the limiter is active
+    np.testing.assert_allclose(tot(o.get_field(abi.FIELD_UQ)), tot(U0), rtol=1e-13, atol=1e-12)
+    o.close()
+
+
+def test_gauss_converges_faster_than_lobatto():
+    """Zhang-Shu on the smooth vortex (examples/convergence/isentropic-vortex-convergence.jl
+    runs this pairing): the Gauss error is below the LGL one and falls at a high rate."""
+    errs = {}
+    for basis in ("lobatto", "gauss"):
+        errs[basis] = []
+        for Kx in (4, 8):
+            kw = dict(GAUSS) if basis == "gauss" else {}
+            param, ic, bcf, ex = problems.isentropic_vortex(N=3, Kx=Kx, Ky=Kx, T=0.3, strength=1.0, CFL=0.25, dt0=0.3,
+                                                            rhs_limiter=ZhangShuLimiter(), **kw)
+            md = S.mesh_for(param)
+            desc = S.make_descriptor(param, md, bcf(param, md))
+            o = Oracle(desc, nthreads=2)
+            o.set_Uq(S.evaluate_initial_condition(param, md, ic))
+            t, _, _ = o.run()
+            U = o.get_field(abi.FIELD_UQ).reshape(-1, 4)
+            Ue = S.evaluate_initial_condition(
+                param, md, lambda prm, x, y: problems.primitive_to_conservative(prm.equation, ex(prm.equation, x, y, t)))
+            errs[basis].append(np.abs(U - np.reshape(Ue, U.shape))[:, 0].max())
+            o.close()
+    assert errs["gauss"][1] < errs["lobatto"][1]
+    assert np.log2(errs["gauss"][0] / errs["gauss"][1]) > 2.0
+
+
+def test_gauss_mesh_face_points():
+    """Face nodes sit at the face Gauss points, not at volume nodes; periodic partners
+    coincide up to the period."""
+    from p2de.mesh import gauss_rule
+
+    md = p2de.make_periodic(p2de.uniform_mesh(3, 3, 2, (0.0, 0.0), (3.0, 2.0), basis="gauss"))
+    r, w = gauss_rule(3)
+    assert abs(w.sum() - 2.0) < 1e-14 and np.all(np.abs(r) < 1)
+    xf, yf = md.xf.ravel(), md.yf.ravel()
+    mP = md.mapP.ravel() - 1
+    assert np.all((np.abs(xf - xf[mP]) < 1e-12) | (np.abs(np.abs(xf - xf[mP]) - 3.0) < 1e-12))
+    assert np.all((np.abs(yf - yf[mP]) < 1e-12) | (np.abs(np.abs(yf - yf[mP]) - 2.0) < 1e-12))
+    assert np.allclose(md.xf[0, :4], 0.0)  # face r = -1 of the first element
+    d = np.hypot(md.xf[0][:, None] - md.x[0][None, :], md.yf[0][:, None] - md.y[0][None, :])
+    assert d.min() > 1e-3  # no face point is a node
 
 
 def test_reference_semantics_give_low_order_rhs():
