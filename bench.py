@@ -50,10 +50,19 @@ KERNEL_A_TRAFFIC_BYTES = 142.2e6
 KERNEL_A_FP64_PIPE_BUSY = 0.857
 
 
-def workload(name: str, precision: str):
+def workload(name: str, precision: str, basis: str = "lobatto"):
     from p2de import problems
+    from p2de.types import GaussCollocation, NodewiseScaledExtrapolation, PositivityBound, SubcellLimiter
 
-    if name == "dmr":
+    if name == "dmr" and basis == "gauss":
+        # the reference's Gauss configuration (examples/2D/kelvin-helmholtz.jl:44-55):
+        # GaussCollocation, NodewiseScaledExtrapolation, SubcellLimiter(PositivityBound)
+        param, ic, bcf = problems.double_mach_reflection(
+            N=3, Kx=480, Ky=120, T=0.2, precision=precision, approximation_basis=GaussCollocation(),
+            entropyproj_limiter=NodewiseScaledExtrapolation(), rhs_limiter=SubcellLimiter(bound=PositivityBound()))
+        desc = ("double Mach reflection 480x120 quads, N=3, SSP-RK3 CFL 0.5, GaussCollocation + "
+                "NodewiseScaledExtrapolation, positivity bound")
+    elif name == "dmr":
         param, ic, bcf = problems.double_mach_reflection(N=3, Kx=480, Ky=120, T=0.2, precision=precision)
         desc = "double Mach reflection 480x120 quads, N=3, SSP-RK3 CFL 0.5"
     elif name == "kh256":
@@ -172,7 +181,7 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    param, ic, bcf, wdesc = workload(args.workload, "fp64")
+    param, ic, bcf, wdesc = workload(args.workload, "fp64", args.basis)
     md, bc, desc, U0 = build_descriptor(param, ic, bcf)
     from oracle.binding import Oracle, num_threads
 
@@ -509,7 +518,9 @@ def run_limiter_report(args):
 
     from p2de import problems
     from p2de.types import (
+        GaussCollocation,
         HennemannShockCapture,
+        NodewiseScaledExtrapolation,
         PositivityAndCellEntropyBound,
         PositivityAndMinEntropyBound,
         PositivityAndRelaxedCellEntropyBound,
@@ -532,13 +543,17 @@ def run_limiter_report(args):
         "tvd-and-min-entropy": SubcellLimiter(bound=TVDAndMinEntropyBound()),
         "relaxed-cell-entropy(0.5)": SubcellLimiter(bound=PositivityAndRelaxedCellEntropyBound(beta=0.5)),
         "zhang-shu": ZhangShuLimiter(),
+        "gauss + scaled extrapolation, positivity": SubcellLimiter(bound=PositivityBound()),
+        "gauss + scaled extrapolation, zhang-shu": ZhangShuLimiter(),
     }
+    gauss = dict(approximation_basis=GaussCollocation(), entropyproj_limiter=NodewiseScaledExtrapolation())
     res = {}
     for name, lim in limiters.items():
         rep = {}
         for refsem in (True, False):
+            kw = gauss if name.startswith("gauss") else {}
             param, ic, bcf = problems.double_mach_reflection(N=3, Kx=480, Ky=120, T=0.2, rhs_limiter=lim,
-                                                             reference_semantics=refsem)
+                                                             reference_semantics=refsem, **kw)
             md, bc, desc, U0 = build_descriptor(param, ic, bcf)
             sec, U, n = _timed_alone(param, md, desc, U0, args.warmup, args.steps, tune=not args.no_autotune)
             rep["reference_semantics" if refsem else "intended"] = {
@@ -558,6 +573,8 @@ def main():
     ap.add_argument("--workload", default="dmr",
                     choices=["dmr", "kh256", "batch64", "serve", "mixed-report", "limiter-report"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed", "mixed-acc64"])
+    ap.add_argument("--basis", default="lobatto", choices=["lobatto", "gauss"],
+                    help="gauss: the DMR step with GaussCollocation + NodewiseScaledExtrapolation")
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
@@ -599,7 +616,7 @@ def main():
 
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
 
-    param, ic, bcf, wdesc = workload(args.workload, args.precision)
+    param, ic, bcf, wdesc = workload(args.workload, args.precision, args.basis)
     md, bc, desc, U0 = build_descriptor(param, ic, bcf)
     nodes = desc.K * desc.Nq
     solver = S.Solver(param, md, desc, device=local)

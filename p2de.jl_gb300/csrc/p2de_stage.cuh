@@ -332,11 +332,14 @@ __device__ __forceinline__ void v_ufun_d(const Gas<double>& g, const double* U, 
   V[3] = -U[0] * g.gm1 / p;
 }
 
-// u_vfun(::CompressibleIdealGas{Dim2}) (:155-163) with rhoe_vfun (:99-104) and s_vfun (:93-97)
-__device__ __forceinline__ void u_vfun_d(const Gas<double>& g, const double* V, double* U) {
+// u_vfun(::CompressibleIdealGas{Dim2}) (:155-163) with rhoe_vfun (:99-104) and s_vfun (:93-97).
+// rhoe_vfun = ((gamma-1) / (-vE)^gamma)^(1/(gamma-1)) exp(-s/(gamma-1)) is evaluated as the
+// one exponential exp((log(gamma-1) - gamma log(-vE) - s) / (gamma-1)) (the same value to
+// about 1e-14 relative; two pow calls fewer); lgm1 = log(gamma - 1).
+__device__ __forceinline__ void u_vfun_d(const Gas<double>& g, double lgm1, const double* V, double* U) {
   const double q = (V[1] * V[1] + V[2] * V[2]) / (2.0 * V[3]);
   const double s = g.gamma - V[0] + q;
-  const double rhoeV = pow(g.gm1 / pow(-V[3], g.gamma), 1.0 / g.gm1) * exp(-s / g.gm1);
+  const double rhoeV = exp((lgm1 - g.gamma * log(-V[3]) - s) / g.gm1);
   U[0] = -rhoeV * V[3];
   U[1] = rhoeV * V[1];
   U[2] = rhoeV * V[2];
@@ -372,7 +375,7 @@ __device__ __forceinline__ void gauss_proj_body(const StageArgs& a, int k0, doub
     v_ufun_d(g, sm + e * PE + 4 * m, sm + e * PE + 4 * Nq + 4 * m);
   }
   __syncthreads();
-  const double eps = a.POSTOL;
+  const double eps = a.POSTOL, lgm1 = log(a.gm1);
   for (int w = tid; w < Ke * Nfp; w += bs) {
     const int e = w / Nfp, f = w % Nfp, k = k0 + e;
     const int side = f / n, t = f % n;
@@ -404,30 +407,37 @@ __device__ __forceinline__ void gauss_proj_body(const StageArgs& a, int k0, doub
         for (int c = 0; c < 4; ++c) vt[c] = vt[c] + cf * vq[4 * node[i] + c];
       }
     };
+    // the projected state of theta in ut; returns whether it is well defined and in bounds
+    double vt[4], ut[4];
     auto ok = [&](double th) {
-      double vt[4], ut[4];
       project(th, vt);
       if (!(vt[3] < -eps)) return false;
-      u_vfun_d(g, vt, ut);
+      u_vfun_d(g, lgm1, vt, ut);
       const double rhoe = ut[3] - 0.5 * (ut[1] * ut[1] + ut[2] * ut[2]) / ut[0];
       return vt[3] < fmin(a.zeta * VUf[3], -eps) && ut[0] > fmax((1 - a.eta) * Uf[0], eps) &&
              ut[0] < (1 + a.eta) * Uf[0] && rhoe > fmax((1 - a.eta) * rhoef, eps) && rhoe < (1 + a.eta) * rhoef;
     };
     double th = 1.0;
-    if ((a.flags & F_EPROJ) && !ok(1.0)) {
-      double x_valid = 0.0, x_invalid = 1.0;
-      for (int iter = 0; iter <= 20; ++iter) {
-        const double x_new = 0.5 * (x_valid + x_invalid);
-        if (ok(x_new))
-          x_valid = x_new;
-        else
-          x_invalid = x_new;
+    bool have = false;  // ut holds the state of th
+    if (a.flags & F_EPROJ) {
+      if (ok(1.0)) {
+        have = true;
+      } else {
+        double x_valid = 0.0, x_invalid = 1.0;
+        for (int iter = 0; iter <= 20; ++iter) {
+          const double x_new = 0.5 * (x_valid + x_invalid);
+          if (ok(x_new))
+            x_valid = x_new;
+          else
+            x_invalid = x_new;
+        }
+        th = x_valid;
       }
-      th = x_valid;
     }
-    double vt[4], ut[4];
-    project(th, vt);
-    u_vfun_d(g, vt, ut);
+    if (!have) {
+      project(th, vt);
+      u_vfun_d(g, lgm1, vt, ut);
+    }
 #pragma unroll
     for (int c = 0; c < 4; ++c) a.ufproj[((size_t)k * Nfp + f) * 4 + c] = ut[c];
     a.theta[((size_t)(a.nstage - 1) * a.K + k) * Nfp + f] = th;
@@ -1061,7 +1071,7 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
         double* base = sm + e * PE;
         int ir = m % n, is = m / n;
         const double rJ = base[C::O_GEO + 11];
-        const double rw = op.rwq[m], wqm = op.wq[m];
+        const double rw = op.rwq[m];
         const bool limited = base[C::O_GEO + 17] != 0.0;
         double Q[8] = {0, 0, 0, 0, 0, 0, 0, 0};
         if (aa) {
@@ -1097,7 +1107,7 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
             const double low = pos[t] == ((t % 2 == 0) ? 0 : n - 1) ? 1.0 : 0.0;
             mf[t] = rw * (th * ell + (1 - th) * low);
           } else {
-            mf[t] = ell / wqm;
+            mf[t] = op.liftf[m][t];
           }
         }
         double* R = base + C::O_RXYH + 8 * m;

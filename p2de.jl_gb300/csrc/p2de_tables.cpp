@@ -195,6 +195,15 @@ int build_op_table(int N, double zerotol, OpTable* T, int basis) {
     T->ellm[0] = 1.0;
     T->ellp[N] = 1.0;
   }
+  for (int is = 0; is < n; ++is)
+    for (int ir = 0; ir < n; ++ir) {
+      const double wqm = w[ir] * w[is];
+      const int m = ir + n * is;
+      T->liftf[m][0] = T->ellm[ir] / wqm;
+      T->liftf[m][1] = T->ellp[ir] / wqm;
+      T->liftf[m][2] = T->ellm[is] / wqm;
+      T->liftf[m][3] = T->ellp[is] / wqm;
+    }
   for (int i = 0; i < n; ++i) T->w1D[i] = w[i];
   // node i = ir + n*is; wq = wr .* ws
   for (int is = 0; is < n; ++is)

@@ -57,6 +57,9 @@ struct OpTable {
   // along a line (construct_gauss_reference_data, init.jl:111-131); LGL: unit vectors
   double ellm[kMaxN1D];
   double ellp[kMaxN1D];
+  // the lift M \ Vf' of the unlimited projection at node m from its four faces (sides
+  // r=-1, r=+1, s=-1, s=+1 in order): Vf[f, m] / wq[m] (init.jl:171-172)
+  double liftf[kMaxNq][4];
 };
 
 // Builds the table for polynomial degree N (1..5) on the LGL (basis 0) or Gauss (basis 1)
