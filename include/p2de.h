@@ -69,6 +69,15 @@ typedef enum p2de_bound_type {
   P2DE_BOUND_TVD_AND_RELAXED_CELL_ENTROPY = 9         /* TVDAndRelaxedCellEntropyBound(beta) */
 } p2de_bound_type;
 
+/* Equations (Solver.jl:97-121). KPP{Dim2} (src/math/KPP.jl) is the scalar rotating-wave
+ * law u_t + (sin u)_x + (cos u)_y = 0 with wavespeed 1; its state arrays have one
+ * component per node (Nc = 1, p2de_solver_field_count), on LGL nodes, with the subcell
+ * limiter's factor equal to the shock-capture blending factor (subcell.jl:389-402). */
+typedef enum p2de_equation {
+  P2DE_EQUATION_COMPRESSIBLE_EULER = 0, /* CompressibleEulerIdealGas{Dim2}(gamma) */
+  P2DE_EQUATION_KPP = 1                 /* KPP{Dim2}() */
+} p2de_equation;
+
 /* Approximation bases (Solver.jl:38-40): collocation on the tensor-product LGL nodes, or
  * on the Gauss nodes with extrapolation to the face Gauss points (init.jl:83-131). */
 typedef enum p2de_basis {
@@ -92,8 +101,9 @@ typedef enum p2de_rhs_limiter {
                                  bound_type is not read */
 } p2de_rhs_limiter;
 
-/* Surface flux types (Solver.jl:19-22). Low order: LaxFriedrichsOnNodalVal only;
- * high order: LaxFriedrichsOnProjectedVal only. */
+/* Surface flux types (Solver.jl:19-22). Low order: LaxFriedrichsOnNodalVal, or
+ * LaxFriedrichsOnProjectedVal on LGL nodes (whose CFL adds alpha lambdaB + |B| ws / 2 per
+ * face, low_order_graph_viscosity.jl:245-318); high order: LaxFriedrichsOnProjectedVal. */
 typedef enum p2de_surface_flux {
   P2DE_FLUX_LAX_FRIEDRICHS_ON_NODAL_VAL = 0,
   P2DE_FLUX_LAX_FRIEDRICHS_ON_PROJECTED_VAL = 1
@@ -140,6 +150,8 @@ typedef struct p2de_param {
   double bound_beta;               /* beta of the Relaxed...CellEntropyBound types, else unused */
   int32_t approximation_basis;     /* p2de_basis */
   int32_t entropyproj_limiter;     /* p2de_entropyproj_limiter */
+  int32_t equation;                /* p2de_equation */
+  int32_t reserved_;               /* 0 */
 } p2de_param;
 
 /* Mesh and boundary data. geom/mapP/mapI/mapO/Ival follow StateParam.bcdata
@@ -191,8 +203,12 @@ typedef struct p2de_solver p2de_solver;
 /* Version of this ABI (P2DE_ABI_VERSION). */
 int p2de_abi_version(void);
 
-/* Number of doubles in a field for a solver of degree N with K elements. */
+/* Number of doubles in a field for a solver of degree N with K elements
+ * (CompressibleEulerIdealGas, Nc = 4). */
 int p2de_field_count(int32_t N, int32_t K, int32_t field, int64_t* count);
+
+/* Number of doubles in a field of this solver (its equation's Nc). */
+int p2de_solver_field_count(p2de_solver* s, int32_t field, int64_t* count);
 
 /* Replaces initialize_DG (src/dg/init.jl:44-60): builds the GLL operators for
  * degree N, uploads the mesh/BC data and allocates the device state on `device`.

@@ -105,8 +105,9 @@ class Oracle:
 
     def count(self, field: int) -> int:
         n, Nq, Nfp, K = self.N1D, self.Nq, self.Nfp, self.K
-        return {0: 4 * Nq * K, 1: 4 * Nq * K, 2: 4 * Nq * K, 3: 4 * Nq * K, 4: 8 * Nq * K, 5: 8 * Nq * K,
-                6: 8 * Nfp * K, 7: 8 * Nfp * K, 8: (Nq + n) * 2 * K, 9: 4 * Nq * K, 10: K, 11: Nfp * K}[field]
+        c = 1 if getattr(self.desc.param, "equation", 0) == 1 else 4  # KPP: one component
+        return {0: c * Nq * K, 1: c * Nq * K, 2: c * Nq * K, 3: c * Nq * K, 4: 2 * c * Nq * K, 5: 2 * c * Nq * K,
+                6: 2 * c * Nfp * K, 7: 2 * c * Nfp * K, 8: (Nq + n) * 2 * K, 9: c * Nq * K, 10: K, 11: Nfp * K}[field]
 
     def set_Uq(self, Uq):
         U = np.ascontiguousarray(Uq, dtype=np.float64).ravel()

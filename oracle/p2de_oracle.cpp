@@ -82,6 +82,7 @@ inline V4 vmul(const V4& a, const V4& b) { return {a[0] * b[0], a[1] * b[1], a[2
 // ---------------------------------------------------------------------------
 struct Euler {
   double gamma;
+  bool kpp = false;  // KPP{Dim2} (src/math/KPP.jl): the scalar in component 0, the rest 0
 
   // :24-28
   double pfun(const V4& U) const {
@@ -101,6 +102,7 @@ struct Euler {
   }
   // :59-62
   double wavespeed(const V4& U, double n1, double n2) const {
+    if (kpp) return 1.0;  // KPP.jl:1-3
     double un = n1 * U[1] + n2 * U[2];
     return wavespeed1(U[0], un, U[3]);
   }
@@ -121,6 +123,7 @@ struct Euler {
   }
   // :134-144
   V4 v_ufun(const V4& U) const {
+    if (kpp) return U;  // KPP.jl:5-7
     double s = sfun(U);
     double p = pfun(U);
     double v1 = (gamma + 1.0 - s) - (gamma - 1.0) * U[3] / p;
@@ -131,6 +134,7 @@ struct Euler {
   }
   // :155-163
   V4 u_vfun(const V4& V) const {
+    if (kpp) return V;  // KPP.jl:9-11
     double rhoeV = rhoe_vfun(V);
     double rho = -rhoeV * V[3];
     double rhou = rhoeV * V[1];
@@ -145,6 +149,12 @@ struct Euler {
   }
   // :175-194
   V2x4 fluxes(const V4& U) const {
+    if (kpp) {  // KPP.jl:13-18
+      V2x4 f;
+      f.x = {std::sin(U[0]), 0.0, 0.0, 0.0};
+      f.y = {std::cos(U[0]), 0.0, 0.0, 0.0};
+      return f;
+    }
     double rho = U[0], rhou = U[1], rhov = U[2], E = U[3];
     double p = pfun(U);
     double u = rhou / rho;
@@ -167,6 +177,18 @@ struct Euler {
     } else {
       return -da / (logL - logR);
     }
+  }
+  // fS(::KPP{Dim2}) (KPP.jl:25-38) with psi = (-cos u, sin u)
+  static V2x4 fS_kpp(double uL, double uR) {
+    V2x4 F;
+    if (std::fabs(uR - uL) < 1e-12) {
+      F.x = {0.5 * (std::sin(uL) + std::sin(uR)), 0.0, 0.0, 0.0};
+      F.y = {0.5 * (std::cos(uL) + std::cos(uR)), 0.0, 0.0, 0.0};
+    } else {
+      F.x = {(-std::cos(uR) - -std::cos(uL)) / (uR - uL), 0.0, 0.0, 0.0};
+      F.y = {(std::sin(uR) - std::sin(uL)) / (uR - uL), 0.0, 0.0, 0.0};
+    }
+    return F;
   }
   // :220-249; UL/UR = (rho, u, v, beta, log rho, log beta)
   V2x4 fS(const double* UL, const double* UR) const {
@@ -474,7 +496,7 @@ struct Solver {
       std::vector<double> ind(Nq), modal(Nq);
       for (int i = 0; i < Nq; ++i) {
         const V4& U = Uq[i + (size_t)Nq * k];
-        ind[i] = U[0] * eq.pfun(U);
+        ind[i] = eq.kpp ? U[0] : U[0] * eq.pfun(U);  // initialize_indicator! (shock_capture.jl:83-105)
       }
       for (int i = 0; i < Nq; ++i) {
         double sum = 0.0;
@@ -811,10 +833,13 @@ struct Solver {
   // rhs_low_graph_visc! (low_order_graph_viscosity.jl:4-41)
   // ---------------------------------------------------------------------------
   double rhs_low_graph_visc(double t, double dt, int nstage) {
-    // calculate_wavespeed_and_inviscid_flux! (:43-92) with LaxFriedrichsOnNodalVal (:51-61)
+    // calculate_wavespeed_and_inviscid_flux! (:43-92): face values by update_face_values!,
+    // LaxFriedrichsOnNodalVal (:51-61) or LaxFriedrichsOnProjectedVal (:63-71)
+    const bool lf_proj = prm.low_order_surface_flux == P2DE_FLUX_LAX_FRIEDRICHS_ON_PROJECTED_VAL;
 #pragma omp parallel for schedule(static)
     for (int k = 0; k < K; ++k) {
-      for (int f = 0; f < Nfp; ++f) Uf[f + (size_t)Nfp * k] = Uq[fq2q[f] + (size_t)Nq * k];
+      for (int f = 0; f < Nfp; ++f)
+        Uf[f + (size_t)Nfp * k] = lf_proj ? u_tilde[Nq + f + (size_t)Nh * k] : Uq[fq2q[f] + (size_t)Nq * k];
       for (int i = 0; i < Nq; ++i) flux[i + (size_t)Nh * k] = eq.fluxes(Uq[i + (size_t)Nq * k]);
       for (int f = 0; f < Nfp; ++f) {
         const V4& u = Uf[f + (size_t)Nfp * k];
@@ -955,7 +980,17 @@ struct Solver {
           for (int i = 0; i < Nq; ++i) {
             double li = 0.0;
             for (int j = 0; j < Nq; ++j) li += lambda[i + (size_t)Nq * (j + (size_t)Nq * k)];
-            for (int f : q2fq[i]) li += lambdaB[f + (size_t)Nfp * k];
+            for (int f : q2fq[i]) {
+              const size_t fk = f + (size_t)Nfp * k;
+              if (lf_proj) {  // lambda_B_CFL(::LaxFriedrichsOnProjectedVal) (:305-309)
+                auto B = Bx(f, k);
+                const double nn = norm2(B[0], B[1]);
+                li += find_alpha(Uq[fq2q[f] + (size_t)Nq * k], u_tilde[Nq + f + (size_t)Nh * k]) * lambdaB[fk] +
+                      0.5 * nn * wavespeed_f[fk];
+              } else {
+                li += lambdaB[fk];
+              }
+            }
             double wJq = Jq[i + (size_t)Nq * k] * wq[i];
             dtl = jmin(dtl, prm.CFL * 0.5 * wJq / li);
           }
@@ -967,14 +1002,37 @@ struct Solver {
     return dt;
   }
 
+  // find_alpha (low_order_graph_viscosity.jl:316-345): KPP 1; Euler, the alpha with
+  // alpha ui - uitilde of positive density and internal energy, doubling then bisecting
+  double find_alpha(const V4& ui, const V4& ut) const {
+    if (eq.kpp) return 1.0;
+    const double POSTOL = prm.POSTOL;
+    auto ok = [&](double al) {
+      V4 sub_ = sub(scal(al, ui), ut);
+      return sub_[0] > POSTOL && eq.rhoe_ufun(sub_) > POSTOL;
+    };
+    double alphaL = 0.0, alphaR = 1.0;
+    while (!ok(alphaR)) alphaR = 2 * alphaR;
+    const int maxit = 50;
+    double iter = 0.0;
+    const double tolerance = 1e-8;
+    while (iter < maxit || (alphaL - alphaR) > tolerance) {
+      const double alphaM = (alphaL + alphaR) / 2;
+      if (ok(alphaM)) alphaR = alphaM;
+      else alphaL = alphaM;
+      iter = iter + 1;
+    }
+    return alphaR;
+  }
+
   // ---------------------------------------------------------------------------
   // rhs_fluxdiff! (flux_differencing.jl:4-37)
   // ---------------------------------------------------------------------------
   void rhs_fluxdiff(double t, int nstage) {
-    // calculate_primitive_variables! (:39-70)
+    // calculate_primitive_variables! (:39-70; KPP only gathers uP, :72-88)
 #pragma omp parallel for schedule(static)
     for (int k = 0; k < K; ++k)
-      for (int i = 0; i < Nh; ++i) {
+      for (int i = 0; i < Nh && !eq.kpp; ++i) {
         size_t ik = i + (size_t)Nh * k;
         psi_tilde[ik] = eq.psi_ufun(u_tilde[ik]);
         beta[ik] = eq.betafun(u_tilde[ik]);
@@ -1041,10 +1099,15 @@ struct Solver {
         size_t ik = i + (size_t)Nh * k, jk = j + (size_t)Nh * k;
         const V4& ui = u_tilde[ik];
         const V4& uj = u_tilde[jk];
-        double Ui[6] = {ui[0], ui[1] / ui[0], ui[2] / ui[0], beta[ik], rholog[ik], betalog[ik]};
-        double Uj[6] = {uj[0], uj[1] / uj[0], uj[2] / uj[0], beta[jk], rholog[jk], betalog[jk]};
         auto S = Sx(i, j, k);
-        V2x4 F = eq.fS(Ui, Uj);
+        V2x4 F;
+        if (eq.kpp) {
+          F = Euler::fS_kpp(ui[0], uj[0]);
+        } else {
+          double Ui[6] = {ui[0], ui[1] / ui[0], ui[2] / ui[0], beta[ik], rholog[ik], betalog[ik]};
+          double Uj[6] = {uj[0], uj[1] / uj[0], uj[2] / uj[0], beta[jk], rholog[jk], betalog[jk]};
+          F = eq.fS(Ui, Uj);
+        }
         V2x4 SF;
         SF.x = scal(S[0], F.x);
         SF.y = scal(S[1], F.y);
@@ -1313,8 +1376,14 @@ struct Solver {
     // initialize_entropy_bounds!: lbound_s_modified = 0.0 except for the min-entropy
     // bounds (subcell.jl:4-19)
     update_smoothness();
-    if (min_entropy()) initialize_entropy_bounds(t, nstage);
-    if (tvd()) initialize_TVD_bounds(dt);
+    if (eq.kpp) {  // subcell_bound_limiter!(dim, ::KPP) (subcell.jl:389-402): 1 capped by blending
+      const int s2 = nstage - 1;
+      for (int k = 0; k < K; ++k)
+        for (int i = 0; i < Nq + N1D; ++i)
+          for (int d = 0; d < 2; ++d) L_local[LL(i, d, k, s2)] = jmin(1.0, blending_factor[k]);
+    }
+    if (!eq.kpp && min_entropy()) initialize_entropy_bounds(t, nstage);
+    if (!eq.kpp && tvd()) initialize_TVD_bounds(dt);
     // accumulate_f_bar!(::Dim2) (subcell.jl:163-206)
 #pragma omp parallel for schedule(static)
     for (int k = 0; k < K; ++k) {
@@ -1351,6 +1420,7 @@ struct Solver {
     const double zeta = prm.zeta;
 #pragma omp parallel for schedule(static)
     for (int k = 0; k < K; ++k) {
+      if (eq.kpp) continue;  // set above
       std::vector<V4> uL(Nq);
       for (int i = 0; i < Nq; ++i) {
         size_t ik = i + (size_t)Nq * k;
@@ -1608,7 +1678,7 @@ struct Solver {
 #pragma omp parallel for schedule(static)
     for (int k = 0; k < K; ++k) {
       double l = 1.0;
-      for (int i = 0; i < Nq; ++i) {
+      for (int i = 0; i < Nq && !eq.kpp; ++i) {  // zhang_shu_bound_limiter!(::KPP): 1 (zhangshu.jl:58-60)
         const size_t ik = i + (size_t)Nq * k;
         const V4 uL = add(Uq[ik], scal(dt, rhsL[ik]));
         const V4 P = scal(dt, sub(rhsH[ik], rhsL[ik]));
@@ -1703,7 +1773,22 @@ int validate(const p2de_param* p, const p2de_mesh* m, std::string& err) {
     err = "bound_type must be in 0..9 and rhs_limiter in 0..1";
     return P2DE_ERR_INVALID_ARGUMENT;
   }
-  if (p->low_order_surface_flux != P2DE_FLUX_LAX_FRIEDRICHS_ON_NODAL_VAL ||
+  if (p->equation < 0 || p->equation > 1) {
+    err = "equation must be 0 (CompressibleEulerIdealGas) or 1 (KPP)";
+    return P2DE_ERR_INVALID_ARGUMENT;
+  }
+  if (p->equation == P2DE_EQUATION_KPP &&
+      (p->approximation_basis != P2DE_BASIS_LOBATTO || m->nI || m->nO || m->nW || m->nS ||
+       (p->rhs_limiter == P2DE_LIMITER_SUBCELL && p->bound_type != P2DE_BOUND_POSITIVITY))) {
+    err = "KPP: LGL nodes, periodic or self-connected faces, PositivityBound or ZhangShu";
+    return P2DE_ERR_UNSUPPORTED;
+  }
+  if (p->low_order_surface_flux == P2DE_FLUX_LAX_FRIEDRICHS_ON_PROJECTED_VAL && p->approximation_basis != P2DE_BASIS_LOBATTO) {
+    err = "the LaxFriedrichsOnProjectedVal low-order flux is built on LGL nodes only";
+    return P2DE_ERR_UNSUPPORTED;
+  }
+  if ((p->low_order_surface_flux != P2DE_FLUX_LAX_FRIEDRICHS_ON_NODAL_VAL &&
+       p->low_order_surface_flux != P2DE_FLUX_LAX_FRIEDRICHS_ON_PROJECTED_VAL) ||
       p->high_order_surface_flux != P2DE_FLUX_LAX_FRIEDRICHS_ON_PROJECTED_VAL) {
     err = "only LaxFriedrichsOnNodalVal (low) and LaxFriedrichsOnProjectedVal (high) surface fluxes";
     return P2DE_ERR_UNSUPPORTED;
@@ -1735,6 +1820,7 @@ int oracle_create(const p2de_param* prm, const p2de_mesh* mesh, int nthreads, or
   s.N = prm->N;
   s.K = prm->K;
   s.eq.gamma = prm->gamma;
+  s.eq.kpp = prm->equation == P2DE_EQUATION_KPP;
   s.nthreads = nthreads;
 #ifdef _OPENMP
   if (nthreads > 0) omp_set_num_threads(nthreads);
@@ -1788,6 +1874,10 @@ int oracle_destroy(oracle_solver* o) {
 }
 
 int oracle_set_Uq(oracle_solver* o, const double* Uq) {
+  if (o->s.eq.kpp) {  // one component per node
+    for (size_t i = 0; i < o->s.Uq.size(); ++i) o->s.Uq[i] = {Uq[i], 0.0, 0.0, 0.0};
+    return P2DE_OK;
+  }
   std::memcpy(o->s.Uq.data(), Uq, sizeof(double) * 4 * o->s.Uq.size());
   return P2DE_OK;
 }
@@ -1819,8 +1909,22 @@ int oracle_ssp33(oracle_solver* o, double* t_out, int64_t* steps, double* dt_las
 
 int oracle_get_field(oracle_solver* o, int field, int nstage, double* out) {
   Solver& s = o->s;
-  auto cp4 = [&](const std::vector<V4>& a) { std::memcpy(out, a.data(), sizeof(double) * 4 * a.size()); };
-  auto cp8 = [&](const std::vector<V2x4>& a) { std::memcpy(out, a.data(), sizeof(double) * 8 * a.size()); };
+  const bool kpp = s.eq.kpp;  // KPP: component 0 of each state, (x, y) of each flux pair
+  auto cp4 = [&](const std::vector<V4>& a) {
+    if (kpp)
+      for (size_t i = 0; i < a.size(); ++i) out[i] = a[i][0];
+    else
+      std::memcpy(out, a.data(), sizeof(double) * 4 * a.size());
+  };
+  auto cp8 = [&](const std::vector<V2x4>& a) {
+    if (kpp)
+      for (size_t i = 0; i < a.size(); ++i) {
+        out[2 * i] = a[i].x[0];
+        out[2 * i + 1] = a[i].y[0];
+      }
+    else
+      std::memcpy(out, a.data(), sizeof(double) * 8 * a.size());
+  };
   switch (field) {
     case P2DE_FIELD_UQ: cp4(s.Uq); break;
     case P2DE_FIELD_RHSU: cp4(s.rhsU); break;

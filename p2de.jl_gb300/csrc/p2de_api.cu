@@ -262,6 +262,7 @@ struct p2de_solver {
   double* Lelem = nullptr;                                                 // 3 x K ZhangShuLimiter factors
   double* phimin = nullptr;                                                // initial min of phi
   bool gauss = false;                                                      // GaussCollocation
+  bool kpp = false;                                                        // KPP{Dim2}: Nc = 1
   double *ufproj = nullptr, *theta = nullptr;                              // Gauss face projection
   int diag_nblocks = 0;
   StageArgs base{};
@@ -333,6 +334,8 @@ int flags_for(const p2de_solver* s, int nstage, bool update, bool debug) {
   }
   if (s->prm.precision == P2DE_PRECISION_MIXED_ACC64) f |= F_ACC64;
   if (s->prm.shock_capture == 1 && (f & (F_DO_LIMIT | F_ZHANG_SHU))) f |= F_SHOCK;
+  if (s->kpp) f |= F_KPP;
+  if (s->prm.low_order_surface_flux == P2DE_FLUX_LAX_FRIEDRICHS_ON_PROJECTED_VAL) f |= F_LFPROJ;
   if (s->gauss) {
     f |= F_GAUSS;
     if (s->prm.entropyproj_limiter == P2DE_ENTROPYPROJ_NODEWISE_SCALED_EXTRAPOLATION) f |= F_EPROJ;
@@ -420,10 +423,23 @@ int p2de_initialize_DG(const p2de_param* prm, const p2de_mesh* mesh, int device,
   if (prm->N < 1 || prm->N > 5) return fail(nullptr, P2DE_ERR_INVALID_ARGUMENT, "N=%d outside 1..5", prm->N);
   if (prm->K < 1) return fail(nullptr, P2DE_ERR_INVALID_ARGUMENT, "K=%d", prm->K);
   if (!mesh->geom || !mesh->mapP) return fail(nullptr, P2DE_ERR_INVALID_ARGUMENT, "geom and mapP are required");
-  if (prm->low_order_surface_flux != P2DE_FLUX_LAX_FRIEDRICHS_ON_NODAL_VAL ||
+  if ((prm->low_order_surface_flux != P2DE_FLUX_LAX_FRIEDRICHS_ON_NODAL_VAL &&
+       prm->low_order_surface_flux != P2DE_FLUX_LAX_FRIEDRICHS_ON_PROJECTED_VAL) ||
       prm->high_order_surface_flux != P2DE_FLUX_LAX_FRIEDRICHS_ON_PROJECTED_VAL)
     return fail(nullptr, P2DE_ERR_UNSUPPORTED,
-                "surface fluxes: only LaxFriedrichsOnNodalVal (low order) and LaxFriedrichsOnProjectedVal (high order)");
+                "surface fluxes: LaxFriedrichsOnNodalVal or LaxFriedrichsOnProjectedVal (low order), "
+                "LaxFriedrichsOnProjectedVal (high order)");
+  if (prm->low_order_surface_flux == P2DE_FLUX_LAX_FRIEDRICHS_ON_PROJECTED_VAL &&
+      prm->approximation_basis != P2DE_BASIS_LOBATTO)
+    return fail(nullptr, P2DE_ERR_UNSUPPORTED, "the LaxFriedrichsOnProjectedVal low-order flux is built on LGL nodes");
+  if (prm->equation < 0 || prm->equation > 1)
+    return fail(nullptr, P2DE_ERR_INVALID_ARGUMENT, "equation %d out of range", prm->equation);
+  if (prm->equation == P2DE_EQUATION_KPP &&
+      (prm->approximation_basis != P2DE_BASIS_LOBATTO || prm->precision != P2DE_PRECISION_FP64 || mesh->nI ||
+       mesh->nO || mesh->nW || mesh->nS ||
+       (prm->rhs_limiter == P2DE_LIMITER_SUBCELL && prm->bound_type != P2DE_BOUND_POSITIVITY)))
+    return fail(nullptr, P2DE_ERR_UNSUPPORTED,
+                "KPP: LGL nodes, FP64, periodic or self-connected faces, PositivityBound or ZhangShuLimiter");
   if (prm->rhs_type < 0 || prm->rhs_type > 2 || prm->bound_type < 0 || prm->bound_type > 9 || prm->precision < 0 ||
       prm->precision > 2 || prm->shock_capture < 0 || prm->shock_capture > 1 || prm->rhs_limiter < 0 ||
       prm->rhs_limiter > 1)
@@ -500,6 +516,7 @@ int p2de_initialize_DG(const p2de_param* prm, const p2de_mesh* mesh, int device,
   }
   s->NSF = s->geo.nsf;
   s->gauss = prm->approximation_basis == P2DE_BASIS_GAUSS;
+  s->kpp = prm->equation == P2DE_EQUATION_KPP;
   if (s->gauss) {  // kernel A's Gauss layout is larger: its own elements per block
     s->geo.elems_per_block = s->geo.elems_per_block_gauss;
     s->geo.elems_per_block_max = s->geo.elems_per_block_max_gauss;
@@ -656,7 +673,16 @@ int p2de_destroy(p2de_solver* s) {
 int p2de_set_Uq(p2de_solver* s, const double* Uq) {
   if (!s || !Uq) return P2DE_ERR_INVALID_ARGUMENT;
   CK(cudaSetDevice(s->device));
-  CK(cudaMemcpyAsync(s->Uq, Uq, sizeof(double) * 4 * s->Nq * (size_t)s->K, cudaMemcpyHostToDevice, s->stream));
+  const size_t nodes = (size_t)s->Nq * s->K;
+  if (s->kpp) {  // one component per node, held as the first of four (the rest 0)
+    std::vector<double> full(4 * nodes, 0.0);
+    for (size_t i = 0; i < nodes; ++i) full[4 * i] = Uq[i];
+    CK(cudaMemcpyAsync(s->Uq, full.data(), sizeof(double) * full.size(), cudaMemcpyHostToDevice, s->stream));
+    CK(cudaMemsetAsync(s->status, 0, sizeof(int), s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return P2DE_OK;
+  }
+  CK(cudaMemcpyAsync(s->Uq, Uq, sizeof(double) * 4 * nodes, cudaMemcpyHostToDevice, s->stream));
   CK(cudaMemsetAsync(s->status, 0, sizeof(int), s->stream));
   CK(cudaStreamSynchronize(s->stream));
   return P2DE_OK;
@@ -695,8 +721,36 @@ int p2de_get_field(p2de_solver* s, int32_t field, int32_t nstage, double* out) {
       break;
   }
   CK(cudaSetDevice(s->device));
+  const bool state4 = field == P2DE_FIELD_UQ || field == P2DE_FIELD_RHSU || field == P2DE_FIELD_RHSL ||
+                      field == P2DE_FIELD_RHSH || field == P2DE_FIELD_RESW;
+  const bool flux8 = field == P2DE_FIELD_RHSXYL || field == P2DE_FIELD_RHSXYH || field == P2DE_FIELD_BF_L ||
+                     field == P2DE_FIELD_BF_H;
+  if (s->kpp && (state4 || flux8)) {  // the first component of each state / of each flux half
+    std::vector<double> full(cnt);
+    CK(cudaMemcpyAsync(full.data(), src, sizeof(double) * cnt, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    const int64_t items = state4 ? cnt / 4 : cnt / 8;
+    for (int64_t i = 0; i < items; ++i) {
+      if (state4) {
+        out[i] = full[4 * i];
+      } else {
+        out[2 * i] = full[8 * i];
+        out[2 * i + 1] = full[8 * i + 4];
+      }
+    }
+    return P2DE_OK;
+  }
   CK(cudaMemcpyAsync(out, src, sizeof(double) * cnt, cudaMemcpyDeviceToHost, s->stream));
   CK(cudaStreamSynchronize(s->stream));
+  return P2DE_OK;
+}
+
+int p2de_solver_field_count(p2de_solver* s, int32_t field, int64_t* count) {
+  if (!s || !count) return P2DE_ERR_INVALID_ARGUMENT;
+  int rc = p2de_field_count(s->N, s->K, field, count);
+  if (rc != P2DE_OK) return rc;
+  if (s->kpp && field != P2DE_FIELD_L_LOCAL && field != P2DE_FIELD_L && field != P2DE_FIELD_THETA_LOCAL)
+    *count /= 4;
   return P2DE_OK;
 }
 
@@ -1064,6 +1118,12 @@ int p2de_calculate_error(p2de_solver* s, const double* exact_Uq, double out[3]) 
   int rc = diag_prepare(s, true);
   if (rc != P2DE_OK) return rc;
   const size_t n = (size_t)4 * s->Nq * s->K;
+  std::vector<double> full;
+  if (s->kpp) {  // one component per node
+    full.assign(n, 0.0);
+    for (size_t i = 0; i < n / 4; ++i) full[4 * i] = exact_Uq[i];
+    exact_Uq = full.data();
+  }
   CK(cudaMemcpyAsync(s->exact, exact_Uq, sizeof(double) * n, cudaMemcpyHostToDevice, s->stream));
   CK(launch_error_norms(s->Uq, s->exact, s->geom, device_wq(s), s->Nq, (long long)s->Nq * s->K, s->diag_nblocks,
                         s->diag_partial, s->diag_out, s->stream));

@@ -30,7 +30,9 @@ enum : int {
   F_MIN_ENTROPY = 1 << 16,  // min-entropy bounds: bisection for phi >= Lphi - POSTOL
   F_RELAXED = 1 << 17,      // relaxed bounds: smoothness factor from the modal energies
   F_GAUSS = 1 << 18,        // GaussCollocation: projected face states, face pairs, Vf lift
-  F_EPROJ = 1 << 19         // NodewiseScaledExtrapolation: theta per face node
+  F_EPROJ = 1 << 19,        // NodewiseScaledExtrapolation: theta per face node
+  F_KPP = 1 << 20,          // KPP{Dim2}: the scalar in component 0, the others 0
+  F_LFPROJ = 1 << 21        // LaxFriedrichsOnProjectedVal low-order flux: its CFL term
 };
 
 // boundary codes per face node

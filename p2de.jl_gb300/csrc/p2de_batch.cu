@@ -224,7 +224,8 @@ int validate_solve(const p2de_param* p, const p2de_mesh* m, std::string& why) {
   if (p->low_order_surface_flux != P2DE_FLUX_LAX_FRIEDRICHS_ON_NODAL_VAL ||
       p->high_order_surface_flux != P2DE_FLUX_LAX_FRIEDRICHS_ON_PROJECTED_VAL || p->rhs_type < 0 || p->rhs_type > 2 ||
       p->bound_type < 0 || p->bound_type > 1 || p->shock_capture < 0 || p->shock_capture > 1 ||
-      p->rhs_limiter != P2DE_LIMITER_SUBCELL || p->approximation_basis != P2DE_BASIS_LOBATTO) {
+      p->rhs_limiter != P2DE_LIMITER_SUBCELL || p->approximation_basis != P2DE_BASIS_LOBATTO ||
+      p->equation != P2DE_EQUATION_COMPRESSIBLE_EULER) {
     why = "unsupported method";
     return P2DE_ERR_UNSUPPORTED;
   }

@@ -114,7 +114,7 @@ extern "C" int p2de_rhs_noalloc(const p2de_param* prm, const p2de_device_mesh* m
       prm->high_order_surface_flux != P2DE_FLUX_LAX_FRIEDRICHS_ON_PROJECTED_VAL || prm->rhs_type < 0 ||
       prm->rhs_type > 2 || prm->bound_type < 0 || prm->bound_type > 1 || prm->shock_capture < 0 ||
       prm->shock_capture > 1 || prm->rhs_limiter != P2DE_LIMITER_SUBCELL ||
-      prm->approximation_basis != P2DE_BASIS_LOBATTO)
+      prm->approximation_basis != P2DE_BASIS_LOBATTO || prm->equation != P2DE_EQUATION_COMPRESSIBLE_EULER)
     return P2DE_ERR_UNSUPPORTED;
   const int n1d = prm->N + 1;
   const size_t K = (size_t)prm->K;

@@ -294,6 +294,40 @@ __device__ __forceinline__ double density_bound(double U0, double P0, double Lrh
   return l;
 }
 
+// fS(::KPP{Dim2}) (KPP.jl:25-38), psi = (-cos u, sin u): the scalar fluxes in component 0
+__device__ __forceinline__ void fS_kpp(double uL, double uR, double* Fx, double* Fy) {
+  if (fabs(uR - uL) < 1e-12) {
+    Fx[0] = 0.5 * (sin(uL) + sin(uR));
+    Fy[0] = 0.5 * (cos(uL) + cos(uR));
+  } else {
+    Fx[0] = (-cos(uR) - -cos(uL)) / (uR - uL);
+    Fy[0] = (sin(uR) - sin(uL)) / (uR - uL);
+  }
+#pragma unroll
+  for (int c = 1; c < 4; ++c) Fx[c] = Fy[c] = 0.0;
+}
+
+// find_alpha(::CompressibleIdealGas) (low_order_graph_viscosity.jl:316-340): doubling, then
+// 50 halvings toward the alpha with alpha ui - uitilde of positive density and rhoe
+__device__ __forceinline__ double find_alpha(const double* ui, const double* ut, double POSTOL) {
+  auto ok = [&](double al) {
+    double q[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) q[c] = al * ui[c] - ut[c];
+    return q[0] > POSTOL && q[3] - 0.5 * (q[1] * q[1] + q[2] * q[2]) / q[0] > POSTOL;
+  };
+  double alphaL = 0.0, alphaR = 1.0;
+  for (int guard = 0; guard < 1100 && !ok(alphaR); ++guard) alphaR = 2 * alphaR;
+  for (int iter = 0; iter < 50; ++iter) {
+    const double alphaM = (alphaL + alphaR) / 2;
+    if (ok(alphaM))
+      alphaR = alphaM;
+    else
+      alphaL = alphaM;
+  }
+  return alphaR;
+}
+
 // s_modified_ufun (compressible_Navier_Stokes.jl:80-85): phi = rhoe rho^(-gamma), with
 // rhoe_ufun written as the reference writes it
 __device__ __forceinline__ double s_modified(double rho, double rhou, double rhov, double E, double gamma) {
@@ -513,6 +547,18 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
     double* base = sm + e * PE;
     const double* G = base + C::O_GEO;
     const double* U = base + C::O_U + 4 * m;
+    if (flags & F_KPP) {  // fluxes (sin u, cos u) (KPP.jl:13-18), wavespeed 1, indicator u
+      double* F = base + C::O_FLUX + 8 * m;
+#pragma unroll
+      for (int c = 0; c < 8; ++c) F[c] = 0.0;
+      F[0] = sin(U[0]);
+      F[4] = cos(U[0]);
+      base[C::O_WS + 2 * m] = 1.0;
+      base[C::O_WS + 2 * m + 1] = 1.0;
+      if (flags & F_SHOCK) base[C::O_LAMI + m] = U[0];
+      base[C::O_PRIM + 6 * m] = U[0];
+      continue;
+    }
     double rho = U[0], rhou = U[1], rhov = U[2], E = U[3];
     double rr = rcp(rho);
     double p = g.gm1 * fma(-0.5, (rhou * rhou + rhov * rhov) * rr, E);
@@ -768,9 +814,10 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
 #pragma unroll
       for (int c = 0; c < 4; ++c) uP[c] = post ? a.shock_post[c] : a.shock_pre[c];
     }
-    double rrP = rcp(uP[0]);
+    const bool kpp = flags & F_KPP;
+    double rrP = kpp ? 0.0 : rcp(uP[0]);
     double wsP = ws_own;
-    if (!self) {
+    if (!self && !kpp) {
       double rrN = (code == BC_INTERIOR) ? rrP : rcp(Unb[0]);
       wsP = wavespeed_r(g, rrN, n1 * Unb[1] + n2 * Unb[2], Unb[3]);
     }
@@ -784,7 +831,12 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
     if (aa) {
       // sxJ = ryJ = 0: the face's terms have only its own axis' half; the other is zero
       double fP[4];
-      flux_axis_r(g, uP, rrP, xs, fP);
+      if (kpp) {
+        fP[0] = xs ? sin(uP[0]) : cos(uP[0]);
+        fP[1] = fP[2] = fP[3] = 0.0;
+      } else {
+        flux_axis_r(g, uP, rrP, xs, fP);
+      }
       const double hB = xs ? hB1 : hB2;
       const int o = xs ? 0 : 4;
 #pragma unroll
@@ -799,7 +851,13 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
       }
     } else {
       double fPx[4], fPy[4];
-      fluxes_r(g, uP, rrP, fPx, fPy);
+      if (kpp) {
+        fPx[0] = sin(uP[0]);
+        fPy[0] = cos(uP[0]);
+        fPx[1] = fPx[2] = fPx[3] = fPy[1] = fPy[2] = fPy[3] = 0.0;
+      } else {
+        fluxes_r(g, uP, rrP, fPx, fPy);
+      }
 #pragma unroll
       for (int c = 0; c < 4; ++c) {
         double lf = lamB * (uP[c] - Uf[c]);
@@ -815,7 +873,13 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
         }
       }
     }
-    base[C::O_LAMB + f] = lamB;
+    // the face's CFL term: lambda_B_CFL (low_order_graph_viscosity.jl:301-309): lambdaB, or
+    // with the projected-value flux alpha lambdaB + |B| ws / 2 (alpha = 1 for KPP, else
+    // find_alpha of the face values, which are the nodal values on LGL nodes)
+    double lam_cfl = lamB;
+    if ((flags & F_LFPROJ) && (flags & F_CFL))
+      lam_cfl = (kpp ? 1.0 : find_alpha(Uf, Uf, a.POSTOL)) * lamB + 0.5 * nn * ws_own;
+    base[C::O_LAMB + f] = lam_cfl;
   }
   __syncthreads();
   if (GAUSS && do_high) {
@@ -981,7 +1045,10 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
       double* out = base + C::O_SCR + 8 * pp;
       if (sizeof(TH) == 8) {
         double Fx[4], Fy[4];
-        fS_fast(g, base + C::O_PRIM + 6 * i, base + C::O_PRIM + 6 * j, Fx, Fy);
+        if (flags & F_KPP)
+          fS_kpp(base[C::O_PRIM + 6 * i], base[C::O_PRIM + 6 * j], Fx, Fy);
+        else
+          fS_fast(g, base + C::O_PRIM + 6 * i, base + C::O_PRIM + 6 * j, Fx, Fy);
         if (!aa || ax == 0) {
 #pragma unroll
           for (int c = 0; c < 4; ++c) out[c] = Sxx * Fx[c];
@@ -1265,6 +1332,10 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
         uL[c] = low_update(U[c], dt_lim, rl[c]);
         P[c] = dt_lim * ((R[c] + R[4 + c]) - rl[c]);
       }
+      if (flags & F_KPP) {  // zhang_shu_bound_limiter!(::KPP) (zhangshu.jl:58-60)
+        base[C::O_SCR + m] = 1.0;
+        continue;
+      }
       const double Lrhoe = a.zeta * fma(-0.5, (uL[1] * uL[1] + uL[2] * uL[2]) * rcp(uL[0]), uL[3]);
       double l = density_bound(uL[0], P[0], a.zeta * uL[0], __longlong_as_double(0x7ff0000000000000LL), false, 0.0);
       l = fmin(l, rhoe_quadratic_solve(uL, P, Lrhoe, a.ZEROTOL));
@@ -1395,7 +1466,9 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
   // change the face's factor when every density bound of that face is nonzero, so only
   // those evaluations go to a list, solved with all lanes busy.
   // the 5-tuple bound (Lrho, Lrhoe, Lphi = 0, Urho_i, Urhoe = Inf) read as 4 names under
-  // the reference semantics: Urho = 0 and Urhoe = Urho_i (limiter_utils.jl:66-70)
+  // the reference semantics: Urho = 0 and Urhoe = Urho_i (limiter_utils.jl:66-70).
+  // KPP evaluates no bound (subcell_bound_limiter!(dim, ::KPP), subcell.jl:389-402).
+  if (!(flags & F_KPP)) {
   const bool upper0 = flags & F_REF_SEM;
   for (int w = tid; w < Ke * NEV; w += bs) {
     int e = w / NEV, r = w % NEV;
@@ -1466,6 +1539,7 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
   }
   if (a.counters && tid == 0 && nlist) atomicAdd(&a.counters[0], (unsigned long long)nlist);
   __syncthreads();
+  }
 
   // ---- P10: combine evaluations per subcell face; blending factor 1 (NoShockCapture)
   for (int w = tid; w < Ke * 2 * NSF; w += bs) {
@@ -1475,6 +1549,10 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
     const double* ev = base + C::O_EV;
     // 1, or the element's shock-capture blending factor (the final min of subcell.jl:345)
     double L = (flags & F_SHOCK) ? base[C::O_GEO + 15] : 1.0;
+    if (flags & F_KPP) {  // min(1, blending factor)
+      base[C::O_L + r] = fmin(1.0, L);
+      continue;
+    }
     if (d == 0) {
       int si = fi % (n + 1), sj = fi / (n + 1);
       if (si < n) L = min_nonneg_bits(L, ev[0 * Nq + si + n * sj]);
@@ -1793,9 +1871,10 @@ __device__ __forceinline__ void stage_b_body(const StageArgs& a, int k0, double*
       long long kr = order_key(U[0]), ke = order_key(re);
       rmin = kr < rmin ? kr : rmin;
       emin = ke < emin ? ke : emin;
-      // not (> 0): -0, negative or NaN, i.e. bits <= 0 or above +Inf's
-      if (__double_as_longlong(U[0]) <= 0 || __double_as_longlong(U[0]) > 0x7ff0000000000000LL ||
-          __double_as_longlong(re) <= 0 || __double_as_longlong(re) > 0x7ff0000000000000LL)
+      // not (> 0): -0, negative or NaN, i.e. bits <= 0 or above +Inf's; KPP has no positivity
+      if (!(flags & F_KPP) &&
+          (__double_as_longlong(U[0]) <= 0 || __double_as_longlong(U[0]) > 0x7ff0000000000000LL ||
+           __double_as_longlong(re) <= 0 || __double_as_longlong(re) > 0x7ff0000000000000LL))
         atomicOr(a.status, ST_NOT_POSITIVE);
     }
   }

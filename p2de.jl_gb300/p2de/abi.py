@@ -68,6 +68,9 @@ FIELD_L_LOCAL = 8
 FIELD_RESW = 9
 FIELD_L = 10
 FIELD_THETA_LOCAL = 11
+# p2de_equation
+EQUATION_COMPRESSIBLE_EULER = 0
+EQUATION_KPP = 1
 # p2de_basis, p2de_entropyproj_limiter
 BASIS_LOBATTO = 0
 BASIS_GAUSS = 1
@@ -101,6 +104,8 @@ class P2deParam(ctypes.Structure):
         ("bound_beta", c_double),
         ("approximation_basis", c_int32),
         ("entropyproj_limiter", c_int32),
+        ("equation", c_int32),
+        ("reserved_", c_int32),
     ]
 
 
@@ -157,6 +162,7 @@ class P2deError(RuntimeError):
 SOLVER_P = c_void_p
 EXPORTS = [
     ("p2de_abi_version", c_int, []),
+    ("p2de_solver_field_count", c_int, [SOLVER_P, c_int32, POINTER(c_int64)]),
     ("p2de_field_count", c_int, [c_int32, c_int32, c_int32, POINTER(c_int64)]),
     ("p2de_initialize_DG", c_int, [POINTER(P2deParam), POINTER(P2deMesh), c_int, POINTER(c_void_p)]),
     ("p2de_destroy", c_int, [SOLVER_P]),

@@ -171,6 +171,38 @@ def riemann2d(N=3, Kx=64, Ky=64, T=0.2, seed=0, **kw):
 
 
 # --- isentropic vortex ----------------------------------------------------------------
+def kpp_exact(equation=None, x=None, y=None, t=0.0):
+    """exact_sol of examples/2D/KPP.jl:9-16 (the initial data): 7 pi / 2 in the unit disc,
+    pi / 4 outside."""
+    r2 = np.asarray(x) ** 2 + np.asarray(y) ** 2
+    return np.where(r2 <= 1, 7 * np.pi / 2, np.pi / 4)
+
+
+def kpp(N=3, Kx=64, Ky=64, T=1.0, rhs_limiter=None, reference_semantics=True, **kw):
+    """examples/2D/KPP.jl:40-55: KPP{Dim2} on the periodic [-2, 2]^2, LGL nodes,
+    ESLimitedLowOrderPos(LaxFriedrichsOnProjectedVal, LaxFriedrichsOnProjectedVal),
+    SubcellLimiter(shockcapture=HennemannShockCapture()), zeta 0.1, eta 1.0, CFL 0.5,
+    dt0 1e-3."""
+    from dataclasses import replace
+
+    from .types import HennemannShockCapture, KPP, LaxFriedrichsOnProjectedVal
+
+    kw.setdefault("CFL", 0.5)
+    kw.setdefault("dt0", 1e-3)
+    if rhs_limiter is None:
+        rhs_limiter = SubcellLimiter(shockcapture=HennemannShockCapture())
+    param = default_param(N, (Kx, Ky), (-2.0, -2.0), (2.0, 2.0), T, rhs_limiter=rhs_limiter,
+                          reference_semantics=reference_semantics, **kw)
+    param = replace(param, equation=KPP(), limiting_param=LimitingParameter(zeta=0.1, eta=1.0),
+                    rhs=ESLimitedLowOrderPos(low_order_surface_flux=LaxFriedrichsOnProjectedVal(),
+                                             high_order_surface_flux=LaxFriedrichsOnProjectedVal()))
+
+    def initial_condition(param, x, y):
+        return kpp_exact(param.equation, x, y, 0.0)
+
+    return param, initial_condition, periodic_bc, kpp_exact
+
+
 def isentropic_vortex_exact(strength=8.5, x0=4.5, y0=5.0, ux=1.0, uy=0.0):
     """exact_sol of test/test_smoke.jl:6-20 with strength beta and advection (ux, uy)."""
 

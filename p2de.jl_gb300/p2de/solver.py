@@ -43,6 +43,8 @@ from .types import (
     TVDBound,
     HennemannShockCapture,
     ZhangShuLimiter,
+    KPP,
+    num_components,
 )
 
 
@@ -121,8 +123,15 @@ def lower_param(param: Param, K: int) -> abi.P2deParam:
         low, high = LaxFriedrichsOnNodalVal(), rhs.surface_flux
     else:
         raise UnsupportedMethod(f"rhs type {type(rhs).__name__} is not built")
-    if not isinstance(low, LaxFriedrichsOnNodalVal) or not isinstance(high, LaxFriedrichsOnProjectedVal):
-        raise UnsupportedMethod("surface fluxes: LaxFriedrichsOnNodalVal (low), LaxFriedrichsOnProjectedVal (high)")
+    if not isinstance(high, LaxFriedrichsOnProjectedVal):
+        raise UnsupportedMethod("high-order surface flux: LaxFriedrichsOnProjectedVal")
+    if isinstance(low, LaxFriedrichsOnNodalVal):
+        low_code = abi.FLUX_LF_NODAL
+    elif isinstance(low, LaxFriedrichsOnProjectedVal) and basis == abi.BASIS_LOBATTO:
+        low_code = abi.FLUX_LF_PROJECTED
+    else:
+        raise UnsupportedMethod("low-order surface flux: LaxFriedrichsOnNodalVal, or LaxFriedrichsOnProjectedVal on LGL")
+    kpp = isinstance(param.equation, KPP)
     lim = param.rhs_limiter
     bound = abi.BOUND_POSITIVITY
     limiter, beta = abi.LIMITER_SUBCELL, 0.0
@@ -144,13 +153,17 @@ def lower_param(param: Param, K: int) -> abi.P2deParam:
             beta = float(getattr(lim.bound, "beta", 0.0))
             if basis == abi.BASIS_GAUSS and "CellEntropy" in type(lim.bound).__name__:
                 raise UnsupportedMethod("cell-entropy bounds on Gauss collocation are not built")
+            if kpp and not isinstance(lim.bound, PositivityBound):
+                raise UnsupportedMethod("KPP: the subcell limiter reads no bound; use PositivityBound")
+    if kpp and basis != abi.BASIS_LOBATTO:
+        raise UnsupportedMethod("KPP on LGL nodes only")
     if param.precision not in abi.PRECISIONS:
         raise UnsupportedMethod("precision must be one of " + ", ".join(abi.PRECISIONS))
     gc, ts, lp = param.global_constants, param.timestepping_param, param.limiting_param
     return abi.P2deParam(
         N=param.N,
         K=K,
-        gamma=param.equation.gamma,
+        gamma=getattr(param.equation, "gamma", 1.4),
         POSTOL=gc.POSTOL,
         ZEROTOL=gc.ZEROTOL,
         zeta=lp.zeta,
@@ -161,7 +174,7 @@ def lower_param(param: Param, K: int) -> abi.P2deParam:
         T=ts.T,
         rhs_type=rhs_type,
         bound_type=bound,
-        low_order_surface_flux=abi.FLUX_LF_NODAL,
+        low_order_surface_flux=low_code,
         high_order_surface_flux=abi.FLUX_LF_PROJECTED,
         shock_capture=shock,
         shock_capture_a=sc_a,
@@ -170,6 +183,7 @@ def lower_param(param: Param, K: int) -> abi.P2deParam:
         bound_beta=beta,
         approximation_basis=basis,
         entropyproj_limiter=eproj,
+        equation=abi.EQUATION_KPP if kpp else abi.EQUATION_COMPRESSIBLE_EULER,
         reference_semantics=1 if param.reference_semantics else 0,
         precision=abi.PRECISIONS[param.precision],
     )
@@ -217,8 +231,11 @@ def evaluate_initial_condition(param: Param, md: MeshData, initial_condition) ->
     if isinstance(u, (tuple, list)):
         u = np.stack([np.broadcast_to(np.asarray(c, dtype=np.float64), md.x.shape) for c in u], axis=-1)
     u = np.ascontiguousarray(np.asarray(u, dtype=np.float64))
-    if u.shape != md.x.shape + (4,):
-        raise ValueError(f"initial condition returned shape {u.shape}, expected {md.x.shape + (4,)}")
+    nc = num_components(param.equation)
+    if nc == 1 and u.shape == md.x.shape:
+        u = u[..., None]
+    if u.shape != md.x.shape + (nc,):
+        raise ValueError(f"initial condition returned shape {u.shape}, expected {md.x.shape + (nc,)}")
     return u
 
 
@@ -256,7 +273,7 @@ class Solver:
 
     def field_count(self, field: int) -> int:
         c = c_int64()
-        self._check(self.lib.p2de_field_count(self.N, self.K, field, byref(c)))
+        self._check(self.lib.p2de_solver_field_count(self.handle, field, byref(c)))
         return c.value
 
     def get_field(self, field: int, nstage: int = 1) -> np.ndarray:

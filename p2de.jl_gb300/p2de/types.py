@@ -27,6 +27,13 @@ class CompressibleEulerIdealGas:
     dim: type = Dim2
 
 
+@dataclass(frozen=True)
+class KPP:
+    """KPP{Dim2}() (src/math/KPP.jl): u_t + (sin u)_x + (cos u)_y = 0."""
+
+    dim: type = Dim2
+
+
 def get_gamma(equation: CompressibleEulerIdealGas) -> float:
     return equation.gamma
 
@@ -210,7 +217,8 @@ def num_elements(param: Param) -> int:
 
 
 def num_components(equation=None) -> int:
-    return 4
+    """num_components (src/common/traits.jl:145-155)."""
+    return 1 if isinstance(equation, KPP) else 4
 
 
 # --- boundary data and time parameters ------------------------------------------------

@@ -459,6 +459,46 @@ def test_gauss_mesh_face_points():
     assert d.min() > 1e-3  # no face point is a node
 
 
+def test_kpp_conserves_and_keeps_constants():
+    """KPP (src/math/KPP.jl, examples/2D/KPP.jl): a constant state has no RHS; the
+    reference example's discontinuous data conserve the integral of u over periodic
+    steps, and the subcell factors are the blending factors (alphamax 1/2 on the disc's
+    edge, subcell.jl:389-402)."""
+    param, md, bc, desc, U0 = setup(problems.kpp, N=3, Kx=8, Ky=8, T=0.05)
+    o = Oracle(desc, nthreads=2)
+    o.set_Uq(np.full_like(U0, 1.3))
+    o.rhs(0.0, 5e-4, 1)
+    assert np.abs(o.get_field(abi.FIELD_RHSU)).max() < 1e-13
+    o.set_Uq(U0)
+    from p2de.mesh import gll_rule
+
+    w = np.outer(*(2 * [gll_rule(3)[1]])).ravel()
+    tot = lambda U: np.einsum("k,i,ki->", md.geom[:, 0], w, np.reshape(U, (desc.K, -1)))
+    t = 0.0
+    for _ in range(5):
+        t, _ = o.step(t)
+    assert abs(tot(o.get_field(abi.FIELD_UQ)) - tot(U0)) <= 1e-13 * abs(tot(U0))
+    L = o.get_field(abi.FIELD_L_LOCAL, 1).reshape(desc.K, -1)
+    assert L.min() == 0.5 and L.max() <= 1.0
+    o.close()
+
+
+def test_find_alpha_of_equal_states_is_just_above_one():
+    """find_alpha (low_order_graph_viscosity.jl:316-340) with ui = uitilde: (alpha - 1) ui
+    must have positive density and internal energy, so alpha lands just above 1."""
+    from dataclasses import replace
+
+    param, md, bc, desc, U0 = setup(problems.riemann2d, N=2, Kx=4, Ky=4, T=0.2, seed=4)
+    pp = replace(param, rhs=p2de.ESLimitedLowOrderPos(low_order_surface_flux=p2de.LaxFriedrichsOnProjectedVal()))
+    dts = []
+    for prm in (param, pp):
+        o = Oracle(S.make_descriptor(prm, md, bc), nthreads=1)
+        o.set_Uq(U0)
+        dts.append(o.rhs(0.0, 0.2, 1))
+        o.close()
+    assert dts[1] < dts[0]  # the extra |B| ws / 2 per face shortens the step
+
+
 def test_reference_semantics_give_low_order_rhs():
     """With the reference's bound destructuring (limiter_utils.jl:66-70) every interior
     subcell face gets factor 0 and rhsU equals the low-order rhsL up to rounding."""
