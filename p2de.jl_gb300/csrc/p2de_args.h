@@ -34,6 +34,8 @@ enum : int {
   F_KPP = 1 << 20,          // KPP{Dim2}: the scalar in component 0, the others 0
   F_LFPROJ = 1 << 21        // LaxFriedrichsOnProjectedVal low-order flux: its CFL term
 };
+// the modes whose branches only the EXT instantiation of stage kernel A compiles
+constexpr int kExtFlags = F_ZHANG_SHU | F_MIN_ENTROPY | F_RELAXED | F_GAUSS | F_EPROJ | F_KPP | F_LFPROJ;
 
 // boundary codes per face node
 enum : int8_t { BC_INTERIOR = 0, BC_INFLOW = 1, BC_OUTFLOW = 2, BC_WALL = 3, BC_SHOCK = 4 };

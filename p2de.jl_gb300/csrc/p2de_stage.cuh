@@ -60,9 +60,9 @@ struct Cfg {
   static constexpr int SCR = cmax(cmax(NPL * 9, NPH * 8), 16 * NSF);
   // shared-memory doubles per element, kernel A; regions whose lifetimes (phases) do not
   // overlap share storage
-  static constexpr int O_GEO = 0;                  // 18: J, rxJ, sxJ, ryJ, syJ, |gr|, nr, |gs|, ns, 1/J,
-                                                   // FP32 copies (12-14), blending (15), smoothness (16) factors
-  static constexpr int O_U = O_GEO + 18;           // 4 Nq
+  static constexpr int O_GEO = 0;                  // 16: J, rxJ, sxJ, ryJ, syJ, |gr|, nr, |gs|, ns, 1/J,
+                                                   // FP32 copies (12-14), blending factor (15)
+  static constexpr int O_U = O_GEO + 16;           // 4 Nq
   static constexpr int O_PRIM = O_U + 4 * Nq;      // 6 Nq: primitives (P1-P6); uL[4], Lrhoe, 4dt/(wq J) (P8-P9)
   static constexpr int O_FLUX = O_PRIM + 6 * Nq;   // 8 Nq: nodal fluxes (P1-P4)
   static constexpr int O_RXYH = O_FLUX;            //       high-order rhsxy (P7-P8)
@@ -92,9 +92,16 @@ struct Cfg {
   static constexpr int E_MAX_RAW = (int)((224 * 1024 - 64) / (sizeof(double) * PER_ELEM_A + sizeof(int) * NEV));
   static constexpr int E_MAX = E_MAX_RAW < 32 ? E_MAX_RAW : 32;
   static constexpr int FBAR = 16 * NSF;  // per element: [dir][H/L][face][c]
-  // GaussCollocation (kernel A with GAUSS): after the LGL layout, the projected face
-  // states, their primitives, theta, the face rows of QF1 and the volume-face pair terms
-  static constexpr int O_UF = (O_SCR + SCR + 1) & ~1;  // 4 Nfp
+  // EXT instantiations of kernel A: two more doubles per element after the LGL layout,
+  // the relaxed bounds' smoothness factor (O_XT) and the Gauss limited flag (O_XT + 1)
+  static constexpr int O_XT = PER_ELEM_A;
+  static constexpr int PER_ELEM_X = PER_ELEM_A + 2;
+  static constexpr size_t smem_x(int e) { return sizeof(double) * PER_ELEM_X * e + sizeof(int) * (NEV * e + 4); }
+  static_assert((224 * 1024 - 64) / (sizeof(double) * PER_ELEM_X + sizeof(int) * NEV) >= (size_t)E_MAX,
+                "the EXT layout fits every elements-per-block value of the LGL one");
+  // GaussCollocation (kernel A with GAUSS): after those, the projected face states, their
+  // primitives, theta, the face rows of QF1 and the volume-face pair terms
+  static constexpr int O_UF = PER_ELEM_X;                // 4 Nfp
   static constexpr int O_PF = O_UF + 4 * Nfp;       // 6 Nfp
   static constexpr int O_TH = O_PF + 6 * Nfp;       // Nfp
   static constexpr int O_QFF = O_TH + Nfp;          // 8 Nfp
@@ -489,11 +496,13 @@ __global__ void __launch_bounds__(Cfg<N1D>::THREADS) k_gauss_proj(StageArgs a) {
 // =====================================================================================
 // Body of kernel A for the E elements k0 .. k0+E-1 of the solve `a`; every early return
 // is uniform over the block. Used by the one-solve kernel and the batched kernel.
-template <int N1D, typename TH, bool GAUSS = false>
+// EXT: compiles the branches of kExtFlags; without it those flags are masked off, so their
+// tests fold away and the common modes run a lean instruction stream.
+template <int N1D, typename TH, bool GAUSS = false, bool EXT = false>
 __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double* sm) {
   using C = Cfg<N1D>;
   constexpr int n = C::n, Nq = C::Nq, Nfp = C::Nfp, NSF = C::NSF, NEV = C::NEV;
-  constexpr int PE = GAUSS ? C::PER_ELEM_G : C::PER_ELEM_A;
+  constexpr int PE = GAUSS ? C::PER_ELEM_G : (EXT ? C::PER_ELEM_X : C::PER_ELEM_A);
   static_assert(!GAUSS || sizeof(TH) == 8, "Gauss collocation runs in FP64");
   if (a.scal[S_DONE] != 0.0) return;
   const int E = a.epb;
@@ -502,7 +511,8 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
   const int tid = threadIdx.x, bs = blockDim.x;
   const int Ke = min(E, a.K - k0);
   if (Ke <= 0) return;
-  const int flags = a.flags;
+  static_assert(!GAUSS || EXT, "Gauss collocation is an EXT mode");
+  const int flags = EXT ? a.flags : (a.flags & ~kExtFlags);
   const bool aa = flags & F_AXIS_ALIGNED;
   Gas<double> g{a.gamma, a.gm1, 2.0 * a.gm1};
   const double dt_lim = a.scal[S_DT_LIM];
@@ -611,13 +621,13 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
       Pm[4] = log(U[0]);
       Pm[5] = log(beta);
     }
-    // is_Vf_limited (flux_differencing.jl:316-318): any theta < 1 on the element, into G[17]
+    // is_Vf_limited (flux_differencing.jl:316-318): any theta < 1 on the element, into O_XT + 1
     for (int e = tid; e < Ke; e += bs) {
       double* base = sm + e * PE;
       double lim = 0.0;
       for (int f = 0; f < Nfp; ++f)
         if (base[C::O_TH + f] < 1.0) lim = 1.0;
-      base[C::O_GEO + 17] = lim;
+      base[C::O_XT + 1] = lim;
     }
   }
   __syncthreads();
@@ -625,7 +635,7 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
   // ---- P1b: smoothness indicator (shock_capture.jl:49-81): modal energies of the
   //      indicator through inv(VDM), smoothness max(E_N, E_{N-1}) / E. Hennemann
   //      blending factor max(min(1 - alpha, 1), 1/2) (:118-137) into G[15]; the relaxed
-  //      bounds' smoothness factor (update_smoothness_factor!, subcell.jl:937-956) into G[16]
+  //      bounds' smoothness factor (update_smoothness_factor!, subcell.jl:937-956) into O_XT
   if (flags & (F_SHOCK | F_RELAXED)) {
     for (int w = tid; w < Ke * Nq; w += bs) {
       const int e = w / Nq, i = w % Nq;
@@ -661,7 +671,7 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
           eps = 1.0;
         else
           eps = 0.5 - 0.5 * sin(3.141592653589793 * (sk - a.s0) / 2.0);
-        base[C::O_GEO + 16] = eps;
+        base[C::O_XT] = eps;
       }
     }
     __syncthreads();
@@ -1139,7 +1149,7 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
         int ir = m % n, is = m / n;
         const double rJ = base[C::O_GEO + 11];
         const double rw = op.rwq[m];
-        const bool limited = base[C::O_GEO + 17] != 0.0;
+        const bool limited = base[C::O_XT + 1] != 0.0;
         double Q[8] = {0, 0, 0, 0, 0, 0, 0, 0};
         if (aa) {
 #pragma unroll
@@ -1449,7 +1459,7 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
         lb = fmin(lb, s_modified(Un[0], Un[1], Un[2], Un[3], a.gamma));
       }
       if (flags & F_RELAXED) {
-        const double eps = base[C::O_GEO + 16];
+        const double eps = base[C::O_XT];
         lb = eps * lb + (1 - eps) * a.phimin[0];
       }
       lim[3] = lb - a.POSTOL;
@@ -1662,7 +1672,7 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
         }
       double rhs = sB - sdl;
       // rhs_es of the relaxed bounds (subcell.jl:750-753)
-      if (flags & F_RELAXED) rhs = (1 - a.beta * G[16]) * rhs;
+      if (flags & F_RELAXED) rhs = (1 - a.beta * base[C::O_XT]) * rhs;
       double est = sumLd - rhs;
       double tol = jmax(0.0, sdl - sB);
       if (est > tol) {
@@ -1723,10 +1733,10 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
   }
 }
 
-template <int N1D, typename TH, bool GAUSS = false>
+template <int N1D, typename TH, bool GAUSS = false, bool EXT = false>
 __global__ void __launch_bounds__(Cfg<N1D>::THREADS) k_stage_a(StageArgs a) {
   extern __shared__ __align__(16) double sm[];
-  stage_a_body<N1D, TH, GAUSS>(a, blockIdx.x * a.epb, sm);
+  stage_a_body<N1D, TH, GAUSS, EXT>(a, blockIdx.x * a.epb, sm);
 }
 
 // =====================================================================================

@@ -18,8 +18,14 @@ cudaError_t stage_prepare(StageGeometry* geo) {
   if (e != cudaSuccess) return e;
   e = cudaFuncSetAttribute(k_stage_b<N1D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::smem_b(C::E_MAX));
   if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(k_stage_a<N1D, double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  e = cudaFuncSetAttribute(k_stage_a<N1D, double, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)C::smem_g(C::E_MAX_G));
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(k_stage_a<N1D, double, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)C::smem_x(C::E_MAX));
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(k_stage_a<N1D, float, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)C::smem_x(C::E_MAX));
   if (e != cudaSuccess) return e;
   geo->elems_per_block = C::E;
   geo->elems_per_block_max = C::E_MAX;
@@ -39,13 +45,18 @@ cudaError_t launch_stage_a(const StageArgs& a, bool mixed, cudaStream_t st) {
   if (a.flags & F_GAUSS) {
     if (mixed || a.epb < 1 || a.epb > C::E_MAX_G) return cudaErrorInvalidValue;
     int grid = (a.K + a.epb - 1) / a.epb;
-    k_stage_a<N1D, double, true><<<grid, C::THREADS, C::smem_g(a.epb), st>>>(a);
+    k_stage_a<N1D, double, true, true><<<grid, C::THREADS, C::smem_g(a.epb), st>>>(a);
     return cudaGetLastError();
   }
   if (a.epb < 1 || a.epb > C::E_MAX) return cudaErrorInvalidValue;
   int grid = (a.K + a.epb - 1) / a.epb;
-  if (mixed)
+  const bool ext = a.flags & kExtFlags;
+  if (mixed && ext)
+    k_stage_a<N1D, float, false, true><<<grid, C::THREADS, C::smem_x(a.epb), st>>>(a);
+  else if (mixed)
     k_stage_a<N1D, float><<<grid, C::THREADS, C::smem_a(a.epb), st>>>(a);
+  else if (ext)
+    k_stage_a<N1D, double, false, true><<<grid, C::THREADS, C::smem_x(a.epb), st>>>(a);
   else
     k_stage_a<N1D, double><<<grid, C::THREADS, C::smem_a(a.epb), st>>>(a);
   return cudaGetLastError();
