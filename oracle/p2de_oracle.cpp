@@ -1479,6 +1479,7 @@ struct Solver {
     if (cell_entropy()) {
       initialize_ES_subcell_limiting();
       enforce_ES_subcell_volume(s);
+      if (gauss()) enforce_ES_subcell_interface(s);
       // enforce_ES_subcell_interface!(::LobattoCollocation) is a no-op (subcell.jl:755-757)
     }
     // symmetrize_limiting_parameters!(::Dim2) (subcell.jl:418-456), subcell_index_P_x/y
@@ -1585,6 +1586,57 @@ struct Solver {
           sy += vsum(vmul(dv, fL));
         }
       sum_dvfbarL[k] = {sx, sy};
+    }
+  }
+
+  // enforce_ES_subcell_interface!(::Dim2, ::GaussCollocation) (subcell.jl:759-823) with
+  // solve_l_es_interface! (:811-817): per boundary subcell face, the largest l on the
+  // bisection grid of [0, min(L, L_partner)] with l dvfH + (1 - l) dvfL <= dpsi, written to
+  // the element's own factor. The reference runs this under @batch, where an element reads
+  // its partner's factor before or after the partner's own update; here elements go in
+  // ascending order, as on one thread.
+  void enforce_ES_subcell_interface(int s) {
+    const int N1Dp1 = N1D + 1;
+    auto solve = [&](double& Lown, double Lpar, double dvfH, double dvfL, double dpsi) {
+      const double l = jmin(Lown, Lpar);
+      auto f = [&](double li) { return li * dvfH + (1 - li) * dvfL <= dpsi; };
+      double x_valid = 0.0, x_invalid = l;
+      if (f(x_invalid)) {
+        Lown = x_invalid;
+        return;
+      }
+      for (int iter = 0; iter <= 20; ++iter) {
+        const double x_new = 0.5 * (x_valid + x_invalid);
+        if (f(x_new)) x_valid = x_new;
+        else x_invalid = x_new;
+      }
+      Lown = x_valid;
+    };
+    for (int k = 0; k < K; ++k) {
+      for (int sj = 0; sj < N1D; ++sj)
+        for (int si : {0, N1D}) {
+          const int iface = (si == 0) ? sj : sj + N1D;
+          const size_t fk = iface + (size_t)Nfp * k, fP = (size_t)(mapP[fk] - 1);
+          int iP, kP;
+          face_of(mapP[fk], iP, kP);
+          const int sjP = iP % N1D, siP = (iP / N1D == 0) ? 0 : N1D;
+          const V4 dv = sub(vf[fk], vf[fP]);
+          const double dpsi = psif[fk][0] - psif[fP][0];
+          solve(L_local[LL(si + N1Dp1 * sj, 0, k, s)], L_local[LL(siP + N1Dp1 * sjP, 0, kP, s)],
+                vsum(vmul(dv, fstar_H[fk].x)), vsum(vmul(dv, fstar_L[fk].x)), dpsi);
+        }
+      for (int si = 0; si < N1D; ++si)
+        for (int sj : {0, N1D}) {
+          const int iface = (sj == 0) ? si + 2 * N1D : si + 3 * N1D;
+          const size_t fk = iface + (size_t)Nfp * k, fP = (size_t)(mapP[fk] - 1);
+          int iP, kP;
+          face_of(mapP[fk], iP, kP);
+          const int siP = iP % N1D, sjP = (iP / N1D == 2) ? 0 : N1D;
+          const V4 dv = sub(vf[fk], vf[fP]);
+          const double dpsi = psif[fk][1] - psif[fP][1];
+          solve(L_local[LL(si + N1D * sj, 1, k, s)], L_local[LL(siP + N1D * sjP, 1, kP, s)],
+                vsum(vmul(dv, fstar_H[fk].y)), vsum(vmul(dv, fstar_L[fk].y)), dpsi);
+        }
     }
   }
 

@@ -180,8 +180,21 @@ cudaError_t launch_a_one(int n1d, const StageArgs& a, bool mixed, cudaStream_t s
 bool needs_phi_min(const StageArgs& a) {
   return (a.flags & F_MIN_ENTROPY) && (a.flags & F_RELAXED) && a.nstage == 1;
 }
+// Gauss collocation with a cell-entropy bound: the interface step between kernels A and B
+bool needs_es_interface(const StageArgs& a) { return (a.flags & F_GAUSS) && (a.flags & F_CELL_ENTROPY); }
 int a_launches(const StageArgs& a) {
-  return ((a.flags & F_TVD) ? 2 : 1) + (needs_phi_min(a) ? 1 : 0) + ((a.flags & F_GAUSS) ? 1 : 0);
+  return ((a.flags & F_TVD) ? 2 : 1) + (needs_phi_min(a) ? 1 : 0) + ((a.flags & F_GAUSS) ? 1 : 0) +
+         (needs_es_interface(a) ? 1 : 0);
+}
+cudaError_t launch_es_interface_n1d(int n1d, const StageArgs& a, cudaStream_t st) {
+  switch (n1d) {
+    case 2: return launch_es_interface<2>(a, st);
+    case 3: return launch_es_interface<3>(a, st);
+    case 4: return launch_es_interface<4>(a, st);
+    case 5: return launch_es_interface<5>(a, st);
+    case 6: return launch_es_interface<6>(a, st);
+  }
+  return cudaErrorInvalidValue;
 }
 cudaError_t launch_gauss_proj_n1d(int n1d, const StageArgs& a, cudaStream_t st) {
   switch (n1d) {
@@ -211,7 +224,9 @@ cudaError_t launch_a_n1d(int n1d, const StageArgs& a, bool mixed, cudaStream_t s
     cudaError_t e = launch_a_one(n1d, lo, mixed, st);
     if (e != cudaSuccess) return e;
   }
-  return launch_a_one(n1d, a, mixed, st);
+  cudaError_t e = launch_a_one(n1d, a, mixed, st);
+  if (e != cudaSuccess || !needs_es_interface(a)) return e;
+  return launch_es_interface_n1d(n1d, a, st);
 }
 cudaError_t launch_b_n1d(int n1d, const StageArgs& a, cudaStream_t st) {
   switch (n1d) {
@@ -450,8 +465,6 @@ int p2de_initialize_DG(const p2de_param* prm, const p2de_mesh* mesh, int device,
   if (prm->approximation_basis == P2DE_BASIS_GAUSS) {
     if (prm->precision != P2DE_PRECISION_FP64)
       return fail(nullptr, P2DE_ERR_UNSUPPORTED, "GaussCollocation runs in FP64 only");
-    if (prm->rhs_limiter == P2DE_LIMITER_SUBCELL && (bound_flags(prm->bound_type) & F_CELL_ENTROPY))
-      return fail(nullptr, P2DE_ERR_UNSUPPORTED, "cell-entropy bounds on GaussCollocation are not built");
   }
   const int64_t n1 = prm->N + 1, Nfp = 4 * n1, Nq = n1 * n1;
   const int64_t nfk = Nfp * prm->K;

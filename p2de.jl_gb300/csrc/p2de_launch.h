@@ -27,6 +27,8 @@ template <int N1D>
 cudaError_t launch_stage_b(const StageArgs& a, cudaStream_t st);
 template <int N1D>
 cudaError_t launch_gauss_proj(const StageArgs& a, cudaStream_t st);
+template <int N1D>
+cudaError_t launch_es_interface(const StageArgs& a, cudaStream_t st);
 
 // Per-element geometry factors (geom_factor) for K elements: out has 16 doubles per element.
 cudaError_t launch_geom_table(const double* geom, int K, double* out, cudaStream_t st);

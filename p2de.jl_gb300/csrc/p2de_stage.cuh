@@ -373,6 +373,19 @@ __device__ __forceinline__ void v_ufun_d(const Gas<double>& g, const double* U, 
   V[3] = -U[0] * g.gm1 / p;
 }
 
+// v_ufun_d with every operation an explicit round-to-nearest intrinsic: the compiler cannot
+// contract it into FMAs, so equal states give bitwise-equal entropy variables wherever it is
+// inlined (the interface step compares their jumps with 0)
+__device__ __forceinline__ void v_ufun_rn(const Gas<double>& g, const double* U, double* V) {
+  const double ke = __ddiv_rn(__dmul_rn(0.5, __dadd_rn(__dmul_rn(U[1], U[1]), __dmul_rn(U[2], U[2]))), U[0]);
+  const double p = __dmul_rn(g.gm1, __dsub_rn(U[3], ke));
+  const double s = __dsub_rn(log(p), __dmul_rn(g.gamma, log(U[0])));
+  V[0] = __dsub_rn(__dsub_rn(__dadd_rn(g.gamma, 1.0), s), __ddiv_rn(__dmul_rn(g.gm1, U[3]), p));
+  V[1] = __ddiv_rn(__dmul_rn(U[1], g.gm1), p);
+  V[2] = __ddiv_rn(__dmul_rn(U[2], g.gm1), p);
+  V[3] = __ddiv_rn(__dmul_rn(-U[0], g.gm1), p);
+}
+
 // u_vfun(::CompressibleIdealGas{Dim2}) (:155-163) with rhoe_vfun (:99-104) and s_vfun (:93-97).
 // rhoe_vfun = ((gamma-1) / (-vE)^gamma)^(1/(gamma-1)) exp(-s/(gamma-1)) is evaluated as the
 // one exponential exp((log(gamma-1) - gamma log(-vE) - s) / (gamma-1)) (the same value to
@@ -483,6 +496,89 @@ __device__ __forceinline__ void gauss_proj_body(const StageArgs& a, int k0, doub
     for (int c = 0; c < 4; ++c) a.ufproj[((size_t)k * Nfp + f) * 4 + c] = ut[c];
     a.theta[((size_t)(a.nstage - 1) * a.K + k) * Nfp + f] = th;
   }
+}
+
+// enforce_ES_subcell_interface!(::Dim2, ::GaussCollocation) (subcell.jl:759-823) with
+// solve_l_es_interface! (:811-817) on the factors before symmetrization: every boundary
+// subcell face (one per face node) takes the largest l on the bisection grid of
+// [0, min(L, L_partner)] with l dvfH + (1 - l) dvfL <= dpsi, dv and dpsi the jumps of v and
+// psi at the face nodes' volume nodes, f* = BF / B on the face's axis. In the order of one
+// thread (elements ascending; x faces by line, lower face first, then y faces) the face
+// that comes first reads its partner's old factor and the second one the first's new
+// one; each pair is done by the item of its first face.
+template <int N1D>
+__device__ __forceinline__ void es_interface_body(const StageArgs& a, long long w) {
+  using C = Cfg<N1D>;
+  constexpr int n = C::n, Nq = C::Nq, Nfp = C::Nfp, NSF = C::NSF;
+  if (a.scal[S_DONE] != 0.0) return;
+  if (w >= (long long)a.K * Nfp) return;
+  const OpTable& op = *a.ops;
+  const Gas<double> g{a.gamma, a.gm1, 2.0 * a.gm1};
+  const int k = (int)(w / Nfp), f = (int)(w % Nfp);
+  const int lin = a.nbr[(size_t)k * Nfp + f];
+  const int kP = lin / Nfp, fP = lin % Nfp;
+  auto pos = [&](int ff) { return ff < 2 * n ? 2 * (ff % n) + ff / n : 2 * n + 2 * (ff % n) + (ff / n - 2); };
+  const long long key = (long long)k * Nfp + pos(f), keyP = (long long)kP * Nfp + pos(fP);
+  if (key >= keyP) return;  // the partner's item (or a face without a partner)
+  auto node = [&](int ff) {
+    const int side = ff / n, tt = ff % n;
+    return side == 0 ? n * tt : side == 1 ? (n - 1) + n * tt : side == 2 ? tt : tt + n * (n - 1);
+  };
+  auto lidx = [&](int kk, int ff) {  // the factor of face node ff in Lpre
+    const int side = ff / n, tt = ff % n;
+    const int idx = side == 0 ? (n + 1) * tt : side == 1 ? n + (n + 1) * tt : side == 2 ? tt : tt + n * n;
+    return (size_t)kk * 2 * NSF + (side < 2 ? 0 : NSF) + idx;
+  };
+  double vA[4], vB[4];
+  const double* UA = a.Uq + 4 * ((size_t)k * Nq + node(f));
+  const double* UB = a.Uq + 4 * ((size_t)kP * Nq + node(fP));
+  v_ufun_rn(g, UA, vA);
+  v_ufun_rn(g, UB, vB);
+  const int d = f < 2 * n ? 0 : 1;  // both faces lie on the same axis
+  // every product rounded by itself (no FMA contraction), as the reference's psif and
+  // dv .* f* are: equal states must give a jump of exactly 0
+  const double dpsi = __dsub_rn(__dmul_rn(a.gm1, UA[1 + d]), __dmul_rn(a.gm1, UB[1 + d]));
+  // BF / B on the axis: the x (y) component of f* at an x (y) face
+  auto dvf = [&](int kk, int ff, const double* dv, const double* BF) {
+    const double* G = a.geomx + (size_t)kk * kGeomStride;
+    const int side = ff / n, tt = ff % n;
+    const double Bf = (side == 0 || side == 2) ? -op.w1D[tt] : op.w1D[tt];
+    const double B = (d == 0 ? (side < 2 ? G[1] : G[2]) : (side < 2 ? G[3] : G[4])) * Bf;
+    double p[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) p[c] = __dmul_rn(dv[c], __ddiv_rn(BF[((size_t)kk * Nfp + ff) * 8 + 4 * d + c], B));
+    return __dadd_rn(__dadd_rn(__dadd_rn(p[0], p[1]), p[2]), p[3]);
+  };
+  auto solve = [&](double Lown, double Lpar, double dvfH, double dvfL, double dps) {
+    const double l = fmin(Lown, Lpar);
+    auto fok = [&](double li) { return __dadd_rn(__dmul_rn(li, dvfH), __dmul_rn(1.0 - li, dvfL)) <= dps; };
+    if (fok(l)) return l;
+    double x_valid = 0.0, x_invalid = l;
+    for (int iter = 0; iter <= 20; ++iter) {
+      const double x_new = 0.5 * (x_valid + x_invalid);
+      if (fok(x_new))
+        x_valid = x_new;
+      else
+        x_invalid = x_new;
+    }
+    return x_valid;
+  };
+  double dvA[4], dvB[4];
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    dvA[c] = __dsub_rn(vA[c], vB[c]);
+    dvB[c] = __dsub_rn(vB[c], vA[c]);
+  }
+  const size_t iA = lidx(k, f), iB = lidx(kP, fP);
+  const double LA = solve(a.Lpre[iA], a.Lpre[iB], dvf(k, f, dvA, a.BFH), dvf(k, f, dvA, a.BFL), dpsi);
+  const double LB = solve(a.Lpre[iB], LA, dvf(kP, fP, dvB, a.BFH), dvf(kP, fP, dvB, a.BFL), -dpsi);
+  a.Lpre[iA] = LA;
+  a.Lpre[iB] = LB;
+}
+
+template <int N1D>
+__global__ void __launch_bounds__(256) k_es_interface(StageArgs a) {
+  es_interface_body<N1D>(a, blockIdx.x * (long long)blockDim.x + threadIdx.x);
 }
 
 template <int N1D>
@@ -1313,8 +1409,8 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
       a.rhsH[(size_t)k0 * Nq * 4 + w] = R[c] + R[4 + c];
     }
   }
-  if (dbg) {
-    for (int w = tid; w < Ke * Nq * 8; w += bs) {
+  if (dbg || (GAUSS && (flags & F_CELL_ENTROPY))) {
+    for (int w = tid; w < Ke * Nq * 8 && dbg; w += bs) {
       int e = w / (Nq * 8), r = w % (Nq * 8);
       if (do_low) a.rhsxyL[(size_t)k0 * Nq * 8 + w] = sm[e * PE + C::O_RXYL + r];
       if (do_high) a.rhsxyH[(size_t)k0 * Nq * 8 + w] = sm[e * PE + C::O_RXYH + r];

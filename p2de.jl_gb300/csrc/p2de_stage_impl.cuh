@@ -72,6 +72,13 @@ cudaError_t launch_gauss_proj(const StageArgs& a, cudaStream_t st) {
 }
 
 template <int N1D>
+cudaError_t launch_es_interface(const StageArgs& a, cudaStream_t st) {
+  const long long items = (long long)a.K * Cfg<N1D>::Nfp;
+  k_es_interface<N1D><<<(int)((items + 255) / 256), 256, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+template <int N1D>
 cudaError_t launch_stage_b(const StageArgs& a, cudaStream_t st) {
   using C = Cfg<N1D>;
   if (a.epb < 1 || a.epb > C::E_MAX) return cudaErrorInvalidValue;

@@ -6,4 +6,5 @@ template cudaError_t stage_prepare<2>(StageGeometry*);
 template cudaError_t launch_stage_a<2>(const StageArgs&, bool, cudaStream_t);
 template cudaError_t launch_stage_b<2>(const StageArgs&, cudaStream_t);
 template cudaError_t launch_gauss_proj<2>(const StageArgs&, cudaStream_t);
+template cudaError_t launch_es_interface<2>(const StageArgs&, cudaStream_t);
 }  // namespace p2de

@@ -151,8 +151,6 @@ def lower_param(param: Param, K: int) -> abi.P2deParam:
                 raise UnsupportedMethod(f"bound {type(lim.bound).__name__} is not built")
             bound = code
             beta = float(getattr(lim.bound, "beta", 0.0))
-            if basis == abi.BASIS_GAUSS and "CellEntropy" in type(lim.bound).__name__:
-                raise UnsupportedMethod("cell-entropy bounds on Gauss collocation are not built")
             if kpp and not isinstance(lim.bound, PositivityBound):
                 raise UnsupportedMethod("KPP: the subcell limiter reads no bound; use PositivityBound")
     if kpp and basis != abi.BASIS_LOBATTO:

@@ -50,11 +50,13 @@ def compare_theta(g, o, K, nstage):
     np.testing.assert_array_equal(tg, to)
 
 
+@pytest.mark.parametrize("refsem", [True, False])
 @pytest.mark.parametrize("N", [1, 2, 3, 4, 5])
 @pytest.mark.parametrize("problem", list(PROBLEMS))
-def test_gauss_rhs(N, problem):
+def test_gauss_rhs(N, problem, refsem):
     prob, kw = PROBLEMS[problem]
-    param, md, bc, desc, U0 = setup(prob, N=N, rhs_limiter=LIMITERS["positivity"], **GAUSS, **kw)
+    param, md, bc, desc, U0 = setup(prob, N=N, rhs_limiter=LIMITERS["positivity"], reference_semantics=refsem,
+                                    **GAUSS, **kw)
     compare_rhs(param, md, desc, U0, dt=1e-3, nstage=1)
     o = oracle_for(desc, U0)
     g = gpu_for(param, md, desc, U0)
@@ -125,12 +127,67 @@ def test_gauss_reference_example_configuration():
 def test_gauss_rejects_what_is_not_built():
     from dataclasses import replace
 
-    from p2de.types import PositivityAndCellEntropyBound
-
     param, md, bc, desc, U0 = setup(problems.riemann2d, N=2, Kx=4, Ky=4, T=0.2, seed=4,
                                     rhs_limiter=SubcellLimiter(bound=PositivityBound()), **GAUSS)
-    with pytest.raises(S.UnsupportedMethod):
-        S.lower_param(replace(param, rhs_limiter=SubcellLimiter(bound=PositivityAndCellEntropyBound())), desc.K)
     mixed = S.make_descriptor(replace(param, precision="mixed"), md, bc)
     with pytest.raises(p2de.P2deError):
         S.Solver(replace(param, precision="mixed"), md, mixed)
+
+
+CELL_BOUNDS = {
+    "cell": "PositivityAndCellEntropyBound",
+    "tvd-cell": "TVDAndCellEntropyBound",
+    "relaxed-cell": "PositivityAndRelaxedCellEntropyBound",
+}
+# intended semantics: the volume greedy reacts to rounding-level entropy production
+# (see test_gpu_parity.py); under the reference's semantics it never fires
+TOL_INTENDED_CELL = 1e-6
+
+
+def _cell_bound(name):
+    import p2de.types as T
+
+    cls = getattr(T, CELL_BOUNDS[name])
+    return cls(beta=0.5) if "Relaxed" in CELL_BOUNDS[name] else cls()
+
+
+@pytest.mark.parametrize("refsem", [True, False])
+@pytest.mark.parametrize("bound", list(CELL_BOUNDS))
+@pytest.mark.parametrize("N", [2, 3, 5])
+def test_gauss_cell_entropy_rhs(N, bound, refsem):
+    """enforce_ES_subcell_interface!(::GaussCollocation) (subcell.jl:759-823): the
+    interface step between kernels A and B, in the one-thread order of the oracle."""
+    param, md, bc, desc, U0 = setup(problems.riemann2d, N=N, Kx=6, Ky=5, T=0.2, seed=4,
+                                    rhs_limiter=SubcellLimiter(bound=_cell_bound(bound)), reference_semantics=refsem,
+                                    **GAUSS)
+    tol = TOL if refsem else TOL_INTENDED_CELL
+    compare_rhs(param, md, desc, U0, dt=1e-3, nstage=1, tol=tol, interior_L=False)
+    o = oracle_for(desc, U0)
+    g = gpu_for(param, md, desc, U0)
+    o.rhs(0.0, 1e-3, 2)
+    S.rhs_bang(None, g, None, p2de.TimeParam(0.0, 1e-3, 2))
+    # under the reference's semantics a Gauss face's factor is 0 or 1 by the sign of the
+    # density difference of the two face fluxes, which is rounding where they agree (a
+    # one-ulp change of the input flips 27-70 factors of the oracle, rhsU moves 3e-16):
+    # rhsU is compared, the factors only for their range
+    Lg = g.get_field(abi.FIELD_L_LOCAL, 2)
+    assert np.all((Lg >= 0) & (Lg <= 1))
+    assert relerr(g.get_field(abi.FIELD_RHSU), o.get_field(abi.FIELD_RHSU)) <= tol
+    g.close()
+    o.close()
+
+
+@pytest.mark.parametrize("bound", ["cell", "tvd-cell"])
+def test_gauss_cell_entropy_steps(bound):
+    param, md, bc, desc, U0 = setup(problems.riemann2d, N=3, Kx=6, Ky=5, T=0.2, seed=7,
+                                    rhs_limiter=SubcellLimiter(bound=_cell_bound(bound)), **GAUSS)
+    o = oracle_for(desc, U0)
+    g = gpu_for(param, md, desc, U0)
+    to, tg = 0.0, 0.0
+    for _ in range(3):
+        to, _ = o.step(to)
+        tg, _ = S.ssp33_step(g, tg)
+    assert abs(tg - to) <= 1e-13 * abs(to)
+    assert relerr(g.get_field(abi.FIELD_UQ), o.get_field(abi.FIELD_UQ)) <= TOL
+    g.close()
+    o.close()

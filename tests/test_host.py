@@ -73,8 +73,7 @@ def test_lowering_rejects_what_is_not_built():
     assert S.lower_param(param, K).rhs_type == 0
     assert S.lower_param(replace(param, rhs=LowOrderPositivity()), K).rhs_type == 1
     assert S.lower_param(replace(param, rhs=EntropyStable()), K).rhs_type == 2
-    with pytest.raises(S.UnsupportedMethod):  # cell-entropy bounds on Gauss nodes
-        S.lower_param(replace(param, approximation_basis=GaussCollocation()), K)
+    assert S.lower_param(replace(param, approximation_basis=GaussCollocation()), K).approximation_basis == abi.BASIS_GAUSS
     g = S.lower_param(replace(param, approximation_basis=GaussCollocation(), entropyproj_limiter=NodewiseScaledExtrapolation(),
                               rhs_limiter=SubcellLimiter(bound=PositivityBound())), K)
     assert g.approximation_basis == abi.BASIS_GAUSS
