@@ -101,9 +101,10 @@ typedef enum p2de_rhs_limiter {
                                  bound_type is not read */
 } p2de_rhs_limiter;
 
-/* Surface flux types (Solver.jl:19-22). Low order: LaxFriedrichsOnNodalVal, or
- * LaxFriedrichsOnProjectedVal on LGL nodes (whose CFL adds alpha lambdaB + |B| ws / 2 per
- * face, low_order_graph_viscosity.jl:245-318); high order: LaxFriedrichsOnProjectedVal. */
+/* Surface flux types (Solver.jl:19-22). Low order: LaxFriedrichsOnNodalVal or
+ * LaxFriedrichsOnProjectedVal (the entropy-projected face states; its CFL adds
+ * alpha lambdaB + |B| ws / 2 per face, low_order_graph_viscosity.jl:245-318); high order:
+ * LaxFriedrichsOnProjectedVal. */
 typedef enum p2de_surface_flux {
   P2DE_FLUX_LAX_FRIEDRICHS_ON_NODAL_VAL = 0,
   P2DE_FLUX_LAX_FRIEDRICHS_ON_PROJECTED_VAL = 1

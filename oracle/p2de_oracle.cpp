@@ -1835,10 +1835,6 @@ int validate(const p2de_param* p, const p2de_mesh* m, std::string& err) {
     err = "KPP: LGL nodes, periodic or self-connected faces, PositivityBound or ZhangShu";
     return P2DE_ERR_UNSUPPORTED;
   }
-  if (p->low_order_surface_flux == P2DE_FLUX_LAX_FRIEDRICHS_ON_PROJECTED_VAL && p->approximation_basis != P2DE_BASIS_LOBATTO) {
-    err = "the LaxFriedrichsOnProjectedVal low-order flux is built on LGL nodes only";
-    return P2DE_ERR_UNSUPPORTED;
-  }
   if ((p->low_order_surface_flux != P2DE_FLUX_LAX_FRIEDRICHS_ON_NODAL_VAL &&
        p->low_order_surface_flux != P2DE_FLUX_LAX_FRIEDRICHS_ON_PROJECTED_VAL) ||
       p->high_order_surface_flux != P2DE_FLUX_LAX_FRIEDRICHS_ON_PROJECTED_VAL) {

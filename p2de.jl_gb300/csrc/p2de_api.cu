@@ -444,9 +444,6 @@ int p2de_initialize_DG(const p2de_param* prm, const p2de_mesh* mesh, int device,
     return fail(nullptr, P2DE_ERR_UNSUPPORTED,
                 "surface fluxes: LaxFriedrichsOnNodalVal or LaxFriedrichsOnProjectedVal (low order), "
                 "LaxFriedrichsOnProjectedVal (high order)");
-  if (prm->low_order_surface_flux == P2DE_FLUX_LAX_FRIEDRICHS_ON_PROJECTED_VAL &&
-      prm->approximation_basis != P2DE_BASIS_LOBATTO)
-    return fail(nullptr, P2DE_ERR_UNSUPPORTED, "the LaxFriedrichsOnProjectedVal low-order flux is built on LGL nodes");
   if (prm->equation < 0 || prm->equation > 1)
     return fail(nullptr, P2DE_ERR_INVALID_ARGUMENT, "equation %d out of range", prm->equation);
   if (prm->equation == P2DE_EQUATION_KPP &&

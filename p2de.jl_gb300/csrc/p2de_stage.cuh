@@ -873,8 +873,13 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
     double B1 = g1 * Bf, B2 = g2 * Bf;
     double nn = wt * gn;
     double n1 = Bf < 0 ? -nh1 : nh1, n2 = Bf < 0 ? -nh2 : nh2;
-    const double* Uf = base + C::O_U + 4 * q;
-    double ws_own = base[C::O_WS + 2 * q + (xs ? 0 : 1)];
+    // the face values of the low-order flux: the node's (LaxFriedrichsOnNodalVal) or, with
+    // LaxFriedrichsOnProjectedVal on Gauss nodes, the projected face state (update_face_values!,
+    // low_order_graph_viscosity.jl:51-71), the neighbour's from ufproj
+    const bool projL = GAUSS && (flags & F_LFPROJ);
+    const double* Uf = projL ? base + C::O_UF + 4 * f : base + C::O_U + 4 * q;
+    double ws_own = projL ? wavespeed_r(g, rcp(Uf[0]), n1 * Uf[1] + n2 * Uf[2], Uf[3])
+                          : base[C::O_WS + 2 * q + (xs ? 0 : 1)];
     size_t fk = (size_t)k * Nfp + f;
     int lin = a.nbr[fk];
     bool self = lin == (int)fk;
@@ -882,6 +887,9 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
     if (self) {
 #pragma unroll
       for (int c = 0; c < 4; ++c) Unb[c] = Uf[c];
+    } else if (projL) {
+#pragma unroll
+      for (int c = 0; c < 4; ++c) Unb[c] = __ldg(a.ufproj + 4 * (size_t)lin + c);
     } else {
       int kP = lin / Nfp, iP = lin % Nfp;
       int sP = iP / n, tP = iP % n;
@@ -905,9 +913,10 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
       const double* iv = a.Ival + 4 * (size_t)a.bcidx[fk];
 #pragma unroll
       for (int c = 0; c < 4; ++c) uP[c] = iv[c];
-    } else if (code == BC_OUTFLOW) {
+    } else if (code == BC_OUTFLOW) {  // the own node's Uq (get_uP_and_enforce_BC!, :117-123)
+      const double* Uq = base + C::O_U + 4 * q;
 #pragma unroll
-      for (int c = 0; c < 4; ++c) uP[c] = Uf[c];
+      for (int c = 0; c < 4; ++c) uP[c] = Uq[c];
     } else if (code == BC_WALL) {
       double mn = Uf[1] * n1 + Uf[2] * n2;
       uP[0] = Uf[0];
@@ -928,7 +937,9 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
       wsP = wavespeed_r(g, rrN, n1 * Unb[1] + n2 * Unb[2], Unb[3]);
     }
     double lamB = 0.5 * nn * fmax(ws_own, wsP);
-    const double* Ff = base + C::O_FLUX + 8 * q;
+    double Fp[8];  // the projected face state's fluxes (projL)
+    if (projL) fluxes_r(g, Uf, rcp(Uf[0]), Fp, Fp + 4);
+    const double* Ff = projL ? Fp : base + C::O_FLUX + 8 * q;
     double* BL = base + C::O_BFL + 8 * f;
     double* BH = base + C::O_BFH + 8 * f;
     bool lf_zero_high = (code == BC_INFLOW || code == BC_OUTFLOW || code == BC_SHOCK);
@@ -984,7 +995,7 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
     // find_alpha of the face values, which are the nodal values on LGL nodes)
     double lam_cfl = lamB;
     if ((flags & F_LFPROJ) && (flags & F_CFL))
-      lam_cfl = (kpp ? 1.0 : find_alpha(Uf, Uf, a.POSTOL)) * lamB + 0.5 * nn * ws_own;
+      lam_cfl = (kpp ? 1.0 : find_alpha(base + C::O_U + 4 * q, Uf, a.POSTOL)) * lamB + 0.5 * nn * ws_own;
     base[C::O_LAMB + f] = lam_cfl;
   }
   __syncthreads();

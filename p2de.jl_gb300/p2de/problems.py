@@ -171,6 +171,45 @@ def riemann2d(N=3, Kx=64, Ky=64, T=0.2, seed=0, **kw):
 
 
 # --- isentropic vortex ----------------------------------------------------------------
+def sedov_exact(gamma=1.4, r_ini=4 * 3 / 80):
+    """exact_sol of examples/2D/sedov.jl:9-20 (the initial data): rho 1, at rest, pressure
+    (gamma - 1) / (pi r_ini^2) inside r < r_ini (r_ini = 12 / 80 there, whatever the mesh)
+    and 1e-5 outside."""
+
+    def exact_sol(equation, x, y, t):
+        r = np.sqrt(np.asarray(x) ** 2 + np.asarray(y) ** 2)
+        p = np.where(r < r_ini, (gamma - 1) * 1 / np.pi / r_ini / r_ini, 1e-5)
+        one = np.ones_like(r)
+        return (one, 0 * one, 0 * one, p)
+
+    return exact_sol
+
+
+def sedov(N=3, Kx=80, Ky=80, T=1.0, rhs_limiter=None, reference_semantics=True, **kw):
+    """examples/2D/sedov.jl:42-55: periodic [-1.5, 1.5]^2, GaussCollocation with
+    NodewiseScaledExtrapolation, ESLimitedLowOrderPos(LaxFriedrichsOnProjectedVal,
+    LaxFriedrichsOnProjectedVal), ZhangShuLimiter, zeta 0.1, eta 0.1, CFL 0.5, dt0 1e-3."""
+    from dataclasses import replace
+
+    from .types import GaussCollocation, LaxFriedrichsOnProjectedVal, NodewiseScaledExtrapolation, ZhangShuLimiter
+
+    kw.setdefault("CFL", 0.5)
+    kw.setdefault("dt0", 1e-3)
+    param = default_param(N, (Kx, Ky), (-1.5, -1.5), (1.5, 1.5), T,
+                          rhs_limiter=rhs_limiter if rhs_limiter is not None else ZhangShuLimiter(),
+                          reference_semantics=reference_semantics, approximation_basis=GaussCollocation(),
+                          entropyproj_limiter=NodewiseScaledExtrapolation(), **kw)
+    param = replace(param, limiting_param=LimitingParameter(zeta=0.1, eta=0.1),
+                    rhs=ESLimitedLowOrderPos(low_order_surface_flux=LaxFriedrichsOnProjectedVal(),
+                                             high_order_surface_flux=LaxFriedrichsOnProjectedVal()))
+    exact = sedov_exact(param.equation.gamma)
+
+    def initial_condition(param, x, y):
+        return primitive_to_conservative(param.equation, exact(param.equation, x, y, 0.0))
+
+    return param, initial_condition, periodic_bc, exact
+
+
 def kpp_exact(equation=None, x=None, y=None, t=0.0):
     """exact_sol of examples/2D/KPP.jl:9-16 (the initial data): 7 pi / 2 in the unit disc,
     pi / 4 outside."""

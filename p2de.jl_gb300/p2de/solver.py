@@ -127,10 +127,10 @@ def lower_param(param: Param, K: int) -> abi.P2deParam:
         raise UnsupportedMethod("high-order surface flux: LaxFriedrichsOnProjectedVal")
     if isinstance(low, LaxFriedrichsOnNodalVal):
         low_code = abi.FLUX_LF_NODAL
-    elif isinstance(low, LaxFriedrichsOnProjectedVal) and basis == abi.BASIS_LOBATTO:
+    elif isinstance(low, LaxFriedrichsOnProjectedVal):
         low_code = abi.FLUX_LF_PROJECTED
     else:
-        raise UnsupportedMethod("low-order surface flux: LaxFriedrichsOnNodalVal, or LaxFriedrichsOnProjectedVal on LGL")
+        raise UnsupportedMethod("low-order surface flux: LaxFriedrichsOnNodalVal or LaxFriedrichsOnProjectedVal")
     kpp = isinstance(param.equation, KPP)
     lim = param.rhs_limiter
     bound = abi.BOUND_POSITIVITY

@@ -191,3 +191,47 @@ def test_gauss_cell_entropy_steps(bound):
     assert relerr(g.get_field(abi.FIELD_UQ), o.get_field(abi.FIELD_UQ)) <= TOL
     g.close()
     o.close()
+
+
+@pytest.mark.parametrize("N", [2, 3, 5])
+@pytest.mark.parametrize("problem", ["riemann", "dmr"])
+@pytest.mark.parametrize("limiter", ["positivity", "zhang-shu"])
+def test_gauss_projected_low_order_flux(N, problem, limiter):
+    """LaxFriedrichsOnProjectedVal as the low-order flux on Gauss nodes: the projected face
+    states in the graph-viscosity surface term, outflow from the own node's Uq, and the
+    CFL term alpha lambdaB + |B| ws / 2 with find_alpha of the nodal and projected states."""
+    from dataclasses import replace
+
+    prob, kw = PROBLEMS[problem]
+    param, md, bc, desc, U0 = setup(prob, N=N, rhs_limiter=LIMITERS[limiter], **GAUSS, **kw)
+    param = replace(param, rhs=p2de.ESLimitedLowOrderPos(low_order_surface_flux=p2de.LaxFriedrichsOnProjectedVal()))
+    desc = S.make_descriptor(param, md, bc)
+    compare_rhs(param, md, desc, U0, dt=0.2, nstage=1, interior_L=False)
+    o = oracle_for(desc, U0)
+    g = gpu_for(param, md, desc, U0)
+    to, tg = 0.0, 0.0
+    for _ in range(3):
+        to, _ = o.step(to)
+        tg, _ = S.ssp33_step(g, tg)
+    assert abs(tg - to) <= 1e-13 * abs(to)
+    assert relerr(g.get_field(abi.FIELD_UQ), o.get_field(abi.FIELD_UQ)) <= TOL
+    g.close()
+    o.close()
+
+
+def test_reference_sedov_configuration():
+    """examples/2D/sedov.jl's configuration (Gauss, NodewiseScaledExtrapolation, projected
+    low- and high-order fluxes, Zhang-Shu, eta 0.1; pressure 1e-5 around the blast) on a
+    16 x 16 mesh of its domain, 5 steps."""
+    param, md, bc, desc, U0 = setup(problems.sedov, N=3, Kx=16, Ky=16, T=0.1)
+    o = oracle_for(desc, U0)
+    g = gpu_for(param, md, desc, U0)
+    to, tg = 0.0, 0.0
+    for _ in range(5):
+        to, _ = o.step(to)
+        tg, _ = S.ssp33_step(g, tg)
+    assert abs(tg - to) <= 1e-13 * abs(to)
+    assert relerr(g.get_field(abi.FIELD_UQ), o.get_field(abi.FIELD_UQ)) <= TOL
+    assert g.get_field(abi.FIELD_THETA_LOCAL, 1).min() < 1.0
+    g.close()
+    o.close()
