@@ -25,7 +25,7 @@
 extern "C" {
 #endif
 
-#define P2DE_ABI_VERSION 3
+#define P2DE_ABI_VERSION 4
 
 typedef enum p2de_status {
   P2DE_OK = 0,
@@ -73,9 +73,20 @@ typedef enum p2de_bound_type {
  * law u_t + (sin u)_x + (cos u)_y = 0 with wavespeed 1; its state arrays have one
  * component per node (Nc = 1, p2de_solver_field_count), on LGL nodes, with the subcell
  * limiter's factor equal to the shock-capture blending factor (subcell.jl:389-402). */
+/* CompressibleEulerIdealGas{Dim1}(gamma) (Solver.jl:97-121, compressible_Navier_Stokes.jl
+ * Dim1 methods) on a line of K elements: Nq = N+1 nodes and Nfp = 2 face nodes (r = -1, +1)
+ * per element, states (rho, rhou, E) (Nc = 3), mesh geom rows (J, rxJ, 0, 0, 0), Ival nI x 3.
+ * The reference's own Dim1 path does not run: Bx(::Dim1) passes its arguments to
+ * reference_to_physical in the wrong order (rhs_utils.jl:18), a MethodError in every RHS.
+ * With reference_semantics = 1 the solver is therefore refused (P2DE_ERR_UNSUPPORTED); with 0
+ * it runs the Dim1 methods with their evident meaning: Bx = Br rxJ; the subcell bound from
+ * rho_bound(dim, ...) (subcell.jl:225-237); N entries of dvdf per element (State.jl:184 sizes
+ * them Nq - N1D = 0); and the element-boundary factors symmetrized across mapP with the last
+ * used subcell face Nq+1 (subcell.jl:405-415 pairs index `end` = 2 N1D of element k-1 mod K). */
 typedef enum p2de_equation {
-  P2DE_EQUATION_COMPRESSIBLE_EULER = 0, /* CompressibleEulerIdealGas{Dim2}(gamma) */
-  P2DE_EQUATION_KPP = 1                 /* KPP{Dim2}() */
+  P2DE_EQUATION_COMPRESSIBLE_EULER = 0,   /* CompressibleEulerIdealGas{Dim2}(gamma) */
+  P2DE_EQUATION_KPP = 1,                  /* KPP{Dim2}() */
+  P2DE_EQUATION_COMPRESSIBLE_EULER_1D = 2 /* CompressibleEulerIdealGas{Dim1}(gamma) */
 } p2de_equation;
 
 /* Approximation bases (Solver.jl:38-40): collocation on the tensor-product LGL nodes, or
@@ -181,7 +192,10 @@ typedef struct p2de_mesh {
   double shock_pre[4];
 } p2de_mesh;
 
-/* Fields readable with p2de_get_field (state.preallocation members). */
+/* Fields readable with p2de_get_field (state.preallocation members). Shapes are those of
+ * CompressibleEulerIdealGas{Dim2}; p2de_solver_field_count gives each solver's size. KPP has
+ * one double per state; CompressibleEulerIdealGas{Dim1} has SVector{3} states, SVector{1,
+ * SVector{3}} flux pairs (3 doubles) and L_local (Nq+N1D) x 1 x K per stage. */
 typedef enum p2de_field {
   P2DE_FIELD_UQ = 0,      /* Nq x K SVector{4} */
   P2DE_FIELD_RHSU = 1,    /* Nq x K SVector{4} */

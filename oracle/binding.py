@@ -89,8 +89,10 @@ class Oracle:
         self.h = h
         self.N, self.K = desc.N, desc.K
         self.N1D = self.N + 1
-        self.Nq = self.N1D**2
-        self.Nfp = 4 * self.N1D
+        eqn = getattr(desc.param, "equation", 0)
+        self.dim1 = eqn == 2  # CompressibleEulerIdealGas{Dim1}
+        self.Nq = self.N1D if self.dim1 else self.N1D**2
+        self.Nfp = 2 if self.dim1 else 4 * self.N1D
 
     def close(self):
         if getattr(self, "h", None):
@@ -105,9 +107,11 @@ class Oracle:
 
     def count(self, field: int) -> int:
         n, Nq, Nfp, K = self.N1D, self.Nq, self.Nfp, self.K
-        c = 1 if getattr(self.desc.param, "equation", 0) == 1 else 4  # KPP: one component
-        return {0: c * Nq * K, 1: c * Nq * K, 2: c * Nq * K, 3: c * Nq * K, 4: 2 * c * Nq * K, 5: 2 * c * Nq * K,
-                6: 2 * c * Nfp * K, 7: 2 * c * Nfp * K, 8: (Nq + n) * 2 * K, 9: c * Nq * K, 10: K, 11: Nfp * K}[field]
+        eqn = getattr(self.desc.param, "equation", 0)
+        c = {1: 1, 2: 3}.get(eqn, 4)  # KPP: one component; Dim1: (rho, rhou, E)
+        d = 1 if self.dim1 else 2
+        return {0: c * Nq * K, 1: c * Nq * K, 2: c * Nq * K, 3: c * Nq * K, 4: d * c * Nq * K, 5: d * c * Nq * K,
+                6: d * c * Nfp * K, 7: d * c * Nfp * K, 8: (Nq + n) * d * K, 9: c * Nq * K, 10: K, 11: Nfp * K}[field]
 
     def set_Uq(self, Uq):
         U = np.ascontiguousarray(Uq, dtype=np.float64).ravel()

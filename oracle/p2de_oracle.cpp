@@ -350,6 +350,10 @@ void gauss_rule(int N, std::vector<double>& r, std::vector<double>& w, std::vect
 struct Solver {
   // sizes (SizeData, Solver.jl:173-183)
   int N, N1D, Nq, Nfp, Nh, K, Ns = 3;
+  // CompressibleEulerIdealGas{Dim1}: Nd = 1, Nq = N1D, Nfp = 2; states keep four slots with
+  // the y momentum 0, so every Dim2 point function gives the Dim1 value exactly
+  bool dim1 = false;
+  int Nd = 2;
   p2de_param prm;
   Euler eq;
   int nthreads = 1;
@@ -397,7 +401,7 @@ struct Solver {
   std::vector<double> dvdf[2];
 
   // ---- index helpers (0-based) ----
-  size_t LL(int i, int d, int k, int s) const { return (size_t)i + (size_t)(Nq + N1D) * (d + 2 * ((size_t)k + (size_t)K * s)); }
+  size_t LL(int i, int d, int k, int s) const { return (size_t)i + (size_t)(Nq + N1D) * (d + Nd * ((size_t)k + (size_t)K * s)); }
   void face_of(int64_t m1, int& iP, int& kP) const {  // mapP value (1-based) -> (face node, element)
     iP = (int)((m1 - 1) % Nfp);
     kP = (int)((m1 - 1) / Nfp);
@@ -447,11 +451,16 @@ struct Solver {
   }
   void build_vdm_inv() {
     std::vector<double> A((size_t)Nq * Nq), Inv((size_t)Nq * Nq, 0.0);
-    for (int is = 0; is < N1D; ++is)
-      for (int ir = 0; ir < N1D; ++ir)
-        for (int j = 0; j < N1D; ++j)
-          for (int i = 0; i < N1D; ++i)
-            A[(size_t)(ir + N1D * is) * Nq + (i + N1D * j)] = legendre_orthonormal(i, r1D[ir]) * legendre_orthonormal(j, r1D[is]);
+    if (dim1) {  // Line: P_j(r_i), mode j
+      for (int i = 0; i < N1D; ++i)
+        for (int j = 0; j < N1D; ++j) A[(size_t)i * Nq + j] = legendre_orthonormal(j, r1D[i]);
+    } else {
+      for (int is = 0; is < N1D; ++is)
+        for (int ir = 0; ir < N1D; ++ir)
+          for (int j = 0; j < N1D; ++j)
+            for (int i = 0; i < N1D; ++i)
+              A[(size_t)(ir + N1D * is) * Nq + (i + N1D * j)] = legendre_orthonormal(i, r1D[ir]) * legendre_orthonormal(j, r1D[is]);
+    }
     for (int i = 0; i < Nq; ++i) Inv[(size_t)i * Nq + i] = 1.0;
     // Gauss-Jordan elimination with partial pivoting
     for (int c = 0; c < Nq; ++c) {
@@ -505,11 +514,11 @@ struct Solver {
       }
       double modeN = 0.0, modeNm1 = 0.0, total = 0.0;
       int count = 0;
-      for (int j = 0; j <= N; ++j)
+      for (int j = 0; j <= (dim1 ? 0 : N); ++j)  // initialize_smoothness_indicator!(::Dim1) (shock_capture.jl:14-45): modes i
         for (int i = 0; i <= N; ++i) {
           const double energy = modal[count] * modal[count];
-          if (i == N || j == N) modeN += energy;
-          if (i == N - 1 || j == N - 1) modeNm1 += energy;
+          if (i == N || (!dim1 && j == N)) modeN += energy;
+          if (i == N - 1 || (!dim1 && j == N - 1)) modeNm1 += energy;
           total += energy;
           ++count;
         }
@@ -540,6 +549,10 @@ struct Solver {
   }
 
   void build_operators() {
+    if (dim1) {
+      build_operators_1d();
+      return;
+    }
     N1D = N + 1;
     Nq = N1D * N1D;
     Nfp = 4 * N1D;
@@ -685,6 +698,88 @@ struct Solver {
         if (Vf_low[f + (size_t)Nfp * i] == 1.0) q2fq[i].push_back(f);
   }
 
+  // initialize_reference_data(::Dim1) (init.jl:66-80) and initialize_operators (:133-228) on
+  // a Line: LGL or Gauss nodes (Gauss through construct_gauss_reference_data, :83-131), faces
+  // r = -1, +1 with nrJ = -1, +1 and wf = 1, and the low-order Sr0 = (Q0 - Q0')/2 of the
+  // tridiagonal Q0 (construct_low_order_operators_1D, :276-301; no mass weights on a Line).
+  // On LGL nodes Vq and Vf are taken as the exact identity and selection, where the
+  // reference's Vandermonde products carry rounding of about 1e-16.
+  void build_operators_1d() {
+    N1D = N + 1;
+    Nq = N1D;
+    Nfp = 2;
+    Nh = Nq + Nfp;
+    std::vector<double> ell_m1, ell_p1;
+    if (gauss())
+      gauss_rule(N, r1D, w1D, D1D, ell_m1, ell_p1);
+    else
+      gll_rule(N, r1D, w1D, D1D);
+    build_vdm_inv();
+    const double ZEROTOL = prm.ZEROTOL;
+    wq = w1D;
+    std::vector<double> Qr(Nq * Nq, 0.0);  // M Dr, column-major
+    for (int i = 0; i < Nq; ++i)
+      for (int j = 0; j < Nq; ++j) {
+        const double q = wq[i] * D1D[i * N1D + j];
+        Qr[i + Nq * j] = std::fabs(q) <= ZEROTOL ? 0.0 : q;
+      }
+    fq2q = {0, N};
+    Br = {-1.0, 1.0};
+    Bs = {0.0, 0.0};
+    Vf.assign(Nfp * Nq, 0.0);
+    Vf[0 + (size_t)Nfp * 0] = 1.0;
+    Vf[1 + (size_t)Nfp * N] = 1.0;
+    Vf_low = Vf;
+    if (gauss())
+      for (int i = 0; i < Nq; ++i) {
+        Vf[0 + (size_t)Nfp * i] = std::fabs(ell_m1[i]) <= ZEROTOL ? 0.0 : ell_m1[i];
+        Vf[1 + (size_t)Nfp * i] = std::fabs(ell_p1[i]) <= ZEROTOL ? 0.0 : ell_p1[i];
+      }
+    // Srh_db = [Q - Q', Ef' B; -B Ef, 0] (init.jl:152-155)
+    Srh_db.assign((size_t)Nh * Nh, 0.0);
+    Ssh_db.assign((size_t)Nh * Nh, 0.0);
+    for (int j = 0; j < Nq; ++j)
+      for (int i = 0; i < Nq; ++i) Srh_db[i + (size_t)Nh * j] = Qr[i + Nq * j] - Qr[j + Nq * i];
+    for (int f = 0; f < Nfp; ++f)
+      for (int i = 0; i < Nq; ++i) {
+        const double e = Vf[f + (size_t)Nfp * i];
+        if (e == 0.0) continue;
+        Srh_db[i + (size_t)Nh * (Nq + f)] = e * Br[f];
+        Srh_db[(Nq + f) + (size_t)Nh * i] = -(Br[f] * e);
+      }
+    if (gauss())
+      for (auto& q : Srh_db)
+        if (std::fabs(0.5 * q) <= ZEROTOL) q = 0.0;
+    MinvVhT.assign((size_t)Nq * Nh, 0.0);
+    MinvVfT.assign((size_t)Nq * Nfp, 0.0);
+    for (int i = 0; i < Nq; ++i) MinvVhT[i + (size_t)Nq * i] = 1.0 / wq[i];
+    for (int f = 0; f < Nfp; ++f)
+      for (int i = 0; i < Nq; ++i) {
+        const double e = Vf[f + (size_t)Nfp * i];
+        if (e == 0.0) continue;
+        MinvVhT[i + (size_t)Nq * (Nq + f)] = e / wq[i];
+        MinvVfT[i + (size_t)Nq * f] = e / wq[i];
+      }
+    // Q0: d = (-1/2, 0, ..., 0, 1/2), dl = -1/2, du = 1/2; Sr0 = (Q0 - Q0')/2
+    Sr0.assign(Nq * Nq, 0.0);
+    Ss0.assign(Nq * Nq, 0.0);
+    for (int i = 0; i + 1 < Nq; ++i) {
+      Sr0[i + Nq * (i + 1)] = 0.5 * (0.5 - -0.5);
+      Sr0[(i + 1) + Nq * i] = 0.5 * (-0.5 - 0.5);
+    }
+    Srsh_nnz.clear();
+    for (int j = 0; j < Nh; ++j)
+      for (int i = j + 1; i < Nh; ++i)
+        if (std::fabs(Srh_db[i + (size_t)Nh * j]) != 0.0) Srsh_nnz.push_back({i, j});
+    Srs0_nnz.clear();
+    for (int j = 0; j < Nq; ++j)
+      for (int i = j + 1; i < Nq; ++i)
+        if (std::fabs(Sr0[i + Nq * j]) != 0.0) Srs0_nnz.push_back({i, j});
+    q2fq.assign(Nq, {});
+    q2fq[0].push_back(0);
+    q2fq[N].push_back(1);
+  }
+
   void allocate() {
     size_t nq = (size_t)Nq * K, nh = (size_t)Nh * K, nf = (size_t)Nfp * K;
     Uq.assign(nq, V4{});
@@ -704,7 +799,7 @@ struct Solver {
     BF_L.assign(nf, V2x4{});
     fstar_H.assign(nf, V2x4{});
     fstar_L.assign(nf, V2x4{});
-    L_local.assign((size_t)(Nq + N1D) * 2 * K * Ns, 0.0);
+    L_local.assign((size_t)(Nq + N1D) * Nd * K * Ns, 0.0);
     L_elem.assign((size_t)K * Ns, 0.0);
     theta_local.assign((size_t)Nfp * K * Ns, 1.0);
     flux.assign(nh, V2x4{});
@@ -730,7 +825,7 @@ struct Solver {
       f_bar_H[d].assign((size_t)(Nq + N1D) * K, V4{});
       f_bar_L[d].assign((size_t)(Nq + N1D) * K, V4{});
       f_bar_lim[d].assign((size_t)(Nq + N1D) * K, V4{});
-      dvdf[d].assign((size_t)(Nq - N1D) * K, 0.0);
+      dvdf[d].assign((size_t)(dim1 ? N1D - 1 : Nq - N1D) * K, 0.0);
     }
     vf.assign(nf, V4{});
     psif.assign(nf, {0.0, 0.0});
@@ -1295,6 +1390,26 @@ struct Solver {
     if (j + 1 <= N) { qq[3] = q + N1D; kk[3] = k; } else qq[3] = quad_index_to_quad_index_P(q, k, 2, kk[3]);
   }
 
+  // low_order_stencil(::Dim1) (limiter_utils.jl:214-220): left, right neighbour; across an
+  // element face through quad_index_to_quad_index_P(::Dim1) (:184-195)
+  void low_order_stencil_1d(int q, int k, int kk[2], int qq[2]) const {
+    auto across = [&](int& kP) {
+      int iP;
+      face_of(mapP[q2fq[q][0] + (size_t)Nfp * k], iP, kP);
+      return fq2q[iP];
+    };
+    if (q - 1 >= 0) { qq[0] = q - 1; kk[0] = k; } else qq[0] = across(kk[0]);
+    if (q + 1 <= N) { qq[1] = q + 1; kk[1] = k; } else qq[1] = across(kk[1]);
+  }
+  int stencil(int q, int k, int kk[4], int qq[4]) const {
+    if (dim1) {
+      low_order_stencil_1d(q, k, kk, qq);
+      return 2;
+    }
+    low_order_stencil(q, k, kk, qq);
+    return 4;
+  }
+
   // initialize_s_modified! (subcell.jl:21-35) and initialize_lower_bound!(::Dim2) (:53-72):
   // Lphi = eps_k min(phi over the node and its stencil) + (1 - eps_k) min phi(initial)
   std::vector<double> s_mod, lbound_s_modified;
@@ -1314,9 +1429,9 @@ struct Solver {
       const double epsk = smooth_factor[k];
       for (int q = 0; q < Nq; ++q) {
         int kk[4], qq[4];
-        low_order_stencil(q, k, kk, qq);
+        const int ns = stencil(q, k, kk, qq);
         double lb = s_mod[q + (size_t)Nq * k];
-        for (int t4 = 0; t4 < 4; ++t4) lb = jmin(lb, s_mod[qq[t4] + (size_t)Nq * kk[t4]]);
+        for (int t4 = 0; t4 < ns; ++t4) lb = jmin(lb, s_mod[qq[t4] + (size_t)Nq * kk[t4]]);
         lbound_s_modified[q + (size_t)Nq * k] = epsk * lb + (1 - epsk) * s_modified_min;
       }
     }
@@ -1338,7 +1453,7 @@ struct Solver {
   }
 
   // initialize_TVD_bounds!(::Dim2) (subcell.jl:112-141) with low_order_stencil
-  // (limiter_utils.jl:222-231)
+  // (limiter_utils.jl:222-231); ::Dim1 (:86-110) with the two-point stencil
   std::vector<double> rhoL_tvd, lbound_rho, ubound_rho;
   void initialize_TVD_bounds(double dt) {
     rhoL_tvd.assign((size_t)Nq * K, 0.0);
@@ -1352,20 +1467,18 @@ struct Solver {
       }
 #pragma omp parallel for schedule(static)
     for (int k = 0; k < K; ++k)
-      for (int j = 0; j < N1D; ++j)
-        for (int i = 0; i < N1D; ++i) {
-          const int q = i + N1D * j;
-          int kk[4], qq[4];
-          low_order_stencil(q, k, kk, qq);
-          double lb = rhoL_tvd[q + (size_t)Nq * k], ub = lb;
-          for (int s = 0; s < 4; ++s) {
-            double v = rhoL_tvd[qq[s] + (size_t)Nq * kk[s]];
-            lb = jmin(lb, v);
-            ub = jmax(ub, v);
-          }
-          lbound_rho[q + (size_t)Nq * k] = lb;
-          ubound_rho[q + (size_t)Nq * k] = ub;
+      for (int q = 0; q < Nq; ++q) {
+        int kk[4], qq[4];
+        const int ns = stencil(q, k, kk, qq);
+        double lb = rhoL_tvd[q + (size_t)Nq * k], ub = lb;
+        for (int s = 0; s < ns; ++s) {
+          double v = rhoL_tvd[qq[s] + (size_t)Nq * kk[s]];
+          lb = jmin(lb, v);
+          ub = jmax(ub, v);
         }
+        lbound_rho[q + (size_t)Nq * k] = lb;
+        ubound_rho[q + (size_t)Nq * k] = ub;
+      }
   }
 
   // apply_rhs_limiter!(::SubcellLimiter) (limiter.jl:20-56)
@@ -1384,6 +1497,10 @@ struct Solver {
     }
     if (!eq.kpp && min_entropy()) initialize_entropy_bounds(t, nstage);
     if (!eq.kpp && tvd()) initialize_TVD_bounds(dt);
+    if (dim1) {
+      subcell_limiter_1d(dt, s);
+      return;
+    }
     // accumulate_f_bar!(::Dim2) (subcell.jl:163-206)
 #pragma omp parallel for schedule(static)
     for (int k = 0; k < K; ++k) {
@@ -1540,6 +1657,160 @@ struct Solver {
           rhsxyU[qk] = r;
           rhsU[qk] = add(r.x, r.y);
         }
+    }
+  }
+
+  // The subcell limiter's Dim1 methods: accumulate_f_bar! (subcell.jl:144-160),
+  // subcell_bound_limiter! (:208-246) with rho_bound(dim, ...) where the reference writes
+  // rho_bound(dim(solver), bound(solver), ...) (:225, :233; dim is the Dim1 argument there),
+  // enforce_ES_subcell! (:462-466) through the Dim1 methods of :468-505 and :567-628 with N
+  // entries of dvdf per element, symmetrize_limiting_parameters! (:405-415) across mapP
+  // between subcell faces 1 and Nq+1 of the two elements, accumulate_f_bar_limited!
+  // (:826-839) and apply_subcell_limiter! (:878-892)
+  void subcell_limiter_1d(double dt, int s) {
+    const int NS = Nq + N1D;  // rows of L_local
+#pragma omp parallel for schedule(static)
+    for (int k = 0; k < K; ++k) {
+      V4* fH = &f_bar_H[0][(size_t)NS * k];
+      V4* fL = &f_bar_L[0][(size_t)NS * k];
+      fH[0] = BF_H[0 + (size_t)Nfp * k].x;
+      fL[0] = BF_L[0 + (size_t)Nfp * k].x;
+      for (int i = 1; i <= Nq; ++i) {
+        const size_t qk = (i - 1) + (size_t)Nq * k;
+        const double wJ = Jq[qk] * wq[i - 1];
+        fH[i] = add(fH[i - 1], scal(wJ, rhsH[qk]));
+        fL[i] = add(fL[i - 1], scal(wJ, rhsL[qk]));
+      }
+    }
+    const double zeta = prm.zeta;
+#pragma omp parallel for schedule(static)
+    for (int k = 0; k < K; ++k) {
+      std::vector<V4> uL(Nq);
+      for (int i = 0; i < Nq; ++i) {
+        const size_t ik = i + (size_t)Nq * k;
+        uL[i] = add(Uq[ik], scal(dt, rhsL[ik]));
+      }
+      for (int i = 0; i < NS; ++i) L_local[LL(i, 0, k, s)] = 1.0;
+      const V4* fH = &f_bar_H[0][(size_t)NS * k];
+      const V4* fL = &f_bar_L[0][(size_t)NS * k];
+      auto eval = [&](int q, const V4& dF, double sgn) {
+        const double wJ = wq[q] * Jq[q + (size_t)Nq * k];
+        const V4& u = uL[q];
+        double Lrho = zeta * u[0], Urho = kInf;
+        if (tvd()) {
+          Lrho = lbound_rho[q + (size_t)Nq * k];
+          Urho = ubound_rho[q + (size_t)Nq * k];
+        }
+        const double Lphi = min_entropy() ? lbound_s_modified[q + (size_t)Nq * k] : 0.0;
+        double bv[5] = {Lrho, zeta * eq.rhoe_ufun(u), Lphi, Urho, kInf};
+        V4 P;
+        for (int c = 0; c < 4; ++c) P[c] = sgn * 2.0 * dt * dF[c] / wJ;
+        return min_entropy() ? limiting_param_min_entropy(u, P, bv) : limiting_param(u, P, bv);
+      };
+      for (int i = 0; i < Nq; ++i) {
+        double& l = L_local[LL(i, 0, k, s)];
+        l = jmin(l, eval(i, sub(fH[i], fL[i]), -1.0));
+      }
+      for (int i = 1; i <= Nq; ++i) {
+        double& l = L_local[LL(i, 0, k, s)];
+        l = jmin(l, eval(i - 1, sub(fH[i], fL[i]), 1.0));
+      }
+      for (int i = 0; i < NS; ++i) L_local[LL(i, 0, k, s)] = jmin(L_local[LL(i, 0, k, s)], blending_factor[k]);
+    }
+    if (cell_entropy()) {
+      initialize_ES_subcell_limiting_1d();
+      enforce_ES_subcell_volume_1d(s);
+    }
+    {
+      std::vector<double> Lold(L_local.begin() + (size_t)NS * K * s, L_local.begin() + (size_t)NS * K * (s + 1));
+#pragma omp parallel for schedule(static)
+      for (int k = 0; k < K; ++k)
+        for (int f = 0; f < Nfp; ++f) {
+          int iP, kP;
+          face_of(mapP[f + (size_t)Nfp * k], iP, kP);
+          const int si = f == 0 ? 0 : Nq, siP = iP == 0 ? 0 : Nq;
+          L_local[LL(si, 0, k, s)] = jmin(Lold[si + (size_t)NS * k], Lold[siP + (size_t)NS * kP]);
+        }
+    }
+#pragma omp parallel for schedule(static)
+    for (int k = 0; k < K; ++k) {
+      const size_t o = (size_t)NS * k;
+      for (int i = 0; i <= Nq; ++i) {
+        const double l = L_local[LL(i, 0, k, s)];
+        f_bar_lim[0][o + i] = add(scal(l, f_bar_H[0][o + i]), scal(1.0 - l, f_bar_L[0][o + i]));
+      }
+      for (int i = 0; i < Nq; ++i) {
+        const size_t ik = i + (size_t)Nq * k;
+        const double wJ = wq[i] * Jq[ik];
+        rhsU[ik] = divs(sub(f_bar_lim[0][o + i + 1], f_bar_lim[0][o + i]), wJ);
+      }
+    }
+  }
+
+  // initialize_ES_subcell_limiting!(::Dim1) (subcell.jl:468-505)
+  void initialize_ES_subcell_limiting_1d() {
+    const int NS = Nq + N1D;
+#pragma omp parallel for schedule(static)
+    for (int k = 0; k < K; ++k) {
+      for (int i = 0; i < Nq; ++i) vq[i + (size_t)Nq * k] = eq.v_ufun(Uq[i + (size_t)Nq * k]);
+      double sB = 0.0;
+      for (int f = 0; f < Nfp; ++f) {
+        const size_t fk = f + (size_t)Nfp * k;
+        const V4& uf = Uq[fq2q[f] + (size_t)Nq * k];
+        vf[fk] = eq.v_ufun(uf);
+        psif[fk] = eq.psi_ufun(uf);
+        sB = sB + Bx(f, k)[0] * psif[fk][0];
+      }
+      sum_Bpsi[k] = {sB, 0.0};
+      const V4* v = &vq[(size_t)Nq * k];
+      const V4* fH = &f_bar_H[0][(size_t)NS * k];
+      const V4* fL = &f_bar_L[0][(size_t)NS * k];
+      double* d = &dvdf[0][(size_t)N * k];
+      double sx = 0.0;
+      for (int si = 1; si <= N; ++si) {
+        const V4 df = sub(fH[si], fL[si]);
+        const V4 dv = sub(v[si - 1], v[si]);
+        d[si - 1] = vsum(vmul(dv, df));
+        sx += vsum(vmul(dv, fL[si]));
+      }
+      sum_dvfbarL[k] = {sx, 0.0};
+    }
+  }
+
+  // enforce_ES_subcell_volume!(::Dim1) (subcell.jl:567-628), rhs_es (:746-753)
+  void enforce_ES_subcell_volume_1d(int s) {
+    const int M = N;
+#pragma omp parallel for schedule(static)
+    for (int k = 0; k < K; ++k) {
+      const double* d = &dvdf[0][(size_t)M * k];
+      auto L = [&](int si) -> double& { return L_local[LL(si, 0, k, s)]; };
+      double sum = 0.0;
+      for (int si = 1; si <= N; ++si) sum += L(si) * d[si - 1];
+      double rhs = sum_Bpsi[k][0] - sum_dvfbarL[k][0];
+      if (relaxed()) rhs = (1 - prm.bound_beta * smooth_factor[k]) * rhs;
+      const double est = sum - rhs;
+      const double tol = jmax(0.0, sum_dvfbarL[k][0] - sum_Bpsi[k][0]);
+      if (!(est > tol)) continue;
+      std::vector<std::pair<double, int>> order(M);
+      for (int i = 0; i < M; ++i) order[i] = {d[i], i + 1};
+      std::sort(order.begin(), order.end(), [](const std::pair<double, int>& a, const std::pair<double, int>& b) {
+        if (jisless(b.first, a.first)) return true;
+        if (jisless(a.first, b.first)) return false;
+        return b.second < a.second;
+      });
+      int curr = 1;
+      double lhs = sum;
+      while (lhs > rhs + tol && curr <= Nq - 1) {
+        const int idx = order[curr - 1].second;  // subcell face idx + 1 (1-based)
+        if (d[idx - 1] < prm.ZEROTOL) break;
+        lhs = lhs - L(idx) * d[idx - 1];
+        curr += 1;
+      }
+      for (int i = 1; i <= curr - 1; ++i) {
+        const int idx = order[i - 1].second;
+        const double l_new = (i == curr - 1) ? jmax((rhs + tol - lhs) / d[idx - 1], 0.0) : 0.0;
+        L(idx) = jmin(L(idx), l_new);
+      }
     }
   }
 
@@ -1825,9 +2096,28 @@ int validate(const p2de_param* p, const p2de_mesh* m, std::string& err) {
     err = "bound_type must be in 0..9 and rhs_limiter in 0..1";
     return P2DE_ERR_INVALID_ARGUMENT;
   }
-  if (p->equation < 0 || p->equation > 1) {
-    err = "equation must be 0 (CompressibleEulerIdealGas) or 1 (KPP)";
+  if (p->equation < 0 || p->equation > 2) {
+    err = "equation must be 0 (CompressibleEulerIdealGas{Dim2}), 1 (KPP) or 2 (CompressibleEulerIdealGas{Dim1})";
     return P2DE_ERR_INVALID_ARGUMENT;
+  }
+  if (p->equation == P2DE_EQUATION_COMPRESSIBLE_EULER_1D) {
+    if (p->reference_semantics) {
+      err = "CompressibleEulerIdealGas{Dim1}: the reference raises a MethodError in every RHS "
+            "(Bx(::Dim1) calls reference_to_physical with dim last, rhs_utils.jl:18)";
+      return P2DE_ERR_UNSUPPORTED;
+    }
+    if (m->nW || m->nS) {
+      err = "CompressibleEulerIdealGas{Dim1}: periodic, inflow and outflow faces only";
+      return P2DE_ERR_UNSUPPORTED;
+    }
+    const bool cell = p->bound_type == P2DE_BOUND_POSITIVITY_AND_CELL_ENTROPY || p->bound_type == P2DE_BOUND_TVD_AND_CELL_ENTROPY ||
+                      p->bound_type == P2DE_BOUND_POSITIVITY_AND_RELAXED_CELL_ENTROPY ||
+                      p->bound_type == P2DE_BOUND_TVD_AND_RELAXED_CELL_ENTROPY;
+    if (cell && p->rhs_limiter == P2DE_LIMITER_SUBCELL && p->approximation_basis == P2DE_BASIS_GAUSS) {
+      err = "CompressibleEulerIdealGas{Dim1}: no cell-entropy bounds on Gauss nodes "
+            "(enforce_ES_subcell_interface! has no Dim1 method for GaussCollocation, subcell.jl:755-759)";
+      return P2DE_ERR_UNSUPPORTED;
+    }
   }
   if (p->equation == P2DE_EQUATION_KPP &&
       (p->approximation_basis != P2DE_BASIS_LOBATTO || m->nI || m->nO || m->nW || m->nS ||
@@ -1869,6 +2159,8 @@ int oracle_create(const p2de_param* prm, const p2de_mesh* mesh, int nthreads, or
   s.K = prm->K;
   s.eq.gamma = prm->gamma;
   s.eq.kpp = prm->equation == P2DE_EQUATION_KPP;
+  s.dim1 = prm->equation == P2DE_EQUATION_COMPRESSIBLE_EULER_1D;
+  s.Nd = s.dim1 ? 1 : 2;
   s.nthreads = nthreads;
 #ifdef _OPENMP
   if (nthreads > 0) omp_set_num_threads(nthreads);
@@ -1896,8 +2188,12 @@ int oracle_create(const p2de_param* prm, const p2de_mesh* mesh, int nthreads, or
   if (mesh->nI > 0) {
     s.mapI.assign(mesh->mapI, mesh->mapI + mesh->nI);
     s.Ival.resize(mesh->nI);
-    for (int64_t i = 0; i < mesh->nI; ++i)
-      for (int c = 0; c < 4; ++c) s.Ival[i][c] = mesh->Ival[4 * i + c];
+    for (int64_t i = 0; i < mesh->nI; ++i) {
+      if (s.dim1)  // (rho, rhou, E)
+        s.Ival[i] = {mesh->Ival[3 * i], mesh->Ival[3 * i + 1], 0.0, mesh->Ival[3 * i + 2]};
+      else
+        for (int c = 0; c < 4; ++c) s.Ival[i][c] = mesh->Ival[4 * i + c];
+    }
   }
   if (mesh->nO > 0) s.mapO.assign(mesh->mapO, mesh->mapO + mesh->nO);
   if (mesh->nW > 0) s.mapW.assign(mesh->mapW, mesh->mapW + mesh->nW);
@@ -1924,6 +2220,10 @@ int oracle_destroy(oracle_solver* o) {
 int oracle_set_Uq(oracle_solver* o, const double* Uq) {
   if (o->s.eq.kpp) {  // one component per node
     for (size_t i = 0; i < o->s.Uq.size(); ++i) o->s.Uq[i] = {Uq[i], 0.0, 0.0, 0.0};
+    return P2DE_OK;
+  }
+  if (o->s.dim1) {  // (rho, rhou, E) per node
+    for (size_t i = 0; i < o->s.Uq.size(); ++i) o->s.Uq[i] = {Uq[3 * i], Uq[3 * i + 1], 0.0, Uq[3 * i + 2]};
     return P2DE_OK;
   }
   std::memcpy(o->s.Uq.data(), Uq, sizeof(double) * 4 * o->s.Uq.size());
@@ -1958,14 +2258,24 @@ int oracle_ssp33(oracle_solver* o, double* t_out, int64_t* steps, double* dt_las
 int oracle_get_field(oracle_solver* o, int field, int nstage, double* out) {
   Solver& s = o->s;
   const bool kpp = s.eq.kpp;  // KPP: component 0 of each state, (x, y) of each flux pair
+  const bool d1 = s.dim1;     // Dim1: (rho, rhou, E) of each state, of the x part of each pair
+  auto put3 = [&](size_t i, const V4& u) {
+    out[3 * i] = u[0];
+    out[3 * i + 1] = u[1];
+    out[3 * i + 2] = u[3];
+  };
   auto cp4 = [&](const std::vector<V4>& a) {
-    if (kpp)
+    if (d1)
+      for (size_t i = 0; i < a.size(); ++i) put3(i, a[i]);
+    else if (kpp)
       for (size_t i = 0; i < a.size(); ++i) out[i] = a[i][0];
     else
       std::memcpy(out, a.data(), sizeof(double) * 4 * a.size());
   };
   auto cp8 = [&](const std::vector<V2x4>& a) {
-    if (kpp)
+    if (d1)
+      for (size_t i = 0; i < a.size(); ++i) put3(i, a[i].x);
+    else if (kpp)
       for (size_t i = 0; i < a.size(); ++i) {
         out[2 * i] = a[i].x[0];
         out[2 * i + 1] = a[i].y[0];
@@ -1984,7 +2294,7 @@ int oracle_get_field(oracle_solver* o, int field, int nstage, double* out) {
     case P2DE_FIELD_BF_H: cp8(s.BF_H); break;
     case P2DE_FIELD_L_LOCAL: {
       if (nstage < 1 || nstage > 3) return P2DE_ERR_INVALID_ARGUMENT;
-      size_t n = (size_t)(s.Nq + s.N1D) * 2 * s.K;
+      size_t n = (size_t)(s.Nq + s.N1D) * s.Nd * s.K;
       std::memcpy(out, s.L_local.data() + n * (nstage - 1), sizeof(double) * n);
       break;
     }

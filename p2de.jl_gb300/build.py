@@ -38,7 +38,9 @@ def _deps() -> list[Path]:
 
 def _compile(nvcc: str, src: Path, verbose: bool) -> Path:
     obj = BUILD / (src.name + ".o")
-    cmd = [nvcc, *NVCC_FLAGS, "-c", str(src), "-o", str(obj)]
+    # the Line path keeps each a*b+c as two rounded operations, as the FP64 restatement does
+    extra = ["-fmad=false"] if src.name == "p2de_line.cu" else []
+    cmd = [nvcc, *NVCC_FLAGS, *extra, "-c", str(src), "-o", str(obj)]
     if verbose:
         print(" ".join(cmd), flush=True)
     r = subprocess.run(cmd, capture_output=True, text=True)

@@ -16,6 +16,7 @@
 #include "p2de_args.h"
 #include "p2de_diag.h"
 #include "p2de_launch.h"
+#include "p2de_line.h"
 #include "p2de_physics.cuh"
 #include "p2de_stage.cuh"
 #include "p2de_tables.h"
@@ -279,9 +280,11 @@ struct p2de_solver {
   bool gauss = false;                                                      // GaussCollocation
   bool kpp = false;                                                        // KPP{Dim2}: Nc = 1
   double *ufproj = nullptr, *theta = nullptr;                              // Gauss face projection
+  LineSolve* line = nullptr;                                               // CompressibleEulerIdealGas{Dim1}
   int diag_nblocks = 0;
   StageArgs base{};
   int64_t launches = 0;
+  double line_dt = 0.0;  // last dt of the Line path
   cudaGraphExec_t graph = nullptr;
   std::string err;
   std::vector<void*> allocs;
@@ -398,10 +401,82 @@ int step_launches(const p2de_solver* s) {
 }
 
 void free_all(p2de_solver* s) {
+  if (s->line) line_destroy(s->line);
+  s->line = nullptr;
   if (s->graph) cudaGraphExecDestroy(s->graph);
   for (void* p : s->allocs) cudaFree(p);
   s->allocs.clear();
   if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
+}
+
+// CompressibleEulerIdealGas{Dim1}: the handle's common fields point at the Line state, so
+// the diagnostics (min rho/rhoe, conservation, errors, stage minima) serve both
+int create_line(const p2de_param* prm, const p2de_mesh* mesh, int device, p2de_solver** out) {
+  if (prm->reference_semantics)
+    return fail(nullptr, P2DE_ERR_UNSUPPORTED,
+                "CompressibleEulerIdealGas{Dim1}: the reference raises a MethodError in every RHS (Bx(::Dim1) calls "
+                "reference_to_physical with dim last, rhs_utils.jl:18); use reference_semantics = 0");
+  if (prm->N < 1 || prm->N > 5 || prm->K < 1)
+    return fail(nullptr, P2DE_ERR_INVALID_ARGUMENT, "N=%d outside 1..5 or K=%d", prm->N, prm->K);
+  if ((prm->low_order_surface_flux != P2DE_FLUX_LAX_FRIEDRICHS_ON_NODAL_VAL &&
+       prm->low_order_surface_flux != P2DE_FLUX_LAX_FRIEDRICHS_ON_PROJECTED_VAL) ||
+      prm->high_order_surface_flux != P2DE_FLUX_LAX_FRIEDRICHS_ON_PROJECTED_VAL)
+    return fail(nullptr, P2DE_ERR_UNSUPPORTED, "surface fluxes: LaxFriedrichsOnNodalVal or LaxFriedrichsOnProjectedVal");
+  if (prm->rhs_type < 0 || prm->rhs_type > 2 || prm->bound_type < 0 || prm->bound_type > 9 || prm->shock_capture < 0 ||
+      prm->shock_capture > 1 || prm->rhs_limiter < 0 || prm->rhs_limiter > 1 || prm->approximation_basis < 0 ||
+      prm->approximation_basis > 1 || prm->entropyproj_limiter < 0 || prm->entropyproj_limiter > 1)
+    return fail(nullptr, P2DE_ERR_INVALID_ARGUMENT, "rhs_type/bound_type/rhs_limiter/basis out of range");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(nullptr, P2DE_ERR_NO_DEVICE, "no CUDA device");
+  if (device < 0 || device >= ndev) return fail(nullptr, P2DE_ERR_INVALID_ARGUMENT, "device %d of %d", device, ndev);
+  auto* s = new p2de_solver();
+  s->device = device;
+  s->prm = *prm;
+  s->N = prm->N;
+  s->N1D = prm->N + 1;
+  s->Nq = s->N1D;
+  s->Nfp = 2;
+  s->K = prm->K;
+  s->gauss = prm->approximation_basis == P2DE_BASIS_GAUSS;
+  auto bail = [&](int code) {
+    {
+      std::lock_guard<std::mutex> lk(g_err_mu);
+      g_last_create_error = s->err;
+    }
+    free_all(s);
+    delete s;
+    return code;
+  };
+  if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    fail(s, P2DE_ERR_CUDA, "device setup failed");
+    return bail(P2DE_ERR_CUDA);
+  }
+  s->own_stream = true;
+  std::string err;
+  const int rc = line_create(prm, mesh, s->stream, &s->line, err);
+  if (rc != P2DE_OK) {
+    s->err = err;
+    return bail(rc);
+  }
+  if (dalloc(s, &s->minbuf, 2) != cudaSuccess || dalloc(s, &s->counters, 8) != cudaSuccess) {
+    fail(s, P2DE_ERR_OUT_OF_MEMORY, "cudaMalloc");
+    return bail(P2DE_ERR_OUT_OF_MEMORY);
+  }
+  s->Uq = s->line->Uq;
+  s->resW = s->line->resW;
+  s->rhsL = s->line->rhsL;
+  s->rhsH = s->line->rhsH;
+  s->rhsU = s->line->rhsU;
+  s->geom = s->line->geom;
+  s->minrec = s->line->minrec;
+  s->status = s->line->status;
+  *out = s;
+  return P2DE_OK;
+}
+
+int line_status(p2de_solver* s, int rc, const std::string& err) {
+  if (rc != P2DE_OK) s->err = err;
+  return rc;
 }
 
 }  // namespace
@@ -438,13 +513,14 @@ int p2de_initialize_DG(const p2de_param* prm, const p2de_mesh* mesh, int device,
   if (prm->N < 1 || prm->N > 5) return fail(nullptr, P2DE_ERR_INVALID_ARGUMENT, "N=%d outside 1..5", prm->N);
   if (prm->K < 1) return fail(nullptr, P2DE_ERR_INVALID_ARGUMENT, "K=%d", prm->K);
   if (!mesh->geom || !mesh->mapP) return fail(nullptr, P2DE_ERR_INVALID_ARGUMENT, "geom and mapP are required");
+  if (prm->equation == P2DE_EQUATION_COMPRESSIBLE_EULER_1D) return create_line(prm, mesh, device, out);
   if ((prm->low_order_surface_flux != P2DE_FLUX_LAX_FRIEDRICHS_ON_NODAL_VAL &&
        prm->low_order_surface_flux != P2DE_FLUX_LAX_FRIEDRICHS_ON_PROJECTED_VAL) ||
       prm->high_order_surface_flux != P2DE_FLUX_LAX_FRIEDRICHS_ON_PROJECTED_VAL)
     return fail(nullptr, P2DE_ERR_UNSUPPORTED,
                 "surface fluxes: LaxFriedrichsOnNodalVal or LaxFriedrichsOnProjectedVal (low order), "
                 "LaxFriedrichsOnProjectedVal (high order)");
-  if (prm->equation < 0 || prm->equation > 1)
+  if (prm->equation < 0 || prm->equation > 2)
     return fail(nullptr, P2DE_ERR_INVALID_ARGUMENT, "equation %d out of range", prm->equation);
   if (prm->equation == P2DE_EQUATION_KPP &&
       (prm->approximation_basis != P2DE_BASIS_LOBATTO || prm->precision != P2DE_PRECISION_FP64 || mesh->nI ||
@@ -683,6 +759,10 @@ int p2de_destroy(p2de_solver* s) {
 int p2de_set_Uq(p2de_solver* s, const double* Uq) {
   if (!s || !Uq) return P2DE_ERR_INVALID_ARGUMENT;
   CK(cudaSetDevice(s->device));
+  if (s->line) {
+    std::string err;
+    return line_status(s, line_set_Uq(s->line, Uq, err), err);
+  }
   const size_t nodes = (size_t)s->Nq * s->K;
   if (s->kpp) {  // one component per node, held as the first of four (the rest 0)
     std::vector<double> full(4 * nodes, 0.0);
@@ -700,6 +780,11 @@ int p2de_set_Uq(p2de_solver* s, const double* Uq) {
 
 int p2de_get_field(p2de_solver* s, int32_t field, int32_t nstage, double* out) {
   if (!s || !out) return P2DE_ERR_INVALID_ARGUMENT;
+  if (s->line) {
+    CK(cudaSetDevice(s->device));
+    std::string err;
+    return line_status(s, line_get_field(s->line, field, nstage, out, err), err);
+  }
   int64_t cnt = 0;
   if (p2de_field_count(s->N, s->K, field, &cnt) != P2DE_OK) return fail(s, P2DE_ERR_INVALID_ARGUMENT, "bad field %d", field);
   const double* src = nullptr;
@@ -757,6 +842,12 @@ int p2de_get_field(p2de_solver* s, int32_t field, int32_t nstage, double* out) {
 
 int p2de_solver_field_count(p2de_solver* s, int32_t field, int64_t* count) {
   if (!s || !count) return P2DE_ERR_INVALID_ARGUMENT;
+  if (s->line) {
+    const int64_t c = line_field_count(s->line, field);
+    if (c < 0) return P2DE_ERR_INVALID_ARGUMENT;
+    *count = c;
+    return P2DE_OK;
+  }
   int rc = p2de_field_count(s->N, s->K, field, count);
   if (rc != P2DE_OK) return rc;
   if (s->kpp && field != P2DE_FIELD_L_LOCAL && field != P2DE_FIELD_L && field != P2DE_FIELD_THETA_LOCAL)
@@ -767,6 +858,14 @@ int p2de_solver_field_count(p2de_solver* s, int32_t field, int64_t* count) {
 int p2de_rhs(p2de_solver* s, double t, double dt, int32_t nstage, double* dt_out) {
   if (!s || !dt_out || nstage < 1 || nstage > 3) return P2DE_ERR_INVALID_ARGUMENT;
   CK(cudaSetDevice(s->device));
+  if (s->line) {
+    std::string err;
+    CK(cudaMemsetAsync(s->status, 0, sizeof(int), s->stream));
+    const int64_t before = s->line->launches;
+    const int rc = line_rhs(s->line, t, dt, nstage, dt_out, err);
+    s->launches += s->line->launches - before;
+    return line_status(s, rc, err);
+  }
   double sc[S_NSCAL] = {0};
   sc[S_T] = t;
   sc[S_DT_LIM] = dt;
@@ -822,6 +921,13 @@ static int step_impl(p2de_solver* s, double* t, double* dt_out) {
 int p2de_ssp33_step(p2de_solver* s, double* t, double* dt_out) {
   if (!s || !t || !dt_out) return P2DE_ERR_INVALID_ARGUMENT;
   CK(cudaSetDevice(s->device));
+  if (s->line) {
+    std::string err;
+    const int64_t before = s->line->launches;
+    const int rc = line_step(s->line, t, dt_out, err);
+    s->launches += s->line->launches - before;
+    return line_status(s, rc, err);
+  }
   return step_impl(s, t, dt_out);
 }
 
@@ -852,6 +958,19 @@ static int build_graph(p2de_solver* s) {
 int p2de_ssp33_advance(p2de_solver* s, int64_t nsteps, double* t, int64_t* steps_done) {
   if (!s || !t || nsteps < 0) return P2DE_ERR_INVALID_ARGUMENT;
   CK(cudaSetDevice(s->device));
+  if (s->line) {  // the Line path launches each step (it reads dt back per step)
+    int64_t done = 0;
+    int rc = P2DE_OK;
+    for (int64_t i = 0; i < nsteps && *t < s->prm.T; ++i) {
+      double dt = 0.0;
+      rc = p2de_ssp33_step(s, t, &dt);
+      if (rc != P2DE_OK) break;
+      ++done;
+      s->line_dt = dt;
+    }
+    if (steps_done) *steps_done = done;
+    return rc;
+  }
   int rc = build_graph(s);
   if (rc != P2DE_OK) return rc;
   double sc[S_NSCAL];
@@ -883,17 +1002,22 @@ int p2de_ssp33(p2de_solver* s, double* t_out, int64_t* steps_out, double* dt_las
     total += done;
     if (rc != P2DE_OK || done < 64 || !(t < s->prm.T)) break;
   }
+  if (t_out) *t_out = t;
+  if (steps_out) *steps_out = total;
+  if (s->line) {
+    if (dt_last) *dt_last = s->line_dt;
+    return rc;
+  }
   double sc[S_NSCAL];
   CK(cudaMemcpyAsync(sc, s->scal, sizeof sc, cudaMemcpyDeviceToHost, s->stream));
   CK(cudaStreamSynchronize(s->stream));
-  if (t_out) *t_out = t;
-  if (steps_out) *steps_out = total;
   if (dt_last) *dt_last = sc[S_DT];
   return rc;
 }
 
 int p2de_profile_steps(p2de_solver* s, int64_t nsteps, double* t, double ms[3]) {
   if (!s || !t || !ms || nsteps < 1) return P2DE_ERR_INVALID_ARGUMENT;
+  if (s->line) return fail(s, P2DE_ERR_UNSUPPORTED, "stage kernel timings: Dim2 solves");
   CK(cudaSetDevice(s->device));
   cudaEvent_t ev[8];
   for (int i = 0; i < 8; ++i) CK(cudaEventCreate(&ev[i]));
@@ -939,6 +1063,7 @@ int p2de_profile_steps(p2de_solver* s, int64_t nsteps, double* t, double ms[3]) 
 
 int p2de_set_elements_per_block(p2de_solver* s, int32_t epb) {
   if (!s) return P2DE_ERR_INVALID_ARGUMENT;
+  if (s->line) return fail(s, P2DE_ERR_UNSUPPORTED, "the Line path runs one element per thread");
   if (epb < 1 || epb > s->geo.elems_per_block_max)
     return fail(s, P2DE_ERR_INVALID_ARGUMENT, "elements per block %d outside 1..%d", epb, s->geo.elems_per_block_max);
   CK(cudaSetDevice(s->device));
@@ -962,6 +1087,7 @@ int p2de_get_elements_per_block(p2de_solver* s, int32_t* epb, int32_t* epb_max) 
 // candidate elements-per-block and keeps the fastest.
 int p2de_autotune(p2de_solver* s, int32_t* best_epb, double* best_ms) {
   if (!s) return P2DE_ERR_INVALID_ARGUMENT;
+  if (s->line) return fail(s, P2DE_ERR_UNSUPPORTED, "the Line path runs one element per thread");
   CK(cudaSetDevice(s->device));
   const int emax = s->geo.elems_per_block_max, edef = s->geo.elems_per_block;
   std::vector<int> cand;
@@ -1037,7 +1163,7 @@ int p2de_device_ptr(p2de_solver* s, int32_t field, void** dptr) {
     case P2DE_FIELD_RHSL: *dptr = s->rhsL; break;
     case P2DE_FIELD_RHSH: *dptr = s->rhsH; break;
     case P2DE_FIELD_RESW: *dptr = s->resW; break;
-    case P2DE_FIELD_L_LOCAL: *dptr = s->Lfin; break;
+    case P2DE_FIELD_L_LOCAL: *dptr = s->line ? s->line->Lloc : s->Lfin; break;
     default: return fail(s, P2DE_ERR_INVALID_ARGUMENT, "no device pointer for field %d", field);
   }
   return P2DE_OK;
@@ -1054,6 +1180,7 @@ int p2de_set_stream(p2de_solver* s, void* stream) {
   if (s->own_stream) cudaStreamDestroy(s->stream);
   s->own_stream = false;
   s->stream = (cudaStream_t)stream;
+  if (s->line) s->line->stream = s->stream;
   return P2DE_OK;
 }
 
@@ -1096,6 +1223,8 @@ int diag_prepare(p2de_solver* s, bool exact) {
 }
 
 const double* device_wq(const p2de_solver* s) {
+  if (s->line)
+    return reinterpret_cast<const double*>(reinterpret_cast<const char*>(s->line->ops) + offsetof(LineOps, wq));
   const OpTable* t = table_of(s);
   return reinterpret_cast<const double*>(reinterpret_cast<const char*>(t) + offsetof(OpTable, wq));
 }
@@ -1114,9 +1243,15 @@ int p2de_check_conservation(p2de_solver* s, double totals[4], double* sum) {
   double t[4];
   CK(cudaMemcpyAsync(t, s->diag_out, sizeof t, cudaMemcpyDeviceToHost, s->stream));
   CK(cudaStreamSynchronize(s->stream));
+  if (s->line) {  // (rho, rhou, E): the Line state's y-momentum slot is 0
+    t[2] = t[3];
+    t[3] = 0.0;
+    if (sum) *sum = (t[0] + t[1]) + t[2];
+  } else if (sum) {
+    *sum = ((t[0] + t[1]) + t[2]) + t[3];
+  }
   if (totals)
     for (int c = 0; c < 4; ++c) totals[c] = t[c];
-  if (sum) *sum = ((t[0] + t[1]) + t[2]) + t[3];
   return P2DE_OK;
 }
 
@@ -1132,6 +1267,14 @@ int p2de_calculate_error(p2de_solver* s, const double* exact_Uq, double out[3]) 
   if (s->kpp) {  // one component per node
     full.assign(n, 0.0);
     for (size_t i = 0; i < n / 4; ++i) full[4 * i] = exact_Uq[i];
+    exact_Uq = full.data();
+  } else if (s->line) {  // (rho, rhou, E) per node
+    full.assign(n, 0.0);
+    for (size_t i = 0; i < n / 4; ++i) {
+      full[4 * i] = exact_Uq[3 * i];
+      full[4 * i + 1] = exact_Uq[3 * i + 1];
+      full[4 * i + 3] = exact_Uq[3 * i + 2];
+    }
     exact_Uq = full.data();
   }
   CK(cudaMemcpyAsync(s->exact, exact_Uq, sizeof(double) * n, cudaMemcpyHostToDevice, s->stream));

@@ -1,0 +1,1194 @@
+// CompressibleEulerIdealGas{Dim1} on a Line mesh: P2DE.jl's RHS (rhs.jl:183-213) of the
+// LimitedDG / LowOrderPositivity / FluxDiffRHS dispatches with the Dim1 methods of the
+// subcell limiter (subcell.jl) or the Zhang-Shu limiter (zhangshu.jl), and the SSP-RK3
+// stage update (SSPRK33.jl:125-139).
+//
+// One thread per element. A 1D solve has at most a few thousand elements, so the kernels
+// are launch-bound; they are written for agreement with the FP64 restatement: this
+// translation unit is compiled without FMA contraction (-fmad=false) and keeps the
+// reference's association order, so away from limiter decisions the results differ only
+// through the last bits of log, exp and pow.
+//
+// States keep four slots per node, (rho, rhou, 0, E): with the y momentum 0 every Dim2
+// point function below gives the Dim1 value of compressible_Navier_Stokes.jl exactly.
+// Kernels of one stage: face projection -> low order (+ CFL) -> [initial min phi] ->
+// high order + limiter factors -> symmetrization, limited fluxes, RK update.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+
+#include "p2de_args.h"
+#include "p2de_line.h"
+#include "p2de_physics.cuh"
+
+namespace p2de {
+
+namespace {
+
+enum : int {
+  LF_LOW = 1 << 0,         // low-order RHS
+  LF_HIGH = 1 << 1,        // high-order RHS
+  LF_SUBCELL = 1 << 2,     // SubcellLimiter
+  LF_ZS = 1 << 3,          // ZhangShuLimiter
+  LF_RHSU_L = 1 << 4,      // rhsU = rhsL (LowOrderPositivity)
+  LF_RHSU_H = 1 << 5,      // rhsU = rhsH (FluxDiffRHS)
+  LF_CFL = 1 << 6,         // stage 1 of a low-order RHS: the positivity CFL
+  LF_LFPROJ = 1 << 7,      // LaxFriedrichsOnProjectedVal low-order flux
+  LF_NSE = 1 << 8,         // NodewiseScaledExtrapolation on Gauss nodes
+  LF_SHOCK = 1 << 9,       // HennemannShockCapture
+  LF_TVD = 1 << 10,        // TVD density bounds
+  LF_MINENT = 1 << 11,     // min-entropy bound
+  LF_RELAXED = 1 << 12,    // relaxed bounds (smoothness factor)
+  LF_CELL = 1 << 13,       // cell-entropy bound
+  LF_UPDATE = 1 << 14,     // RK stage update of Uq
+};
+
+constexpr int kThreads = 128;
+constexpr int MQ = kMaxN1D;     // nodes per element at most
+constexpr int MH = kLineMaxNh;  // nodes + face nodes
+constexpr int MS = 2 * kMaxN1D; // rows of L_local
+
+struct LineArgs {
+  int K, N1D, nstage, flags;
+  const LineOps* ops;
+  double *Uq, *resW, *rhsL, *rhsH, *rhsU, *BFL, *BFH, *uf, *theta, *Lloc, *Lraw, *fbar, *Lelem;
+  const double *geom, *Ival;
+  long long* phikey;
+  const int32_t *nbr, *bcidx;
+  const int8_t* bc;
+  unsigned long long* dtkey;
+  long long* minrec;
+  int* status;
+  double gamma, POSTOL, ZEROTOL, zeta, eta, CFL, beta, sc_TN, sc_sfac, s0;
+};
+
+// ---- point functions (compressible_Navier_Stokes.jl; four slots, y momentum 0) ----------
+__device__ double pfun4(double gamma, const double* U) {
+  return (gamma - 1.0) * (U[3] - 0.5 * (U[1] * U[1] + U[2] * U[2]) / U[0]);
+}
+__device__ double rhoe4(const double* U) { return U[3] - 0.5 * (U[1] * U[1] + U[2] * U[2]) / U[0]; }
+__device__ double betafun4(double gamma, const double* U) { return U[0] / (2.0 * pfun4(gamma, U)); }
+// wavespeed_estimate(::Dim1) (:48-52) of (rho, un, E)
+__device__ double wavespeed1(double gamma, double rho, double rhou, double E) {
+  const double p = (gamma - 1.0) * (E - 0.5 * (rhou * rhou) / rho);
+  return fabs(rhou / rho) + sqrt(gamma * p / rho);
+}
+__device__ double wavespeed4(double gamma, const double* U, double n1, double n2) {
+  return wavespeed1(gamma, U[0], n1 * U[1] + n2 * U[2], U[3]);
+}
+__device__ void fluxes4(double gamma, const double* U, double* f) {  // the x flux
+  const double rho = U[0], rhou = U[1], rhov = U[2], E = U[3];
+  const double p = pfun4(gamma, U);
+  const double u = rhou / rho, v = rhov / rho;
+  f[0] = rhou;
+  f[1] = rhou * u + p;
+  f[2] = rho * u * v;
+  f[3] = u * (E + p);
+}
+__device__ void v_ufun4(double gamma, const double* U, double* V) {
+  const double p = pfun4(gamma, U);
+  const double s = log(p / pow(U[0], gamma));
+  V[0] = (gamma + 1.0 - s) - (gamma - 1.0) * U[3] / p;
+  V[1] = U[1] * (gamma - 1.0) / p;
+  V[2] = U[2] * (gamma - 1.0) / p;
+  V[3] = -U[0] * (gamma - 1.0) / p;
+}
+__device__ void u_vfun4(double gamma, const double* V, double* U) {
+  const double s = gamma - V[0] + (V[1] * V[1] + V[2] * V[2]) / (2.0 * V[3]);
+  const double rhoeV = pow((gamma - 1.0) / pow(-V[3], gamma), 1.0 / (gamma - 1.0)) * exp(-s / (gamma - 1.0));
+  U[0] = -rhoeV * V[3];
+  U[1] = rhoeV * V[1];
+  U[2] = rhoeV * V[2];
+  U[3] = rhoeV * (1.0 - (V[1] * V[1] + V[2] * V[2]) / (2.0 * V[3]));
+}
+// logmean (:307-321)
+__device__ double logmean(double aL, double aR, double logL, double logR) {
+  const double da = aR - aL, aavg = 0.5 * (aR + aL);
+  const double f = da / aavg, v = f * f;
+  if (fabs(f) < 1e-4) return aavg * (1.0 + v * (-0.2 - v * (0.0512 - v * 0.026038857142857)));
+  return -da / (logL - logR);
+}
+// fS (:196-218) as the Dim2 x flux with v = 0; U = (rho, u, v, beta, log rho, log beta)
+__device__ void fS4(double gamma, const double* UL, const double* UR, double* F) {
+  const double rholog = logmean(UL[0], UR[0], UL[4], UR[4]);
+  const double betalog = logmean(UL[3], UR[3], UL[5], UR[5]);
+  const double rhoavg = 0.5 * (UL[0] + UR[0]);
+  const double uavg = 0.5 * (UL[1] + UR[1]);
+  const double vavg = 0.5 * (UL[2] + UR[2]);
+  const double unorm = UL[1] * UR[1] + UL[2] * UR[2];
+  const double pa = rhoavg / (UL[3] + UR[3]);
+  const double f4aux = rholog / (2.0 * (gamma - 1.0) * betalog) + pa + 0.5 * rholog * unorm;
+  const double FxS1 = rholog * uavg;
+  F[0] = FxS1;
+  F[1] = FxS1 * uavg + pa;
+  F[2] = FxS1 * vavg;
+  F[3] = f4aux * uavg;
+}
+__device__ double s_modified4(double gamma, const double* U) { return rhoe4(U) * pow(U[0], -gamma); }
+// isless on Float64 (NaN last, -0.0 before 0.0)
+__device__ bool jisless(double a, double b) {
+  if (isnan(a)) return false;
+  if (isnan(b)) return true;
+  if (a < b) return true;
+  if (a == b) return signbit(a) && !signbit(b);
+  return false;
+}
+__device__ double decode_key(long long k) { return __longlong_as_double(k ^ ((k >> 63) & 0x7fffffffffffffffLL)); }
+__device__ long long encode_key(double x) {
+  const long long b = __double_as_longlong(x);
+  return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+}
+
+// ---- limiter helpers (limiter_utils.jl) ----------------------------------------------
+// :108-132 with the coefficients of :141-146
+__device__ double rhoe_quadratic_solve(const double* U, const double* P, double Lrhoe, double ZEROTOL) {
+  if (Lrhoe == INFINITY) return 1.0;
+  const double a = P[0] * P[3] - 1.0 / 2.0 * (P[1] * P[1] + P[2] * P[2]);
+  const double b = U[3] * P[0] + U[0] * P[3] - U[1] * P[1] - U[2] * P[2] - P[0] * Lrhoe;
+  const double c = U[3] * U[0] - 1.0 / 2.0 * (U[1] * U[1] + U[2] * U[2]) - U[0] * Lrhoe;
+  double l = 1.0;
+  if (b * b - 4.0 * a * c >= 0.0) {
+    const double r1 = (-b + sqrt(b * b - 4.0 * a * c)) / (2.0 * a);
+    const double r2 = (-b - sqrt(b * b - 4.0 * a * c)) / (2.0 * a);
+    if (r1 > ZEROTOL && r2 > ZEROTOL)
+      l = jmin(r1, r2);
+    else if (r1 > ZEROTOL && r2 < -ZEROTOL)
+      l = r1;
+    else if (r2 > ZEROTOL && r1 < -ZEROTOL)
+      l = r2;
+  }
+  return l;
+}
+// :82-96
+__device__ double bound_rho_rhoe(const double* U, const double* P, double Lrho, double Lrhoe, double Urho,
+                                 double Urhoe, double ZEROTOL) {
+  double l = 1.0;
+  if (U[0] + P[0] < Lrho) l = jmax((Lrho - U[0]) / P[0], 0.0);
+  if (U[0] + P[0] > Urho) l = jmin(l, jmax((Urho - U[0]) / P[0], 0.0));
+  return jmin(jmin(l, rhoe_quadratic_solve(U, P, Lrhoe, ZEROTOL)), rhoe_quadratic_solve(U, P, Urhoe, ZEROTOL));
+}
+// find_alpha (low_order_graph_viscosity.jl:316-345), the doubling bounded
+__device__ double find_alpha(const double* ui, const double* ut, double POSTOL) {
+  auto ok = [&](double al) {
+    double q[4];
+    for (int c = 0; c < 4; ++c) q[c] = al * ui[c] - ut[c];
+    return q[0] > POSTOL && rhoe4(q) > POSTOL;
+  };
+  double alphaL = 0.0, alphaR = 1.0;
+  for (int guard = 0; guard < 1100 && !ok(alphaR); ++guard) alphaR = 2 * alphaR;
+  for (int iter = 0; iter < 50; ++iter) {
+    const double alphaM = (alphaL + alphaR) / 2;
+    if (ok(alphaM))
+      alphaR = alphaM;
+    else
+      alphaL = alphaM;
+  }
+  return alphaR;
+}
+
+__device__ void ld4(const double* p, double* u) {
+  for (int c = 0; c < 4; ++c) u[c] = p[c];
+}
+__device__ void st4(double* p, const double* u) {
+  for (int c = 0; c < 4; ++c) p[c] = u[c];
+}
+
+// Face state of the element's own low-order flux: the projected face value
+// (LaxFriedrichsOnProjectedVal) or the face node's value (LaxFriedrichsOnNodalVal)
+__device__ void low_face_state(const LineArgs& a, int k, int f, double* u) {
+  const int N = a.N1D - 1;
+  if (a.flags & LF_LFPROJ)
+    ld4(a.uf + 4 * (2 * (size_t)k + f), u);
+  else
+    ld4(a.Uq + 4 * ((size_t)a.N1D * k + (f == 0 ? 0 : N)), u);
+}
+
+// Bx (rhs_utils.jl:13-19) with the Dim2 reference_to_physical of geometry (J, rxJ, sxJ, ryJ, syJ)
+__device__ void Bx(const LineArgs& a, int k, int f, double& b0, double& b1) {
+  const double* g = a.geom + 5 * (size_t)k;
+  const double Br = a.ops->rxf[f], Bs = 0.0;
+  b0 = g[1] * Br + g[2] * Bs;
+  b1 = g[3] * Br + g[4] * Bs;
+}
+__device__ double norm2(double x, double y) {
+  const double m = fmax(fabs(x), fabs(y));
+  if (m == 0.0 || isinf(m) || isnan(m)) return m;
+  return sqrt(x * x + y * y);
+}
+
+// smoothness indicator (shock_capture.jl:14-45), blending factor (:118-137) and smoothness
+// factor (subcell.jl:927-956) of element k
+__device__ void smoothness(const LineArgs& a, const double (*U)[4], double& blend, double& epsk) {
+  const int n = a.N1D, N = n - 1;
+  const bool need = (a.flags & (LF_SHOCK | LF_RELAXED)) != 0;
+  double ind = 0.0;
+  if (need) {
+    double iv[MQ];
+    for (int i = 0; i < n; ++i) iv[i] = U[i][0] * pfun4(a.gamma, U[i]);
+    double modeN = 0.0, modeNm1 = 0.0, total = 0.0;
+    for (int i = 0; i <= N; ++i) {
+      double m = 0.0;
+      for (int j = 0; j < n; ++j) m += a.ops->VDMinv[i * n + j] * iv[j];
+      const double energy = m * m;
+      if (i == N) modeN += energy;
+      if (i == N - 1) modeNm1 += energy;
+      total += energy;
+    }
+    ind = jmax(modeN / total, modeNm1 / total);
+  }
+  blend = 1.0;
+  if (a.flags & LF_SHOCK) {
+    const double alpha = 1.0 / (1.0 + exp(-a.sc_sfac / a.sc_TN * (ind - a.sc_TN)));
+    blend = jmax(jmin(1.0 - alpha, 1.0), 0.5);
+  }
+  epsk = (a.flags & LF_MINENT) ? 1.0 : 0.0;
+  if (a.flags & LF_RELAXED) {
+    const double kappa = 1.0;
+    const double sk = log(ind) / log(10.0);
+    if (sk < a.s0 - kappa)
+      epsk = 0.0;
+    else if (sk > a.s0 + kappa)
+      epsk = 1.0;
+    else
+      epsk = 0.5 - 0.5 * sin(3.141592653589793 * (sk - a.s0) / (2 * kappa));
+  }
+}
+
+// ---- kernels ----------------------------------------------------------------------------
+// step begin: the stage's dt key, the per-stage minima, the initial min of phi
+__global__ void k_line_begin(LineArgs a, double dt, int reset_min, int reset_phi) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  *a.dtkey = (unsigned long long)__double_as_longlong(dt);
+  if (reset_min)
+    for (int i = 0; i < 6; ++i) a.minrec[i] = encode_key(INFINITY);
+  if (reset_phi) *a.phikey = encode_key(INFINITY);
+}
+
+// entropy_projection! (rhs.jl:59-133) with solve_theta!(::NodewiseScaledExtrapolation)
+// (filter.jl:6-62, 91-130) on Gauss nodes: theta_local and the projected face states
+__global__ void k_line_face(LineArgs a) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= a.K) return;
+  const int n = a.N1D, N = n - 1, s = a.nstage - 1;
+  const LineOps& o = *a.ops;
+  double U[MQ][4], v[MQ][4];
+  for (int i = 0; i < n; ++i) {
+    ld4(a.Uq + 4 * ((size_t)n * k + i), U[i]);
+    v_ufun4(a.gamma, U[i], v[i]);
+  }
+  for (int f = 0; f < 2; ++f) {
+    const int fn = f == 0 ? 0 : N;
+    auto face_var = [&](double th, double* acc) {
+      for (int c = 0; c < 4; ++c) acc[c] = 0.0;
+      for (int j = 0; j < n; ++j) {
+        const double c = th * o.Vf[f][j] + (1.0 - th) * (j == fn ? 1.0 : 0.0);
+        for (int q = 0; q < 4; ++q) acc[q] = acc[q] + c * v[j][q];
+      }
+    };
+    double th = 1.0;
+    if (a.flags & LF_NSE) {
+      double Ufv[4] = {0, 0, 0, 0}, VUf[4] = {0, 0, 0, 0};
+      for (int j = 0; j < n; ++j)
+        for (int q = 0; q < 4; ++q) {
+          Ufv[q] = Ufv[q] + o.Vf[f][j] * U[j][q];
+          VUf[q] = VUf[q] + o.Vf[f][j] * v[j][q];
+        }
+      const double rhoef = rhoe4(Ufv), eps = a.POSTOL, zeta = a.zeta, eta = a.eta;
+      auto ok = [&](double t) {
+        double vt[4], ut[4];
+        face_var(t, vt);
+        if (!(vt[3] < -eps)) return false;
+        u_vfun4(a.gamma, vt, ut);
+        const double rho = ut[0], re = rhoe4(ut);
+        return vt[3] < jmin(zeta * VUf[3], -eps) && rho > jmax((1 - eta) * Ufv[0], eps) && rho < (1 + eta) * Ufv[0] &&
+               re > jmax((1 - eta) * rhoef, eps) && re < (1 + eta) * rhoef;
+      };
+      double x_valid = 0.0, x_invalid = 1.0;
+      if (ok(x_invalid)) {
+        th = x_invalid;
+      } else {
+        for (int iter = 0; iter <= 20; ++iter) {
+          const double x_new = 0.5 * (x_valid + x_invalid);
+          if (ok(x_new))
+            x_valid = x_new;
+          else
+            x_invalid = x_new;
+        }
+        th = x_valid;
+      }
+    }
+    a.theta[2 * ((size_t)a.K * s + k) + f] = th;
+    double acc[4], u[4];
+    face_var(th, acc);
+    u_vfun4(a.gamma, acc, u);
+    st4(a.uf + 4 * (2 * (size_t)k + f), u);
+  }
+}
+
+// rhs_low_graph_visc! (low_order_graph_viscosity.jl:4-41) with the Dim1 graph viscosity and
+// LF placement (rhs_utils.jl:78-113); stage 1: the element's positivity CFL (:222-309)
+__global__ void k_line_low(LineArgs a) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= a.K) return;
+  const int n = a.N1D, N = n - 1;
+  const LineOps& o = *a.ops;
+  const double* g = a.geom + 5 * (size_t)k;
+  const double J = g[0];
+  double U[MQ][4], fl[MQ][4], r[MQ][4], lamR[MQ];
+  for (int i = 0; i < n; ++i) {
+    ld4(a.Uq + 4 * ((size_t)n * k + i), U[i]);
+    fluxes4(a.gamma, U[i], fl[i]);
+    for (int c = 0; c < 4; ++c) r[i][c] = 0.0;
+    lamR[i] = 0.0;
+  }
+  // accumulate_low_order_rhs_volume! (:139-173): pairs (j+1, j), Sr0[j+1, j] = -1/2
+  for (int j = 0; j < N; ++j) {
+    const int i = j + 1;
+    const double Sr0 = 0.5 * (-0.5 - 0.5), Ss0 = 0.0;
+    const double S0 = g[1] * Sr0 + g[2] * Ss0, S1 = g[3] * Sr0 + g[4] * Ss0;
+    const double nn = norm2(S0, S1), n1 = S0 / nn, n2 = S1 / nn;
+    const double ws = jmax(wavespeed4(a.gamma, U[i], n1, n2), wavespeed4(a.gamma, U[j], -n1, -n2));
+    const double lij = nn * ws;
+    lamR[j] = lij;
+    for (int c = 0; c < 4; ++c) {
+      const double F = 0.5 * (fl[i][c] + fl[j][c]);
+      const double SF = 2.0 * S0 * F - lij * (U[j][c] - U[i][c]);
+      r[i][c] = r[i][c] + SF;  // Q0F1, negated below
+      r[j][c] = r[j][c] + -SF;
+    }
+  }
+  for (int i = 0; i < n; ++i)
+    for (int c = 0; c < 4; ++c) r[i][c] = 0.0 - r[i][c];
+  // accumulate_low_order_rhs_surface! (:175-204) with get_uP_and_enforce_BC! (:94-124)
+  double lamB[2], wsf[2];
+  for (int f = 0; f < 2; ++f) {
+    const int fk = 2 * k + f, p = a.nbr[fk], kP = p / 2, iP = p % 2;
+    double Uf[4], UfP[4], uP[4], b0, b1, bP0, bP1;
+    low_face_state(a, k, f, Uf);
+    low_face_state(a, kP, iP, UfP);
+    Bx(a, k, f, b0, b1);
+    Bx(a, kP, iP, bP0, bP1);
+    const double nn = norm2(b0, b1), nnP = norm2(bP0, bP1);
+    wsf[f] = wavespeed4(a.gamma, Uf, b0 / nn, b1 / nn);
+    const double wsP = wavespeed4(a.gamma, UfP, bP0 / nnP, bP1 / nnP);
+    const int8_t bc = a.bc[fk];
+    if (bc == BC_INFLOW) {
+      const double* I = a.Ival + 3 * (size_t)a.bcidx[fk];
+      uP[0] = I[0], uP[1] = I[1], uP[2] = 0.0, uP[3] = I[2];
+    } else if (bc == BC_OUTFLOW) {
+      ld4(U[f == 0 ? 0 : N], uP);
+    } else {
+      ld4(UfP, uP);
+    }
+    lamB[f] = 0.5 * nn * jmax(wsf[f], wsP);
+    double ff[4], fP[4];
+    fluxes4(a.gamma, Uf, ff);
+    fluxes4(a.gamma, uP, fP);
+    double BF[4];
+    for (int c = 0; c < 4; ++c) {
+      const double fs = 0.5 * (ff[c] + fP[c]);
+      BF[c] = b0 * fs - lamB[f] * (uP[c] - Uf[c]);
+    }
+    st4(a.BFL + 4 * (size_t)fk, BF);
+    const int q = f == 0 ? 0 : N;
+    for (int c = 0; c < 4; ++c) r[q][c] = r[q][c] - BF[c];
+  }
+  // scale_low_order_rhs_by_mass! (:206-220)
+  for (int i = 0; i < n; ++i) {
+    const double wJq = J * o.wq[i];
+    double rl[4];
+    for (int c = 0; c < 4; ++c) rl[c] = r[i][c] / wJq + 0.0;
+    st4(a.rhsL + 4 * ((size_t)n * k + i), rl);
+    if (a.flags & LF_RHSU_L) st4(a.rhsU + 4 * ((size_t)n * k + i), rl);
+  }
+  if (a.flags & LF_CFL) {
+    double dtl = INFINITY;
+    for (int i = 0; i < n; ++i) {
+      double li = 0.0;
+      for (int j = 0; j < n; ++j) li += (j == i - 1) ? lamR[j] : ((j == i + 1) ? lamR[i] : 0.0);
+      if (i == 0 || i == N) {
+        const int f = i == 0 ? 0 : 1;
+        if (a.flags & LF_LFPROJ) {
+          double b0, b1, ut[4];
+          Bx(a, k, f, b0, b1);
+          ld4(a.uf + 4 * (2 * (size_t)k + f), ut);
+          li += find_alpha(U[i], ut, a.POSTOL) * lamB[f] + 0.5 * norm2(b0, b1) * wsf[f];
+        } else {
+          li += lamB[f];
+        }
+      }
+      const double wJq = J * o.wq[i];
+      dtl = jmin(dtl, a.CFL * 0.5 * wJq / li);
+    }
+    if (dtl > 0.0)
+      atomicMin(a.dtkey, (unsigned long long)__double_as_longlong(dtl));
+    else
+      atomicOr(a.status, ST_BAD_DT);
+  }
+}
+
+// initialize_s_modified! (subcell.jl:21-35): the min of phi over all nodes
+__global__ void k_line_phimin(LineArgs a) {
+  const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= (long long)a.K * a.N1D) return;
+  double U[4];
+  ld4(a.Uq + 4 * g, U);
+  atomicMin(a.phikey, encode_key(s_modified4(a.gamma, U)));
+}
+
+// rhs_fluxdiff! (flux_differencing.jl:4-37, 331-361) and the limiter's per-element part:
+// Zhang-Shu (zhangshu.jl:4-45) or the subcell factors before symmetrization (subcell.jl:
+// Dim1 methods of accumulate_f_bar!, initialize_lower_bound!, initialize_TVD_bounds!,
+// subcell_bound_limiter!, enforce_ES_subcell!)
+__global__ void k_line_high(LineArgs a) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= a.K) return;
+  const int n = a.N1D, N = n - 1, Nh = n + 2, s = a.nstage - 1;
+  const LineOps& o = *a.ops;
+  const double* g = a.geom + 5 * (size_t)k;
+  const double J = g[0];
+  const double dt = __longlong_as_double((long long)*a.dtkey);
+  double U[MQ][4], ut[MH][4], beta[MH], rl[MH], bl[MH], QF[MH][4];
+  for (int i = 0; i < n; ++i) {
+    ld4(a.Uq + 4 * ((size_t)n * k + i), U[i]);
+    ld4(U[i], ut[i]);
+  }
+  for (int f = 0; f < 2; ++f) ld4(a.uf + 4 * (2 * (size_t)k + f), ut[n + f]);
+  for (int h = 0; h < Nh; ++h) {
+    beta[h] = betafun4(a.gamma, ut[h]);
+    rl[h] = log(ut[h][0]);
+    bl[h] = log(beta[h]);
+    for (int c = 0; c < 4; ++c) QF[h][c] = 0.0;
+  }
+  // exterior states, interface dissipation coefficients and BCs (:39-151)
+  // (the exterior beta and logs of :56-70 enter no flux of this path: the surface flux is
+  // LaxFriedrichsOnProjectedVal of the exterior state itself)
+  double uP[2][4], LFc[2];
+  for (int f = 0; f < 2; ++f) {
+    const int fk = 2 * k + f, p = a.nbr[fk], kP = p / 2, iP = p % 2;
+    ld4(a.uf + 4 * (size_t)p, uP[f]);
+    double b0, b1, c0, c1;
+    Bx(a, k, f, b0, b1);
+    Bx(a, kP, iP, c0, c1);
+    const double nn = norm2(b0, b1), nnP = norm2(c0, c1);
+    const double lam = wavespeed4(a.gamma, ut[n + f], b0 / nn, b1 / nn);
+    const double lamP = wavespeed4(a.gamma, uP[f], c0 / nnP, c1 / nnP);
+    LFc[f] = 0.5 * nn * jmax(lam, lamP);
+    const int8_t bc = a.bc[fk];
+    if (bc == BC_INFLOW || bc == BC_OUTFLOW) {
+      LFc[f] = 0.0;
+      if (bc == BC_INFLOW) {
+        const double* I = a.Ival + 3 * (size_t)a.bcidx[fk];
+        uP[f][0] = I[0], uP[f][1] = I[1], uP[f][2] = 0.0, uP[f][3] = I[2];
+      } else {
+        ld4(U[f == 0 ? 0 : N], uP[f]);
+      }
+    }
+  }
+  // flux_differencing_volume! (:164-211) over the nonzero pairs of Srh_db
+  for (int p = 0; p < o.npair; ++p) {
+    const int i = o.pi[p], j = o.pj[p];
+    const double Sr = o.Sh[i + Nh * j], Ss = 0.0;
+    const double S0 = g[1] * Sr + g[2] * Ss;
+    const double Ui[6] = {ut[i][0], ut[i][1] / ut[i][0], ut[i][2] / ut[i][0], beta[i], rl[i], bl[i]};
+    const double Uj[6] = {ut[j][0], ut[j][1] / ut[j][0], ut[j][2] / ut[j][0], beta[j], rl[j], bl[j]};
+    double F[4];
+    fS4(a.gamma, Ui, Uj, F);
+    for (int c = 0; c < 4; ++c) {
+      const double SF = S0 * F[c];
+      QF[i][c] = QF[i][c] + SF;
+      QF[j][c] = QF[j][c] + -SF;
+    }
+  }
+  // flux_differencing_surface! (:223-272)
+  double BF[2][4];
+  for (int f = 0; f < 2; ++f) {
+    double ff[4], fP[4], b0, b1;
+    fluxes4(a.gamma, ut[n + f], ff);
+    fluxes4(a.gamma, uP[f], fP);
+    Bx(a, k, f, b0, b1);
+    for (int c = 0; c < 4; ++c) BF[f][c] = b0 * (0.5 * (ff[c] + fP[c])) - LFc[f] * (uP[f][c] - ut[n + f][c]);
+    st4(a.BFH + 4 * (2 * (size_t)k + f), BF[f]);
+  }
+  // assemble_rhs! (:274-361): lift by M \ Vh', or by (1/wq) [I, Vf_new'] when a theta < 1
+  const double th0 = a.theta[2 * ((size_t)a.K * s + k)], th1 = a.theta[2 * ((size_t)a.K * s + k) + 1];
+  const bool limited = th0 < 1.0 || th1 < 1.0;
+  double rH[MQ][4], rL[MQ][4];
+  for (int i = 0; i < n; ++i) {
+    const double rw = 1 / o.wq[i];
+    auto m = [&](int col) -> double {
+      if (!limited) return o.MinvVhT[i + n * col];
+      if (col < n) return col == i ? rw * 1.0 : 0.0;
+      const int f = col - n;
+      const double th = f == 0 ? th0 : th1;
+      const double low = (i == (f == 0 ? 0 : N)) ? 1.0 : 0.0;
+      return rw * (th * o.Vf[f][i] + (1 - th) * low);
+    };
+    double A[4] = {0, 0, 0, 0}, B[4] = {0, 0, 0, 0};
+    for (int j = 0; j < Nh; ++j) {
+      const double mm = m(j);
+      for (int c = 0; c < 4; ++c) A[c] = A[c] + mm * QF[j][c];
+    }
+    for (int f = 0; f < 2; ++f) {
+      const double mm = m(n + f);
+      for (int c = 0; c < 4; ++c) B[c] = B[c] + mm * BF[f][c];
+    }
+    for (int c = 0; c < 4; ++c) rH[i][c] = -(A[c] + B[c]) / J;
+    st4(a.rhsH + 4 * ((size_t)n * k + i), rH[i]);
+    ld4(a.rhsL + 4 * ((size_t)n * k + i), rL[i]);
+    if (a.flags & LF_RHSU_H) st4(a.rhsU + 4 * ((size_t)n * k + i), rH[i]);
+  }
+  if (!(a.flags & (LF_ZS | LF_SUBCELL))) return;
+  double blend, epsk;
+  smoothness(a, U, blend, epsk);
+  const double zeta = a.zeta;
+  if (a.flags & LF_ZS) {  // zhang_shu_bound_limiter! (zhangshu.jl:35-45)
+    double l = 1.0;
+    for (int i = 0; i < n; ++i) {
+      double uL[4], P[4];
+      for (int c = 0; c < 4; ++c) {
+        uL[c] = U[i][c] + dt * rL[i][c];
+        P[c] = dt * (rH[i][c] - rL[i][c]);
+      }
+      const double li = jmin(1.0, bound_rho_rhoe(uL, P, zeta * uL[0], zeta * rhoe4(uL), INFINITY, INFINITY, a.ZEROTOL));
+      l = jmin(l, li);
+    }
+    a.Lelem[(size_t)a.K * s + k] = l;
+    l = jmin(l, blend);
+    for (int i = 0; i < n; ++i) {
+      double r[4];
+      for (int c = 0; c < 4; ++c) r[c] = (1 - l) * rL[i][c] + l * rH[i][c];
+      st4(a.rhsU + 4 * ((size_t)n * k + i), r);
+    }
+    return;
+  }
+  // the two-point stencil of node q (low_order_stencil(::Dim1), limiter_utils.jl:184-220)
+  auto stencil = [&](int q, int* kk, int* qq) {
+    for (int t = 0; t < 2; ++t) {
+      const int qn = q + (t == 0 ? -1 : 1);
+      if (qn >= 0 && qn <= N) {
+        kk[t] = k;
+        qq[t] = qn;
+      } else {
+        const int p = a.nbr[2 * k + (q == 0 ? 0 : 1)];
+        kk[t] = p / 2;
+        qq[t] = (p % 2 == 0) ? 0 : N;
+      }
+    }
+  };
+  double Lphi[MQ], Lrho[MQ], Urho[MQ];
+  double uL[MQ][4];
+  const double phimin = decode_key(*a.phikey);
+  for (int q = 0; q < n; ++q) {
+    for (int c = 0; c < 4; ++c) uL[q][c] = U[q][c] + dt * rL[q][c];
+    int kk[2], qq[2];
+    stencil(q, kk, qq);
+    Lphi[q] = 0.0;
+    if (a.flags & LF_MINENT) {  // initialize_lower_bound!(::Dim1) (subcell.jl:37-51)
+      double lb = s_modified4(a.gamma, U[q]);
+      for (int t = 0; t < 2; ++t) {
+        double Un[4];
+        ld4(a.Uq + 4 * ((size_t)n * kk[t] + qq[t]), Un);
+        lb = jmin(lb, s_modified4(a.gamma, Un));
+      }
+      Lphi[q] = epsk * lb + (1 - epsk) * phimin;
+    }
+    Lrho[q] = zeta * uL[q][0];
+    Urho[q] = INFINITY;
+    if (a.flags & LF_TVD) {  // initialize_TVD_bounds!(::Dim1) (:86-110)
+      double lb = U[q][0] + dt * rL[q][0], ub = lb;
+      for (int t = 0; t < 2; ++t) {
+        const size_t m = (size_t)n * kk[t] + qq[t];
+        const double v = a.Uq[4 * m] + dt * a.rhsL[4 * m];
+        lb = jmin(lb, v);
+        ub = jmax(ub, v);
+      }
+      Lrho[q] = lb;
+      Urho[q] = ub;
+    }
+  }
+  // accumulate_f_bar!(::Dim1) (:144-160)
+  double fH[MQ + 1][4], fL[MQ + 1][4];
+  ld4(BF[0], fH[0]);
+  ld4(a.BFL + 4 * (2 * (size_t)k), fL[0]);
+  for (int i = 1; i <= n; ++i) {
+    const double wJ = J * o.wq[i - 1];
+    for (int c = 0; c < 4; ++c) {
+      fH[i][c] = fH[i - 1][c] + wJ * rH[i - 1][c];
+      fL[i][c] = fL[i - 1][c] + wJ * rL[i - 1][c];
+    }
+  }
+  // subcell_bound_limiter!(::Dim1) (:208-246)
+  double L[MS];
+  for (int i = 0; i < 2 * n; ++i) L[i] = 1.0;
+  auto eval = [&](int q, int i, double sgn) {
+    const double wJ = o.wq[q] * J;
+    double P[4];
+    for (int c = 0; c < 4; ++c) P[c] = sgn * 2.0 * dt * (fH[i][c] - fL[i][c]) / wJ;
+    const double Lrhoe = zeta * rhoe4(uL[q]);
+    const double lpos = bound_rho_rhoe(uL[q], P, Lrho[q], Lrhoe, Urho[q], INFINITY, a.ZEROTOL);
+    if (!(a.flags & LF_MINENT)) return lpos;
+    // limiting_param_bound_phi (limiter_utils.jl:43-50) by bisection on [0, lpos]
+    const double thr = Lphi[q] - a.POSTOL;
+    auto okp = [&](double l) {
+      double W[4];
+      for (int c = 0; c < 4; ++c) W[c] = uL[q][c] + l * P[c];
+      return s_modified4(a.gamma, W) >= thr;
+    };
+    double x_valid = 0.0, x_invalid = lpos;
+    if (okp(x_invalid)) return x_invalid;
+    for (int iter = 0; iter <= 20; ++iter) {
+      const double x_new = 0.5 * (x_valid + x_invalid);
+      if (okp(x_new))
+        x_valid = x_new;
+      else
+        x_invalid = x_new;
+    }
+    return x_valid;
+  };
+  for (int i = 0; i < n; ++i) L[i] = jmin(L[i], eval(i, i, -1.0));
+  for (int i = 1; i <= n; ++i) L[i] = jmin(L[i], eval(i - 1, i, 1.0));
+  for (int i = 0; i < 2 * n; ++i) L[i] = jmin(L[i], blend);
+  if (a.flags & LF_CELL) {  // Dim1 methods of subcell.jl:468-505, 567-628, rhs_es :746-753
+    double v[MQ][4];
+    for (int i = 0; i < n; ++i) v_ufun4(a.gamma, U[i], v[i]);
+    double sB = 0.0;
+    for (int f = 0; f < 2; ++f) {
+      double b0, b1;
+      Bx(a, k, f, b0, b1);
+      const double psi = (a.gamma - 1.0) * U[f == 0 ? 0 : N][1];
+      sB = sB + b0 * psi;
+    }
+    double d[MQ], sx = 0.0;
+    for (int si = 1; si <= N; ++si) {
+      double dvdf = 0.0, dvfl = 0.0;
+      double t1[4], t2[4];
+      for (int c = 0; c < 4; ++c) {
+        const double dv = v[si - 1][c] - v[si][c];
+        t1[c] = dv * (fH[si][c] - fL[si][c]);
+        t2[c] = dv * fL[si][c];
+      }
+      dvdf = ((t1[0] + t1[1]) + t1[2]) + t1[3];
+      dvfl = ((t2[0] + t2[1]) + t2[2]) + t2[3];
+      d[si - 1] = dvdf;
+      sx += dvfl;
+    }
+    double sum = 0.0;
+    for (int si = 1; si <= N; ++si) sum += L[si] * d[si - 1];
+    double rhs = sB - sx;
+    if (a.flags & LF_RELAXED) rhs = (1 - a.beta * epsk) * rhs;
+    const double tol = jmax(0.0, sx - sB);
+    if (sum - rhs > tol) {
+      // indices 1..N by dvdf descending (sort!(..., rev=true) on (value, index) tuples)
+      int order[MQ];
+      for (int i = 0; i < N; ++i) order[i] = i + 1;
+      for (int i = 1; i < N; ++i)
+        for (int j = i; j > 0; --j) {
+          const int x = order[j - 1], y = order[j];
+          const bool y_first = jisless(d[x - 1], d[y - 1]) || (!jisless(d[y - 1], d[x - 1]) && x < y);
+          if (!y_first) break;
+          order[j - 1] = y;
+          order[j] = x;
+        }
+      int curr = 1;
+      double lhs = sum;
+      while (lhs > rhs + tol && curr <= n - 1) {
+        const int idx = order[curr - 1];
+        if (d[idx - 1] < a.ZEROTOL) break;
+        lhs = lhs - L[idx] * d[idx - 1];
+        curr += 1;
+      }
+      for (int i = 1; i <= curr - 1; ++i) {
+        const int idx = order[i - 1];
+        const double l_new = (i == curr - 1) ? jmax((rhs + tol - lhs) / d[idx - 1], 0.0) : 0.0;
+        L[idx] = jmin(L[idx], l_new);
+      }
+    }
+  }
+  double* Lr = a.Lraw + (size_t)2 * n * k;
+  for (int i = 0; i < 2 * n; ++i) Lr[i] = L[i];
+  double* fb = a.fbar + (size_t)8 * (n + 1) * k;
+  for (int i = 0; i <= n; ++i) {
+    st4(fb + 4 * i, fH[i]);
+    st4(fb + 4 * (n + 1 + i), fL[i]);
+  }
+}
+
+// symmetrize_limiting_parameters!(::Dim1) (subcell.jl:405-415) across mapP,
+// accumulate_f_bar_limited!(::Dim1) (:826-839), apply_subcell_limiter!(::Dim1) (:878-892);
+// then the SSP-RK3 stage update (SSPRK33.jl:125-139) and the positivity record
+__global__ void k_line_update(LineArgs a) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= a.K) return;
+  const int n = a.N1D, s = a.nstage - 1;
+  const LineOps& o = *a.ops;
+  const double J = a.geom[5 * (size_t)k];
+  double* rU = a.rhsU + 4 * (size_t)n * k;
+  if (a.flags & LF_SUBCELL) {
+    const double* Lr = a.Lraw + (size_t)2 * n * k;
+    double L[MS];
+    for (int i = 0; i < 2 * n; ++i) L[i] = Lr[i];
+    for (int f = 0; f < 2; ++f) {
+      const int p = a.nbr[2 * k + f], kP = p / 2, iP = p % 2;
+      const int si = f == 0 ? 0 : n, siP = iP == 0 ? 0 : n;
+      L[si] = jmin(Lr[si], a.Lraw[(size_t)2 * n * kP + siP]);
+    }
+    double* Lo = a.Lloc + (size_t)2 * n * ((size_t)a.K * s + k);
+    for (int i = 0; i < 2 * n; ++i) Lo[i] = L[i];
+    const double* fb = a.fbar + (size_t)8 * (n + 1) * k;
+    double flim[MQ + 1][4];
+    for (int i = 0; i <= n; ++i)
+      for (int c = 0; c < 4; ++c) flim[i][c] = L[i] * fb[4 * i + c] + (1.0 - L[i]) * fb[4 * (n + 1 + i) + c];
+    for (int i = 0; i < n; ++i) {
+      const double wJ = o.wq[i] * J;
+      for (int c = 0; c < 4; ++c) rU[4 * i + c] = (flim[i + 1][c] - flim[i][c]) / wJ;
+    }
+  }
+  if (!(a.flags & LF_UPDATE)) return;
+  const double dt = __longlong_as_double((long long)*a.dtkey);
+  double rmin = INFINITY, emin = INFINITY;
+  int bad = 0;
+  for (int i = 0; i < n; ++i) {
+    double* u = a.Uq + 4 * ((size_t)n * k + i);
+    double* w = a.resW + 4 * ((size_t)n * k + i);
+    for (int c = 0; c < 4; ++c) {
+      if (a.nstage == 1) {
+        w[c] = u[c];
+        u[c] = w[c] + dt * rU[4 * i + c];
+      } else {
+        const double z = u[c] + dt * rU[4 * i + c];
+        u[c] = a.nstage == 2 ? 3.0 / 4.0 * w[c] + 1.0 / 4.0 * z : 1.0 / 3.0 * w[c] + 2.0 / 3.0 * z;
+      }
+    }
+    const double re = rhoe4(u);
+    if (isnan(u[0]) || isnan(re)) bad |= ST_NAN;
+    if (!(u[0] > 0.0) || !(re > 0.0)) bad |= ST_NOT_POSITIVE;
+    rmin = fmin(rmin, u[0]);
+    emin = fmin(emin, re);
+  }
+  if (bad) atomicOr(a.status, bad);
+  atomicMin(&a.minrec[2 * s], encode_key(rmin));
+  atomicMin(&a.minrec[2 * s + 1], encode_key(emin));
+}
+
+template <typename T>
+cudaError_t dalloc(LineSolve* L, T** p, size_t count) {
+  void* q = nullptr;
+  const size_t bytes = sizeof(T) * (count > 0 ? count : 1);
+  cudaError_t e = cudaMalloc(&q, bytes);
+  if (e != cudaSuccess) return e;
+  e = cudaMemsetAsync(q, 0, bytes, L->stream);
+  if (e != cudaSuccess) return e;
+  L->allocs.push_back(q);
+  *p = (T*)q;
+  return cudaSuccess;
+}
+
+bool is_one_of(int b, std::initializer_list<int> l) {
+  for (int x : l)
+    if (b == x) return true;
+  return false;
+}
+
+int line_flags(const LineSolve* L, int nstage, bool update) {
+  const p2de_param& p = L->prm;
+  int f = 0;
+  switch (p.rhs_type) {
+    case P2DE_RHS_LOW_ORDER_POSITIVITY: f |= LF_LOW | LF_RHSU_L; break;
+    case P2DE_RHS_ENTROPY_STABLE: f |= LF_HIGH | LF_RHSU_H; break;
+    default: f |= LF_LOW | LF_HIGH | (p.rhs_limiter == P2DE_LIMITER_ZHANG_SHU ? LF_ZS : LF_SUBCELL); break;
+  }
+  if ((f & LF_LOW) && nstage == 1) f |= LF_CFL;
+  if (p.low_order_surface_flux == P2DE_FLUX_LAX_FRIEDRICHS_ON_PROJECTED_VAL) f |= LF_LFPROJ;
+  if (p.approximation_basis == P2DE_BASIS_GAUSS && p.entropyproj_limiter == P2DE_ENTROPYPROJ_NODEWISE_SCALED_EXTRAPOLATION)
+    f |= LF_NSE;
+  if ((f & (LF_ZS | LF_SUBCELL)) && p.shock_capture == 1) f |= LF_SHOCK;
+  if (f & LF_SUBCELL) {
+    const int b = p.bound_type;
+    if (is_one_of(b, {P2DE_BOUND_TVD, P2DE_BOUND_TVD_AND_CELL_ENTROPY, P2DE_BOUND_TVD_AND_MIN_ENTROPY,
+                      P2DE_BOUND_TVD_AND_RELAXED_MIN_ENTROPY, P2DE_BOUND_TVD_AND_RELAXED_CELL_ENTROPY}))
+      f |= LF_TVD;
+    if (is_one_of(b, {P2DE_BOUND_POSITIVITY_AND_MIN_ENTROPY, P2DE_BOUND_POSITIVITY_AND_RELAXED_MIN_ENTROPY,
+                      P2DE_BOUND_TVD_AND_MIN_ENTROPY, P2DE_BOUND_TVD_AND_RELAXED_MIN_ENTROPY}))
+      f |= LF_MINENT;
+    if (is_one_of(b, {P2DE_BOUND_POSITIVITY_AND_RELAXED_MIN_ENTROPY, P2DE_BOUND_TVD_AND_RELAXED_MIN_ENTROPY,
+                      P2DE_BOUND_POSITIVITY_AND_RELAXED_CELL_ENTROPY, P2DE_BOUND_TVD_AND_RELAXED_CELL_ENTROPY}))
+      f |= LF_RELAXED;
+    if (is_one_of(b, {P2DE_BOUND_POSITIVITY_AND_CELL_ENTROPY, P2DE_BOUND_TVD_AND_CELL_ENTROPY,
+                      P2DE_BOUND_POSITIVITY_AND_RELAXED_CELL_ENTROPY, P2DE_BOUND_TVD_AND_RELAXED_CELL_ENTROPY}))
+      f |= LF_CELL;
+  }
+  if (update) f |= LF_UPDATE;
+  return f;
+}
+
+LineArgs args_of(const LineSolve* L, int nstage, int flags) {
+  const p2de_param& p = L->prm;
+  LineArgs a{};
+  a.K = L->K;
+  a.N1D = L->N1D;
+  a.nstage = nstage;
+  a.flags = flags;
+  a.ops = L->ops;
+  a.Uq = L->Uq;
+  a.resW = L->resW;
+  a.rhsL = L->rhsL;
+  a.rhsH = L->rhsH;
+  a.rhsU = L->rhsU;
+  a.BFL = L->BFL;
+  a.BFH = L->BFH;
+  a.uf = L->uf;
+  a.theta = L->theta;
+  a.Lloc = L->Lloc;
+  a.Lraw = L->Lraw;
+  a.fbar = L->fbar;
+  a.Lelem = L->Lelem;
+  a.geom = L->geom;
+  a.Ival = L->Ival;
+  a.phikey = reinterpret_cast<long long*>(L->phimin);
+  a.nbr = L->nbr;
+  a.bcidx = L->bcidx;
+  a.bc = L->bc;
+  a.dtkey = L->dtkey;
+  a.minrec = L->minrec;
+  a.status = L->status;
+  a.gamma = p.gamma;
+  a.POSTOL = p.POSTOL;
+  a.ZEROTOL = p.ZEROTOL;
+  a.zeta = p.zeta;
+  a.eta = p.eta;
+  a.CFL = p.CFL;
+  a.beta = p.bound_beta;
+  // HennemannShockCapture (shock_capture.jl:118-137): threshold and sigmoid sharpness
+  const int N = L->N1D - 1;
+  a.sc_TN = p.shock_capture_a * std::pow(10.0, -p.shock_capture_c * std::pow((double)(N + 1), 0.25));
+  a.sc_sfac = std::log((1 - 0.0001) / 0.0001);
+  a.s0 = std::log(1.0 / ((double)N * N * N * N)) / std::log(10.0);
+  return a;
+}
+
+double host_jmin(double x, double y) {
+  if (std::isnan(x) || std::isnan(y)) return NAN;
+  if (x == y) return std::signbit(x) ? x : y;
+  return x < y ? x : y;
+}
+
+// the launches of one stage; dt_set: the stage's dt when the low-order CFL does not set it
+cudaError_t launch_stage(LineSolve* L, double t, int nstage, double dt_set, bool update) {
+  const int flags = line_flags(L, nstage, update);
+  LineArgs a = args_of(L, nstage, flags);
+  const int grid = (L->K + kThreads - 1) / kThreads;
+  const bool phimin = (flags & LF_MINENT) && t == L->prm.t0 && nstage == 1;
+  const bool begin = nstage == 1 || !update;
+  if (begin) {
+    // a step starts from min(CFL dt0, T - t) (SSPRK33.jl:125-127), which the stage-1 CFL of a
+    // low-order RHS lowers; a lone RHS keeps the dt it is given unless it sets the CFL
+    const bool initial = (nstage == 1 && update) || (flags & LF_CFL);
+    const double dt0 = initial ? host_jmin(L->prm.CFL * L->prm.dt0, L->prm.T - t) : dt_set;
+    k_line_begin<<<1, 32, 0, L->stream>>>(a, dt0, nstage == 1 ? 1 : 0, phimin ? 1 : 0);
+    L->launches += 1;
+  }
+  k_line_face<<<grid, kThreads, 0, L->stream>>>(a);
+  L->launches += 1;
+  if (flags & LF_LOW) {
+    k_line_low<<<grid, kThreads, 0, L->stream>>>(a);
+    L->launches += 1;
+  }
+  if (phimin) {
+    const long long nodes = (long long)L->K * L->N1D;
+    k_line_phimin<<<(int)((nodes + 255) / 256), 256, 0, L->stream>>>(a);
+    L->launches += 1;
+  }
+  if (flags & LF_HIGH) {
+    k_line_high<<<grid, kThreads, 0, L->stream>>>(a);
+    L->launches += 1;
+  }
+  if (flags & (LF_SUBCELL | LF_UPDATE)) {
+    k_line_update<<<grid, kThreads, 0, L->stream>>>(a);
+    L->launches += 1;
+  }
+  return cudaGetLastError();
+}
+
+int check(LineSolve* L, std::string& err) {
+  int st = 0;
+  cudaError_t e = cudaMemcpyAsync(&st, L->status, sizeof(int), cudaMemcpyDeviceToHost, L->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(L->stream);
+  if (e != cudaSuccess) {
+    err = std::string("line solve: ") + cudaGetErrorString(e);
+    return P2DE_ERR_CUDA;
+  }
+  if (st & (ST_NOT_POSITIVE | ST_NAN)) {
+    err = "density or internal energy not positive (status " + std::to_string(st) + ")";
+    return P2DE_ERR_NOT_POSITIVE;
+  }
+  if (st & ST_BAD_DT) {
+    err = "time step not positive (status " + std::to_string(st) + ")";
+    return P2DE_ERR_BAD_DT;
+  }
+  return P2DE_OK;
+}
+
+double read_dt(LineSolve* L, cudaError_t& e) {
+  unsigned long long b = 0;
+  e = cudaMemcpyAsync(&b, L->dtkey, sizeof b, cudaMemcpyDeviceToHost, L->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(L->stream);
+  double d;
+  std::memcpy(&d, &b, sizeof d);
+  return d;
+}
+
+}  // namespace
+
+int line_create(const p2de_param* prm, const p2de_mesh* mesh, cudaStream_t st, LineSolve** out, std::string& err) {
+  *out = nullptr;
+  if (prm->reference_semantics) {
+    err = "CompressibleEulerIdealGas{Dim1}: the reference raises a MethodError in every RHS (Bx(::Dim1) "
+          "calls reference_to_physical with dim last, rhs_utils.jl:18); use reference_semantics = 0";
+    return P2DE_ERR_UNSUPPORTED;
+  }
+  if (prm->precision != P2DE_PRECISION_FP64 || mesh->nW || mesh->nS) {
+    err = "CompressibleEulerIdealGas{Dim1}: FP64, periodic, inflow and outflow faces";
+    return P2DE_ERR_UNSUPPORTED;
+  }
+  const int b = prm->bound_type;
+  if (prm->approximation_basis == P2DE_BASIS_GAUSS && prm->rhs_limiter == P2DE_LIMITER_SUBCELL &&
+      prm->rhs_type == P2DE_RHS_ES_LIMITED_LOW_ORDER_POS &&
+      is_one_of(b, {P2DE_BOUND_POSITIVITY_AND_CELL_ENTROPY, P2DE_BOUND_TVD_AND_CELL_ENTROPY,
+                    P2DE_BOUND_POSITIVITY_AND_RELAXED_CELL_ENTROPY, P2DE_BOUND_TVD_AND_RELAXED_CELL_ENTROPY})) {
+    err = "CompressibleEulerIdealGas{Dim1}: no cell-entropy bounds on Gauss nodes (enforce_ES_subcell_interface! "
+          "has no Dim1 method for GaussCollocation, subcell.jl:755-759)";
+    return P2DE_ERR_UNSUPPORTED;
+  }
+  const int K = prm->K, n = prm->N + 1;
+  const int64_t nfk = 2 * (int64_t)K;
+  for (int64_t i = 0; i < nfk; ++i)
+    if (mesh->mapP[i] < 1 || mesh->mapP[i] > nfk) {
+      err = "mapP[" + std::to_string(i) + "] out of 1.." + std::to_string(nfk);
+      return P2DE_ERR_INVALID_ARGUMENT;
+    }
+  auto check_list = [&](const int64_t* m, int64_t cnt, const char* name) {
+    if (cnt < 0 || (cnt > 0 && !m)) return false;
+    for (int64_t i = 0; i < cnt; ++i)
+      if (m[i] < 1 || m[i] > nfk) return false;
+    (void)name;
+    return true;
+  };
+  if (!check_list(mesh->mapI, mesh->nI, "mapI") || !check_list(mesh->mapO, mesh->nO, "mapO") ||
+      (mesh->nI > 0 && !mesh->Ival)) {
+    err = "mapI/mapO/Ival: bad list";
+    return P2DE_ERR_INVALID_ARGUMENT;
+  }
+  for (int k = 0; k < K; ++k)
+    if (!(mesh->geom[5 * (size_t)k] > 0.0)) {
+      err = "J[" + std::to_string(k) + "] is not positive";
+      return P2DE_ERR_INVALID_ARGUMENT;
+    }
+  LineOps ops;
+  if (build_line_ops(prm->N, prm->ZEROTOL, &ops, prm->approximation_basis) != 0) {
+    err = "Line operators: degree out of range";
+    return P2DE_ERR_INVALID_ARGUMENT;
+  }
+  auto* L = new LineSolve();
+  L->prm = *prm;
+  L->N1D = n;
+  L->K = K;
+  L->stream = st;
+  std::vector<int32_t> nbr(nfk), bcidx(nfk, 0);
+  std::vector<int8_t> bc(nfk, BC_INTERIOR);
+  for (int64_t i = 0; i < nfk; ++i) nbr[i] = (int32_t)(mesh->mapP[i] - 1);
+  for (int64_t i = 0; i < mesh->nI; ++i) {
+    bc[mesh->mapI[i] - 1] = BC_INFLOW;
+    bcidx[mesh->mapI[i] - 1] = (int32_t)i;
+  }
+  for (int64_t i = 0; i < mesh->nO; ++i) bc[mesh->mapO[i] - 1] = BC_OUTFLOW;
+  const size_t nq = (size_t)4 * n * K;
+  cudaError_t e = cudaSuccess;
+  auto A = [&](auto** p, size_t cnt) {
+    if (e == cudaSuccess) e = dalloc(L, p, cnt);
+  };
+  A(&L->Uq, nq);
+  A(&L->resW, nq);
+  A(&L->rhsL, nq);
+  A(&L->rhsH, nq);
+  A(&L->rhsU, nq);
+  A(&L->BFL, (size_t)8 * K);
+  A(&L->BFH, (size_t)8 * K);
+  A(&L->uf, (size_t)8 * K);
+  A(&L->theta, (size_t)3 * 2 * K);
+  A(&L->Lloc, (size_t)3 * 2 * n * K);
+  A(&L->Lraw, (size_t)2 * n * K);
+  A(&L->fbar, (size_t)8 * (n + 1) * K);
+  A(&L->Lelem, (size_t)3 * K);
+  A(&L->geom, (size_t)5 * K);
+  A(&L->Ival, (size_t)3 * (mesh->nI > 0 ? mesh->nI : 1));
+  A(&L->phimin, 1);
+  A(&L->nbr, (size_t)nfk);
+  A(&L->bcidx, (size_t)nfk);
+  A(&L->bc, (size_t)nfk);
+  A(&L->dtkey, 1);
+  A(&L->minrec, 6);
+  A(&L->status, 1);
+  A(&L->ops, 1);
+  auto up = [&](void* dst, const void* src, size_t bytes) {
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st);
+  };
+  up(L->geom, mesh->geom, sizeof(double) * 5 * K);
+  if (mesh->nI > 0) up(L->Ival, mesh->Ival, sizeof(double) * 3 * mesh->nI);
+  up(L->nbr, nbr.data(), sizeof(int32_t) * nfk);
+  up(L->bcidx, bcidx.data(), sizeof(int32_t) * nfk);
+  up(L->bc, bc.data(), (size_t)nfk);
+  up(L->ops, &ops, sizeof ops);
+  // zeros(Float64, 1) of s_modified_min until t == t0 at stage 1
+  long long k0 = 0;  // the ordered key of +0.0
+  up(L->phimin, &k0, sizeof k0);
+  std::vector<double> ones((size_t)3 * 2 * K, 1.0);
+  up(L->theta, ones.data(), sizeof(double) * ones.size());
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) {
+    err = std::string("Line setup: ") + cudaGetErrorString(e);
+    line_destroy(L);
+    return P2DE_ERR_CUDA;
+  }
+  *out = L;
+  return P2DE_OK;
+}
+
+void line_destroy(LineSolve* L) {
+  if (!L) return;
+  if (L->stream) cudaStreamSynchronize(L->stream);
+  for (void* p : L->allocs) cudaFree(p);
+  delete L;
+}
+
+int64_t line_field_count(const LineSolve* L, int field) {
+  const int64_t n = L->N1D, K = L->K;
+  switch (field) {
+    case P2DE_FIELD_UQ:
+    case P2DE_FIELD_RHSU:
+    case P2DE_FIELD_RHSL:
+    case P2DE_FIELD_RHSH:
+    case P2DE_FIELD_RESW:
+    case P2DE_FIELD_RHSXYL:
+    case P2DE_FIELD_RHSXYH: return 3 * n * K;
+    case P2DE_FIELD_BF_L:
+    case P2DE_FIELD_BF_H: return 3 * 2 * K;
+    case P2DE_FIELD_L_LOCAL: return 2 * n * K;
+    case P2DE_FIELD_L: return K;
+    case P2DE_FIELD_THETA_LOCAL: return 2 * K;
+    default: return -1;
+  }
+}
+
+int line_set_Uq(LineSolve* L, const double* Uq, std::string& err) {
+  const size_t nodes = (size_t)L->N1D * L->K;
+  std::vector<double> full(4 * nodes);
+  for (size_t i = 0; i < nodes; ++i) {
+    full[4 * i] = Uq[3 * i];
+    full[4 * i + 1] = Uq[3 * i + 1];
+    full[4 * i + 2] = 0.0;
+    full[4 * i + 3] = Uq[3 * i + 2];
+  }
+  cudaError_t e = cudaMemcpyAsync(L->Uq, full.data(), sizeof(double) * full.size(), cudaMemcpyHostToDevice, L->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(L->status, 0, sizeof(int), L->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(L->stream);
+  if (e != cudaSuccess) {
+    err = std::string("set_Uq: ") + cudaGetErrorString(e);
+    return P2DE_ERR_CUDA;
+  }
+  return P2DE_OK;
+}
+
+int line_get_field(LineSolve* L, int field, int nstage, double* out, std::string& err) {
+  const int64_t cnt = line_field_count(L, field);
+  if (cnt < 0) return P2DE_ERR_INVALID_ARGUMENT;
+  const bool staged = field == P2DE_FIELD_L_LOCAL || field == P2DE_FIELD_L || field == P2DE_FIELD_THETA_LOCAL;
+  if (staged && (nstage < 1 || nstage > 3)) return P2DE_ERR_INVALID_ARGUMENT;
+  const double* src = nullptr;
+  bool states = true;
+  switch (field) {
+    case P2DE_FIELD_UQ: src = L->Uq; break;
+    case P2DE_FIELD_RHSU: src = L->rhsU; break;
+    case P2DE_FIELD_RHSL:
+    case P2DE_FIELD_RHSXYL: src = L->rhsL; break;
+    case P2DE_FIELD_RHSH:
+    case P2DE_FIELD_RHSXYH: src = L->rhsH; break;
+    case P2DE_FIELD_RESW: src = L->resW; break;
+    case P2DE_FIELD_BF_L: src = L->BFL; break;
+    case P2DE_FIELD_BF_H: src = L->BFH; break;
+    case P2DE_FIELD_L_LOCAL: src = L->Lloc + cnt * (nstage - 1), states = false; break;
+    case P2DE_FIELD_L: src = L->Lelem + cnt * (nstage - 1), states = false; break;
+    case P2DE_FIELD_THETA_LOCAL: src = L->theta + cnt * (nstage - 1), states = false; break;
+  }
+  cudaError_t e;
+  if (states) {  // four slots per state -> (rho, rhou, E)
+    std::vector<double> full((size_t)cnt / 3 * 4);
+    e = cudaMemcpyAsync(full.data(), src, sizeof(double) * full.size(), cudaMemcpyDeviceToHost, L->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(L->stream);
+    for (int64_t i = 0; i < cnt / 3; ++i) {
+      out[3 * i] = full[4 * i];
+      out[3 * i + 1] = full[4 * i + 1];
+      out[3 * i + 2] = full[4 * i + 3];
+    }
+  } else {
+    e = cudaMemcpyAsync(out, src, sizeof(double) * cnt, cudaMemcpyDeviceToHost, L->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(L->stream);
+  }
+  if (e != cudaSuccess) {
+    err = std::string("get_field: ") + cudaGetErrorString(e);
+    return P2DE_ERR_CUDA;
+  }
+  return P2DE_OK;
+}
+
+int line_rhs(LineSolve* L, double t, double dt, int nstage, double* dt_out, std::string& err) {
+  if (nstage < 1 || nstage > 3) return P2DE_ERR_INVALID_ARGUMENT;
+  cudaError_t e = launch_stage(L, t, nstage, dt, false);
+  if (e != cudaSuccess) {
+    err = std::string("line rhs: ") + cudaGetErrorString(e);
+    return P2DE_ERR_CUDA;
+  }
+  const double d = read_dt(L, e);
+  if (e != cudaSuccess) {
+    err = std::string("line rhs: ") + cudaGetErrorString(e);
+    return P2DE_ERR_CUDA;
+  }
+  if (dt_out) *dt_out = d;
+  return check(L, err);
+}
+
+int line_step(LineSolve* L, double* t, double* dt_out, std::string& err) {
+  if (!(*t < L->prm.T)) {  // the time loop has ended (SSPRK33.jl:125)
+    if (dt_out) *dt_out = 0.0;
+    return P2DE_OK;
+  }
+  cudaError_t e = cudaSuccess;
+  for (int stage = 1; stage <= 3 && e == cudaSuccess; ++stage) e = launch_stage(L, *t, stage, 0.0, true);
+  if (e != cudaSuccess) {
+    err = std::string("line step: ") + cudaGetErrorString(e);
+    return P2DE_ERR_CUDA;
+  }
+  const double dt = read_dt(L, e);
+  if (e != cudaSuccess) {
+    err = std::string("line step: ") + cudaGetErrorString(e);
+    return P2DE_ERR_CUDA;
+  }
+  const int rc = check(L, err);
+  if (rc != P2DE_OK) return rc;
+  *t = *t + dt;
+  if (dt_out) *dt_out = dt;
+  return P2DE_OK;
+}
+
+int line_step_launches(const LineSolve* L) {
+  int c = 0;
+  for (int stage = 1; stage <= 3; ++stage) {
+    const int f = line_flags(L, stage, true);
+    c += (stage == 1 ? 1 : 0) + 1 + ((f & LF_LOW) ? 1 : 0) + ((f & LF_HIGH) ? 1 : 0) + 1;
+  }
+  return c;
+}
+
+}  // namespace p2de

@@ -1,0 +1,52 @@
+// CompressibleEulerIdealGas{Dim1} on a Line mesh: device state and host driver of the
+// RHS and SSP-RK3 stage (p2de_line.cu). Reached through the p2de_* entry points when
+// param.equation is P2DE_EQUATION_COMPRESSIBLE_EULER_1D.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/p2de.h"
+#include "p2de_tables.h"
+
+namespace p2de {
+
+struct LineSolve {
+  p2de_param prm{};
+  int N1D = 0, K = 0;
+  cudaStream_t stream = nullptr;
+  // states hold four slots per node, (rho, rhou, 0, E), like the Dim2 layout
+  double *Uq = nullptr, *resW = nullptr, *rhsL = nullptr, *rhsH = nullptr, *rhsU = nullptr;
+  double *BFL = nullptr, *BFH = nullptr;  // 2 x 4 per element (the x part)
+  double *uf = nullptr;                   // projected face states u_tilde, 2 x 4 per element
+  double *theta = nullptr;                // theta_local, 3 stages x K x 2
+  double *Lloc = nullptr;                 // L_local, 3 stages x K x 2 N1D
+  double *Lraw = nullptr;                 // L_local before symmetrization, K x 2 N1D
+  double *fbar = nullptr;                 // f_bar_H, f_bar_L: K x 2 x (N1D+1) x 4
+  double *Lelem = nullptr;                // ZhangShuLimiter L, 3 stages x K
+  double *geom = nullptr, *Ival = nullptr, *phimin = nullptr;
+  int32_t *nbr = nullptr, *bcidx = nullptr;
+  int8_t* bc = nullptr;
+  unsigned long long* dtkey = nullptr;  // bits of the stage's dt (positive: ordered)
+  long long* minrec = nullptr;          // min rho, min rhoe per stage (ordered keys)
+  int* status = nullptr;
+  LineOps* ops = nullptr;
+  int64_t launches = 0;
+  std::vector<void*> allocs;
+};
+
+int line_create(const p2de_param* prm, const p2de_mesh* mesh, cudaStream_t st, LineSolve** out, std::string& err);
+void line_destroy(LineSolve* L);
+int64_t line_field_count(const LineSolve* L, int field);
+int line_set_Uq(LineSolve* L, const double* Uq, std::string& err);
+int line_get_field(LineSolve* L, int field, int nstage, double* out, std::string& err);
+// rhs!(state, solver, state_param, TimeParam(t, dt, nstage)) without the stage update
+int line_rhs(LineSolve* L, double t, double dt, int nstage, double* dt_out, std::string& err);
+// one SSP33! loop body from *t
+int line_step(LineSolve* L, double* t, double* dt_out, std::string& err);
+// kernel launches of one step
+int line_step_launches(const LineSolve* L);
+
+}  // namespace p2de

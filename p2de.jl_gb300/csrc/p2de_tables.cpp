@@ -344,3 +344,68 @@ int build_op_table(int N, double zerotol, OpTable* T, int basis) {
 }
 
 }  // namespace p2de
+
+namespace p2de {
+
+int build_line_ops(int N, double zerotol, LineOps* T, int basis) {
+  if (N < 1 || N + 1 > kMaxN1D || basis < 0 || basis > 1) return 1;
+  std::memset(T, 0, sizeof(LineOps));
+  const int n = N + 1, Nh = n + 2;
+  double r[kMaxN1D], w[kMaxN1D], D[kMaxN1D * kMaxN1D], ellm[kMaxN1D], ellp[kMaxN1D];
+  if (basis == 1) {
+    gauss_rule(N, r, w, D, ellm, ellp);
+  } else {
+    gll_rule(N, r, w, D);
+    for (int i = 0; i < n; ++i) ellm[i] = ellp[i] = 0.0;
+    ellm[0] = 1.0;
+    ellp[N] = 1.0;
+  }
+  T->N1D = n;
+  T->basis = basis;
+  T->rxf[0] = -1.0;
+  T->rxf[1] = 1.0;
+  for (int i = 0; i < n; ++i) {
+    T->wq[i] = w[i];
+    T->Vf[0][i] = std::fabs(ellm[i]) <= zerotol ? 0.0 : ellm[i];
+    T->Vf[1][i] = std::fabs(ellp[i]) <= zerotol ? 0.0 : ellp[i];
+  }
+  // Q = M Dr with droptol! (init.jl:149); Srh_db of the hybridized operator (init.jl:150-155)
+  std::vector<double> Q((size_t)n * n);
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) {
+      const double q = w[i] * D[i * n + j];
+      Q[i + (size_t)n * j] = std::fabs(q) <= zerotol ? 0.0 : q;
+    }
+  for (int j = 0; j < n; ++j)
+    for (int i = 0; i < n; ++i) T->Sh[i + Nh * j] = Q[i + (size_t)n * j] - Q[j + (size_t)n * i];
+  for (int f = 0; f < 2; ++f)
+    for (int i = 0; i < n; ++i) {
+      const double e = T->Vf[f][i];
+      if (e == 0.0) continue;
+      T->Sh[i + Nh * (n + f)] = e * T->rxf[f];
+      T->Sh[(n + f) + Nh * i] = -(T->rxf[f] * e);
+    }
+  if (basis == 1)
+    for (int i = 0; i < Nh * Nh; ++i)
+      if (std::fabs(0.5 * T->Sh[i]) <= zerotol) T->Sh[i] = 0.0;
+  int np = 0;
+  for (int j = 0; j < Nh; ++j)
+    for (int i = j + 1; i < Nh; ++i)
+      if (T->Sh[i + Nh * j] != 0.0) {
+        T->pi[np] = (int8_t)i;
+        T->pj[np] = (int8_t)j;
+        ++np;
+      }
+  T->npair = np;
+  for (int i = 0; i < n; ++i) {
+    T->MinvVhT[i + n * i] = 1.0 / w[i];
+    for (int f = 0; f < 2; ++f)
+      if (T->Vf[f][i] != 0.0) T->MinvVhT[i + n * (n + f)] = T->Vf[f][i] / w[i];
+  }
+  std::vector<double> V((size_t)n * n);
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) V[(size_t)i * n + j] = legendre_normalized(j, r[i]);
+  return invert(V, n, T->VDMinv) ? 0 : 2;
+}
+
+}  // namespace p2de

@@ -66,6 +66,24 @@ struct OpTable {
 // nodes. Returns 0 on success.
 int build_op_table(int N, double zerotol, OpTable* out, int basis = 0);
 
+// Operators of a Line element (initialize_reference_data(::Dim1), init.jl:66-80, with
+// initialize_operators, :133-228): N1D nodes, face nodes r = -1 (0) and r = +1 (1).
+constexpr int kLineMaxNh = kMaxN1D + 2;
+constexpr int kLineMaxPairs = kLineMaxNh * (kLineMaxNh - 1) / 2;
+struct LineOps {
+  int32_t N1D, basis, npair;
+  double wq[kMaxN1D];
+  double rxf[2];                          // Br: -1, +1 (nrJ with wf = 1)
+  double Vf[2][kMaxN1D];                  // face extrapolation (LGL: unit vectors)
+  double Sh[kLineMaxNh * kLineMaxNh];     // Srh_db = [Q - Q', Ef' B; -B Ef, 0], column-major Nh x Nh
+  int8_t pi[kLineMaxPairs], pj[kLineMaxPairs];  // its nonzero pairs i > j, j outer (init.jl:188-195)
+  double MinvVhT[kMaxN1D * kLineMaxNh];   // M \ Vh' = (1/wq) [I, Vf'], column-major Nq x Nh
+  double VDMinv[kMaxN1D * kMaxN1D];       // inv(VDM) of the orthonormal Legendre modes, row-major
+};
+
+// Builds the Line operators for degree N (1..5) on LGL (basis 0) or Gauss (basis 1) nodes.
+int build_line_ops(int N, double zerotol, LineOps* out, int basis);
+
 // The 1D Gauss-Legendre rule (nodes, weights), differentiation matrix (row-major) and the
 // Lagrange basis at -1 and +1.
 void gauss_rule(int N, double* r, double* w, double* D, double* ellm, double* ellp);

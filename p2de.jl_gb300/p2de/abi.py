@@ -71,6 +71,7 @@ FIELD_THETA_LOCAL = 11
 # p2de_equation
 EQUATION_COMPRESSIBLE_EULER = 0
 EQUATION_KPP = 1
+EQUATION_COMPRESSIBLE_EULER_1D = 2
 # p2de_basis, p2de_entropyproj_limiter
 BASIS_LOBATTO = 0
 BASIS_GAUSS = 1

@@ -104,6 +104,7 @@ class MeshData:
     mapB: np.ndarray  # boundary face nodes (1-based), those with mapP == mapM
     geom: np.ndarray  # (K, 5): J, rxJ, sxJ, ryJ, syJ
     sides: dict = field(default_factory=dict)  # 'left','right','bottom','top' -> 1-based face nodes
+    dim1: bool = False  # a Line mesh (K = (K, 1), y = 0, two face nodes per element)
 
     @property
     def xq(self):
@@ -164,6 +165,33 @@ def uniform_mesh(N: int, Kx: int, Ky: int, xL=(0.0, 0.0), xR=(1.0, 1.0), basis: 
     geom[:, 1] = hy / 2.0
     geom[:, 4] = hx / 2.0
     return MeshData(N, (Kx, Ky), tuple(xL), tuple(xR), x, y, xf, yf, mapM, mapP, mapB, geom, sides)
+
+
+def uniform_mesh_1d(N: int, K: int, xL: float = 0.0, xR: float = 1.0, basis: str = "lobatto",
+                    periodic: bool = False) -> MeshData:
+    """initialize_uniform_mesh_data(::Line) (init.jl:230-239): K equal elements on [xL, xR],
+    nodes on the LGL or Gauss points, face nodes at r = -1, +1; StartUpDG's MeshData for a Line
+    maps the two domain ends to themselves unless periodic. geom rows (J, rxJ) = (h/2, 1)."""
+    n = N + 1
+    r, _ = gauss_rule(N) if basis == "gauss" else gll_rule(N)
+    h = (xR - xL) / K
+    k = np.arange(K)
+    x = xL + h * k[:, None] + 0.5 * (r[None, :] + 1.0) * h
+    xf = xL + h * k[:, None] + 0.5 * (np.array([-1.0, 1.0])[None, :] + 1.0) * h
+    mapM = 1 + np.arange(2)[None, :] + 2 * k[:, None]
+    mapP = mapM.copy()
+    mapP[1:, 0] = mapM[:-1, 1]
+    mapP[:-1, 1] = mapM[1:, 0]
+    if periodic:
+        mapP[0, 0], mapP[-1, 1] = mapM[-1, 1], mapM[0, 0]
+    mapB = np.sort(mapM[mapP == mapM])
+    geom = np.zeros((K, 5))
+    geom[:, 0] = h / 2.0
+    geom[:, 1] = 1.0
+    sides = {"left": np.array([1]) if not periodic else np.array([], dtype=int),
+             "right": np.array([2 * K]) if not periodic else np.array([], dtype=int)}
+    return MeshData(N, (K, 1), (xL, 0.0), (xR, 0.0), x, np.zeros_like(x), xf, np.zeros_like(xf), mapM, mapP,
+                    mapB, geom, sides, dim1=True)
 
 
 def make_periodic(md: MeshData, periodic=(True, True)) -> MeshData:

@@ -33,8 +33,11 @@ from .types import (
 
 def primitive_to_conservative(equation, prim) -> np.ndarray:
     """primitive_to_conservative(::CompressibleIdealGas{Dim2}) (compressible_Navier_Stokes.jl:9-16),
-    vectorised: (rho, u, v, p) arrays -> (..., 4)."""
+    vectorised: (rho, u, v, p) arrays -> (..., 4); (rho, u, p) -> (..., 3) on a Line."""
     gamma = equation.gamma
+    if len(prim) == 3:  # primitive_to_conservative(::CompressibleIdealGas{Dim1}) (:1-7)
+        rho, u, p = np.broadcast_arrays(*(np.asarray(a, dtype=np.float64) for a in prim))
+        return np.stack([rho, rho * u, p / (gamma - 1) + 0.5 * rho * u**2], axis=-1)
     rho, u, v, p = (np.asarray(a, dtype=np.float64) for a in prim)
     rho, u, v, p = np.broadcast_arrays(rho, u, v, p)
     E = p / (gamma - 1) + 0.5 * rho * (u**2 + v**2)
@@ -275,3 +278,128 @@ def isentropic_vortex(N=3, Kx=5, Ky=5, T=0.02, strength=8.5, ux=1.0, uy=0.0, **k
 
 def with_precision(param: Param, precision: str) -> Param:
     return replace(param, precision=precision)
+
+
+# --- CompressibleEulerIdealGas{Dim1} --------------------------------------------------
+# The reference's Dim1 path raises before its first RHS (Bx(::Dim1) calls
+# reference_to_physical with its arguments in the wrong order, rhs_utils.jl:18), so these
+# problems run with reference_semantics=False: the Dim1 methods with their evident meaning.
+def line_param(N, K, xL, xR, T, gamma=1.4, CFL=0.5, dt0=None, t0=0.0, zeta=0.1, eta=0.5, rhs_limiter=None,
+               approximation_basis=None, entropyproj_limiter=None, rhs=None, **kw):
+    """Param of a CompressibleEulerIdealGas{Dim1} solve on [xL, xR] with K elements."""
+    from .types import Dim1, PositivityBound
+
+    if rhs_limiter is None:
+        rhs_limiter = SubcellLimiter(bound=PositivityBound())
+    kw.pop("reference_semantics", None)
+    p = default_param(N, (K, 1), (xL, 0.0), (xR, 0.0), T, CFL=CFL, dt0=dt0, rhs_limiter=rhs_limiter,
+                      approximation_basis=approximation_basis, entropyproj_limiter=entropyproj_limiter,
+                      reference_semantics=False, **kw)
+    return replace(p, K=int(K), xL=float(xL), xR=float(xR), equation=CompressibleEulerIdealGas(gamma, Dim1),
+                   limiting_param=LimitingParameter(zeta=zeta, eta=eta),
+                   timestepping_param=TimesteppingParameter(T=T, CFL=CFL, dt0=T if dt0 is None else dt0, t0=t0),
+                   rhs=rhs if rhs is not None else ESLimitedLowOrderPos())
+
+
+def inflow_outflow_1d(state_left):
+    """initial_boundary_conditions of examples/1D/shu-osher.jl:16-32: mapI = [1] with the
+    conservative state_left, mapO = [2K], mapP of the Line mesh."""
+
+    def bc(param, md: MeshData) -> BCData:
+        K = md.num_elements
+        return BCData(mapP=md.mapP, mapI=np.array([1]), mapO=np.array([2 * K]),
+                      Ival=np.asarray(state_left, dtype=np.float64).reshape(1, 3))
+
+    return bc
+
+
+def shu_osher_exact(equation=None, x=None, t=0.0):
+    """exact_sol of examples/1D/shu-osher.jl:8-14 (the initial data)."""
+    x = np.asarray(x, dtype=np.float64)
+    left = x < -4.0
+    rho = np.where(left, 3.857143, 1 + 0.2 * np.sin(5 * x))
+    u = np.where(left, 2.629369, 0.0)
+    p = np.where(left, 10.3333, 1.0)
+    return rho, u, p
+
+
+def shu_osher(N=3, K=64, T=1.8, **kw):
+    """examples/1D/shu-osher.jl:44-56: [-5, 5], gamma 1.4, CFL 0.5, dt0 1e-4, zeta 0.1,
+    eta 1.0, GaussCollocation with NodewiseScaledExtrapolation, ESLimitedLowOrderPos(
+    LaxFriedrichsOnNodalVal, LaxFriedrichsOnProjectedVal), SubcellLimiter(PositivityBound)."""
+    from .types import GaussCollocation, NodewiseScaledExtrapolation
+
+    kw.setdefault("dt0", 1e-4)
+    kw.setdefault("eta", 1.0)
+    kw.setdefault("approximation_basis", GaussCollocation())
+    kw.setdefault("entropyproj_limiter", NodewiseScaledExtrapolation())
+    param = line_param(N, K, -5.0, 5.0, T, **kw)
+    eq = param.equation
+
+    def initial_condition(param, x):
+        return primitive_to_conservative(param.equation, shu_osher_exact(param.equation, x, 0.0))
+
+    left = primitive_to_conservative(eq, (3.857143, 2.629369, 10.3333))
+    return param, initial_condition, inflow_outflow_1d(left), shu_osher_exact
+
+
+def leblanc_exact(equation, x, t):
+    """exact_sol of examples/convergence/leblanc-convergence.jl:9-40: the Leblanc shock tube
+    (rho 1 | 1e-3, p (gamma-1) 1e-1 | (gamma-1) 1e-10, interface at x = 0.33)."""
+    gamma = equation.gamma
+    x = np.asarray(x, dtype=np.float64)
+    rhoL, rhoR, pL, pR = 1.0, 1e-3, (gamma - 1) * 1e-1, (gamma - 1) * 1e-10
+    if t == 0:
+        left = x < 0.33
+        return np.where(left, rhoL, rhoR), np.zeros_like(x), np.where(left, pL, pR)
+    xi = (x - 0.33) / t
+    rhoLstar, rhoRstar = 5.4079335349316249e-2, 3.9999980604299963e-3
+    vstar, pstar = 0.62183867139173454, 0.51557792765096996e-3
+    lambda1, lambda3 = 0.49578489518897934, 0.82911836253346982
+    fan = (xi > -1 / 3) & (xi <= lambda1)
+    rho = np.select([xi <= -1 / 3, fan, xi <= vstar, xi <= lambda3], [rhoL, (0.75 - 0.75 * xi) ** 3, rhoLstar, rhoRstar], rhoR)
+    u = np.select([xi <= -1 / 3, fan, xi <= lambda3], [0.0, 0.75 * (1 / 3 + xi), vstar], 0.0)
+    p = np.select([xi <= -1 / 3, fan, xi <= lambda3], [pL, 1 / 15 * (0.75 - 0.75 * xi) ** 5, pstar], pR)
+    return rho, u, p
+
+
+def leblanc(N=2, K=50, T=2 / 3, **kw):
+    """examples/convergence/leblanc-convergence.jl:75-89: [0, 1], gamma 5/3, CFL 0.5, dt0 1e-3,
+    t0 0.01 (the initial data is the exact solution there), zeta 0.1, eta 0.1; inflow at the
+    left end, outflow at the right. The limiter and basis come from kw (default
+    SubcellLimiter(PositivityBound) on LGL nodes)."""
+    kw.setdefault("dt0", 1e-3)
+    kw.setdefault("eta", 0.1)
+    kw.setdefault("t0", 0.01)
+    param = line_param(N, K, 0.0, 1.0, T, gamma=5 / 3, **kw)
+    eq = param.equation
+
+    def initial_condition(param, x):
+        t0 = param.timestepping_param.t0
+        return primitive_to_conservative(param.equation, leblanc_exact(param.equation, x, t0))
+
+    left = primitive_to_conservative(eq, (1.0, 0.0, (eq.gamma - 1) * 1e-1))
+    return param, initial_condition, inflow_outflow_1d(left), leblanc_exact
+
+
+def density_wave_1d_exact(equation=None, x=None, t=0.0, amp=0.2, u=1.0, p=1.0):
+    """A smooth periodic density wave on [0, 1]: rho = 1 + amp sin(2 pi (x - u t)), u, p
+    constant (an exact Euler solution)."""
+    x = np.asarray(x, dtype=np.float64)
+    return 1.0 + amp * np.sin(2 * np.pi * (x - u * t)), np.full_like(x, u), np.full_like(x, p)
+
+
+def density_wave_1d(N=3, K=16, T=0.1, **kw):
+    """The periodic density wave on [0, 1] (a smooth test of the Line path)."""
+
+    param = line_param(N, K, 0.0, 1.0, T, **kw)
+
+    def initial_condition(param, x):
+        return primitive_to_conservative(param.equation, density_wave_1d_exact(param.equation, x, 0.0))
+
+    def bc(param, md):
+        from .mesh import uniform_mesh_1d
+        basis = "gauss" if type(param.approximation_basis).__name__ == "GaussCollocation" else "lobatto"
+        return BCData(mapP=uniform_mesh_1d(param.N, md.num_elements, md.xL[0], md.xR[0], basis, periodic=True).mapP)
+
+    return param, initial_condition, bc, density_wave_1d_exact

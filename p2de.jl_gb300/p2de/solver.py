@@ -13,7 +13,7 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import abi
-from .mesh import MeshData, uniform_mesh
+from .mesh import MeshData, uniform_mesh, uniform_mesh_1d
 from .types import (
     BCData,
     DataHistory,
@@ -44,6 +44,7 @@ from .types import (
     HennemannShockCapture,
     ZhangShuLimiter,
     KPP,
+    is_dim1,
     num_components,
 )
 
@@ -87,14 +88,15 @@ class Descriptor:
     keep: tuple
     N: int
     K: int
+    dim1: bool = False
 
     @property
     def Nq(self) -> int:
-        return (self.N + 1) ** 2
+        return self.N + 1 if self.dim1 else (self.N + 1) ** 2
 
     @property
     def Nfp(self) -> int:
-        return 4 * (self.N + 1)
+        return 2 if self.dim1 else 4 * (self.N + 1)
 
 
 def lower_param(param: Param, K: int) -> abi.P2deParam:
@@ -181,7 +183,8 @@ def lower_param(param: Param, K: int) -> abi.P2deParam:
         bound_beta=beta,
         approximation_basis=basis,
         entropyproj_limiter=eproj,
-        equation=abi.EQUATION_KPP if kpp else abi.EQUATION_COMPRESSIBLE_EULER,
+        equation=abi.EQUATION_KPP if kpp else (abi.EQUATION_COMPRESSIBLE_EULER_1D if is_dim1(param.equation)
+                                               else abi.EQUATION_COMPRESSIBLE_EULER),
         reference_semantics=1 if param.reference_semantics else 0,
         precision=abi.PRECISIONS[param.precision],
     )
@@ -191,6 +194,8 @@ def mesh_for(param: Param) -> MeshData:
     """The uniform mesh of initialize_uniform_mesh_data (init.jl:241-252) with the nodes
     of param's basis."""
     basis = "gauss" if isinstance(param.approximation_basis, GaussCollocation) else "lobatto"
+    if is_dim1(param.equation):  # initialize_uniform_mesh_data(::Line) (init.jl:230-239)
+        return uniform_mesh_1d(param.N, int(param.K), float(param.xL), float(param.xR), basis=basis)
     return uniform_mesh(param.N, param.K[0], param.K[1], param.xL, param.xR, basis=basis)
 
 
@@ -199,9 +204,11 @@ def make_descriptor(param: Param, md: MeshData, bc: BCData) -> Descriptor:
     geom = _f64(md.geom)
     mapP = _i64(bc.mapP)
     mapI, mapO, mapW, mapS = _i64(bc.mapI), _i64(bc.mapO), _i64(bc.mapW), _i64(bc.mapS)
-    Ival = _f64(bc.Ival if len(bc.Ival) else np.zeros((0, 4))).reshape(-1, 4)
+    dim1 = is_dim1(param.equation)
+    nc = 3 if dim1 else 4
+    Ival = _f64(bc.Ival if len(bc.Ival) else np.zeros((0, nc))).reshape(-1, nc)
     xyS = _f64(bc.xyS if len(bc.xyS) else np.zeros((0, 2))).reshape(-1, 2)
-    if mapP.size != K * 4 * (param.N + 1):
+    if mapP.size != K * (2 if dim1 else 4 * (param.N + 1)):
         raise ValueError("mapP has the wrong size")
     m = abi.P2deMesh()
     m.geom = abi.dptr(geom)
@@ -219,13 +226,14 @@ def make_descriptor(param: Param, md: MeshData, bc: BCData) -> Descriptor:
         m.shock_post[c] = bc.shock_post[c]
         m.shock_pre[c] = bc.shock_pre[c]
     p = lower_param(param, K)
-    return Descriptor(p, m, (geom, mapP, mapI, mapO, mapW, mapS, Ival, xyS), param.N, K)
+    return Descriptor(p, m, (geom, mapP, mapI, mapO, mapW, mapS, Ival, xyS), param.N, K, dim1)
 
 
 def evaluate_initial_condition(param: Param, md: MeshData, initial_condition) -> np.ndarray:
     """init_U! (init.jl:342-361): Uq[i,k] = initial_condition(param, x, y), vectorised.
-    Returns (K, Nq, 4) float64 (Julia's Uq memory layout)."""
-    u = initial_condition(param, md.x, md.y)
+    Returns (K, Nq, Nc) float64 (Julia's Uq memory layout); on a Line initial_condition(param,
+    x) (set_initial_condition!(::Dim1), init.jl:352-355)."""
+    u = initial_condition(param, md.x) if md.dim1 else initial_condition(param, md.x, md.y)
     if isinstance(u, (tuple, list)):
         u = np.stack([np.broadcast_to(np.asarray(c, dtype=np.float64), md.x.shape) for c in u], axis=-1)
     u = np.ascontiguousarray(np.asarray(u, dtype=np.float64))
@@ -252,8 +260,8 @@ class Solver:
         self.K = desc.K
         self.N = param.N
         self.N1D = param.N + 1
-        self.Nq = self.N1D**2
-        self.Nfp = 4 * self.N1D
+        self.Nq = desc.Nq
+        self.Nfp = desc.Nfp
 
     def close(self):
         if getattr(self, "handle", None):
@@ -423,7 +431,10 @@ def exact_nodal_values(solver: Solver, exact_sol, t: float) -> np.ndarray:
     every node: conservative values in the layout of Uq."""
     from .problems import primitive_to_conservative
 
-    prim = exact_sol(solver.param.equation, solver.md.x, solver.md.y, t)
+    if solver.md.dim1:  # exact_solution(::CompressibleIdealGas{Dim1}) (postprocess.jl:48-52)
+        prim = exact_sol(solver.param.equation, solver.md.x, t)
+    else:
+        prim = exact_sol(solver.param.equation, solver.md.x, solver.md.y, t)
     return np.ascontiguousarray(primitive_to_conservative(solver.param.equation, prim), dtype=np.float64)
 
 

@@ -21,10 +21,15 @@ class Dim2:
 
 @dataclass(frozen=True)
 class CompressibleEulerIdealGas:
-    """CompressibleEulerIdealGas{Dim2}(gamma)."""
+    """CompressibleEulerIdealGas{Dim2}(gamma); dim=Dim1 for CompressibleEulerIdealGas{Dim1}."""
 
     gamma: float = 1.4
     dim: type = Dim2
+
+
+def is_dim1(equation) -> bool:
+    """dim(equation) isa Dim1 (src/common/traits.jl:133-139)."""
+    return getattr(equation, "dim", Dim2) is Dim1
 
 
 @dataclass(frozen=True)
@@ -213,12 +218,15 @@ class Param:
 
 
 def num_elements(param: Param) -> int:
-    return param.K[0] * param.K[1]
+    """num_elements (src/common/traits.jl:162-171): K on a Line, K[0] K[1] on quads."""
+    return int(param.K) if np.isscalar(param.K) else param.K[0] * param.K[1]
 
 
 def num_components(equation=None) -> int:
     """num_components (src/common/traits.jl:145-155)."""
-    return 1 if isinstance(equation, KPP) else 4
+    if isinstance(equation, KPP):
+        return 1
+    return 3 if is_dim1(equation) else 4
 
 
 # --- boundary data and time parameters ------------------------------------------------

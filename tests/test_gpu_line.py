@@ -1,0 +1,193 @@
+"""GPU parity of CompressibleEulerIdealGas{Dim1} (the Line path) against the FP64 oracle.
+
+The reference's own Dim1 path raises before its first RHS (Bx(::Dim1) passes its arguments
+to reference_to_physical in the wrong order, rhs_utils.jl:18), so both sides run the Dim1
+methods with their evident meaning (reference_semantics = False): the RHS of rhs.jl:183-213
+on LGL and Gauss nodes (NodewiseScaledExtrapolation), the subcell limiter's Dim1 methods
+(subcell.jl:144-246, 405-415, 468-628, 826-892) for every bound, Zhang-Shu, Hennemann shock
+capture, periodic / inflow / outflow faces, and the examples' configurations
+(examples/1D/shu-osher.jl, examples/convergence/leblanc-convergence.jl).
+
+Both sides evaluate a*b+c as two rounded operations in the same order (the Line kernels are
+compiled with -fmad=false), so single RHS evaluations agree to the last bits of log, exp and
+pow, and runs to where a limiter decision turns on those bits.
+"""
+import numpy as np
+import pytest
+
+import p2de
+from p2de import abi, problems
+from p2de import solver as S
+from p2de.types import (
+    EntropyStable,
+    ESLimitedLowOrderPos,
+    GaussCollocation,
+    HennemannShockCapture,
+    LaxFriedrichsOnProjectedVal,
+    LobattoCollocation,
+    LowOrderPositivity,
+    NodewiseScaledExtrapolation,
+    NoEntropyProjectionLimiter,
+    PositivityAndCellEntropyBound,
+    PositivityAndMinEntropyBound,
+    PositivityAndRelaxedCellEntropyBound,
+    PositivityAndRelaxedMinEntropyBound,
+    PositivityBound,
+    SubcellLimiter,
+    TVDAndCellEntropyBound,
+    TVDAndMinEntropyBound,
+    TVDBound,
+    ZhangShuLimiter,
+)
+
+from conftest import relerr
+from helpers import setup
+from test_gpu_parity import TOL, gpu_for, oracle_for
+
+pytestmark = pytest.mark.gpu
+
+TOL_RUN = 1e-9
+
+LIMITERS = {
+    "pos": SubcellLimiter(bound=PositivityBound()),
+    "cell": SubcellLimiter(bound=PositivityAndCellEntropyBound()),
+    "relaxed-cell": SubcellLimiter(bound=PositivityAndRelaxedCellEntropyBound(beta=0.5)),
+    "minent": SubcellLimiter(bound=PositivityAndMinEntropyBound()),
+    "relaxed-minent": SubcellLimiter(bound=PositivityAndRelaxedMinEntropyBound()),
+    "tvd": SubcellLimiter(bound=TVDBound()),
+    "tvd-cell": SubcellLimiter(bound=TVDAndCellEntropyBound()),
+    "tvd-minent": SubcellLimiter(bound=TVDAndMinEntropyBound()),
+    "pos+hennemann": SubcellLimiter(bound=PositivityBound(), shockcapture=HennemannShockCapture()),
+    "zhang-shu": ZhangShuLimiter(),
+    "zhang-shu+hennemann": ZhangShuLimiter(shockcapture=HennemannShockCapture()),
+}
+CELL = ("cell", "relaxed-cell", "tvd-cell")
+
+
+def basis_kw(basis):
+    if basis == "gauss":
+        return dict(approximation_basis=GaussCollocation(), entropyproj_limiter=NodewiseScaledExtrapolation())
+    return dict(approximation_basis=LobattoCollocation(), entropyproj_limiter=NoEntropyProjectionLimiter())
+
+
+def compare_line_rhs(param, md, desc, U0, t, dt, nstage, tol=TOL):
+    o = oracle_for(desc, U0)
+    g = gpu_for(param, md, desc, U0)
+    dto = o.rhs(t, dt, nstage)
+    dtg = S.rhs_bang(None, g, None, p2de.TimeParam(t, dt, nstage))
+    assert abs(dtg - dto) <= 1e-13 * abs(dto), (dtg, dto)
+    fields = [abi.FIELD_RHSU, abi.FIELD_RHSL, abi.FIELD_RHSH, abi.FIELD_BF_L, abi.FIELD_BF_H]
+    if not isinstance(param.rhs, ESLimitedLowOrderPos):
+        fields = [abi.FIELD_RHSU]
+    for f in fields:
+        a, b = g.get_field(f), o.get_field(f)
+        assert a.size == b.size == g.field_count(f)
+        assert relerr(a, b, floor=1e-300) <= tol, (f, relerr(a, b, floor=1e-300))
+    th_g, th_o = g.get_field(abi.FIELD_THETA_LOCAL, nstage), o.get_field(abi.FIELD_THETA_LOCAL, nstage)
+    np.testing.assert_allclose(th_g, th_o, rtol=0, atol=1e-15)
+    lim = param.rhs_limiter
+    if isinstance(param.rhs, ESLimitedLowOrderPos) and isinstance(lim, SubcellLimiter):
+        n1 = param.N + 1
+        Lg = g.get_field(abi.FIELD_L_LOCAL, nstage).reshape(desc.K, 2 * n1)[:, : n1 + 1]
+        Lo = o.get_field(abi.FIELD_L_LOCAL, nstage).reshape(desc.K, 2 * n1)[:, : n1 + 1]
+        assert np.all((Lg >= 0) & (Lg <= 1))
+        np.testing.assert_allclose(Lg, Lo, rtol=0, atol=1e-12)
+    if isinstance(lim, ZhangShuLimiter):
+        np.testing.assert_allclose(g.get_field(abi.FIELD_L, nstage), o.get_field(abi.FIELD_L, nstage), atol=1e-12)
+    g.close()
+    o.close()
+
+
+@pytest.mark.parametrize("basis", ["lobatto", "gauss"])
+@pytest.mark.parametrize("limiter", list(LIMITERS))
+@pytest.mark.parametrize("problem", ["density-wave", "leblanc"])
+def test_line_rhs(basis, limiter, problem):
+    if basis == "gauss" and limiter in CELL:
+        pytest.skip("no cell-entropy bound on Gauss nodes in 1D (no Dim1 interface method)")
+    kw = dict(rhs_limiter=LIMITERS[limiter], **basis_kw(basis))
+    if problem == "density-wave":
+        param, md, bc, desc, U0 = setup(problems.density_wave_1d, N=3, K=12, T=0.1, **kw)
+        t0 = 0.0
+    else:
+        param, md, bc, desc, U0 = setup(problems.leblanc, N=2, K=40, **kw)
+        t0 = param.timestepping_param.t0
+    for nstage in (1, 2):
+        compare_line_rhs(param, md, desc, U0, t0, 1e-3, nstage)
+
+
+@pytest.mark.parametrize("N", [1, 2, 3, 4, 5])
+@pytest.mark.parametrize("basis", ["lobatto", "gauss"])
+def test_line_rhs_degrees(N, basis):
+    param, md, bc, desc, U0 = setup(problems.shu_osher, N=N, K=24, **basis_kw(basis))
+    compare_line_rhs(param, md, desc, U0, 0.0, 1e-4, 1)
+
+
+@pytest.mark.parametrize("rhs", ["low", "es", "lfproj"])
+@pytest.mark.parametrize("basis", ["lobatto", "gauss"])
+def test_line_rhs_types(rhs, basis):
+    r = {"low": LowOrderPositivity(), "es": EntropyStable(),
+         "lfproj": ESLimitedLowOrderPos(low_order_surface_flux=LaxFriedrichsOnProjectedVal())}[rhs]
+    param, md, bc, desc, U0 = setup(problems.leblanc, N=3, K=30, rhs=r, **basis_kw(basis))
+    compare_line_rhs(param, md, desc, U0, param.timestepping_param.t0, 1e-3, 1)
+
+
+@pytest.mark.parametrize("limiter", ["pos", "minent", "tvd", "cell", "zhang-shu+hennemann"])
+@pytest.mark.parametrize("basis", ["lobatto", "gauss"])
+def test_line_steps(limiter, basis):
+    if basis == "gauss" and limiter in CELL:
+        pytest.skip("no cell-entropy bound on Gauss nodes in 1D")
+    param, md, bc, desc, U0 = setup(problems.leblanc, N=2, K=50, T=0.05, rhs_limiter=LIMITERS[limiter],
+                                    **basis_kw(basis))
+    o = oracle_for(desc, U0)
+    g = gpu_for(param, md, desc, U0)
+    to = tg = param.timestepping_param.t0
+    for _ in range(20):
+        to, dto = o.step(to)
+        tg, dtg = S.ssp33_step(g, tg)
+        assert abs(dtg - dto) <= 1e-12 * dto
+    assert relerr(g.get_field(abi.FIELD_UQ), o.get_field(abi.FIELD_UQ)) <= TOL_RUN
+    U = g.get_field(abi.FIELD_UQ).reshape(-1, 3)
+    assert U[:, 0].min() > 0 and (U[:, 2] - 0.5 * U[:, 1] ** 2 / U[:, 0]).min() > 0
+    g.close()
+    o.close()
+
+
+@pytest.mark.parametrize("basis", ["lobatto", "gauss"])
+def test_line_periodic_conservation(basis):
+    param, md, bc, desc, U0 = setup(problems.density_wave_1d, N=4, K=16, T=0.05,
+                                    rhs_limiter=LIMITERS["pos"], **basis_kw(basis))
+    g = gpu_for(param, md, desc, U0)
+    before = S.conservation_totals(g)
+    t, n, _ = S.ssp33(g)
+    after = S.conservation_totals(g)
+    assert abs(t - 0.05) < 1e-14 and n > 10
+    np.testing.assert_allclose(after, before, rtol=0, atol=1e-13)
+    assert after[3] == 0.0  # (rho, rhou, E) and a zero slot
+    g.close()
+
+
+def test_shu_osher_example_run():
+    """examples/1D/shu-osher.jl's configuration (Gauss, NodewiseScaledExtrapolation,
+    PositivityBound, dt0 1e-4) to T = 0.1: 2001 steps."""
+    param, md, bc, desc, U0 = setup(problems.shu_osher, T=0.1)
+    o = oracle_for(desc, U0)
+    to, no, _ = o.run()
+    g = gpu_for(param, md, desc, U0)
+    tg, ng, _ = S.ssp33(g)
+    assert ng == no and abs(tg - to) <= 1e-12
+    assert relerr(g.get_field(abi.FIELD_UQ), o.get_field(abi.FIELD_UQ)) <= TOL_RUN
+    th = g.get_field(abi.FIELD_THETA_LOCAL, 3)
+    assert th.min() < 1.0  # the projection limiter is active at the shock
+    g.close()
+    o.close()
+
+
+def test_line_error_against_exact():
+    """calculate_error on the device for the Line state against the density wave."""
+    param, md, bc, desc, U0 = setup(problems.density_wave_1d, N=3, K=16, T=0.02,
+                                    rhs_limiter=LIMITERS["pos"])
+    g = gpu_for(param, md, desc, U0)
+    S.ssp33(g)
+    err = S.calculate_error(None, g, problems.density_wave_1d_exact)
+    assert 0 < err.L1err < 1e-5 and err.L2err < 1e-5 and err.Linferr < 1e-4
+    g.close()

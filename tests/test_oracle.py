@@ -563,3 +563,70 @@ def test_oracle_matches_golden(name):
     np.testing.assert_allclose(o.get_field(abi.FIELD_L_LOCAL), ref["L_local"], atol=1e-13)
     o.step(0.0)
     assert relerr(o.get_field(abi.FIELD_UQ), ref["step_Uq"]) <= 1e-13
+
+
+# --- CompressibleEulerIdealGas{Dim1} (the Line path) ----------------------------------
+def _line(problem, **kw):
+    from oracle.binding import Oracle
+
+    param, md, bc, desc, U0 = setup(problem, **kw)
+    o = Oracle(desc, nthreads=2)
+    o.set_Uq(U0)
+    return param, md, desc, U0, o
+
+
+@pytest.mark.parametrize("basis", ["lobatto", "gauss"])
+def test_line_density_wave_conserves_and_converges(basis):
+    """The periodic density wave: totals kept to rounding, and the error falls at about
+    order N+1 with the element size (positivity bound, inactive on smooth data)."""
+    from p2de.types import GaussCollocation, NodewiseScaledExtrapolation, PositivityBound, SubcellLimiter
+
+    kw = dict(approximation_basis=GaussCollocation(), entropyproj_limiter=NodewiseScaledExtrapolation()) \
+        if basis == "gauss" else {}
+    errs = []
+    for K in (8, 16):
+        param, md, desc, U0, o = _line(problems.density_wave_1d, N=3, K=K, T=0.1,
+                                       rhs_limiter=SubcellLimiter(bound=PositivityBound()), **kw)
+        w = np.asarray(o.operator(7))[None, :] * md.geom[:, :1]
+        tot0 = (U0 * w[..., None]).sum((0, 1))
+        t, n, _ = o.run()
+        U = o.get_field(0).reshape(K, -1, 3)
+        np.testing.assert_allclose((U * w[..., None]).sum((0, 1)), tot0, rtol=0, atol=1e-13)
+        ex = problems.primitive_to_conservative(param.equation, problems.density_wave_1d_exact(None, md.x, t))
+        errs.append(np.abs(U - ex).max())
+        o.close()
+    assert errs[1] < errs[0] / 8, errs
+
+
+def test_line_free_stream_and_positivity():
+    """A constant state stays constant (to rounding) through every bound; Leblanc's shock
+    tube keeps positive density and internal energy."""
+    from p2de.types import PositivityAndCellEntropyBound, PositivityAndMinEntropyBound, SubcellLimiter, TVDBound
+
+    for bound in (PositivityAndCellEntropyBound(), PositivityAndMinEntropyBound(), TVDBound()):
+        param, md, desc, U0, o = _line(problems.density_wave_1d, N=2, K=8, T=0.05,
+                                       rhs_limiter=SubcellLimiter(bound=bound))
+        U1 = np.broadcast_to(np.array([1.0, 0.5, 2.5]), U0.shape).copy()
+        o.set_Uq(U1)
+        o.run()
+        np.testing.assert_allclose(o.get_field(0).reshape(U0.shape), U1, rtol=0, atol=1e-13)
+        o.close()
+    param, md, desc, U0, o = _line(problems.leblanc, N=3, K=40, T=0.1)
+    o.run()
+    U = o.get_field(0).reshape(-1, 3)
+    assert U[:, 0].min() > 0 and (U[:, 2] - 0.5 * U[:, 1] ** 2 / U[:, 0]).min() > 0
+    o.close()
+
+
+def test_line_reference_semantics_refused():
+    """The reference's Dim1 RHS raises (rhs_utils.jl:18): reference_semantics = 1 is refused
+    by the oracle and by the library before any device work."""
+    from ctypes import byref, c_void_p
+
+    param, md, bc, desc, U0 = setup(problems.density_wave_1d, N=2, K=4, T=0.1)
+    desc.param.reference_semantics = 1
+    with pytest.raises(RuntimeError, match="status 2"):
+        Oracle(desc)
+    lib = abi.load_library()
+    h = c_void_p()
+    assert lib.p2de_initialize_DG(byref(desc.param), byref(desc.mesh), 0, byref(h)) == 2  # P2DE_ERR_UNSUPPORTED
