@@ -257,10 +257,17 @@ __device__ void smoothness(const LineArgs& a, const double (*U)[4], double& blen
 }
 
 // ---- kernels ----------------------------------------------------------------------------
-// step begin: the stage's dt key, the per-stage minima, the initial min of phi
-__global__ void k_line_begin(LineArgs a, double dt, int reset_min, int reset_phi) {
+// stage begin. dtkey[0]: the step's dt (lowered by the stage-1 CFL), dtkey[1]: the stage's
+// TimeParam dt, which the limiter reads (at stage 1 the dt before the CFL, rhs.jl:41-55 with
+// SSPRK33.jl:30-37). mode 0: both set to (dt, dt_lim); mode 1: dtkey[1] = dtkey[0].
+__global__ void k_line_begin(LineArgs a, int mode, double dt, double dt_lim, int reset_min, int reset_phi) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  *a.dtkey = (unsigned long long)__double_as_longlong(dt);
+  if (mode == 0) {
+    a.dtkey[0] = (unsigned long long)__double_as_longlong(dt);
+    a.dtkey[1] = (unsigned long long)__double_as_longlong(dt_lim);
+  } else {
+    a.dtkey[1] = a.dtkey[0];
+  }
   if (reset_min)
     for (int i = 0; i < 6; ++i) a.minrec[i] = encode_key(INFINITY);
   if (reset_phi) *a.phikey = encode_key(INFINITY);
@@ -423,7 +430,7 @@ __global__ void k_line_low(LineArgs a) {
       dtl = jmin(dtl, a.CFL * 0.5 * wJq / li);
     }
     if (dtl > 0.0)
-      atomicMin(a.dtkey, (unsigned long long)__double_as_longlong(dtl));
+      atomicMin(&a.dtkey[0], (unsigned long long)__double_as_longlong(dtl));
     else
       atomicOr(a.status, ST_BAD_DT);
   }
@@ -449,7 +456,7 @@ __global__ void k_line_high(LineArgs a) {
   const LineOps& o = *a.ops;
   const double* g = a.geom + 5 * (size_t)k;
   const double J = g[0];
-  const double dt = __longlong_as_double((long long)*a.dtkey);
+  const double dt = __longlong_as_double((long long)a.dtkey[1]);  // the limiter's TimeParam dt
   double U[MQ][4], ut[MH][4], beta[MH], rl[MH], bl[MH], QF[MH][4];
   for (int i = 0; i < n; ++i) {
     ld4(a.Uq + 4 * ((size_t)n * k + i), U[i]);
@@ -747,7 +754,7 @@ __global__ void k_line_update(LineArgs a) {
     }
   }
   if (!(a.flags & LF_UPDATE)) return;
-  const double dt = __longlong_as_double((long long)*a.dtkey);
+  const double dt = __longlong_as_double((long long)a.dtkey[0]);  // the step's dt
   double rmin = INFINITY, emin = INFINITY;
   int bad = 0;
   for (int i = 0; i < n; ++i) {
@@ -881,15 +888,18 @@ cudaError_t launch_stage(LineSolve* L, double t, int nstage, double dt_set, bool
   LineArgs a = args_of(L, nstage, flags);
   const int grid = (L->K + kThreads - 1) / kThreads;
   const bool phimin = (flags & LF_MINENT) && t == L->prm.t0 && nstage == 1;
-  const bool begin = nstage == 1 || !update;
-  if (begin) {
-    // a step starts from min(CFL dt0, T - t) (SSPRK33.jl:125-127), which the stage-1 CFL of a
-    // low-order RHS lowers; a lone RHS keeps the dt it is given unless it sets the CFL
-    const bool initial = (nstage == 1 && update) || (flags & LF_CFL);
-    const double dt0 = initial ? host_jmin(L->prm.CFL * L->prm.dt0, L->prm.T - t) : dt_set;
-    k_line_begin<<<1, 32, 0, L->stream>>>(a, dt0, nstage == 1 ? 1 : 0, phimin ? 1 : 0);
-    L->launches += 1;
+  // a step starts from dt = min(CFL dt0, T - t) (SSPRK33.jl:30-32), which the stage-1 CFL of
+  // a low-order RHS lowers for the update; the limiter reads the TimeParam dt. A lone RHS
+  // takes the dt it is given, except for the CFL's starting value.
+  if (nstage == 1 || !update) {
+    const double dinit = host_jmin(L->prm.CFL * L->prm.dt0, L->prm.T - t);
+    const double dlim = update ? dinit : dt_set;
+    const double dkey = (flags & LF_CFL) ? dinit : dlim;
+    k_line_begin<<<1, 32, 0, L->stream>>>(a, 0, dkey, dlim, nstage == 1 ? 1 : 0, phimin ? 1 : 0);
+  } else {
+    k_line_begin<<<1, 32, 0, L->stream>>>(a, 1, 0.0, 0.0, 0, 0);
   }
+  L->launches += 1;
   k_line_face<<<grid, kThreads, 0, L->stream>>>(a);
   L->launches += 1;
   if (flags & LF_LOW) {
@@ -1028,7 +1038,7 @@ int line_create(const p2de_param* prm, const p2de_mesh* mesh, cudaStream_t st, L
   A(&L->nbr, (size_t)nfk);
   A(&L->bcidx, (size_t)nfk);
   A(&L->bc, (size_t)nfk);
-  A(&L->dtkey, 1);
+  A(&L->dtkey, 2);
   A(&L->minrec, 6);
   A(&L->status, 1);
   A(&L->ops, 1);
@@ -1186,7 +1196,7 @@ int line_step_launches(const LineSolve* L) {
   int c = 0;
   for (int stage = 1; stage <= 3; ++stage) {
     const int f = line_flags(L, stage, true);
-    c += (stage == 1 ? 1 : 0) + 1 + ((f & LF_LOW) ? 1 : 0) + ((f & LF_HIGH) ? 1 : 0) + 1;
+    c += 1 + 1 + ((f & LF_LOW) ? 1 : 0) + ((f & LF_HIGH) ? 1 : 0) + 1;
   }
   return c;
 }

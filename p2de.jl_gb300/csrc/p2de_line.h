@@ -29,7 +29,7 @@ struct LineSolve {
   double *geom = nullptr, *Ival = nullptr, *phimin = nullptr;
   int32_t *nbr = nullptr, *bcidx = nullptr;
   int8_t* bc = nullptr;
-  unsigned long long* dtkey = nullptr;  // bits of the stage's dt (positive: ordered)
+  unsigned long long* dtkey = nullptr;  // bits of the step's dt (positive: ordered) and of the limiter's dt
   long long* minrec = nullptr;          // min rho, min rhoe per stage (ordered keys)
   int* status = nullptr;
   LineOps* ops = nullptr;

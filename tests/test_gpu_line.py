@@ -47,6 +47,12 @@ from test_gpu_parity import TOL, gpu_for, oracle_for
 pytestmark = pytest.mark.gpu
 
 TOL_RUN = 1e-9
+# The smooth density wave is ill-conditioned in the reference's own arithmetic: its node
+# pairs put the log mean (compressible_Navier_Stokes.jl:307-321) just past the 1e-4
+# threshold of its series, where -da / (log aL - log aR) magnifies one ulp of a log by
+# 1e4. Perturbing the state by two ulps moves the oracle's own rhsU by up to 2.4e-11 (LGL)
+# and 9.3e-11 (Gauss); Leblanc's and Shu-Osher's states move it by at most 2e-14.
+TOL_WAVE = 1e-9
 
 LIMITERS = {
     "pos": SubcellLimiter(bound=PositivityBound()),
@@ -76,7 +82,7 @@ def compare_line_rhs(param, md, desc, U0, t, dt, nstage, tol=TOL):
     dto = o.rhs(t, dt, nstage)
     dtg = S.rhs_bang(None, g, None, p2de.TimeParam(t, dt, nstage))
     assert abs(dtg - dto) <= 1e-13 * abs(dto), (dtg, dto)
-    fields = [abi.FIELD_RHSU, abi.FIELD_RHSL, abi.FIELD_RHSH, abi.FIELD_BF_L, abi.FIELD_BF_H]
+    fields = [abi.FIELD_RHSL, abi.FIELD_RHSH, abi.FIELD_BF_L, abi.FIELD_BF_H, abi.FIELD_RHSU]
     if not isinstance(param.rhs, ESLimitedLowOrderPos):
         fields = [abi.FIELD_RHSU]
     for f in fields:
@@ -91,9 +97,25 @@ def compare_line_rhs(param, md, desc, U0, t, dt, nstage, tol=TOL):
         Lg = g.get_field(abi.FIELD_L_LOCAL, nstage).reshape(desc.K, 2 * n1)[:, : n1 + 1]
         Lo = o.get_field(abi.FIELD_L_LOCAL, nstage).reshape(desc.K, 2 * n1)[:, : n1 + 1]
         assert np.all((Lg >= 0) & (Lg <= 1))
-        np.testing.assert_allclose(Lg, Lo, rtol=0, atol=1e-12)
+        # A factor is a decision when the subcell flux difference it limits is at the
+        # rounding level (e.g. a TVD bound met with equality at a smooth extremum): one ulp
+        # of the state flips it between 0 and 1 there, while its product with that
+        # difference (rhsU, compared above) stays put. The factors that move when the
+        # oracle's own input moves by two ulps are left out; the rest must agree.
+        unstable = np.zeros(Lo.shape, dtype=bool)
+        rng = np.random.default_rng(1)
+        for _ in range(4):
+            o.set_Uq(U0 * (1 + 2.2e-16 * rng.integers(-2, 3, np.shape(U0))))
+            o.rhs(t, dt, nstage)
+            Lp = o.get_field(abi.FIELD_L_LOCAL, nstage).reshape(desc.K, 2 * n1)[:, : n1 + 1]
+            unstable |= np.abs(Lp - Lo) > max(tol, 1e-12)
+        # (TVD bounds in Leblanc's flat states are met with equality in about one factor in
+        # eight; the smooth wave has two such faces in sixty)
+        assert unstable.sum() <= 0.5 * unstable.size
+        np.testing.assert_allclose(Lg[~unstable], Lo[~unstable], rtol=0, atol=max(tol, 1e-12))
     if isinstance(lim, ZhangShuLimiter):
-        np.testing.assert_allclose(g.get_field(abi.FIELD_L, nstage), o.get_field(abi.FIELD_L, nstage), atol=1e-12)
+        np.testing.assert_allclose(g.get_field(abi.FIELD_L, nstage), o.get_field(abi.FIELD_L, nstage),
+                                   atol=max(tol, 1e-12))
     g.close()
     o.close()
 
@@ -107,12 +129,12 @@ def test_line_rhs(basis, limiter, problem):
     kw = dict(rhs_limiter=LIMITERS[limiter], **basis_kw(basis))
     if problem == "density-wave":
         param, md, bc, desc, U0 = setup(problems.density_wave_1d, N=3, K=12, T=0.1, **kw)
-        t0 = 0.0
+        t0, tol = 0.0, TOL_WAVE
     else:
         param, md, bc, desc, U0 = setup(problems.leblanc, N=2, K=40, **kw)
-        t0 = param.timestepping_param.t0
+        t0, tol = param.timestepping_param.t0, TOL
     for nstage in (1, 2):
-        compare_line_rhs(param, md, desc, U0, t0, 1e-3, nstage)
+        compare_line_rhs(param, md, desc, U0, t0, 1e-3, nstage, tol=tol)
 
 
 @pytest.mark.parametrize("N", [1, 2, 3, 4, 5])
