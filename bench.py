@@ -77,7 +77,7 @@ def build_descriptor(param, ic, bcf):
     import p2de
     from p2de import solver as S
 
-    md = p2de.uniform_mesh(param.N, *param.K, param.xL, param.xR)
+    md = S.mesh_for(param)  # the nodes of param's basis; a Line mesh for 1D Euler
     bc = bcf(param, md)
     desc = S.make_descriptor(param, md, bc)
     U0 = S.evaluate_initial_condition(param, md, ic)
@@ -564,6 +564,40 @@ def run_limiter_report(args):
                       "data": "synthetic", "report": res}), flush=True)
 
 
+def run_line_report(args):
+    """1D Euler (the Line path, CompressibleEulerIdealGas{Dim1}) on the reference's 1D
+    configurations and on a long line: GPU seconds per SSP-RK3 step (CUDA events around the
+    host-driven steps, so launch gaps and the per-step dt read-back are included) against
+    the FP64 oracle on every host core for the same workload."""
+    import torch
+
+    from p2de import problems
+    from p2de.types import LobattoCollocation, NoEntropyProjectionLimiter
+
+    torch.cuda.set_device(0)
+    lgl = dict(approximation_basis=LobattoCollocation(), entropyproj_limiter=NoEntropyProjectionLimiter())
+    cases = {
+        "shu-osher K=64 N=3 (examples/1D/shu-osher.jl: Gauss, scaled extrapolation, positivity)":
+            (problems.shu_osher, dict(N=3, K=64, T=1.8)),
+        "leblanc K=400 N=5 (leblanc-convergence.jl's largest: LGL, positivity)":
+            (problems.leblanc, dict(N=5, K=400, **lgl)),
+        "shu-osher K=131072 N=3 (a long line)": (problems.shu_osher, dict(N=3, K=131072, T=1.8)),
+    }
+    res = {}
+    for name, (prob, kw) in cases.items():
+        param, ic, bcf = prob(**kw)[:3]
+        md, bc, desc, U0 = build_descriptor(param, ic, bcf)
+        steps = min(args.steps, 200)
+        sec, U, n = _timed_alone(param, md, desc, U0, args.warmup, steps, tune=False)
+        dofs = desc.K * desc.Nq
+        cpu = cpu_baseline(desc, U0, dofs, budget_s=4.0)
+        res[name] = {"gpu_dof_stage_per_s": dofs * 3 * n / sec, "gpu_ms_per_step": 1e3 * sec / n, "steps": n,
+                     "cpu": cpu, "gpu_over_cpu": (dofs * 3 * n / sec) / cpu["value"],
+                     "min_rho": float(np.reshape(U, (-1, 3))[:, 0].min())}
+    print(json.dumps({"metric": METRIC, "unit": UNIT, "workload": "1D Euler (Line path), FP64",
+                      "data": "synthetic", "report": res}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -571,7 +605,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="dmr",
-                    choices=["dmr", "kh256", "batch64", "serve", "mixed-report", "limiter-report"])
+                    choices=["dmr", "kh256", "batch64", "serve", "mixed-report", "limiter-report", "line-report"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed", "mixed-acc64"])
     ap.add_argument("--basis", default="lobatto", choices=["lobatto", "gauss"],
                     help="gauss: the DMR step with GaussCollocation + NodewiseScaledExtrapolation")
@@ -598,6 +632,8 @@ def main():
         return run_serve(args)
     if args.workload == "mixed-report":
         return run_mixed_report(args)
+    if args.workload == "line-report":
+        return run_line_report(args)
     if args.workload == "limiter-report":
         return run_limiter_report(args)
 
