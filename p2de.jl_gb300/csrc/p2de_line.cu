@@ -45,7 +45,10 @@ enum : int {
   LF_UPDATE = 1 << 14,     // RK stage update of Uq
 };
 
-constexpr int kThreads = 128;
+// One warp per block: a block's warps share their SM's FP64 pipe, which issues a warp
+// instruction in the same time however many lanes it carries, so a small solve is fastest
+// with its elements spread one warp per SM (32-thread blocks still fill an SM at large K).
+constexpr int kThreads = 32;
 constexpr int MQ = kMaxN1D;     // nodes per element at most
 constexpr int MH = kLineMaxNh;  // nodes + face nodes
 constexpr int MS = 2 * kMaxN1D; // rows of L_local
@@ -53,7 +56,7 @@ constexpr int MS = 2 * kMaxN1D; // rows of L_local
 struct LineArgs {
   int K, N1D, nstage, flags;
   const LineOps* ops;
-  double *Uq, *resW, *rhsL, *rhsH, *rhsU, *BFL, *BFH, *uf, *theta, *Lloc, *Lraw, *fbar, *Lelem;
+  double *Uq, *resW, *rhsL, *rhsH, *rhsU, *BFL, *BFH, *uf, *theta, *Lloc, *Lraw, *fbar, *Lelem, *sf;
   const double *geom, *Ival;
   long long* phikey;
   const int32_t *nbr, *bcidx;
@@ -274,10 +277,12 @@ __global__ void k_line_begin(LineArgs a, int mode, double dt, double dt_lim, int
 }
 
 // entropy_projection! (rhs.jl:59-133) with solve_theta!(::NodewiseScaledExtrapolation)
-// (filter.jl:6-62, 91-130) on Gauss nodes: theta_local and the projected face states
+// (filter.jl:6-62, 91-130) on Gauss nodes: theta_local and the projected face states. One
+// thread per face node (the two bisections of an element run side by side).
 __global__ void k_line_face(LineArgs a) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= a.K) return;
+  const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= 2LL * a.K) return;
+  const int k = (int)(g / 2), f = (int)(g % 2);
   const int n = a.N1D, N = n - 1, s = a.nstage - 1;
   const LineOps& o = *a.ops;
   double U[MQ][4], v[MQ][4];
@@ -285,7 +290,7 @@ __global__ void k_line_face(LineArgs a) {
     ld4(a.Uq + 4 * ((size_t)n * k + i), U[i]);
     v_ufun4(a.gamma, U[i], v[i]);
   }
-  for (int f = 0; f < 2; ++f) {
+  {
     const int fn = f == 0 ? 0 : N;
     auto face_var = [&](double th, double* acc) {
       for (int c = 0; c < 4; ++c) acc[c] = 0.0;
@@ -445,6 +450,37 @@ __global__ void k_line_phimin(LineArgs a) {
   atomicMin(a.phikey, encode_key(s_modified4(a.gamma, U)));
 }
 
+// the volume two-point terms S_ij fS(u_i, u_j) of flux_differencing_volume!
+// (flux_differencing.jl:164-211), one thread per (element, nonzero pair of Srh_db), with
+// beta and the logs of each state evaluated as k_line_high evaluates them
+__global__ void k_line_pairs(LineArgs a) {
+  const LineOps& o = *a.ops;
+  const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= (long long)a.K * o.npair) return;
+  const int k = (int)(g / o.npair), p = (int)(g % o.npair);
+  const int n = a.N1D, Nh = n + 2;
+  const int i = o.pi[p], j = o.pj[p];
+  auto state = [&](int h, double* u) {
+    if (h < n)
+      ld4(a.Uq + 4 * ((size_t)n * k + h), u);
+    else
+      ld4(a.uf + 4 * (2 * (size_t)k + (h - n)), u);
+  };
+  double ui[4], uj[4];
+  state(i, ui);
+  state(j, uj);
+  const double bi = betafun4(a.gamma, ui), bj = betafun4(a.gamma, uj);
+  const double Ui[6] = {ui[0], ui[1] / ui[0], ui[2] / ui[0], bi, log(ui[0]), log(bi)};
+  const double Uj[6] = {uj[0], uj[1] / uj[0], uj[2] / uj[0], bj, log(uj[0]), log(bj)};
+  const double* gg = a.geom + 5 * (size_t)k;
+  const double Sr = o.Sh[i + Nh * j], Ss = 0.0;
+  const double S0 = gg[1] * Sr + gg[2] * Ss;
+  double F[4];
+  fS4(a.gamma, Ui, Uj, F);
+  double* out = a.sf + (size_t)4 * (kLineMaxPairs * (size_t)k + p);
+  for (int c = 0; c < 4; ++c) out[c] = S0 * F[c];
+}
+
 // rhs_fluxdiff! (flux_differencing.jl:4-37, 331-361) and the limiter's per-element part:
 // Zhang-Shu (zhangshu.jl:4-45) or the subcell factors before symmetrization (subcell.jl:
 // Dim1 methods of accumulate_f_bar!, initialize_lower_bound!, initialize_TVD_bounds!,
@@ -457,18 +493,14 @@ __global__ void k_line_high(LineArgs a) {
   const double* g = a.geom + 5 * (size_t)k;
   const double J = g[0];
   const double dt = __longlong_as_double((long long)a.dtkey[1]);  // the limiter's TimeParam dt
-  double U[MQ][4], ut[MH][4], beta[MH], rl[MH], bl[MH], QF[MH][4];
+  double U[MQ][4], ut[MH][4], QF[MH][4];
   for (int i = 0; i < n; ++i) {
     ld4(a.Uq + 4 * ((size_t)n * k + i), U[i]);
     ld4(U[i], ut[i]);
   }
   for (int f = 0; f < 2; ++f) ld4(a.uf + 4 * (2 * (size_t)k + f), ut[n + f]);
-  for (int h = 0; h < Nh; ++h) {
-    beta[h] = betafun4(a.gamma, ut[h]);
-    rl[h] = log(ut[h][0]);
-    bl[h] = log(beta[h]);
+  for (int h = 0; h < Nh; ++h)
     for (int c = 0; c < 4; ++c) QF[h][c] = 0.0;
-  }
   // exterior states, interface dissipation coefficients and BCs (:39-151)
   // (the exterior beta and logs of :56-70 enter no flux of this path: the surface flux is
   // LaxFriedrichsOnProjectedVal of the exterior state itself)
@@ -494,17 +526,13 @@ __global__ void k_line_high(LineArgs a) {
       }
     }
   }
-  // flux_differencing_volume! (:164-211) over the nonzero pairs of Srh_db
+  // flux_differencing_volume! (:164-211): the pair terms S F of k_line_pairs, accumulated
+  // in pair order
+  const double* SFk = a.sf + (size_t)4 * kLineMaxPairs * k;
   for (int p = 0; p < o.npair; ++p) {
     const int i = o.pi[p], j = o.pj[p];
-    const double Sr = o.Sh[i + Nh * j], Ss = 0.0;
-    const double S0 = g[1] * Sr + g[2] * Ss;
-    const double Ui[6] = {ut[i][0], ut[i][1] / ut[i][0], ut[i][2] / ut[i][0], beta[i], rl[i], bl[i]};
-    const double Uj[6] = {ut[j][0], ut[j][1] / ut[j][0], ut[j][2] / ut[j][0], beta[j], rl[j], bl[j]};
-    double F[4];
-    fS4(a.gamma, Ui, Uj, F);
     for (int c = 0; c < 4; ++c) {
-      const double SF = S0 * F[c];
+      const double SF = SFk[4 * p + c];
       QF[i][c] = QF[i][c] + SF;
       QF[j][c] = QF[j][c] + -SF;
     }
@@ -852,6 +880,7 @@ LineArgs args_of(const LineSolve* L, int nstage, int flags) {
   a.Lraw = L->Lraw;
   a.fbar = L->fbar;
   a.Lelem = L->Lelem;
+  a.sf = L->sf;
   a.geom = L->geom;
   a.Ival = L->Ival;
   a.phikey = reinterpret_cast<long long*>(L->phimin);
@@ -900,7 +929,7 @@ cudaError_t launch_stage(LineSolve* L, double t, int nstage, double dt_set, bool
     k_line_begin<<<1, 32, 0, L->stream>>>(a, 1, 0.0, 0.0, 0, 0);
   }
   L->launches += 1;
-  k_line_face<<<grid, kThreads, 0, L->stream>>>(a);
+  k_line_face<<<(2 * L->K + kThreads - 1) / kThreads, kThreads, 0, L->stream>>>(a);
   L->launches += 1;
   if (flags & LF_LOW) {
     k_line_low<<<grid, kThreads, 0, L->stream>>>(a);
@@ -912,8 +941,10 @@ cudaError_t launch_stage(LineSolve* L, double t, int nstage, double dt_set, bool
     L->launches += 1;
   }
   if (flags & LF_HIGH) {
+    const long long np = (long long)L->K * L->npair;
+    k_line_pairs<<<(int)((np + kThreads - 1) / kThreads), kThreads, 0, L->stream>>>(a);
     k_line_high<<<grid, kThreads, 0, L->stream>>>(a);
-    L->launches += 1;
+    L->launches += 2;
   }
   if (flags & (LF_SUBCELL | LF_UPDATE)) {
     k_line_update<<<grid, kThreads, 0, L->stream>>>(a);
@@ -1005,6 +1036,7 @@ int line_create(const p2de_param* prm, const p2de_mesh* mesh, cudaStream_t st, L
   L->prm = *prm;
   L->N1D = n;
   L->K = K;
+  L->npair = ops.npair;
   L->stream = st;
   std::vector<int32_t> nbr(nfk), bcidx(nfk, 0);
   std::vector<int8_t> bc(nfk, BC_INTERIOR);
@@ -1032,6 +1064,7 @@ int line_create(const p2de_param* prm, const p2de_mesh* mesh, cudaStream_t st, L
   A(&L->Lraw, (size_t)2 * n * K);
   A(&L->fbar, (size_t)8 * (n + 1) * K);
   A(&L->Lelem, (size_t)3 * K);
+  A(&L->sf, (size_t)4 * kLineMaxPairs * K);
   A(&L->geom, (size_t)5 * K);
   A(&L->Ival, (size_t)3 * (mesh->nI > 0 ? mesh->nI : 1));
   A(&L->phimin, 1);
@@ -1196,7 +1229,7 @@ int line_step_launches(const LineSolve* L) {
   int c = 0;
   for (int stage = 1; stage <= 3; ++stage) {
     const int f = line_flags(L, stage, true);
-    c += 1 + 1 + ((f & LF_LOW) ? 1 : 0) + ((f & LF_HIGH) ? 1 : 0) + 1;
+    c += 1 + 1 + ((f & LF_LOW) ? 1 : 0) + ((f & LF_HIGH) ? 2 : 0) + 1;
   }
   return c;
 }

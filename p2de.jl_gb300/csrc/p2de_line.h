@@ -26,6 +26,8 @@ struct LineSolve {
   double *Lraw = nullptr;                 // L_local before symmetrization, K x 2 N1D
   double *fbar = nullptr;                 // f_bar_H, f_bar_L: K x 2 x (N1D+1) x 4
   double *Lelem = nullptr;                // ZhangShuLimiter L, 3 stages x K
+  double *sf = nullptr;                   // volume two-point terms S fS, K x kLineMaxPairs x 4
+  int npair = 0;                          // nonzero pairs of Srh_db per element
   double *geom = nullptr, *Ival = nullptr, *phimin = nullptr;
   int32_t *nbr = nullptr, *bcidx = nullptr;
   int8_t* bc = nullptr;
