@@ -958,18 +958,14 @@ static int build_graph(p2de_solver* s) {
 int p2de_ssp33_advance(p2de_solver* s, int64_t nsteps, double* t, int64_t* steps_done) {
   if (!s || !t || nsteps < 0) return P2DE_ERR_INVALID_ARGUMENT;
   CK(cudaSetDevice(s->device));
-  if (s->line) {  // the Line path launches each step (it reads dt back per step)
+  if (s->line) {
+    std::string err;
+    const int64_t before = s->line->launches;
     int64_t done = 0;
-    int rc = P2DE_OK;
-    for (int64_t i = 0; i < nsteps && *t < s->prm.T; ++i) {
-      double dt = 0.0;
-      rc = p2de_ssp33_step(s, t, &dt);
-      if (rc != P2DE_OK) break;
-      ++done;
-      s->line_dt = dt;
-    }
+    const int rc = line_advance(s->line, nsteps, t, &done, &s->line_dt, err);
+    s->launches += s->line->launches - before;
     if (steps_done) *steps_done = done;
-    return rc;
+    return line_status(s, rc, err);
   }
   int rc = build_graph(s);
   if (rc != P2DE_OK) return rc;

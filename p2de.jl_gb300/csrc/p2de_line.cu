@@ -52,6 +52,8 @@ constexpr int kThreads = 32;
 constexpr int MQ = kMaxN1D;     // nodes per element at most
 constexpr int MH = kLineMaxNh;  // nodes + face nodes
 constexpr int MS = 2 * kMaxN1D; // rows of L_local
+// the device-resident time state of a solve
+enum : int { TS_T = 0, TS_DT = 1, TS_DONE = 2, TS_STEPS = 3, TS_PHI = 4, TS_N = 8 };
 
 struct LineArgs {
   int K, N1D, nstage, flags;
@@ -64,8 +66,12 @@ struct LineArgs {
   unsigned long long* dtkey;
   long long* minrec;
   int* status;
-  double gamma, POSTOL, ZEROTOL, zeta, eta, CFL, beta, sc_TN, sc_sfac, s0;
+  double* ts;  // TS_* slots
+  double gamma, POSTOL, ZEROTOL, zeta, eta, CFL, beta, sc_TN, sc_sfac, s0, T, dt0, t0;
 };
+
+// a finished time loop turns every later launch of the step into a no-op
+__device__ __forceinline__ bool done(const LineArgs& a) { return a.ts[TS_DONE] != 0.0; }
 
 // ---- point functions (compressible_Navier_Stokes.jl; four slots, y momentum 0) ----------
 __device__ double pfun4(double gamma, const double* U) {
@@ -262,18 +268,40 @@ __device__ void smoothness(const LineArgs& a, const double (*U)[4], double& blen
 // ---- kernels ----------------------------------------------------------------------------
 // stage begin. dtkey[0]: the step's dt (lowered by the stage-1 CFL), dtkey[1]: the stage's
 // TimeParam dt, which the limiter reads (at stage 1 the dt before the CFL, rhs.jl:41-55 with
-// SSPRK33.jl:30-37). mode 0: both set to (dt, dt_lim); mode 1: dtkey[1] = dtkey[0].
-__global__ void k_line_begin(LineArgs a, int mode, double dt, double dt_lim, int reset_min, int reset_phi) {
+// SSPRK33.jl:30-37). mode 0 (a lone RHS): (dt, dt_lim) from the host, phi reset as given;
+// mode 1 (stages 2, 3 of a step): dtkey[1] = dtkey[0]; mode 2 (stage 1 of a step): from the
+// device time t, the loop's end test (SSPRK33.jl:29), dt = min(CFL dt0, T - t) for both,
+// the stage minima reset, and the initial min of phi reset when t == t0 (subcell.jl:31-34).
+__global__ void k_line_begin(LineArgs a, int mode, double dt, double dt_lim, int phi) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  if (mode == 0) {
-    a.dtkey[0] = (unsigned long long)__double_as_longlong(dt);
-    a.dtkey[1] = (unsigned long long)__double_as_longlong(dt_lim);
-  } else {
+  if (mode == 1) {
     a.dtkey[1] = a.dtkey[0];
+    return;
   }
-  if (reset_min)
-    for (int i = 0; i < 6; ++i) a.minrec[i] = encode_key(INFINITY);
-  if (reset_phi) *a.phikey = encode_key(INFINITY);
+  if (mode == 2) {
+    const double t = a.ts[TS_T];
+    if (!(t < a.T)) {
+      a.ts[TS_DONE] = 1.0;
+      return;
+    }
+    dt = dt_lim = jmin(a.CFL * a.dt0, a.T - t);
+    phi = phi && t == a.t0;
+  }
+  a.ts[TS_DONE] = 0.0;
+  a.ts[TS_PHI] = phi ? 1.0 : 0.0;
+  a.dtkey[0] = (unsigned long long)__double_as_longlong(dt);
+  a.dtkey[1] = (unsigned long long)__double_as_longlong(dt_lim);
+  for (int i = 0; i < 6; ++i) a.minrec[i] = encode_key(INFINITY);
+  if (phi) *a.phikey = encode_key(INFINITY);
+}
+
+// step end (SSPRK33.jl:38-39): t += dt, the step count
+__global__ void k_line_end(LineArgs a) {
+  if (threadIdx.x != 0 || blockIdx.x != 0 || done(a)) return;
+  const double dt = __longlong_as_double((long long)a.dtkey[0]);
+  a.ts[TS_T] = a.ts[TS_T] + dt;
+  a.ts[TS_DT] = dt;
+  a.ts[TS_STEPS] = a.ts[TS_STEPS] + 1.0;
 }
 
 // entropy_projection! (rhs.jl:59-133) with solve_theta!(::NodewiseScaledExtrapolation)
@@ -281,7 +309,7 @@ __global__ void k_line_begin(LineArgs a, int mode, double dt, double dt_lim, int
 // thread per face node (the two bisections of an element run side by side).
 __global__ void k_line_face(LineArgs a) {
   const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= 2LL * a.K) return;
+  if (g >= 2LL * a.K || done(a)) return;
   const int k = (int)(g / 2), f = (int)(g % 2);
   const int n = a.N1D, N = n - 1, s = a.nstage - 1;
   const LineOps& o = *a.ops;
@@ -343,7 +371,7 @@ __global__ void k_line_face(LineArgs a) {
 // LF placement (rhs_utils.jl:78-113); stage 1: the element's positivity CFL (:222-309)
 __global__ void k_line_low(LineArgs a) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= a.K) return;
+  if (k >= a.K || done(a)) return;
   const int n = a.N1D, N = n - 1;
   const LineOps& o = *a.ops;
   const double* g = a.geom + 5 * (size_t)k;
@@ -444,7 +472,7 @@ __global__ void k_line_low(LineArgs a) {
 // initialize_s_modified! (subcell.jl:21-35): the min of phi over all nodes
 __global__ void k_line_phimin(LineArgs a) {
   const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= (long long)a.K * a.N1D) return;
+  if (g >= (long long)a.K * a.N1D || done(a) || a.ts[TS_PHI] == 0.0) return;
   double U[4];
   ld4(a.Uq + 4 * g, U);
   atomicMin(a.phikey, encode_key(s_modified4(a.gamma, U)));
@@ -456,7 +484,7 @@ __global__ void k_line_phimin(LineArgs a) {
 __global__ void k_line_pairs(LineArgs a) {
   const LineOps& o = *a.ops;
   const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= (long long)a.K * o.npair) return;
+  if (g >= (long long)a.K * o.npair || done(a)) return;
   const int k = (int)(g / o.npair), p = (int)(g % o.npair);
   const int n = a.N1D, Nh = n + 2;
   const int i = o.pi[p], j = o.pj[p];
@@ -487,7 +515,7 @@ __global__ void k_line_pairs(LineArgs a) {
 // subcell_bound_limiter!, enforce_ES_subcell!)
 __global__ void k_line_high(LineArgs a) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= a.K) return;
+  if (k >= a.K || done(a)) return;
   const int n = a.N1D, N = n - 1, Nh = n + 2, s = a.nstage - 1;
   const LineOps& o = *a.ops;
   const double* g = a.geom + 5 * (size_t)k;
@@ -756,7 +784,7 @@ __global__ void k_line_high(LineArgs a) {
 // then the SSP-RK3 stage update (SSPRK33.jl:125-139) and the positivity record
 __global__ void k_line_update(LineArgs a) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= a.K) return;
+  if (k >= a.K || done(a)) return;
   const int n = a.N1D, s = a.nstage - 1;
   const LineOps& o = *a.ops;
   const double J = a.geom[5 * (size_t)k];
@@ -890,6 +918,10 @@ LineArgs args_of(const LineSolve* L, int nstage, int flags) {
   a.dtkey = L->dtkey;
   a.minrec = L->minrec;
   a.status = L->status;
+  a.ts = L->ts;
+  a.T = p.T;
+  a.dt0 = p.dt0;
+  a.t0 = p.t0;
   a.gamma = p.gamma;
   a.POSTOL = p.POSTOL;
   a.ZEROTOL = p.ZEROTOL;
@@ -911,22 +943,20 @@ double host_jmin(double x, double y) {
   return x < y ? x : y;
 }
 
-// the launches of one stage; dt_set: the stage's dt when the low-order CFL does not set it
-cudaError_t launch_stage(LineSolve* L, double t, int nstage, double dt_set, bool update) {
-  const int flags = line_flags(L, nstage, update);
+// the launches of one stage. step: a stage of SSP33!'s loop body with t and dt on the device
+// (mode 2 / 1 of k_line_begin); otherwise a lone RHS at host time t with dt_set.
+cudaError_t launch_stage(LineSolve* L, double t, int nstage, double dt_set, bool step) {
+  const int flags = line_flags(L, nstage, step);
   LineArgs a = args_of(L, nstage, flags);
   const int grid = (L->K + kThreads - 1) / kThreads;
-  const bool phimin = (flags & LF_MINENT) && t == L->prm.t0 && nstage == 1;
-  // a step starts from dt = min(CFL dt0, T - t) (SSPRK33.jl:30-32), which the stage-1 CFL of
-  // a low-order RHS lowers for the update; the limiter reads the TimeParam dt. A lone RHS
-  // takes the dt it is given, except for the CFL's starting value.
-  if (nstage == 1 || !update) {
-    const double dinit = host_jmin(L->prm.CFL * L->prm.dt0, L->prm.T - t);
-    const double dlim = update ? dinit : dt_set;
-    const double dkey = (flags & LF_CFL) ? dinit : dlim;
-    k_line_begin<<<1, 32, 0, L->stream>>>(a, 0, dkey, dlim, nstage == 1 ? 1 : 0, phimin ? 1 : 0);
+  const bool minent = (flags & LF_MINENT) && nstage == 1;
+  if (step) {
+    k_line_begin<<<1, 32, 0, L->stream>>>(a, nstage == 1 ? 2 : 1, 0.0, 0.0, minent ? 1 : 0);
   } else {
-    k_line_begin<<<1, 32, 0, L->stream>>>(a, 1, 0.0, 0.0, 0, 0);
+    // a lone RHS takes the dt it is given, except for the CFL's starting value
+    const double dinit = host_jmin(L->prm.CFL * L->prm.dt0, L->prm.T - t);
+    const double dkey = (flags & LF_CFL) ? dinit : dt_set;
+    k_line_begin<<<1, 32, 0, L->stream>>>(a, 0, dkey, dt_set, (minent && t == L->prm.t0) ? 1 : 0);
   }
   L->launches += 1;
   k_line_face<<<(2 * L->K + kThreads - 1) / kThreads, kThreads, 0, L->stream>>>(a);
@@ -935,7 +965,7 @@ cudaError_t launch_stage(LineSolve* L, double t, int nstage, double dt_set, bool
     k_line_low<<<grid, kThreads, 0, L->stream>>>(a);
     L->launches += 1;
   }
-  if (phimin) {
+  if (minent) {  // gated on the device by the begin kernel's t == t0 test
     const long long nodes = (long long)L->K * L->N1D;
     k_line_phimin<<<(int)((nodes + 255) / 256), 256, 0, L->stream>>>(a);
     L->launches += 1;
@@ -950,6 +980,16 @@ cudaError_t launch_stage(LineSolve* L, double t, int nstage, double dt_set, bool
     k_line_update<<<grid, kThreads, 0, L->stream>>>(a);
     L->launches += 1;
   }
+  return cudaGetLastError();
+}
+
+// the launches of one SSP33! loop body on L->stream
+cudaError_t enqueue_step(LineSolve* L) {
+  cudaError_t e = cudaSuccess;
+  for (int stage = 1; stage <= 3 && e == cudaSuccess; ++stage) e = launch_stage(L, 0.0, stage, 0.0, true);
+  if (e != cudaSuccess) return e;
+  k_line_end<<<1, 32, 0, L->stream>>>(args_of(L, 3, 0));
+  L->launches += 1;
   return cudaGetLastError();
 }
 
@@ -1073,6 +1113,7 @@ int line_create(const p2de_param* prm, const p2de_mesh* mesh, cudaStream_t st, L
   A(&L->bc, (size_t)nfk);
   A(&L->dtkey, 2);
   A(&L->minrec, 6);
+  A(&L->ts, TS_N);
   A(&L->status, 1);
   A(&L->ops, 1);
   auto up = [&](void* dst, const void* src, size_t bytes) {
@@ -1102,6 +1143,7 @@ int line_create(const p2de_param* prm, const p2de_mesh* mesh, cudaStream_t st, L
 void line_destroy(LineSolve* L) {
   if (!L) return;
   if (L->stream) cudaStreamSynchronize(L->stream);
+  if (L->graph) cudaGraphExecDestroy(L->graph);
   for (void* p : L->allocs) cudaFree(p);
   delete L;
 }
@@ -1202,34 +1244,81 @@ int line_rhs(LineSolve* L, double t, double dt, int nstage, double* dt_out, std:
   return check(L, err);
 }
 
+namespace {
+
+// sets the device time, runs `nsteps` loop bodies (one CUDA graph replayed), reads back the
+// time state and the status word once
+int run_steps(LineSolve* L, double* t, int64_t nsteps, double ts_out[TS_N], std::string& err) {
+  cudaError_t e = cudaMemcpyAsync(L->ts + TS_T, t, sizeof(double), cudaMemcpyHostToDevice, L->stream);
+  if (e == cudaSuccess && nsteps > 1 && !L->graph) {  // capture one body on a private stream
+    cudaStream_t cap, user = L->stream;
+    e = cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking);
+    if (e == cudaSuccess) {
+      cudaGraph_t g = nullptr;
+      const int64_t before = L->launches;
+      L->stream = cap;
+      e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+      const cudaError_t e1 = e == cudaSuccess ? enqueue_step(L) : e;
+      const cudaError_t e2 = e == cudaSuccess ? cudaStreamEndCapture(cap, &g) : e;
+      L->stream = user;
+      L->launches = before;
+      cudaStreamDestroy(cap);
+      e = e1 != cudaSuccess ? e1 : e2;
+      if (e == cudaSuccess) e = cudaGraphInstantiate(&L->graph, g, 0);
+      if (g) cudaGraphDestroy(g);
+    }
+  }
+  for (int64_t i = 0; i < nsteps && e == cudaSuccess; ++i) {
+    if (L->graph) {
+      e = cudaGraphLaunch(L->graph, L->stream);
+      L->launches += line_step_launches(L);
+    } else {
+      e = enqueue_step(L);
+    }
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(ts_out, L->ts, sizeof(double) * TS_N, cudaMemcpyDeviceToHost, L->stream);
+  if (e != cudaSuccess) {
+    err = std::string("line steps: ") + cudaGetErrorString(e);
+    return P2DE_ERR_CUDA;
+  }
+  const int rc = check(L, err);  // synchronizes
+  *t = ts_out[TS_T];
+  return rc;
+}
+
+}  // namespace
+
 int line_step(LineSolve* L, double* t, double* dt_out, std::string& err) {
-  if (!(*t < L->prm.T)) {  // the time loop has ended (SSPRK33.jl:125)
-    if (dt_out) *dt_out = 0.0;
-    return P2DE_OK;
-  }
-  cudaError_t e = cudaSuccess;
-  for (int stage = 1; stage <= 3 && e == cudaSuccess; ++stage) e = launch_stage(L, *t, stage, 0.0, true);
-  if (e != cudaSuccess) {
-    err = std::string("line step: ") + cudaGetErrorString(e);
-    return P2DE_ERR_CUDA;
-  }
-  const double dt = read_dt(L, e);
-  if (e != cudaSuccess) {
-    err = std::string("line step: ") + cudaGetErrorString(e);
-    return P2DE_ERR_CUDA;
-  }
-  const int rc = check(L, err);
+  double ts[TS_N];
+  double tt = *t;
+  const int rc = run_steps(L, &tt, 1, ts, err);
   if (rc != P2DE_OK) return rc;
-  *t = *t + dt;
-  if (dt_out) *dt_out = dt;
+  const bool stepped = ts[TS_DONE] == 0.0;
+  if (dt_out) *dt_out = stepped ? ts[TS_DT] : 0.0;
+  if (stepped) *t = tt;
   return P2DE_OK;
 }
 
+int line_advance(LineSolve* L, int64_t nsteps, double* t, int64_t* steps_done, double* dt_last, std::string& err) {
+  double ts[TS_N];
+  cudaError_t e = cudaMemcpyAsync(ts, L->ts, sizeof ts, cudaMemcpyDeviceToHost, L->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(L->stream);
+  if (e != cudaSuccess) {
+    err = std::string("line advance: ") + cudaGetErrorString(e);
+    return P2DE_ERR_CUDA;
+  }
+  const double steps0 = ts[TS_STEPS];
+  const int rc = run_steps(L, t, nsteps, ts, err);
+  if (steps_done) *steps_done = (int64_t)(ts[TS_STEPS] - steps0);
+  if (dt_last) *dt_last = ts[TS_DT];
+  return rc;
+}
+
 int line_step_launches(const LineSolve* L) {
-  int c = 0;
+  int c = 1;  // k_line_end
   for (int stage = 1; stage <= 3; ++stage) {
     const int f = line_flags(L, stage, true);
-    c += 1 + 1 + ((f & LF_LOW) ? 1 : 0) + ((f & LF_HIGH) ? 2 : 0) + 1;
+    c += 1 + 1 + ((f & LF_LOW) ? 1 : 0) + ((f & LF_MINENT) && stage == 1 ? 1 : 0) + ((f & LF_HIGH) ? 2 : 0) + 1;
   }
   return c;
 }

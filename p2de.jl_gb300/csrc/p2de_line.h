@@ -33,6 +33,8 @@ struct LineSolve {
   int8_t* bc = nullptr;
   unsigned long long* dtkey = nullptr;  // bits of the step's dt (positive: ordered) and of the limiter's dt
   long long* minrec = nullptr;          // min rho, min rhoe per stage (ordered keys)
+  double* ts = nullptr;                 // device time state: t, dt, done, steps, phi flag
+  cudaGraphExec_t graph = nullptr;      // one SSP-RK3 step, replayed by line_advance
   int* status = nullptr;
   LineOps* ops = nullptr;
   int64_t launches = 0;
@@ -48,6 +50,9 @@ int line_get_field(LineSolve* L, int field, int nstage, double* out, std::string
 int line_rhs(LineSolve* L, double t, double dt, int nstage, double* dt_out, std::string& err);
 // one SSP33! loop body from *t
 int line_step(LineSolve* L, double* t, double* dt_out, std::string& err);
+// nsteps loop bodies from *t with t and dt on the device (a captured step replayed); steps
+// after the final time are no-ops
+int line_advance(LineSolve* L, int64_t nsteps, double* t, int64_t* steps_done, double* dt_last, std::string& err);
 // kernel launches of one step
 int line_step_launches(const LineSolve* L);
 
