@@ -585,6 +585,8 @@ def run_line_report(args):
     }
     res = {}
     for name, (prob, kw) in cases.items():
+        if args.line_case and not name.startswith(args.line_case):
+            continue
         param, ic, bcf = prob(**kw)[:3]
         md, bc, desc, U0 = build_descriptor(param, ic, bcf)
         steps = min(args.steps, 200)
@@ -607,6 +609,7 @@ def main():
     ap.add_argument("--workload", default="dmr",
                     choices=["dmr", "kh256", "batch64", "serve", "mixed-report", "limiter-report", "line-report"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed", "mixed-acc64"])
+    ap.add_argument("--line-case", default="", help="line-report: only the cases whose name starts with this")
     ap.add_argument("--basis", default="lobatto", choices=["lobatto", "gauss"],
                     help="gauss: the DMR step with GaussCollocation + NodewiseScaledExtrapolation")
     ap.add_argument("--e2e-steps", type=int, default=20)
