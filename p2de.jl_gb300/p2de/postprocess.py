@@ -29,12 +29,22 @@ def _ascii(a: np.ndarray) -> str:
 
 
 def write_snapshot(path: str | Path, N: int, K: tuple[int, int], x: np.ndarray, y: np.ndarray, Uq: np.ndarray) -> Path:
-    """One structured-grid file (.vts) of the state Uq (K, Nq, 4) on nodes x, y (K, Nq)."""
+    """One structured-grid file (.vts) of the state Uq (K, Nq, 4) on nodes x, y (K, Nq). A
+    Line state (K, N+1, 3) of CompressibleEulerIdealGas{Dim1} is one row of (N+1) K points
+    in element order with fields rho, rhou, E."""
     path = Path(path)
     if path.suffix != ".vts":
         path = path.with_suffix(".vts")
-    X, Y = grid_arrays(N, K, x), grid_arrays(N, K, y)
-    U = grid_arrays(N, K, np.asarray(Uq).reshape(np.shape(x)[0], np.shape(x)[1], 4))
+    Uq = np.asarray(Uq)
+    fields = FIELDS
+    if Uq.size == 3 * np.size(x):  # a Line: nodes in element order along x
+        fields = ("rho", "rhou", "E")
+        X = np.asarray(x, dtype=np.float64).reshape(1, -1)
+        Y = np.zeros_like(X)
+        U = Uq.reshape(1, -1, 3)
+    else:
+        X, Y = grid_arrays(N, K, x), grid_arrays(N, K, y)
+        U = grid_arrays(N, K, Uq.reshape(np.shape(x)[0], np.shape(x)[1], 4))
     ny, nx = X.shape
     ext = f"0 {nx - 1} 0 {ny - 1} 0 0"
     pts = np.stack([X, Y, np.zeros_like(X)], axis=-1)
@@ -45,7 +55,7 @@ def write_snapshot(path: str | Path, N: int, K: tuple[int, int], x: np.ndarray, 
         f'    <Piece Extent="{ext}">',
         "      <PointData>",
     ]
-    for c, name in enumerate(FIELDS):
+    for c, name in enumerate(fields):
         lines.append(f'        <DataArray type="Float64" Name="{name}" format="ascii">{_ascii(U[..., c])}</DataArray>')
     lines += [
         "      </PointData>",
@@ -65,7 +75,7 @@ def construct_vtk_file(param, md, data_hist, output_path: str | Path, filename: 
     data_hist (Uhist, thist) and a .pvd collection, named as the reference names them."""
     out = Path(output_path)
     out.mkdir(parents=True, exist_ok=True)
-    stem = f"{filename}_N={param.N}_K={tuple(param.K)}"
+    stem = f"{filename}_N={param.N}_K={tuple(np.atleast_1d(param.K))}"
     entries = []
     for U, t in zip(data_hist.Uhist, data_hist.thist):
         f = write_snapshot(out / f"{stem}_t={t}.vts", param.N, param.K, md.x, md.y, U)

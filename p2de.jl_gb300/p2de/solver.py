@@ -322,7 +322,8 @@ class State:
 
     @property
     def Uq(self) -> np.ndarray:
-        return self._s.get_field(abi.FIELD_UQ).reshape(self._s.K, self._s.Nq, 4)
+        """(K, Nq, Nc): Nc = 4, 1 (KPP) or 3 (CompressibleEulerIdealGas{Dim1})."""
+        return self._s.get_field(abi.FIELD_UQ).reshape(self._s.K, self._s.Nq, -1)
 
     @Uq.setter
     def Uq(self, value):
@@ -333,19 +334,20 @@ class State:
 
     @property
     def rhsU(self):
-        return self.field(abi.FIELD_RHSU).reshape(self._s.K, self._s.Nq, 4)
+        return self.field(abi.FIELD_RHSU).reshape(self._s.K, self._s.Nq, -1)
 
     @property
     def rhsL(self):
-        return self.field(abi.FIELD_RHSL).reshape(self._s.K, self._s.Nq, 4)
+        return self.field(abi.FIELD_RHSL).reshape(self._s.K, self._s.Nq, -1)
 
     @property
     def rhsH(self):
-        return self.field(abi.FIELD_RHSH).reshape(self._s.K, self._s.Nq, 4)
+        return self.field(abi.FIELD_RHSH).reshape(self._s.K, self._s.Nq, -1)
 
     def L_local(self, nstage: int) -> np.ndarray:
-        n = self._s.N1D
-        return self.field(abi.FIELD_L_LOCAL, nstage).reshape(self._s.K, 2, n * n + n)
+        """L_local[:, :, :, nstage] as (K, Nd, Nq + N1D)."""
+        nd = 1 if self._s.desc.dim1 else 2
+        return self.field(abi.FIELD_L_LOCAL, nstage).reshape(self._s.K, nd, self._s.Nq + self._s.N1D)
 
 
 @dataclass

@@ -48,3 +48,19 @@ def test_collection_lists_every_snapshot(tmp_path):
     files = sorted(p.name for p in tmp_path.glob("*.vts"))
     assert len(files) == 2
     np.testing.assert_array_equal(P.read_snapshot(tmp_path / files[1])["rho"], 2.0)
+
+
+def test_line_snapshot_round_trip(tmp_path):
+    """A Line state (K, N+1, 3) is written as one row of points in element order."""
+    from p2de import problems
+    from p2de.mesh import uniform_mesh_1d
+
+    md = uniform_mesh_1d(3, 5, -1.0, 1.0)
+    eq = problems.line_param(3, 5, -1.0, 1.0, 0.1).equation
+    U = problems.primitive_to_conservative(eq, problems.density_wave_1d_exact(None, md.x, 0.0))
+    f = P.write_snapshot(tmp_path / "line", 3, (5, 1), md.x, md.y, U)
+    back = P.read_snapshot(f)
+    assert set(back) == {"rho", "rhou", "E", "x", "y"}
+    np.testing.assert_array_equal(back["x"].ravel(), md.x.ravel())
+    np.testing.assert_array_equal(back["rho"].ravel(), U[..., 0].ravel())
+    np.testing.assert_array_equal(back["E"].ravel(), U[..., 2].ravel())
