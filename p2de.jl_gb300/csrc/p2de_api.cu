@@ -412,20 +412,11 @@ void free_all(p2de_solver* s) {
 // CompressibleEulerIdealGas{Dim1}: the handle's common fields point at the Line state, so
 // the diagnostics (min rho/rhoe, conservation, errors, stage minima) serve both
 int create_line(const p2de_param* prm, const p2de_mesh* mesh, int device, p2de_solver** out) {
-  if (prm->reference_semantics)
-    return fail(nullptr, P2DE_ERR_UNSUPPORTED,
-                "CompressibleEulerIdealGas{Dim1}: the reference raises a MethodError in every RHS (Bx(::Dim1) calls "
-                "reference_to_physical with dim last, rhs_utils.jl:18); use reference_semantics = 0");
-  if (prm->N < 1 || prm->N > 5 || prm->K < 1)
-    return fail(nullptr, P2DE_ERR_INVALID_ARGUMENT, "N=%d outside 1..5 or K=%d", prm->N, prm->K);
-  if ((prm->low_order_surface_flux != P2DE_FLUX_LAX_FRIEDRICHS_ON_NODAL_VAL &&
-       prm->low_order_surface_flux != P2DE_FLUX_LAX_FRIEDRICHS_ON_PROJECTED_VAL) ||
-      prm->high_order_surface_flux != P2DE_FLUX_LAX_FRIEDRICHS_ON_PROJECTED_VAL)
-    return fail(nullptr, P2DE_ERR_UNSUPPORTED, "surface fluxes: LaxFriedrichsOnNodalVal or LaxFriedrichsOnProjectedVal");
-  if (prm->rhs_type < 0 || prm->rhs_type > 2 || prm->bound_type < 0 || prm->bound_type > 9 || prm->shock_capture < 0 ||
-      prm->shock_capture > 1 || prm->rhs_limiter < 0 || prm->rhs_limiter > 1 || prm->approximation_basis < 0 ||
-      prm->approximation_basis > 1 || prm->entropyproj_limiter < 0 || prm->entropyproj_limiter > 1)
-    return fail(nullptr, P2DE_ERR_INVALID_ARGUMENT, "rhs_type/bound_type/rhs_limiter/basis out of range");
+  {
+    std::string err;
+    const int rc = line_validate(prm, mesh, err);
+    if (rc != P2DE_OK) return fail(nullptr, rc, "%s", err.c_str());
+  }
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(nullptr, P2DE_ERR_NO_DEVICE, "no CUDA device");
   if (device < 0 || device >= ndev) return fail(nullptr, P2DE_ERR_INVALID_ARGUMENT, "device %d of %d", device, ndev);

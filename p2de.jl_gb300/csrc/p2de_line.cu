@@ -1023,11 +1023,27 @@ double read_dt(LineSolve* L, cudaError_t& e) {
 
 }  // namespace
 
-int line_create(const p2de_param* prm, const p2de_mesh* mesh, cudaStream_t st, LineSolve** out, std::string& err) {
-  *out = nullptr;
+int line_validate(const p2de_param* prm, const p2de_mesh* mesh, std::string& err) {
   if (prm->reference_semantics) {
     err = "CompressibleEulerIdealGas{Dim1}: the reference raises a MethodError in every RHS (Bx(::Dim1) "
           "calls reference_to_physical with dim last, rhs_utils.jl:18); use reference_semantics = 0";
+    return P2DE_ERR_UNSUPPORTED;
+  }
+  if (prm->N < 1 || prm->N > 5 || prm->K < 1) {
+    err = "N outside 1..5 or K < 1";
+    return P2DE_ERR_INVALID_ARGUMENT;
+  }
+  if (prm->rhs_type < 0 || prm->rhs_type > 2 || prm->bound_type < 0 || prm->bound_type > 9 ||
+      prm->shock_capture < 0 || prm->shock_capture > 1 || prm->rhs_limiter < 0 || prm->rhs_limiter > 1 ||
+      prm->approximation_basis < 0 || prm->approximation_basis > 1 || prm->entropyproj_limiter < 0 ||
+      prm->entropyproj_limiter > 1) {
+    err = "rhs_type/bound_type/rhs_limiter/basis out of range";
+    return P2DE_ERR_INVALID_ARGUMENT;
+  }
+  if ((prm->low_order_surface_flux != P2DE_FLUX_LAX_FRIEDRICHS_ON_NODAL_VAL &&
+       prm->low_order_surface_flux != P2DE_FLUX_LAX_FRIEDRICHS_ON_PROJECTED_VAL) ||
+      prm->high_order_surface_flux != P2DE_FLUX_LAX_FRIEDRICHS_ON_PROJECTED_VAL) {
+    err = "surface fluxes: LaxFriedrichsOnNodalVal or LaxFriedrichsOnProjectedVal";
     return P2DE_ERR_UNSUPPORTED;
   }
   if (prm->precision != P2DE_PRECISION_FP64 || mesh->nW || mesh->nS) {
@@ -1043,30 +1059,40 @@ int line_create(const p2de_param* prm, const p2de_mesh* mesh, cudaStream_t st, L
           "has no Dim1 method for GaussCollocation, subcell.jl:755-759)";
     return P2DE_ERR_UNSUPPORTED;
   }
-  const int K = prm->K, n = prm->N + 1;
-  const int64_t nfk = 2 * (int64_t)K;
+  const int64_t nfk = 2 * (int64_t)prm->K;
+  if (!mesh->geom || !mesh->mapP) {
+    err = "geom and mapP are required";
+    return P2DE_ERR_INVALID_ARGUMENT;
+  }
   for (int64_t i = 0; i < nfk; ++i)
     if (mesh->mapP[i] < 1 || mesh->mapP[i] > nfk) {
       err = "mapP[" + std::to_string(i) + "] out of 1.." + std::to_string(nfk);
       return P2DE_ERR_INVALID_ARGUMENT;
     }
-  auto check_list = [&](const int64_t* m, int64_t cnt, const char* name) {
+  auto list_ok = [&](const int64_t* m, int64_t cnt) {
     if (cnt < 0 || (cnt > 0 && !m)) return false;
     for (int64_t i = 0; i < cnt; ++i)
       if (m[i] < 1 || m[i] > nfk) return false;
-    (void)name;
     return true;
   };
-  if (!check_list(mesh->mapI, mesh->nI, "mapI") || !check_list(mesh->mapO, mesh->nO, "mapO") ||
-      (mesh->nI > 0 && !mesh->Ival)) {
+  if (!list_ok(mesh->mapI, mesh->nI) || !list_ok(mesh->mapO, mesh->nO) || (mesh->nI > 0 && !mesh->Ival)) {
     err = "mapI/mapO/Ival: bad list";
     return P2DE_ERR_INVALID_ARGUMENT;
   }
-  for (int k = 0; k < K; ++k)
+  for (int k = 0; k < prm->K; ++k)
     if (!(mesh->geom[5 * (size_t)k] > 0.0)) {
       err = "J[" + std::to_string(k) + "] is not positive";
       return P2DE_ERR_INVALID_ARGUMENT;
     }
+  return P2DE_OK;
+}
+
+int line_create(const p2de_param* prm, const p2de_mesh* mesh, cudaStream_t st, LineSolve** out, std::string& err) {
+  *out = nullptr;
+  const int rc = line_validate(prm, mesh, err);
+  if (rc != P2DE_OK) return rc;
+  const int K = prm->K, n = prm->N + 1;
+  const int64_t nfk = 2 * (int64_t)K;
   LineOps ops;
   if (build_line_ops(prm->N, prm->ZEROTOL, &ops, prm->approximation_basis) != 0) {
     err = "Line operators: degree out of range";

@@ -41,6 +41,8 @@ struct LineSolve {
   std::vector<void*> allocs;
 };
 
+// host-side checks of a Dim1 descriptor (no device needed)
+int line_validate(const p2de_param* prm, const p2de_mesh* mesh, std::string& err);
 int line_create(const p2de_param* prm, const p2de_mesh* mesh, cudaStream_t st, LineSolve** out, std::string& err);
 void line_destroy(LineSolve* L);
 int64_t line_field_count(const LineSolve* L, int field);

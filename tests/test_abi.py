@@ -83,3 +83,38 @@ def test_no_device_is_a_status_not_a_crash():
     assert st == 7  # P2DE_ERR_NO_DEVICE
     with pytest.raises(p2de.P2deError):
         S.Solver(param, md, desc)
+
+
+def test_line_descriptors_checked_before_the_device():
+    """CompressibleEulerIdealGas{Dim1} descriptors are checked on the host: what the Line
+    path refuses comes back as P2DE_ERR_UNSUPPORTED (2) or INVALID_ARGUMENT (1) with no
+    device; an accepted one reaches the device query (P2DE_ERR_NO_DEVICE, 7, here)."""
+    from ctypes import byref, c_void_p
+
+    from p2de import problems
+    from p2de.types import GaussCollocation, NodewiseScaledExtrapolation, PositivityAndCellEntropyBound, SubcellLimiter
+
+    from helpers import setup
+
+    lib = abi.load_library()
+
+    def status(desc):
+        h = c_void_p()
+        return lib.p2de_initialize_DG(byref(desc.param), byref(desc.mesh), 0, byref(h))
+
+    ok = setup(problems.leblanc, N=2, K=8)[3]
+    assert status(ok) in (0, 7)
+    refsem = setup(problems.leblanc, N=2, K=8)[3]
+    refsem.param.reference_semantics = 1
+    assert status(refsem) == 2
+    gauss_cell = setup(problems.leblanc, N=2, K=8, approximation_basis=GaussCollocation(),
+                       entropyproj_limiter=NodewiseScaledExtrapolation(),
+                       rhs_limiter=SubcellLimiter(bound=PositivityAndCellEntropyBound()))[3]
+    assert status(gauss_cell) == 2
+    mixed = setup(problems.leblanc, N=2, K=8)[3]
+    mixed.param.precision = 1
+    assert status(mixed) == 2
+    bad_map = setup(problems.leblanc, N=2, K=8)
+    desc = bad_map[3]
+    desc.keep[1][3] = 99  # a mapP entry outside 1..2K
+    assert status(desc) == 1
