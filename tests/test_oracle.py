@@ -630,3 +630,44 @@ def test_line_reference_semantics_refused():
     lib = abi.load_library()
     h = c_void_p()
     assert lib.p2de_initialize_DG(byref(desc.param), byref(desc.mesh), 0, byref(h)) == 2  # P2DE_ERR_UNSUPPORTED
+
+
+def test_line_interface_factors_symmetric():
+    """Across every element interface the two subcell factors agree after
+    symmetrization (mapP pairing of subcell faces 1 and Nq+1), so the limited interface
+    flux is one value and the scheme conserves; self-mapped domain ends keep their own."""
+    from p2de.types import PositivityAndMinEntropyBound, SubcellLimiter, TVDBound
+
+    for lim in (SubcellLimiter(), SubcellLimiter(bound=TVDBound()), SubcellLimiter(bound=PositivityAndMinEntropyBound())):
+        param, md, desc, U0, o = _line(problems.leblanc, N=3, K=20, rhs_limiter=lim)
+        o.rhs(param.timestepping_param.t0, 1e-3, 1)
+        n1 = param.N + 1
+        L = o.get_field(abi.FIELD_L_LOCAL, 1).reshape(desc.K, 2 * n1)
+        np.testing.assert_array_equal(L[:-1, n1], L[1:, 0])
+        assert L[:, : n1 + 1].min() < 1.0  # the limiter acts at the contact and shock
+        o.close()
+
+
+def test_line_cell_entropy_greedy_acts():
+    """The cell-entropy bound's greedy step (enforce_ES_subcell_volume!(::Dim1) with N dvdf
+    entries per element) lowers factors below the positivity bound's somewhere on the same
+    state: the Shu-Osher data on LGL nodes after 30 steps."""
+    from p2de.types import LobattoCollocation, NoEntropyProjectionLimiter, PositivityAndCellEntropyBound
+    from p2de.types import PositivityBound, SubcellLimiter
+
+    lgl = dict(approximation_basis=LobattoCollocation(), entropyproj_limiter=NoEntropyProjectionLimiter())
+    param, md, desc, U0, o = _line(problems.shu_osher, N=3, K=64, rhs_limiter=SubcellLimiter(bound=PositivityBound()), **lgl)
+    t = 0.0
+    for _ in range(30):
+        t, _ = o.step(t)
+    U = o.get_field(abi.FIELD_UQ)
+    o.close()
+    Ls = []
+    for bound in (PositivityBound(), PositivityAndCellEntropyBound()):
+        param, md, desc, U0, o = _line(problems.shu_osher, N=3, K=64, rhs_limiter=SubcellLimiter(bound=bound), **lgl)
+        o.set_Uq(U)
+        o.rhs(t, 1e-3, 1)
+        n1 = param.N + 1
+        Ls.append(o.get_field(abi.FIELD_L_LOCAL, 1).reshape(desc.K, 2 * n1)[:, : n1 + 1])
+        o.close()
+    assert np.all(Ls[1] <= Ls[0]) and (Ls[1] < Ls[0]).sum() >= 5
