@@ -3,16 +3,17 @@
 // subcell limiter (subcell.jl) or the Zhang-Shu limiter (zhangshu.jl), and the SSP-RK3
 // stage update (SSPRK33.jl:125-139).
 //
-// One thread per element. A 1D solve has at most a few thousand elements, so the kernels
-// are launch-bound; they are written for agreement with the FP64 restatement: this
+// One thread per element (per face node in the projection, per nonzero pair for the volume
+// two-point terms). The kernels are written for agreement with the FP64 restatement: this
 // translation unit is compiled without FMA contraction (-fmad=false) and keeps the
 // reference's association order, so away from limiter decisions the results differ only
 // through the last bits of log, exp and pow.
 //
 // States keep four slots per node, (rho, rhou, 0, E): with the y momentum 0 every Dim2
 // point function below gives the Dim1 value of compressible_Navier_Stokes.jl exactly.
-// Kernels of one stage: face projection -> low order (+ CFL) -> [initial min phi] ->
-// high order + limiter factors -> symmetrization, limited fluxes, RK update.
+// Kernels of one stage: begin (dt) -> face projection -> low order (+ CFL) -> [initial
+// min phi] -> volume pair terms -> high order + limiter factors -> symmetrization, limited
+// fluxes, RK update; a step ends with t += dt on the device and is captured as one graph.
 #include <cuda_runtime.h>
 
 #include <cmath>
