@@ -308,11 +308,13 @@ __global__ void k_line_end(LineArgs a) {
 // entropy_projection! (rhs.jl:59-133) with solve_theta!(::NodewiseScaledExtrapolation)
 // (filter.jl:6-62, 91-130) on Gauss nodes: theta_local and the projected face states. One
 // thread per face node (the two bisections of an element run side by side).
+template <int NQ>
 __global__ void k_line_face(LineArgs a) {
   const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= 2LL * a.K || done(a)) return;
   const int k = (int)(g / 2), f = (int)(g % 2);
-  const int n = a.N1D, N = n - 1, s = a.nstage - 1;
+  constexpr int n = NQ, N = n - 1;
+  const int s = a.nstage - 1;
   const LineOps& o = *a.ops;
   double U[MQ][4], v[MQ][4];
   for (int i = 0; i < n; ++i) {
@@ -370,10 +372,11 @@ __global__ void k_line_face(LineArgs a) {
 
 // rhs_low_graph_visc! (low_order_graph_viscosity.jl:4-41) with the Dim1 graph viscosity and
 // LF placement (rhs_utils.jl:78-113); stage 1: the element's positivity CFL (:222-309)
+template <int NQ>
 __global__ void k_line_low(LineArgs a) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= a.K || done(a)) return;
-  const int n = a.N1D, N = n - 1;
+  constexpr int n = NQ, N = n - 1;
   const LineOps& o = *a.ops;
   const double* g = a.geom + 5 * (size_t)k;
   const double J = g[0];
@@ -404,6 +407,7 @@ __global__ void k_line_low(LineArgs a) {
     for (int c = 0; c < 4; ++c) r[i][c] = 0.0 - r[i][c];
   // accumulate_low_order_rhs_surface! (:175-204) with get_uP_and_enforce_BC! (:94-124)
   double lamB[2], wsf[2];
+#pragma unroll
   for (int f = 0; f < 2; ++f) {
     const int fk = 2 * k + f, p = a.nbr[fk], kP = p / 2, iP = p % 2;
     double Uf[4], UfP[4], uP[4], b0, b1, bP0, bP1;
@@ -514,10 +518,12 @@ __global__ void k_line_pairs(LineArgs a) {
 // Zhang-Shu (zhangshu.jl:4-45) or the subcell factors before symmetrization (subcell.jl:
 // Dim1 methods of accumulate_f_bar!, initialize_lower_bound!, initialize_TVD_bounds!,
 // subcell_bound_limiter!, enforce_ES_subcell!)
+template <int NQ>
 __global__ void k_line_high(LineArgs a) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= a.K || done(a)) return;
-  const int n = a.N1D, N = n - 1, Nh = n + 2, s = a.nstage - 1;
+  constexpr int n = NQ, N = n - 1, Nh = n + 2;
+  const int s = a.nstage - 1;
   const LineOps& o = *a.ops;
   const double* g = a.geom + 5 * (size_t)k;
   const double J = g[0];
@@ -558,14 +564,18 @@ __global__ void k_line_high(LineArgs a) {
   // flux_differencing_volume! (:164-211): the pair terms S F of k_line_pairs, accumulated
   // in pair order
   const double* SFk = a.sf + (size_t)4 * kLineMaxPairs * k;
-  for (int p = 0; p < o.npair; ++p) {
-    const int i = o.pi[p], j = o.pj[p];
-    for (int c = 0; c < 4; ++c) {
-      const double SF = SFk[4 * p + c];
-      QF[i][c] = QF[i][c] + SF;
-      QF[j][c] = QF[j][c] + -SF;
+  // each node gathers its pair terms in pair order (the order of the sequential scatter)
+#pragma unroll
+  for (int h = 0; h < Nh; ++h)
+    for (int p = 0; p < o.npair; ++p) {
+      const int i = o.pi[p], j = o.pj[p];
+      if (i != h && j != h) continue;
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const double SF = SFk[4 * p + c];
+        QF[h][c] = QF[h][c] + (i == h ? SF : -SF);
+      }
     }
-  }
   // flux_differencing_surface! (:223-272)
   double BF[2][4];
   for (int f = 0; f < 2; ++f) {
@@ -783,10 +793,12 @@ __global__ void k_line_high(LineArgs a) {
 // symmetrize_limiting_parameters!(::Dim1) (subcell.jl:405-415) across mapP,
 // accumulate_f_bar_limited!(::Dim1) (:826-839), apply_subcell_limiter!(::Dim1) (:878-892);
 // then the SSP-RK3 stage update (SSPRK33.jl:125-139) and the positivity record
+template <int NQ>
 __global__ void k_line_update(LineArgs a) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= a.K || done(a)) return;
-  const int n = a.N1D, s = a.nstage - 1;
+  constexpr int n = NQ;
+  const int s = a.nstage - 1;
   const LineOps& o = *a.ops;
   const double J = a.geom[5 * (size_t)k];
   double* rU = a.rhsU + 4 * (size_t)n * k;
@@ -944,6 +956,16 @@ double host_jmin(double x, double y) {
   return x < y ? x : y;
 }
 
+// kern<N1D> for the solve's degree
+#define LINE_LAUNCH(kern, grid, args)                                            \
+  switch (L->N1D) {                                                              \
+    case 2: kern<2><<<(grid), kThreads, 0, L->stream>>>(args); break;            \
+    case 3: kern<3><<<(grid), kThreads, 0, L->stream>>>(args); break;            \
+    case 4: kern<4><<<(grid), kThreads, 0, L->stream>>>(args); break;            \
+    case 5: kern<5><<<(grid), kThreads, 0, L->stream>>>(args); break;            \
+    default: kern<6><<<(grid), kThreads, 0, L->stream>>>(args); break;           \
+  }
+
 // the launches of one stage. step: a stage of SSP33!'s loop body with t and dt on the device
 // (mode 2 / 1 of k_line_begin); otherwise a lone RHS at host time t with dt_set.
 cudaError_t launch_stage(LineSolve* L, double t, int nstage, double dt_set, bool step) {
@@ -960,10 +982,10 @@ cudaError_t launch_stage(LineSolve* L, double t, int nstage, double dt_set, bool
     k_line_begin<<<1, 32, 0, L->stream>>>(a, 0, dkey, dt_set, (minent && t == L->prm.t0) ? 1 : 0);
   }
   L->launches += 1;
-  k_line_face<<<(2 * L->K + kThreads - 1) / kThreads, kThreads, 0, L->stream>>>(a);
+  LINE_LAUNCH(k_line_face, (2 * L->K + kThreads - 1) / kThreads, a);
   L->launches += 1;
   if (flags & LF_LOW) {
-    k_line_low<<<grid, kThreads, 0, L->stream>>>(a);
+    LINE_LAUNCH(k_line_low, grid, a);
     L->launches += 1;
   }
   if (minent) {  // gated on the device by the begin kernel's t == t0 test
@@ -974,11 +996,11 @@ cudaError_t launch_stage(LineSolve* L, double t, int nstage, double dt_set, bool
   if (flags & LF_HIGH) {
     const long long np = (long long)L->K * L->npair;
     k_line_pairs<<<(int)((np + kThreads - 1) / kThreads), kThreads, 0, L->stream>>>(a);
-    k_line_high<<<grid, kThreads, 0, L->stream>>>(a);
+    LINE_LAUNCH(k_line_high, grid, a);
     L->launches += 2;
   }
   if (flags & (LF_SUBCELL | LF_UPDATE)) {
-    k_line_update<<<grid, kThreads, 0, L->stream>>>(a);
+    LINE_LAUNCH(k_line_update, grid, a);
     L->launches += 1;
   }
   return cudaGetLastError();
