@@ -50,6 +50,20 @@ KERNEL_A_TRAFFIC_BYTES = 142.2e6
 KERNEL_A_FP64_PIPE_BUSY = 0.857
 
 
+def fma_probe_library():
+    """libp2de_probe.so (built beside the solver library by build()): the FP64/FP32 FMA
+    throughput probe whose FP64 figure is kernel A's roofline denominator."""
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location("p2de_build", ROOT / "p2de.jl_gb300" / "build.py")
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    lib = ctypes.CDLL(str(mod.build_probe()))
+    lib.p2de_probe_fma_peak.argtypes = [ctypes.c_int, ctypes.c_int32, ctypes.POINTER(c_double)]
+    lib.p2de_probe_fma_peak.restype = ctypes.c_int
+    return lib
+
+
 def workload(name: str, precision: str, basis: str = "lobatto"):
     from p2de import problems
     from p2de.types import GaussCollocation, NodewiseScaledExtrapolation, PositivityBound, SubcellLimiter
@@ -704,7 +718,10 @@ def main():
     quad_per_launch = cnt[0] / (3 * prof_steps)
     flops_a = roofline.stage_a_flops(param.N, desc.K, quad_per_launch)
     peak = c_double()
-    solver._check(lib.p2de_probe_fma_peak(local, 1, byref(peak)))
+    probe = fma_probe_library()
+    rc = probe.p2de_probe_fma_peak(local, 1, byref(peak))
+    if rc != 0:
+        raise RuntimeError(f"FMA probe failed with status {rc}")
     achieved = flops_a / (kms[0] * 1e-3) / 1e12
 
     # ---- end-to-end through the public ABI with host buffers
@@ -783,7 +800,7 @@ def main():
                 "ms_per_launch": kms[0],
                 "ms_per_launch_stage_b": kms[1],
                 "stage_b_hbm_gbs": bytes_ab["stage_b"] / (kms[1] * 1e-3) / 1e9,
-                "peak_source": "p2de_probe_fma_peak: FP64 FMA chains on this GPU in this run (MEASURED_PEAKS.json has no FP64 figure)",
+                "peak_source": "libp2de_probe.so p2de_probe_fma_peak: FP64 FMA chains on this GPU in this run (MEASURED_PEAKS.json has no FP64 figure)",
             },
             "min_rho_rhoe_last_step": [float(mins[4]), float(mins[5])],
             "cpu_baseline": cpu,

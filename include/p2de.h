@@ -293,10 +293,6 @@ int p2de_profile_steps(p2de_solver* s, int64_t nsteps, double* t, double ms[3]);
  * solves evaluated (limiter_utils.jl:108-132); the others are skipped exactly. */
 int p2de_read_counters(p2de_solver* s, uint64_t out[1], int32_t reset);
 
-/* FMA throughput of `device` in TFLOP/s (2 flops per FMA), FP64 (fp64 = 1) or FP32:
- * the denominator of the FP64-pipe roofline. */
-int p2de_probe_fma_peak(int device, int32_t fp64, double* tflops);
-
 /* Elements per thread block of the stage kernels (1..epb_max, the shared-memory limit).
  * Results do not depend on it: each element's arithmetic is the same at every value.
  * No counterpart in the reference (a launch parameter of this implementation). */
@@ -367,16 +363,18 @@ int p2de_server_destroy(p2de_server* s);
 /* ---- Right-hand side without device allocation -------------------------------------
  * No counterpart in the reference. For callers that cannot call cudaMalloc when they
  * need a right-hand side: a process whose device memory is reserved up front by its own
- * pool allocator (a Julia or serving process with a fixed HBM budget), or code running
- * while a stream is captured into a CUDA graph, where cudaMalloc/cudaFree are not
- * allowed. All scratch (subcell fluxes, blending factors, device scalars, operator
- * table) lives in one static device array of P2DE_NOALLOC_SCRATCH_BYTES that every GPU
- * loading this entry point keeps until the process exits; problems needing more are
- * rejected with P2DE_ERR_BUDGET (p2de_noalloc_max_elements gives the limit per degree).
- * The array is shared by all calls and keeps the last call's contents, so calls that
- * overlap on the GPU race. The first call on a device does a one-time set-up (the
- * array's device address and kernel attributes) and should come before any stream
- * capture. Inputs and outputs are caller-owned device arrays in the layouts above. */
+ * pool allocator (a Julia or serving process with a fixed HBM budget, where one more
+ * cudaMalloc fails or breaks the budget), or an application that allocates device memory
+ * only at start-up. All scratch (subcell fluxes, blending factors, device scalars,
+ * operator table) lives in one static device array of P2DE_NOALLOC_SCRATCH_BYTES that
+ * every GPU loading this entry point keeps until the process exits; problems needing
+ * more are rejected with P2DE_ERR_BUDGET (p2de_noalloc_max_elements gives the limit per
+ * degree). The array is shared by all calls and keeps the last call's contents (the
+ * operator table is rebuilt when N or ZEROTOL changes; everything else a call reads is
+ * written by that call), so calls that overlap on the GPU race. The first call on a
+ * device does a one-time set-up (the array's device address and kernel attributes) and
+ * should come before any stream capture. Each call synchronizes `stream` before it
+ * returns. Inputs and outputs are caller-owned device arrays in the layouts above. */
 #define P2DE_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
 
 typedef struct p2de_device_mesh {

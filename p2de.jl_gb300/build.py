@@ -16,6 +16,9 @@ PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = BUILD / "libp2de_gpu.so"
+# the benchmark's FP64/FP32 FMA-throughput probe (roofline denominator), kept out of the solver
+PROBE_SRC = CSRC / "probe" / "p2de_fma_probe.cu"
+PROBE_LIB = BUILD / "libp2de_probe.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"] + ARCH
@@ -56,8 +59,25 @@ def up_to_date() -> bool:
     return all(p.stat().st_mtime <= t for p in _deps())
 
 
+def build_probe(force: bool = False, verbose: bool = False) -> Path:
+    """libp2de_probe.so: the benchmark's FMA-throughput probe, one translation unit."""
+    if not force and PROBE_LIB.exists() and PROBE_LIB.stat().st_mtime >= PROBE_SRC.stat().st_mtime:
+        return PROBE_LIB
+    BUILD.mkdir(parents=True, exist_ok=True)
+    tmp = PROBE_LIB.with_suffix(".so.tmp")
+    cmd = [_nvcc(), *NVCC_FLAGS, "-shared", str(PROBE_SRC), "-o", str(tmp)]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"nvcc failed for {PROBE_SRC.name}:\n{r.stdout}\n{r.stderr}")
+    os.replace(tmp, PROBE_LIB)
+    return PROBE_LIB
+
+
 def build(force: bool = False, verbose: bool = False) -> Path:
     if not force and up_to_date():
+        build_probe(force, verbose)
         return LIB
     BUILD.mkdir(parents=True, exist_ok=True)
     nvcc = _nvcc()
@@ -72,6 +92,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    build_probe(force, verbose)
     return LIB
 
 

@@ -2,10 +2,12 @@
 // stage update) with every piece of scratch memory in one file-scope device array,
 // for callers that cannot allocate device memory. Some hosts cannot call cudaMalloc
 // at the moment they need a right-hand side: a Julia or serving process whose device
-// memory is reserved up front by its own pool allocator, or code that runs while a
-// stream is being captured into a CUDA graph, where cudaMalloc and cudaFree are not
-// allowed. This entry point only launches kernels and copies a few bytes of
-// parameters; it calls no cudaMalloc, cudaFree or allocating library routine.
+// memory is reserved up front by its own pool allocator (a further cudaMalloc would
+// fail or break the budget the pool enforces), or an application that allows device
+// allocation only during its start-up. This entry point only launches kernels and copies
+// a few bytes of parameters and results; it calls no cudaMalloc, cudaFree or allocating
+// library routine. It synchronizes its stream before returning (the index check, the
+// status word and dt are read back to the host).
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -42,7 +44,10 @@ constexpr size_t H_DATA = H_TABLE + kTableDoubles;
 struct DeviceState {
   bool ready = false;
   double* scratch = nullptr;  // device address of g_noalloc_scratch on this device
-  int table_N = 0;            // degree whose OpTable the scratch holds
+  // the OpTable the scratch holds: build_op_table depends on the degree and on ZEROTOL
+  // (entries below it are set to zero), so both are its key
+  int table_N = 0;
+  uint64_t table_zerotol_bits = 0;
 };
 std::mutex g_mu;
 DeviceState g_dev[64];
@@ -128,6 +133,7 @@ extern "C" int p2de_rhs_noalloc(const p2de_param* prm, const p2de_device_mesh* m
     // set-up, once per device, with that device current: the address of the scratch
     // array (a host-side symbol is not a device address) and the kernels' shared-memory
     // limits; the first call on a device should therefore come before any stream capture
+    // on that device
     std::lock_guard<std::mutex> lk(g_mu);
     DeviceState& d = g_dev[dev];
     if (!d.ready) {
@@ -138,13 +144,17 @@ extern "C" int p2de_rhs_noalloc(const p2de_param* prm, const p2de_device_mesh* m
     }
     if (prepare(n1d, &geo) != cudaSuccess) return P2DE_ERR_CUDA;
     scr = d.scratch;
-    if (d.table_N != prm->N) {
+    uint64_t zbits;
+    std::memcpy(&zbits, &prm->ZEROTOL, sizeof zbits);
+    if (d.table_N != prm->N || d.table_zerotol_bits != zbits) {
       OpTable tab;
       if (build_op_table(prm->N, prm->ZEROTOL, &tab) != 0) return P2DE_ERR_INVALID_ARGUMENT;
+      d.table_N = 0;  // invalid until the copy below has completed
       if (cudaMemcpyAsync(scr + H_TABLE, &tab, sizeof tab, cudaMemcpyHostToDevice, st) != cudaSuccess ||
           cudaStreamSynchronize(st) != cudaSuccess)
         return P2DE_ERR_CUDA;
       d.table_N = prm->N;
+      d.table_zerotol_bits = zbits;
     }
   }
   const size_t nsf = geo.nsf, nq = (size_t)n1d * n1d;

@@ -1,8 +1,11 @@
-// Roofline denominator probe: FMA throughput of this GPU (independent FMA chains per
-// thread, no memory traffic but one store per thread), in FP64 or FP32.
+// Roofline denominator probe for the benchmark (built as libp2de_probe.so, not part of the
+// solver library): FMA throughput of this GPU (independent FMA chains per thread, no memory
+// traffic but one store per thread), in FP64 or FP32. Returns 0 on success, 3 on a CUDA
+// error, 4 when the output buffer cannot be allocated.
 #include <cuda_runtime.h>
+#include <stdint.h>
 
-#include "../../include/p2de.h"
+enum { PROBE_OK = 0, PROBE_ERR_ARG = 1, PROBE_ERR_CUDA = 3, PROBE_ERR_OOM = 4 };
 
 namespace {
 
@@ -25,12 +28,12 @@ __global__ void k_fma_chains(T* out, int iters, T a, T b) {
 
 template <typename T>
 int run(int device, int iters, double* tflops) {
-  if (cudaSetDevice(device) != cudaSuccess) return P2DE_ERR_CUDA;
+  if (cudaSetDevice(device) != cudaSuccess) return PROBE_ERR_CUDA;
   cudaDeviceProp p;
-  if (cudaGetDeviceProperties(&p, device) != cudaSuccess) return P2DE_ERR_CUDA;
+  if (cudaGetDeviceProperties(&p, device) != cudaSuccess) return PROBE_ERR_CUDA;
   const int threads = 256, blocks = p.multiProcessorCount * 8;
   T* out = nullptr;
-  if (cudaMalloc(&out, sizeof(T) * blocks * threads) != cudaSuccess) return P2DE_ERR_OUT_OF_MEMORY;
+  if (cudaMalloc(&out, sizeof(T) * blocks * threads) != cudaSuccess) return PROBE_ERR_OOM;
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
@@ -44,14 +47,14 @@ int run(int device, int iters, double* tflops) {
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   cudaFree(out);
-  if (e != cudaSuccess || ms <= 0) return P2DE_ERR_CUDA;
+  if (e != cudaSuccess || ms <= 0) return PROBE_ERR_CUDA;
   *tflops = 2.0 * 8.0 * (double)iters * blocks * threads / (ms * 1e-3) / 1e12;
-  return P2DE_OK;
+  return PROBE_OK;
 }
 
 }  // namespace
 
 extern "C" int p2de_probe_fma_peak(int device, int32_t fp64, double* tflops) {
-  if (!tflops) return P2DE_ERR_INVALID_ARGUMENT;
+  if (!tflops) return PROBE_ERR_ARG;
   return fp64 ? run<double>(device, 4096, tflops) : run<float>(device, 16384, tflops);
 }

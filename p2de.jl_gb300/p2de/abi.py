@@ -180,7 +180,6 @@ EXPORTS = [
     ("p2de_stage_minima", c_int, [SOLVER_P, POINTER(c_double)]),
     ("p2de_profile_steps", c_int, [SOLVER_P, c_int64, POINTER(c_double), POINTER(c_double)]),
     ("p2de_read_counters", c_int, [SOLVER_P, POINTER(ctypes.c_uint64), c_int32]),
-    ("p2de_probe_fma_peak", c_int, [c_int, c_int32, POINTER(c_double)]),
     ("p2de_check_conservation", c_int, [SOLVER_P, POINTER(c_double), POINTER(c_double)]),
     ("p2de_calculate_error", c_int, [SOLVER_P, POINTER(c_double), POINTER(c_double)]),
     ("p2de_set_elements_per_block", c_int, [SOLVER_P, c_int32]),
