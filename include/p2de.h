@@ -25,7 +25,7 @@
 extern "C" {
 #endif
 
-#define P2DE_ABI_VERSION 4
+#define P2DE_ABI_VERSION 5
 
 typedef enum p2de_status {
   P2DE_OK = 0,
@@ -209,8 +209,14 @@ typedef enum p2de_field {
   P2DE_FIELD_RESW = 9,    /* Nq x K SVector{4} */
   P2DE_FIELD_L = 10,      /* K for one stage: ZhangShuLimiter's factor L[k, nstage] before the
                              shock-capture cap (zhangshu.jl:44) */
-  P2DE_FIELD_THETA_LOCAL = 11 /* Nfp x K for one stage: the entropy-projection limiting factor
-                                 theta_local[i, k, nstage] (1 without the limiter) */
+  P2DE_FIELD_THETA_LOCAL = 11, /* Nfp x K for one stage: the entropy-projection limiting factor
+                                  theta_local[i, k, nstage] (1 without the limiter) */
+  /* The subcell fluxes f_bar_H, f_bar_L of the limiter cache (State.jl:131-185) of the last
+   * limited stage (subcell limiter, LimitedDG; accumulate_f_bar!, subcell.jl:163-206): the
+   * reference's tuple of two (Nq+N1D) x K SVector{4} arrays, x then y, one after the other:
+   * F[c + 4*(i + (Nq+N1D)*(k + K*d))], d = 0 (x: face si + (N1D+1) sj), 1 (y: si + N1D sj) */
+  P2DE_FIELD_F_BAR_H = 12,
+  P2DE_FIELD_F_BAR_L = 13
 } p2de_field;
 
 typedef struct p2de_solver p2de_solver;

@@ -111,7 +111,8 @@ class Oracle:
         c = {1: 1, 2: 3}.get(eqn, 4)  # KPP: one component; Dim1: (rho, rhou, E)
         d = 1 if self.dim1 else 2
         return {0: c * Nq * K, 1: c * Nq * K, 2: c * Nq * K, 3: c * Nq * K, 4: d * c * Nq * K, 5: d * c * Nq * K,
-                6: d * c * Nfp * K, 7: d * c * Nfp * K, 8: (Nq + n) * d * K, 9: c * Nq * K, 10: K, 11: Nfp * K}[field]
+                6: d * c * Nfp * K, 7: d * c * Nfp * K, 8: (Nq + n) * d * K, 9: c * Nq * K, 10: K, 11: Nfp * K,
+                12: (Nq + n) * d * K * c, 13: (Nq + n) * d * K * c}[field]
 
     def set_Uq(self, Uq):
         U = np.ascontiguousarray(Uq, dtype=np.float64).ravel()

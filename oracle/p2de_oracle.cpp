@@ -2310,6 +2310,27 @@ int oracle_get_field(oracle_solver* o, int field, int nstage, double* out) {
       std::memcpy(out, s.theta_local.data() + n * (nstage - 1), sizeof(double) * n);
       break;
     }
+    case P2DE_FIELD_F_BAR_H:
+    case P2DE_FIELD_F_BAR_L: {  // f_bar[1] then f_bar[2], each (Nq+N1D) x K (Dim1: f_bar[1] only)
+      const auto& fb = field == P2DE_FIELD_F_BAR_H ? s.f_bar_H : s.f_bar_L;
+      const size_t n = fb[0].size();
+      for (int d = 0; d < s.Nd; ++d) {
+        if (fb[d].size() != n) return P2DE_ERR_INVALID_ARGUMENT;
+        double* o = out + (size_t)d * n * (d1 ? 3 : kpp ? 1 : 4);
+        for (size_t i = 0; i < n; ++i) {
+          if (d1) {
+            o[3 * i] = fb[d][i][0];
+            o[3 * i + 1] = fb[d][i][1];
+            o[3 * i + 2] = fb[d][i][3];
+          } else if (kpp) {
+            o[i] = fb[d][i][0];
+          } else {
+            for (int c = 0; c < 4; ++c) o[4 * i + c] = fb[d][i][c];
+          }
+        }
+      }
+      break;
+    }
     default: return P2DE_ERR_INVALID_ARGUMENT;
   }
   return P2DE_OK;

@@ -492,6 +492,8 @@ int p2de_field_count(int32_t N, int32_t K, int32_t field, int64_t* count) {
     case P2DE_FIELD_L_LOCAL: *count = (Nq + n) * 2 * K; break;
     case P2DE_FIELD_L: *count = K; break;
     case P2DE_FIELD_THETA_LOCAL: *count = Nfp * K; break;
+    case P2DE_FIELD_F_BAR_H:
+    case P2DE_FIELD_F_BAR_L: *count = 4 * (Nq + n) * 2 * K; break;
     default: return P2DE_ERR_INVALID_ARGUMENT;
   }
   return P2DE_OK;
@@ -805,6 +807,24 @@ int p2de_get_field(p2de_solver* s, int32_t field, int32_t nstage, double* out) {
       }
       src = s->theta + (size_t)(nstage - 1) * cnt;
       break;
+    case P2DE_FIELD_F_BAR_H:
+    case P2DE_FIELD_F_BAR_L: {
+      // device layout per element [d][H/L][face][c] (stage kernel A, P12) -> the
+      // reference's f_bar[d][face, k]
+      CK(cudaSetDevice(s->device));
+      const size_t nsf = (size_t)s->N1D * (s->N1D + 1), K = (size_t)s->K;
+      std::vector<double> fb(16 * nsf * K);
+      CK(cudaMemcpyAsync(fb.data(), s->fbar, sizeof(double) * fb.size(), cudaMemcpyDeviceToHost, s->stream));
+      CK(cudaStreamSynchronize(s->stream));
+      const int hl = field == P2DE_FIELD_F_BAR_H ? 0 : 1;
+      const int nc = s->kpp ? 1 : 4;  // KPP: the scalar in component 0
+      for (size_t d = 0; d < 2; ++d)
+        for (size_t k = 0; k < K; ++k)
+          for (size_t f = 0; f < nsf; ++f)
+            for (int c = 0; c < nc; ++c)
+              out[nc * (f + nsf * (k + K * d)) + c] = fb[16 * nsf * k + ((d * 2 + hl) * nsf + f) * 4 + c];
+      return P2DE_OK;
+    }
   }
   CK(cudaSetDevice(s->device));
   const bool state4 = field == P2DE_FIELD_UQ || field == P2DE_FIELD_RHSU || field == P2DE_FIELD_RHSL ||
@@ -885,8 +905,12 @@ int p2de_rhs(p2de_solver* s, double t, double dt, int32_t nstage, double* dt_out
   } else if ((a.flags & F_DO_LOW) && nstage == 1) {
     result = dinit;
   }
+  // a non-positive or NaN state (kernel A's node phase), a NaN CFL candidate or a
+  // non-positive CFL minimum; the reference would stop with a DomainError
   int rc = check_status(s);
-  if (rc == P2DE_ERR_BAD_DT || rc == P2DE_ERR_CUDA) return rc;
+  if (rc != P2DE_OK) return rc;
+  if ((a.flags & F_DO_LOW) && nstage == 1 && !(result > 0.0))
+    return fail(s, P2DE_ERR_BAD_DT, "stage-1 time step %g is not positive", result);
   *dt_out = result;
   return P2DE_OK;
 }

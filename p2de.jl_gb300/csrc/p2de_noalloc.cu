@@ -247,6 +247,7 @@ extern "C" int p2de_rhs_noalloc(const p2de_param* prm, const p2de_device_mesh* m
     dtres = dinit;
   }
   if (cudaStreamSynchronize(st) != cudaSuccess) return P2DE_ERR_CUDA;
+  if (stv & (ST_NOT_POSITIVE | ST_NAN)) return P2DE_ERR_NOT_POSITIVE;
   if (stv & ST_BAD_DT) return P2DE_ERR_BAD_DT;
   *dt_out = dtres;
   return P2DE_OK;

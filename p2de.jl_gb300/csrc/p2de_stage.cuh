@@ -668,6 +668,11 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
     double rho = U[0], rhou = U[1], rhov = U[2], E = U[3];
     double rr = rcp(rho);
     double p = g.gm1 * fma(-0.5, (rhou * rhou + rhov * rhov) * rr, E);
+    // a state the reference would stop on (DomainError from log or sqrt of a negative,
+    // flux_differencing.jl:49-50): density or pressure -0, negative or NaN, by their bits
+    if (__double_as_longlong(rho) <= 0 || __double_as_longlong(rho) > 0x7ff0000000000000LL ||
+        __double_as_longlong(p) <= 0 || __double_as_longlong(p) > 0x7ff0000000000000LL)
+      atomicOr(a.status, ST_NOT_POSITIVE);
     double u = rhou * rr, v = rhov * rr;
     double* F = base + C::O_FLUX + 8 * m;
     double Ep = E + p;

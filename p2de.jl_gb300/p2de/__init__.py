@@ -11,10 +11,13 @@ from .mesh import MeshData, gll_rule, make_periodic, uniform_mesh
 from .problems import primitive_to_conservative
 from .solver import (
     Descriptor,
+    HostState,
+    Preallocation,
     Solver,
     State,
     StateParam,
     SSP33_bang,
+    SSP33_host_loop,
     UnsupportedMethod,
     calculate_error,
     check_conservation,
@@ -39,10 +42,13 @@ __all__ = [
     "uniform_mesh",
     "primitive_to_conservative",
     "Descriptor",
+    "HostState",
+    "Preallocation",
     "Solver",
     "State",
     "StateParam",
     "SSP33_bang",
+    "SSP33_host_loop",
     "UnsupportedMethod",
     "calculate_error",
     "check_conservation",

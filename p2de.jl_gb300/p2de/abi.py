@@ -68,6 +68,8 @@ FIELD_L_LOCAL = 8
 FIELD_RESW = 9
 FIELD_L = 10
 FIELD_THETA_LOCAL = 11
+FIELD_F_BAR_H = 12  # f_bar_H of the last limited stage: 2 x (Nq+N1D) x K states, x then y
+FIELD_F_BAR_L = 13
 # p2de_equation
 EQUATION_COMPRESSIBLE_EULER = 0
 EQUATION_KPP = 1

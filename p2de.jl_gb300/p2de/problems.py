@@ -213,6 +213,20 @@ def sedov(N=3, Kx=80, Ky=80, T=1.0, rhs_limiter=None, reference_semantics=True, 
     return param, initial_condition, periodic_bc, exact
 
 
+def sedov_lgl(N=3, Kx=16, Ky=16, T=0.05, r_ini=0.3, **kw):
+    """The Sedov initial data of examples/2D/sedov.jl:9-20 (rho 1 at rest, pressure
+    (gamma - 1) / (pi r_ini^2) inside r < r_ini and 1e-5 outside) on the periodic
+    [-1.5, 1.5]^2 with LGL nodes and the default method of default_param (subcell limiter),
+    r_ini wide enough to cover a few elements: a blast that keeps the limiter busy."""
+    param = default_param(N, (Kx, Ky), (-1.5, -1.5), (1.5, 1.5), T, **kw)
+    exact = sedov_exact(param.equation.gamma, r_ini=r_ini)
+
+    def initial_condition(param, x, y):
+        return primitive_to_conservative(param.equation, exact(param.equation, x, y, 0.0))
+
+    return param, initial_condition, periodic_bc
+
+
 def kpp_exact(equation=None, x=None, y=None, t=0.0):
     """exact_sol of examples/2D/KPP.jl:9-16 (the initial data): 7 pi / 2 in the unit disc,
     pi / 4 outside."""

@@ -367,11 +367,83 @@ def initialize_DG(param: Param, initial_condition, initial_boundary_conditions, 
     return solver, state, StateParam(bcdata)
 
 
-def rhs_bang(state: State, solver: Solver, state_param: StateParam, time_param: TimeParam) -> float:
-    """rhs!(state, solver, state_param, time_param) (rhs.jl:5-13): fills rhsU, returns dt."""
+@dataclass
+class Preallocation:
+    """The members of Preallocation (State.jl:1-26) that SSP33! and its callers read and
+    write, as host arrays: Uq, rhsU, resW, resZ (K, Nq, Nc) and L_local (Ns, K, Nd, Nq+N1D)."""
+
+    Uq: np.ndarray
+    rhsU: np.ndarray
+    resW: np.ndarray
+    resZ: np.ndarray
+    L_local: np.ndarray
+
+
+class HostState:
+    """State (State.jl:258-261) holding host arrays, as the reference's does: the caller
+    mutates preallocation.Uq between right-hand-side evaluations (SSP33!, SSPRK33.jl:30-39),
+    and rhs_bang uploads Uq before and downloads rhsU and the stage's L_local after the
+    device evaluation."""
+
+    def __init__(self, solver, Uq: np.ndarray):
+        """solver: a Solver, or anything with param, K, Nq, N1D and desc (Descriptor)."""
+        nc = num_components(solver.param.equation)
+        U = np.array(Uq, dtype=np.float64).reshape(solver.K, solver.Nq, nc)
+        nd = 1 if solver.desc.dim1 else 2
+        self.preallocation = Preallocation(
+            Uq=U, rhsU=np.zeros_like(U), resW=np.zeros_like(U), resZ=np.zeros_like(U),
+            L_local=np.ones((3, solver.K, nd, solver.Nq + solver.N1D)))
+
+
+def rhs_bang(state, solver: Solver, state_param: StateParam, time_param: TimeParam) -> float:
+    """rhs!(state, solver, state_param, time_param) (rhs.jl:5-13): fills rhsU, returns dt.
+
+    With a HostState, Uq is read from state.preallocation.Uq and rhsU (and, under the
+    subcell limiter, L_local[:, :, :, nstage]) written back to it, so host code that changes
+    Uq between stages sees the reference's behaviour. With a device-resident State (or
+    None) the device Uq is used as it is."""
+    host = isinstance(state, HostState)
+    if host:
+        solver.set_Uq(state.preallocation.Uq)
     out = c_double()
     solver._check(solver.lib.p2de_rhs(solver.handle, time_param.t, time_param.dt, time_param.nstage, byref(out)))
+    if host:
+        pre = state.preallocation
+        pre.rhsU[...] = solver.get_field(abi.FIELD_RHSU).reshape(pre.rhsU.shape)
+        lim = solver.param.rhs_limiter
+        if isinstance(solver.param.rhs, ESLimitedLowOrderPos) and isinstance(lim, SubcellLimiter):
+            s = time_param.nstage - 1
+            pre.L_local[s] = solver.get_field(abi.FIELD_L_LOCAL, time_param.nstage).reshape(pre.L_local[s].shape)
     return out.value
+
+
+def SSP33_host_loop(state: HostState, solver, state_param: StateParam, nsteps: int | None = None, rhs=None,
+                    t_start: float | None = None):
+    """The time loop of SSP33! (SSPRK33.jl:25-41) written over host arrays, calling rhs!
+    (rhs_bang unless `rhs` is given) three times per step exactly as the reference does:
+    resW = Uq; dt = rhs!(stage 1); Uq = resW + dt rhsU; rhs!(stage 2); resZ = Uq + dt rhsU;
+    Uq = 3/4 resW + 1/4 resZ; rhs!(stage 3); resZ = Uq + dt rhsU; Uq = 1/3 resW + 2/3 resZ.
+    Starts at t_start (default t0) and stops at T or after nsteps steps; returns
+    (t, dt history)."""
+    rhs_bang_ = rhs if rhs is not None else rhs_bang
+    ts = solver.param.timestepping_param
+    pre = state.preallocation
+    t = ts.t0 if t_start is None else t_start
+    dthist = []
+    while t < ts.T and (nsteps is None or len(dthist) < nsteps):
+        dt = min(ts.CFL * ts.dt0, ts.T - t)
+        pre.resW[...] = pre.Uq
+        dt = rhs_bang_(state, solver, state_param, TimeParam(t, dt, 1))
+        pre.Uq[...] = pre.resW + dt * pre.rhsU
+        rhs_bang_(state, solver, state_param, TimeParam(t, dt, 2))
+        pre.resZ[...] = pre.Uq + dt * pre.rhsU
+        pre.Uq[...] = 3 / 4 * pre.resW + 1 / 4 * pre.resZ
+        rhs_bang_(state, solver, state_param, TimeParam(t, dt, 3))
+        pre.resZ[...] = pre.Uq + dt * pre.rhsU
+        pre.Uq[...] = 1 / 3 * pre.resW + 2 / 3 * pre.resZ
+        t = t + dt
+        dthist.append(dt)
+    return t, dthist
 
 
 def ssp33_step(solver: Solver, t: float) -> tuple[float, float]:
