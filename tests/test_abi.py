@@ -34,7 +34,7 @@ def test_library_exports_every_declared_symbol():
     for name in declared_functions():
         assert hasattr(lib, name), name
     lib2 = abi.load_library()
-    assert lib2.p2de_abi_version() == 4
+    assert lib2.p2de_abi_version() == 5
 
 
 def test_field_counts():
