@@ -64,21 +64,25 @@ def fma_probe_library():
     return lib
 
 
-def workload(name: str, precision: str, basis: str = "lobatto"):
+def workload(name: str, precision: str, basis: str = "lobatto", mesh: str = ""):
+    """The benchmark's workloads; mesh "KXxKY" replaces the double Mach reflection's 480x120
+    (a smaller case for profiler captures)."""
     from p2de import problems
     from p2de.types import GaussCollocation, NodewiseScaledExtrapolation, PositivityBound, SubcellLimiter
+
+    kx, ky = (480, 120) if not mesh else tuple(int(v) for v in mesh.lower().split("x"))
 
     if name == "dmr" and basis == "gauss":
         # the reference's Gauss configuration (examples/2D/kelvin-helmholtz.jl:44-55):
         # GaussCollocation, NodewiseScaledExtrapolation, SubcellLimiter(PositivityBound)
         param, ic, bcf = problems.double_mach_reflection(
-            N=3, Kx=480, Ky=120, T=0.2, precision=precision, approximation_basis=GaussCollocation(),
+            N=3, Kx=kx, Ky=ky, T=0.2, precision=precision, approximation_basis=GaussCollocation(),
             entropyproj_limiter=NodewiseScaledExtrapolation(), rhs_limiter=SubcellLimiter(bound=PositivityBound()))
-        desc = ("double Mach reflection 480x120 quads, N=3, SSP-RK3 CFL 0.5, GaussCollocation + "
+        desc = (f"double Mach reflection {kx}x{ky} quads, N=3, SSP-RK3 CFL 0.5, GaussCollocation + "
                 "NodewiseScaledExtrapolation, positivity bound")
     elif name == "dmr":
-        param, ic, bcf = problems.double_mach_reflection(N=3, Kx=480, Ky=120, T=0.2, precision=precision)
-        desc = "double Mach reflection 480x120 quads, N=3, SSP-RK3 CFL 0.5"
+        param, ic, bcf = problems.double_mach_reflection(N=3, Kx=kx, Ky=ky, T=0.2, precision=precision)
+        desc = f"double Mach reflection {kx}x{ky} quads, N=3, SSP-RK3 CFL 0.5"
     elif name == "kh256":
         param, ic, bcf = problems.kelvin_helmholtz(N=3, Kx=256, Ky=256, T=1.0, precision=precision)
         desc = "Kelvin-Helmholtz 256x256 quads, N=3, SSP-RK3 CFL 0.5"
@@ -195,7 +199,7 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    param, ic, bcf, wdesc = workload(args.workload, "fp64", args.basis)
+    param, ic, bcf, wdesc = workload(args.workload, "fp64", args.basis, args.mesh)
     md, bc, desc, U0 = build_descriptor(param, ic, bcf)
     from oracle.binding import Oracle, num_threads
 
@@ -628,6 +632,7 @@ def main():
                     help="gauss: the DMR step with GaussCollocation + NodewiseScaledExtrapolation")
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--mesh", default="", help="dmr: KXxKY instead of 480x120 (smaller profiler captures)")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--serve-rates", default="20,100,500")
     ap.add_argument("--serve-requests", type=int, default=100)
@@ -669,7 +674,7 @@ def main():
 
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
 
-    param, ic, bcf, wdesc = workload(args.workload, args.precision, args.basis)
+    param, ic, bcf, wdesc = workload(args.workload, args.precision, args.basis, args.mesh)
     md, bc, desc, U0 = build_descriptor(param, ic, bcf)
     nodes = desc.K * desc.Nq
     solver = S.Solver(param, md, desc, device=local)
@@ -748,6 +753,46 @@ def main():
     mins = np.zeros(6)
     solver._check(lib.p2de_stage_minima(solver.handle, abi.dptr(mins)))
 
+    # ---- the same workload under the intended limiter semantics (the 5-tuple bound read
+    #      with five names, so the positivity and cell-entropy limiting is active rather than
+    #      the first-order scheme the reference's 4-name destructuring gives): same launch
+    #      shape, warm-up and step count, CUDA events on the launching stream
+    intended = None
+    if param.reference_semantics:
+        from dataclasses import replace as dc_replace
+
+        p_int = dc_replace(param, reference_semantics=False)
+        d_int = S.make_descriptor(p_int, md, bc)
+        si = S.Solver(p_int, md, d_int, device=local)
+        si._check(lib.p2de_set_stream(si.handle, ctypes.c_void_p(stream.cuda_stream)))
+        si.set_Uq(U0)
+        si.set_elements_per_block(epb)
+        si.set_layout(solver.layout())
+        ti, ni = c_double(0.0), c_int64()
+        si._check(lib.p2de_ssp33_advance(si.handle, args.warmup, byref(ti), byref(ni)))
+        barrier()
+        e4, e5 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e4.record(stream)
+        si._check(lib.p2de_ssp33_advance(si.handle, args.steps, byref(ti), byref(ni)))
+        e5.record(stream)
+        torch.cuda.synchronize()
+        ms_int = e4.elapsed_time(e5)
+        if dist is not None:
+            mt = torch.tensor([ms_int], device="cuda")
+            dist.all_reduce(mt, op=dist.ReduceOp.MAX)
+            ms_int = float(mt.item())
+        mins_i = np.zeros(6)
+        si._check(lib.p2de_stage_minima(si.handle, abi.dptr(mins_i)))
+        intended = {
+            "value": world * nodes * 3 * ni.value / (ms_int * 1e-3),
+            "unit": UNIT,
+            "ms_per_step": ms_int / max(ni.value, 1),
+            "steps": ni.value,
+            "limiter": "positivity + cell entropy, bound tuple read with five names (reference_semantics = 0)",
+            "min_rho_rhoe_last_step": [float(mins_i[4]), float(mins_i[5])],
+        }
+        si.close()
+
     if rank == 0:
         cpu = None
         if not args.no_cpu_baseline:
@@ -776,6 +821,7 @@ def main():
                 "timing": "CUDA-graph replay of whole steps, CUDA events on the launching stream",
                 "elements_per_block": epb,
                 "elements_per_block_source": "default" if args.no_autotune else f"autotuned (default {epb_default})",
+                "layout": ["flat", "lines per warp"][solver.layout()],
             },
             "e2e": {
                 "value": e2e_value,
@@ -803,6 +849,7 @@ def main():
                 "peak_source": "libp2de_probe.so p2de_probe_fma_peak: FP64 FMA chains on this GPU in this run (MEASURED_PEAKS.json has no FP64 figure)",
             },
             "min_rho_rhoe_last_step": [float(mins[4]), float(mins[5])],
+            "intended_semantics": intended,
             "cpu_baseline": cpu,
         }
         print(json.dumps(line), flush=True)

@@ -299,13 +299,28 @@ int p2de_profile_steps(p2de_solver* s, int64_t nsteps, double* t, double ms[3]);
  * solves evaluated (limiter_utils.jl:108-132); the others are skipped exactly. */
 int p2de_read_counters(p2de_solver* s, uint64_t out[1], int32_t reset);
 
+/* Thread layouts of the high-order volume phases of stage kernel A (the two-point fluxes
+ * of every node pair of a line and their gather into each node). Results do not depend on
+ * the layout: each pair and each node half is computed by the same code in both. No
+ * counterpart in the reference (a launch parameter of this implementation). */
+typedef enum p2de_layout {
+  P2DE_LAYOUT_FLAT = 0,          /* flat loops over (element, pair) and (element, node) */
+  P2DE_LAYOUT_LINES_PER_WARP = 1 /* whole 1D lines per warp: a warp computes the pairs of its
+                                    lines, synchronizes only itself and gathers its lines'
+                                    nodes (axis-aligned LGL elements; others run flat) */
+} p2de_layout;
+
+int p2de_set_layout(p2de_solver* s, int32_t layout);
+int p2de_get_layout(p2de_solver* s, int32_t* layout);
+
 /* Elements per thread block of the stage kernels (1..epb_max, the shared-memory limit).
  * Results do not depend on it: each element's arithmetic is the same at every value.
  * No counterpart in the reference (a launch parameter of this implementation). */
 int p2de_set_elements_per_block(p2de_solver* s, int32_t epb);
 int p2de_get_elements_per_block(p2de_solver* s, int32_t* epb, int32_t* epb_max);
-/* Times stage kernel A at candidate elements-per-block (stage scratch only: the
- * state is unchanged), keeps the fastest and returns it with its milliseconds. */
+/* Times stage kernel A at candidate elements-per-block and thread layouts (stage scratch
+ * only: the state is unchanged), keeps the fastest pair and returns its elements per block
+ * and milliseconds; p2de_get_layout gives the layout kept. */
 int p2de_autotune(p2de_solver* s, int32_t* best_epb, double* best_ms);
 
 /* ---- Batches of independent solves ---------------------------------------------------
@@ -339,9 +354,13 @@ int p2de_batch_last_error(p2de_batch* b, char* buf, size_t len);
  * results do not depend on it. */
 int p2de_batch_set_elements_per_block(p2de_batch* b, int32_t N, int32_t epb);
 int p2de_batch_get_elements_per_block(p2de_batch* b, int32_t N, int32_t* epb, int32_t* epb_max);
+/* Thread layout (p2de_layout) of the batch's tasks for degree N; results do not depend on it. */
+int p2de_batch_set_layout(p2de_batch* b, int32_t N, int32_t layout);
+int p2de_batch_get_layout(p2de_batch* b, int32_t N, int32_t* layout);
 /* Per degree present, times batched stage kernel A over that degree's members at
- * candidate elements-per-block (no state changes) and keeps the fastest;
- * best_epb[N-1] receives it (0 for absent degrees). */
+ * candidate elements-per-block and thread layouts (no state changes) and keeps the
+ * fastest; best_epb[N-1] receives its elements per block (0 for absent degrees) and
+ * p2de_batch_get_layout its layout. */
 int p2de_batch_autotune(p2de_batch* b, int32_t best_epb[5]);
 
 /* ---- Continuous-batching server -------------------------------------------------------

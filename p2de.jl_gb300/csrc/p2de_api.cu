@@ -83,38 +83,10 @@ __global__ void k_geom_table(const double* geom, int K, double* out) {
   geom_factor(geom + 5 * (size_t)k, q, out + (size_t)k * kGeomStride);
 }
 
-// initialize_s_modified! (subcell.jl:21-35): at t == t0, stage 1, the minimum of
-// phi = rhoe rho^(-gamma) over every node (NaN if any is NaN, as Julia's minimum). One
-// block of 1024 threads, so the result does not depend on the order of atomics.
+// initialize_s_modified! (subcell.jl:21-35) for one solve (phi_min_body, one block of 1024)
 __global__ void __launch_bounds__(1024) k_phi_min(const double* Uq, size_t nodes, double gamma, const double* scal,
                                                   double t0, double* out) {
-  if (scal[S_DONE] != 0.0 || scal[S_T] != t0) return;
-  __shared__ double wmin[32];
-  __shared__ int wnan[32];
-  double m = INFINITY;
-  int isn = 0;
-  for (size_t i = threadIdx.x; i < nodes; i += blockDim.x) {
-    const double* U = Uq + 4 * i;
-    const double v = s_modified(U[0], U[1], U[2], U[3], gamma);
-    if (isnan(v)) isn = 1;
-    else m = fmin(m, v);
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    m = fmin(m, __shfl_xor_sync(0xffffffffu, m, o));
-    isn |= __shfl_xor_sync(0xffffffffu, isn, o);
-  }
-  if ((threadIdx.x & 31) == 0) {
-    wmin[threadIdx.x >> 5] = m;
-    wnan[threadIdx.x >> 5] = isn;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
-      m = fmin(m, wmin[w]);
-      isn |= wnan[w];
-    }
-    *out = isn ? NAN : m;
-  }
+  phi_min_body(Uq, nodes, gamma, scal, t0, out);
 }
 
 double key_to_double(long long k) {
@@ -126,30 +98,41 @@ double key_to_double(long long k) {
 
 // --- operator tables per device -------------------------------------------------------
 
+// The tables depend on the degree, the basis and ZEROTOL (build_op_table drops entries at
+// or below it), so each device keeps one set per ZEROTOL value in use, until exit.
 struct DeviceTables {
-  OpTable* d_tables = nullptr;  // index N1D - 2
-  bool ready = false;
+  uint64_t zerotol_bits = 0;
+  OpTable* d_tables = nullptr;  // LGL N1D = 2..6, then Gauss N1D = 2..6
 };
 std::mutex g_tab_mu;
-DeviceTables g_tabs[64];
+std::vector<DeviceTables> g_tabs[64];
 
 cudaError_t device_tables(int dev, double zerotol, OpTable** out) {
   std::lock_guard<std::mutex> lk(g_tab_mu);
   if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
-  DeviceTables& t = g_tabs[dev];
-  if (!t.ready) {
-    // LGL tables for N1D = 2..6, then the Gauss tables in the same order
-    std::vector<OpTable> h(2 * (kMaxN1D - 1));
-    for (int N = 1; N < kMaxN1D; ++N) {
-      build_op_table(N, zerotol, &h[N - 1], 0);
-      build_op_table(N, zerotol, &h[kMaxN1D - 1 + N - 1], 1);
+  uint64_t bits;
+  std::memcpy(&bits, &zerotol, sizeof bits);
+  for (const DeviceTables& t : g_tabs[dev])
+    if (t.zerotol_bits == bits) {
+      *out = t.d_tables;
+      return cudaSuccess;
     }
-    cudaError_t e = cudaMalloc(&t.d_tables, sizeof(OpTable) * h.size());
-    if (e != cudaSuccess) return e;
-    e = cudaMemcpy(t.d_tables, h.data(), sizeof(OpTable) * h.size(), cudaMemcpyHostToDevice);
-    if (e != cudaSuccess) return e;
-    t.ready = true;
+  // LGL tables for N1D = 2..6, then the Gauss tables in the same order
+  std::vector<OpTable> h(2 * (kMaxN1D - 1));
+  for (int N = 1; N < kMaxN1D; ++N) {
+    build_op_table(N, zerotol, &h[N - 1], 0);
+    build_op_table(N, zerotol, &h[kMaxN1D - 1 + N - 1], 1);
   }
+  DeviceTables t;
+  t.zerotol_bits = bits;
+  cudaError_t e = cudaMalloc(&t.d_tables, sizeof(OpTable) * h.size());
+  if (e != cudaSuccess) return e;
+  e = cudaMemcpy(t.d_tables, h.data(), sizeof(OpTable) * h.size(), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    cudaFree(t.d_tables);
+    return e;
+  }
+  g_tabs[dev].push_back(t);
   *out = t.d_tables;
   return cudaSuccess;
 }
@@ -1087,6 +1070,27 @@ int p2de_set_elements_per_block(p2de_solver* s, int32_t epb) {
   return P2DE_OK;
 }
 
+int p2de_set_layout(p2de_solver* s, int32_t layout) {
+  if (!s) return P2DE_ERR_INVALID_ARGUMENT;
+  if (s->line) return fail(s, P2DE_ERR_UNSUPPORTED, "the Line path runs one element per thread");
+  if (layout != P2DE_LAYOUT_FLAT && layout != P2DE_LAYOUT_LINES_PER_WARP)
+    return fail(s, P2DE_ERR_INVALID_ARGUMENT, "layout %d", layout);
+  CK(cudaSetDevice(s->device));
+  CK(cudaStreamSynchronize(s->stream));
+  s->base.layout = layout;
+  if (s->graph) {
+    cudaGraphExecDestroy(s->graph);
+    s->graph = nullptr;
+  }
+  return P2DE_OK;
+}
+
+int p2de_get_layout(p2de_solver* s, int32_t* layout) {
+  if (!s || !layout) return P2DE_ERR_INVALID_ARGUMENT;
+  *layout = s->base.layout;
+  return P2DE_OK;
+}
+
 int p2de_get_elements_per_block(p2de_solver* s, int32_t* epb, int32_t* epb_max) {
   if (!s) return P2DE_ERR_INVALID_ARGUMENT;
   if (epb) *epb = s->base.epb;
@@ -1095,7 +1099,7 @@ int p2de_get_elements_per_block(p2de_solver* s, int32_t* epb, int32_t* epb_max) 
 }
 
 // Times stage kernel A (stage 2 flags, state left unchanged: no update) for each
-// candidate elements-per-block and keeps the fastest.
+// candidate elements-per-block and thread layout and keeps the fastest.
 int p2de_autotune(p2de_solver* s, int32_t* best_epb, double* best_ms) {
   if (!s) return P2DE_ERR_INVALID_ARGUMENT;
   if (s->line) return fail(s, P2DE_ERR_UNSUPPORTED, "the Line path runs one element per thread");
@@ -1104,6 +1108,11 @@ int p2de_autotune(p2de_solver* s, int32_t* best_epb, double* best_ms) {
   std::vector<int> cand;
   for (int e : {1, 2, 3, 4, 6, 8, 12, 16, 24, 32, edef})
     if (e <= emax && std::find(cand.begin(), cand.end(), e) == cand.end()) cand.push_back(e);
+  // the lines-per-warp layout differs from the flat one on axis-aligned LGL elements only
+  std::vector<int> layouts{P2DE_LAYOUT_FLAT};
+  if (!s->gauss && !s->kpp && (flags_for(s, 2, false, false) & F_AXIS_ALIGNED))
+    layouts.push_back(P2DE_LAYOUT_LINES_PER_WARP);
+  int best_layout = s->base.layout;
   double sc[S_NSCAL] = {0};
   CK(cudaMemcpyAsync(sc, s->scal, sizeof sc, cudaMemcpyDeviceToHost, s->stream));
   CK(cudaStreamSynchronize(s->stream));
@@ -1119,9 +1128,11 @@ int p2de_autotune(p2de_solver* s, int32_t* best_epb, double* best_ms) {
   auto timings = [&]() -> int {
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
+  for (int lay : layouts)
   for (int e : cand) {
     StageArgs a = s->base;
     a.epb = e;
+    a.layout = lay;
     a.nstage = 2;
     a.flags = flags_for(s, 2, false, false);
     float tot = 0.f;
@@ -1139,6 +1150,7 @@ int p2de_autotune(p2de_solver* s, int32_t* best_epb, double* best_ms) {
     if (ms < bms) {
       bms = ms;
       best = e;
+      best_layout = lay;
     }
   }
   return P2DE_OK;
@@ -1149,7 +1161,8 @@ int p2de_autotune(p2de_solver* s, int32_t* best_epb, double* best_ms) {
   CK(cudaMemcpyAsync(s->scal, keep, sizeof keep, cudaMemcpyHostToDevice, s->stream));
   CK(cudaStreamSynchronize(s->stream));
   if (rt != P2DE_OK) return rt;
-  int rc = p2de_set_elements_per_block(s, best);
+  int rc = p2de_set_layout(s, best_layout);
+  if (rc == P2DE_OK) rc = p2de_set_elements_per_block(s, best);
   if (best_epb) *best_epb = best;
   if (best_ms) *best_ms = bms;
   return rc;

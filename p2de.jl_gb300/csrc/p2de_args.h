@@ -51,6 +51,9 @@ struct StageArgs {
   int nstage;  // 1..3
   int flags;
   int epb;  // elements per block (<= the degree's maximum, Cfg::E_MAX)
+  // thread layout of the high-order pair and gather phases (p2de_layout): 0 flat (element,
+  // pair) and (element, node) loops; 1 whole lines per warp on axis-aligned LGL elements
+  int layout;
   const OpTable* ops;
   double* Uq;
   double* resW;

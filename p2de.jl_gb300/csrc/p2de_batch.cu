@@ -102,7 +102,8 @@ class Pool {
 
 // offsets of a solve's arrays inside its pool block
 struct Layout {
-  size_t Uq, resW, rhsU, rhsL, rhsH, geom, geomx, fbar, Lpre, Lfin, Ival, xyS, nbr, bcidx, bc, total;
+  size_t Uq, resW, rhsU, rhsL, rhsH, geom, geomx, fbar, Lpre, Lfin, Ival, xyS, nbr, bcidx, bc, rhoL, Lelem, phimin,
+      total;
 };
 
 Layout layout_for(const p2de_param& p, int64_t nI, int64_t nS) {
@@ -130,17 +131,54 @@ Layout layout_for(const p2de_param& p, int64_t nI, int64_t nS) {
   L.nbr = take(4 * Nfp * K);
   L.bcidx = take(4 * Nfp * K);
   L.bc = take(Nfp * K);
+  // TVD bounds: the low-order densities; Zhang-Shu: the per-element factors of the three
+  // stages; min-entropy bounds: the initial minimum of phi
+  const bool tvd = p.rhs_limiter == P2DE_LIMITER_SUBCELL && (bound_flags(p.bound_type) & F_TVD);
+  L.rhoL = take(tvd ? 8 * Nq * K : 8);
+  L.Lelem = take(p.rhs_limiter == P2DE_LIMITER_ZHANG_SHU ? 8 * 3 * K : 8);
+  L.phimin = take(8);
   L.total = o;
   return L;
+}
+
+// The flags of a member as the one-solve path sets them for its stage kernels (without
+// the stage-dependent F_CFL, F_UPDATE and the debug outputs), so that each member runs the
+// same arithmetic in the batch as alone.
+int member_flags(const p2de_param& p, bool axis_aligned, int precision) {
+  int f = 0;
+  switch (p.rhs_type) {
+    case P2DE_RHS_LOW_ORDER_POSITIVITY: f |= F_DO_LOW | F_RHSU_FROM_L; break;
+    case P2DE_RHS_ENTROPY_STABLE: f |= F_DO_HIGH | F_RHSU_FROM_H; break;
+    default: f |= F_DO_LOW | F_DO_HIGH | F_DO_LIMIT; break;
+  }
+  if (axis_aligned) f |= F_AXIS_ALIGNED;
+  if (f & F_DO_LIMIT) {
+    if (p.rhs_limiter == P2DE_LIMITER_ZHANG_SHU) {
+      f = (f & ~F_DO_LIMIT) | F_ZHANG_SHU;
+    } else {
+      f |= bound_flags(p.bound_type);
+      if (p.reference_semantics && !(f & F_MIN_ENTROPY)) f |= F_REF_SEM;
+    }
+  }
+  if (precision == P2DE_PRECISION_MIXED_ACC64) f |= F_ACC64;
+  if (p.shock_capture == 1 && (f & (F_DO_LIMIT | F_ZHANG_SHU))) f |= F_SHOCK;
+  if (p.low_order_surface_flux == P2DE_FLUX_LAX_FRIEDRICHS_ON_PROJECTED_VAL) f |= F_LFPROJ;
+  return f;
 }
 
 struct Slot {
   bool active = false;
   p2de_param prm{};
   int n1d = 0;
+  int flags = 0;  // member_flags
   size_t off = 0;
   Layout lay{};
 };
+
+// Task segments of a batch: the members' tasks for the plain and the EXT instantiation of
+// kernel A, then the same members' tasks again for the low-only pass of the TVD bounds.
+// Kernel B runs over segments 0 and 1, which are contiguous.
+enum : int { SEG_PLAIN = 0, SEG_EXT = 1, SEG_LOW_PLAIN = 2, SEG_LOW_EXT = 3, NSEG = 4 };
 
 double now_s() {
   using namespace std::chrono;
@@ -168,12 +206,19 @@ struct p2de_batch {
   long long* d_minrec = nullptr;
   int* d_status = nullptr;
   unsigned long long* d_work = nullptr;
+  // operator tables by ZEROTOL (build_op_table drops entries at or below it): group g
+  // holds N1D = 2..6 for the value whose bits are table_zerotol[g]
   OpTable* d_tables = nullptr;
+  std::vector<uint64_t> table_zerotol;
   int task_cap = 0;
   int sms = 0;
-  int grid_a = 0, grid_b = 0;
-  size_t smem_a = 0, smem_b = 0;  // launch shared memory of the captured graph
+  int grid_a = 0, grid_x = 0, grid_b = 0;
+  // launch shared memory of the captured graph: plain and EXT kernel A, kernel B
+  size_t smem_a = 0, smem_x = 0, smem_b = 0;
+  int seg_off[NSEG] = {}, seg_cnt[NSEG] = {};  // task segments (offsets into d_tasks)
+  bool phi_min = false;                         // some member needs the initial min of phi
   int epb[kMaxN1D + 1] = {};     // elements per block per N1D
+  int layout[kMaxN1D + 1] = {};  // thread layout (p2de_layout) per N1D
   cudaGraphExec_t graph = nullptr;
   bool tasks_dirty = true;
   int64_t launches = 0;
@@ -182,6 +227,27 @@ struct p2de_batch {
 };
 
 namespace {
+
+constexpr int kBatchTableGroups = 8;  // distinct ZEROTOL values one batch can hold
+
+// The table group of b for ZEROTOL value z, built and uploaded on first use; -1 when all
+// groups are taken or the upload fails.
+int batch_table_group(p2de_batch* b, double z) {
+  uint64_t bits;
+  std::memcpy(&bits, &z, sizeof bits);
+  for (size_t g = 0; g < b->table_zerotol.size(); ++g)
+    if (b->table_zerotol[g] == bits) return (int)g;
+  if ((int)b->table_zerotol.size() >= kBatchTableGroups) return -1;
+  std::vector<OpTable> tabs(kMaxN1D - 1);
+  for (int N = 1; N < kMaxN1D; ++N) build_op_table(N, z, &tabs[N - 1]);
+  const size_t g = b->table_zerotol.size();
+  if (cudaMemcpyAsync(b->d_tables + g * (kMaxN1D - 1), tabs.data(), sizeof(OpTable) * tabs.size(),
+                      cudaMemcpyHostToDevice, b->stream) != cudaSuccess ||
+      cudaStreamSynchronize(b->stream) != cudaSuccess)
+    return -1;
+  b->table_zerotol.push_back(bits);
+  return (int)g;
+}
 
 int bfail(p2de_batch* b, int code, const char* fmt, ...) {
   char buf[512];
@@ -221,12 +287,18 @@ int validate_solve(const p2de_param* p, const p2de_mesh* m, std::string& why) {
     why = "N outside 1..5 or K < 1";
     return P2DE_ERR_INVALID_ARGUMENT;
   }
-  if (p->low_order_surface_flux != P2DE_FLUX_LAX_FRIEDRICHS_ON_NODAL_VAL ||
+  // every bound and RHS limiter of the one-solve path on LGL nodes for 2D Euler; Gauss
+  // collocation (its face projection and interface launches) and KPP run one solve per handle
+  if ((p->low_order_surface_flux != P2DE_FLUX_LAX_FRIEDRICHS_ON_NODAL_VAL &&
+       p->low_order_surface_flux != P2DE_FLUX_LAX_FRIEDRICHS_ON_PROJECTED_VAL) ||
       p->high_order_surface_flux != P2DE_FLUX_LAX_FRIEDRICHS_ON_PROJECTED_VAL || p->rhs_type < 0 || p->rhs_type > 2 ||
-      p->bound_type < 0 || p->bound_type > 1 || p->shock_capture < 0 || p->shock_capture > 1 ||
-      p->rhs_limiter != P2DE_LIMITER_SUBCELL || p->approximation_basis != P2DE_BASIS_LOBATTO ||
-      p->equation != P2DE_EQUATION_COMPRESSIBLE_EULER) {
+      p->bound_type < 0 || p->bound_type > 9 || p->shock_capture < 0 || p->shock_capture > 1 ||
+      (p->rhs_limiter != P2DE_LIMITER_SUBCELL && p->rhs_limiter != P2DE_LIMITER_ZHANG_SHU)) {
     why = "unsupported method";
+    return P2DE_ERR_UNSUPPORTED;
+  }
+  if (p->approximation_basis != P2DE_BASIS_LOBATTO || p->equation != P2DE_EQUATION_COMPRESSIBLE_EULER) {
+    why = "batches run 2D Euler on LGL nodes; GaussCollocation and KPP solves run one per handle";
     return P2DE_ERR_UNSUPPORTED;
   }
   const int64_t nfk = (int64_t)4 * (p->N + 1) * p->K;
@@ -255,33 +327,58 @@ int validate_solve(const p2de_param* p, const p2de_mesh* m, std::string& why) {
   return P2DE_OK;
 }
 
-std::vector<BatchTask> build_tasks(const p2de_batch* b, size_t* smem_a, size_t* smem_b) {
-  std::vector<BatchTask> t;
-  *smem_a = 0;
-  *smem_b = 0;
+// The tasks of one member: elements in runs of the degree's elements per block.
+void member_tasks(const p2de_batch* b, int s, std::vector<BatchTask>& t) {
+  const Slot& sl = b->slots[s];
+  const int E = b->epb[sl.n1d];
+  for (int k0 = 0; k0 < sl.prm.K; k0 += E) t.push_back(BatchTask{s, k0, sl.n1d, E, b->layout[sl.n1d]});
+}
+
+// The task list in its segments, largest tasks first within each (work per task grows
+// with elements * N1D^3), and the kernels' shared memory for each instantiation.
+std::vector<BatchTask> build_tasks(p2de_batch* b, size_t* smem_a, size_t* smem_x, size_t* smem_b) {
+  std::vector<BatchTask> seg[NSEG];
+  *smem_a = *smem_x = *smem_b = 0;
   for (int s = 0; s < b->max_solves; ++s) {
     const Slot& sl = b->slots[s];
     if (!sl.active) continue;
-    int E = b->epb[sl.n1d];
-    *smem_a = std::max(*smem_a, batch_smem_a(sl.n1d, E));
+    const bool ext = sl.flags & kExtFlags, tvd = sl.flags & F_TVD;
+    const int E = b->epb[sl.n1d];
+    (ext ? *smem_x : *smem_a) = std::max(ext ? *smem_x : *smem_a, batch_smem_a(sl.n1d, E, ext));
     *smem_b = std::max(*smem_b, batch_smem_b(sl.n1d, E));
-    for (int k0 = 0; k0 < sl.prm.K; k0 += E) t.push_back(BatchTask{s, k0, sl.n1d, E});
+    member_tasks(b, s, seg[ext ? SEG_EXT : SEG_PLAIN]);
+    if (tvd) member_tasks(b, s, seg[ext ? SEG_LOW_EXT : SEG_LOW_PLAIN]);
   }
-  // largest tasks first (work per task grows with elements * N1D^3)
-  std::stable_sort(t.begin(), t.end(), [](const BatchTask& x, const BatchTask& y) {
-    auto cost = [](const BatchTask& q) { return q.epb * q.n1d * q.n1d * q.n1d; };
-    return cost(x) > cost(y);
-  });
-  if (*smem_a == 0) *smem_a = batch_smem_a(2, 1);
+  std::vector<BatchTask> t;
+  for (int g = 0; g < NSEG; ++g) {
+    std::stable_sort(seg[g].begin(), seg[g].end(), [](const BatchTask& x, const BatchTask& y) {
+      auto cost = [](const BatchTask& q) { return q.epb * q.n1d * q.n1d * q.n1d; };
+      return cost(x) > cost(y);
+    });
+    b->seg_off[g] = (int)t.size();
+    b->seg_cnt[g] = (int)seg[g].size();
+    t.insert(t.end(), seg[g].begin(), seg[g].end());
+  }
+  if (*smem_a == 0) *smem_a = batch_smem_a(2, 1, false);
+  if (*smem_x == 0) *smem_x = batch_smem_a(2, 1, true);
   if (*smem_b == 0) *smem_b = batch_smem_b(2, 1);
   return t;
 }
 
 int upload_tasks(p2de_batch* b) {
-  size_t sa = 0, sb = 0;
-  std::vector<BatchTask> t = build_tasks(b, &sa, &sb);
-  if (sa != b->smem_a || sb != b->smem_b) {  // launch configuration changes: new capture
+  size_t sa = 0, sx = 0, sb = 0;
+  int cnt_before[NSEG];
+  std::memcpy(cnt_before, b->seg_cnt, sizeof cnt_before);
+  const bool phi_before = b->phi_min;
+  std::vector<BatchTask> t = build_tasks(b, &sa, &sx, &sb);
+  b->phi_min = false;
+  for (int s = 0; s < b->max_solves; ++s)
+    if (b->slots[s].active && (b->slots[s].flags & F_MIN_ENTROPY) && (b->slots[s].flags & F_RELAXED)) b->phi_min = true;
+  bool relaunch = sa != b->smem_a || sx != b->smem_x || sb != b->smem_b || b->phi_min != phi_before;
+  for (int g = 0; g < NSEG; ++g) relaunch |= (cnt_before[g] > 0) != (b->seg_cnt[g] > 0);
+  if (relaunch) {  // launch configuration or the set of launches changes: new capture
     b->smem_a = sa;
+    b->smem_x = sx;
     b->smem_b = sb;
     if (b->graph) {
       BCK(cudaStreamSynchronize(b->stream));
@@ -305,30 +402,59 @@ int upload_tasks(p2de_batch* b) {
   }
   int nt = (int)t.size();
   if (nt) BCK(cudaMemcpyAsync(b->d_tasks, t.data(), sizeof(BatchTask) * nt, cudaMemcpyHostToDevice, b->stream));
-  BCK(cudaMemcpyAsync(b->d_ntasks, &nt, sizeof nt, cudaMemcpyHostToDevice, b->stream));
+  // task counts: segments 0..3, then segments 0 and 1 together (kernel B)
+  int counts[NSEG + 1];
+  for (int g = 0; g < NSEG; ++g) counts[g] = b->seg_cnt[g];
+  counts[NSEG] = b->seg_cnt[SEG_PLAIN] + b->seg_cnt[SEG_EXT];
+  BCK(cudaMemcpyAsync(b->d_ntasks, counts, sizeof counts, cudaMemcpyHostToDevice, b->stream));
   BCK(cudaMemcpyAsync(b->d_active, b->active.data(), b->max_solves, cudaMemcpyHostToDevice, b->stream));
   BCK(cudaStreamSynchronize(b->stream));  // the host vectors above are temporaries
   b->tasks_dirty = false;
   return P2DE_OK;
 }
 
+// One step: the step begin, then per stage, in the one-solve path's order, the initial
+// minimum of phi (stage 1, relaxed min-entropy members), the low-only pass of the TVD
+// members, kernel A over the plain and the EXT members, and kernel B over all of them.
+// Passes without tasks are left out (the graph is recaptured when that set changes).
 int enqueue_batch_step(p2de_batch* b) {
   BCK(launch_batch_begin(b->d_solves, b->d_active, b->max_solves, b->d_counters, b->stream));
   for (int stage = 1; stage <= 3; ++stage) {
-    BCK(launch_batch_a(b->mixed, b->grid_a, b->smem_a, b->d_solves, b->d_tasks, b->d_ntasks,
-                       b->d_counters + 2 * (stage - 1), stage, b->stream));
-    BCK(launch_batch_b(b->grid_b, b->smem_b, b->d_solves, b->d_tasks, b->d_ntasks, b->d_counters + 2 * (stage - 1) + 1,
-                       stage, b->stream));
+    unsigned* ctr = b->d_counters + kBatchCountersPerStage * (stage - 1);
+    if (stage == 1 && b->phi_min) BCK(launch_batch_phi_min(b->d_solves, b->d_active, b->max_solves, b->stream));
+    struct Pass {
+      int seg, mode;
+      bool ext;
+    } passes[4] = {{SEG_LOW_PLAIN, BATCH_A_LOW_ONLY, false},
+                   {SEG_LOW_EXT, BATCH_A_LOW_ONLY, true},
+                   {SEG_PLAIN, BATCH_A_FULL, false},
+                   {SEG_EXT, BATCH_A_FULL, true}};
+    for (int i = 0; i < 4; ++i) {
+      const Pass& q = passes[i];
+      if (b->seg_cnt[q.seg] == 0) continue;
+      BCK(launch_batch_a(b->mixed, q.ext, q.mode, q.ext ? b->grid_x : b->grid_a, q.ext ? b->smem_x : b->smem_a,
+                         b->d_solves, b->d_tasks + b->seg_off[q.seg], b->d_ntasks + q.seg, ctr + i, stage, b->stream));
+    }
+    BCK(launch_batch_b(b->grid_b, b->smem_b, b->d_solves, b->d_tasks, b->d_ntasks + NSEG, ctr + 4, stage, b->stream));
   }
   return P2DE_OK;
 }
 
+// launches of one step (the launch counter)
+int step_launch_count(const p2de_batch* b) {
+  int n = 1 + (b->phi_min ? 1 : 0);
+  for (int g = 0; g < NSEG; ++g) n += 3 * (b->seg_cnt[g] > 0 ? 1 : 0);
+  return n + 3;
+}
+
 // persistent grids: resident blocks per SM at the current shared memory, times the SMs
 int size_grids(p2de_batch* b) {
-  int bpa = 0, bpb = 0;
-  BCK(batch_occupancy(b->mixed, b->smem_a, b->smem_b, &bpa, &bpb));
-  if (bpa < 1 || bpb < 1) return bfail(b, P2DE_ERR_CUDA, "batched kernels do not fit an SM");
+  int bpa = 0, bpb = 0, bpx = 0, bpb2 = 0;
+  BCK(batch_occupancy(b->mixed, false, b->smem_a, b->smem_b, &bpa, &bpb));
+  BCK(batch_occupancy(b->mixed, true, b->smem_x, b->smem_b, &bpx, &bpb2));
+  if (bpa < 1 || bpb < 1 || bpx < 1) return bfail(b, P2DE_ERR_CUDA, "batched kernels do not fit an SM");
   b->grid_a = b->sms * bpa;
+  b->grid_x = b->sms * bpx;
   b->grid_b = b->sms * bpb;
   return P2DE_OK;
 }
@@ -383,17 +509,13 @@ int p2de_batch_create(int device, int32_t precision, size_t pool_bytes, int32_t 
     return bail(P2DE_ERR_CUDA);
   if (b->pool.init(pool_bytes) != cudaSuccess) return bail(P2DE_ERR_OUT_OF_MEMORY);
   if (balloc(b, &b->d_solves, max_solves) != cudaSuccess || balloc(b, &b->d_active, max_solves) != cudaSuccess ||
-      balloc(b, &b->d_ntasks, 1) != cudaSuccess || balloc(b, &b->d_counters, 8) != cudaSuccess ||
+      balloc(b, &b->d_ntasks, NSEG + 1) != cudaSuccess || balloc(b, &b->d_counters, kBatchCounters + 1) != cudaSuccess ||
       balloc(b, &b->d_scal, (size_t)max_solves * S_NSCAL) != cudaSuccess ||
       balloc(b, &b->d_dtmin, max_solves) != cudaSuccess || balloc(b, &b->d_minrec, (size_t)6 * max_solves) != cudaSuccess ||
       balloc(b, &b->d_status, max_solves) != cudaSuccess || balloc(b, &b->d_work, 8) != cudaSuccess ||
-      balloc(b, &b->d_tables, kMaxN1D - 1) != cudaSuccess)
+      balloc(b, &b->d_tables, (size_t)kBatchTableGroups * (kMaxN1D - 1)) != cudaSuccess)
     return bail(P2DE_ERR_OUT_OF_MEMORY);
-  std::vector<OpTable> tabs(kMaxN1D - 1);
-  for (int N = 1; N < kMaxN1D; ++N) build_op_table(N, 5e-16, &tabs[N - 1]);
-  if (cudaMemcpyAsync(b->d_tables, tabs.data(), sizeof(OpTable) * tabs.size(), cudaMemcpyHostToDevice, b->stream) !=
-      cudaSuccess)
-    return bail(P2DE_ERR_CUDA);
+  if (batch_table_group(b, 5e-16) < 0) return bail(P2DE_ERR_CUDA);
   for (int n = 2; n <= kMaxN1D; ++n) {
     StageGeometry geo;
     cudaError_t e = cudaSuccess;
@@ -484,20 +606,18 @@ int p2de_batch_add(p2de_batch* b, const p2de_param* p, const p2de_mesh* m, const
   StageArgs a{};
   a.K = p->K;
   a.nstage = 1;
-  int f = 0;
-  switch (p->rhs_type) {
-    case P2DE_RHS_LOW_ORDER_POSITIVITY: f |= F_DO_LOW | F_RHSU_FROM_L; break;
-    case P2DE_RHS_ENTROPY_STABLE: f |= F_DO_HIGH | F_RHSU_FROM_H; break;
-    default: f |= F_DO_LOW | F_DO_HIGH | F_DO_LIMIT; break;
-  }
-  if (aa) f |= F_AXIS_ALIGNED;
-  if (p->reference_semantics) f |= F_REF_SEM;
-  if (p->bound_type == P2DE_BOUND_POSITIVITY_AND_CELL_ENTROPY) f |= F_CELL_ENTROPY;
-  if (b->precision == P2DE_PRECISION_MIXED_ACC64) f |= F_ACC64;
-  if (p->shock_capture == 1 && (f & F_DO_LIMIT)) f |= F_SHOCK;
+  const int f = member_flags(*p, aa, b->precision);
   a.flags = f;
   set_shock_capture(a, p->N, p->shock_capture_a, p->shock_capture_c);
-  a.ops = b->d_tables + (n - 2);
+  set_bound_constants(a, p->N, p->t0, p->POSTOL, p->bound_beta);
+  a.eta = p->eta;
+  a.rhoL = (double*)(base + lay.rhoL);
+  a.Lelem = (double*)(base + lay.Lelem);
+  a.phimin = (double*)(base + lay.phimin);
+  const int tg = batch_table_group(b, p->ZEROTOL);
+  if (tg < 0)
+    return bfail(b, P2DE_ERR_UNSUPPORTED, "more than %d distinct ZEROTOL values in one batch", kBatchTableGroups);
+  a.ops = b->d_tables + (size_t)tg * (kMaxN1D - 1) + (n - 2);
   a.Uq = (double*)(base + lay.Uq);
   a.resW = (double*)(base + lay.resW);
   a.geom = (const double*)(base + lay.geom);
@@ -544,6 +664,7 @@ int p2de_batch_add(p2de_batch* b, const p2de_param* p, const p2de_mesh* m, const
   sl.active = true;
   sl.prm = *p;
   sl.n1d = (int)n;
+  sl.flags = f;
   sl.off = off;
   sl.lay = lay;
   b->active[slot] = 1;
@@ -574,7 +695,7 @@ int p2de_batch_step(p2de_batch* b, int64_t nsteps) {
   if (rc != P2DE_OK) return rc;
   for (int64_t i = 0; i < nsteps; ++i) {
     BCK(cudaGraphLaunch(b->graph, b->stream));
-    b->launches += 7;
+    b->launches += step_launch_count(b);
   }
   BCK(cudaStreamSynchronize(b->stream));
   return P2DE_OK;
@@ -589,6 +710,23 @@ int p2de_batch_set_elements_per_block(p2de_batch* b, int32_t N, int32_t epb) {
     b->epb[N + 1] = epb;
     b->tasks_dirty = true;
   }
+  return P2DE_OK;
+}
+
+int p2de_batch_set_layout(p2de_batch* b, int32_t N, int32_t layout) {
+  if (!b || N < 1 || N + 1 > kMaxN1D) return P2DE_ERR_INVALID_ARGUMENT;
+  if (layout != P2DE_LAYOUT_FLAT && layout != P2DE_LAYOUT_LINES_PER_WARP)
+    return bfail(b, P2DE_ERR_INVALID_ARGUMENT, "layout %d", layout);
+  if (b->layout[N + 1] != layout) {
+    b->layout[N + 1] = layout;
+    b->tasks_dirty = true;
+  }
+  return P2DE_OK;
+}
+
+int p2de_batch_get_layout(p2de_batch* b, int32_t N, int32_t* layout) {
+  if (!b || !layout || N < 1 || N + 1 > kMaxN1D) return P2DE_ERR_INVALID_ARGUMENT;
+  *layout = b->layout[N + 1];
   return P2DE_OK;
 }
 
@@ -638,7 +776,7 @@ int p2de_batch_autotune(p2de_batch* b, int32_t best_epb[5]) {
   b->tasks_dirty = true;
   BCK(cudaMemcpyAsync(b->d_scal, sc.data(), sizeof(double) * sc.size(), cudaMemcpyHostToDevice, b->stream));
   cudaEvent_t e0 = nullptr, e1 = nullptr;
-  unsigned* counter = b->d_counters + 6;
+  unsigned* counter = b->d_counters + kBatchCounters;  // the spare counter
   // the timings; whatever they return, the events go and the scalars come back below
   auto timings = [&]() -> int {
   BCK(cudaEventCreate(&e0));
@@ -648,42 +786,58 @@ int p2de_batch_autotune(p2de_batch* b, int32_t best_epb[5]) {
     for (int s = 0; s < b->max_solves; ++s) present |= b->slots[s].active && b->slots[s].n1d == n1d;
     if (!present) continue;
     const int emax = batch_elems_per_block_max(n1d), edef = batch_elems_per_block(n1d);
-    int best = b->epb[n1d];
+    int best = b->epb[n1d], best_layout = b->layout[n1d];
     double bms = 1e30;
+    for (int lay : {(int)P2DE_LAYOUT_FLAT, (int)P2DE_LAYOUT_LINES_PER_WARP})
     for (int e : {1, 2, 3, 4, 6, 8, 12, 16, 24, 32, edef}) {
       if (e > emax) continue;
-      std::vector<BatchTask> t;
+      // this degree's members, plain and EXT instantiation, full pass at stage 2
+      std::vector<BatchTask> t[2];
       for (int s = 0; s < b->max_solves; ++s) {
         const Slot& sl = b->slots[s];
         if (!sl.active || sl.n1d != n1d) continue;
-        for (int k0 = 0; k0 < sl.prm.K; k0 += e) t.push_back(BatchTask{s, k0, n1d, e});
+        const int x = (sl.flags & kExtFlags) ? 1 : 0;
+        for (int k0 = 0; k0 < sl.prm.K; k0 += e) t[x].push_back(BatchTask{s, k0, n1d, e, lay});
       }
-      int nt = (int)t.size();
-      int bpa = 0, bpb = 0;
-      const size_t sma = batch_smem_a(n1d, e);
-      cudaError_t ce = batch_occupancy(b->mixed, sma, batch_smem_b(n1d, e), &bpa, &bpb);
-      if (ce != cudaSuccess || bpa < 1) continue;
-      const int grid = std::min(b->sms * bpa, nt);
-      BCK(cudaMemcpyAsync(b->d_tasks, t.data(), sizeof(BatchTask) * nt, cudaMemcpyHostToDevice, b->stream));
-      BCK(cudaMemcpyAsync(b->d_ntasks, &nt, sizeof nt, cudaMemcpyHostToDevice, b->stream));
+      int grid[2] = {0, 0}, nt[2] = {(int)t[0].size(), (int)t[1].size()};
+      size_t sm[2] = {batch_smem_a(n1d, e, false), batch_smem_a(n1d, e, true)};
+      bool fits = true;
+      for (int x = 0; x < 2; ++x) {
+        if (!nt[x]) continue;
+        int bpa = 0, bpb = 0;
+        cudaError_t ce = batch_occupancy(b->mixed, x == 1, sm[x], batch_smem_b(n1d, e), &bpa, &bpb);
+        if (ce != cudaSuccess || bpa < 1) fits = false;
+        grid[x] = std::min(b->sms * bpa, nt[x]);
+      }
+      if (!fits) continue;
+      std::vector<BatchTask> all = t[0];
+      all.insert(all.end(), t[1].begin(), t[1].end());
+      BCK(cudaMemcpyAsync(b->d_tasks, all.data(), sizeof(BatchTask) * all.size(), cudaMemcpyHostToDevice, b->stream));
+      BCK(cudaMemcpyAsync(b->d_ntasks, nt, sizeof nt, cudaMemcpyHostToDevice, b->stream));
       float tot = 0.f;
       for (int rep = 0; rep < 4; ++rep) {
-        BCK(cudaMemsetAsync(counter, 0, sizeof(unsigned), b->stream));
         BCK(cudaEventRecord(e0, b->stream));
-        BCK(launch_batch_a(b->mixed, grid, sma, b->d_solves, b->d_tasks, b->d_ntasks, counter, 2, b->stream));
+        for (int x = 0; x < 2; ++x) {
+          if (!nt[x]) continue;
+          BCK(cudaMemsetAsync(counter, 0, sizeof(unsigned), b->stream));
+          BCK(launch_batch_a(b->mixed, x == 1, BATCH_A_FULL, grid[x], sm[x], b->d_solves, b->d_tasks + (x ? nt[0] : 0),
+                             b->d_ntasks + x, counter, 2, b->stream));
+          b->launches += 1;
+        }
         BCK(cudaEventRecord(e1, b->stream));
         BCK(cudaEventSynchronize(e1));
         float ms;
         BCK(cudaEventElapsedTime(&ms, e0, e1));
         if (rep > 0) tot += ms;  // first launch warms up
       }
-      b->launches += 4;
       if (tot / 3.0 < bms) {
         bms = tot / 3.0;
         best = e;
+        best_layout = lay;
       }
     }
     b->epb[n1d] = best;
+    b->layout[n1d] = best_layout;
     if (best_epb) best_epb[n1d - 2] = best;
   }
   return P2DE_OK;

@@ -46,27 +46,51 @@ __device__ __forceinline__ float logmean_f32(float aL, float aR) {
   return (aL + aR) / (2.0f * F);
 }
 
-// fS(Dim2) in FP32 with the Ismail-Roe log mean; UL/UR = (rho, u, v, beta).
+// The parts of fS(Dim2) in FP32 that both directions share (Ismail-Roe log mean);
+// UL/UR = (rho, u, v, beta).
+struct FSCommonF {
+  float rholog, uavg, vavg, pa, f4aux;
+};
+__device__ __forceinline__ FSCommonF fS_common_f32(const Gas<float>& g, const float* UL, const float* UR) {
+  FSCommonF c;
+  c.rholog = logmean_f32(UL[0], UR[0]);
+  const float betalog = logmean_f32(UL[3], UR[3]);
+  const float rhoavg = 0.5f * (UL[0] + UR[0]);
+  c.uavg = 0.5f * (UL[1] + UR[1]);
+  c.vavg = 0.5f * (UL[2] + UR[2]);
+  const float unorm = fmaf(UL[1], UR[1], UL[2] * UR[2]);
+  c.pa = rhoavg / (UL[3] + UR[3]);
+  c.f4aux = fmaf(0.5f * c.rholog, unorm, c.rholog / (g.two_gm1 * betalog) + c.pa);
+  return c;
+}
+
+// fS(Dim2) in FP32, both directions
 __device__ __forceinline__ void fS_f32(const Gas<float>& g, const float* UL, const float* UR, float* Fx, float* Fy) {
-  float rholog = logmean_f32(UL[0], UR[0]);
-  float betalog = logmean_f32(UL[3], UR[3]);
-  float rhoavg = 0.5f * (UL[0] + UR[0]);
-  float uavg = 0.5f * (UL[1] + UR[1]);
-  float vavg = 0.5f * (UL[2] + UR[2]);
-  float unorm = UL[1] * UR[1] + UL[2] * UR[2];
-  float pa = rhoavg / (UL[3] + UR[3]);
-  float f4aux = rholog / (g.two_gm1 * betalog) + pa + 0.5f * rholog * unorm;
-  float FxS1 = rholog * uavg;
-  float FxS3 = FxS1 * vavg;
-  float FyS1 = rholog * vavg;
+  const FSCommonF c = fS_common_f32(g, UL, UR);
+  const float FxS1 = c.rholog * c.uavg;
+  const float FxS3 = FxS1 * c.vavg;
+  const float FyS1 = c.rholog * c.vavg;
   Fx[0] = FxS1;
-  Fx[1] = FxS1 * uavg + pa;
+  Fx[1] = fmaf(FxS1, c.uavg, c.pa);
   Fx[2] = FxS3;
-  Fx[3] = f4aux * uavg;
+  Fx[3] = c.f4aux * c.uavg;
   Fy[0] = FyS1;
   Fy[1] = FxS3;
-  Fy[2] = FyS1 * vavg + pa;
-  Fy[3] = f4aux * vavg;
+  Fy[2] = fmaf(FyS1, c.vavg, c.pa);
+  Fy[3] = c.f4aux * c.vavg;
+}
+
+// the x (ax = 0) or y (ax = 1) flux of fS_f32 alone (axis-aligned elements)
+__device__ __forceinline__ void fS_f32_axis(const Gas<float>& g, const float* UL, const float* UR, int ax, float* F) {
+  const FSCommonF c = fS_common_f32(g, UL, UR);
+  const float un = ax ? c.vavg : c.uavg;
+  const float F0 = c.rholog * un;
+  const float Ft = (c.rholog * c.uavg) * c.vavg;
+  const float Fn = fmaf(F0, un, c.pa);
+  F[0] = F0;
+  F[1] = ax ? Ft : Fn;
+  F[2] = ax ? Fn : Ft;
+  F[3] = c.f4aux * un;
 }
 
 // Julia min/max semantics on Float64: NaN propagates, -0.0 < 0.0.

@@ -45,6 +45,7 @@
 namespace p2de {
 
 __host__ __device__ constexpr int cmax(int a, int b) { return a > b ? a : b; }
+__host__ __device__ constexpr int cmin(int a, int b) { return a < b ? a : b; }
 
 template <int N1D>
 struct Cfg {
@@ -120,8 +121,58 @@ struct Cfg {
 // U + dt rhsL, the low-order update (one form everywhere, so values agree bitwise)
 __device__ __forceinline__ double low_update(double u, double dt, double r) { return fma(dt, r, u); }
 
-// 1/x correctly rounded (the same value as 1.0 / x)
-__device__ __forceinline__ double rcp(double x) { return __drcp_rn(x); }
+// 1/x: for |x| in [2^-1022, 2^1022) (a normal reciprocal) two Newton-Raphson steps
+// y <- y + y (1 - x y) from the hardware's approximate reciprocal (rcp.approx.ftz.f64),
+// each residual formed by an FMA; the result is the correctly rounded 1/x unless 1/x lies
+// within about 2^-88 relative of a rounding tie (the same bits as __drcp_rn on 4M random
+// arguments), in 5 FP64 instructions against 6. Other x (0, subnormal, huge, inf, NaN) take
+// __drcp_rn.
+__device__ __forceinline__ double rcp(double x) {
+  const unsigned long long a = (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffULL;
+  if (a - 0x0010000000000000ULL >= 0x7fc0000000000000ULL) return __drcp_rn(x);
+  double y;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+  double e = fma(-x, y, 1.0);
+  y = fma(y, e, y);
+  e = fma(-x, y, 1.0);
+  return fma(y, e, y);
+}
+
+// Natural logarithm by the table-driven method of P. T. P. Tang ("Table-driven implementation
+// of the logarithm function in IEEE floating-point arithmetic", ACM TOMS 16(4), 1990):
+// x = 2^k m with m in [sqrt(1/2), sqrt(2)), F = m rounded to a multiple of 1/256 (table
+// entry j), r = (m - F) / F (m - F exact), log x = k log 2 + log F + log(1 + r), the last
+// by its Taylor polynomial to r^6 (|r| < 2^-8.5: the omitted terms are below 2^-56 of the
+// result). 15 FP64 instructions against 31 for log(); within one unit in the last place of
+// the correctly rounded value (checked against an extended-precision log on 4M arguments
+// from 1e-9 to 2e8 and around 1), like log(). Positive normal finite x; anything else
+// goes to log().
+__device__ __forceinline__ double log_fast(double x, const OpTable& op) {
+  const long long b = __double_as_longlong(x);
+  if ((unsigned long long)(b - 0x0010000000000000LL) >= 0x7fe0000000000000ULL) return log(x);
+  long long k = (b >> 52) - 1023;
+  long long mb = (b & 0x000fffffffffffffLL) | 0x3ff0000000000000LL;  // m in [1, 2)
+  if (((mb >> 44) & 0xff) >= 106) {  // m >= 1 + 106/256: use m/2 in [0.707, 1)
+    mb -= 0x0010000000000000LL;
+    k += 1;
+  }
+  const double m = __longlong_as_double(mb);
+  const double t = m + 0x1p44;  // m rounded to a multiple of 2^-8 in the low mantissa bits
+  const int j = (int)(__double_as_longlong(t) & 0x1ff);
+  const double F = t - 0x1p44;
+  const double* T = op.logtab[j - kLogTabLo];
+  const double r = (m - F) * T[0];
+  double q = fma(r, -1.0 / 6.0, 1.0 / 5.0);
+  q = fma(q, r, -0.25);
+  q = fma(q, r, 1.0 / 3.0);
+  q = fma(q, r, -0.5);
+  const double p = fma(r * r, q, r);
+  // (double)k without a conversion: 1.5 2^52 + k in the bits of 1.5 2^52, minus 1.5 2^52
+  const double kd = __longlong_as_double(0x4338000000000000LL + k) - 0x1.8p52;
+  const double hi = fma(kd, op.ln2_hi, T[1]);
+  const double lo = fma(kd, op.ln2_lo, T[2]);
+  return hi + (p + lo);
+}
 
 // Geometry factor q of an element from gg = (J, rxJ, sxJ, ryJ, syJ): slots 0-4 copy gg,
 // then |gr|, nr (2), |gs|, ns (2), 1/J; slots 12-14 hold FP32 rxJ, sxJ, ryJ, syJ, 1/J
@@ -216,10 +267,13 @@ __device__ __forceinline__ double logmean_series(double aavg, double x) {
   return aavg * (1.0 + v * (-0.2 - v * (0.0512 - v * 0.026038857142857)));
 }
 
-// fS(Dim2) (:220-249); UL/UR = (rho, u, v, beta, log rho, log beta). The quotients of
+// The parts of fS(Dim2) (:220-249) that both flux directions share: the log means, the
+// averages, pa and f4aux. UL/UR = (rho, u, v, beta, log rho, log beta). The quotients of
 // the two log means (logmean_1div) share one reciprocal: da_r/den_r = da_r den_b/(den_r den_b).
-__device__ __forceinline__ void fS_fast(const Gas<double>& g, const double* UL, const double* UR, double* Fx,
-                                        double* Fy) {
+struct FSCommon {
+  double rholog, uavg, vavg, pa, f4aux;
+};
+__device__ __forceinline__ FSCommon fS_common(const Gas<double>& g, const double* UL, const double* UR) {
   const double da_r = UR[0] - UL[0], av_r = 0.5 * (UR[0] + UL[0]);
   const bool ser_r = fabs(da_r) < 1e-4 * fabs(av_r);
   const double den_r = ser_r ? av_r : (UL[4] - UR[4]);
@@ -228,28 +282,52 @@ __device__ __forceinline__ void fS_fast(const Gas<double>& g, const double* UL, 
   const double den_b = ser_b ? av_b : (UL[5] - UR[5]);
   const double rd = rcp(den_r * den_b);
   const double x_r = da_r * (den_b * rd), x_b = da_b * (den_r * rd);
-  double rholog = ser_r ? logmean_series(av_r, x_r) : -x_r;
-  double betalog = ser_b ? logmean_series(av_b, x_b) : -x_b;
-  double rhoavg = 0.5 * (UL[0] + UR[0]);
-  double uavg = 0.5 * (UL[1] + UR[1]);
-  double vavg = 0.5 * (UL[2] + UR[2]);
-  double unorm = UL[1] * UR[1] + UL[2] * UR[2];
-  double d1 = UL[3] + UR[3];
-  double d2 = g.two_gm1 * betalog;
-  double r12 = rcp(d1 * d2);
-  double pa = rhoavg * d2 * r12;
-  double f4aux = rholog * d1 * r12 + pa + 0.5 * rholog * unorm;
-  double FxS1 = rholog * uavg;
-  double FxS3 = FxS1 * vavg;
-  double FyS1 = rholog * vavg;
+  FSCommon c;
+  c.rholog = ser_r ? logmean_series(av_r, x_r) : -x_r;
+  const double betalog = ser_b ? logmean_series(av_b, x_b) : -x_b;
+  const double rhoavg = 0.5 * (UL[0] + UR[0]);
+  c.uavg = 0.5 * (UL[1] + UR[1]);
+  c.vavg = 0.5 * (UL[2] + UR[2]);
+  const double unorm = fma(UL[1], UR[1], UL[2] * UR[2]);
+  const double d1 = UL[3] + UR[3];
+  const double d2 = g.two_gm1 * betalog;
+  const double r12 = rcp(d1 * d2);
+  c.pa = rhoavg * d2 * r12;
+  c.f4aux = fma(c.rholog * d1, r12, c.pa) + (0.5 * c.rholog) * unorm;
+  return c;
+}
+
+// fS(Dim2) (:220-249), both directions
+__device__ __forceinline__ void fS_fast(const Gas<double>& g, const double* UL, const double* UR, double* Fx,
+                                        double* Fy) {
+  const FSCommon c = fS_common(g, UL, UR);
+  const double FxS1 = c.rholog * c.uavg;
+  const double FxS3 = FxS1 * c.vavg;
+  const double FyS1 = c.rholog * c.vavg;
   Fx[0] = FxS1;
-  Fx[1] = FxS1 * uavg + pa;
+  Fx[1] = fma(FxS1, c.uavg, c.pa);
   Fx[2] = FxS3;
-  Fx[3] = f4aux * uavg;
+  Fx[3] = c.f4aux * c.uavg;
   Fy[0] = FyS1;
   Fy[1] = FxS3;
-  Fy[2] = FyS1 * vavg + pa;
-  Fy[3] = f4aux * vavg;
+  Fy[2] = fma(FyS1, c.vavg, c.pa);
+  Fy[3] = c.f4aux * c.vavg;
+}
+
+// the x (ax = 0) or y (ax = 1) flux of fS_fast alone, with the same operations for each
+// component: on axis-aligned elements a pair on an r-line needs only the x flux and a pair
+// on an s-line only the y flux, and one instruction stream serves both
+__device__ __forceinline__ void fS_axis(const Gas<double>& g, const double* UL, const double* UR, int ax,
+                                        double* F) {
+  const FSCommon c = fS_common(g, UL, UR);
+  const double un = ax ? c.vavg : c.uavg;
+  const double F0 = c.rholog * un;                 // FxS1 or FyS1
+  const double Ft = (c.rholog * c.uavg) * c.vavg;  // FxS3: Fx[2] and Fy[1]
+  const double Fn = fma(F0, un, c.pa);             // Fx[1] or Fy[2]
+  F[0] = F0;
+  F[1] = ax ? Ft : Fn;
+  F[2] = ax ? Fn : Ft;
+  F[3] = c.f4aux * un;
 }
 
 // limiter_utils.jl:108-132 for a finite Lrhoe
@@ -340,6 +418,42 @@ __device__ __forceinline__ double find_alpha(const double* ui, const double* ut,
 __device__ __forceinline__ double s_modified(double rho, double rhou, double rhov, double E, double gamma) {
   const double rhoe = E - 0.5 * (rhou * rhou + rhov * rhov) / rho;
   return rhoe * pow(rho, -gamma);
+}
+
+// initialize_s_modified! (subcell.jl:21-35): at t == t0, stage 1, the minimum of
+// phi = rhoe rho^(-gamma) over every node (NaN if any is NaN, as Julia's minimum), by one
+// block of 1024 threads in a fixed order, so the result does not depend on scheduling.
+__device__ __forceinline__ void phi_min_body(const double* Uq, size_t nodes, double gamma, const double* scal,
+                                             double t0, double* out) {
+  if (scal[S_DONE] != 0.0 || scal[S_T] != t0) return;
+  __shared__ double wmin[32];
+  __shared__ int wnan[32];
+  double m = INFINITY;
+  int isn = 0;
+  for (size_t i = threadIdx.x; i < nodes; i += blockDim.x) {
+    const double* U = Uq + 4 * i;
+    const double v = s_modified(U[0], U[1], U[2], U[3], gamma);
+    if (isnan(v))
+      isn = 1;
+    else
+      m = fmin(m, v);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    m = fmin(m, __shfl_xor_sync(0xffffffffu, m, o));
+    isn |= __shfl_xor_sync(0xffffffffu, isn, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    wmin[threadIdx.x >> 5] = m;
+    wnan[threadIdx.x >> 5] = isn;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
+      m = fmin(m, wmin[w]);
+      isn |= wnan[w];
+    }
+    *out = isn ? NAN : m;
+  }
 }
 
 // limiting_param_bound_phi (limiter_utils.jl:43-50) through bisection (nonlinear_solvers.jl:3-20):
@@ -590,6 +704,123 @@ __global__ void __launch_bounds__(Cfg<N1D>::THREADS) k_gauss_proj(StageArgs a) {
 // =====================================================================================
 // Kernel A
 // =====================================================================================
+
+// Phase P6 for one high-order pair pp of an axis-aligned element: the pair's own axis only
+// (fS_axis; the other half of the pair's scratch slot is not written, and not read), scaled
+// by S and the element's geometry. Every layout calls this one body for such pairs.
+template <int N1D, typename TH>
+__device__ __forceinline__ void pair_term_aa(const OpTable& op, const Gas<double>& g, const Gas<float>& gf,
+                                             double* base, int pp, bool acc64) {
+  using C = Cfg<N1D>;
+  const double* G = base + C::O_GEO;
+  const int i = op.hp_i[pp], j = op.hp_j[pp], ax = op.hp_axis[pp];
+  if (sizeof(TH) == 8) {
+    const double Sa = (ax == 0 ? G[1] : G[4]) * op.hp_S[pp];
+    double F[4];
+    fS_axis(g, base + C::O_PRIM + 6 * i, base + C::O_PRIM + 6 * j, ax, F);
+    double* out = base + C::O_SCR + 8 * pp;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) out[4 * ax + c] = Sa * F[c];
+  } else {
+    const float4* Pf = reinterpret_cast<const float4*>(base + C::O_PRIM);
+    const float4 qi = Pf[i], qj = Pf[j];
+    const float UL[4] = {qi.x, qi.y, qi.z, qi.w};
+    const float UR[4] = {qj.x, qj.y, qj.z, qj.w};
+    const float* Gf = reinterpret_cast<const float*>(G + 12);
+    const float sa = (ax == 0 ? Gf[0] : Gf[3]) * op.hp_Sf[pp];
+    float F[4];
+    fS_f32_axis(gf, UL, UR, ax, F);
+    if (acc64) {
+      double* outd = base + C::O_SCR + 8 * pp;
+#pragma unroll
+      for (int c = 0; c < 4; ++c) outd[4 * ax + c] = (double)(sa * F[c]);
+    } else {
+      float* outf = reinterpret_cast<float*>(base + C::O_SCR) + 8 * pp;
+#pragma unroll
+      for (int c = 0; c < 4; ++c) outf[4 * ax + c] = sa * F[c];
+    }
+  }
+}
+
+// Phase P7 for the axis-ax half of node m of an axis-aligned element (assemble_rhs!,
+// flux_differencing.jl:331-361): the pair terms of the node's line in the merged gather
+// order, the node's face term on that axis, lift by 1/wq and scale by 1/J. Every layout
+// calls this one body for such nodes.
+template <int N1D, typename TH>
+__device__ __forceinline__ void node_half_aa(const OpTable& op, double* base, int m, int ax, bool acc64) {
+  using C = Cfg<N1D>;
+  constexpr int n = C::n;
+  const int ir = m % n, is = m / n;
+  const int f = ax == 0 ? (ir == 0 ? is : (ir == n - 1 ? n + is : -1))
+                        : (is == 0 ? 2 * n + ir : (is == n - 1 ? 3 * n + ir : -1));
+  const double* BH = base + C::O_BFH + 8 * (f < 0 ? 0 : f) + 4 * ax;
+  double* R = base + C::O_RXYH + 8 * m + 4 * ax;
+  if (sizeof(TH) == 8 || acc64) {
+    const double rJ = base[C::O_GEO + 11];
+    const double rw = op.rwq[m];
+    double Q[4] = {0, 0, 0, 0};
+    for (int t = 0; t < n - 1; ++t) {
+      const double* sf = base + C::O_SCR + 8 * op.hga_pair[ax][m][t] + 4 * ax;
+      const int sg = op.hga_sign[ax][m][t];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) Q[c] = Q[c] + signed_by(sf[c], sg);
+    }
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const double Bs = f < 0 ? 0.0 : rw * BH[c];
+      R[c] = (-(rw * Q[c] + Bs)) * rJ;
+    }
+  } else {
+    const float* sfb = reinterpret_cast<const float*>(base + C::O_SCR);
+    const float rwf = op.rwqf[m];
+    const float rJf = reinterpret_cast<const float*>(base + C::O_GEO + 12)[4];
+    float Q[4] = {0, 0, 0, 0};
+    for (int t = 0; t < n - 1; ++t) {
+      const float* sf = sfb + 8 * op.hga_pair[ax][m][t] + 4 * ax;
+      const int sg = op.hga_sign[ax][m][t];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) Q[c] = Q[c] + signed_by(sf[c], sg);
+    }
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const float Bs = f < 0 ? 0.0f : rwf * (float)BH[c];
+      R[c] = (double)((-(rwf * Q[c] + Bs)) * rJf);
+    }
+  }
+}
+
+// Phases P6 and P7 of axis-aligned elements with whole lines per warp: the block's lines
+// (element e, axis ax, line l) are dealt to its warps LPW at a time; a warp computes its
+// lines' pairs (lane -> line, pair), synchronizes only itself, and then gathers and lifts
+// its lines' node halves (lane -> line, node), since on such elements the x half of a
+// node's volume term depends only on the pairs of its r-line and the y half only on its
+// s-line. The arithmetic is the flat layout's (pair_term_aa, node_half_aa), so the results
+// are the same bits.
+template <int N1D, typename TH>
+__device__ __forceinline__ void pairs_lines_per_warp(const OpTable& op, const Gas<double>& g, const Gas<float>& gf,
+                                                     double* sm, int PE, int Ke, bool acc64) {
+  using C = Cfg<N1D>;
+  constexpr int n = C::n;
+  constexpr int PPL = n * (n - 1) / 2;  // pairs per line
+  // lines per warp: as many as both steps fit in 32 lanes (PPL pairs, then n nodes, per line)
+  constexpr int LPW = cmin(32 / PPL, 32 / n);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int nlines = Ke * 2 * n;  // line id = (e * 2 + ax) * n + l
+  for (int l0 = warp * LPW; l0 < nlines; l0 += nwarps * LPW) {
+    const int lp = l0 + lane / PPL;
+    if (lane < LPW * PPL && lp < nlines) {
+      const int e = lp / (2 * n), ax = (lp / n) % 2, l = lp % n;
+      pair_term_aa<N1D, TH>(op, g, gf, sm + e * PE, (ax * n + l) * PPL + lane % PPL, acc64);
+    }
+    __syncwarp();
+    const int ln = l0 + lane / n;
+    if (lane < LPW * n && ln < nlines) {
+      const int e = ln / (2 * n), ax = (ln / n) % 2, l = ln % n, a2 = lane % n;
+      node_half_aa<N1D, TH>(op, sm + e * PE, ax == 0 ? a2 + n * l : l + n * a2, ax, acc64);
+    }
+    __syncwarp();
+  }
+}
 // Body of kernel A for the E elements k0 .. k0+E-1 of the solve `a`; every early return
 // is uniform over the block. Used by the one-solve kernel and the batched kernel.
 // EXT: compiles the branches of kExtFlags; without it those flags are masked off, so their
@@ -696,8 +927,8 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
         Pm[1] = u;
         Pm[2] = v;
         Pm[3] = beta;
-        Pm[4] = log(rho);
-        Pm[5] = log(beta);
+        Pm[4] = log_fast(rho, op);
+        Pm[5] = log_fast(beta, op);
       } else {
         // FP32 (rho, u, v, beta) per node, converted once here rather than per pair
         float rf = (float)rho;
@@ -719,8 +950,8 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
       Pm[1] = U[1] * rr;
       Pm[2] = U[2] * rr;
       Pm[3] = beta;
-      Pm[4] = log(U[0]);
-      Pm[5] = log(beta);
+      Pm[4] = log_fast(U[0], op);
+      Pm[5] = log_fast(beta, op);
     }
     // is_Vf_limited (flux_differencing.jl:316-318): any theta < 1 on the element, into O_XT + 1
     for (int e = tid; e < Ke; e += bs) {
@@ -1155,11 +1386,20 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
   // ---- P6: high-order volume pairs (flux_differencing_volume!, :164-211)
   // FP32 kernel with FP64 accumulation of the pair terms
   const bool acc64 = sizeof(TH) == 4 && (flags & F_ACC64);
-  if (do_high) {
-    const Gas<float> gf{(float)a.gamma, (float)a.gm1, (float)(2.0 * a.gm1)};
+  const Gas<float> gf{(float)a.gamma, (float)a.gm1, (float)(2.0 * a.gm1)};
+  // whole lines per warp (a.layout 1) for axis-aligned LGL elements; the flat (element,
+  // pair) and (element, node) loops otherwise. Both give the same bits.
+  const bool lpw = !GAUSS && aa && !(flags & F_KPP) && a.layout == 1;
+  if (do_high && lpw) {
+    pairs_lines_per_warp<N1D, TH>(op, g, gf, sm, PE, Ke, acc64);
+  } else if (do_high) {
     for (int w = tid; w < Ke * C::NPH; w += bs) {
       int e = w / C::NPH, pp = w % C::NPH;
       double* base = sm + e * PE;
+      if (aa && !(flags & F_KPP)) {
+        pair_term_aa<N1D, TH>(op, g, gf, base, pp, acc64);
+        continue;
+      }
       const double* G = base + C::O_GEO;
       int i = op.hp_i[pp], j = op.hp_j[pp], ax = op.hp_axis[pp];
       double S = op.hp_S[pp];
@@ -1330,10 +1570,15 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
       // pairs and y faces the y half (gathers in the merged lists' order)
       const int fx = ir == 0 ? is : (ir == n - 1 ? n + is : -1);
       const int fy = is == 0 ? 2 * n + ir : (is == n - 1 ? 3 * n + ir : -1);
+      if (aa && !(flags & F_KPP)) {
+        node_half_aa<N1D, TH>(op, base, m, 0, acc64);
+        node_half_aa<N1D, TH>(op, base, m, 1, acc64);
+        continue;
+      }
       if (sizeof(TH) == 8 || acc64) {
         double Q[8] = {0, 0, 0, 0, 0, 0, 0, 0};
         double Bs[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-        if (aa) {
+        if (aa) {  // KPP: the pair terms of both axes are written (fS_kpp)
 #pragma unroll
           for (int ax = 0; ax < 2; ++ax)
             for (int t = 0; t < n - 1; ++t) {

@@ -175,9 +175,27 @@ bool invert(std::vector<double> A, int m, double* inv) {
 
 }  // namespace
 
+// The table of log_fast (in the stage kernels): a value rounded to double and cut to its
+// leading `bits` significant bits, and the rest.
+static void split_hi_lo(long double v, int bits, double* hi, double* lo) {
+  double h = (double)v;
+  uint64_t b;
+  std::memcpy(&b, &h, sizeof b);
+  b &= ~((1ull << (52 - (bits - 1))) - 1);
+  std::memcpy(&h, &b, sizeof b);
+  *hi = h;
+  *lo = (double)(v - (long double)h);
+}
+
 int build_op_table(int N, double zerotol, OpTable* T, int basis) {
   if (N < 1 || N + 1 > kMaxN1D || basis < 0 || basis > 1) return 1;
   std::memset(T, 0, sizeof(OpTable));
+  for (int i = 0; i < kLogTabN; ++i) {
+    const int j = kLogTabLo + i;
+    T->logtab[i][0] = 256.0 / j;
+    split_hi_lo(std::log((long double)j / 256.0L), 41, &T->logtab[i][1], &T->logtab[i][2]);
+  }
+  split_hi_lo(std::log(2.0L), 42, &T->ln2_hi, &T->ln2_lo);
   const int n = N + 1, Nq = n * n;
   T->N1D = n;
   T->Nq = Nq;
@@ -292,13 +310,16 @@ int build_op_table(int N, double zerotol, OpTable* T, int basis) {
   }
   Q01[0] = -0.5;
   Q01[(n - 1) * n + (n - 1)] = 0.5;
+  // Qr0 = droptol!(kron(M1D, Q01D)), Qs0 = droptol!(kron(Q01D, M1D)), and Sr0, Ss0 =
+  // droptol!(0.5 (Q0 - Q0')) (low_order_operators, init.jl:312-321)
+  auto drop = [&](double v) { return std::fabs(v) <= zerotol ? 0.0 : v; };
   auto Qr0 = [&](int i, int j) {
     int ir = i % n, is = i / n, jr = j % n, js = j / n;
-    return (is == js ? w[is] : 0.0) * Q01[ir * n + jr];
+    return drop((is == js ? w[is] : 0.0) * Q01[ir * n + jr]);
   };
   auto Qs0 = [&](int i, int j) {
     int ir = i % n, is = i / n, jr = j % n, js = j / n;
-    return Q01[is * n + js] * (ir == jr ? w[ir] : 0.0);
+    return drop(Q01[is * n + js] * (ir == jr ? w[ir] : 0.0));
   };
   p = 0;
   for (int is = 0; is < n; ++is)
@@ -307,7 +328,7 @@ int build_op_table(int N, double zerotol, OpTable* T, int basis) {
       T->lp_i[p] = (int16_t)i;
       T->lp_j[p] = (int16_t)j;
       T->lp_axis[p] = 0;
-      T->lp_S[p] = 0.5 * (Qr0(i, j) - Qr0(j, i));
+      T->lp_S[p] = drop(0.5 * (Qr0(i, j) - Qr0(j, i)));
       ++p;
     }
   for (int ir = 0; ir < n; ++ir)
@@ -316,7 +337,7 @@ int build_op_table(int N, double zerotol, OpTable* T, int basis) {
       T->lp_i[p] = (int16_t)i;
       T->lp_j[p] = (int16_t)j;
       T->lp_axis[p] = 1;
-      T->lp_S[p] = 0.5 * (Qs0(i, j) - Qs0(j, i));
+      T->lp_S[p] = drop(0.5 * (Qs0(i, j) - Qs0(j, i)));
       ++p;
     }
   T->npl = p;

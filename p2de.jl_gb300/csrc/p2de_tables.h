@@ -13,6 +13,10 @@
 namespace p2de {
 
 constexpr int kMaxN1D = 6;
+// the table of log_fast: F_j = j / 256 for j = kLogTabLo .. kLogTabLo + kLogTabN - 1, which
+// covers the reduced mantissas [sqrt(1/2), sqrt(2)) to the nearest 1/256
+constexpr int kLogTabLo = 181;
+constexpr int kLogTabN = 182;
 constexpr int kMaxNq = kMaxN1D * kMaxN1D;
 constexpr int kMaxPairsHi = kMaxN1D * kMaxN1D * (kMaxN1D - 1);  // 180
 constexpr int kMaxPairsLo = 2 * kMaxN1D * (kMaxN1D - 1);        // 60
@@ -60,6 +64,10 @@ struct OpTable {
   // the lift M \ Vf' of the unlimited projection at node m from its four faces (sides
   // r=-1, r=+1, s=-1, s=+1 in order): Vf[f, m] / wq[m] (init.jl:171-172)
   double liftf[kMaxNq][4];
+  // log_fast: per j, 1/F_j, log F_j to 41 significant bits and the rest of log F_j; log 2 in
+  // the same two parts (42 significant bits, so that k log2_hi is exact for |k| < 2048)
+  double logtab[kLogTabN][3];
+  double ln2_hi, ln2_lo;
 };
 
 // Builds the table for polynomial degree N (1..5) on the LGL (basis 0) or Gauss (basis 1)

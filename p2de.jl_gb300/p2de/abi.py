@@ -68,6 +68,8 @@ FIELD_L_LOCAL = 8
 FIELD_RESW = 9
 FIELD_L = 10
 FIELD_THETA_LOCAL = 11
+LAYOUT_FLAT = 0  # p2de_layout
+LAYOUT_LINES_PER_WARP = 1
 FIELD_F_BAR_H = 12  # f_bar_H of the last limited stage: 2 x (Nq+N1D) x K states, x then y
 FIELD_F_BAR_L = 13
 # p2de_equation
@@ -186,6 +188,8 @@ EXPORTS = [
     ("p2de_calculate_error", c_int, [SOLVER_P, POINTER(c_double), POINTER(c_double)]),
     ("p2de_set_elements_per_block", c_int, [SOLVER_P, c_int32]),
     ("p2de_get_elements_per_block", c_int, [SOLVER_P, POINTER(c_int32), POINTER(c_int32)]),
+    ("p2de_set_layout", c_int, [SOLVER_P, c_int32]),
+    ("p2de_get_layout", c_int, [SOLVER_P, POINTER(c_int32)]),
     ("p2de_autotune", c_int, [SOLVER_P, POINTER(c_int32), POINTER(c_double)]),
     ("p2de_batch_create", c_int, [c_int, c_int32, c_size_t, c_int32, POINTER(c_void_p)]),
     ("p2de_batch_destroy", c_int, [c_void_p]),
@@ -205,6 +209,8 @@ EXPORTS = [
     ("p2de_batch_last_error", c_int, [c_void_p, c_char_p, c_size_t]),
     ("p2de_batch_set_elements_per_block", c_int, [c_void_p, c_int32, c_int32]),
     ("p2de_batch_get_elements_per_block", c_int, [c_void_p, c_int32, POINTER(c_int32), POINTER(c_int32)]),
+    ("p2de_batch_set_layout", c_int, [c_void_p, c_int32, c_int32]),
+    ("p2de_batch_get_layout", c_int, [c_void_p, c_int32, POINTER(c_int32)]),
     ("p2de_batch_autotune", c_int, [c_void_p, POINTER(c_int32)]),
     ("p2de_server_create", c_int, [c_int, c_int32, c_size_t, c_int32, c_int32, POINTER(c_void_p)]),
     ("p2de_server_submit", c_int, [c_void_p, POINTER(P2deParam), POINTER(P2deMesh), POINTER(c_double), POINTER(c_int64)]),

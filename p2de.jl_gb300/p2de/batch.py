@@ -93,6 +93,14 @@ class Batch:
     def set_elements_per_block(self, N: int, epb: int) -> None:
         self._check(self.lib.p2de_batch_set_elements_per_block(self.h, N, int(epb)))
 
+    def layout(self, N: int) -> int:
+        v = c_int32()
+        self._check(self.lib.p2de_batch_get_layout(self.h, N, byref(v)))
+        return v.value
+
+    def set_layout(self, N: int, layout: int) -> None:
+        self._check(self.lib.p2de_batch_set_layout(self.h, N, int(layout)))
+
     def autotune(self) -> dict[int, int]:
         """Fastest elements-per-block per degree present; {N: epb}."""
         out = (c_int32 * 5)()

@@ -307,8 +307,18 @@ class Solver:
     def set_elements_per_block(self, epb: int) -> None:
         self._check(self.lib.p2de_set_elements_per_block(self.handle, int(epb)))
 
+    def layout(self) -> int:
+        """Thread layout of the high-order pair phases (abi.LAYOUT_*)."""
+        v = c_int32()
+        self._check(self.lib.p2de_get_layout(self.handle, byref(v)))
+        return v.value
+
+    def set_layout(self, layout: int) -> None:
+        self._check(self.lib.p2de_set_layout(self.handle, int(layout)))
+
     def autotune(self) -> tuple[int, float]:
-        """Keeps the fastest elements-per-block for stage kernel A; returns it with its ms."""
+        """Keeps the fastest elements-per-block and thread layout for stage kernel A;
+        returns the elements per block with its ms (layout() gives the layout kept)."""
         e, ms = c_int32(), c_double()
         self._check(self.lib.p2de_autotune(self.handle, byref(e), byref(ms)))
         return e.value, ms.value

@@ -1,7 +1,8 @@
-"""Elements per block of the stage kernels and the autotuner: the launch shape does not
-change any result (each element's arithmetic is the same at every value, and the only
-cross-element reductions are exact minima), so runs at any elements-per-block, and
-runs after autotuning, are bitwise equal to runs at the default."""
+"""Elements per block, thread layouts of the pair phases and the autotuner: the launch
+shape does not change any result (each element's arithmetic is the same at every value
+and in every layout, and the only cross-element reductions are exact minima), so runs at
+any elements-per-block, in either layout, and runs after autotuning, are bitwise equal to
+runs at the default."""
 from ctypes import byref, c_double, c_int64
 
 import numpy as np
@@ -17,15 +18,19 @@ from test_gpu_batch import alone, mix_cases
 pytestmark = pytest.mark.gpu
 
 
-def run_steps(param, md, desc, U0, nsteps, epb=None, tune=False):
+def run_steps(param, md, desc, U0, nsteps, epb=None, tune=False, layout=None):
     g = S.Solver(param, md, desc)
     g.set_Uq(U0)
     if epb is not None:
         g.set_elements_per_block(epb)
+    if layout is not None:
+        g.set_layout(layout)
+        assert g.layout() == layout
     if tune:
         best, ms = g.autotune()
         assert 1 <= best <= g.elements_per_block()[1] and ms > 0
         assert g.elements_per_block()[0] == best
+        assert g.layout() in (abi.LAYOUT_FLAT, abi.LAYOUT_LINES_PER_WARP)
         # tuning leaves the state alone
         np.testing.assert_array_equal(g.get_field(abi.FIELD_UQ), np.ravel(U0))
     t, n = c_double(0.0), c_int64()
@@ -105,5 +110,71 @@ def test_batch_elements_per_block_keeps_members_equal_alone(how):
         U_alone, t_alone, n_alone = alone(param, md, desc, U0)
         assert st[slot, 2] == 1.0 and st[slot, 3] == 0
         assert st[slot, 0] == t_alone and int(st[slot, 1]) == n_alone
+        np.testing.assert_array_equal(b.Uq(slot), U_alone)
+    b.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed", "mixed-acc64"])
+@pytest.mark.parametrize(
+    "problem,N,kw",
+    [
+        (problems.kelvin_helmholtz, 1, dict(Kx=12, Ky=10)),
+        (problems.double_mach_reflection, 2, dict(Kx=16, Ky=4)),
+        (problems.kelvin_helmholtz, 3, dict(Kx=9, Ky=7)),
+        (problems.riemann2d, 4, dict(Kx=6, Ky=5, seed=3)),
+        (problems.riemann2d, 5, dict(Kx=5, Ky=3, seed=8)),
+    ],
+)
+def test_lines_per_warp_layout_gives_the_same_bits(problem, N, kw, precision):
+    """The whole-lines-per-warp layout of the pair phases against the flat layout, at the
+    default and at extreme elements per block (partial warps of lines at the block's end)."""
+    param, md, bc, desc, U0 = setup(problem, N=N, T=0.2, precision=precision, **kw)
+    U_ref, t_ref = run_steps(param, md, desc, U0, 4, layout=abi.LAYOUT_FLAT)
+    g = S.Solver(param, md, desc)
+    edef, emax = g.elements_per_block()
+    g.close()
+    for e in sorted({1, edef, emax}):
+        U, t = run_steps(param, md, desc, U0, 4, epb=e, layout=abi.LAYOUT_LINES_PER_WARP)
+        assert t == t_ref
+        np.testing.assert_array_equal(U, U_ref, err_msg=f"epb={e}")
+
+
+def test_lines_per_warp_layout_on_rotated_elements_runs_flat():
+    """Elements that are not axis-aligned have pair terms on both axes; the layout setting
+    leaves them on the flat loops, with the same result."""
+    import p2de
+
+    param, ic, bcf = problems.isentropic_vortex(N=3, Kx=5, Ky=5, reference_semantics=False)[:3]
+    md = p2de.mesh.rotated(p2de.uniform_mesh(param.N, *param.K, param.xL, param.xR), 0.3)
+    bc = bcf(param, md)
+    desc = S.make_descriptor(param, md, bc)
+    U0 = S.evaluate_initial_condition(param, md, ic)
+    U_ref, _ = run_steps(param, md, desc, U0, 3, layout=abi.LAYOUT_FLAT)
+    U, _ = run_steps(param, md, desc, U0, 3, layout=abi.LAYOUT_LINES_PER_WARP)
+    np.testing.assert_array_equal(U, U_ref)
+
+
+def test_layout_value_is_checked():
+    param, md, bc, desc, U0 = setup(problems.kelvin_helmholtz, N=2, Kx=4, Ky=4, T=0.1)
+    g = S.Solver(param, md, desc)
+    for bad in (-1, 2):
+        with pytest.raises(abi.P2deError) as ei:
+            g.set_layout(bad)
+        assert ei.value.status == 1
+    assert g.layout() == abi.LAYOUT_FLAT
+    g.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_batch_layout_keeps_members_equal_alone(precision):
+    cases = mix_cases(precision)
+    b = Batch(pool_bytes=2 << 30, max_solves=16, precision=precision)
+    slots = [b.add(c[3], c[4]) for c in cases]
+    for N in {c[0].N for c in cases}:
+        b.set_layout(N, abi.LAYOUT_LINES_PER_WARP)
+        assert b.layout(N) == abi.LAYOUT_LINES_PER_WARP
+    b.run_to_end(chunk=20)
+    for slot, (param, md, bc, desc, U0) in zip(slots, cases):
+        U_alone, t_alone, n_alone = alone(param, md, desc, U0)
         np.testing.assert_array_equal(b.Uq(slot), U_alone)
     b.close()

@@ -125,8 +125,12 @@ def test_rhs_noalloc_rebuilds_the_operator_table_when_zerotol_changes():
     import torch
 
     lib = abi.load_library()
-    param, md, bc, desc, U0 = setup(problems.kelvin_helmholtz, N=3, Kx=8, Ky=8, T=0.1)
-    # a threshold that drops the smallest entries wq D of the N = 3 operator (0.02 drops none)
+    # the intended limiter semantics, under which the high-order volume terms reach rhsU
+    # (under the reference's they are limited away and only low-order terms remain)
+    param, md, bc, desc, U0 = setup(problems.kelvin_helmholtz, N=3, Kx=8, Ky=8, T=0.1,
+                                    reference_semantics=False, bound=p2de.PositivityBound())
+    desc = S.make_descriptor(param, md, bc)
+    # a threshold that drops the smallest entries wq D of the N = 3 operator
     param2 = replace(param, global_constants=replace(param.global_constants, ZEROTOL=0.2))
     desc2 = S.make_descriptor(param2, md, bc)
     arrs = device_mesh_arrays(bc, md.geom)
