@@ -312,15 +312,18 @@ typedef enum p2de_layout {
 
 int p2de_set_layout(p2de_solver* s, int32_t layout);
 int p2de_get_layout(p2de_solver* s, int32_t* layout);
+/* Threads per block of stage kernel A: 64 or 128 (the default). Results do not depend on it. */
+int p2de_set_threads_per_block(p2de_solver* s, int32_t threads);
+int p2de_get_threads_per_block(p2de_solver* s, int32_t* threads);
 
 /* Elements per thread block of the stage kernels (1..epb_max, the shared-memory limit).
  * Results do not depend on it: each element's arithmetic is the same at every value.
  * No counterpart in the reference (a launch parameter of this implementation). */
 int p2de_set_elements_per_block(p2de_solver* s, int32_t epb);
 int p2de_get_elements_per_block(p2de_solver* s, int32_t* epb, int32_t* epb_max);
-/* Times stage kernel A at candidate elements-per-block and thread layouts (stage scratch
- * only: the state is unchanged), keeps the fastest pair and returns its elements per block
- * and milliseconds; p2de_get_layout gives the layout kept. */
+/* Times stage kernel A at candidate elements-per-block, thread layouts and threads per block
+ * (stage scratch only: the state is unchanged), keeps the fastest and returns its elements
+ * per block and milliseconds; p2de_get_layout and p2de_get_threads_per_block give the rest. */
 int p2de_autotune(p2de_solver* s, int32_t* best_epb, double* best_ms);
 
 /* ---- Batches of independent solves ---------------------------------------------------

@@ -1091,6 +1091,27 @@ int p2de_get_layout(p2de_solver* s, int32_t* layout) {
   return P2DE_OK;
 }
 
+int p2de_set_threads_per_block(p2de_solver* s, int32_t threads) {
+  if (!s) return P2DE_ERR_INVALID_ARGUMENT;
+  if (s->line) return fail(s, P2DE_ERR_UNSUPPORTED, "the Line path runs one element per thread");
+  if (threads != 64 && threads != s->geo.threads)
+    return fail(s, P2DE_ERR_INVALID_ARGUMENT, "threads per block %d: 64 or %d", threads, s->geo.threads);
+  CK(cudaSetDevice(s->device));
+  CK(cudaStreamSynchronize(s->stream));
+  s->base.threads = threads;
+  if (s->graph) {
+    cudaGraphExecDestroy(s->graph);
+    s->graph = nullptr;
+  }
+  return P2DE_OK;
+}
+
+int p2de_get_threads_per_block(p2de_solver* s, int32_t* threads) {
+  if (!s || !threads) return P2DE_ERR_INVALID_ARGUMENT;
+  *threads = s->base.threads > 0 ? s->base.threads : s->geo.threads;
+  return P2DE_OK;
+}
+
 int p2de_get_elements_per_block(p2de_solver* s, int32_t* epb, int32_t* epb_max) {
   if (!s) return P2DE_ERR_INVALID_ARGUMENT;
   if (epb) *epb = s->base.epb;
@@ -1113,6 +1134,10 @@ int p2de_autotune(p2de_solver* s, int32_t* best_epb, double* best_ms) {
   if (!s->gauss && !s->kpp && (flags_for(s, 2, false, false) & F_AXIS_ALIGNED))
     layouts.push_back(P2DE_LAYOUT_LINES_PER_WARP);
   int best_layout = s->base.layout;
+  int best_threads = s->base.threads > 0 ? s->base.threads : s->geo.threads;
+  // Gauss kernel A launches at its own fixed block size
+  std::vector<int> threads{s->geo.threads};
+  if (!s->gauss) threads.push_back(64);
   double sc[S_NSCAL] = {0};
   CK(cudaMemcpyAsync(sc, s->scal, sizeof sc, cudaMemcpyDeviceToHost, s->stream));
   CK(cudaStreamSynchronize(s->stream));
@@ -1128,11 +1153,13 @@ int p2de_autotune(p2de_solver* s, int32_t* best_epb, double* best_ms) {
   auto timings = [&]() -> int {
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
+  for (int th : threads)
   for (int lay : layouts)
   for (int e : cand) {
     StageArgs a = s->base;
     a.epb = e;
     a.layout = lay;
+    a.threads = th;
     a.nstage = 2;
     a.flags = flags_for(s, 2, false, false);
     float tot = 0.f;
@@ -1151,6 +1178,7 @@ int p2de_autotune(p2de_solver* s, int32_t* best_epb, double* best_ms) {
       bms = ms;
       best = e;
       best_layout = lay;
+      best_threads = th;
     }
   }
   return P2DE_OK;
@@ -1162,6 +1190,7 @@ int p2de_autotune(p2de_solver* s, int32_t* best_epb, double* best_ms) {
   CK(cudaStreamSynchronize(s->stream));
   if (rt != P2DE_OK) return rt;
   int rc = p2de_set_layout(s, best_layout);
+  if (rc == P2DE_OK) rc = p2de_set_threads_per_block(s, best_threads);
   if (rc == P2DE_OK) rc = p2de_set_elements_per_block(s, best);
   if (best_epb) *best_epb = best;
   if (best_ms) *best_ms = bms;

@@ -54,6 +54,8 @@ struct StageArgs {
   // thread layout of the high-order pair and gather phases (p2de_layout): 0 flat (element,
   // pair) and (element, node) loops; 1 whole lines per warp on axis-aligned LGL elements
   int layout;
+  // threads per block of stage kernel A (a multiple of 32 up to Cfg::THREADS; 0: Cfg::THREADS)
+  int threads;
   const OpTable* ops;
   double* Uq;
   double* resW;

@@ -256,7 +256,7 @@ __device__ void smoothness(const LineArgs& a, const double (*U)[4], double& blen
   epsk = (a.flags & LF_MINENT) ? 1.0 : 0.0;
   if (a.flags & LF_RELAXED) {
     const double kappa = 1.0;
-    const double sk = log(ind) / log(10.0);
+    const double sk = log(ind) / 2.302585092994046;  // log(10), correctly rounded
     if (sk < a.s0 - kappa)
       epsk = 0.0;
     else if (sk > a.s0 + kappa)

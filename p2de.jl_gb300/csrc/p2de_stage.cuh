@@ -994,8 +994,10 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
         base[C::O_GEO + 15] = fmax(fmin(1.0 - alpha, 1.0), 0.5);
       }
       if (flags & F_RELAXED) {
-        // kappa = 1; log(10, x) = log(x) / log(10)
-        const double sk = log(smooth) / log(10.0);
+        // kappa = 1; log(10, x) = log(x) / log(10), log(10) as the correctly rounded
+        // constant (a device log(10.0) may be folded at compile time in one translation
+        // unit and evaluated in another, which would give batch members other bits)
+        const double sk = log(smooth) / 2.302585092994046;
         double eps;
         if (sk < a.s0 - 1.0)
           eps = 0.0;

@@ -49,16 +49,18 @@ cudaError_t launch_stage_a(const StageArgs& a, bool mixed, cudaStream_t st) {
     return cudaGetLastError();
   }
   if (a.epb < 1 || a.epb > C::E_MAX) return cudaErrorInvalidValue;
+  const int th = a.threads > 0 ? a.threads : C::THREADS;
+  if (th % 32 != 0 || th > C::THREADS) return cudaErrorInvalidValue;
   int grid = (a.K + a.epb - 1) / a.epb;
   const bool ext = a.flags & kExtFlags;
   if (mixed && ext)
-    k_stage_a<N1D, float, false, true><<<grid, C::THREADS, C::smem_x(a.epb), st>>>(a);
+    k_stage_a<N1D, float, false, true><<<grid, th, C::smem_x(a.epb), st>>>(a);
   else if (mixed)
-    k_stage_a<N1D, float><<<grid, C::THREADS, C::smem_a(a.epb), st>>>(a);
+    k_stage_a<N1D, float><<<grid, th, C::smem_a(a.epb), st>>>(a);
   else if (ext)
-    k_stage_a<N1D, double, false, true><<<grid, C::THREADS, C::smem_x(a.epb), st>>>(a);
+    k_stage_a<N1D, double, false, true><<<grid, th, C::smem_x(a.epb), st>>>(a);
   else
-    k_stage_a<N1D, double><<<grid, C::THREADS, C::smem_a(a.epb), st>>>(a);
+    k_stage_a<N1D, double><<<grid, th, C::smem_a(a.epb), st>>>(a);
   return cudaGetLastError();
 }
 

@@ -190,6 +190,8 @@ EXPORTS = [
     ("p2de_get_elements_per_block", c_int, [SOLVER_P, POINTER(c_int32), POINTER(c_int32)]),
     ("p2de_set_layout", c_int, [SOLVER_P, c_int32]),
     ("p2de_get_layout", c_int, [SOLVER_P, POINTER(c_int32)]),
+    ("p2de_set_threads_per_block", c_int, [SOLVER_P, c_int32]),
+    ("p2de_get_threads_per_block", c_int, [SOLVER_P, POINTER(c_int32)]),
     ("p2de_autotune", c_int, [SOLVER_P, POINTER(c_int32), POINTER(c_double)]),
     ("p2de_batch_create", c_int, [c_int, c_int32, c_size_t, c_int32, POINTER(c_void_p)]),
     ("p2de_batch_destroy", c_int, [c_void_p]),

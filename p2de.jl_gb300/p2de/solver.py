@@ -316,8 +316,16 @@ class Solver:
     def set_layout(self, layout: int) -> None:
         self._check(self.lib.p2de_set_layout(self.handle, int(layout)))
 
+    def threads_per_block(self) -> int:
+        v = c_int32()
+        self._check(self.lib.p2de_get_threads_per_block(self.handle, byref(v)))
+        return v.value
+
+    def set_threads_per_block(self, threads: int) -> None:
+        self._check(self.lib.p2de_set_threads_per_block(self.handle, int(threads)))
+
     def autotune(self) -> tuple[int, float]:
-        """Keeps the fastest elements-per-block and thread layout for stage kernel A;
+        """Keeps the fastest elements-per-block, thread layout and block size for stage kernel A;
         returns the elements per block with its ms (layout() gives the layout kept)."""
         e, ms = c_int32(), c_double()
         self._check(self.lib.p2de_autotune(self.handle, byref(e), byref(ms)))

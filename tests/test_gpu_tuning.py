@@ -18,9 +18,12 @@ from test_gpu_batch import alone, mix_cases
 pytestmark = pytest.mark.gpu
 
 
-def run_steps(param, md, desc, U0, nsteps, epb=None, tune=False, layout=None):
+def run_steps(param, md, desc, U0, nsteps, epb=None, tune=False, layout=None, threads=None):
     g = S.Solver(param, md, desc)
     g.set_Uq(U0)
+    if threads is not None:
+        g.set_threads_per_block(threads)
+        assert g.threads_per_block() == threads
     if epb is not None:
         g.set_elements_per_block(epb)
     if layout is not None:
@@ -178,3 +181,23 @@ def test_batch_layout_keeps_members_equal_alone(precision):
         U_alone, t_alone, n_alone = alone(param, md, desc, U0)
         np.testing.assert_array_equal(b.Uq(slot), U_alone)
     b.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize(
+    "problem,N,kw",
+    [
+        (problems.kelvin_helmholtz, 1, dict(Kx=12, Ky=10)),
+        (problems.double_mach_reflection, 3, dict(Kx=16, Ky=4)),
+        (problems.riemann2d, 5, dict(Kx=5, Ky=3, seed=8)),
+    ],
+)
+def test_threads_per_block_gives_the_same_bits(problem, N, kw, precision):
+    """Stage kernel A with 64 threads per block (every phase loops over its items with the
+    block's size) against the default 128, in both layouts."""
+    param, md, bc, desc, U0 = setup(problem, N=N, T=0.2, precision=precision, **kw)
+    U_ref, t_ref = run_steps(param, md, desc, U0, 4)
+    for layout in (abi.LAYOUT_FLAT, abi.LAYOUT_LINES_PER_WARP):
+        U, t = run_steps(param, md, desc, U0, 4, threads=64, layout=layout)
+        assert t == t_ref
+        np.testing.assert_array_equal(U, U_ref, err_msg=f"layout {layout}")
