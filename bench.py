@@ -822,6 +822,7 @@ def main():
                 "elements_per_block": epb,
                 "elements_per_block_source": "default" if args.no_autotune else f"autotuned (default {epb_default})",
                 "layout": ["flat", "lines per warp"][solver.layout()],
+                "threads_per_block_stage_a": solver.threads_per_block(),
             },
             "e2e": {
                 "value": e2e_value,

@@ -38,6 +38,38 @@ def test_periodic_mapP_is_an_involution_matching_coordinates(N, Kx, Ky):
     assert np.all((dy < 1e-12) | (np.abs(dy - 3.0) < 1e-12))
 
 
+@pytest.mark.parametrize("N,Kx,Ky", [(1, 3, 2), (3, 4, 5), (4, 3, 3)])
+def test_face_order_matches_the_reference_subcell_index_maps(N, Kx, Ky):
+    """The face-node order and the mapP partners that the reference's limiter code takes for
+    granted, independently of how mesh.py builds them: subcell_face_idx_to_quad_face_index_x/y
+    and subcell_index_P_x/y (src/dg/limiter/limiter_utils.jl:97-181) read face node
+    f = sj (r = -1), N1D + sj (r = +1), 2 N1D + si (s = -1), 3 N1D + si (s = +1) with
+    volume node q = si + N1D sj (0-based), and take an r-face's partner on the neighbour's
+    r-faces at the same sj and an s-face's partner on its s-faces at the same si."""
+    md = p2de.make_periodic(p2de.uniform_mesh(N, Kx, Ky, (0.0, 0.0), (2.0, 1.0)))
+    n = N + 1
+    x, y, xf, yf = md.x, md.y, md.xf, md.yf
+    # volume nodes: r (x) fastest, then s (y)
+    X = x.reshape(-1, n, n)
+    Y = y.reshape(-1, n, n)
+    assert np.all(np.diff(X, axis=2) > 0) and np.all(np.abs(np.diff(X, axis=1)) < 1e-14)
+    assert np.all(np.diff(Y, axis=1) > 0) and np.all(np.abs(np.diff(Y, axis=2)) < 1e-14)
+    for f in range(4 * n):
+        side, t = divmod(f, n)
+        si, sj = ((0, t), (N, t), (t, 0), (t, N))[side]
+        q = si + n * sj
+        assert np.allclose(xf[:, f], x[:, q], atol=1e-14) and np.allclose(yf[:, f], y[:, q], atol=1e-14), f
+    mP = md.mapP - 1
+    for k in range(md.num_elements):
+        for f in range(4 * n):
+            kP, iP = divmod(int(mP[k, f]), 4 * n)
+            side, t = divmod(f, n)
+            sideP, tP = divmod(iP, n)
+            assert tP == t, (k, f, iP)
+            assert sideP == {0: 1, 1: 0, 2: 3, 3: 2}[side], (k, f, iP)
+            assert kP != k or (Kx == 1 and side < 2) or (Ky == 1 and side >= 2)
+
+
 def test_boundary_sides_of_an_open_mesh():
     N, Kx, Ky = 2, 4, 3
     md = p2de.uniform_mesh(N, Kx, Ky)
