@@ -1936,7 +1936,19 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
   __syncthreads();
 
   // ---- P11: cell entropy bound (enforce_ES_subcell!, subcell.jl:462-744)
+  // Every product and sum of this phase is an explicitly rounded operation (__dmul_rn,
+  // __dadd_rn, ...), none left for the compiler to contract into an FMA: the greedy below
+  // amplifies a one-ulp change of its inputs, and a contraction chosen differently in the
+  // batch kernel than in the single-solve kernel would give a batch member other bits
+  // than its solo run. The sums follow the oracle's order, unfused as there. The per-face
+  // products run one item per face (P11c) on all lanes; only the ordered sums, the sort
+  // and the greedy run per element and direction (P11d).
   if (flags & F_CELL_ENTROPY) {
+    constexpr int M = Nq - n;  // interior subcell faces per direction
+    // scratch in the primitives region (uL is dead after P9): dvdf [2][M], sum_c dv fL
+    // [2][M], B psi [2][Nfp]
+    constexpr int O_DV = C::O_PRIM, O_DL = O_DV + 2 * M, O_BP = O_DL + 2 * M;
+    static_assert(4 * M + 2 * Nfp <= 6 * Nq, "cell-entropy scratch fits the primitives region");
     // An element-direction whose interior factors are all zero has sum(L*dvdf) = 0
     // (or NaN) and the check of subcell.jl:676-677 is false: nothing to do.
     for (int w = tid; w < Ke * 2; w += bs) {
@@ -1952,88 +1964,96 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
       base[C::O_MISC + d] = any ? 1.0 : 0.0;
     }
     __syncthreads();
-    // entropy variables v_ufun (compressible_Navier_Stokes.jl:134-144) at the nodes of
-    // the elements that need them
+    // P11b: entropy variables v_ufun (compressible_Navier_Stokes.jl:134-144) at the nodes
+    // of the elements that need them; s = log(p) - gamma log(rho) for log(p / rho^gamma)
     for (int w = tid; w < Ke * Nq; w += bs) {
       int e = w / Nq, m = w % Nq;
       double* base = sm + e * PE;
       if (base[C::O_MISC] == 0.0 && base[C::O_MISC + 1] == 0.0) continue;
       const double* U = base + C::O_U + 4 * m;
-      double p = pfun(g, U[0], U[1], U[2], U[3]);
-      double s = log(p) - a.gamma * log(U[0]);  // log(p / rho^gamma)
-      double rp = 1.0 / p;
+      const double ke = __dadd_rn(__dmul_rn(U[1], U[1]), __dmul_rn(U[2], U[2]));
+      const double p = __dmul_rn(a.gm1, __dsub_rn(U[3], __ddiv_rn(__dmul_rn(0.5, ke), U[0])));
+      const double s = __dsub_rn(log_fast(p, op), __dmul_rn(a.gamma, log_fast(U[0], op)));
+      const double rp = rcp(p);
       double* vq = base + C::O_FLUX + 4 * m;
-      vq[0] = (a.gamma + 1.0 - s) - a.gm1 * U[3] * rp;
-      vq[1] = U[1] * a.gm1 * rp;
-      vq[2] = U[2] * a.gm1 * rp;
-      vq[3] = -U[0] * a.gm1 * rp;
+      vq[0] = __dsub_rn(__dsub_rn(__dadd_rn(a.gamma, 1.0), s), __dmul_rn(__dmul_rn(a.gm1, U[3]), rp));
+      vq[1] = __dmul_rn(__dmul_rn(U[1], a.gm1), rp);
+      vq[2] = __dmul_rn(__dmul_rn(U[2], a.gm1), rp);
+      vq[3] = __dmul_rn(__dmul_rn(-U[0], a.gm1), rp);
     }
     __syncthreads();
+    // P11c: per interior face, dvdf = sum_c dv_c (fH - fL)_c and sum_c dv_c fL_c
+    // (subcell.jl:540-562); per face node, B psi (:521-529). dvdf index of a face: x,
+    // (si-1) + (n-1) sj; y, si + n (sj-1).
+    for (int w = tid; w < Ke * 2 * (M + Nfp); w += bs) {
+      const int e = w / (2 * (M + Nfp)), r = w % (2 * (M + Nfp));
+      const int d = r / (M + Nfp), j = r % (M + Nfp);
+      double* base = sm + e * PE;
+      if (base[C::O_MISC + d] == 0.0) continue;
+      if (j < M) {
+        int fi, qm, qp;
+        if (d == 0) {
+          const int si = j % (n - 1) + 1, sj = j / (n - 1);
+          fi = si + (n + 1) * sj;
+          qm = (si - 1) + n * sj;
+          qp = si + n * sj;
+        } else {
+          const int si = j % n, sj = j / n + 1;
+          fi = si + n * sj;
+          qm = si + n * (sj - 1);
+          qp = si + n * sj;
+        }
+        const double* vq = base + C::O_FLUX;
+        const double* fH = base + C::O_SCR + (d * 2 + 0) * NSF * 4 + fi * 4;
+        const double* fL = base + C::O_SCR + (d * 2 + 1) * NSF * 4 + fi * 4;
+        double pr_d[4], pr_l[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          const double dv = __dsub_rn(vq[4 * qm + c], vq[4 * qp + c]);
+          pr_d[c] = __dmul_rn(dv, __dsub_rn(fH[c], fL[c]));
+          pr_l[c] = __dmul_rn(dv, fL[c]);
+        }
+        base[O_DV + d * M + j] = __dadd_rn(__dadd_rn(__dadd_rn(pr_d[0], pr_d[1]), pr_d[2]), pr_d[3]);
+        base[O_DL + d * M + j] = __dadd_rn(__dadd_rn(__dadd_rn(pr_l[0], pr_l[1]), pr_l[2]), pr_l[3]);
+      } else {
+        const int f = j - M, side = f / n, tt = f % n;
+        const int q = side == 0 ? n * tt : side == 1 ? (n - 1) + n * tt : side == 2 ? tt : tt + n * (n - 1);
+        const double* G = base + C::O_GEO;
+        const double Br = side == 0 ? -op.w1D[tt] : side == 1 ? op.w1D[tt] : 0.0;
+        const double Bsv = side == 2 ? -op.w1D[tt] : side == 3 ? op.w1D[tt] : 0.0;
+        const double Bd = d == 0 ? __dadd_rn(__dmul_rn(G[1], Br), __dmul_rn(G[2], Bsv))
+                                 : __dadd_rn(__dmul_rn(G[3], Br), __dmul_rn(G[4], Bsv));
+        base[O_BP + d * Nfp + f] = __dmul_rn(Bd, __dmul_rn(a.gm1, base[C::O_U + 4 * q + 1 + d]));
+      }
+    }
+    __syncthreads();
+    // P11d: per element and direction, the sums in the oracle's order, rhs_es and the greedy
     for (int w = tid; w < Ke * 2; w += bs) {
       int e = w / 2, d = w % 2;
       double* base = sm + e * PE;
       if (base[C::O_MISC + d] == 0.0) continue;
-      const double* G = base + C::O_GEO;
-      const double* vq = base + C::O_FLUX;
-      const double* fb = base + C::O_SCR;
-      const double* fH = fb + (d * 2 + 0) * NSF * 4;
-      const double* fL = fb + (d * 2 + 1) * NSF * 4;
       double* L = base + C::O_L + d * NSF;
-      // sum_Bpsi over all face nodes in order (subcell.jl:521-529)
+      // sum_Bpsi over all face nodes in order
       double sB = 0.0;
-      for (int f = 0; f < Nfp; ++f) {
-        int side = f / n, tt = f % n;
-        int q = side == 0 ? n * tt : side == 1 ? (n - 1) + n * tt : side == 2 ? tt : tt + n * (n - 1);
-        double Br = side == 0 ? -op.w1D[tt] : side == 1 ? op.w1D[tt] : 0.0;
-        double Bsv = side == 2 ? -op.w1D[tt] : side == 3 ? op.w1D[tt] : 0.0;
-        double Bd = d == 0 ? G[1] * Br + G[2] * Bsv : G[3] * Br + G[4] * Bsv;
-        double psi = a.gm1 * base[C::O_U + 4 * q + 1 + d];
-        sB = sB + Bd * psi;
-      }
-      constexpr int M = Nq - n;
+      for (int f = 0; f < Nfp; ++f) sB = __dadd_rn(sB, base[O_BP + d * Nfp + f]);
       double dvdf[M];
-      // dvdf and sum_dvfbarL (subcell.jl:540-562) in the reference loop order:
-      // x: line sj outer, face si = 1..n-1 inner, dvdf index (si-1) + (n-1)*sj;
-      // y: line si outer, face sj = 1..n-1 inner, dvdf index si + n*(sj-1).
-      double sdl = 0.0;
-      for (int a2 = 0; a2 < n; ++a2)
-        for (int b2 = 1; b2 < n; ++b2) {
-          int fi, idx, qm, qp;
-          if (d == 0) {
-            fi = b2 + (n + 1) * a2;
-            idx = (b2 - 1) + (n - 1) * a2;
-            qm = (b2 - 1) + n * a2;
-            qp = b2 + n * a2;
-          } else {
-            fi = a2 + n * b2;
-            idx = a2 + n * (b2 - 1);
-            qm = a2 + n * (b2 - 1);
-            qp = a2 + n * b2;
-          }
-          double pr_d[4], pr_l[4];
 #pragma unroll
-          for (int c = 0; c < 4; ++c) {
-            double fLc = fL[fi * 4 + c];
-            double dv = vq[4 * qm + c] - vq[4 * qp + c];
-            pr_d[c] = dv * (fH[fi * 4 + c] - fLc);
-            pr_l[c] = dv * fLc;
-          }
-          dvdf[idx] = ((pr_d[0] + pr_d[1]) + pr_d[2]) + pr_d[3];
-          sdl += ((pr_l[0] + pr_l[1]) + pr_l[2]) + pr_l[3];
-        }
-      // sum of L*dvdf (subcell.jl:654-670)
-      double sumLd = 0.0;
+      for (int i2 = 0; i2 < M; ++i2) dvdf[i2] = base[O_DV + d * M + i2];
+      // sum_dvfbarL and sum of L*dvdf (subcell.jl:540-562, 654-670) in the reference loop
+      // order: x: line sj outer, face si = 1..n-1 inner; y: line si outer, face sj inner
+      double sdl = 0.0, sumLd = 0.0;
       for (int a2 = 0; a2 < n; ++a2)
         for (int b2 = 1; b2 < n; ++b2) {
-          int fi = d == 0 ? b2 + (n + 1) * a2 : a2 + n * b2;
-          int idx = d == 0 ? (b2 - 1) + (n - 1) * a2 : a2 + n * (b2 - 1);
-          sumLd += L[fi] * dvdf[idx];
+          const int fi = d == 0 ? b2 + (n + 1) * a2 : a2 + n * b2;
+          const int idx = d == 0 ? (b2 - 1) + (n - 1) * a2 : a2 + n * (b2 - 1);
+          sdl = __dadd_rn(sdl, base[O_DL + d * M + idx]);
+          sumLd = __dadd_rn(sumLd, __dmul_rn(L[fi], dvdf[idx]));
         }
-      double rhs = sB - sdl;
+      double rhs = __dsub_rn(sB, sdl);
       // rhs_es of the relaxed bounds (subcell.jl:750-753)
-      if (flags & F_RELAXED) rhs = (1 - a.beta * base[C::O_XT]) * rhs;
-      double est = sumLd - rhs;
-      double tol = jmax(0.0, sdl - sB);
+      if (flags & F_RELAXED) rhs = __dmul_rn(__dsub_rn(1.0, __dmul_rn(a.beta, base[C::O_XT])), rhs);
+      double est = __dsub_rn(sumLd, rhs);
+      double tol = jmax(0.0, __dsub_rn(sdl, sB));
       if (est > tol) {
         // sort (dvdf, index) descending in Julia's isless order, ties by index descending
         int ord[M];
@@ -2064,16 +2084,17 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
         };
         int curr = 0;
         double lhs = sumLd;
-        while (lhs > rhs + tol && curr < M) {
+        const double target = __dadd_rn(rhs, tol);
+        while (lhs > target && curr < M) {
           int idx = ord[curr];
           if (dvdf[idx] < a.ZEROTOL) break;
-          lhs = lhs - L[face_of_idx(idx)] * dvdf[idx];
+          lhs = __dsub_rn(lhs, __dmul_rn(L[face_of_idx(idx)], dvdf[idx]));
           ++curr;
         }
         for (int i2 = 0; i2 < curr; ++i2) {
           int idx = ord[i2];
           int fi = face_of_idx(idx);
-          double l_new = (i2 == curr - 1) ? jmax((rhs + tol - lhs) / dvdf[idx], 0.0) : 0.0;
+          double l_new = (i2 == curr - 1) ? jmax(__ddiv_rn(__dsub_rn(target, lhs), dvdf[idx]), 0.0) : 0.0;
           L[fi] = jmin(L[fi], l_new);
         }
       }
