@@ -916,8 +916,15 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
     F[6] = rhov * v + p;
     F[7] = v * Ep;
     double* Ws = base + C::O_WS + 2 * m;
-    Ws[0] = wavespeed_r(g, rr, G[6] * rhou + G[7] * rhov, E);
-    Ws[1] = wavespeed_r(g, rr, G[9] * rhou + G[10] * rhov, E);
+    if (aa) {
+      // the unit normals are (+-1, 0) and (0, +-1) exactly (g/sqrt(g^2) = +-1), so the
+      // normal momentum is +-rhou or +-rhov, and its sign does not enter the wavespeed
+      Ws[0] = wavespeed_r(g, rr, rhou, E);
+      Ws[1] = wavespeed_r(g, rr, rhov, E);
+    } else {
+      Ws[0] = wavespeed_r(g, rr, G[6] * rhou + G[7] * rhov, E);
+      Ws[1] = wavespeed_r(g, rr, G[9] * rhou + G[10] * rhov, E);
+    }
     if (flags & (F_SHOCK | F_RELAXED)) base[C::O_LAMI + m] = rho * p;  // the indicator rho p (shock_capture.jl:92-103)
     if (do_high) {
       if (sizeof(TH) == 8) {
@@ -1172,7 +1179,7 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
     double wsP = ws_own;
     if (!self && !kpp) {
       double rrN = (code == BC_INTERIOR) ? rrP : rcp(Unb[0]);
-      wsP = wavespeed_r(g, rrN, n1 * Unb[1] + n2 * Unb[2], Unb[3]);
+      wsP = wavespeed_r(g, rrN, aa ? (xs ? Unb[1] : Unb[2]) : n1 * Unb[1] + n2 * Unb[2], Unb[3]);
     }
     double lamB = 0.5 * nn * fmax(ws_own, wsP);
     double Fp[8];  // the projected face state's fluxes (projL)
@@ -1949,6 +1956,10 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
     // [2][M], B psi [2][Nfp]
     constexpr int O_DV = C::O_PRIM, O_DL = O_DV + 2 * M, O_BP = O_DL + 2 * M;
     static_assert(4 * M + 2 * Nfp <= 6 * Nq, "cell-entropy scratch fits the primitives region");
+    // and in the low-order rhsxy region (dead after P8): the sort keys of dvdf [2][M]
+    // (long long) and the sorted order [2][M] (int)
+    constexpr int O_KEY = C::O_RXYL, O_ORD = O_KEY + 2 * M;
+    static_assert(3 * M <= 8 * Nq, "sort scratch fits the low-order rhsxy region");
     // An element-direction whose interior factors are all zero has sum(L*dvdf) = 0
     // (or NaN) and the check of subcell.jl:676-677 is false: nothing to do.
     for (int w = tid; w < Ke * 2; w += bs) {
@@ -1969,7 +1980,7 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
     for (int w = tid; w < Ke * Nq; w += bs) {
       int e = w / Nq, m = w % Nq;
       double* base = sm + e * PE;
-      if (base[C::O_MISC] == 0.0 && base[C::O_MISC + 1] == 0.0) continue;
+      if (is_zero_bits(base[C::O_MISC]) && is_zero_bits(base[C::O_MISC + 1])) continue;
       const double* U = base + C::O_U + 4 * m;
       const double ke = __dadd_rn(__dmul_rn(U[1], U[1]), __dmul_rn(U[2], U[2]));
       const double p = __dmul_rn(a.gm1, __dsub_rn(U[3], __ddiv_rn(__dmul_rn(0.5, ke), U[0])));
@@ -1982,14 +1993,15 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
       vq[3] = __dmul_rn(__dmul_rn(-U[0], a.gm1), rp);
     }
     __syncthreads();
-    // P11c: per interior face, dvdf = sum_c dv_c (fH - fL)_c and sum_c dv_c fL_c
+    // P11c: per interior face, dvdf = sum_c dv_c (fH - fL)_c, its sort key (Julia's
+    // isless order as an integer: NaN above everything, -0 below +0) and sum_c dv_c fL_c
     // (subcell.jl:540-562); per face node, B psi (:521-529). dvdf index of a face: x,
     // (si-1) + (n-1) sj; y, si + n (sj-1).
     for (int w = tid; w < Ke * 2 * (M + Nfp); w += bs) {
       const int e = w / (2 * (M + Nfp)), r = w % (2 * (M + Nfp));
       const int d = r / (M + Nfp), j = r % (M + Nfp);
       double* base = sm + e * PE;
-      if (base[C::O_MISC + d] == 0.0) continue;
+      if (is_zero_bits(base[C::O_MISC + d])) continue;
       if (j < M) {
         int fi, qm, qp;
         if (d == 0) {
@@ -2013,8 +2025,12 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
           pr_d[c] = __dmul_rn(dv, __dsub_rn(fH[c], fL[c]));
           pr_l[c] = __dmul_rn(dv, fL[c]);
         }
-        base[O_DV + d * M + j] = __dadd_rn(__dadd_rn(__dadd_rn(pr_d[0], pr_d[1]), pr_d[2]), pr_d[3]);
+        const double dvdf = __dadd_rn(__dadd_rn(__dadd_rn(pr_d[0], pr_d[1]), pr_d[2]), pr_d[3]);
+        base[O_DV + d * M + j] = dvdf;
         base[O_DL + d * M + j] = __dadd_rn(__dadd_rn(__dadd_rn(pr_l[0], pr_l[1]), pr_l[2]), pr_l[3]);
+        const long long bits = __double_as_longlong(dvdf);
+        reinterpret_cast<long long*>(base + O_KEY)[d * M + j] =
+            (bits & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL ? 0x7fffffffffffffffLL : order_key(dvdf);
       } else {
         const int f = j - M, side = f / n, tt = f % n;
         const int q = side == 0 ? n * tt : side == 1 ? (n - 1) + n * tt : side == 2 ? tt : tt + n * (n - 1);
@@ -2027,18 +2043,31 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
       }
     }
     __syncthreads();
+    // P11e: the descending sort of (dvdf, index) as ranks, one item per face: the faces
+    // that sort before face i are those with a larger key, or an equal key and a larger
+    // index (sort!(rev = true) on the (value, index) tuples, subcell.jl:676-741)
+    for (int w = tid; w < Ke * 2 * M; w += bs) {
+      const int e = w / (2 * M), r = w % (2 * M), d = r / M, i = r % M;
+      double* base = sm + e * PE;
+      if (is_zero_bits(base[C::O_MISC + d])) continue;
+      const long long* key = reinterpret_cast<const long long*>(base + O_KEY) + d * M;
+      const long long ki = key[i];
+      int rank = 0;
+#pragma unroll
+      for (int j = 0; j < M; ++j) rank += (key[j] > ki || (key[j] == ki && j > i)) ? 1 : 0;
+      reinterpret_cast<int*>(base + O_ORD)[d * M + rank] = i;
+    }
+    __syncthreads();
     // P11d: per element and direction, the sums in the oracle's order, rhs_es and the greedy
     for (int w = tid; w < Ke * 2; w += bs) {
       int e = w / 2, d = w % 2;
       double* base = sm + e * PE;
-      if (base[C::O_MISC + d] == 0.0) continue;
+      if (is_zero_bits(base[C::O_MISC + d])) continue;
       double* L = base + C::O_L + d * NSF;
       // sum_Bpsi over all face nodes in order
       double sB = 0.0;
       for (int f = 0; f < Nfp; ++f) sB = __dadd_rn(sB, base[O_BP + d * Nfp + f]);
-      double dvdf[M];
-#pragma unroll
-      for (int i2 = 0; i2 < M; ++i2) dvdf[i2] = base[O_DV + d * M + i2];
+      const double* dvdf = base + O_DV + d * M;
       // sum_dvfbarL and sum of L*dvdf (subcell.jl:540-562, 654-670) in the reference loop
       // order: x: line sj outer, face si = 1..n-1 inner; y: line si outer, face sj inner
       double sdl = 0.0, sumLd = 0.0;
@@ -2055,25 +2084,7 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
       double est = __dsub_rn(sumLd, rhs);
       double tol = jmax(0.0, __dsub_rn(sdl, sB));
       if (est > tol) {
-        // sort (dvdf, index) descending in Julia's isless order, ties by index descending
-        int ord[M];
-        for (int i2 = 0; i2 < M; ++i2) ord[i2] = i2;
-        auto key_gt = [&](int x, int y) {  // true if (dvdf[x], x+1) sorts before (dvdf[y], y+1)
-          double vx = dvdf[x], vy = dvdf[y];
-          long long kx = isnan(vx) ? 0x7fffffffffffffffLL : order_key(vx);
-          long long ky = isnan(vy) ? 0x7fffffffffffffffLL : order_key(vy);
-          if (kx != ky) return kx > ky;
-          return x > y;
-        };
-        for (int i2 = 1; i2 < M; ++i2) {
-          int v = ord[i2];
-          int j2 = i2 - 1;
-          while (j2 >= 0 && key_gt(v, ord[j2])) {
-            ord[j2 + 1] = ord[j2];
-            --j2;
-          }
-          ord[j2 + 1] = v;
-        }
+        const int* ord = reinterpret_cast<const int*>(base + O_ORD) + d * M;
         auto face_of_idx = [&](int idx) {  // 0-based dvdf index -> L face index
           if (d == 0) {
             int si = idx % (n - 1) + 1, sj = idx / (n - 1);
