@@ -299,15 +299,19 @@ int p2de_profile_steps(p2de_solver* s, int64_t nsteps, double* t, double ms[3]);
  * solves evaluated (limiter_utils.jl:108-132); the others are skipped exactly. */
 int p2de_read_counters(p2de_solver* s, uint64_t out[1], int32_t reset);
 
-/* Thread layouts of the high-order volume phases of stage kernel A (the two-point fluxes
- * of every node pair of a line and their gather into each node). Results do not depend on
- * the layout: each pair and each node half is computed by the same code in both. No
- * counterpart in the reference (a launch parameter of this implementation). */
+/* Thread layouts. 2D solves: the layout of the high-order volume phases of stage kernel A
+ * (the two-point fluxes of every node pair of a line and their gather into each node), FLAT
+ * or LINES_PER_WARP. Line (1D) solves: the layout of the high-order and limiter kernel, FLAT
+ * (one thread per element) or TEAM (a team of 16 lanes per element, for solves too small to
+ * fill the GPU one thread per element); a Line solve starts with TEAM below 16384 elements,
+ * FLAT from there. Results do not depend on the layout: every value is computed by the same
+ * code in each. No counterpart in the reference (a launch parameter of this implementation). */
 typedef enum p2de_layout {
-  P2DE_LAYOUT_FLAT = 0,          /* flat loops over (element, pair) and (element, node) */
-  P2DE_LAYOUT_LINES_PER_WARP = 1 /* whole 1D lines per warp: a warp computes the pairs of its
-                                    lines, synchronizes only itself and gathers its lines'
-                                    nodes (axis-aligned LGL elements; others run flat) */
+  P2DE_LAYOUT_FLAT = 0,           /* flat loops over (element, pair) and (element, node) */
+  P2DE_LAYOUT_LINES_PER_WARP = 1, /* whole 1D lines per warp: a warp computes the pairs of its
+                                     lines, synchronizes only itself and gathers its lines'
+                                     nodes (axis-aligned LGL elements; others run flat) */
+  P2DE_LAYOUT_TEAM = 2            /* Line solves: a team of lanes per element */
 } p2de_layout;
 
 int p2de_set_layout(p2de_solver* s, int32_t layout);

@@ -898,10 +898,16 @@ int p2de_rhs(p2de_solver* s, double t, double dt, int32_t nstage, double* dt_out
   return P2DE_OK;
 }
 
+static int build_graph(p2de_solver* s);
+
+// One step from host time t: the step's CUDA graph (the launches p2de_ssp33_advance
+// replays), then t, dt and the status read back.
 static int step_impl(p2de_solver* s, double* t, double* dt_out) {
-  CK(cudaMemcpyAsync(s->scal + S_T, t, sizeof(double), cudaMemcpyHostToDevice, s->stream));
-  int rc = enqueue_step(s);
+  int rc = build_graph(s);
   if (rc != P2DE_OK) return rc;
+  CK(cudaMemcpyAsync(s->scal + S_T, t, sizeof(double), cudaMemcpyHostToDevice, s->stream));
+  CK(cudaGraphLaunch(s->graph, s->stream));
+  s->launches += step_launches(s);
   double sc[S_NSCAL];
   CK(cudaMemcpyAsync(sc, s->scal, sizeof sc, cudaMemcpyDeviceToHost, s->stream));
   CK(cudaStreamSynchronize(s->stream));
@@ -1072,7 +1078,11 @@ int p2de_set_elements_per_block(p2de_solver* s, int32_t epb) {
 
 int p2de_set_layout(p2de_solver* s, int32_t layout) {
   if (!s) return P2DE_ERR_INVALID_ARGUMENT;
-  if (s->line) return fail(s, P2DE_ERR_UNSUPPORTED, "the Line path runs one element per thread");
+  if (s->line) {
+    CK(cudaSetDevice(s->device));
+    std::string err;
+    return line_status(s, line_set_layout(s->line, layout, err), err);
+  }
   if (layout != P2DE_LAYOUT_FLAT && layout != P2DE_LAYOUT_LINES_PER_WARP)
     return fail(s, P2DE_ERR_INVALID_ARGUMENT, "layout %d", layout);
   CK(cudaSetDevice(s->device));
@@ -1087,7 +1097,7 @@ int p2de_set_layout(p2de_solver* s, int32_t layout) {
 
 int p2de_get_layout(p2de_solver* s, int32_t* layout) {
   if (!s || !layout) return P2DE_ERR_INVALID_ARGUMENT;
-  *layout = s->base.layout;
+  *layout = s->line ? line_layout(s->line) : s->base.layout;
   return P2DE_OK;
 }
 
@@ -1354,7 +1364,8 @@ int p2de_stage_minima(p2de_solver* s, double out[6]) {
   if (!s || !out) return P2DE_ERR_INVALID_ARGUMENT;
   CK(cudaSetDevice(s->device));
   long long k[6];
-  CK(cudaMemcpyAsync(k, s->minrec, sizeof k, cudaMemcpyDeviceToHost, s->stream));
+  const long long* rec = s->line ? s->line->minrec : s->minrec;
+  CK(cudaMemcpyAsync(k, rec, sizeof k, cudaMemcpyDeviceToHost, s->stream));
   CK(cudaStreamSynchronize(s->stream));
   for (int i = 0; i < 6; ++i) out[i] = key_to_double(k[i]);
   return P2DE_OK;

@@ -50,6 +50,12 @@ enum : int {
 // instruction in the same time however many lanes it carries, so a small solve is fastest
 // with its elements spread one warp per SM (32-thread blocks still fill an SM at large K).
 constexpr int kThreads = 32;
+// The team layout (P2DE_LAYOUT_TEAM): kTeam lanes per element, kTeamE elements per one-warp
+// block, for solves too small to fill the GPU one thread per element; a Line solve starts with
+// it below kTeamMaxK elements.
+constexpr int kTeam = 16;
+constexpr int kTeamE = 32 / kTeam;
+constexpr int kTeamMaxK = 16384;
 constexpr int MQ = kMaxN1D;     // nodes per element at most
 constexpr int MH = kLineMaxNh;  // nodes + face nodes
 constexpr int MS = 2 * kMaxN1D; // rows of L_local
@@ -370,6 +376,106 @@ __global__ void k_line_face(LineArgs a) {
   }
 }
 
+// k_line_face with one warp per element, a team of kTeam lanes per face node. The entropy
+// variables of the nodes are formed once per element (one lane per node), and the bisection
+// of solve_theta! runs speculatively: each round, lanes 1..15 of a team evaluate the 15
+// midpoints of the next four levels of the bisection tree below the current interval (lane j
+// replays the midpoints on the path to heap node j, the very operations the sequential
+// bisection performs on that path), and the team walks the tree with the results. The 21
+// halvings then take six rounds, the first one with lane 0 testing theta = 1. theta and the
+// projected face state are the bits of the one-thread kernel.
+template <int NQ>
+__global__ void k_line_face_team(LineArgs a) {
+  constexpr int n = NQ, N = n - 1, D = 4;  // tree levels per round: 2^D - 1 = 15 lanes
+  static_assert(kTeam == 16 && (1 << D) == kTeam, "a team of 16 lanes evaluates a 4-level tree");
+  const int k = blockIdx.x;
+  if (k >= a.K || done(a)) return;  // the same for the whole block
+  const int lane = threadIdx.x % kTeam, f = threadIdx.x / kTeam;
+  const int s = a.nstage - 1;
+  const LineOps& o = *a.ops;
+  __shared__ double sU[n][4], sv[n][4];
+  if (threadIdx.x < n) {
+    ld4(a.Uq + 4 * ((size_t)n * k + threadIdx.x), sU[threadIdx.x]);
+    v_ufun4(a.gamma, sU[threadIdx.x], sv[threadIdx.x]);
+  }
+  __syncwarp();
+  const int fn = f == 0 ? 0 : N;
+  auto face_var = [&](double th, double* acc) {
+    for (int c = 0; c < 4; ++c) acc[c] = 0.0;
+    for (int j = 0; j < n; ++j) {
+      const double c = th * o.Vf[f][j] + (1.0 - th) * (j == fn ? 1.0 : 0.0);
+      for (int q = 0; q < 4; ++q) acc[q] = acc[q] + c * sv[j][q];
+    }
+  };
+  double th = 1.0;
+  if (a.flags & LF_NSE) {
+    double Ufv[4] = {0, 0, 0, 0}, VUf[4] = {0, 0, 0, 0};
+    for (int j = 0; j < n; ++j)
+      for (int q = 0; q < 4; ++q) {
+        Ufv[q] = Ufv[q] + o.Vf[f][j] * sU[j][q];
+        VUf[q] = VUf[q] + o.Vf[f][j] * sv[j][q];
+      }
+    const double rhoef = rhoe4(Ufv), eps = a.POSTOL, zeta = a.zeta, eta = a.eta;
+    auto ok = [&](double t) {
+      double vt[4], ut[4];
+      face_var(t, vt);
+      if (!(vt[3] < -eps)) return false;
+      u_vfun4(a.gamma, vt, ut);
+      const double rho = ut[0], re = rhoe4(ut);
+      return vt[3] < jmin(zeta * VUf[3], -eps) && rho > jmax((1 - eta) * Ufv[0], eps) && rho < (1 + eta) * Ufv[0] &&
+             re > jmax((1 - eta) * rhoef, eps) && re < (1 + eta) * rhoef;
+    };
+    double x_valid = 0.0, x_invalid = 1.0;
+    bool settled = false;  // theta = 1 passed
+    int left = 21;         // halvings of the sequential loop (iter = 0..20)
+    // six rounds (4 + 4 + 4 + 4 + 4 + 1 levels) for every team of the warp, so that both
+    // teams take part in every ballot; a settled team evaluates nothing
+    for (int round = 0; round < 6; ++round) {
+      // lane j (1..15): the midpoint of heap node j below (x_valid, x_invalid); lane 0, in
+      // the first round, tests theta = 1
+      const int levels = left < D ? left : D;
+      bool res = false;
+      if (lane == 0) {
+        if (round == 0) res = ok(x_invalid);
+      } else if (!settled && 31 - __clz(lane) < levels) {
+        const int d = 31 - __clz(lane);  // depth of the heap node
+        double xv = x_valid, xi = x_invalid;
+        for (int l = 0; l < d; ++l) {
+          const double mid = 0.5 * (xv + xi);
+          if ((lane >> (d - 1 - l)) & 1)
+            xv = mid;
+          else
+            xi = mid;
+        }
+        res = ok(0.5 * (xv + xi));
+      }
+      const unsigned ball = __ballot_sync(0xffffffffu, res) >> (kTeam * f);
+      if (round == 0 && (ball & 1u)) settled = true;
+      if (!settled) {
+        int j = 1;
+        for (int l = 0; l < levels; ++l) {
+          const double x_new = 0.5 * (x_valid + x_invalid);
+          const int r = (ball >> j) & 1;
+          if (r)
+            x_valid = x_new;
+          else
+            x_invalid = x_new;
+          j = 2 * j + r;
+        }
+      }
+      left -= levels;
+    }
+    th = settled ? x_invalid : x_valid;
+  }
+  if (lane == 0) {
+    a.theta[2 * ((size_t)a.K * s + k) + f] = th;
+    double acc[4], u[4];
+    face_var(th, acc);
+    u_vfun4(a.gamma, acc, u);
+    st4(a.uf + 4 * (2 * (size_t)k + f), u);
+  }
+}
+
 // rhs_low_graph_visc! (low_order_graph_viscosity.jl:4-41) with the Dim1 graph viscosity and
 // LF placement (rhs_utils.jl:78-113); stage 1: the element's positivity CFL (:222-309)
 template <int NQ>
@@ -467,6 +573,132 @@ __global__ void k_line_low(LineArgs a) {
       const double wJq = J * o.wq[i];
       dtl = jmin(dtl, a.CFL * 0.5 * wJq / li);
     }
+    if (dtl > 0.0)
+      atomicMin(&a.dtkey[0], (unsigned long long)__double_as_longlong(dtl));
+    else
+      atomicOr(a.status, ST_BAD_DT);
+  }
+}
+
+// k_line_low with a team of kTeam lanes per element (kTeamE elements per one-warp block): the
+// node fluxes, the N low-order pairs, the two faces and the nodes' mass scaling and CFL terms
+// on separate lanes, each value formed by the same expression and in the same order as in
+// k_line_low (same bits); the element's CFL minimum is taken in node order on the team's
+// first lane.
+template <int NQ>
+__global__ void k_line_low_team(LineArgs a) {
+  constexpr int n = NQ, N = n - 1, E = kTeamE;
+  static_assert(n <= kTeam / 2, "pairs and faces on separate lanes");
+  const int lane = threadIdx.x % kTeam, e = threadIdx.x / kTeam;
+  const int k = blockIdx.x * E + e;
+  if (done(a)) return;  // the same for the whole grid
+  const bool live = k < a.K;
+  const LineOps& o = *a.ops;
+  __shared__ double sU[E][n][4], sfl[E][n][4], sSF[E][n][4], slamR[E][n], sBF[E][2][4], slamB[E][2], swsf[E][2];
+  __shared__ double scand[E][n];
+  double(*U)[4] = sU[e];
+  double(*fl)[4] = sfl[e];
+  double(*SF)[4] = sSF[e];
+  double* lamR = slamR[e];
+  double(*BF)[4] = sBF[e];
+  double *lamB = slamB[e], *wsf = swsf[e];
+  const double* g = live ? a.geom + 5 * (size_t)k : a.geom;
+  const double J = g[0];
+  if (live && lane < n) {
+    ld4(a.Uq + 4 * ((size_t)n * k + lane), U[lane]);
+    fluxes4(a.gamma, U[lane], fl[lane]);
+    lamR[lane] = 0.0;
+  }
+  __syncwarp();
+  // accumulate_low_order_rhs_volume! (:139-173): pair (j+1, j) on lane j, Sr0[j+1, j] = -1/2
+  if (live && lane < N) {
+    const int j = lane, i = j + 1;
+    const double Sr0 = 0.5 * (-0.5 - 0.5), Ss0 = 0.0;
+    const double S0 = g[1] * Sr0 + g[2] * Ss0, S1 = g[3] * Sr0 + g[4] * Ss0;
+    const double nn = norm2(S0, S1), n1 = S0 / nn, n2 = S1 / nn;
+    const double ws = jmax(wavespeed4(a.gamma, U[i], n1, n2), wavespeed4(a.gamma, U[j], -n1, -n2));
+    const double lij = nn * ws;
+    lamR[j] = lij;
+    for (int c = 0; c < 4; ++c) {
+      const double F = 0.5 * (fl[i][c] + fl[j][c]);
+      SF[j][c] = 2.0 * S0 * F - lij * (U[j][c] - U[i][c]);
+    }
+  }
+  // accumulate_low_order_rhs_surface! (:175-204) with get_uP_and_enforce_BC! (:94-124), face f
+  // on lane kTeam/2 + f
+  if (live && lane >= kTeam / 2 && lane < kTeam / 2 + 2) {
+    const int f = lane - kTeam / 2;
+    const int fk = 2 * k + f, p = a.nbr[fk], kP = p / 2, iP = p % 2;
+    double Uf[4], UfP[4], uP[4], b0, b1, bP0, bP1;
+    low_face_state(a, k, f, Uf);
+    low_face_state(a, kP, iP, UfP);
+    Bx(a, k, f, b0, b1);
+    Bx(a, kP, iP, bP0, bP1);
+    const double nn = norm2(b0, b1), nnP = norm2(bP0, bP1);
+    wsf[f] = wavespeed4(a.gamma, Uf, b0 / nn, b1 / nn);
+    const double wsP = wavespeed4(a.gamma, UfP, bP0 / nnP, bP1 / nnP);
+    const int8_t bc = a.bc[fk];
+    if (bc == BC_INFLOW) {
+      const double* I = a.Ival + 3 * (size_t)a.bcidx[fk];
+      uP[0] = I[0], uP[1] = I[1], uP[2] = 0.0, uP[3] = I[2];
+    } else if (bc == BC_OUTFLOW) {
+      ld4(U[f == 0 ? 0 : N], uP);
+    } else {
+      ld4(UfP, uP);
+    }
+    lamB[f] = 0.5 * nn * jmax(wsf[f], wsP);
+    double ff[4], fP[4];
+    fluxes4(a.gamma, Uf, ff);
+    fluxes4(a.gamma, uP, fP);
+    for (int c = 0; c < 4; ++c) {
+      const double fs = 0.5 * (ff[c] + fP[c]);
+      BF[f][c] = b0 * fs - lamB[f] * (uP[c] - Uf[c]);
+    }
+    st4(a.BFL + 4 * (size_t)fk, BF[f]);
+  }
+  __syncwarp();
+  // per node: Q0F1 in pair order (+SF of pair m-1, then -SF of pair m), negated, the face
+  // term, scale_low_order_rhs_by_mass! (:206-220) and the node's CFL term (:222-309)
+  if (live && lane < n) {
+    const int m = lane;
+    double r[4] = {0.0, 0.0, 0.0, 0.0};
+    if (m >= 1)
+      for (int c = 0; c < 4; ++c) r[c] = r[c] + SF[m - 1][c];
+    if (m < N)
+      for (int c = 0; c < 4; ++c) r[c] = r[c] + -SF[m][c];
+    for (int c = 0; c < 4; ++c) r[c] = 0.0 - r[c];
+    if (m == 0)
+      for (int c = 0; c < 4; ++c) r[c] = r[c] - BF[0][c];
+    if (m == N)
+      for (int c = 0; c < 4; ++c) r[c] = r[c] - BF[1][c];
+    const double wJq = J * o.wq[m];
+    double rl[4];
+    for (int c = 0; c < 4; ++c) rl[c] = r[c] / wJq + 0.0;
+    st4(a.rhsL + 4 * ((size_t)n * k + m), rl);
+    if (a.flags & LF_RHSU_L) st4(a.rhsU + 4 * ((size_t)n * k + m), rl);
+    if (a.flags & LF_CFL) {
+      const int i = m;
+      double li = 0.0;
+      for (int j = 0; j < n; ++j) li += (j == i - 1) ? lamR[j] : ((j == i + 1) ? lamR[i] : 0.0);
+      if (i == 0 || i == N) {
+        const int f = i == 0 ? 0 : 1;
+        if (a.flags & LF_LFPROJ) {
+          double b0, b1, ut[4];
+          Bx(a, k, f, b0, b1);
+          ld4(a.uf + 4 * (2 * (size_t)k + f), ut);
+          li += find_alpha(U[i], ut, a.POSTOL) * lamB[f] + 0.5 * norm2(b0, b1) * wsf[f];
+        } else {
+          li += lamB[f];
+        }
+      }
+      scand[e][i] = a.CFL * 0.5 * wJq / li;
+    }
+  }
+  if (!(a.flags & LF_CFL)) return;
+  __syncwarp();
+  if (live && lane == 0) {
+    double dtl = INFINITY;
+    for (int i = 0; i < n; ++i) dtl = jmin(dtl, scand[e][i]);
     if (dtl > 0.0)
       atomicMin(&a.dtkey[0], (unsigned long long)__double_as_longlong(dtl));
     else
@@ -790,6 +1022,325 @@ __global__ void k_line_high(LineArgs a) {
   }
 }
 
+// k_line_high with a team of kTeam lanes per element (kTeamE elements per one-warp block),
+// for solves too small to fill the GPU one thread per element: there each element's work is
+// one long dependent chain, so its independent parts — the rows of the gather and the lift,
+// the two faces, the nodes' bounds, the eight prefix-sum columns and the 2n bound
+// evaluations — run on separate lanes. Every value is formed by the same expression, in the
+// same order, as in k_line_high (this unit is compiled without FMA contraction), so both
+// kernels give the same bits; the sequential parts (the smoothness factor, the cell-entropy
+// sums and greedy) run on every lane or on the team's first lane.
+template <int NQ>
+__global__ void k_line_high_team(LineArgs a) {
+  constexpr int n = NQ, N = n - 1, Nh = n + 2, E = kTeamE;
+  const int lane = threadIdx.x % kTeam, e = threadIdx.x / kTeam;
+  const int k = blockIdx.x * E + e;
+  if (done(a)) return;  // the same for the whole grid
+  const bool live = k < a.K;
+  const int s = a.nstage - 1;
+  const LineOps& o = *a.ops;
+  __shared__ double sU[E][n][4], sut[E][Nh][4], sQF[E][Nh][4], suP[E][2][4], sLFc[E][2], sBF[E][2][4];
+  __shared__ double srH[E][n][4], srL[E][n][4], sli[E][n], suL[E][n][4], sLphi[E][n], sLrho[E][n], sUrho[E][n];
+  __shared__ double sfH[E][n + 1][4], sfL[E][n + 1][4], sev[E][2 * n], sL[E][2 * n], sv[E][n][4];
+  double(*U)[4] = sU[e];
+  double(*ut)[4] = sut[e];
+  double(*QF)[4] = sQF[e];
+  double(*uP)[4] = suP[e];
+  double* LFc = sLFc[e];
+  double(*BF)[4] = sBF[e];
+  double(*rH)[4] = srH[e];
+  double(*rL)[4] = srL[e];
+  const double J = live ? a.geom[5 * (size_t)k] : 1.0;
+  const double dt = __longlong_as_double((long long)a.dtkey[1]);  // the limiter's TimeParam dt
+  if (live) {
+    if (lane < n) {
+      ld4(a.Uq + 4 * ((size_t)n * k + lane), U[lane]);
+      ld4(U[lane], ut[lane]);
+    } else if (lane < Nh) {
+      ld4(a.uf + 4 * (2 * (size_t)k + (lane - n)), ut[lane]);
+    }
+    if (lane < Nh)
+      for (int c = 0; c < 4; ++c) QF[lane][c] = 0.0;
+  }
+  __syncwarp();
+  // exterior states, interface dissipation coefficients and BCs (:39-151), one lane per face
+  if (live && lane < 2) {
+    const int f = lane;
+    const int fk = 2 * k + f, p = a.nbr[fk], kP = p / 2, iP = p % 2;
+    ld4(a.uf + 4 * (size_t)p, uP[f]);
+    double b0, b1, c0, c1;
+    Bx(a, k, f, b0, b1);
+    Bx(a, kP, iP, c0, c1);
+    const double nn = norm2(b0, b1), nnP = norm2(c0, c1);
+    const double lam = wavespeed4(a.gamma, ut[n + f], b0 / nn, b1 / nn);
+    const double lamP = wavespeed4(a.gamma, uP[f], c0 / nnP, c1 / nnP);
+    LFc[f] = 0.5 * nn * jmax(lam, lamP);
+    const int8_t bc = a.bc[fk];
+    if (bc == BC_INFLOW || bc == BC_OUTFLOW) {
+      LFc[f] = 0.0;
+      if (bc == BC_INFLOW) {
+        const double* I = a.Ival + 3 * (size_t)a.bcidx[fk];
+        uP[f][0] = I[0], uP[f][1] = I[1], uP[f][2] = 0.0, uP[f][3] = I[2];
+      } else {
+        ld4(U[f == 0 ? 0 : N], uP[f]);
+      }
+    }
+  }
+  // flux_differencing_volume! (:164-211): one lane per row h gathers its pair terms in
+  // pair order
+  if (live && lane < Nh) {
+    const int h = lane;
+    const double* SFk = a.sf + (size_t)4 * kLineMaxPairs * k;
+    for (int p = 0; p < o.npair; ++p) {
+      const int i = o.pi[p], j = o.pj[p];
+      if (i != h && j != h) continue;
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const double SF = SFk[4 * p + c];
+        QF[h][c] = QF[h][c] + (i == h ? SF : -SF);
+      }
+    }
+  }
+  __syncwarp();
+  // flux_differencing_surface! (:223-272), one lane per face
+  if (live && lane < 2) {
+    const int f = lane;
+    double ff[4], fP[4], b0, b1;
+    fluxes4(a.gamma, ut[n + f], ff);
+    fluxes4(a.gamma, uP[f], fP);
+    Bx(a, k, f, b0, b1);
+    for (int c = 0; c < 4; ++c) BF[f][c] = b0 * (0.5 * (ff[c] + fP[c])) - LFc[f] * (uP[f][c] - ut[n + f][c]);
+    st4(a.BFH + 4 * (2 * (size_t)k + f), BF[f]);
+  }
+  __syncwarp();
+  // assemble_rhs! (:274-361), one lane per row i
+  const double th0 = live ? a.theta[2 * ((size_t)a.K * s + k)] : 1.0;
+  const double th1 = live ? a.theta[2 * ((size_t)a.K * s + k) + 1] : 1.0;
+  const bool limited = th0 < 1.0 || th1 < 1.0;
+  if (live && lane < n) {
+    const int i = lane;
+    const double rw = 1 / o.wq[i];
+    auto m = [&](int col) -> double {
+      if (!limited) return o.MinvVhT[i + n * col];
+      if (col < n) return col == i ? rw * 1.0 : 0.0;
+      const int f = col - n;
+      const double th = f == 0 ? th0 : th1;
+      const double low = (i == (f == 0 ? 0 : N)) ? 1.0 : 0.0;
+      return rw * (th * o.Vf[f][i] + (1 - th) * low);
+    };
+    double A[4] = {0, 0, 0, 0}, B[4] = {0, 0, 0, 0};
+    for (int j = 0; j < Nh; ++j) {
+      const double mm = m(j);
+      for (int c = 0; c < 4; ++c) A[c] = A[c] + mm * QF[j][c];
+    }
+    for (int f = 0; f < 2; ++f) {
+      const double mm = m(n + f);
+      for (int c = 0; c < 4; ++c) B[c] = B[c] + mm * BF[f][c];
+    }
+    for (int c = 0; c < 4; ++c) rH[i][c] = -(A[c] + B[c]) / J;
+    st4(a.rhsH + 4 * ((size_t)n * k + i), rH[i]);
+    ld4(a.rhsL + 4 * ((size_t)n * k + i), rL[i]);
+    if (a.flags & LF_RHSU_H) st4(a.rhsU + 4 * ((size_t)n * k + i), rH[i]);
+  }
+  if (!(a.flags & (LF_ZS | LF_SUBCELL))) return;
+  __syncwarp();
+  double blend = 1.0, epsk = 0.0;
+  if (live) smoothness(a, U, blend, epsk);  // on every lane, from the same shared state
+  const double zeta = a.zeta;
+  if (a.flags & LF_ZS) {  // zhang_shu_bound_limiter! (zhangshu.jl:35-45)
+    if (live && lane < n) {
+      const int i = lane;
+      double uL[4], P[4];
+      for (int c = 0; c < 4; ++c) {
+        uL[c] = U[i][c] + dt * rL[i][c];
+        P[c] = dt * (rH[i][c] - rL[i][c]);
+      }
+      sli[e][i] = jmin(1.0, bound_rho_rhoe(uL, P, zeta * uL[0], zeta * rhoe4(uL), INFINITY, INFINITY, a.ZEROTOL));
+    }
+    __syncwarp();
+    if (live && lane < n) {
+      double l = 1.0;
+      for (int i = 0; i < n; ++i) l = jmin(l, sli[e][i]);
+      if (lane == 0) a.Lelem[(size_t)a.K * s + k] = l;
+      l = jmin(l, blend);
+      const int i = lane;
+      double r[4];
+      for (int c = 0; c < 4; ++c) r[c] = (1 - l) * rL[i][c] + l * rH[i][c];
+      st4(a.rhsU + 4 * ((size_t)n * k + i), r);
+    }
+    return;
+  }
+  double(*uL)[4] = suL[e];
+  double *Lphi = sLphi[e], *Lrho = sLrho[e], *Urho = sUrho[e];
+  // node bounds, one lane per node
+  if (live && lane < n) {
+    const int q = lane;
+    const double phimin = decode_key(*a.phikey);
+    for (int c = 0; c < 4; ++c) uL[q][c] = U[q][c] + dt * rL[q][c];
+    // the two-point stencil of node q (low_order_stencil(::Dim1), limiter_utils.jl:184-220)
+    int kk[2], qq[2];
+    for (int t = 0; t < 2; ++t) {
+      const int qn = q + (t == 0 ? -1 : 1);
+      if (qn >= 0 && qn <= N) {
+        kk[t] = k;
+        qq[t] = qn;
+      } else {
+        const int p = a.nbr[2 * k + (q == 0 ? 0 : 1)];
+        kk[t] = p / 2;
+        qq[t] = (p % 2 == 0) ? 0 : N;
+      }
+    }
+    Lphi[q] = 0.0;
+    if (a.flags & LF_MINENT) {  // initialize_lower_bound!(::Dim1) (subcell.jl:37-51)
+      double lb = s_modified4(a.gamma, U[q]);
+      for (int t = 0; t < 2; ++t) {
+        double Un[4];
+        ld4(a.Uq + 4 * ((size_t)n * kk[t] + qq[t]), Un);
+        lb = jmin(lb, s_modified4(a.gamma, Un));
+      }
+      Lphi[q] = epsk * lb + (1 - epsk) * phimin;
+    }
+    Lrho[q] = zeta * uL[q][0];
+    Urho[q] = INFINITY;
+    if (a.flags & LF_TVD) {  // initialize_TVD_bounds!(::Dim1) (:86-110)
+      double lb = U[q][0] + dt * rL[q][0], ub = lb;
+      for (int t = 0; t < 2; ++t) {
+        const size_t m = (size_t)n * kk[t] + qq[t];
+        const double v = a.Uq[4 * m] + dt * a.rhsL[4 * m];
+        lb = jmin(lb, v);
+        ub = jmax(ub, v);
+      }
+      Lrho[q] = lb;
+      Urho[q] = ub;
+    }
+  }
+  // accumulate_f_bar!(::Dim1) (:144-160), one lane per (H or L, component)
+  double(*fH)[4] = sfH[e];
+  double(*fL)[4] = sfL[e];
+  if (live && lane < 8) {
+    const int c = lane % 4;
+    const bool hi = lane < 4;
+    double(*fb)[4] = hi ? fH : fL;
+    double(*r)[4] = hi ? rH : rL;
+    fb[0][c] = hi ? BF[0][c] : a.BFL[4 * (2 * (size_t)k) + c];
+    for (int i = 1; i <= n; ++i) {
+      const double wJ = J * o.wq[i - 1];
+      fb[i][c] = fb[i - 1][c] + wJ * r[i - 1][c];
+    }
+  }
+  __syncwarp();
+  // subcell_bound_limiter!(::Dim1) (:208-246): the 2n evaluations, one lane each; lane i < n
+  // limits face i from node i (sign -1), lane n + i - 1 face i from node i - 1 (sign +1)
+  double* ev = sev[e];
+  if (live && lane < 2 * n) {
+    const int q = lane < n ? lane : lane - n;
+    const int i = lane < n ? lane : lane - n + 1;
+    const double sgn = lane < n ? -1.0 : 1.0;
+    const double wJ = o.wq[q] * J;
+    double P[4];
+    for (int c = 0; c < 4; ++c) P[c] = sgn * 2.0 * dt * (fH[i][c] - fL[i][c]) / wJ;
+    const double Lrhoe = zeta * rhoe4(uL[q]);
+    double l = bound_rho_rhoe(uL[q], P, Lrho[q], Lrhoe, Urho[q], INFINITY, a.ZEROTOL);
+    if (a.flags & LF_MINENT) {
+      // limiting_param_bound_phi (limiter_utils.jl:43-50) by bisection on [0, lpos]
+      const double thr = Lphi[q] - a.POSTOL;
+      auto okp = [&](double lv) {
+        double W[4];
+        for (int c = 0; c < 4; ++c) W[c] = uL[q][c] + lv * P[c];
+        return s_modified4(a.gamma, W) >= thr;
+      };
+      double x_valid = 0.0, x_invalid = l;
+      if (!okp(x_invalid)) {
+        for (int iter = 0; iter <= 20; ++iter) {
+          const double x_new = 0.5 * (x_valid + x_invalid);
+          if (okp(x_new))
+            x_valid = x_new;
+          else
+            x_invalid = x_new;
+        }
+        l = x_valid;
+      }
+    }
+    ev[lane] = l;
+  }
+  __syncwarp();
+  double* L = sL[e];
+  if (live && lane < 2 * n) {
+    const int i = lane;
+    double Li = 1.0;
+    if (i < n) Li = jmin(Li, ev[i]);
+    if (i >= 1 && i <= n) Li = jmin(Li, ev[n + i - 1]);
+    L[i] = jmin(Li, blend);
+  }
+  __syncwarp();
+  if (a.flags & LF_CELL) {  // Dim1 methods of subcell.jl:468-505, 567-628, rhs_es :746-753
+    double(*v)[4] = sv[e];
+    if (live && lane < n) v_ufun4(a.gamma, U[lane], v[lane]);
+    __syncwarp();
+    if (live && lane == 0) {
+      double sB = 0.0;
+      for (int f = 0; f < 2; ++f) {
+        double b0, b1;
+        Bx(a, k, f, b0, b1);
+        const double psi = (a.gamma - 1.0) * U[f == 0 ? 0 : N][1];
+        sB = sB + b0 * psi;
+      }
+      double d[MQ], sx = 0.0;
+      for (int si = 1; si <= N; ++si) {
+        double dvdf = 0.0, dvfl = 0.0;
+        double t1[4], t2[4];
+        for (int c = 0; c < 4; ++c) {
+          const double dv = v[si - 1][c] - v[si][c];
+          t1[c] = dv * (fH[si][c] - fL[si][c]);
+          t2[c] = dv * fL[si][c];
+        }
+        dvdf = ((t1[0] + t1[1]) + t1[2]) + t1[3];
+        dvfl = ((t2[0] + t2[1]) + t2[2]) + t2[3];
+        d[si - 1] = dvdf;
+        sx += dvfl;
+      }
+      double sum = 0.0;
+      for (int si = 1; si <= N; ++si) sum += L[si] * d[si - 1];
+      double rhs = sB - sx;
+      if (a.flags & LF_RELAXED) rhs = (1 - a.beta * epsk) * rhs;
+      const double tol = jmax(0.0, sx - sB);
+      if (sum - rhs > tol) {
+        // indices 1..N by dvdf descending (sort!(..., rev=true) on (value, index) tuples)
+        int order[MQ];
+        for (int i = 0; i < N; ++i) order[i] = i + 1;
+        for (int i = 1; i < N; ++i)
+          for (int j = i; j > 0; --j) {
+            const int x = order[j - 1], y = order[j];
+            const bool y_first = jisless(d[x - 1], d[y - 1]) || (!jisless(d[y - 1], d[x - 1]) && x < y);
+            if (!y_first) break;
+            order[j - 1] = y;
+            order[j] = x;
+          }
+        int curr = 1;
+        double lhs = sum;
+        while (lhs > rhs + tol && curr <= n - 1) {
+          const int idx = order[curr - 1];
+          if (d[idx - 1] < a.ZEROTOL) break;
+          lhs = lhs - L[idx] * d[idx - 1];
+          curr += 1;
+        }
+        for (int i = 1; i <= curr - 1; ++i) {
+          const int idx = order[i - 1];
+          const double l_new = (i == curr - 1) ? jmax((rhs + tol - lhs) / d[idx - 1], 0.0) : 0.0;
+          L[idx] = jmin(L[idx], l_new);
+        }
+      }
+    }
+  }
+  __syncwarp();
+  if (live && lane < 2 * n) a.Lraw[(size_t)2 * n * k + lane] = L[lane];
+  if (live && lane <= n) {
+    double* fb = a.fbar + (size_t)8 * (n + 1) * k;
+    st4(fb + 4 * lane, fH[lane]);
+    st4(fb + 4 * (n + 1 + lane), fL[lane]);
+  }
+}
+
 // symmetrize_limiting_parameters!(::Dim1) (subcell.jl:405-415) across mapP,
 // accumulate_f_bar_limited!(::Dim1) (:826-839), apply_subcell_limiter!(::Dim1) (:878-892);
 // then the SSP-RK3 stage update (SSPRK33.jl:125-139) and the positivity record
@@ -847,6 +1398,93 @@ __global__ void k_line_update(LineArgs a) {
   if (bad) atomicOr(a.status, bad);
   atomicMin(&a.minrec[2 * s], encode_key(rmin));
   atomicMin(&a.minrec[2 * s + 1], encode_key(emin));
+}
+
+// k_line_update with a team of kTeam lanes per element: the symmetrized factors, the limited
+// subcell fluxes and the nodes' rhsU and stage update on separate lanes, each value formed as
+// in k_line_update (same bits); the element's minima are taken in node order on the team's
+// first lane.
+template <int NQ>
+__global__ void k_line_update_team(LineArgs a) {
+  constexpr int n = NQ, E = kTeamE;
+  static_assert(2 * n <= kTeam, "one lane per factor");
+  const int lane = threadIdx.x % kTeam, e = threadIdx.x / kTeam;
+  const int k = blockIdx.x * E + e;
+  if (done(a)) return;  // the same for the whole grid
+  const bool live = k < a.K;
+  const int s = a.nstage - 1;
+  const LineOps& o = *a.ops;
+  __shared__ double sL[E][2 * n], sflim[E][n + 1][4], smin[E][n][2];
+  const double J = live ? a.geom[5 * (size_t)k] : 1.0;
+  double* rU = a.rhsU + 4 * (size_t)n * (live ? k : 0);
+  double ru[4];
+  if (a.flags & LF_SUBCELL) {
+    double* L = sL[e];
+    if (live && lane < 2 * n) {
+      const double* Lr = a.Lraw + (size_t)2 * n * k;
+      double Li = Lr[lane];
+      for (int f = 0; f < 2; ++f) {
+        const int si = f == 0 ? 0 : n;
+        if (lane != si) continue;
+        const int p = a.nbr[2 * k + f], kP = p / 2, iP = p % 2;
+        const int siP = iP == 0 ? 0 : n;
+        Li = jmin(Lr[si], a.Lraw[(size_t)2 * n * kP + siP]);
+      }
+      L[lane] = Li;
+      a.Lloc[(size_t)2 * n * ((size_t)a.K * s + k) + lane] = Li;
+    }
+    __syncwarp();
+    double(*flim)[4] = sflim[e];
+    if (live && lane <= n) {
+      const int i = lane;
+      const double* fb = a.fbar + (size_t)8 * (n + 1) * k;
+      for (int c = 0; c < 4; ++c) flim[i][c] = L[i] * fb[4 * i + c] + (1.0 - L[i]) * fb[4 * (n + 1 + i) + c];
+    }
+    __syncwarp();
+    if (live && lane < n) {
+      const int i = lane;
+      const double wJ = o.wq[i] * J;
+      for (int c = 0; c < 4; ++c) {
+        ru[c] = (flim[i + 1][c] - flim[i][c]) / wJ;
+        rU[4 * i + c] = ru[c];
+      }
+    }
+  } else if (live && lane < n) {
+    for (int c = 0; c < 4; ++c) ru[c] = rU[4 * lane + c];
+  }
+  if (!(a.flags & LF_UPDATE)) return;
+  const double dt = __longlong_as_double((long long)a.dtkey[0]);  // the step's dt
+  if (live && lane < n) {
+    const int i = lane;
+    double* u = a.Uq + 4 * ((size_t)n * k + i);
+    double* w = a.resW + 4 * ((size_t)n * k + i);
+    for (int c = 0; c < 4; ++c) {
+      if (a.nstage == 1) {
+        w[c] = u[c];
+        u[c] = w[c] + dt * ru[c];
+      } else {
+        const double z = u[c] + dt * ru[c];
+        u[c] = a.nstage == 2 ? 3.0 / 4.0 * w[c] + 1.0 / 4.0 * z : 1.0 / 3.0 * w[c] + 2.0 / 3.0 * z;
+      }
+    }
+    const double re = rhoe4(u);
+    int bad = 0;
+    if (isnan(u[0]) || isnan(re)) bad |= ST_NAN;
+    if (!(u[0] > 0.0) || !(re > 0.0)) bad |= ST_NOT_POSITIVE;
+    if (bad) atomicOr(a.status, bad);
+    smin[e][i][0] = u[0];
+    smin[e][i][1] = re;
+  }
+  __syncwarp();
+  if (live && lane == 0) {
+    double rmin = INFINITY, emin = INFINITY;
+    for (int i = 0; i < n; ++i) {
+      rmin = fmin(rmin, smin[e][i][0]);
+      emin = fmin(emin, smin[e][i][1]);
+    }
+    atomicMin(&a.minrec[2 * s], encode_key(rmin));
+    atomicMin(&a.minrec[2 * s + 1], encode_key(emin));
+  }
 }
 
 template <typename T>
@@ -982,10 +1620,18 @@ cudaError_t launch_stage(LineSolve* L, double t, int nstage, double dt_set, bool
     k_line_begin<<<1, 32, 0, L->stream>>>(a, 0, dkey, dt_set, (minent && t == L->prm.t0) ? 1 : 0);
   }
   L->launches += 1;
-  LINE_LAUNCH(k_line_face, (2 * L->K + kThreads - 1) / kThreads, a);
+  if (line_layout(L) == P2DE_LAYOUT_TEAM) {
+    LINE_LAUNCH(k_line_face_team, L->K, a);
+  } else {
+    LINE_LAUNCH(k_line_face, (2 * L->K + kThreads - 1) / kThreads, a);
+  }
   L->launches += 1;
   if (flags & LF_LOW) {
-    LINE_LAUNCH(k_line_low, grid, a);
+    if (line_layout(L) == P2DE_LAYOUT_TEAM) {
+      LINE_LAUNCH(k_line_low_team, (L->K + kTeamE - 1) / kTeamE, a);
+    } else {
+      LINE_LAUNCH(k_line_low, grid, a);
+    }
     L->launches += 1;
   }
   if (minent) {  // gated on the device by the begin kernel's t == t0 test
@@ -996,11 +1642,19 @@ cudaError_t launch_stage(LineSolve* L, double t, int nstage, double dt_set, bool
   if (flags & LF_HIGH) {
     const long long np = (long long)L->K * L->npair;
     k_line_pairs<<<(int)((np + kThreads - 1) / kThreads), kThreads, 0, L->stream>>>(a);
-    LINE_LAUNCH(k_line_high, grid, a);
+    if (line_layout(L) == P2DE_LAYOUT_TEAM) {
+      LINE_LAUNCH(k_line_high_team, (L->K + kTeamE - 1) / kTeamE, a);
+    } else {
+      LINE_LAUNCH(k_line_high, grid, a);
+    }
     L->launches += 2;
   }
   if (flags & (LF_SUBCELL | LF_UPDATE)) {
-    LINE_LAUNCH(k_line_update, grid, a);
+    if (line_layout(L) == P2DE_LAYOUT_TEAM) {
+      LINE_LAUNCH(k_line_update_team, (L->K + kTeamE - 1) / kTeamE, a);
+    } else {
+      LINE_LAUNCH(k_line_update, grid, a);
+    }
     L->launches += 1;
   }
   return cudaGetLastError();
@@ -1361,6 +2015,29 @@ int line_advance(LineSolve* L, int64_t nsteps, double* t, int64_t* steps_done, d
   if (steps_done) *steps_done = (int64_t)(ts[TS_STEPS] - steps0);
   if (dt_last) *dt_last = ts[TS_DT];
   return rc;
+}
+
+int line_layout(const LineSolve* L) {
+  if (L->layout >= 0) return L->layout;
+  return L->K < kTeamMaxK ? P2DE_LAYOUT_TEAM : P2DE_LAYOUT_FLAT;
+}
+
+int line_set_layout(LineSolve* L, int layout, std::string& err) {
+  if (layout != P2DE_LAYOUT_FLAT && layout != P2DE_LAYOUT_TEAM) {
+    err = "a Line solve takes P2DE_LAYOUT_FLAT or P2DE_LAYOUT_TEAM, not " + std::to_string(layout);
+    return P2DE_ERR_INVALID_ARGUMENT;
+  }
+  cudaError_t e = cudaStreamSynchronize(L->stream);
+  if (e != cudaSuccess) {
+    err = cudaGetErrorString(e);
+    return P2DE_ERR_CUDA;
+  }
+  L->layout = layout;
+  if (L->graph) {  // the captured step holds the old kernel
+    cudaGraphExecDestroy(L->graph);
+    L->graph = nullptr;
+  }
+  return P2DE_OK;
 }
 
 int line_step_launches(const LineSolve* L) {

@@ -28,6 +28,7 @@ struct LineSolve {
   double *Lelem = nullptr;                // ZhangShuLimiter L, 3 stages x K
   double *sf = nullptr;                   // volume two-point terms S fS, K x kLineMaxPairs x 4
   int npair = 0;                          // nonzero pairs of Srh_db per element
+  int layout = -1;                        // P2DE_LAYOUT_FLAT or _TEAM; -1: by the element count
   double *geom = nullptr, *Ival = nullptr, *phimin = nullptr;
   int32_t *nbr = nullptr, *bcidx = nullptr;
   int8_t* bc = nullptr;
@@ -57,5 +58,9 @@ int line_step(LineSolve* L, double* t, double* dt_out, std::string& err);
 int line_advance(LineSolve* L, int64_t nsteps, double* t, int64_t* steps_done, double* dt_last, std::string& err);
 // kernel launches of one step
 int line_step_launches(const LineSolve* L);
+// the layout of the high-order and limiter kernel: P2DE_LAYOUT_FLAT (one thread per element)
+// or P2DE_LAYOUT_TEAM (a team of lanes per element); the default follows the element count
+int line_set_layout(LineSolve* L, int layout, std::string& err);
+int line_layout(const LineSolve* L);
 
 }  // namespace p2de

@@ -70,6 +70,7 @@ FIELD_L = 10
 FIELD_THETA_LOCAL = 11
 LAYOUT_FLAT = 0  # p2de_layout
 LAYOUT_LINES_PER_WARP = 1
+LAYOUT_TEAM = 2  # Line solves: a team of lanes per element
 FIELD_F_BAR_H = 12  # f_bar_H of the last limited stage: 2 x (Nq+N1D) x K states, x then y
 FIELD_F_BAR_L = 13
 # p2de_equation

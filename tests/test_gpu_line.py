@@ -213,3 +213,54 @@ def test_line_error_against_exact():
     err = S.calculate_error(None, g, problems.density_wave_1d_exact)
     assert 0 < err.L1err < 1e-5 and err.L2err < 1e-5 and err.Linferr < 1e-4
     g.close()
+
+
+@pytest.mark.parametrize("N", [1, 3, 5])
+@pytest.mark.parametrize("basis", ["lobatto", "gauss"])
+@pytest.mark.parametrize("limiter", ["pos", "cell", "relaxed-cell", "minent", "tvd-minent", "pos+hennemann",
+                                     "zhang-shu+hennemann"])
+def test_line_team_layout_gives_the_same_bits(limiter, basis, N):
+    """The team layout of the Line kernels (a team of lanes per element, the default below
+    16384 elements; the face projection's bisection speculative across a team) against one
+    thread per element: the state, the right-hand sides, the face fluxes, theta, the subcell
+    factors and the stage minima after ten steps, bitwise."""
+    if basis == "gauss" and limiter in CELL:
+        pytest.skip("no cell-entropy bound on Gauss nodes in 1D")
+    param, md, bc, desc, U0 = setup(problems.leblanc, N=N, K=50, T=0.05, rhs_limiter=LIMITERS[limiter],
+                                    **basis_kw(basis))
+    out = {}
+    for layout in (abi.LAYOUT_FLAT, abi.LAYOUT_TEAM):
+        g = gpu_for(param, md, desc, U0)
+        g.set_layout(layout)
+        assert g.layout() == layout
+        t = param.timestepping_param.t0
+        for _ in range(10):
+            t, _ = S.ssp33_step(g, t)
+        fields = [g.get_field(abi.FIELD_UQ), g.get_field(abi.FIELD_RHSU), g.get_field(abi.FIELD_RHSH),
+                  g.get_field(abi.FIELD_RHSL), g.get_field(abi.FIELD_BF_L), g.get_field(abi.FIELD_BF_H)]
+        fields += [g.get_field(abi.FIELD_THETA_LOCAL, s) for s in (1, 2, 3)]
+        mins = np.zeros(6)
+        g._check(g.lib.p2de_stage_minima(g.handle, abi.dptr(mins)))
+        fields.append(mins)
+        if isinstance(LIMITERS[limiter], SubcellLimiter):
+            fields += [g.get_field(abi.FIELD_L_LOCAL, s) for s in (1, 2, 3)]
+        else:
+            fields += [g.get_field(abi.FIELD_L, s) for s in (1, 2, 3)]
+        out[layout] = (t, fields)
+        g.close()
+    assert out[abi.LAYOUT_FLAT][0] == out[abi.LAYOUT_TEAM][0]
+    for a, b in zip(out[abi.LAYOUT_FLAT][1], out[abi.LAYOUT_TEAM][1]):
+        np.testing.assert_array_equal(a, b)
+
+
+def test_line_layout_default_and_values():
+    param, md, bc, desc, U0 = setup(problems.shu_osher, N=1, K=16384)
+    g = gpu_for(param, md, desc, U0)
+    assert g.layout() == abi.LAYOUT_FLAT  # one thread per element fills the GPU from 16384 elements
+    with pytest.raises(abi.P2deError):
+        g.set_layout(abi.LAYOUT_LINES_PER_WARP)
+    g.close()
+    param, md, bc, desc, U0 = setup(problems.shu_osher, N=1, K=64)
+    g = gpu_for(param, md, desc, U0)
+    assert g.layout() == abi.LAYOUT_TEAM
+    g.close()
