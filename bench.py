@@ -46,8 +46,8 @@ UNIT = "DOF-stage updates/s"
 # stage kernel A on this workload from one ncu capture
 # (profiles/k_stage_a_dmr480x120_n3_fp64.md): DRAM traffic per launch
 # (dram__bytes_read.sum + dram__bytes_write.sum) and the FP64 pipe's busy fraction
-KERNEL_A_TRAFFIC_BYTES = 142.2e6
-KERNEL_A_FP64_PIPE_BUSY = 0.857
+KERNEL_A_TRAFFIC_BYTES = 147.9e6
+KERNEL_A_FP64_PIPE_BUSY = 0.825
 
 
 def fma_probe_library():
