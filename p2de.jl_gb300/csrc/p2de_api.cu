@@ -1063,7 +1063,7 @@ int p2de_profile_steps(p2de_solver* s, int64_t nsteps, double* t, double ms[3]) 
 
 int p2de_set_elements_per_block(p2de_solver* s, int32_t epb) {
   if (!s) return P2DE_ERR_INVALID_ARGUMENT;
-  if (s->line) return fail(s, P2DE_ERR_UNSUPPORTED, "the Line path runs one element per thread");
+  if (s->line) return fail(s, P2DE_ERR_UNSUPPORTED, "the Line path has no elements-per-block parameter (p2de_set_layout)");
   if (epb < 1 || epb > s->geo.elems_per_block_max)
     return fail(s, P2DE_ERR_INVALID_ARGUMENT, "elements per block %d outside 1..%d", epb, s->geo.elems_per_block_max);
   CK(cudaSetDevice(s->device));
@@ -1103,7 +1103,7 @@ int p2de_get_layout(p2de_solver* s, int32_t* layout) {
 
 int p2de_set_threads_per_block(p2de_solver* s, int32_t threads) {
   if (!s) return P2DE_ERR_INVALID_ARGUMENT;
-  if (s->line) return fail(s, P2DE_ERR_UNSUPPORTED, "the Line path runs one element per thread");
+  if (s->line) return fail(s, P2DE_ERR_UNSUPPORTED, "the Line path has fixed 32-thread blocks (p2de_set_layout)");
   if (threads != 64 && threads != s->geo.threads)
     return fail(s, P2DE_ERR_INVALID_ARGUMENT, "threads per block %d: 64 or %d", threads, s->geo.threads);
   CK(cudaSetDevice(s->device));
@@ -1133,7 +1133,7 @@ int p2de_get_elements_per_block(p2de_solver* s, int32_t* epb, int32_t* epb_max) 
 // candidate elements-per-block and thread layout and keeps the fastest.
 int p2de_autotune(p2de_solver* s, int32_t* best_epb, double* best_ms) {
   if (!s) return P2DE_ERR_INVALID_ARGUMENT;
-  if (s->line) return fail(s, P2DE_ERR_UNSUPPORTED, "the Line path runs one element per thread");
+  if (s->line) return fail(s, P2DE_ERR_UNSUPPORTED, "the Line path picks its layout by the element count (p2de_set_layout)");
   CK(cudaSetDevice(s->device));
   const int emax = s->geo.elems_per_block_max, edef = s->geo.elems_per_block;
   std::vector<int> cand;

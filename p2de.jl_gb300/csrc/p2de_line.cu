@@ -376,21 +376,25 @@ __global__ void k_line_face(LineArgs a) {
   }
 }
 
-// k_line_face with one warp per element, a team of kTeam lanes per face node. The entropy
-// variables of the nodes are formed once per element (one lane per node), and the bisection
-// of solve_theta! runs speculatively: each round, lanes 1..15 of a team evaluate the 15
-// midpoints of the next four levels of the bisection tree below the current interval (lane j
-// replays the midpoints on the path to heap node j, the very operations the sequential
-// bisection performs on that path), and the team walks the tree with the results. The 21
-// halvings then take six rounds, the first one with lane 0 testing theta = 1. theta and the
-// projected face state are the bits of the one-thread kernel.
+// k_line_face with one warp per face node (two per element, a block of 64 threads). The
+// entropy variables of the nodes are formed once per element (one lane per node), and the
+// bisection of solve_theta! runs speculatively: each round, lanes 1..31 of a warp evaluate
+// the 31 midpoints of the next five levels of the bisection tree below the current interval
+// (lane j replays the midpoints on the path to heap node j, the very operations the
+// sequential bisection performs on that path), and the warp walks the tree with a ballot of
+// the results. The 21 halvings take five rounds, the first one with lane 0 testing theta = 1.
+// The projected face state at the final theta is the one the test of that theta formed on
+// its lane (the same face_var and u_vfun4 of the same theta), passed by a shuffle; it is
+// formed anew only when no test passed (theta = 0). theta and the projected face state are
+// the bits of the one-thread kernel.
+constexpr int kFaceTeamThreads = 64;
+
 template <int NQ>
 __global__ void k_line_face_team(LineArgs a) {
-  constexpr int n = NQ, N = n - 1, D = 4;  // tree levels per round: 2^D - 1 = 15 lanes
-  static_assert(kTeam == 16 && (1 << D) == kTeam, "a team of 16 lanes evaluates a 4-level tree");
+  constexpr int n = NQ, N = n - 1, D = 5;  // tree levels per round: 2^D - 1 = 31 lanes
   const int k = blockIdx.x;
   if (k >= a.K || done(a)) return;  // the same for the whole block
-  const int lane = threadIdx.x % kTeam, f = threadIdx.x / kTeam;
+  const int lane = threadIdx.x % 32, f = threadIdx.x / 32;
   const int s = a.nstage - 1;
   const LineOps& o = *a.ops;
   __shared__ double sU[n][4], sv[n][4];
@@ -398,7 +402,7 @@ __global__ void k_line_face_team(LineArgs a) {
     ld4(a.Uq + 4 * ((size_t)n * k + threadIdx.x), sU[threadIdx.x]);
     v_ufun4(a.gamma, sU[threadIdx.x], sv[threadIdx.x]);
   }
-  __syncwarp();
+  __syncthreads();
   const int fn = f == 0 ? 0 : N;
   auto face_var = [&](double th, double* acc) {
     for (int c = 0; c < 4; ++c) acc[c] = 0.0;
@@ -408,6 +412,8 @@ __global__ void k_line_face_team(LineArgs a) {
     }
   };
   double th = 1.0;
+  double u[4];
+  bool have_u = false;  // u holds u_vfun(face_var(th)) (the same on every lane of the warp)
   if (a.flags & LF_NSE) {
     double Ufv[4] = {0, 0, 0, 0}, VUf[4] = {0, 0, 0, 0};
     for (int j = 0; j < n; ++j)
@@ -416,8 +422,9 @@ __global__ void k_line_face_team(LineArgs a) {
         VUf[q] = VUf[q] + o.Vf[f][j] * sv[j][q];
       }
     const double rhoef = rhoe4(Ufv), eps = a.POSTOL, zeta = a.zeta, eta = a.eta;
-    auto ok = [&](double t) {
-      double vt[4], ut[4];
+    // the test of solve_theta!; ut: the projected state it formed (when it got that far)
+    auto ok = [&](double t, double* ut) {
+      double vt[4];
       face_var(t, vt);
       if (!(vt[3] < -eps)) return false;
       u_vfun4(a.gamma, vt, ut);
@@ -428,15 +435,16 @@ __global__ void k_line_face_team(LineArgs a) {
     double x_valid = 0.0, x_invalid = 1.0;
     bool settled = false;  // theta = 1 passed
     int left = 21;         // halvings of the sequential loop (iter = 0..20)
-    // six rounds (4 + 4 + 4 + 4 + 4 + 1 levels) for every team of the warp, so that both
-    // teams take part in every ballot; a settled team evaluates nothing
-    for (int round = 0; round < 6; ++round) {
-      // lane j (1..15): the midpoint of heap node j below (x_valid, x_invalid); lane 0, in
+    double ut[4] = {0, 0, 0, 0};
+    // five rounds (5 + 5 + 5 + 5 + 1 levels); the branch conditions below are the same on
+    // every lane of the warp (they depend on ballots only), so each shuffle is warp-uniform
+    for (int round = 0; round < 5; ++round) {
+      // lane j (1..31): the midpoint of heap node j below (x_valid, x_invalid); lane 0, in
       // the first round, tests theta = 1
       const int levels = left < D ? left : D;
       bool res = false;
       if (lane == 0) {
-        if (round == 0) res = ok(x_invalid);
+        if (round == 0) res = ok(x_invalid, ut);
       } else if (!settled && 31 - __clz(lane) < levels) {
         const int d = 31 - __clz(lane);  // depth of the heap node
         double xv = x_valid, xi = x_invalid;
@@ -447,21 +455,31 @@ __global__ void k_line_face_team(LineArgs a) {
           else
             xi = mid;
         }
-        res = ok(0.5 * (xv + xi));
+        res = ok(0.5 * (xv + xi), ut);
       }
-      const unsigned ball = __ballot_sync(0xffffffffu, res) >> (kTeam * f);
-      if (round == 0 && (ball & 1u)) settled = true;
+      const unsigned ball = __ballot_sync(0xffffffffu, res);
+      int src = -1;  // the lane whose test set the warp's current x_valid (or passed theta = 1)
+      if (round == 0 && (ball & 1u)) {
+        settled = true;
+        src = 0;
+      }
       if (!settled) {
         int j = 1;
         for (int l = 0; l < levels; ++l) {
           const double x_new = 0.5 * (x_valid + x_invalid);
           const int r = (ball >> j) & 1;
-          if (r)
+          if (r) {
             x_valid = x_new;
-          else
+            src = j;
+          } else {
             x_invalid = x_new;
+          }
           j = 2 * j + r;
         }
+      }
+      if (src >= 0) {
+        for (int c = 0; c < 4; ++c) u[c] = __shfl_sync(0xffffffffu, ut[c], src);
+        have_u = true;
       }
       left -= levels;
     }
@@ -469,9 +487,11 @@ __global__ void k_line_face_team(LineArgs a) {
   }
   if (lane == 0) {
     a.theta[2 * ((size_t)a.K * s + k) + f] = th;
-    double acc[4], u[4];
-    face_var(th, acc);
-    u_vfun4(a.gamma, acc, u);
+    if (!have_u) {
+      double acc[4];
+      face_var(th, acc);
+      u_vfun4(a.gamma, acc, u);
+    }
     st4(a.uf + 4 * (2 * (size_t)k + f), u);
   }
 }
@@ -1621,7 +1641,13 @@ cudaError_t launch_stage(LineSolve* L, double t, int nstage, double dt_set, bool
   }
   L->launches += 1;
   if (line_layout(L) == P2DE_LAYOUT_TEAM) {
-    LINE_LAUNCH(k_line_face_team, L->K, a);
+    switch (L->N1D) {
+      case 2: k_line_face_team<2><<<L->K, kFaceTeamThreads, 0, L->stream>>>(a); break;
+      case 3: k_line_face_team<3><<<L->K, kFaceTeamThreads, 0, L->stream>>>(a); break;
+      case 4: k_line_face_team<4><<<L->K, kFaceTeamThreads, 0, L->stream>>>(a); break;
+      case 5: k_line_face_team<5><<<L->K, kFaceTeamThreads, 0, L->stream>>>(a); break;
+      default: k_line_face_team<6><<<L->K, kFaceTeamThreads, 0, L->stream>>>(a); break;
+    }
   } else {
     LINE_LAUNCH(k_line_face, (2 * L->K + kThreads - 1) / kThreads, a);
   }

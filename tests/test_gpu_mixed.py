@@ -51,3 +51,32 @@ def test_mixed_double_mach_positivity(precision):
         t, _ = S.ssp33_step(g, t)
         g._check(g.lib.p2de_stage_minima(g.handle, abi.dptr(mins)))
         assert np.all(mins > 0)
+
+
+def test_mixed_kelvin_helmholtz_long_run():
+    """The config-2 comparison on a smaller mesh over a long run (Kelvin-Helmholtz 64^2,
+    N=3, to t = 0.5, ~6,900 steps): L1 and Linf of every component against FP64, the total
+    entropy drift and the positivity margin. mixed-acc64 stays at FP64 level (its FP32 pair
+    terms add exactly before they reach rhsU under the reference semantics); mixed, whose
+    FP32 sums do not telescope exactly at element faces, within 1e-5 (3.7e-6 at 256^2, t = 1)."""
+    from p2de import workloads as W
+
+    param, md, bc, desc, U0 = setup(problems.kelvin_helmholtz, N=3, Kx=64, Ky=64, T=0.5)
+    Wq = W.quadrature_weights(3, md.geom)
+    out = {}
+    for precision in ("fp64", "mixed", "mixed-acc64"):
+        pm = replace(param, precision=precision)
+        dm = S.make_descriptor(pm, md, bc)
+        out[precision] = run(pm, md, dm, U0)
+    ref = out["fp64"]
+    for precision, (tol_l1, tol_linf) in (("mixed-acc64", (1e-10, 1e-9)), ("mixed", (1e-5, 1e-4))):
+        err = W.relative_errors(out[precision], ref, Wq)
+        for comp in ("rho", "rhou", "rhov", "E"):
+            assert err[comp]["L1"] <= tol_l1 and err[comp]["Linf"] <= tol_linf, (precision, comp, err[comp])
+        U = out[precision]
+        rhoe = U[:, 3] - 0.5 * (U[:, 1] ** 2 + U[:, 2] ** 2) / U[:, 0]
+        assert U[:, 0].min() > 0.5 and rhoe.min() > 1.0
+    s = {p: W.total_entropy(out[p], Wq, param.equation.gamma) for p in out}
+    s0 = W.total_entropy(np.asarray(U0).reshape(-1, 4), Wq, param.equation.gamma)
+    drift = {p: (s[p] - s0) / abs(s0) for p in s}
+    assert abs(drift["mixed-acc64"] - drift["fp64"]) <= 1e-10 and abs(drift["mixed"] - drift["fp64"]) <= 1e-4, drift
