@@ -458,22 +458,31 @@ __device__ __forceinline__ void phi_min_body(const double* Uq, size_t nodes, dou
 
 // limiting_param_bound_phi (limiter_utils.jl:43-50) through bisection (nonlinear_solvers.jl:3-20):
 // the l in [0, lpos] closest to lpos, on the grid of 21 halvings, with
-// phi(U + l P) >= thr (thr = Lphi - POSTOL); f(0) is assumed, as the reference does.
-__device__ __forceinline__ double bisect_phi(const double* U, const double* P, double lpos, double thr,
-                                             double gamma) {
-  auto f = [&](double l) {
-    return s_modified(U[0] + l * P[0], U[1] + l * P[1], U[2] + l * P[2], U[3] + l * P[3], gamma) >= thr;
-  };
+// phi(U + l P) >= thr (thr = Lphi - POSTOL); f(0) is assumed, as the reference does. The
+// first test, at lpos (phi_at_least), and the 21 halvings after it (bisect_phi_halvings).
+__device__ __forceinline__ bool phi_at_least(const double* U, const double* P, double l, double thr, double gamma) {
+  return s_modified(U[0] + l * P[0], U[1] + l * P[1], U[2] + l * P[2], U[3] + l * P[3], gamma) >= thr;
+}
+
+__device__ __forceinline__ double bisect_phi_halvings(const double* U, const double* P, double lpos, double thr,
+                                                      double gamma) {
   double x_valid = 0.0, x_invalid = lpos;
-  if (f(x_invalid)) return x_invalid;
   for (int iter = 0; iter <= 20; ++iter) {
     const double x_new = 0.5 * (x_valid + x_invalid);
-    if (f(x_new))
+    if (phi_at_least(U, P, x_new, thr, gamma))
       x_valid = x_new;
     else
       x_invalid = x_new;
   }
   return x_valid;
+}
+
+// Slot s of P9's list of bisections: in the low-order rhsxy region of the block's elements
+// (16 Nq ints each, four times an element's evaluations), element s / (16 Nq) first.
+template <typename C>
+__device__ __forceinline__ int& bisect_slot(double* sm, int PE, int s) {
+  constexpr int cap = 16 * C::Nq;
+  return reinterpret_cast<int*>(sm + (s / cap) * PE + C::O_RXYL)[s % cap];
 }
 
 // v_ufun(::CompressibleIdealGas{Dim2}) (compressible_Navier_Stokes.jl:134-144), with
@@ -860,7 +869,10 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
       geom_factor(a.geom + 5 * (size_t)(k0 + e), q, sm + e * PE + C::O_GEO);
     }
   }
-  if (tid == 0) s_list[0] = 0;
+  if (tid == 0) {
+    s_list[0] = 0;
+    s_list[NEV * E + 1] = 0;  // the count of the bisections' list (P9)
+  }
   for (int w = tid; w < Ke * Nq * 4; w += bs) {
     int e = w / (Nq * 4), r = w % (Nq * 4);
     sm[e * PE + C::O_U + r] = a.Uq[(size_t)k0 * Nq * 4 + w];
@@ -1909,12 +1921,48 @@ __device__ __forceinline__ void stage_a_body(const StageArgs& a, int k0, double*
     // density bound) under the reference semantics, else Inf, for which it returns 1.0
     const double Urhoe = upper0 ? base[C::O_RHSL + 4 * m + 2] : __longlong_as_double(0x7ff0000000000000LL);
     if (upper0 && (flags & F_TVD)) l = fmin(l, rhoe_quadratic_solve(uL, P, Urhoe, a.ZEROTOL));
-    // min-entropy bounds (limiter_utils.jl:19-24): l is lpos, then the bisection
-    if (flags & F_MIN_ENTROPY) l = bisect_phi(uL, P, l, base[C::O_RHSL + 4 * m + 3], a.gamma);
+    // min-entropy bounds (limiter_utils.jl:19-24): l is lpos, then the bisection. Its first
+    // test (at lpos) runs here; an evaluation that fails it goes, with lpos, to a second list
+    // whose 21 halvings run below with every lane busy (a warp issues each pow of the loop
+    // once for all its lanes, so a few bisecting lanes among finished ones would cost the
+    // warp the whole loop). The list lives in the low-order rhsxy region, dead after P8.
+    if (flags & F_MIN_ENTROPY) {
+      if (!phi_at_least(uL, P, l, base[C::O_RHSL + 4 * m + 3], a.gamma)) {
+        base[C::O_EV + r] = l;
+        const int slot = atomicAdd(&s_list[NEV * E + 1], 1);
+        bisect_slot<C>(sm, PE, slot) = id;
+        continue;
+      }
+    }
     base[C::O_EV + r] = fmin(l, 1.0);
   }
   if (a.counters && tid == 0 && nlist) atomicAdd(&a.counters[0], (unsigned long long)nlist);
   __syncthreads();
+  if (flags & F_MIN_ENTROPY) {
+    const int nbis = s_list[NEV * E + 1];
+    for (int w = tid; w < nbis; w += bs) {
+      const int id = bisect_slot<C>(sm, PE, w);
+      const int e = id / NEV, r = id % NEV;
+      const int dh = r / Nq, m = r % Nq;
+      const int ir = m % n, is = m / n;
+      const int d = dh >> 1, h = dh & 1;
+      double* base = sm + e * PE;
+      const double* fb = base + C::O_SCR;
+      const int fi = (d == 0) ? (ir + h) + (n + 1) * is : ir + n * (is + h);
+      const double* fH = fb + ((d * 2 + 0) * NSF + fi) * 4;
+      const double* fL = fb + ((d * 2 + 1) * NSF + fi) * 4;
+      const double* uL = base + C::O_PRIM + 6 * m;
+      double P[4];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        double t = (fH[c] - fL[c]) * uL[5];
+        P[c] = h == 0 ? -t : t;
+      }
+      const double l = bisect_phi_halvings(uL, P, base[C::O_EV + r], base[C::O_RHSL + 4 * m + 3], a.gamma);
+      base[C::O_EV + r] = fmin(l, 1.0);
+    }
+    __syncthreads();
+  }
   }
 
   // ---- P10: combine evaluations per subcell face; blending factor 1 (NoShockCapture)
