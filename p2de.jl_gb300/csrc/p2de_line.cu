@@ -1053,6 +1053,7 @@ __global__ void k_line_high(LineArgs a) {
 template <int NQ>
 __global__ void k_line_high_team(LineArgs a) {
   constexpr int n = NQ, N = n - 1, Nh = n + 2, E = kTeamE;
+  static_assert(2 * n <= kTeam && Nh <= kTeam, "one lane per evaluation and per gather row");
   const int lane = threadIdx.x % kTeam, e = threadIdx.x / kTeam;
   const int k = blockIdx.x * E + e;
   if (done(a)) return;  // the same for the whole grid

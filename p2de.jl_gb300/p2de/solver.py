@@ -308,7 +308,8 @@ class Solver:
         self._check(self.lib.p2de_set_elements_per_block(self.handle, int(epb)))
 
     def layout(self) -> int:
-        """Thread layout of the high-order pair phases (abi.LAYOUT_*)."""
+        """Thread layout (abi.LAYOUT_*): of the high-order pair phases of a 2D solve (FLAT or
+        LINES_PER_WARP), of the Line kernels of a 1D solve (FLAT or TEAM)."""
         v = c_int32()
         self._check(self.lib.p2de_get_layout(self.handle, byref(v)))
         return v.value
