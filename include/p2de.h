@@ -303,7 +303,7 @@ int p2de_read_counters(p2de_solver* s, uint64_t out[1], int32_t reset);
  * (the two-point fluxes of every node pair of a line and their gather into each node), FLAT
  * or LINES_PER_WARP. Line (1D) solves: the layout of the high-order and limiter kernel, FLAT
  * (one thread per element) or TEAM (a team of 16 lanes per element, for solves too small to
- * fill the GPU one thread per element); a Line solve starts with TEAM below 16384 elements,
+ * fill the GPU one thread per element); a Line solve starts with TEAM below 2048 elements,
  * FLAT from there. Results do not depend on the layout: every value is computed by the same
  * code in each. No counterpart in the reference (a launch parameter of this implementation). */
 typedef enum p2de_layout {

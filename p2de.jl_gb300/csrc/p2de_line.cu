@@ -52,10 +52,14 @@ enum : int {
 constexpr int kThreads = 32;
 // The team layout (P2DE_LAYOUT_TEAM): kTeam lanes per element, kTeamE elements per one-warp
 // block, for solves too small to fill the GPU one thread per element; a Line solve starts with
-// it below kTeamMaxK elements.
+// it below kTeamMaxK elements. The team kernels trade total work for a shorter chain per
+// element (the speculative bisection evaluates 155 midpoints per face node where the loop
+// evaluates 22), so they win only while the GPU is idle: Shu-Osher data, N = 3, ms per step
+// one thread per element / team: K = 1024 1.35 / 0.70, K = 4096 1.40 / 1.88, K = 8192
+// 1.40 / 3.64.
 constexpr int kTeam = 16;
 constexpr int kTeamE = 32 / kTeam;
-constexpr int kTeamMaxK = 16384;
+constexpr int kTeamMaxK = 2048;
 constexpr int MQ = kMaxN1D;     // nodes per element at most
 constexpr int MH = kLineMaxNh;  // nodes + face nodes
 constexpr int MS = 2 * kMaxN1D; // rows of L_local

@@ -221,7 +221,7 @@ def test_line_error_against_exact():
                                      "zhang-shu+hennemann"])
 def test_line_team_layout_gives_the_same_bits(limiter, basis, N):
     """The team layout of the Line kernels (a team of lanes per element, the default below
-    16384 elements; the face projection's bisection speculative across a team) against one
+    2048 elements; the face projection's bisection speculative across a warp) against one
     thread per element: the state, the right-hand sides, the face fluxes, theta, the subcell
     factors and the stage minima after ten steps, bitwise."""
     if basis == "gauss" and limiter in CELL:
@@ -254,9 +254,9 @@ def test_line_team_layout_gives_the_same_bits(limiter, basis, N):
 
 
 def test_line_layout_default_and_values():
-    param, md, bc, desc, U0 = setup(problems.shu_osher, N=1, K=16384)
+    param, md, bc, desc, U0 = setup(problems.shu_osher, N=1, K=2048)
     g = gpu_for(param, md, desc, U0)
-    assert g.layout() == abi.LAYOUT_FLAT  # one thread per element fills the GPU from 16384 elements
+    assert g.layout() == abi.LAYOUT_FLAT  # from 2048 elements one thread per element is faster
     with pytest.raises(abi.P2deError):
         g.set_layout(abi.LAYOUT_LINES_PER_WARP)
     g.close()
