@@ -80,12 +80,16 @@ cudaError_t launch_es_interface(const StageArgs& a, cudaStream_t st) {
   return cudaGetLastError();
 }
 
+// Kernel B runs C::E elements per block whatever kernel A's tuned value is: its work per
+// element is fixed and it is fastest at the default (at a quarter of that it ran 45% slower,
+// which an autotuner timing kernel A alone would not see); its results do not depend on it.
 template <int N1D>
 cudaError_t launch_stage_b(const StageArgs& a, cudaStream_t st) {
   using C = Cfg<N1D>;
-  if (a.epb < 1 || a.epb > C::E_MAX) return cudaErrorInvalidValue;
-  int grid = (a.K + a.epb - 1) / a.epb;
-  k_stage_b<N1D><<<grid, C::THREADS, C::smem_b(a.epb), st>>>(a);
+  StageArgs b = a;
+  b.epb = C::E;
+  int grid = (b.K + b.epb - 1) / b.epb;
+  k_stage_b<N1D><<<grid, C::THREADS, C::smem_b(b.epb), st>>>(b);
   return cudaGetLastError();
 }
 
